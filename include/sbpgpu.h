@@ -1,0 +1,165 @@
+/*
+ * sbpgpu -- C ABI of the GB300 (sm_103a) implementation of SBP's data-parallel hot
+ * path: the MCMC vertex-move sweep (asynchronous Gibbs, hybrid MCMC,
+ * Metropolis-Hastings) and the block-merge pass, scored by delta-MDL.
+ *
+ * Plain pointers and sizes only; every function returns an sbpgpu_status and the
+ * message of the last failure is available from sbpgpu_last_error().  Host arrays are
+ * read or written synchronously; device state stays resident between calls.
+ *
+ * Each entry point names the reference interface it replaces (path:line inside the
+ * vtsynergy/SBP project).  A context is not thread-safe: use one per host thread.
+ */
+#ifndef SBPGPU_H
+#define SBPGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum sbpgpu_status {
+    SBPGPU_OK = 0,
+    SBPGPU_EINVAL = 1,    /* invalid argument (std::invalid_argument / IndexOutOfBounds in the reference) */
+    SBPGPU_ENOMEM = 2,    /* device allocation failed */
+    SBPGPU_ETIMEOUT = 3,  /* a bounded device-side wait ran out */
+    SBPGPU_EDEVICE = 4,   /* CUDA runtime error or a device-side consistency check failed */
+    SBPGPU_EUNSUPPORTED = 5
+} sbpgpu_status;
+
+typedef struct sbpgpu_ctx sbpgpu_ctx;
+typedef struct sbpgpu_graph sbpgpu_graph;
+typedef struct sbpgpu_bm sbpgpu_bm;
+
+/* Hot-path subset of the reference's Args (include/args.hpp:61-212). */
+typedef struct sbpgpu_config {
+    int32_t algorithm;        /* 0 async_gibbs, 1 hybrid_mcmc (default), 2 metropolis_hastings (--algorithm) */
+    int32_t batches;          /* --batches (default 1) */
+    float   mh_percent;       /* --mh_percent (default 0.075) */
+    int32_t greedy;           /* --greedy switch (default 1) */
+    int32_t ordered;          /* --ordered (default 0) */
+    int32_t approximate;      /* --approximate (default 0) */
+    int32_t asynciterations;  /* --asynciterations (default INT32_MAX) */
+    int32_t max_iterations;   /* MAX_NUM_ITERATIONS, include/finetune.hpp:34 (default 100) */
+} sbpgpu_config;
+
+typedef struct sbpgpu_stats {
+    int64_t proposals;        /* vertex proposals visited by the sweeps */
+    int64_t merge_proposals;  /* block-merge proposals */
+    int64_t moves;            /* vertex moves applied */
+    int64_t mcmc_iterations;
+    int64_t merges;           /* block merges applied */
+    int64_t edges_swept;      /* sum of k_out + k_in over visited vertex proposals */
+    int64_t outer_steps;      /* golden-section iterations */
+    int64_t kernel_launches;  /* kernels launched by this library for the call */
+} sbpgpu_stats;
+
+void sbpgpu_default_config(sbpgpu_config* cfg);
+
+/* ---- context ------------------------------------------------------------------ */
+sbpgpu_status sbpgpu_ctx_create(int32_t device, sbpgpu_ctx** out);
+void sbpgpu_ctx_destroy(sbpgpu_ctx* ctx);
+const char* sbpgpu_last_error(const sbpgpu_ctx* ctx);
+/* Blocks the host until all work of the context has finished. */
+sbpgpu_status sbpgpu_ctx_synchronize(sbpgpu_ctx* ctx);
+/* The CUDA stream (cudaStream_t) all work of the context is issued on. */
+void* sbpgpu_ctx_stream(sbpgpu_ctx* ctx);
+
+/* ---- graph: replaces Graph(out_neighbors, in_neighbors, ...) (include/graph.hpp:29-60)
+ * and Graph::add_edge (src/graph.cpp:10-18).  Directed edges in input order; self-loops
+ * and duplicate edges are kept.  Requires num_edges < 2^31. */
+sbpgpu_status sbpgpu_graph_create(sbpgpu_ctx* ctx, int64_t num_vertices, int64_t num_edges,
+                                  const int32_t* src, const int32_t* dst, sbpgpu_graph** out);
+/* Same, with src/dst already resident in device memory. */
+sbpgpu_status sbpgpu_graph_create_device(sbpgpu_ctx* ctx, int64_t num_vertices, int64_t num_edges,
+                                         const int32_t* d_src, const int32_t* d_dst, sbpgpu_graph** out);
+void sbpgpu_graph_destroy(sbpgpu_graph* g);
+int64_t sbpgpu_graph_num_vertices(const sbpgpu_graph* g);
+int64_t sbpgpu_graph_num_edges(const sbpgpu_graph* g);
+
+/* ---- blockmodel: replaces Blockmodel(num_blocks, graph, rate, assignment) and
+ * Blockmodel::initialize_edge_counts (src/blockmodel/blockmodel.cpp:193-276).
+ * assignment == NULL means the identity assignment (B = N, src/sbp.cpp:23). */
+sbpgpu_status sbpgpu_bm_create(sbpgpu_graph* g, int64_t num_blocks, const int32_t* assignment,
+                               sbpgpu_bm** out);
+/* Blockmodel::copy (src/blockmodel/blockmodel.cpp:139-153): device-to-device. */
+sbpgpu_status sbpgpu_bm_copy(const sbpgpu_bm* bm, sbpgpu_bm** out);
+void sbpgpu_bm_destroy(sbpgpu_bm* bm);
+int64_t sbpgpu_bm_num_blocks(const sbpgpu_bm* bm);
+int64_t sbpgpu_bm_nnz(const sbpgpu_bm* bm);
+/* Blockmodel accessors (include/blockmodel/blockmodel.hpp:90-200): any pointer may be NULL.
+ * degrees/sizes hold num_blocks values; rows/cols/counts hold nnz cells in row-major,
+ * ascending order (the blockmatrix). */
+sbpgpu_status sbpgpu_bm_read(const sbpgpu_bm* bm, int32_t* assignment, int64_t* d_out, int64_t* d_in,
+                             int64_t* d_tot, int64_t* sizes, int32_t* rows, int32_t* cols, int64_t* counts);
+/* Blockmodel::getOverall_entropy / setOverall_entropy */
+double sbpgpu_bm_entropy(const sbpgpu_bm* bm);
+
+/* ---- entropy ------------------------------------------------------------------- */
+/* entropy::mdl (src/entropy.cpp:597-604). */
+sbpgpu_status sbpgpu_mdl(sbpgpu_bm* bm, double* out);
+/* entropy::delta_mdl(Blockmodel, Delta, proposal) (src/entropy.cpp:298-403) for n moves
+ * vertex[i] -> proposal[i] against the current blockmodel. */
+sbpgpu_status sbpgpu_delta_mdl_batch(sbpgpu_bm* bm, int64_t n, const int32_t* vertex,
+                                     const int32_t* proposal, double* out_delta);
+/* entropy::block_merge_delta_mdl (src/entropy.cpp:129-182) for n merges block[i] -> proposal[i]. */
+sbpgpu_status sbpgpu_merge_delta_mdl_batch(sbpgpu_bm* bm, int64_t n, const int32_t* block,
+                                           const int32_t* proposal, double* out_delta);
+
+/* ---- finetune ------------------------------------------------------------------ */
+/* common::propose_new_block under the canonical seeded stream (src/common.cpp:138-198):
+ * proposal for vertex[i] drawn with counter (vertex, c1, c2, c3). */
+sbpgpu_status sbpgpu_propose_batch(sbpgpu_bm* bm, int64_t n, const int32_t* vertex, uint64_t seed,
+                                   uint32_t c1, uint32_t c2, uint32_t c3, int32_t* out_proposal);
+/* One asynchronous-Gibbs batch: propose for vertex[0..n) against one snapshot
+ * (finetune::propose_gibbs_move_v3, src/finetune.cpp:871-901) and apply the accepted
+ * moves in vertex-id order (Blockmodel::move_vertex(VertexMove_v3),
+ * src/blockmodel/blockmodel.cpp:437-494).  out_moves[i] = accepted proposal or -1
+ * (before the block-size-1 rule); returns the number of applied moves in *applied. */
+sbpgpu_status sbpgpu_gibbs_batch(sbpgpu_bm* bm, const sbpgpu_config* cfg, int64_t n, const int32_t* vertex,
+                                 uint64_t seed, uint32_t iteration, uint32_t step, int32_t* out_moves,
+                                 int64_t* applied);
+/* Sequential Metropolis-Hastings over vertex[0..n) in order, each accepted move applied
+ * before the next proposal (finetune::propose_move / move_vertex, src/finetune.cpp:822-869). */
+sbpgpu_status sbpgpu_mh_chain(sbpgpu_bm* bm, const sbpgpu_config* cfg, int64_t n, const int32_t* vertex,
+                              uint64_t seed, uint32_t iteration, uint32_t step, int64_t* applied);
+/* finetune::mcmc (src/finetune.cpp:754-771) dispatching to asynchronous_gibbs (:34-107),
+ * hybrid_mcmc (:563-646) or metropolis_hastings (:773-820). */
+sbpgpu_status sbpgpu_mcmc(sbpgpu_bm* bm, const sbpgpu_config* cfg, uint64_t seed, int32_t step,
+                          int32_t golden_ratio_not_reached, sbpgpu_stats* stats);
+
+/* ---- block merge --------------------------------------------------------------- */
+/* block_merge::merge_blocks (src/block_merge.cpp:178-228): 10 proposals per block,
+ * carry_out_best_merges_advanced (:40-117) or, with cfg->approximate,
+ * Blockmodel::carry_out_best_merges (src/blockmodel/blockmodel.cpp:55-122); then the
+ * blockmodel is rebuilt with num_blocks - num_blocks_to_merge blocks. */
+sbpgpu_status sbpgpu_merge_blocks(sbpgpu_bm* bm, const sbpgpu_config* cfg, uint64_t seed, int32_t step,
+                                  int64_t num_blocks_to_merge, sbpgpu_stats* stats);
+/* The per-block best merge proposals only (block_merge.cpp:189-217). */
+sbpgpu_status sbpgpu_merge_proposals(sbpgpu_bm* bm, uint64_t seed, int32_t step, int32_t* best_proposal,
+                                     double* best_delta);
+
+/* ---- full partition ------------------------------------------------------------ */
+/* sbp::stochastic_block_partition (src/sbp.cpp:16-72) with the golden-section search of
+ * BlockmodelTriplet (src/blockmodel/blockmodel_triplet.cpp:4-105).  Writes the final
+ * assignment (num_vertices values) and returns the number of blocks in *num_blocks. */
+sbpgpu_status sbpgpu_sbp(sbpgpu_graph* g, const sbpgpu_config* cfg, uint64_t seed, int32_t* out_assignment,
+                         int64_t* num_blocks, double* out_mdl, sbpgpu_stats* stats);
+
+/* ---- timing of the dominant kernels (CUDA events on the context's stream) --------- */
+typedef struct sbpgpu_kernel_timing {
+    double gibbs_propose_ms;  int64_t gibbs_propose_launches;  int64_t gibbs_propose_bytes;
+    double mh_chain_ms;       int64_t mh_chain_launches;
+    double merge_propose_ms;  int64_t merge_propose_launches;  int64_t merge_propose_bytes;
+    double carry_out_ms;      int64_t carry_out_launches;
+    double rebuild_ms;        int64_t rebuild_launches;       int64_t rebuild_bytes;
+} sbpgpu_kernel_timing;
+/* Enables (1) or disables (0) event timing; reading resets the accumulators. */
+void sbpgpu_set_timing(sbpgpu_ctx* ctx, int32_t enabled);
+sbpgpu_status sbpgpu_read_timing(sbpgpu_ctx* ctx, sbpgpu_kernel_timing* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,1126 @@
+/*
+ * CPU oracle for the SBP hot path -- TEST INFRASTRUCTURE ONLY (see sbp_oracle.h).
+ *
+ * A restatement of vtsynergy/SBP's serial semantics with ordered maps (so every
+ * iteration is in ascending block order) and the canonical seeded proposal stream.
+ * Citations are path:line inside the reference project.
+ *
+ * Canonical stream (shared with the device implementation, which has its own code):
+ *   key   = (seed & 0xffffffff, seed >> 32)
+ *   ctr   = (c0, c1, c2, c3); outputs w[0..3] of Philox4x32-10.
+ *   Gibbs vertex proposal : ctr = (vertex, iteration, step, DOM_GIBBS)
+ *   MH vertex proposal    : ctr = (vertex, iteration, step, DOM_MH)
+ *   merge proposal i      : ctr = (block, 0, step, DOM_MERGE | i << 8)
+ *   shuffles              : ctr = (position, iteration, step, DOM_SHUFFLE_*)
+ *   u32_below(w, n) = (w * n) >> 32;  u64_below(hi, lo, n) = ((hi:lo) * n) >> 64.
+ *   Multinomials over a block's neighbour weights enumerate the row part (ascending
+ *   column) and then the column part (ascending row), the same concatenation the
+ *   reference builds in DictTransposeMatrix::neighbors_weights
+ *   (dict_transpose_matrix.cpp:176-188) and in propose_new_block's concatenated
+ *   out/in lists (common.cpp:141-142).
+ */
+#include "sbp_oracle.h"
+
+#include <algorithm>
+#include <cfloat>
+#include <climits>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <set>
+#include <utility>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+enum : uint32_t {
+    DOM_GIBBS = 1, DOM_MH = 2, DOM_MERGE = 3, DOM_SHUFFLE_HDV = 4, DOM_SHUFFLE_ALL = 5,
+};
+
+// ---------------------------------------------------------------- Philox4x32-10
+inline void philox_round(uint32_t c[4], const uint32_t k[2]) {
+    const uint64_t p0 = (uint64_t)0xD2511F53u * c[0];
+    const uint64_t p1 = (uint64_t)0xCD9E8D57u * c[2];
+    const uint32_t n0 = (uint32_t)(p1 >> 32) ^ c[1] ^ k[0];
+    const uint32_t n1 = (uint32_t)p1;
+    const uint32_t n2 = (uint32_t)(p0 >> 32) ^ c[3] ^ k[1];
+    const uint32_t n3 = (uint32_t)p0;
+    c[0] = n0; c[1] = n1; c[2] = n2; c[3] = n3;
+}
+
+inline void philox(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
+    uint32_t c[4] = {ctr[0], ctr[1], ctr[2], ctr[3]};
+    uint32_t k[2] = {key[0], key[1]};
+    for (int r = 0; r < 10; ++r) {
+        if (r) { k[0] += 0x9E3779B9u; k[1] += 0xBB67AE85u; }
+        philox_round(c, k);
+    }
+    out[0] = c[0]; out[1] = c[1]; out[2] = c[2]; out[3] = c[3];
+}
+
+inline void draw(uint64_t seed, uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t w[4]) {
+    const uint32_t ctr[4] = {c0, c1, c2, c3};
+    const uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+    philox(ctr, key, w);
+}
+
+inline uint32_t u32_below(uint32_t w, uint32_t n) { return (uint32_t)(((uint64_t)w * n) >> 32); }
+inline uint64_t u64_below(uint32_t hi, uint32_t lo, uint64_t n) {
+    const unsigned __int128 x = (unsigned __int128)((((uint64_t)hi) << 32) | lo) * n;
+    return (uint64_t)(x >> 64);
+}
+/* common::propose_random_block (common.cpp:200-209): uniform over [0, B-2], skip current. */
+inline int64_t random_block(int64_t current, int64_t B, uint32_t w) {
+    int64_t x = (int64_t)u32_below(w, (uint32_t)(B - 1));
+    if (x >= current) x++;
+    return x;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------- graph
+struct ora_graph {
+    int64_t N = 0, E = 0;
+    std::vector<std::vector<int32_t>> out, in, inns;  // inns = in-neighbours without self
+    std::vector<int32_t> selfcnt;
+    std::vector<double> Ld;     // fastlog table: logf((float)x) (fastlog.hpp:21-30)
+    std::vector<int64_t> Lq;    // the same values in units of 2^-24 (exact)
+};
+
+namespace {
+
+const double kFix = 16777216.0;  // 2^24
+const double kInvFix = 1.0 / 16777216.0;
+
+void build_log_tables(ora_graph* g) {
+    const int64_t n = g->E + 2;
+    g->Ld.resize(n);
+    g->Lq.resize(n);
+    g->Ld[0] = 0.0;
+    g->Lq[0] = 0;
+    for (int64_t x = 1; x < n; ++x) {
+        const double v = (double)logf((float)x);
+        g->Ld[x] = v;
+        g->Lq[x] = (int64_t)(v * kFix);
+    }
+}
+
+}  // namespace
+
+extern "C" void ora_philox(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
+    philox(ctr, key, out);
+}
+
+extern "C" ora_graph* ora_graph_create(int64_t N, int64_t E, const int32_t* src, const int32_t* dst) {
+    auto* g = new ora_graph();
+    g->N = N;
+    g->E = E;
+    g->out.assign(N, {});
+    g->in.assign(N, {});
+    g->inns.assign(N, {});
+    g->selfcnt.assign(N, 0);
+    // Graph::add_edge / utils::insert (graph.cpp:10-18): append in input order.
+    for (int64_t e = 0; e < E; ++e) {
+        const int32_t u = src[e], v = dst[e];
+        g->out[u].push_back(v);
+        g->in[v].push_back(u);
+        if (u == v) g->selfcnt[u]++;
+        else g->inns[v].push_back(u);
+    }
+    build_log_tables(g);
+    return g;
+}
+
+extern "C" void ora_graph_destroy(ora_graph* g) { delete g; }
+
+// ---------------------------------------------------------------- blockmodel
+struct ora_bm {
+    const ora_graph* g = nullptr;
+    int64_t B = 0;
+    std::vector<int32_t> asg;
+    std::vector<int64_t> dout, din, dtot, sizes;
+    std::vector<std::map<int32_t, int64_t>> row, col;  // matrix and transpose
+    double entropy = DBL_MAX;
+    int64_t num_blocks_to_merge = 0;
+    bool empty = false;
+
+    int64_t get(int64_t r, int64_t c) const {
+        auto it = row[r].find((int32_t)c);
+        return it == row[r].end() ? 0 : it->second;
+    }
+    /* DictTransposeMatrix::add + add_transpose; erase on zero as sub() and
+     * update_edge_counts() do (dict_transpose_matrix.cpp:3-16, 225-235, 430-446). */
+    void add(int64_t r, int64_t c, int64_t v) {
+        int64_t& a = row[r][(int32_t)c];
+        a += v;
+        int64_t& b = col[c][(int32_t)r];
+        b += v;
+        if (a == 0) {
+            row[r].erase((int32_t)c);
+            col[c].erase((int32_t)r);
+        }
+    }
+};
+
+namespace {
+
+/* Blockmodel::initialize_edge_counts (blockmodel.cpp:193-276). */
+void build(ora_bm* bm) {
+    const ora_graph* g = bm->g;
+    const int64_t B = bm->B;
+    bm->dout.assign(B, 0);
+    bm->din.assign(B, 0);
+    bm->dtot.assign(B, 0);
+    bm->sizes.assign(B, 0);
+    bm->row.assign(B, {});
+    bm->col.assign(B, {});
+    for (int64_t v = 0; v < g->N; ++v) {
+        const int32_t b = bm->asg[v];
+        bm->sizes[b]++;
+        for (int32_t u : g->out[v]) {
+            bm->row[b][bm->asg[u]] += 1;
+            bm->dout[b] += 1;
+            bm->dtot[b] += 1;
+        }
+        for (int32_t w : g->in[v]) {
+            const int32_t nb = bm->asg[w];
+            bm->col[b][nb] += 1;
+            bm->din[b] += 1;
+            if (b != nb) bm->dtot[b] += 1;
+        }
+    }
+}
+
+/* common::cell_entropy (common.hpp:39-50) in the reference's double arithmetic. */
+inline double ce_double(const ora_graph* g, int64_t v, int64_t din, int64_t dout) {
+    if (v == 0) return 0.0;
+    return (double)v * (g->Ld[v] - (g->Ld[din] + g->Ld[dout]));
+}
+/* The same term in units of 2^-24: every fastlog value is a multiple of 2^-24. */
+inline int64_t ce_fixed(const ora_graph* g, int64_t v, int64_t din, int64_t dout) {
+    if (v == 0) return 0;
+    return v * (g->Lq[v] - g->Lq[din] - g->Lq[dout]);
+}
+
+typedef std::map<std::pair<int32_t, int32_t>, int64_t> DeltaMap;  // key presence matters (H3)
+
+inline int64_t delta_get(const DeltaMap& d, int64_t r, int64_t c) {
+    auto it = d.find({(int32_t)r, (int32_t)c});
+    return it == d.end() ? 0 : it->second;
+}
+
+struct VertexInfo {
+    int64_t kout, kin, selfw;
+};
+
+inline VertexInfo vinfo(const ora_graph* g, int64_t v) {
+    return {(int64_t)g->out[v].size(), (int64_t)g->inns[v].size(), g->selfcnt[v] > 0 ? 1 : 0};
+}
+
+/* finetune::blockmodel_delta (finetune.cpp:201-235) with out_edges = all out-neighbours
+ * and in_edges = in-neighbours without the vertex itself (finetune.cpp:880-881). */
+DeltaMap vertex_delta(const ora_bm* bm, int64_t v, int64_t s) {
+    const ora_graph* g = bm->g;
+    const int64_t r = bm->asg[v];
+    DeltaMap d;
+    for (int32_t u : g->out[v]) {
+        const int32_t ob = bm->asg[u];
+        if (u == v) d[{(int32_t)s, (int32_t)s}] += 1;
+        else d[{(int32_t)s, ob}] += 1;
+        d[{(int32_t)r, ob}] -= 1;
+    }
+    for (int32_t w : g->inns[v]) {
+        const int32_t ib = bm->asg[w];
+        d[{ib, (int32_t)s}] += 1;
+        d[{ib, (int32_t)r}] -= 1;
+    }
+    return d;
+}
+
+/* block_merge::blockmodel_delta (block_merge.cpp:14-38). */
+DeltaMap merge_delta(const ora_bm* bm, int64_t r, int64_t s) {
+    DeltaMap d;
+    for (const auto& e : bm->row[r]) {
+        const int32_t c = e.first;
+        const int64_t v = e.second;
+        if (c == r || c == s) d[{(int32_t)s, (int32_t)s}] += v;
+        else d[{(int32_t)s, c}] += v;
+        d[{(int32_t)r, c}] -= v;
+    }
+    for (const auto& e : bm->col[r]) {
+        const int32_t x = e.first;
+        if (x == r) continue;
+        const int64_t v = e.second;
+        if (x == s) d[{(int32_t)s, (int32_t)s}] += v;
+        else d[{x, (int32_t)s}] += v;
+        d[{x, (int32_t)r}] -= v;
+    }
+    return d;
+}
+
+/* entropy::delta_mdl(Blockmodel, Delta, proposal) (entropy.cpp:298-403). */
+template <typename Acc, typename CE>
+Acc delta_mdl_generic(const ora_bm* bm, int64_t v, int64_t s, const DeltaMap& d, CE ce) {
+    const ora_graph* g = bm->g;
+    const int64_t r = bm->asg[v];
+    const VertexInfo vi = vinfo(g, v);
+    auto gin = [&](int64_t i) -> int64_t {
+        int64_t x = bm->din[i];
+        if (i == r) x -= (vi.kin + vi.selfw);
+        else if (i == s) x += (vi.kin + vi.selfw);
+        return x;
+    };
+    auto gout = [&](int64_t i) -> int64_t {
+        int64_t x = bm->dout[i];
+        if (i == r) x -= vi.kout;
+        else if (i == s) x += vi.kout;
+        return x;
+    };
+    Acc dS = 0;
+    for (const auto& e : d) {
+        const int64_t row = e.first.first, col = e.first.second, ch = e.second;
+        const int64_t m = bm->get(row, col);
+        dS += ce(g, m, bm->din[col], bm->dout[row]);
+        dS -= ce(g, m + ch, gin(col), gout(row));
+    }
+    for (const auto& e : bm->row[r]) {
+        const int64_t col = e.first, m = e.second;
+        if (delta_get(d, r, col) != 0) continue;
+        dS += ce(g, m, bm->din[col], bm->dout[r]);
+        dS -= ce(g, m, gin(col), gout(r));
+    }
+    for (const auto& e : bm->row[s]) {
+        const int64_t col = e.first, m = e.second;
+        if (delta_get(d, s, col) != 0) continue;
+        dS += ce(g, m, bm->din[col], bm->dout[s]);
+        dS -= ce(g, m, gin(col), gout(s));
+    }
+    for (const auto& e : bm->col[r]) {
+        const int64_t row = e.first, m = e.second;
+        if (delta_get(d, row, r) != 0 || row == r || row == s) continue;
+        dS += ce(g, m, bm->din[r], bm->dout[row]);
+        dS -= ce(g, m, gin(r), gout(row));
+    }
+    for (const auto& e : bm->col[s]) {
+        const int64_t row = e.first, m = e.second;
+        if (delta_get(d, row, s) != 0 || row == r || row == s) continue;
+        dS += ce(g, m, bm->din[s], bm->dout[row]);
+        dS -= ce(g, m, gin(s), gout(row));
+    }
+    return dS;
+}
+
+/* entropy::block_merge_delta_mdl (entropy.cpp:129-182). */
+template <typename Acc, typename CE>
+Acc merge_delta_mdl_generic(const ora_bm* bm, int64_t r, int64_t s, const DeltaMap& d, CE ce) {
+    const ora_graph* g = bm->g;
+    int64_t kout = 0, kin = 0;  // block_merge.cpp:65-69 (std::accumulate of row / column r)
+    for (const auto& e : bm->row[r]) kout += e.second;
+    for (const auto& e : bm->col[r]) kin += e.second;
+    auto gin = [&](int64_t i) -> int64_t {
+        int64_t x = bm->din[i];
+        if (i == r) x -= kin;
+        else if (i == s) x += kin;
+        return x;
+    };
+    auto gout = [&](int64_t i) -> int64_t {
+        int64_t x = bm->dout[i];
+        if (i == r) x -= kout;
+        else if (i == s) x += kout;
+        return x;
+    };
+    Acc dS = 0;
+    for (const auto& e : d) {
+        const int64_t row = e.first.first, col = e.first.second, ch = e.second;
+        const int64_t m = bm->get(row, col);
+        dS += ce(g, m, bm->din[col], bm->dout[row]);
+        if (row == r || col == r) continue;
+        dS -= ce(g, m + ch, gin(col), gout(row));
+    }
+    for (const auto& e : bm->row[s]) {
+        const int64_t col = e.first, m = e.second;
+        if (delta_get(d, s, col) != 0) continue;
+        dS += ce(g, m, bm->din[col], bm->dout[s]);
+        dS -= ce(g, m, gin(col), gout(s));
+    }
+    for (const auto& e : bm->col[s]) {
+        const int64_t row = e.first, m = e.second;
+        if (delta_get(d, row, s) != 0 || row == r || row == s) continue;
+        dS += ce(g, m, bm->din[s], bm->dout[row]);
+        dS -= ce(g, m, gin(s), gout(row));
+    }
+    return dS;
+}
+
+int64_t merge_dS_fixed(const ora_bm* bm, int64_t r, int64_t s) {
+    const DeltaMap d = merge_delta(bm, r, s);
+    return merge_delta_mdl_generic<int64_t>(bm, r, s, d, ce_fixed);
+}
+
+/* entropy::hastings_correction(vertex, ...) (entropy.cpp:497-561). */
+double hastings(const ora_bm* bm, int64_t v, int64_t s, const DeltaMap& d, int64_t num_neighbor_edges,
+                const ora_config* cfg) {
+    if (num_neighbor_edges == 0 || cfg->greedy) return 1.0;
+    const ora_graph* g = bm->g;
+    const int64_t r = bm->asg[v];
+    const VertexInfo vi = vinfo(g, v);
+    std::map<int32_t, int64_t> counts;
+    for (int32_t u : g->out[v]) counts[bm->asg[u]] += 1;
+    for (int32_t w : g->inns[v]) counts[bm->asg[w]] += 1;
+    double pf = 0.0, pb = 0.0;
+    const double B = (double)bm->B;
+    for (const auto& e : counts) {
+        const int64_t b = e.first;
+        const double cnt = (double)e.second;
+        const double pw = (double)(bm->get(s, b) + bm->get(b, s)) + 1.0;
+        const double bd = (double)bm->dtot[b] + B;
+        const double bw = (double)(bm->get(r, b) + delta_get(d, r, b) + bm->get(b, r) + delta_get(d, b, r)) + 1.0;
+        int64_t nd = bm->dtot[b];
+        if (b == r) {
+            const int64_t self = bm->get(r, r) + delta_get(d, r, r);
+            nd = (bm->dout[r] - vi.kout) + (bm->din[r] - vi.kin) - self;
+        } else if (b == s) {
+            const int64_t self = bm->get(s, s) + delta_get(d, s, s);
+            nd = (bm->dout[s] + vi.kout) + (bm->din[s] + vi.kin) - self;
+        }
+        pf += cnt * pw / bd;
+        pb += cnt * bw / ((double)nd + B);
+    }
+    return pb / pf;
+}
+
+/* finetune::accept (finetune.cpp:22-32). */
+inline bool accept(double dS, double H, const ora_config* cfg, uint32_t w) {
+    if (cfg->greedy) return dS < 0.0;
+    const double u = (double)w * (1.0 / 4294967296.0);
+    double p = exp(-3.0 * dS) * H;
+    p = p >= 1.0 ? 1.0 : p;
+    return u <= p;
+}
+
+/* Walk `m` in ascending key order and return the key at cumulative position t,
+ * skipping keys skip1 / skip2. */
+inline int64_t walk(const std::map<int32_t, int64_t>& m, uint64_t t, int64_t skip1, int64_t skip2) {
+    uint64_t acc = 0;
+    for (const auto& e : m) {
+        if (e.first == skip1 || e.first == skip2) continue;
+        acc += (uint64_t)e.second;
+        if (t < acc) return e.first;
+    }
+    return -1;
+}
+
+inline uint64_t sum_excl(const std::map<int32_t, int64_t>& m, int64_t skip1, int64_t skip2) {
+    uint64_t acc = 0;
+    for (const auto& e : m)
+        if (e.first != skip1 && e.first != skip2) acc += (uint64_t)e.second;
+    return acc;
+}
+
+/* common::propose_new_block(..., block_merge=false) (common.cpp:138-198) under the
+ * canonical stream. */
+int64_t propose_vertex(const ora_bm* bm, int64_t v, const uint32_t w[4]) {
+    const ora_graph* g = bm->g;
+    const int64_t r = bm->asg[v];
+    const int64_t kout = (int64_t)g->out[v].size(), kin = (int64_t)g->inns[v].size();
+    const int64_t k = kout + kin;
+    if (k == 0) return random_block(r, bm->B, w[1]);
+    const int64_t idx = u32_below(w[0], (uint32_t)k);
+    const int32_t nbr = idx < kout ? g->out[v][idx] : g->inns[v][idx - kout];
+    const int64_t nb = bm->asg[nbr];
+    const uint64_t R = sum_excl(bm->row[nb], -1, -1);
+    const uint64_t C = sum_excl(bm->col[nb], nb, -1);
+    const uint64_t t = u64_below(w[1], w[2], R + C);
+    if (t < R) return walk(bm->row[nb], t, -1, -1);
+    return walk(bm->col[nb], t - R, nb, -1);
+}
+
+/* common::propose_new_block(..., block_merge=true) as called by
+ * block_merge::propose_merge_sparse (block_merge.cpp:251-256). */
+int64_t propose_merge(const ora_bm* bm, int64_t r, const uint32_t w[4]) {
+    const uint64_t Rr = sum_excl(bm->row[r], -1, -1);
+    const uint64_t Cr = sum_excl(bm->col[r], -1, -1);
+    if (Rr + Cr == 0) return random_block(r, bm->B, w[0]);
+    const uint64_t t = u64_below(w[0], w[1], Rr + Cr);
+    const int64_t nb = t < Rr ? walk(bm->row[r], t, -1, -1) : walk(bm->col[r], t - Rr, -1, -1);
+    const uint64_t R2 = sum_excl(bm->row[nb], r, -1);
+    const uint64_t C2 = sum_excl(bm->col[nb], nb, r);
+    if (R2 + C2 == 0) return random_block(r, bm->B, w[2]);
+    const uint64_t t2 = u64_below(w[2], w[3], R2 + C2);
+    if (t2 < R2) return walk(bm->row[nb], t2, r, -1);
+    return walk(bm->col[nb], t2 - R2, nb, r);
+}
+
+/* Blockmodel::move_vertex(const VertexMove_v3&) (blockmodel.cpp:437-494). */
+bool apply_v3(ora_bm* bm, int64_t v, int64_t s) {
+    const ora_graph* g = bm->g;
+    const int64_t r = bm->asg[v];
+    if (bm->sizes[r] == 1) return false;
+    for (int32_t u : g->out[v]) {
+        const int64_t ob = bm->asg[u];
+        bm->add(r, ob, -1);
+        bm->dout[r]--;
+        bm->dout[s]++;
+        if (u == v) {
+            bm->add(s, s, 1);
+            bm->din[r]--;
+            bm->din[s]++;
+        } else {
+            bm->add(s, ob, 1);
+        }
+    }
+    for (int32_t w : g->inns[v]) {
+        const int64_t ib = bm->asg[w];
+        bm->add(ib, r, -1);
+        bm->din[r]--;
+        bm->add(ib, s, 1);
+        bm->din[s]++;
+    }
+    bm->dtot[r] = bm->din[r] + bm->dout[r] - bm->get(r, r);
+    bm->dtot[s] = bm->din[s] + bm->dout[s] - bm->get(s, s);
+    bm->asg[v] = (int32_t)s;
+    bm->sizes[r]--;
+    bm->sizes[s]++;
+    return true;
+}
+
+/* Blockmodel::move_vertex(Vertex, Delta, proposal) (blockmodel.cpp:408-435). */
+void apply_delta_move(ora_bm* bm, int64_t v, int64_t s, const DeltaMap& d) {
+    const VertexInfo vi = vinfo(bm->g, v);
+    const int64_t r = bm->asg[v];
+    bm->asg[v] = (int32_t)s;
+    for (const auto& e : d) {
+        if (e.second == 0) {
+            // update_edge_counts inserts then erases a zero cell: no net change.
+            continue;
+        }
+        bm->add(e.first.first, e.first.second, e.second);
+    }
+    bm->dout[r] -= vi.kout;
+    bm->dout[s] += vi.kout;
+    bm->din[r] -= (vi.kin + vi.selfw);
+    bm->din[s] += (vi.kin + vi.selfw);
+    bm->dtot[r] = bm->dout[r] + bm->din[r] - bm->get(r, r);
+    bm->dtot[s] = bm->dout[s] + bm->din[s] - bm->get(s, s);
+    bm->sizes[r]--;
+    bm->sizes[s]++;
+}
+
+/* Canonical MDL log term: round-to-float(log(x)) in units of 2^-24 (see sbp_oracle.h). */
+inline int64_t canon_log_q(double ratio) {
+    const float xf = (float)ratio;
+    const float lf = (float)log((double)xf);
+    return (int64_t)((double)lf * kFix);
+}
+
+void mdl_both(const ora_bm* bm, double* literal, double* canonical) {
+    const ora_graph* g = bm->g;
+    double lp = 0.0;
+    __int128 lpq = 0;
+    for (int64_t r = 0; r < bm->B; ++r) {
+        for (const auto& e : bm->row[r]) {
+            const double v = (double)e.second;
+            const double ratio = v / ((double)bm->dout[r] * (double)bm->din[e.first]);
+            lp += v * (double)logf(ratio);  // utils::nat_log (utils.hpp:228-238)
+            lpq += (__int128)e.second * canon_log_q(ratio);
+        }
+    }
+    const double E = (double)g->E;
+    const double x = pow((double)bm->B, 2) / E;
+    const double h = ((1 + x) * log(1 + x)) - (x * log(x));
+    const double model = (E * h) + ((double)g->N * log((double)bm->B));
+    if (literal) *literal = model - lp;
+    if (canonical) *canonical = model - (double)(int64_t)lpq * kInvFix;
+}
+
+double mdl_canonical(const ora_bm* bm) {
+    double c;
+    mdl_both(bm, nullptr, &c);
+    return c;
+}
+
+/* finetune::early_stop (finetune.cpp:265-283). */
+bool early_stop(int64_t iteration, bool golden_ratio_not_reached, double initial_entropy,
+                const std::vector<double>& d) {
+    const size_t last = d.size() - 1;
+    if (d[last] == 0.0) return true;
+    if (iteration < 3) return false;
+    double average = d[last] + d[last - 1] + d[last - 2];
+    average /= -3.0;
+    const double threshold = golden_ratio_not_reached ? 5e-4 * initial_entropy : 1e-4 * initial_entropy;
+    return average < threshold;
+}
+
+/* Graph::sort_vertices (graph.cpp:235-268): stable sort by degree descending; the first
+ * (mh_percent * N) become high-degree vertices.  mh_percent is a float in the reference. */
+void sort_vertices(const ora_graph* g, float mh_percent, std::vector<int32_t>& hdv, std::vector<int32_t>& ldv) {
+    std::vector<int64_t> deg(g->N);
+    for (int64_t v = 0; v < g->N; ++v)
+        deg[v] = (int64_t)g->out[v].size() + (int64_t)g->in[v].size() - (g->selfcnt[v] > 0 ? 1 : 0);
+    std::vector<int32_t> idx(g->N);
+    for (int64_t v = 0; v < g->N; ++v) idx[v] = (int32_t)v;
+    std::stable_sort(idx.begin(), idx.end(), [&](int32_t a, int32_t b) { return deg[a] > deg[b]; });
+    const float limit = mh_percent * (float)g->N;
+    hdv.clear();
+    ldv.clear();
+    for (int64_t i = 0; i < g->N; ++i) {
+        if ((float)i < limit) hdv.push_back(idx[i]);
+        else ldv.push_back(idx[i]);
+    }
+}
+
+/* Canonical shuffle: order the base list by (philox word, position). */
+void shuffle(std::vector<int32_t>& out, const std::vector<int32_t>& base, uint64_t seed, uint32_t iteration,
+             uint32_t step, uint32_t dom) {
+    std::vector<std::pair<uint64_t, int32_t>> keys(base.size());
+    for (size_t i = 0; i < base.size(); ++i) {
+        uint32_t w[4];
+        draw(seed, (uint32_t)i, iteration, step, dom, w);
+        keys[i] = {((uint64_t)w[0] << 32) | (uint64_t)i, base[i]};
+    }
+    std::sort(keys.begin(), keys.end());
+    out.resize(base.size());
+    for (size_t i = 0; i < base.size(); ++i) out[i] = keys[i].second;
+}
+
+struct Proposal {
+    int32_t s;
+    double dS;
+    bool did_move;
+};
+
+/* finetune::propose_gibbs_move_v3 + eval_vertex_move_v3 (finetune.cpp:871-901, 447-462). */
+Proposal gibbs_proposal(const ora_bm* bm, int64_t v, uint64_t seed, uint32_t iteration, uint32_t step,
+                        const ora_config* cfg) {
+    uint32_t w[4];
+    draw(seed, (uint32_t)v, iteration, step, DOM_GIBBS, w);
+    const int64_t r = bm->asg[v];
+    const int64_t s = propose_vertex(bm, v, w);
+    if (s == r) return {-1, 0.0, false};
+    const DeltaMap d = vertex_delta(bm, v, s);
+    const double dS = (double)delta_mdl_generic<int64_t>(bm, v, s, d, ce_fixed) * kInvFix;
+    const VertexInfo vi = vinfo(bm->g, v);
+    const double H = hastings(bm, v, s, d, vi.kout + vi.kin, cfg);
+    if (accept(dS, H, cfg, w[3])) return {(int32_t)s, dS, true};
+    return {-1, dS, false};
+}
+
+/* finetune::propose_move + move_vertex (finetune.cpp:842-869, 822-840). */
+bool mh_step(ora_bm* bm, int64_t v, uint64_t seed, uint32_t iteration, uint32_t step, const ora_config* cfg,
+             double* dS_out) {
+    const int64_t r = bm->asg[v];
+    if (bm->sizes[r] == 1) return false;
+    uint32_t w[4];
+    draw(seed, (uint32_t)v, iteration, step, DOM_MH, w);
+    const int64_t s = propose_vertex(bm, v, w);
+    if (s == r) return false;
+    const DeltaMap d = vertex_delta(bm, v, s);
+    const double dS = (double)delta_mdl_generic<int64_t>(bm, v, s, d, ce_fixed) * kInvFix;
+    const VertexInfo vi = vinfo(bm->g, v);
+    const double H = hastings(bm, v, s, d, vi.kout + vi.kin, cfg);
+    if (!accept(dS, H, cfg, w[3])) return false;
+    apply_delta_move(bm, v, s, d);
+    if (dS_out) *dS_out = dS;
+    return true;
+}
+
+void add_stats(ora_stats* st, const ora_graph* g, int64_t v) {
+    if (!st) return;
+    st->proposals++;
+    st->edges_swept += (int64_t)g->out[v].size() + (int64_t)g->inns[v].size();
+}
+
+/* One batch: parallel proposals against one snapshot, then the serial apply loop in
+ * vertex-id order (finetune.cpp:63-86 / 604-623). */
+int64_t gibbs_batch(ora_bm* bm, const int32_t* vertices, int64_t n, uint64_t seed, uint32_t iteration,
+                    uint32_t step, const ora_config* cfg, int32_t* out_moves, double* out_dS, ora_stats* st) {
+    const int64_t N = bm->g->N;
+    std::vector<int32_t> moves(N, -1);
+    std::vector<double> dSs(n, 0.0);
+    std::vector<int32_t> props(n, -1);
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int64_t i = 0; i < n; ++i) {
+        const Proposal p = gibbs_proposal(bm, vertices[i], seed, iteration, step, cfg);
+        props[i] = p.did_move ? p.s : -1;
+        dSs[i] = p.dS;
+    }
+    for (int64_t i = 0; i < n; ++i) {
+        moves[vertices[i]] = props[i];
+        if (out_moves) out_moves[i] = props[i];
+        if (out_dS) out_dS[i] = dSs[i];
+        add_stats(st, bm->g, vertices[i]);
+    }
+    int64_t applied = 0;
+    for (int64_t v = 0; v < N; ++v) {
+        if (moves[v] < 0) continue;
+        if (apply_v3(bm, v, moves[v])) applied++;
+    }
+    if (st) st->moves += applied;
+    return applied;
+}
+
+/* finetune::asynchronous_gibbs (finetune.cpp:34-107). */
+void async_gibbs(ora_bm* bm, const ora_config* cfg, uint64_t seed, uint32_t step, bool golden, ora_stats* st) {
+    const ora_graph* g = bm->g;
+    if (bm->B == 1) return;
+    std::vector<double> deltas;
+    const double initial = mdl_canonical(bm);
+    bm->entropy = initial;
+    double last = initial;
+    std::vector<int32_t> base(g->N), order;
+    for (int64_t v = 0; v < g->N; ++v) base[v] = (int32_t)v;
+    for (int it = 0; it < cfg->max_iterations; ++it) {
+        const bool shuffled = !cfg->ordered && cfg->batches > 1;
+        if (shuffled) shuffle(order, base, seed, (uint32_t)it, step, DOM_SHUFFLE_ALL);
+        const std::vector<int32_t>& vs = shuffled ? order : base;
+        const double nb = (double)cfg->batches;
+        const int64_t batch_size = (int64_t)ceil((double)g->N / nb);
+        for (int64_t batch = 0; batch_size > 0 && batch < g->N / batch_size; ++batch) {
+            const int64_t start = batch * batch_size;
+            const int64_t end = std::min(g->N, (batch + 1) * batch_size);
+            gibbs_batch(bm, vs.data() + start, end - start, seed, (uint32_t)it, step, cfg, nullptr, nullptr, st);
+        }
+        const double e = mdl_canonical(bm);
+        deltas.push_back(e - last);
+        last = e;
+        if (st) st->mcmc_iterations++;
+        if (early_stop(it, golden, initial, deltas)) break;
+    }
+    bm->entropy = mdl_canonical(bm);
+}
+
+/* finetune::hybrid_mcmc (finetune.cpp:563-646). */
+void hybrid_mcmc(ora_bm* bm, const ora_config* cfg, uint64_t seed, uint32_t step, bool golden, ora_stats* st) {
+    const ora_graph* g = bm->g;
+    if (bm->B == 1) return;
+    std::vector<double> deltas;
+    const double initial = mdl_canonical(bm);
+    bm->entropy = initial;
+    double last = initial;
+    std::vector<int32_t> hdv0, ldv0, hdv, ldv;
+    sort_vertices(g, cfg->mh_percent, hdv0, ldv0);
+    const int64_t nlow = (int64_t)ldv0.size();
+    const int64_t batch_size = (int64_t)ceil((double)nlow / (double)cfg->batches);
+    for (int it = 0; it < cfg->max_iterations; ++it) {
+        if (!cfg->ordered) {
+            shuffle(hdv, hdv0, seed, (uint32_t)it, step, DOM_SHUFFLE_HDV);
+            if (cfg->batches > 1) shuffle(ldv, ldv0, seed, (uint32_t)it, step, DOM_SHUFFLE_ALL);
+            else ldv = ldv0;
+        } else {
+            hdv = hdv0;
+            ldv = ldv0;
+        }
+        for (int32_t v : hdv) {
+            add_stats(st, g, v);
+            if (mh_step(bm, v, seed, (uint32_t)it, step, cfg, nullptr) && st) st->moves++;
+        }
+        for (int64_t batch = 0; batch_size > 0 && batch < nlow / batch_size; ++batch) {
+            const int64_t start = batch * batch_size;
+            const int64_t end = std::min(nlow, (batch + 1) * batch_size);
+            gibbs_batch(bm, ldv.data() + start, end - start, seed, (uint32_t)it, step, cfg, nullptr, nullptr, st);
+        }
+        const double e = mdl_canonical(bm);
+        deltas.push_back(e - last);
+        last = e;
+        if (st) st->mcmc_iterations++;
+        if (early_stop(it, golden, initial, deltas)) break;
+    }
+    bm->entropy = mdl_canonical(bm);
+}
+
+/* finetune::metropolis_hastings (finetune.cpp:773-820). */
+void metropolis_hastings(ora_bm* bm, const ora_config* cfg, uint64_t seed, uint32_t step, bool golden,
+                         ora_stats* st) {
+    const ora_graph* g = bm->g;
+    if (bm->B == 1) return;
+    std::vector<double> deltas;
+    bm->entropy = mdl_canonical(bm);
+    std::vector<int32_t> base(g->N), order;
+    for (int64_t v = 0; v < g->N; ++v) base[v] = (int32_t)v;
+    for (int it = 0; it < cfg->max_iterations; ++it) {
+        if (!cfg->ordered) shuffle(order, base, seed, (uint32_t)it, step, DOM_SHUFFLE_ALL);
+        const std::vector<int32_t>& vs = cfg->ordered ? base : order;
+        double dsum = 0.0;
+        for (int32_t v : vs) {
+            double dS = 0.0;
+            add_stats(st, g, v);
+            if (mh_step(bm, v, seed, (uint32_t)it, step, cfg, &dS)) {
+                dsum += dS;
+                if (st) st->moves++;
+            }
+        }
+        deltas.push_back(dsum);
+        if (st) st->mcmc_iterations++;
+        if (early_stop(it, golden, bm->entropy, deltas)) break;
+    }
+    bm->entropy = mdl_canonical(bm);
+}
+
+/* Blockmodel::build_mapping (blockmodel.cpp:34-46) + relabel. */
+void relabel(ora_bm* bm) {
+    std::map<int32_t, int32_t> mapping;
+    for (int32_t b : bm->asg) mapping[b] = 0;
+    int32_t c = 0;
+    for (auto& e : mapping) e.second = c++;
+    for (auto& b : bm->asg) b = mapping[b];
+}
+
+/* Blockmodel::merge_block (blockmodel.cpp:337-363) without the O(N) assignment loop,
+ * which the caller replaces by union-find (the resulting labels are identical). */
+void merge_block(ora_bm* bm, int64_t from, int64_t to, const DeltaMap& d) {
+    int64_t kout = 0, kin = 0;
+    for (const auto& e : bm->row[from]) kout += e.second;
+    for (const auto& e : bm->col[from]) kin += e.second;
+    const int64_t self = bm->get(to, to) + delta_get(d, to, to);
+    for (const auto& e : d)
+        if (e.second != 0) bm->add(e.first.first, e.first.second, e.second);
+    bm->dout[from] = 0;
+    bm->dout[to] += kout;
+    bm->din[from] = 0;
+    bm->din[to] += kin;
+    bm->dtot[from] = 0;
+    bm->dtot[to] = bm->dout[to] + bm->din[to] - self;
+    bm->sizes[to] += bm->sizes[from];
+    bm->sizes[from] = 0;
+}
+
+int64_t uf_find(std::vector<int64_t>& parent, int64_t x) {
+    int64_t root = x;
+    while (parent[root] != root) root = parent[root];
+    while (parent[x] != root) {
+        const int64_t nx = parent[x];
+        parent[x] = root;
+        x = nx;
+    }
+    return root;
+}
+
+/* block_merge::carry_out_best_merges_advanced (block_merge.cpp:40-117).  The queue is
+ * ordered by (delta entropy, block); the reference's std::priority_queue leaves ties in
+ * an implementation-defined order. */
+int carry_out_advanced(ora_bm* bm, const std::vector<double>& dS, const std::vector<int64_t>& best,
+                       int64_t num_to_merge, ora_stats* st) {
+    std::set<std::pair<double, int64_t>> queue;
+    std::vector<int64_t> prop(best);
+    for (int64_t i = 0; i < (int64_t)dS.size(); ++i) queue.insert({dS[i], i});
+    std::vector<int64_t> parent(bm->B);
+    for (int64_t i = 0; i < bm->B; ++i) parent[i] = i;
+    int64_t merged = 0;
+    while (merged < num_to_merge && !queue.empty()) {
+        const auto top = *queue.begin();
+        queue.erase(queue.begin());
+        const int64_t from = top.second;
+        const int64_t to = uf_find(parent, prop[from]);
+        if (from == to) continue;
+        const DeltaMap d = merge_delta(bm, from, to);
+        const double actual = (double)merge_delta_mdl_generic<int64_t>(bm, from, to, d, ce_fixed) * kInvFix;
+        if (!queue.empty() && actual > queue.begin()->first) {
+            queue.insert({actual, from});
+            continue;
+        }
+        merge_block(bm, from, to, d);
+        parent[from] = to;
+        merged++;
+    }
+    for (auto& b : bm->asg) b = (int32_t)uf_find(parent, b);
+    relabel(bm);
+    if (st) st->merges += merged;
+    return 0;
+}
+
+/* Blockmodel::carry_out_best_merges (blockmodel.cpp:55-122), used with --approximate. */
+int carry_out_approximate(ora_bm* bm, const std::vector<double>& dS, const std::vector<int64_t>& best,
+                          int64_t num_to_merge, ora_stats* st) {
+    const int64_t B = bm->B;
+    std::vector<int64_t> order(B);
+    for (int64_t i = 0; i < B; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t b) { return dS[a] < dS[b]; });
+    std::vector<int64_t> block_map(B);
+    for (int64_t i = 0; i < B; ++i) block_map[i] = i;
+    auto translate = [&](int64_t b) {
+        do { b = block_map[b]; } while (block_map[b] != b);
+        return b;
+    };
+    int64_t merged = 0, counter = 0;
+    while (merged < num_to_merge && counter < B) {
+        const int64_t from = order[counter];
+        const int64_t to = translate(best[from]);
+        counter++;
+        if (to != from) {
+            block_map[from] = to;
+            merged++;
+        }
+    }
+    for (auto& b : bm->asg) b = (int32_t)translate(b);
+    relabel(bm);
+    if (st) st->merges += merged;
+    return 0;
+}
+
+/* block_merge::merge_blocks (block_merge.cpp:178-228). */
+int merge_blocks(ora_bm* bm, const ora_config* cfg, uint64_t seed, uint32_t step, int64_t num_to_merge,
+                 ora_stats* st) {
+    const int64_t B = bm->B;
+    std::vector<int64_t> best(B, -1);
+    std::vector<double> best_dS(B, DBL_MAX);
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int64_t r = 0; r < B; ++r) {
+        std::set<int64_t> past;
+        for (int i = 0; i < 10; ++i) {  // NUM_AGG_PROPOSALS_PER_BLOCK (block_merge.hpp:23)
+            uint32_t w[4];
+            draw(seed, (uint32_t)r, 0, step, DOM_MERGE | ((uint32_t)i << 8), w);
+            const int64_t s = propose_merge(bm, r, w);
+            double dS = DBL_MAX;
+            if (!past.count(s)) {
+                dS = (double)merge_dS_fixed(bm, r, s) * kInvFix;
+                past.insert(s);
+            }
+            if (dS < best_dS[r]) {
+                best_dS[r] = dS;
+                best[r] = s;
+            }
+        }
+    }
+    if (st) st->merge_proposals += 10 * B;
+    int rc = cfg->approximate ? carry_out_approximate(bm, best_dS, best, num_to_merge, st)
+                              : carry_out_advanced(bm, best_dS, best, num_to_merge, st);
+    if (rc) return rc;
+    bm->B = B - num_to_merge;
+    int32_t mx = -1;
+    for (int32_t b : bm->asg) mx = std::max(mx, b);
+    if (mx + 1 != bm->B) return -2;  // fewer merges than requested: inconsistent labels
+    build(bm);
+    return 0;
+}
+
+int mcmc(ora_bm* bm, const ora_config* cfg, uint64_t seed, int32_t step, bool golden, ora_stats* st) {
+    if (cfg->algorithm == 0 && step < cfg->asynciterations)
+        async_gibbs(bm, cfg, seed, (uint32_t)step, golden, st);
+    else if (cfg->algorithm == 1)
+        hybrid_mcmc(bm, cfg, seed, (uint32_t)step, golden, st);
+    else
+        metropolis_hastings(bm, cfg, seed, (uint32_t)step, golden, st);
+    return 0;
+}
+
+// ---------------------------------------------------------------- golden-section triplet
+/* BlockmodelTriplet (blockmodel_triplet.cpp:4-105), keeping assignments only: a slot is
+ * rebuilt from its assignment when resumed, which gives the same blockmodel state. */
+struct Slot {
+    bool empty = true;
+    int64_t B = 0;
+    double entropy = DBL_MAX;
+    std::vector<int32_t> asg;
+};
+
+struct Triplet {
+    Slot s[3];
+    bool optimal = false;
+    bool golden_ratio_not_reached() const { return s[2].empty; }
+    void update(const ora_bm* bm) {
+        int idx;
+        if (s[1].empty) {
+            idx = 1;
+        } else if (bm->entropy <= s[1].entropy) {
+            const int old = (s[1].B > bm->B) ? 0 : 2;
+            s[old] = s[1];
+            idx = 1;
+        } else {
+            idx = (s[1].B > bm->B) ? 2 : 0;
+        }
+        s[idx].empty = false;
+        s[idx].B = bm->B;
+        s[idx].entropy = bm->entropy;
+        s[idx].asg = bm->asg;
+    }
+    bool is_done() {
+        if ((!s[0].empty && s[0].B - s[2].B == 2) || (s[0].empty && s[1].B - s[2].B == 1)) optimal = true;
+        return optimal;
+    }
+};
+
+}  // namespace
+
+// ---------------------------------------------------------------- C API
+extern "C" ora_bm* ora_bm_create(const ora_graph* g, int64_t B, const int32_t* asg) {
+    auto* bm = new ora_bm();
+    bm->g = g;
+    bm->B = B;
+    bm->asg.assign(asg, asg + g->N);
+    bm->num_blocks_to_merge = (int64_t)((double)B * 0.5);
+    build(bm);
+    return bm;
+}
+extern "C" ora_bm* ora_bm_copy(const ora_bm* bm) { return new ora_bm(*bm); }
+extern "C" void ora_bm_destroy(ora_bm* bm) { delete bm; }
+extern "C" int64_t ora_bm_num_blocks(const ora_bm* bm) { return bm->B; }
+extern "C" int64_t ora_bm_nnz(const ora_bm* bm) {
+    int64_t n = 0;
+    for (const auto& r : bm->row) n += (int64_t)r.size();
+    return n;
+}
+extern "C" void ora_bm_read(const ora_bm* bm, int32_t* asg, int64_t* dout, int64_t* din, int64_t* dtot,
+                            int64_t* sizes, int32_t* rows, int32_t* cols, int64_t* counts) {
+    if (asg) std::copy(bm->asg.begin(), bm->asg.end(), asg);
+    if (dout) std::copy(bm->dout.begin(), bm->dout.end(), dout);
+    if (din) std::copy(bm->din.begin(), bm->din.end(), din);
+    if (dtot) std::copy(bm->dtot.begin(), bm->dtot.end(), dtot);
+    if (sizes) std::copy(bm->sizes.begin(), bm->sizes.end(), sizes);
+    if (rows || cols || counts) {
+        int64_t i = 0;
+        for (int64_t r = 0; r < bm->B; ++r)
+            for (const auto& e : bm->row[r]) {
+                if (rows) rows[i] = (int32_t)r;
+                if (cols) cols[i] = e.first;
+                if (counts) counts[i] = e.second;
+                ++i;
+            }
+    }
+}
+extern "C" int64_t ora_bm_get(const ora_bm* bm, int64_t r, int64_t c) { return bm->get(r, c); }
+
+extern "C" void ora_mdl(const ora_bm* bm, double* literal, double* canonical) { mdl_both(bm, literal, canonical); }
+
+extern "C" void ora_delta_mdl(const ora_bm* bm, int64_t v, int64_t s, double* literal, int64_t* fixed) {
+    const DeltaMap d = vertex_delta(bm, v, s);
+    if (literal) *literal = delta_mdl_generic<double>(bm, v, s, d, ce_double);
+    if (fixed) *fixed = delta_mdl_generic<int64_t>(bm, v, s, d, ce_fixed);
+}
+
+extern "C" void ora_merge_delta_mdl(const ora_bm* bm, int64_t r, int64_t s, double* literal, int64_t* fixed) {
+    const DeltaMap d = merge_delta(bm, r, s);
+    if (literal) *literal = merge_delta_mdl_generic<double>(bm, r, s, d, ce_double);
+    if (fixed) *fixed = merge_delta_mdl_generic<int64_t>(bm, r, s, d, ce_fixed);
+}
+
+static int64_t dump_delta(const DeltaMap& d, int32_t* rows, int32_t* cols, int64_t* vals, int64_t cap) {
+    int64_t i = 0;
+    for (const auto& e : d) {
+        if (i < cap) {
+            rows[i] = e.first.first;
+            cols[i] = e.first.second;
+            vals[i] = e.second;
+        }
+        ++i;
+    }
+    return i;
+}
+
+extern "C" int64_t ora_vertex_delta(const ora_bm* bm, int64_t v, int64_t s, int32_t* rows, int32_t* cols,
+                                    int64_t* vals, int64_t cap) {
+    return dump_delta(vertex_delta(bm, v, s), rows, cols, vals, cap);
+}
+
+extern "C" int64_t ora_merge_delta(const ora_bm* bm, int64_t r, int64_t s, int32_t* rows, int32_t* cols,
+                                   int64_t* vals, int64_t cap) {
+    return dump_delta(merge_delta(bm, r, s), rows, cols, vals, cap);
+}
+
+extern "C" int64_t ora_propose_vertex(const ora_bm* bm, int64_t v, uint64_t seed, uint32_t c1, uint32_t c2,
+                                      uint32_t c3) {
+    uint32_t w[4];
+    draw(seed, (uint32_t)v, c1, c2, c3, w);
+    return propose_vertex(bm, v, w);
+}
+
+extern "C" int64_t ora_propose_merge(const ora_bm* bm, int64_t r, uint64_t seed, uint32_t step, int32_t i) {
+    uint32_t w[4];
+    draw(seed, (uint32_t)r, 0, step, DOM_MERGE | ((uint32_t)i << 8), w);
+    return propose_merge(bm, r, w);
+}
+
+extern "C" int64_t ora_gibbs_batch(ora_bm* bm, const int32_t* vertices, int64_t n, uint64_t seed,
+                                   uint32_t iteration, uint32_t step, const ora_config* cfg, int32_t* out_moves,
+                                   double* out_dS) {
+    return gibbs_batch(bm, vertices, n, seed, iteration, step, cfg, out_moves, out_dS, nullptr);
+}
+
+extern "C" int64_t ora_apply_moves(ora_bm* bm, const int32_t* moves) {
+    int64_t applied = 0;
+    for (int64_t v = 0; v < bm->g->N; ++v)
+        if (moves[v] >= 0 && apply_v3(bm, v, moves[v])) applied++;
+    return applied;
+}
+
+extern "C" int64_t ora_mh_chain(ora_bm* bm, const int32_t* order, int64_t n, uint64_t seed, uint32_t iteration,
+                                uint32_t step, const ora_config* cfg) {
+    int64_t applied = 0;
+    for (int64_t i = 0; i < n; ++i)
+        if (mh_step(bm, order[i], seed, iteration, step, cfg, nullptr)) applied++;
+    return applied;
+}
+
+extern "C" int ora_mcmc(ora_bm* bm, const ora_config* cfg, uint64_t seed, int32_t step,
+                        int32_t golden_ratio_not_reached, ora_stats* st) {
+    return mcmc(bm, cfg, seed, step, golden_ratio_not_reached != 0, st);
+}
+
+extern "C" int ora_merge_blocks(ora_bm* bm, const ora_config* cfg, uint64_t seed, int32_t step,
+                                int64_t num_to_merge, ora_stats* st) {
+    return merge_blocks(bm, cfg, seed, (uint32_t)step, num_to_merge, st);
+}
+
+/* sbp::stochastic_block_partition (sbp.cpp:16-72) with BlockmodelTriplet::get_next_blockmodel
+ * (blockmodel_triplet.cpp:4-37). */
+extern "C" int64_t ora_sbp(const ora_graph* g, const ora_config* cfg, uint64_t seed, int32_t* out_asg,
+                           double* out_mdl, ora_stats* st) {
+    std::vector<int32_t> ident(g->N);
+    for (int64_t v = 0; v < g->N; ++v) ident[v] = (int32_t)v;
+    ora_bm* bm = ora_bm_create(g, g->N, ident.data());
+    bm->entropy = DBL_MAX;
+    Triplet t;
+    int32_t step = 0;
+    while (!t.optimal) {
+        int rc = merge_blocks(bm, cfg, seed, (uint32_t)step, bm->num_blocks_to_merge, st);
+        if (rc) {
+            delete bm;
+            return -1;
+        }
+        mcmc(bm, cfg, seed, step, t.golden_ratio_not_reached(), st);
+        ++step;
+        if (st) st->outer_steps++;
+        // get_next_blockmodel
+        t.update(bm);
+        int64_t next_B, next_merge;
+        const Slot* src;
+        if (t.golden_ratio_not_reached()) {
+            src = &t.s[1];
+            next_B = src->B;
+            next_merge = (int64_t)((double)next_B * 0.5);
+            if (next_merge == 0) t.optimal = true;
+        } else if (t.is_done()) {
+            src = &t.s[1];
+            next_merge = 0;
+        } else {
+            int index = 1;
+            if (t.s[0].empty && t.s[1].B > t.s[2].B) index = 1;
+            else if ((t.s[0].B - t.s[1].B) >= (t.s[1].B - t.s[2].B)) index = 0;
+            else index = 1;
+            int64_t next_try = t.s[index + 1].B;
+            next_try += (int64_t)((double)(t.s[index].B - t.s[index + 1].B) * 0.618);
+            src = &t.s[index];
+            next_merge = src->B - next_try;
+        }
+        delete bm;
+        bm = ora_bm_create(g, src->B, src->asg.data());
+        bm->entropy = src->entropy;
+        bm->num_blocks_to_merge = next_merge;
+    }
+    const int64_t B = bm->B;
+    if (out_asg) std::copy(bm->asg.begin(), bm->asg.end(), out_asg);
+    if (out_mdl) *out_mdl = bm->entropy;
+    delete bm;
+    return B;
+}
+
+extern "C" double ora_null_mdl_v1(double E) {
+    const double log_posterior_p = E * log(1.0 / E);
+    const double x = 1.0 / E;
+    const double h = ((1 + x) * log(1 + x)) - (x * log(x));
+    return (E * h) - log_posterior_p;
+}

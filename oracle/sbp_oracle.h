@@ -1,0 +1,126 @@
+/*
+ * CPU oracle for the SBP hot path -- TEST INFRASTRUCTURE ONLY.
+ *
+ * This library restates, on the CPU and single-address-space, the reference
+ * algorithm of vtsynergy/SBP for the MCMC vertex-move sweep (asynchronous Gibbs,
+ * hybrid MCMC, Metropolis-Hastings) and the block-merge pass, scored by delta-MDL
+ * over the blockmodel.  It is used by the test-suite, by the package's smoke check
+ * and by the CPU-baseline leg of the benchmark as the checker; the product never
+ * links, imports or executes it.
+ *
+ * Every function cites the reference file:line it follows.  Where the reference is
+ * non-reproducible (std::random_device seeding, robin_map iteration order) the
+ * oracle uses the canonical seeded stream that the GPU implementation also uses:
+ * Philox4x32-10 counters and ascending-id iteration (see sbp_oracle.cpp).
+ */
+#ifndef SBP_ORACLE_H
+#define SBP_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct ora_graph ora_graph;
+typedef struct ora_bm ora_bm;
+
+/* Mirrors the hot-path subset of the reference's Args (include/args.hpp:61-212). */
+typedef struct ora_config {
+    int32_t algorithm;        /* 0 async_gibbs, 1 hybrid_mcmc, 2 metropolis_hastings */
+    int32_t batches;          /* --batches */
+    float   mh_percent;       /* --mh_percent (float, as in the reference) */
+    int32_t greedy;           /* --greedy switch (default true) */
+    int32_t ordered;          /* --ordered */
+    int32_t approximate;      /* --approximate */
+    int32_t asynciterations;  /* --asynciterations */
+    int32_t max_iterations;   /* MAX_NUM_ITERATIONS (finetune.hpp:34) = 100 */
+} ora_config;
+
+typedef struct ora_stats {
+    int64_t proposals;        /* vertex proposals evaluated (sweep) */
+    int64_t merge_proposals;  /* merge proposals evaluated */
+    int64_t moves;            /* vertex moves applied */
+    int64_t mcmc_iterations;
+    int64_t merges;           /* block merges applied */
+    int64_t edges_swept;      /* sum of vertex degrees over proposals */
+    int64_t outer_steps;
+} ora_stats;
+
+/* Philox4x32-10 (Salmon et al., SC'11).  ctr[4], key[2] -> out[4]. */
+void ora_philox(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
+
+ora_graph* ora_graph_create(int64_t num_vertices, int64_t num_edges,
+                            const int32_t* src, const int32_t* dst);
+void ora_graph_destroy(ora_graph* g);
+
+/* Blockmodel(num_blocks, graph, 0.5, assignment) (blockmodel.hpp:82-88). */
+ora_bm* ora_bm_create(const ora_graph* g, int64_t num_blocks, const int32_t* assignment);
+ora_bm* ora_bm_copy(const ora_bm* bm);
+void ora_bm_destroy(ora_bm* bm);
+int64_t ora_bm_num_blocks(const ora_bm* bm);
+int64_t ora_bm_nnz(const ora_bm* bm);
+/* assignment[N]; degrees/sizes[B]; cells (row, col, count) in row-major ascending order. */
+void ora_bm_read(const ora_bm* bm, int32_t* assignment, int64_t* d_out, int64_t* d_in,
+                 int64_t* d_tot, int64_t* sizes, int32_t* rows, int32_t* cols, int64_t* counts);
+int64_t ora_bm_get(const ora_bm* bm, int64_t row, int64_t col);
+
+/* entropy::mdl (entropy.cpp:597-604).  literal = reference arithmetic (glibc logf of the
+ * ratio, double sum in row-major order); canonical = exact fixed-point sum of the
+ * correctly-rounded float log, the value the device computes. */
+void ora_mdl(const ora_bm* bm, double* literal, double* canonical);
+
+/* entropy::delta_mdl(Blockmodel, Delta, proposal) (entropy.cpp:298-403) for moving
+ * `vertex` to `proposal`.  literal = reference double arithmetic in ascending order;
+ * fixed = the same sum in units of 2^-24 (exact). */
+void ora_delta_mdl(const ora_bm* bm, int64_t vertex, int64_t proposal,
+                   double* literal, int64_t* fixed);
+/* entropy::block_merge_delta_mdl (entropy.cpp:129-182) for merging block into proposal. */
+void ora_merge_delta_mdl(const ora_bm* bm, int64_t block, int64_t proposal,
+                         double* literal, int64_t* fixed);
+/* finetune::blockmodel_delta (finetune.cpp:201-235): writes up to cap entries. Returns count. */
+int64_t ora_vertex_delta(const ora_bm* bm, int64_t vertex, int64_t proposal,
+                         int32_t* rows, int32_t* cols, int64_t* vals, int64_t cap);
+/* block_merge::blockmodel_delta (block_merge.cpp:14-38). */
+int64_t ora_merge_delta(const ora_bm* bm, int64_t block, int64_t proposal,
+                        int32_t* rows, int32_t* cols, int64_t* vals, int64_t cap);
+
+/* Canonical proposals (common.cpp:138-198) under the seeded stream. */
+int64_t ora_propose_vertex(const ora_bm* bm, int64_t vertex, uint64_t seed,
+                           uint32_t c1, uint32_t c2, uint32_t c3);
+int64_t ora_propose_merge(const ora_bm* bm, int64_t block, uint64_t seed,
+                          uint32_t c2, int32_t proposal_index);
+
+/* One parallel-propose + serial-apply batch over vertices[0..n) (finetune.cpp:65-86):
+ * proposals against the same snapshot, applied in vertex-id order with the
+ * block-size-1 rejection of blockmodel.cpp:437-443. out_moves[i] = proposal or -1. */
+int64_t ora_gibbs_batch(ora_bm* bm, const int32_t* vertices, int64_t n, uint64_t seed,
+                        uint32_t iteration, uint32_t step, const ora_config* cfg,
+                        int32_t* out_moves, double* out_dS);
+/* Apply a precomputed move list (vertex-id order, size-1 rule). Returns moves applied. */
+int64_t ora_apply_moves(ora_bm* bm, const int32_t* moves_per_vertex);
+
+/* Sequential Metropolis-Hastings over order[0..n) (finetune::propose_move, finetune.cpp:842-869)
+ * with draws (vertex, iteration, step, DOM_MH).  Returns the number of applied moves. */
+int64_t ora_mh_chain(ora_bm* bm, const int32_t* order, int64_t n, uint64_t seed, uint32_t iteration,
+                     uint32_t step, const ora_config* cfg);
+
+/* finetune::mcmc dispatcher (finetune.cpp:754-771); mutates bm. */
+int ora_mcmc(ora_bm* bm, const ora_config* cfg, uint64_t seed, int32_t step,
+             int32_t golden_ratio_not_reached, ora_stats* stats);
+/* block_merge::merge_blocks (block_merge.cpp:178-228); mutates bm.  Merges
+ * `num_blocks_to_merge` blocks. */
+int ora_merge_blocks(ora_bm* bm, const ora_config* cfg, uint64_t seed, int32_t step,
+                     int64_t num_blocks_to_merge, ora_stats* stats);
+/* sbp::stochastic_block_partition (sbp.cpp:16-72). Writes the final assignment;
+ * returns the number of blocks (<0 on error). */
+int64_t ora_sbp(const ora_graph* g, const ora_config* cfg, uint64_t seed,
+                int32_t* out_assignment, double* out_mdl, ora_stats* stats);
+
+/* entropy::null_mdl_v1 (entropy.cpp:571-585) for a graph with `num_edges` edges. */
+double ora_null_mdl_v1(double num_edges);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

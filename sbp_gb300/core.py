@@ -1,0 +1,213 @@
+"""Host-side mirror of the reference's hot-path types: Args, Graph, Blockmodel.
+
+Names, argument meaning and error behaviour follow vtsynergy/SBP
+(include/args.hpp, include/graph.hpp, include/blockmodel/blockmodel.hpp); the state
+lives on the GPU behind the libsbpgpu C ABI.  Invalid arguments raise ValueError /
+IndexError like the reference's std::invalid_argument / IndexOutOfBoundsException.
+"""
+import ctypes
+import dataclasses
+
+import numpy as np
+
+from . import _lib
+from ._lib import Config, Stats, check, i32p, i64p, f64p
+
+ALGORITHMS = {"async_gibbs": 0, "hybrid_mcmc": 1, "metropolis_hastings": 2}
+
+
+@dataclasses.dataclass
+class Args:
+    """The hot-path subset of the reference's Args (include/args.hpp:61-212)."""
+    algorithm: str = "hybrid_mcmc"
+    batches: int = 1
+    mh_percent: float = 0.075
+    greedy: bool = True
+    ordered: bool = False
+    approximate: bool = False
+    asynciterations: int = 2**31 - 1
+    threads: int = 1               # accepted for compatibility; the device uses all SMs
+    nonparametric: bool = False
+    seed: int = 0                  # seeds the canonical proposal stream
+    max_iterations: int = 100      # MAX_NUM_ITERATIONS (include/finetune.hpp:34)
+
+    def config(self):
+        if self.algorithm not in ALGORITHMS:
+            raise ValueError("algorithm must be one of %s" % sorted(ALGORITHMS))
+        if self.nonparametric:
+            raise NotImplementedError("--nonparametric entropy is not implemented on the device")
+        if self.batches < 1:
+            raise ValueError("batches must be >= 1")
+        return Config(ALGORITHMS[self.algorithm], int(self.batches), float(self.mh_percent), int(bool(self.greedy)),
+                      int(bool(self.ordered)), int(bool(self.approximate)), int(self.asynciterations),
+                      int(self.max_iterations))
+
+
+class Context:
+    """One CUDA device + stream; not thread-safe."""
+
+    def __init__(self, device=0):
+        self.lib = _lib.load()
+        h = ctypes.c_void_p()
+        st = self.lib.sbpgpu_ctx_create(int(device), ctypes.byref(h))
+        if st != 0:
+            raise _lib.SbpGpuError(st, "cannot create a CUDA context on device %d" % device)
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.sbpgpu_ctx_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def check(self, status):
+        check(status, self.h)
+
+    def synchronize(self):
+        self.check(self.lib.sbpgpu_ctx_synchronize(self.h))
+
+    def set_timing(self, enabled):
+        self.lib.sbpgpu_set_timing(self.h, int(bool(enabled)))
+
+    def read_timing(self):
+        t = _lib.KernelTiming()
+        self.check(self.lib.sbpgpu_read_timing(self.h, ctypes.byref(t)))
+        return t.as_dict()
+
+
+_default_ctx = None
+
+
+def default_context():
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context(0)
+    return _default_ctx
+
+
+def _p(a, t):
+    return a.ctypes.data_as(t)
+
+
+class Graph:
+    """Directed multigraph in input edge order (Graph::add_edge, src/graph.cpp:10-18)."""
+
+    def __init__(self, num_vertices, src, dst, ctx=None):
+        self.ctx = ctx or default_context()
+        self.src = np.ascontiguousarray(src, dtype=np.int32)
+        self.dst = np.ascontiguousarray(dst, dtype=np.int32)
+        if self.src.shape != self.dst.shape or self.src.ndim != 1:
+            raise ValueError("src and dst must be 1-D arrays of equal length")
+        self._N = int(num_vertices)
+        if self.src.size and (min(self.src.min(), self.dst.min()) < 0 or
+                              max(self.src.max(), self.dst.max()) >= self._N):
+            raise IndexError("edge endpoint out of range")
+        h = ctypes.c_void_p()
+        self.ctx.check(self.ctx.lib.sbpgpu_graph_create(self.ctx.h, self._N, int(self.src.size),
+                                                        _p(self.src, i32p), _p(self.dst, i32p), ctypes.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.lib.sbpgpu_graph_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def num_vertices(self):
+        return self._N
+
+    def num_edges(self):
+        return int(self.src.size)
+
+    def out_neighbors(self, v):
+        return self.dst[self.src == v]
+
+    def in_neighbors(self, v):
+        return self.src[self.dst == v]
+
+
+class Blockmodel:
+    """Blockmodel(num_blocks, graph, block_reduction_rate, assignment) (blockmodel.hpp:82-88)."""
+
+    def __init__(self, num_blocks, graph, block_reduction_rate=0.5, assignment=None, _handle=None):
+        self.graph = graph
+        self.ctx = graph.ctx
+        self.block_reduction_rate = block_reduction_rate
+        self.num_blocks_to_merge = 0
+        if _handle is not None:
+            self.h = _handle
+            return
+        h = ctypes.c_void_p()
+        if assignment is None:
+            ptr = None
+            if num_blocks != graph.num_vertices():
+                raise ValueError("without an assignment num_blocks must equal the number of vertices")
+        else:
+            a = np.ascontiguousarray(assignment, dtype=np.int32)
+            if a.shape != (graph.num_vertices(),):
+                raise ValueError("assignment must hold one block per vertex")
+            if a.size and (a.min() < 0 or a.max() >= num_blocks):
+                raise IndexError("assignment value out of range")
+            ptr = _p(a, i32p)
+        self.ctx.check(self.ctx.lib.sbpgpu_bm_create(graph.h, int(num_blocks), ptr, ctypes.byref(h)))
+        self.h = h
+        self.num_blocks_to_merge = int(num_blocks * block_reduction_rate)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.lib.sbpgpu_bm_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def copy(self):
+        """Blockmodel::copy (blockmodel.cpp:139-153): device-to-device."""
+        h = ctypes.c_void_p()
+        self.ctx.check(self.ctx.lib.sbpgpu_bm_copy(self.h, ctypes.byref(h)))
+        return Blockmodel(0, self.graph, self.block_reduction_rate, _handle=h)
+
+    def num_blocks(self):
+        return int(self.ctx.lib.sbpgpu_bm_num_blocks(self.h))
+
+    def nnz(self):
+        return int(self.ctx.lib.sbpgpu_bm_nnz(self.h))
+
+    def getOverall_entropy(self):
+        return float(self.ctx.lib.sbpgpu_bm_entropy(self.h))
+
+    def read(self):
+        B, nnz, N = self.num_blocks(), self.nnz(), self.graph.num_vertices()
+        a = np.zeros(N, np.int32)
+        dout, din, dtot, sizes = (np.zeros(B, np.int64) for _ in range(4))
+        rows, cols = np.zeros(nnz, np.int32), np.zeros(nnz, np.int32)
+        cnt = np.zeros(nnz, np.int64)
+        self.ctx.check(self.ctx.lib.sbpgpu_bm_read(self.h, _p(a, i32p), _p(dout, i64p), _p(din, i64p),
+                                                   _p(dtot, i64p), _p(sizes, i64p), _p(rows, i32p), _p(cols, i32p),
+                                                   _p(cnt, i64p)))
+        return dict(assignment=a, d_out=dout, d_in=din, d_tot=dtot, sizes=sizes, rows=rows, cols=cols, counts=cnt)
+
+    # accessors named as in blockmodel.hpp
+    def block_assignment(self):
+        return self.read()["assignment"]
+
+    def degrees_out(self):
+        return self.read()["d_out"]
+
+    def degrees_in(self):
+        return self.read()["d_in"]
+
+    def degrees(self):
+        return self.read()["d_tot"]
+
+    def block_sizes(self):
+        return self.read()["sizes"]
+
+    def blockmatrix(self):
+        """Dense copy of the block-edge-count matrix (small B only)."""
+        d = self.read()
+        B = self.num_blocks()
+        M = np.zeros((B, B), np.int64)
+        M[d["rows"], d["cols"]] = d["counts"]
+        return M

@@ -1,0 +1,1099 @@
+// Host side of libsbpgpu: the C ABI (include/sbpgpu.h), device allocations and the
+// drivers that sequence the kernels like the reference's host loops:
+//   finetune::mcmc / asynchronous_gibbs / hybrid_mcmc / metropolis_hastings
+//     (reference src/finetune.cpp:34-107, 563-646, 754-820),
+//   block_merge::merge_blocks (src/block_merge.cpp:178-228),
+//   sbp::stochastic_block_partition + BlockmodelTriplet (src/sbp.cpp:16-86,
+//     src/blockmodel/blockmodel_triplet.cpp:4-105).
+// Every entry point catches exceptions and reports them as status codes.
+#include <algorithm>
+#include <cfloat>
+#include <climits>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/sbpgpu.h"
+#include "kernels.cuh"
+#include "prims.cuh"
+
+using namespace sbp;
+
+namespace {
+
+struct CudaError : std::runtime_error {
+    cudaError_t code;
+    CudaError(cudaError_t c, const char* what) : std::runtime_error(what), code(c) {}
+};
+struct ApiError : std::runtime_error {
+    sbpgpu_status code;
+    ApiError(sbpgpu_status c, const std::string& what) : std::runtime_error(what), code(c) {}
+};
+
+#define CK(call)                                                                          \
+    do {                                                                                  \
+        cudaError_t e_ = (call);                                                          \
+        if (e_ != cudaSuccess) {                                                          \
+            std::string m_ = std::string(#call) + ": " + cudaGetErrorString(e_);         \
+            throw CudaError(e_, m_.c_str());                                              \
+        }                                                                                 \
+    } while (0)
+
+template <typename T>
+T* dalloc(std::vector<void*>& owned, size_t n) {
+    void* p = nullptr;
+    const size_t bytes = (n ? n : 1) * sizeof(T);
+    const cudaError_t e = cudaMalloc(&p, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        throw ApiError(SBPGPU_ENOMEM, "cudaMalloc of " + std::to_string(bytes) + " bytes failed");
+    }
+    owned.push_back(p);
+    return static_cast<T*>(p);
+}
+
+double early_threshold(bool golden, double initial) { return golden ? 5e-4 * initial : 1e-4 * initial; }
+
+/* finetune::early_stop (reference src/finetune.cpp:265-283). */
+bool early_stop(int64_t iteration, bool golden, double initial, const std::vector<double>& d) {
+    const size_t last = d.size() - 1;
+    if (d[last] == 0.0) return true;
+    if (iteration < 3) return false;
+    double average = d[last] + d[last - 1] + d[last - 2];
+    average /= -3.0;
+    return average < early_threshold(golden, initial);
+}
+
+}  // namespace
+
+struct TimedSpan {
+    cudaEvent_t a, b;
+    int kind;
+};
+
+struct sbpgpu_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    bool timing = false;
+    std::vector<TimedSpan> pending;
+    std::vector<cudaEvent_t> free_events;
+    sbpgpu_kernel_timing tm{};
+
+    cudaEvent_t ev() {
+        if (!free_events.empty()) {
+            cudaEvent_t e = free_events.back();
+            free_events.pop_back();
+            return e;
+        }
+        cudaEvent_t e;
+        CK(cudaEventCreate(&e));
+        return e;
+    }
+    void collect() {
+        for (auto& s : pending) {
+            float ms = 0.f;
+            CK(cudaEventSynchronize(s.b));
+            CK(cudaEventElapsedTime(&ms, s.a, s.b));
+            switch (s.kind) {
+                case 0: tm.gibbs_propose_ms += ms; tm.gibbs_propose_launches++; break;
+                case 1: tm.mh_chain_ms += ms; tm.mh_chain_launches++; break;
+                case 2: tm.merge_propose_ms += ms; tm.merge_propose_launches++; break;
+                case 3: tm.carry_out_ms += ms; tm.carry_out_launches++; break;
+                case 4: tm.rebuild_ms += ms; tm.rebuild_launches++; break;
+                default: break;
+            }
+            free_events.push_back(s.a);
+            free_events.push_back(s.b);
+        }
+        pending.clear();
+    }
+};
+
+// RAII span recorded only when timing is enabled.
+struct Span {
+    sbpgpu_ctx* c;
+    int kind;
+    cudaEvent_t a = nullptr;
+    Span(sbpgpu_ctx* ctx, int k) : c(ctx), kind(k) {
+        if (c->timing) {
+            a = c->ev();
+            CK(cudaEventRecord(a, c->stream));
+        }
+    }
+    ~Span() {
+        if (c->timing && a) {
+            cudaEvent_t b = c->ev();
+            cudaEventRecord(b, c->stream);
+            c->pending.push_back({a, b, kind});
+        }
+    }
+};
+
+struct sbpgpu_graph {
+    sbpgpu_ctx* ctx = nullptr;
+    int64_t N = 0, E = 0;
+    DevGraph dg{};
+    std::vector<void*> owned;
+    std::vector<int32_t> deg;   // Graph::degrees (graph.cpp:24-31): out + in - self
+    std::vector<int32_t> kdeg;  // out + in without self (proposal neighbour count)
+    int32_t max_k = 0;
+    Work w;
+    DevFlags* flags_host = nullptr;  // pinned
+    int32_t* d_all = nullptr;        // identity vertex list
+    int32_t* d_order = nullptr;      // scratch order [N]
+    int32_t* d_order2 = nullptr;     // scratch order [N]
+    // hdv / ldv split for one mh_percent (Graph::sort_vertices, graph.cpp:235-268)
+    float split_mh = -1.f;
+    int32_t* d_hdv = nullptr;
+    int32_t* d_ldv = nullptr;
+    int32_t n_hdv = 0, n_ldv = 0, max_k_hdv = 0;
+    int64_t hdv_k_sum = 0;
+    sbpgpu_stats st{};
+};
+
+struct sbpgpu_bm {
+    sbpgpu_graph* g = nullptr;
+    DevBM d{};
+    std::vector<void*> owned;
+    double entropy = DBL_MAX;
+    int64_t num_blocks_to_merge = 0;
+};
+
+namespace {
+
+sbpgpu_status fail(sbpgpu_ctx* ctx, sbpgpu_status code, const std::string& msg) {
+    if (ctx) ctx->err = msg;
+    return code;
+}
+
+template <typename F>
+sbpgpu_status guarded(sbpgpu_ctx* ctx, F f) {
+    try {
+        return f();
+    } catch (const ApiError& e) {
+        return fail(ctx, e.code, e.what());
+    } catch (const CudaError& e) {
+        return fail(ctx, SBPGPU_EDEVICE, e.what());
+    } catch (const std::bad_alloc&) {
+        return fail(ctx, SBPGPU_ENOMEM, "host allocation failed");
+    } catch (const std::exception& e) {
+        return fail(ctx, SBPGPU_EDEVICE, e.what());
+    }
+}
+
+void check_flags(sbpgpu_graph* g) {
+    CK(cudaMemcpyAsync(g->flags_host, g->w.flags_dev, sizeof(DevFlags), cudaMemcpyDeviceToHost, g->ctx->stream));
+    CK(cudaStreamSynchronize(g->ctx->stream));
+    CK(cudaGetLastError());
+    const int32_t err = g->flags_host->err;
+    if (err) {
+        g->flags_host->err = 0;
+        CK(cudaMemsetAsync(g->w.flags_dev, 0, sizeof(DevFlags), g->ctx->stream));
+        CK(cudaStreamSynchronize(g->ctx->stream));
+        std::string m = "device check failed (flags 0x" + std::to_string(err) + "):";
+        if (err & ERR_DEGREE) m += " a vertex or block row exceeds the supported neighbour count;";
+        if (err & ERR_HASH_FULL) m += " chain cell store full;";
+        if (err & ERR_POOL_FULL) m += " chain list pool full;";
+        if (err & ERR_STATE) m += " blockmodel consistency check failed;";
+        if (err & ERR_SELECT) m += " cumulative search out of range;";
+        throw ApiError(SBPGPU_EDEVICE, m);
+    }
+}
+
+void alloc_work(sbpgpu_graph* g) {
+    Work& w = g->w;
+    auto& o = g->owned;
+    const int64_t N = g->N, E = g->E;
+    const int64_t KE = std::max<int64_t>(E, 2 * N + 16);
+    w.keys = dalloc<uint64_t>(o, KE);
+    w.keys_alt = dalloc<uint64_t>(o, KE);
+    w.vals = dalloc<int32_t>(o, KE);
+    w.vals_alt = dalloc<int32_t>(o, KE);
+    w.flags = dalloc<int32_t>(o, KE);
+    w.temp_bytes = std::max(radix_temp_bytes(KE), scan_temp_bytes(KE)) + 4096;
+    w.temp = dalloc<char>(o, w.temp_bytes);
+    w.d_scalar = dalloc<int32_t>(o, 16);
+    w.d_acc = dalloc<unsigned long long>(o, 4);
+    w.moves = dalloc<int32_t>(o, N);
+    w.m_out = dalloc<int32_t>(o, N);
+    w.last = dalloc<int32_t>(o, N);
+    w.acc = dalloc<int32_t>(o, N);
+    w.dep = dalloc<int32_t>(o, 2 * N + 16);
+    w.list_small = dalloc<int32_t>(o, 2 * N + 16);
+    w.list_big = dalloc<int32_t>(o, 2 * N + 16);
+    w.list_tmp = dalloc<int32_t>(o, N);
+    // chain cell store: capacity for every cell plus the new cells of one phase.
+    w.chain_cap = 1ull << ceil_log2((uint64_t)(8 * (uint64_t)E + 4096));
+    w.chain_keys = dalloc<unsigned long long>(o, w.chain_cap);
+    w.chain_vals = dalloc<int32_t>(o, w.chain_cap);
+    w.pool_cap = (int32_t)std::min<int64_t>(2 * N + (8 * E) / kChunkItems + 1024, INT32_MAX / 32);
+    w.pool = dalloc<int32_t>(o, (size_t)w.pool_cap * 32);
+    w.row_head = dalloc<int32_t>(o, N);
+    w.col_head = dalloc<int32_t>(o, N);
+    w.best = dalloc<int32_t>(o, N);
+    w.best_dS = dalloc<double>(o, N);
+    w.heap_dS = dalloc<double>(o, N);
+    w.heap_blk = dalloc<int32_t>(o, N);
+    w.parent = dalloc<int32_t>(o, N);
+    w.root = dalloc<int32_t>(o, N);
+    w.used = dalloc<int32_t>(o, N);
+    w.flags_dev = dalloc<DevFlags>(o, 1);
+}
+
+void ensure_split(sbpgpu_graph* g, float mh_percent) {
+    if (g->split_mh == mh_percent) return;
+    std::vector<int32_t> idx(g->N);
+    for (int64_t v = 0; v < g->N; ++v) idx[v] = (int32_t)v;
+    std::stable_sort(idx.begin(), idx.end(), [&](int32_t a, int32_t b) { return g->deg[a] > g->deg[b]; });
+    const float limit = mh_percent * (float)g->N;  // float arithmetic as in graph.cpp:252
+    std::vector<int32_t> hdv, ldv;
+    for (int64_t i = 0; i < g->N; ++i) ((float)i < limit ? hdv : ldv).push_back(idx[i]);
+    if (!g->d_hdv) {
+        g->d_hdv = dalloc<int32_t>(g->owned, g->N);
+        g->d_ldv = dalloc<int32_t>(g->owned, g->N);
+    }
+    g->n_hdv = (int32_t)hdv.size();
+    g->n_ldv = (int32_t)ldv.size();
+    g->max_k_hdv = 0;
+    g->hdv_k_sum = 0;
+    for (int32_t v : hdv) {
+        g->max_k_hdv = std::max(g->max_k_hdv, g->kdeg[v]);
+        g->hdv_k_sum += g->kdeg[v];
+    }
+    if (!hdv.empty())
+        CK(cudaMemcpyAsync(g->d_hdv, hdv.data(), hdv.size() * 4, cudaMemcpyHostToDevice, g->ctx->stream));
+    if (!ldv.empty())
+        CK(cudaMemcpyAsync(g->d_ldv, ldv.data(), ldv.size() * 4, cudaMemcpyHostToDevice, g->ctx->stream));
+    CK(cudaStreamSynchronize(g->ctx->stream));
+    g->split_mh = mh_percent;
+}
+
+void do_rebuild(sbpgpu_bm* bm) {
+    sbpgpu_graph* g = bm->g;
+    Span sp(g->ctx, 4);
+    rebuild(g->dg, bm->d, g->w, g->ctx->stream);
+}
+
+double do_mdl(sbpgpu_bm* bm) {
+    sbpgpu_graph* g = bm->g;
+    launch_mdl(g->dg, bm->d, g->w, g->ctx->stream);
+    unsigned long long acc = 0;
+    CK(cudaMemcpyAsync(&acc, g->w.d_acc, sizeof(acc), cudaMemcpyDeviceToHost, g->ctx->stream));
+    check_flags(g);
+    g->ctx->collect();
+    const long long lpq = (long long)acc;
+    const double E = (double)g->E;
+    const double B = (double)bm->d.B;
+    const double x = pow(B, 2) / E;
+    const double h = ((1 + x) * log(1 + x)) - (x * log(x));
+    return (E * h) + ((double)g->N * log(B)) - (double)lpq * (1.0 / 16777216.0);
+}
+
+void reset_counters(sbpgpu_graph* g) {
+    CK(cudaMemsetAsync(g->w.flags_dev, 0, sizeof(DevFlags), g->ctx->stream));
+}
+
+// Reads the device counters into the graph's running statistics.
+void harvest_counters(sbpgpu_graph* g) {
+    CK(cudaMemcpyAsync(g->flags_host, g->w.flags_dev, sizeof(DevFlags), cudaMemcpyDeviceToHost, g->ctx->stream));
+    check_flags(g);
+    const DevFlags& f = *g->flags_host;
+    g->st.moves += (int64_t)f.counters[2] + (int64_t)f.counters[5];
+    g->st.edges_swept += (int64_t)f.counters[3];
+    g->st.merge_proposals += (int64_t)f.counters[6];
+    reset_counters(g);
+}
+
+void gibbs_batch_dev(sbpgpu_bm* bm, const int32_t* list, int32_t n, uint64_t seed, uint32_t it, uint32_t step,
+                     int greedy) {
+    sbpgpu_graph* g = bm->g;
+    {
+        Span sp(g->ctx, 0);
+        gibbs_propose(g->dg, bm->d, list, n, g->max_k, seed, it, step, greedy, g->w, g->ctx->stream);
+    }
+    gibbs_apply(bm->d, list, n, g->w, g->ctx->stream);
+    g->st.proposals += n;
+    do_rebuild(bm);
+}
+
+void chain_run(sbpgpu_bm* bm, const int32_t* order, int32_t n, int32_t max_k, int64_t k_sum, uint64_t seed,
+               uint32_t it, uint32_t step, int greedy) {
+    sbpgpu_graph* g = bm->g;
+    if (max_k * 2 > (1 << 13)) throw ApiError(SBPGPU_EUNSUPPORTED, "sequential MH supports vertices with k <= 4096");
+    chain_init(bm->d, g->w, (uint64_t)(2 * k_sum + 4 * (int64_t)n), g->ctx->stream);
+    {
+        Span sp(g->ctx, 1);
+        mh_chain(g->dg, bm->d, order, n, max_k, seed, it, step, greedy, g->w, g->ctx->stream);
+    }
+    g->st.proposals += n;
+    do_rebuild(bm);
+}
+
+void require_greedy(const sbpgpu_config& cfg) {
+    if (!cfg.greedy)
+        throw ApiError(SBPGPU_EUNSUPPORTED, "non-greedy acceptance (--greedy switch set) is not implemented on the device");
+}
+
+void async_gibbs(sbpgpu_bm* bm, const sbpgpu_config& cfg, uint64_t seed, int32_t step, bool golden) {
+    sbpgpu_graph* g = bm->g;
+    if (bm->d.B == 1) return;
+    require_greedy(cfg);
+    std::vector<double> deltas;
+    const double initial = do_mdl(bm);
+    bm->entropy = initial;
+    double last = initial;
+    const int64_t N = g->N;
+    const int64_t batch_size = (int64_t)ceil((double)N / (double)cfg.batches);
+    for (int it = 0; it < cfg.max_iterations; ++it) {
+        const int32_t* list = g->d_all;
+        if (!cfg.ordered && cfg.batches > 1) {
+            shuffle(g->d_all, (int32_t)N, seed, (uint32_t)it, (uint32_t)step, DOM_SHUFFLE_ALL, g->d_order, g->w,
+                    g->ctx->stream);
+            list = g->d_order;
+        }
+        for (int64_t b = 0; batch_size > 0 && b < N / batch_size; ++b) {
+            const int64_t s0 = b * batch_size, s1 = std::min(N, (b + 1) * batch_size);
+            gibbs_batch_dev(bm, list + s0, (int32_t)(s1 - s0), seed, (uint32_t)it, (uint32_t)step, cfg.greedy);
+        }
+        const double e = do_mdl(bm);
+        harvest_counters(g);
+        deltas.push_back(e - last);
+        last = e;
+        g->st.mcmc_iterations++;
+        if (early_stop(it, golden, initial, deltas)) break;
+    }
+    bm->entropy = last;
+}
+
+void hybrid_mcmc(sbpgpu_bm* bm, const sbpgpu_config& cfg, uint64_t seed, int32_t step, bool golden) {
+    sbpgpu_graph* g = bm->g;
+    if (bm->d.B == 1) return;
+    require_greedy(cfg);
+    ensure_split(g, cfg.mh_percent);
+    std::vector<double> deltas;
+    const double initial = do_mdl(bm);
+    bm->entropy = initial;
+    double last = initial;
+    const int64_t nlow = g->n_ldv;
+    const int64_t batch_size = (int64_t)ceil((double)nlow / (double)cfg.batches);
+    for (int it = 0; it < cfg.max_iterations; ++it) {
+        if (g->n_hdv > 0) {
+            const int32_t* order = g->d_hdv;
+            if (!cfg.ordered) {
+                shuffle(g->d_hdv, g->n_hdv, seed, (uint32_t)it, (uint32_t)step, DOM_SHUFFLE_HDV, g->d_order, g->w,
+                        g->ctx->stream);
+                order = g->d_order;
+            }
+            chain_run(bm, order, g->n_hdv, g->max_k_hdv, g->hdv_k_sum, seed, (uint32_t)it, (uint32_t)step, cfg.greedy);
+        }
+        const int32_t* list = g->d_ldv;
+        if (!cfg.ordered && cfg.batches > 1) {
+            shuffle(g->d_ldv, (int32_t)nlow, seed, (uint32_t)it, (uint32_t)step, DOM_SHUFFLE_ALL, g->d_order2, g->w,
+                    g->ctx->stream);
+            list = g->d_order2;
+        }
+        for (int64_t b = 0; batch_size > 0 && b < nlow / batch_size; ++b) {
+            const int64_t s0 = b * batch_size, s1 = std::min(nlow, (b + 1) * batch_size);
+            gibbs_batch_dev(bm, list + s0, (int32_t)(s1 - s0), seed, (uint32_t)it, (uint32_t)step, cfg.greedy);
+        }
+        const double e = do_mdl(bm);
+        harvest_counters(g);
+        deltas.push_back(e - last);
+        last = e;
+        g->st.mcmc_iterations++;
+        if (early_stop(it, golden, initial, deltas)) break;
+    }
+    bm->entropy = last;
+}
+
+void metropolis_hastings(sbpgpu_bm* bm, const sbpgpu_config& cfg, uint64_t seed, int32_t step, bool golden) {
+    sbpgpu_graph* g = bm->g;
+    if (bm->d.B == 1) return;
+    require_greedy(cfg);
+    std::vector<double> deltas;
+    bm->entropy = do_mdl(bm);
+    int64_t ksum = 0;
+    for (int64_t v = 0; v < g->N; ++v) ksum += g->kdeg[v];
+    for (int it = 0; it < cfg.max_iterations; ++it) {
+        const int32_t* order = g->d_all;
+        if (!cfg.ordered) {
+            shuffle(g->d_all, (int32_t)g->N, seed, (uint32_t)it, (uint32_t)step, DOM_SHUFFLE_ALL, g->d_order, g->w,
+                    g->ctx->stream);
+            order = g->d_order;
+        }
+        chain_run(bm, order, (int32_t)g->N, g->max_k, ksum, seed, (uint32_t)it, (uint32_t)step, cfg.greedy);
+        CK(cudaMemcpyAsync(g->flags_host, g->w.flags_dev, sizeof(DevFlags), cudaMemcpyDeviceToHost, g->ctx->stream));
+        check_flags(g);
+        const double dsum = (double)(long long)g->flags_host->counters[7] * (1.0 / 16777216.0);
+        harvest_counters(g);
+        deltas.push_back(dsum);
+        g->st.mcmc_iterations++;
+        if (early_stop(it, golden, bm->entropy, deltas)) break;
+    }
+    bm->entropy = do_mdl(bm);
+}
+
+void mcmc_impl(sbpgpu_bm* bm, const sbpgpu_config& cfg, uint64_t seed, int32_t step, bool golden) {
+    if (cfg.algorithm == 0 && step < cfg.asynciterations) async_gibbs(bm, cfg, seed, step, golden);
+    else if (cfg.algorithm == 1) hybrid_mcmc(bm, cfg, seed, step, golden);
+    else metropolis_hastings(bm, cfg, seed, step, golden);
+}
+
+void merge_impl(sbpgpu_bm* bm, const sbpgpu_config& cfg, uint64_t seed, int32_t step, int64_t num_to_merge) {
+    sbpgpu_graph* g = bm->g;
+    if (num_to_merge <= 0) return;  // nothing is merged; the rebuild would reproduce the same state
+    const int32_t B = bm->d.B;
+    if (num_to_merge >= B) throw ApiError(SBPGPU_EINVAL, "num_blocks_to_merge must be < num_blocks");
+    {
+        Span sp(g->ctx, 2);
+        merge_propose(g->dg, bm->d, seed, (uint32_t)step, g->w, g->ctx->stream);
+    }
+    {
+        Span sp(g->ctx, 3);
+        carry_out(g->dg, bm->d, num_to_merge, cfg.approximate, g->w, g->ctx->stream);
+    }
+    int32_t sc[3] = {0, 0, 0};
+    CK(cudaMemcpyAsync(sc, g->w.d_scalar, sizeof(sc), cudaMemcpyDeviceToHost, g->ctx->stream));
+    harvest_counters(g);
+    if (sc[1] != num_to_merge || sc[2] != B - num_to_merge)
+        throw ApiError(SBPGPU_EDEVICE, "merge pass carried out " + std::to_string(sc[1]) + " of " +
+                                           std::to_string(num_to_merge) + " merges (" + std::to_string(sc[2]) +
+                                           " blocks left)");
+    g->st.merges += sc[1];
+    bm->d.B = sc[2];
+    do_rebuild(bm);
+}
+
+void upload_graph(sbpgpu_graph* g, const int32_t* src, const int32_t* dst) {
+    const int64_t N = g->N, E = g->E;
+    std::vector<int32_t> out_off(N + 1, 0), inns_off(N + 1, 0), selfcnt(N, 0), indeg(N, 0);
+    for (int64_t e = 0; e < E; ++e) {
+        const int32_t u = src[e], v = dst[e];
+        if (u < 0 || u >= N || v < 0 || v >= N) throw ApiError(SBPGPU_EINVAL, "edge endpoint out of range");
+        out_off[u + 1]++;
+        indeg[v]++;
+        if (u == v) selfcnt[u]++;
+        else inns_off[v + 1]++;
+    }
+    for (int64_t v = 0; v < N; ++v) {
+        out_off[v + 1] += out_off[v];
+        inns_off[v + 1] += inns_off[v];
+    }
+    std::vector<int32_t> out_nbr(E), esrc(E), inns_nbr(inns_off[N]);
+    std::vector<int32_t> po(out_off.begin(), out_off.end() - 1), pi(inns_off.begin(), inns_off.end() - 1);
+    for (int64_t e = 0; e < E; ++e) {  // stable: neighbour lists keep input order (graph.cpp:10-18)
+        const int32_t u = src[e], v = dst[e];
+        esrc[po[u]] = u;
+        out_nbr[po[u]++] = v;
+        if (u != v) inns_nbr[pi[v]++] = u;
+    }
+    g->deg.resize(N);
+    g->kdeg.resize(N);
+    g->max_k = 0;
+    for (int64_t v = 0; v < N; ++v) {
+        const int32_t outd = out_off[v + 1] - out_off[v];
+        g->deg[v] = outd + indeg[v] - (selfcnt[v] > 0 ? 1 : 0);
+        g->kdeg[v] = outd + (inns_off[v + 1] - inns_off[v]);
+        g->max_k = std::max(g->max_k, g->kdeg[v]);
+    }
+    // fastlog table (fastlog.hpp:21-30): logf((float)x) is a multiple of 2^-24 for x >= 1.
+    std::vector<int32_t> Lq(E + 2);
+    Lq[0] = 0;
+    for (int64_t x = 1; x < E + 2; ++x) Lq[x] = (int32_t)((double)logf((float)x) * 16777216.0);
+    cudaStream_t st = g->ctx->stream;
+    auto& o = g->owned;
+    int32_t* d_out_off = dalloc<int32_t>(o, N + 1);
+    int32_t* d_out_nbr = dalloc<int32_t>(o, E);
+    int32_t* d_inns_off = dalloc<int32_t>(o, N + 1);
+    int32_t* d_inns_nbr = dalloc<int32_t>(o, inns_nbr.size());
+    int32_t* d_self = dalloc<int32_t>(o, N);
+    int32_t* d_esrc = dalloc<int32_t>(o, E);
+    int32_t* d_Lq = dalloc<int32_t>(o, E + 2);
+    CK(cudaMemcpyAsync(d_out_off, out_off.data(), (N + 1) * 4, cudaMemcpyHostToDevice, st));
+    if (E) CK(cudaMemcpyAsync(d_out_nbr, out_nbr.data(), E * 4, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(d_inns_off, inns_off.data(), (N + 1) * 4, cudaMemcpyHostToDevice, st));
+    if (!inns_nbr.empty())
+        CK(cudaMemcpyAsync(d_inns_nbr, inns_nbr.data(), inns_nbr.size() * 4, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(d_self, selfcnt.data(), N * 4, cudaMemcpyHostToDevice, st));
+    if (E) CK(cudaMemcpyAsync(d_esrc, esrc.data(), E * 4, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(d_Lq, Lq.data(), (E + 2) * 4, cudaMemcpyHostToDevice, st));
+    g->dg = DevGraph{(int32_t)N, (int32_t)E, d_out_off, d_out_nbr, d_inns_off, d_inns_nbr, d_self, d_esrc, d_Lq};
+    alloc_work(g);
+    std::vector<int32_t> iota(N);
+    for (int64_t v = 0; v < N; ++v) iota[v] = (int32_t)v;
+    g->d_all = dalloc<int32_t>(o, N);
+    g->d_order = dalloc<int32_t>(o, N);
+    g->d_order2 = dalloc<int32_t>(o, N);
+    CK(cudaMemcpyAsync(g->d_all, iota.data(), N * 4, cudaMemcpyHostToDevice, st));
+    CK(cudaMallocHost(&g->flags_host, sizeof(DevFlags)));
+    memset(g->flags_host, 0, sizeof(DevFlags));
+    reset_counters(g);
+    CK(cudaStreamSynchronize(st));
+}
+
+sbpgpu_bm* new_bm(sbpgpu_graph* g, int64_t B) {
+    auto* bm = new sbpgpu_bm();
+    bm->g = g;
+    const int64_t N = g->N, E = g->E;
+    auto& o = bm->owned;
+    DevBM& d = bm->d;
+    d.B = (int32_t)B;
+    d.asg = dalloc<int32_t>(o, N);
+    d.d_out = dalloc<int32_t>(o, N);
+    d.d_in = dalloc<int32_t>(o, N);
+    d.d_tot = dalloc<int32_t>(o, N);
+    d.sizes = dalloc<int32_t>(o, N);
+    d.diag = dalloc<int32_t>(o, N);
+    d.row_off = dalloc<int32_t>(o, N + 1);
+    d.col_off = dalloc<int32_t>(o, N + 1);
+    d.row_col = dalloc<int32_t>(o, E);
+    d.row_cnt = dalloc<int32_t>(o, E);
+    d.row_cum = dalloc<int32_t>(o, E);
+    d.row_of = dalloc<int32_t>(o, E);
+    d.col_row = dalloc<int32_t>(o, E);
+    d.col_cnt = dalloc<int32_t>(o, E);
+    d.col_cum = dalloc<int32_t>(o, E);
+    return bm;
+}
+
+void free_all(std::vector<void*>& owned) {
+    for (void* p : owned) cudaFree(p);
+    owned.clear();
+}
+
+}  // namespace
+
+// ====================================================================== C ABI
+extern "C" {
+
+void sbpgpu_default_config(sbpgpu_config* cfg) {
+    cfg->algorithm = 1;
+    cfg->batches = 1;
+    cfg->mh_percent = 0.075f;
+    cfg->greedy = 1;
+    cfg->ordered = 0;
+    cfg->approximate = 0;
+    cfg->asynciterations = INT32_MAX;
+    cfg->max_iterations = 100;
+}
+
+sbpgpu_status sbpgpu_ctx_create(int32_t device, sbpgpu_ctx** out) {
+    if (!out) return SBPGPU_EINVAL;
+    *out = nullptr;
+    auto* ctx = new sbpgpu_ctx();
+    ctx->device = device;
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete ctx;
+        cudaGetLastError();
+        return SBPGPU_EDEVICE;
+    }
+    *out = ctx;
+    return SBPGPU_OK;
+}
+
+void sbpgpu_ctx_destroy(sbpgpu_ctx* ctx) {
+    if (!ctx) return;
+    cudaStreamSynchronize(ctx->stream);
+    for (auto& s : ctx->pending) {
+        cudaEventDestroy(s.a);
+        cudaEventDestroy(s.b);
+    }
+    for (auto e : ctx->free_events) cudaEventDestroy(e);
+    cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+const char* sbpgpu_last_error(const sbpgpu_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+sbpgpu_status sbpgpu_ctx_synchronize(sbpgpu_ctx* ctx) {
+    return guarded(ctx, [&] {
+        CK(cudaStreamSynchronize(ctx->stream));
+        return SBPGPU_OK;
+    });
+}
+
+void* sbpgpu_ctx_stream(sbpgpu_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+sbpgpu_status sbpgpu_graph_create(sbpgpu_ctx* ctx, int64_t N, int64_t E, const int32_t* src, const int32_t* dst,
+                                  sbpgpu_graph** out) {
+    if (!ctx || !out) return SBPGPU_EINVAL;
+    *out = nullptr;
+    if (N <= 0 || E < 0 || E >= (int64_t)INT32_MAX - 2 || N >= INT32_MAX / 2 || (E > 0 && (!src || !dst)))
+        return fail(ctx, SBPGPU_EINVAL, "graph needs 0 < N < 2^30, 0 <= E < 2^31 - 2 and edge arrays");
+    auto* g = new sbpgpu_graph();
+    g->ctx = ctx;
+    g->N = N;
+    g->E = E;
+    const sbpgpu_status rc = guarded(ctx, [&] {
+        CK(cudaSetDevice(ctx->device));
+        upload_graph(g, src, dst);
+        return SBPGPU_OK;
+    });
+    if (rc != SBPGPU_OK) {
+        free_all(g->owned);
+        if (g->flags_host) cudaFreeHost(g->flags_host);
+        delete g;
+        return rc;
+    }
+    *out = g;
+    return SBPGPU_OK;
+}
+
+sbpgpu_status sbpgpu_graph_create_device(sbpgpu_ctx* ctx, int64_t N, int64_t E, const int32_t* d_src,
+                                         const int32_t* d_dst, sbpgpu_graph** out) {
+    if (!ctx || !out) return SBPGPU_EINVAL;
+    std::vector<int32_t> src(E), dst(E);
+    const sbpgpu_status rc = guarded(ctx, [&] {
+        if (E) {
+            CK(cudaMemcpy(src.data(), d_src, E * 4, cudaMemcpyDeviceToHost));
+            CK(cudaMemcpy(dst.data(), d_dst, E * 4, cudaMemcpyDeviceToHost));
+        }
+        return SBPGPU_OK;
+    });
+    if (rc != SBPGPU_OK) return rc;
+    return sbpgpu_graph_create(ctx, N, E, src.data(), dst.data(), out);
+}
+
+void sbpgpu_graph_destroy(sbpgpu_graph* g) {
+    if (!g) return;
+    cudaStreamSynchronize(g->ctx->stream);
+    free_all(g->owned);
+    if (g->flags_host) cudaFreeHost(g->flags_host);
+    delete g;
+}
+
+int64_t sbpgpu_graph_num_vertices(const sbpgpu_graph* g) { return g ? g->N : 0; }
+int64_t sbpgpu_graph_num_edges(const sbpgpu_graph* g) { return g ? g->E : 0; }
+
+sbpgpu_status sbpgpu_bm_create(sbpgpu_graph* g, int64_t B, const int32_t* assignment, sbpgpu_bm** out) {
+    if (!g || !out) return SBPGPU_EINVAL;
+    *out = nullptr;
+    sbpgpu_ctx* ctx = g->ctx;
+    if (B <= 0 || B > g->N) return fail(ctx, SBPGPU_EINVAL, "num_blocks must be in [1, N]");
+    if (assignment)
+        for (int64_t v = 0; v < g->N; ++v)
+            if (assignment[v] < 0 || assignment[v] >= B)
+                return fail(ctx, SBPGPU_EINVAL, "assignment value out of range");
+    sbpgpu_bm* bm = nullptr;
+    const sbpgpu_status rc = guarded(ctx, [&] {
+        bm = new_bm(g, B);
+        if (assignment) {
+            CK(cudaMemcpyAsync(bm->d.asg, assignment, g->N * 4, cudaMemcpyHostToDevice, ctx->stream));
+        } else {
+            CK(cudaMemcpyAsync(bm->d.asg, g->d_all, g->N * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+        }
+        bm->num_blocks_to_merge = (int64_t)((double)B * 0.5);
+        do_rebuild(bm);
+        check_flags(g);
+        return SBPGPU_OK;
+    });
+    if (rc != SBPGPU_OK) {
+        if (bm) {
+            free_all(bm->owned);
+            delete bm;
+        }
+        return rc;
+    }
+    *out = bm;
+    return SBPGPU_OK;
+}
+
+sbpgpu_status sbpgpu_bm_copy(const sbpgpu_bm* src, sbpgpu_bm** out) {
+    if (!src || !out) return SBPGPU_EINVAL;
+    sbpgpu_graph* g = src->g;
+    sbpgpu_bm* bm = nullptr;
+    const sbpgpu_status rc = guarded(g->ctx, [&] {
+        bm = new_bm(g, src->d.B);
+        cudaStream_t st = g->ctx->stream;
+        const int64_t N = g->N;
+        const int64_t nnz = src->d.nnz;
+        const DevBM& a = src->d;
+        DevBM& b = bm->d;
+        CK(cudaMemcpyAsync(b.asg, a.asg, N * 4, cudaMemcpyDeviceToDevice, st));
+        for (auto pr : {std::make_pair(b.d_out, a.d_out), std::make_pair(b.d_in, a.d_in),
+                        std::make_pair(b.d_tot, a.d_tot), std::make_pair(b.sizes, a.sizes),
+                        std::make_pair(b.diag, a.diag)})
+            CK(cudaMemcpyAsync(pr.first, pr.second, a.B * 4, cudaMemcpyDeviceToDevice, st));
+        CK(cudaMemcpyAsync(b.row_off, a.row_off, (a.B + 1) * 4, cudaMemcpyDeviceToDevice, st));
+        CK(cudaMemcpyAsync(b.col_off, a.col_off, (a.B + 1) * 4, cudaMemcpyDeviceToDevice, st));
+        if (nnz)
+            for (auto pr : {std::make_pair(b.row_col, a.row_col), std::make_pair(b.row_cnt, a.row_cnt),
+                            std::make_pair(b.row_cum, a.row_cum), std::make_pair(b.row_of, a.row_of),
+                            std::make_pair(b.col_row, a.col_row), std::make_pair(b.col_cnt, a.col_cnt),
+                            std::make_pair(b.col_cum, a.col_cum)})
+                CK(cudaMemcpyAsync(pr.first, pr.second, nnz * 4, cudaMemcpyDeviceToDevice, st));
+        b.nnz = a.nnz;
+        bm->entropy = src->entropy;
+        bm->num_blocks_to_merge = 0;  // Blockmodel::copy (blockmodel.cpp:151)
+        CK(cudaStreamSynchronize(st));
+        return SBPGPU_OK;
+    });
+    if (rc != SBPGPU_OK) {
+        if (bm) {
+            free_all(bm->owned);
+            delete bm;
+        }
+        return rc;
+    }
+    *out = bm;
+    return SBPGPU_OK;
+}
+
+void sbpgpu_bm_destroy(sbpgpu_bm* bm) {
+    if (!bm) return;
+    cudaStreamSynchronize(bm->g->ctx->stream);
+    free_all(bm->owned);
+    delete bm;
+}
+
+int64_t sbpgpu_bm_num_blocks(const sbpgpu_bm* bm) { return bm ? bm->d.B : 0; }
+int64_t sbpgpu_bm_nnz(const sbpgpu_bm* bm) { return bm ? bm->d.nnz : 0; }
+double sbpgpu_bm_entropy(const sbpgpu_bm* bm) { return bm ? bm->entropy : 0.0; }
+
+sbpgpu_status sbpgpu_bm_read(const sbpgpu_bm* bm, int32_t* assignment, int64_t* d_out, int64_t* d_in, int64_t* d_tot,
+                             int64_t* sizes, int32_t* rows, int32_t* cols, int64_t* counts) {
+    if (!bm) return SBPGPU_EINVAL;
+    sbpgpu_graph* g = bm->g;
+    return guarded(g->ctx, [&] {
+        cudaStream_t st = g->ctx->stream;
+        const int64_t B = bm->d.B, nnz = bm->d.nnz;
+        if (assignment) CK(cudaMemcpyAsync(assignment, bm->d.asg, g->N * 4, cudaMemcpyDeviceToHost, st));
+        std::vector<int32_t> tmp;
+        auto widen = [&](const int32_t* src, int64_t* dst, int64_t n) {
+            if (!dst) return;
+            tmp.resize(n);
+            CK(cudaMemcpyAsync(tmp.data(), src, n * 4, cudaMemcpyDeviceToHost, st));
+            CK(cudaStreamSynchronize(st));
+            for (int64_t i = 0; i < n; ++i) dst[i] = tmp[i];
+        };
+        widen(bm->d.d_out, d_out, B);
+        widen(bm->d.d_in, d_in, B);
+        widen(bm->d.d_tot, d_tot, B);
+        widen(bm->d.sizes, sizes, B);
+        if (rows) CK(cudaMemcpyAsync(rows, bm->d.row_of, nnz * 4, cudaMemcpyDeviceToHost, st));
+        if (cols) CK(cudaMemcpyAsync(cols, bm->d.row_col, nnz * 4, cudaMemcpyDeviceToHost, st));
+        widen(bm->d.row_cnt, counts, nnz);
+        CK(cudaStreamSynchronize(st));
+        return SBPGPU_OK;
+    });
+}
+
+sbpgpu_status sbpgpu_mdl(sbpgpu_bm* bm, double* out) {
+    if (!bm || !out) return SBPGPU_EINVAL;
+    return guarded(bm->g->ctx, [&] {
+        *out = do_mdl(bm);
+        return SBPGPU_OK;
+    });
+}
+
+sbpgpu_status sbpgpu_delta_mdl_batch(sbpgpu_bm* bm, int64_t n, const int32_t* vertex, const int32_t* proposal,
+                                     double* out) {
+    if (!bm || n < 0 || (n && (!vertex || !proposal || !out))) return SBPGPU_EINVAL;
+    sbpgpu_graph* g = bm->g;
+    return guarded(g->ctx, [&] {
+        if (n == 0) return SBPGPU_OK;
+        int32_t max_k = 0;
+        for (int64_t i = 0; i < n; ++i) {
+            if (vertex[i] < 0 || vertex[i] >= g->N || proposal[i] < 0 || proposal[i] >= bm->d.B)
+                throw ApiError(SBPGPU_EINVAL, "vertex or proposal out of range");
+            max_k = std::max(max_k, g->kdeg[vertex[i]]);
+        }
+        if (max_k > 8192) throw ApiError(SBPGPU_EUNSUPPORTED, "vertex degree above 8192");
+        std::vector<void*> tmp;
+        int32_t* dv = dalloc<int32_t>(tmp, n);
+        int32_t* ds = dalloc<int32_t>(tmp, n);
+        long long* dout = dalloc<long long>(tmp, n);
+        cudaStream_t st = g->ctx->stream;
+        std::vector<long long> h(n);
+        try {
+            CK(cudaMemcpyAsync(dv, vertex, n * 4, cudaMemcpyHostToDevice, st));
+            CK(cudaMemcpyAsync(ds, proposal, n * 4, cudaMemcpyHostToDevice, st));
+            launch_vertex_dS_batch(g->dg, bm->d, dv, ds, n, max_k, dout, g->w, st);
+            CK(cudaMemcpyAsync(h.data(), dout, n * 8, cudaMemcpyDeviceToHost, st));
+            check_flags(g);
+        } catch (...) {
+            free_all(tmp);
+            throw;
+        }
+        free_all(tmp);
+        for (int64_t i = 0; i < n; ++i) out[i] = (double)h[i] * (1.0 / 16777216.0);
+        return SBPGPU_OK;
+    });
+}
+
+sbpgpu_status sbpgpu_merge_delta_mdl_batch(sbpgpu_bm* bm, int64_t n, const int32_t* block, const int32_t* proposal,
+                                           double* out) {
+    if (!bm || n < 0 || (n && (!block || !proposal || !out))) return SBPGPU_EINVAL;
+    sbpgpu_graph* g = bm->g;
+    return guarded(g->ctx, [&] {
+        if (n == 0) return SBPGPU_OK;
+        for (int64_t i = 0; i < n; ++i)
+            if (block[i] < 0 || block[i] >= bm->d.B || proposal[i] < 0 || proposal[i] >= bm->d.B ||
+                block[i] == proposal[i])
+                throw ApiError(SBPGPU_EINVAL, "block or proposal out of range");
+        std::vector<void*> tmp;
+        int32_t* dr = dalloc<int32_t>(tmp, n);
+        int32_t* ds = dalloc<int32_t>(tmp, n);
+        long long* dout = dalloc<long long>(tmp, n);
+        cudaStream_t st = g->ctx->stream;
+        std::vector<long long> h(n);
+        try {
+            CK(cudaMemcpyAsync(dr, block, n * 4, cudaMemcpyHostToDevice, st));
+            CK(cudaMemcpyAsync(ds, proposal, n * 4, cudaMemcpyHostToDevice, st));
+            launch_merge_dS_batch(g->dg, bm->d, dr, ds, n, dout, g->w, st);
+            CK(cudaMemcpyAsync(h.data(), dout, n * 8, cudaMemcpyDeviceToHost, st));
+            check_flags(g);
+        } catch (...) {
+            free_all(tmp);
+            throw;
+        }
+        free_all(tmp);
+        for (int64_t i = 0; i < n; ++i) out[i] = (double)h[i] * (1.0 / 16777216.0);
+        return SBPGPU_OK;
+    });
+}
+
+sbpgpu_status sbpgpu_propose_batch(sbpgpu_bm* bm, int64_t n, const int32_t* vertex, uint64_t seed, uint32_t c1,
+                                   uint32_t c2, uint32_t c3, int32_t* out) {
+    if (!bm || n < 0 || (n && (!vertex || !out))) return SBPGPU_EINVAL;
+    sbpgpu_graph* g = bm->g;
+    return guarded(g->ctx, [&] {
+        if (n == 0) return SBPGPU_OK;
+        for (int64_t i = 0; i < n; ++i)
+            if (vertex[i] < 0 || vertex[i] >= g->N) throw ApiError(SBPGPU_EINVAL, "vertex out of range");
+        if (bm->d.B < 2) throw ApiError(SBPGPU_EINVAL, "proposals need at least two blocks");
+        std::vector<void*> tmp;
+        int32_t* dv = dalloc<int32_t>(tmp, n);
+        int32_t* dout = dalloc<int32_t>(tmp, n);
+        cudaStream_t st = g->ctx->stream;
+        try {
+            CK(cudaMemcpyAsync(dv, vertex, n * 4, cudaMemcpyHostToDevice, st));
+            launch_propose_batch(g->dg, bm->d, dv, n, seed, c1, c2, c3, dout, st);
+            CK(cudaMemcpyAsync(out, dout, n * 4, cudaMemcpyDeviceToHost, st));
+            check_flags(g);
+        } catch (...) {
+            free_all(tmp);
+            throw;
+        }
+        free_all(tmp);
+        return SBPGPU_OK;
+    });
+}
+
+sbpgpu_status sbpgpu_gibbs_batch(sbpgpu_bm* bm, const sbpgpu_config* cfg, int64_t n, const int32_t* vertex,
+                                 uint64_t seed, uint32_t iteration, uint32_t step, int32_t* out_moves,
+                                 int64_t* applied) {
+    if (!bm || !cfg || n < 0 || (n && !vertex)) return SBPGPU_EINVAL;
+    sbpgpu_graph* g = bm->g;
+    return guarded(g->ctx, [&] {
+        require_greedy(*cfg);
+        if (bm->d.B < 2) throw ApiError(SBPGPU_EINVAL, "proposals need at least two blocks");
+        for (int64_t i = 0; i < n; ++i)
+            if (vertex[i] < 0 || vertex[i] >= g->N) throw ApiError(SBPGPU_EINVAL, "vertex out of range");
+        cudaStream_t st = g->ctx->stream;
+        CK(cudaMemcpyAsync(g->w.list_tmp, vertex, n * 4, cudaMemcpyHostToDevice, st));
+        reset_counters(g);
+        gibbs_batch_dev(bm, g->w.list_tmp, (int32_t)n, seed, iteration, step, cfg->greedy);
+        if (out_moves) {
+            std::vector<int32_t> mv(g->N);
+            CK(cudaMemcpyAsync(mv.data(), g->w.moves, g->N * 4, cudaMemcpyDeviceToHost, st));
+            CK(cudaStreamSynchronize(st));
+            for (int64_t i = 0; i < n; ++i) out_moves[i] = mv[vertex[i]];
+        }
+        CK(cudaMemcpyAsync(g->flags_host, g->w.flags_dev, sizeof(DevFlags), cudaMemcpyDeviceToHost, st));
+        check_flags(g);
+        if (applied) *applied = (int64_t)g->flags_host->counters[2];
+        reset_counters(g);
+        return SBPGPU_OK;
+    });
+}
+
+sbpgpu_status sbpgpu_mh_chain(sbpgpu_bm* bm, const sbpgpu_config* cfg, int64_t n, const int32_t* vertex,
+                              uint64_t seed, uint32_t iteration, uint32_t step, int64_t* applied) {
+    if (!bm || !cfg || n < 0 || (n && !vertex)) return SBPGPU_EINVAL;
+    sbpgpu_graph* g = bm->g;
+    return guarded(g->ctx, [&] {
+        require_greedy(*cfg);
+        if (bm->d.B < 2) throw ApiError(SBPGPU_EINVAL, "proposals need at least two blocks");
+        int32_t max_k = 0;
+        int64_t ksum = 0;
+        for (int64_t i = 0; i < n; ++i) {
+            if (vertex[i] < 0 || vertex[i] >= g->N) throw ApiError(SBPGPU_EINVAL, "vertex out of range");
+            max_k = std::max(max_k, g->kdeg[vertex[i]]);
+            ksum += g->kdeg[vertex[i]];
+        }
+        cudaStream_t st = g->ctx->stream;
+        CK(cudaMemcpyAsync(g->w.list_tmp, vertex, n * 4, cudaMemcpyHostToDevice, st));
+        reset_counters(g);
+        chain_run(bm, g->w.list_tmp, (int32_t)n, max_k, ksum, seed, iteration, step, cfg->greedy);
+        CK(cudaMemcpyAsync(g->flags_host, g->w.flags_dev, sizeof(DevFlags), cudaMemcpyDeviceToHost, st));
+        check_flags(g);
+        if (applied) *applied = (int64_t)g->flags_host->counters[5];
+        reset_counters(g);
+        return SBPGPU_OK;
+    });
+}
+
+sbpgpu_status sbpgpu_mcmc(sbpgpu_bm* bm, const sbpgpu_config* cfg, uint64_t seed, int32_t step,
+                          int32_t golden_ratio_not_reached, sbpgpu_stats* stats) {
+    if (!bm || !cfg) return SBPGPU_EINVAL;
+    sbpgpu_graph* g = bm->g;
+    return guarded(g->ctx, [&] {
+        g->st = sbpgpu_stats{};
+        const int64_t l0 = kernel_launches();
+        reset_counters(g);
+        mcmc_impl(bm, *cfg, seed, step, golden_ratio_not_reached != 0);
+        harvest_counters(g);
+        g->st.kernel_launches = kernel_launches() - l0;
+        if (stats) *stats = g->st;
+        return SBPGPU_OK;
+    });
+}
+
+sbpgpu_status sbpgpu_merge_blocks(sbpgpu_bm* bm, const sbpgpu_config* cfg, uint64_t seed, int32_t step,
+                                  int64_t num_blocks_to_merge, sbpgpu_stats* stats) {
+    if (!bm || !cfg || num_blocks_to_merge < 0) return SBPGPU_EINVAL;
+    sbpgpu_graph* g = bm->g;
+    return guarded(g->ctx, [&] {
+        g->st = sbpgpu_stats{};
+        const int64_t l0 = kernel_launches();
+        reset_counters(g);
+        merge_impl(bm, *cfg, seed, step, num_blocks_to_merge);
+        g->st.kernel_launches = kernel_launches() - l0;
+        if (stats) *stats = g->st;
+        return SBPGPU_OK;
+    });
+}
+
+sbpgpu_status sbpgpu_merge_proposals(sbpgpu_bm* bm, uint64_t seed, int32_t step, int32_t* best_proposal,
+                                     double* best_delta) {
+    if (!bm) return SBPGPU_EINVAL;
+    sbpgpu_graph* g = bm->g;
+    return guarded(g->ctx, [&] {
+        if (bm->d.B < 2) throw ApiError(SBPGPU_EINVAL, "merge proposals need at least two blocks");
+        cudaStream_t st = g->ctx->stream;
+        reset_counters(g);
+        merge_propose(g->dg, bm->d, seed, (uint32_t)step, g->w, st);
+        if (best_proposal) CK(cudaMemcpyAsync(best_proposal, g->w.best, bm->d.B * 4, cudaMemcpyDeviceToHost, st));
+        if (best_delta) CK(cudaMemcpyAsync(best_delta, g->w.best_dS, bm->d.B * 8, cudaMemcpyDeviceToHost, st));
+        check_flags(g);
+        return SBPGPU_OK;
+    });
+}
+
+sbpgpu_status sbpgpu_sbp(sbpgpu_graph* g, const sbpgpu_config* cfg_in, uint64_t seed, int32_t* out_assignment,
+                         int64_t* num_blocks, double* out_mdl, sbpgpu_stats* stats) {
+    if (!g || !cfg_in) return SBPGPU_EINVAL;
+    sbpgpu_ctx* ctx = g->ctx;
+    sbpgpu_bm* bm = nullptr;
+    std::vector<void*> slots_mem;
+    const sbpgpu_status rc = guarded(ctx, [&] {
+        const sbpgpu_config cfg = *cfg_in;
+        require_greedy(cfg);
+        g->st = sbpgpu_stats{};
+        const int64_t l0 = kernel_launches();
+        reset_counters(g);
+        cudaStream_t st = ctx->stream;
+        const int64_t N = g->N;
+        // Blockmodel(N, graph, 0.5) (sbp.cpp:23): identity assignment, B = N.
+        bm = new_bm(g, N);
+        CK(cudaMemcpyAsync(bm->d.asg, g->d_all, N * 4, cudaMemcpyDeviceToDevice, st));
+        do_rebuild(bm);
+        bm->num_blocks_to_merge = (int64_t)((double)N * 0.5);
+        bm->entropy = DBL_MAX;
+        struct Slot {
+            bool empty = true;
+            int64_t B = 0;
+            double entropy = DBL_MAX;
+            int32_t* asg = nullptr;
+        } s[3];
+        for (auto& sl : s) sl.asg = dalloc<int32_t>(slots_mem, N);
+        bool optimal = false;
+        int32_t step = 0;
+        while (!optimal) {
+            merge_impl(bm, cfg, seed, step, bm->num_blocks_to_merge);
+            mcmc_impl(bm, cfg, seed, step, s[2].empty);
+            ++step;
+            g->st.outer_steps++;
+            // BlockmodelTriplet::update (blockmodel_triplet.cpp:82-105)
+            int idx;
+            if (s[1].empty) {
+                idx = 1;
+            } else if (bm->entropy <= s[1].entropy) {
+                const int old = (s[1].B > bm->d.B) ? 0 : 2;
+                std::swap(s[old], s[1]);
+                idx = 1;
+            } else {
+                idx = (s[1].B > bm->d.B) ? 2 : 0;
+            }
+            s[idx].empty = false;
+            s[idx].B = bm->d.B;
+            s[idx].entropy = bm->entropy;
+            CK(cudaMemcpyAsync(s[idx].asg, bm->d.asg, N * 4, cudaMemcpyDeviceToDevice, st));
+            // BlockmodelTriplet::get_next_blockmodel (blockmodel_triplet.cpp:4-37)
+            const Slot* src;
+            int64_t next_merge;
+            if (s[2].empty) {
+                src = &s[1];
+                next_merge = (int64_t)((double)src->B * 0.5);
+                if (next_merge == 0) optimal = true;
+            } else {
+                if ((!s[0].empty && s[0].B - s[2].B == 2) || (s[0].empty && s[1].B - s[2].B == 1)) optimal = true;
+                if (optimal) {
+                    src = &s[1];
+                    next_merge = 0;
+                } else {
+                    int index;
+                    if (s[0].empty && s[1].B > s[2].B) index = 1;
+                    else if ((s[0].B - s[1].B) >= (s[1].B - s[2].B)) index = 0;
+                    else index = 1;
+                    int64_t next_try = s[index + 1].B;
+                    next_try += (int64_t)((double)(s[index].B - s[index + 1].B) * 0.618);
+                    src = &s[index];
+                    next_merge = src->B - next_try;
+                }
+            }
+            CK(cudaMemcpyAsync(bm->d.asg, src->asg, N * 4, cudaMemcpyDeviceToDevice, st));
+            bm->d.B = (int32_t)src->B;
+            bm->entropy = src->entropy;
+            bm->num_blocks_to_merge = next_merge;
+            do_rebuild(bm);
+        }
+        if (out_assignment) CK(cudaMemcpyAsync(out_assignment, bm->d.asg, N * 4, cudaMemcpyDeviceToHost, st));
+        harvest_counters(g);
+        if (num_blocks) *num_blocks = bm->d.B;
+        if (out_mdl) *out_mdl = bm->entropy;
+        g->st.kernel_launches = kernel_launches() - l0;
+        if (stats) *stats = g->st;
+        return SBPGPU_OK;
+    });
+    free_all(slots_mem);
+    if (bm) {
+        free_all(bm->owned);
+        delete bm;
+    }
+    return rc;
+}
+
+void sbpgpu_set_timing(sbpgpu_ctx* ctx, int32_t enabled) {
+    if (ctx) ctx->timing = enabled != 0;
+}
+
+sbpgpu_status sbpgpu_read_timing(sbpgpu_ctx* ctx, sbpgpu_kernel_timing* out) {
+    if (!ctx || !out) return SBPGPU_EINVAL;
+    return guarded(ctx, [&] {
+        ctx->collect();
+        *out = ctx->tm;
+        ctx->tm = sbpgpu_kernel_timing{};
+        return SBPGPU_OK;
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,303 @@
+// Proposal samplers and delta-MDL evaluation on the device.
+//
+// Delta-MDL follows entropy::delta_mdl (reference src/entropy.cpp:298-403) and
+// entropy::block_merge_delta_mdl (:129-182) term by term, with two differences of
+// method that leave the value unchanged:
+//  * every term v * (L[v] - L[din] - L[dout]) is accumulated as an exact int64 in units
+//    of 2^-24 (each logf value of an integer is a multiple of 2^-24), so the sum does
+//    not depend on the order of summation;
+//  * the reference's loops over the unchanged cells of rows r, s and columns r, s only
+//    change their block degrees, so their contribution is
+//    (sum of the unchanged counts) * (L[new degree] - L[old degree]); the unchanged
+//    count is the block degree minus the counts of the cells the move touches.  Only
+//    the O(k) touched cells are looked up.
+// Key presence (a Delta cell whose net change is zero is visited by both loops of the
+// reference) is reproduced exactly: for a vertex move only cells (r,s) and (s,r) can
+// be present with a zero change.
+#pragma once
+
+#include "common.cuh"
+
+namespace sbp {
+
+// Matrix accessors.  row_get(r, c) = M[r, c] searching row r; col_get(c, r) = M[r, c]
+// searching column c.
+struct CsrAcc {
+    DevBM bm;
+    __device__ __forceinline__ int32_t row_get(int32_t r, int32_t c) const {
+        return csr_get(bm.row_off, bm.row_col, bm.row_cnt, r, c);
+    }
+    __device__ __forceinline__ int32_t col_get(int32_t c, int32_t r) const {
+        return csr_get(bm.col_off, bm.col_row, bm.col_cnt, c, r);
+    }
+};
+
+struct ChainAcc {
+    DevChain ch;
+    __device__ __forceinline__ int32_t row_get(int32_t r, int32_t c) const { return chain_get(ch, r, c); }
+    __device__ __forceinline__ int32_t col_get(int32_t c, int32_t r) const { return chain_get(ch, r, c); }
+};
+
+// Thread-group abstraction: one warp (kThreads == 32) or the whole CTA.
+template <int kThreads>
+struct Group {
+    __device__ __forceinline__ static int rank() { return kThreads == 32 ? (int)(threadIdx.x & 31) : (int)threadIdx.x; }
+    __device__ __forceinline__ static void sync() {
+        if (kThreads == 32) __syncwarp();
+        else __syncthreads();
+    }
+    // Sum over the group; red must hold >= 32 long longs of shared memory (CTA case).
+    __device__ __forceinline__ static long long sum(long long x, long long* red) {
+        x = warp_sum_ll(x);
+        if (kThreads == 32) return x;
+        const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+        __syncthreads();
+        if (lane == 0) red[w] = x;
+        __syncthreads();
+        long long t = 0;
+        for (int i = 0; i < kThreads / 32; ++i) t += red[i];
+        __syncthreads();
+        return t;
+    }
+};
+
+// ------------------------------------------------------------------ group hash
+// Open-addressing table in shared (or global) memory aggregating per-block counts.
+__device__ __forceinline__ uint32_t hslot(int32_t b, int log2cap) {
+    return ((uint32_t)b * 0x9E3779B1u) >> (32 - log2cap);
+}
+__device__ __forceinline__ void hinsert(int32_t* keys, int32_t* cnt, int log2cap, int32_t b) {
+    const uint32_t mask = (1u << log2cap) - 1u;
+    uint32_t s = hslot(b, log2cap);
+    for (uint32_t probe = 0; probe <= mask; ++probe) {
+        const int32_t k = ((volatile int32_t*)keys)[s];
+        if (k == b) {
+            atomicAdd(cnt + s, 1);
+            return;
+        }
+        if (k == -1) {
+            const int32_t prev = atomicCAS(keys + s, -1, b);
+            if (prev == -1 || prev == b) {
+                atomicAdd(cnt + s, 1);
+                return;
+            }
+        }
+        s = (s + 1) & mask;
+    }
+}
+
+// ------------------------------------------------------------------ samplers
+// common::propose_new_block(..., block_merge=false) (reference src/common.cpp:138-198):
+// a uniform neighbour among out-neighbours then in-neighbours without the vertex itself,
+// its block nb, then a multinomial over nb's row (ascending column) followed by nb's
+// column without the diagonal (ascending row).  Static CSR/CSC only.
+__device__ __forceinline__ int32_t sample_vertex_proposal(const DevGraph& g, const DevBM& bm, int32_t v, int32_t r,
+                                                          const uint32_t w[4]) {
+    const int32_t o0 = __ldg(g.out_off + v), o1 = __ldg(g.out_off + v + 1);
+    const int32_t i0 = __ldg(g.inns_off + v), i1 = __ldg(g.inns_off + v + 1);
+    const int32_t kout = o1 - o0, k = kout + (i1 - i0);
+    if (k == 0) return random_block(r, bm.B, w[1]);
+    const int32_t idx = (int32_t)u32_below(w[0], (uint32_t)k);
+    const int32_t nbr = idx < kout ? __ldg(g.out_nbr + o0 + idx) : __ldg(g.inns_nbr + i0 + idx - kout);
+    const int32_t nb = bm.asg[nbr];
+    const long long R = bm.d_out[nb];
+    const int32_t dg = bm.diag[nb];
+    const long long C = (long long)bm.d_in[nb] - dg;
+    const long long t = (long long)u64_below(w[1], w[2], (uint64_t)(R + C));
+    if (t < R) return seg_select(bm.row_col, bm.row_cum, bm.row_off[nb], bm.row_off[nb + 1], t, -1, 0, -1, 0);
+    const int32_t p = dg > 0 ? csr_find(bm.col_off, bm.col_row, nb, nb) : -1;
+    return seg_select(bm.col_row, bm.col_cum, bm.col_off[nb], bm.col_off[nb + 1], t - R, p, dg, -1, 0);
+}
+
+// common::propose_new_block(..., block_merge=true) as used by propose_merge_sparse
+// (reference src/block_merge.cpp:251-256): neighbour block drawn from row r then column r
+// weighted by counts; then nb's neighbour weights without block r.
+__device__ __forceinline__ int32_t sample_merge_proposal(const DevBM& bm, int32_t r, const uint32_t w[4]) {
+    const long long Rr = bm.d_out[r], Cr = bm.d_in[r];
+    if (Rr + Cr == 0) return random_block(r, bm.B, w[0]);
+    const long long t = (long long)u64_below(w[0], w[1], (uint64_t)(Rr + Cr));
+    const int32_t nb = t < Rr ? seg_select(bm.row_col, bm.row_cum, bm.row_off[r], bm.row_off[r + 1], t, -1, 0, -1, 0)
+                              : seg_select(bm.col_row, bm.col_cum, bm.col_off[r], bm.col_off[r + 1], t - Rr, -1, 0,
+                                           -1, 0);
+    if (nb < 0) return -1;
+    const int32_t pr = csr_find(bm.row_off, bm.row_col, nb, r);  // (nb, r) in row nb
+    const long long wr = pr >= 0 ? bm.row_cnt[pr] : 0;
+    const long long R2 = (long long)bm.d_out[nb] - wr;
+    int32_t pa = csr_find(bm.col_off, bm.col_row, nb, nb);        // (nb, nb) in column nb
+    long long wa = pa >= 0 ? bm.col_cnt[pa] : 0;
+    int32_t pb = -1;
+    long long wb = 0;
+    if (nb != r) {
+        pb = csr_find(bm.col_off, bm.col_row, nb, r);             // (r, nb) in column nb
+        wb = pb >= 0 ? bm.col_cnt[pb] : 0;
+    }
+    const long long C2 = (long long)bm.d_in[nb] - wa - wb;
+    if (R2 + C2 == 0) return random_block(r, bm.B, w[2]);
+    const long long t2 = (long long)u64_below(w[2], w[3], (uint64_t)(R2 + C2));
+    if (t2 < R2) return seg_select(bm.row_col, bm.row_cum, bm.row_off[nb], bm.row_off[nb + 1], t2, pr, wr, -1, 0);
+    if (pa > pb && pb >= 0) {
+        const int32_t tp = pa;
+        pa = pb;
+        pb = tp;
+        const long long tw = wa;
+        wa = wb;
+        wb = tw;
+    }
+    if (pa < 0) {
+        pa = pb;
+        wa = wb;
+        pb = -1;
+        wb = 0;
+    }
+    return seg_select(bm.col_row, bm.col_cum, bm.col_off[nb], bm.col_off[nb + 1], t2 - R2, pa, wa, pb, wb);
+}
+
+// ------------------------------------------------------------------ vertex delta-MDL
+struct VertexScalars {
+    int32_t kout, kin, L, selfw;
+};
+
+// Accumulates the touched-cell terms of moving v from r to s and returns the exact
+// delta-MDL in units of 2^-24.  hk/hO/hI: group hash of 2^log2cap slots (>= 2k).
+template <int kThreads, typename Acc>
+__device__ long long vertex_delta_fixed(const DevGraph& g, const int32_t* asg, const int32_t* d_out,
+                                        const int32_t* d_in, const Acc& M, int32_t v, int32_t r, int32_t s,
+                                        int32_t* hk, int32_t* hO, int32_t* hI, int log2cap, long long* red) {
+    typedef Group<kThreads> G;
+    const int t = G::rank();
+    const int cap = 1 << log2cap;
+    for (int i = t; i < cap; i += kThreads) {
+        hk[i] = -1;
+        hO[i] = 0;
+        hI[i] = 0;
+    }
+    G::sync();
+    const int32_t o0 = __ldg(g.out_off + v), o1 = __ldg(g.out_off + v + 1);
+    const int32_t i0 = __ldg(g.inns_off + v), i1 = __ldg(g.inns_off + v + 1);
+    for (int32_t i = o0 + t; i < o1; i += kThreads) {
+        const int32_t u = __ldg(g.out_nbr + i);
+        if (u != v) hinsert(hk, hO, log2cap, asg[u]);
+    }
+    for (int32_t i = i0 + t; i < i1; i += kThreads) hinsert(hk, hI, log2cap, asg[__ldg(g.inns_nbr + i)]);
+    G::sync();
+    const LogTab Lq{g.Lq, g.E + 1};
+    const int32_t kout = o1 - o0, kin = i1 - i0, L = __ldg(g.selfcnt + v), selfw = L > 0 ? 1 : 0;
+    const int32_t dout_r = d_out[r], dout_s = d_out[s], din_r = d_in[r], din_s = d_in[s];
+    const int32_t dout_r2 = dout_r - kout, dout_s2 = dout_s + kout;
+    const int32_t din_r2 = din_r - (kin + selfw), din_s2 = din_s + (kin + selfw);
+    long long acc = 0, sRo = 0, sSo = 0, sRi = 0, sSi = 0, spec = 0;
+    for (int i = t; i < cap; i += kThreads) {
+        const int32_t b = hk[i];
+        if (b < 0) continue;
+        const int32_t O = hO[i], I = hI[i];
+        if (b == r) {
+            spec += ((long long)O << 48) | ((long long)I << 32);
+            continue;
+        }
+        if (b == s) {
+            spec += ((long long)O << 16) | (long long)I;
+            continue;
+        }
+        if (O > 0) {
+            const int32_t Mrb = M.row_get(r, b), Msb = M.row_get(s, b), dinb = d_in[b];
+            acc += ce_fixed(Lq, Mrb, dinb, dout_r) - ce_fixed(Lq, Mrb - O, dinb, dout_r2);
+            acc += ce_fixed(Lq, Msb, dinb, dout_s) - ce_fixed(Lq, Msb + O, dinb, dout_s2);
+            sRo += Mrb;
+            sSo += Msb;
+        }
+        if (I > 0) {
+            const int32_t Mbr = M.col_get(r, b), Mbs = M.col_get(s, b), doutb = d_out[b];
+            acc += ce_fixed(Lq, Mbr, din_r, doutb) - ce_fixed(Lq, Mbr - I, din_r2, doutb);
+            acc += ce_fixed(Lq, Mbs, din_s, doutb) - ce_fixed(Lq, Mbs + I, din_s2, doutb);
+            sRi += Mbr;
+            sSi += Mbs;
+        }
+    }
+    acc = G::sum(acc, red);
+    sRo = G::sum(sRo, red);
+    sSo = G::sum(sSo, red);
+    sRi = G::sum(sRi, red);
+    sSi = G::sum(sSi, red);
+    spec = G::sum(spec, red);
+    // Each count is < 2^16 in this packing only when k < 65536; the callers guarantee it.
+    const int32_t Or = (int32_t)((spec >> 48) & 0xffff), Ir = (int32_t)((spec >> 32) & 0xffff);
+    const int32_t Os = (int32_t)((spec >> 16) & 0xffff), Is = (int32_t)(spec & 0xffff);
+    const int32_t Mrr = M.row_get(r, r), Mrs = M.row_get(r, s), Msr = M.row_get(s, r), Mss = M.row_get(s, s);
+    long long tot = acc;
+    {   // (r, r): present iff a neighbour lies in r or a self-loop exists; its change is never zero.
+        const int32_t d = -Or - Ir - L;
+        if (Or | Ir | L) tot += ce_fixed(Lq, Mrr, din_r, dout_r) - ce_fixed(Lq, Mrr + d, din_r2, dout_r2);
+        else tot += ce_delta(Lq, Mrr, din_r, dout_r, din_r2, dout_r2);
+    }
+    {   // (r, s): may be present with a zero change; then both loops count it.
+        const int32_t d = Ir - Os;
+        if (Os | Ir) tot += ce_fixed(Lq, Mrs, din_s, dout_r) - ce_fixed(Lq, Mrs + d, din_s2, dout_r2);
+        if (d == 0) tot += ce_delta(Lq, Mrs, din_s, dout_r, din_s2, dout_r2);
+    }
+    {   // (s, r)
+        const int32_t d = Or - Is;
+        if (Or | Is) tot += ce_fixed(Lq, Msr, din_r, dout_s) - ce_fixed(Lq, Msr + d, din_r2, dout_s2);
+        if (d == 0) tot += ce_delta(Lq, Msr, din_r, dout_s, din_r2, dout_s2);
+    }
+    {   // (s, s)
+        const int32_t d = Os + Is + L;
+        if (Os | Is | L) tot += ce_fixed(Lq, Mss, din_s, dout_s) - ce_fixed(Lq, Mss + d, din_s2, dout_s2);
+        else tot += ce_delta(Lq, Mss, din_s, dout_s, din_s2, dout_s2);
+    }
+    // Unchanged cells of rows r, s and columns r, s (entropy.cpp:346-401).
+    tot += ((long long)dout_r - Mrr - Mrs - sRo) * (Lx(Lq, dout_r2) - Lx(Lq, dout_r));
+    tot += ((long long)dout_s - Msr - Mss - sSo) * (Lx(Lq, dout_s2) - Lx(Lq, dout_s));
+    tot += ((long long)din_r - Mrr - Msr - sRi) * (Lx(Lq, din_r2) - Lx(Lq, din_r));
+    tot += ((long long)din_s - Mrs - Mss - sSi) * (Lx(Lq, din_s2) - Lx(Lq, din_s));
+    return tot;
+}
+
+// ------------------------------------------------------------------ merge delta-MDL
+// entropy::block_merge_delta_mdl for merging r into s over the static CSR/CSC.
+template <int kThreads>
+__device__ long long merge_delta_fixed_csr(const DevGraph& g, const DevBM& bm, int32_t r, int32_t s, long long* red) {
+    typedef Group<kThreads> G;
+    const int t = G::rank();
+    const LogTab Lq{g.Lq, g.E + 1};
+    const int32_t dout_r = bm.d_out[r], din_r = bm.d_in[r], dout_s = bm.d_out[s], din_s = bm.d_in[s];
+    const int32_t dout_s2 = dout_s + dout_r, din_s2 = din_s + din_r;
+    long long acc = 0, sRow = 0, sCol = 0;
+    const int32_t ro0 = bm.row_off[r], ro1 = bm.row_off[r + 1];
+    for (int32_t j = ro0 + t; j < ro1; j += kThreads) {
+        const int32_t c = bm.row_col[j], m = bm.row_cnt[j], dinc = bm.d_in[c];
+        acc += ce_fixed(Lq, m, dinc, dout_r);
+        if (c != r && c != s) {
+            const int32_t Msc = csr_get(bm.row_off, bm.row_col, bm.row_cnt, s, c);
+            acc += ce_fixed(Lq, Msc, dinc, dout_s) - ce_fixed(Lq, Msc + m, dinc, dout_s2);
+            sRow += Msc;
+        }
+    }
+    const int32_t co0 = bm.col_off[r], co1 = bm.col_off[r + 1];
+    for (int32_t j = co0 + t; j < co1; j += kThreads) {
+        const int32_t x = bm.col_row[j], m = bm.col_cnt[j];
+        if (x == r) continue;
+        const int32_t doutx = bm.d_out[x];
+        acc += ce_fixed(Lq, m, din_r, doutx);
+        if (x != s) {
+            const int32_t Mxs = csr_get(bm.col_off, bm.col_row, bm.col_cnt, s, x);
+            acc += ce_fixed(Lq, Mxs, din_s, doutx) - ce_fixed(Lq, Mxs + m, din_s2, doutx);
+            sCol += Mxs;
+        }
+    }
+    acc = G::sum(acc, red);
+    sRow = G::sum(sRow, red);
+    sCol = G::sum(sCol, red);
+    const int32_t Mrr = csr_get(bm.row_off, bm.row_col, bm.row_cnt, r, r);
+    const int32_t Mrs = csr_get(bm.row_off, bm.row_col, bm.row_cnt, r, s);
+    const int32_t Msr = csr_get(bm.row_off, bm.row_col, bm.row_cnt, s, r);
+    const int32_t Mss = csr_get(bm.row_off, bm.row_col, bm.row_cnt, s, s);
+    const int32_t dss = Mrr + Mrs + Msr;
+    long long tot = acc;
+    if (dss > 0) tot += ce_fixed(Lq, Mss, din_s, dout_s) - ce_fixed(Lq, Mss + dss, din_s2, dout_s2);
+    else tot += ce_delta(Lq, Mss, din_s, dout_s, din_s2, dout_s2);
+    tot += ((long long)dout_s - Msr - Mss - sRow) * (Lx(Lq, dout_s2) - Lx(Lq, dout_s));
+    tot += ((long long)din_s - Mrs - Mss - sCol) * (Lx(Lq, din_s2) - Lx(Lq, din_s));
+    return tot;
+}
+
+}  // namespace sbp

@@ -1,0 +1,94 @@
+// Host-side launchers of the sbpgpu kernels (implemented in blockmodel.cu, sweep.cu,
+// merge.cu).  All work is issued on the given stream.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace sbp {
+
+// Device buffers shared by the phases of one graph (sized for B <= N, nnz <= E).
+struct Work {
+    // sort / rebuild
+    uint64_t* keys = nullptr;
+    uint64_t* keys_alt = nullptr;
+    int32_t* vals = nullptr;
+    int32_t* vals_alt = nullptr;
+    int32_t* flags = nullptr;
+    void* temp = nullptr;
+    size_t temp_bytes = 0;
+    int32_t* d_scalar = nullptr;       // [8] small device scalars
+    unsigned long long* d_acc = nullptr;  // [4] device accumulators
+    // sweeps
+    int32_t* moves = nullptr;          // [N] accepted proposal per vertex or -1
+    int32_t* m_out = nullptr;          // [N]
+    int32_t* last = nullptr;           // [N]
+    int32_t* acc = nullptr;            // [N]
+    int32_t* dep = nullptr;            // [2N]
+    int32_t* list_small = nullptr;     // [N]
+    int32_t* list_big = nullptr;       // [N]
+    int32_t* list_tmp = nullptr;       // [N]
+    int32_t* ghash = nullptr;          // global group hash for huge vertices [3 << ghash_log2]
+    int ghash_log2 = 0;
+    // chain state
+    DevChain chain{};
+    unsigned long long* chain_keys = nullptr;
+    int32_t* chain_vals = nullptr;
+    uint64_t chain_cap = 0;            // allocated slots (power of two)
+    int32_t* pool = nullptr;
+    int32_t pool_cap = 0;
+    int32_t* row_head = nullptr;       // [N]
+    int32_t* col_head = nullptr;       // [N]
+    // merge
+    int32_t* best = nullptr;           // [N]
+    double* best_dS = nullptr;         // [N]
+    double* heap_dS = nullptr;         // [N]
+    int32_t* heap_blk = nullptr;       // [N]
+    int32_t* parent = nullptr;         // [N]
+    int32_t* root = nullptr;           // [N]
+    int32_t* used = nullptr;           // [N]
+    DevFlags* flags_dev = nullptr;
+};
+
+int ceil_log2(uint64_t x);
+
+// ---- blockmodel.cu
+// Blockmodel::initialize_edge_counts: rebuilds degrees, sizes and the sorted CSR / CSC
+// of the blockmatrix from bm.asg.  Updates bm.nnz (read back to the host).
+void rebuild(const DevGraph& g, DevBM& bm, Work& w, cudaStream_t st);
+// Sum of v * canonical_log(v / (d_out * d_in)) in units of 2^-24 into w.d_acc[0].
+void launch_mdl(const DevGraph& g, const DevBM& bm, Work& w, cudaStream_t st);
+void launch_vertex_dS_batch(const DevGraph& g, const DevBM& bm, const int32_t* v, const int32_t* s, int64_t n,
+                            int32_t max_k, long long* out, Work& w, cudaStream_t st);
+void launch_merge_dS_batch(const DevGraph& g, const DevBM& bm, const int32_t* r, const int32_t* s, int64_t n,
+                           long long* out, Work& w, cudaStream_t st);
+void launch_propose_batch(const DevGraph& g, const DevBM& bm, const int32_t* v, int64_t n, uint64_t seed,
+                          uint32_t c1, uint32_t c2, uint32_t c3, int32_t* out, cudaStream_t st);
+// Initialises the chain cell store from the current CSR (capacity for extra new keys).
+void chain_init(const DevBM& bm, Work& w, uint64_t extra_keys, cudaStream_t st);
+
+// ---- sweep.cu
+// Proposals for vlist[0..n) against the current snapshot (moves[v] = s or -1), then the
+// vertex-id-order apply with the block-size-1 rule; asg updated (no rebuild).
+void gibbs_propose(const DevGraph& g, const DevBM& bm, const int32_t* vlist, int32_t n, int32_t small_k,
+                   uint64_t seed, uint32_t iter, uint32_t step, int greedy, Work& w, cudaStream_t st);
+void gibbs_apply(const DevBM& bm, const int32_t* vlist, int32_t n, Work& w, cudaStream_t st);
+void mh_chain(const DevGraph& g, DevBM& bm, const int32_t* order, int32_t n, int32_t max_k, uint64_t seed,
+              uint32_t iter, uint32_t step, int greedy, Work& w, cudaStream_t st);
+// order[i] = base[perm(i)] with the canonical shuffle keyed by (i, iter, step, dom).
+void shuffle(const int32_t* base, int32_t n, uint64_t seed, uint32_t iter, uint32_t step, uint32_t dom,
+             int32_t* order, Work& w, cudaStream_t st);
+
+// ---- merge.cu
+void merge_propose(const DevGraph& g, const DevBM& bm, uint64_t seed, uint32_t step, Work& w, cudaStream_t st);
+// Carries out merges; writes the number done to w.d_scalar[1].  Leaves asg relabelled
+// to dense block ids (B - merges blocks); the caller rebuilds.
+void carry_out(const DevGraph& g, DevBM& bm, int64_t num_to_merge, int approximate, Work& w, cudaStream_t st);
+
+// Launch accounting.
+int64_t kernel_launches();
+void count_launches(int64_t n);
+
+}  // namespace sbp

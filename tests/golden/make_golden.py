@@ -1,0 +1,86 @@
+"""Extract the reference's known-answer fixtures into tests/golden/toy_example.json.
+
+Run in a container that has the reference checkout (read-only) mounted:
+
+    python tests/golden/make_golden.py /path/to/SBP
+
+The script reads the reference's own gtest sources as text (it executes nothing
+from them) and records:
+  * the 11-vertex / 23-edge toy graph and its assignments
+    (test/toy_example.hpp:43-73, 130-132, 163, 181-184),
+  * the known answers the reference's tests assert
+    (test/entropy_test.cpp, test/blockmodel_test.cpp, test/finetune_test.cpp,
+     test/block_merge_test.cpp).
+The JSON is committed; the tests never read the reference at run time.
+"""
+import json
+import os
+import re
+import sys
+
+
+def read(root, rel):
+    with open(os.path.join(root, rel)) as f:
+        return f.read()
+
+
+def ints(text):
+    return [int(x) for x in re.findall(r"-?\d+", text)]
+
+
+def main(root):
+    toy = read(root, "test/toy_example.hpp")
+    edges_block = re.search(r"std::vector<std::vector<long>> edges \{(.*?)\};", toy, re.S).group(1)
+    edges = [ints(m) for m in re.findall(r"\{([^{}]*)\}", edges_block)]
+    assignment = ints(re.search(r"\bassignment = \{([^}]*)\};", toy).group(1))
+    entropy = float(re.search(r"const double ENTROPY = ([0-9.]+);", toy).group(1))
+    merge_assignment = ints(re.search(r"assignment2 = \{([^}]*)\};", toy).group(1))
+    complex_assignment = ints(re.search(r"ComplexToySetUp.*?assignment = \{([^}]*)\};", toy, re.S).group(1))
+
+    bm_test = read(root, "test/blockmodel_test.cpp")
+    deg = {}
+    for kind, blk, val in re.findall(r"EXPECT_EQ\(B\.degrees(_out|_in|)\((\d)\), (\d+)\);", bm_test):
+        deg.setdefault(kind or "_tot", {})[int(blk)] = int(val)
+
+    ft = read(root, "test/finetune_test.cpp")
+    body = re.search(r"TEST_F\(FinetuneTest, BlockmodelDeltasAreCorrect\)(.*?)\n}", ft, re.S).group(1)
+    vdelta = {f"{a},{b}": int(c) for a, b, c in re.findall(r"delta\.get\((\d),(\d)\), (-?\d+)\)", body)}
+    vdelta_size = int(re.search(r"entries\(\)\.size\(\), (\d+)\)", body).group(1))
+    body = re.search(r"TEST_F\(FinetuneTest, SpecialCaseBlockmodelDeltasAreCorrect\)(.*?)\n}", ft, re.S).group(1)
+    sdelta = {f"{a},{b}": int(c) for a, b, c in re.findall(r"delta\.get\((\d),(\d)\), (-?\d+)\)", body)}
+
+    bmt = read(root, "test/block_merge_test.cpp")
+    mdelta = {f"{a},{b}": int(c) for a, b, c in re.findall(r"delta\.get\((\d),(\d)\), (-?\d+)\)", bmt)}
+    mdelta_size = int(re.search(r"entries\(\)\.size\(\), (\d+)\)", bmt).group(1))
+
+    et = read(root, "test/entropy_test.cpp")
+    null_mdl = float(re.search(r"hand_calculated_mdl = ([0-9.E+e]+);", et).group(1))
+    big_E = float(re.search(r"const long E = ([0-9.E+e]+);", et).group(1))
+
+    out = {
+        "source": "vtsynergy/SBP test/toy_example.hpp, test/*_test.cpp",
+        "num_vertices": 11,
+        "edges": edges,
+        "assignment": assignment,
+        "num_blocks": 3,
+        "mdl": entropy,
+        "mdl_tolerance": "EXPECT_FLOAT_EQ (4 float ULPs)",
+        "block_degrees_out": [deg["_out"][i] for i in range(3)],
+        "block_degrees_in": [deg["_in"][i] for i in range(3)],
+        "block_degrees": [deg["_tot"][i] for i in range(3)],
+        "vertex_move": {"vertex": 7, "proposal": 0, "delta": vdelta, "delta_entries": vdelta_size,
+                        "after_assignment": [0, 0, 0, 0, 1, 1, 1, 0, 2, 2, 2]},
+        "special_case": {"num_blocks": 6, "assignment": complex_assignment, "vertex": 6, "proposal": 0,
+                         "delta": sdelta},
+        "block_merge": {"block": 0, "proposal": 1, "delta": mdelta, "delta_entries": mdelta_size,
+                        "after_assignment": merge_assignment},
+        "null_mdl_v1": {"num_edges": big_E, "value": null_mdl},
+    }
+    dst = os.path.join(os.path.dirname(os.path.abspath(__file__)), "toy_example.json")
+    with open(dst, "w") as f:
+        json.dump(out, f, indent=1)
+    print("wrote", dst)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

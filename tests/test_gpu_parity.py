@@ -1,0 +1,221 @@
+"""GPU parity: every device result is compared with the CPU oracle on the same seeded
+inputs.  Integer state (assignments, block degrees, sizes, block-edge counts) and
+accept/reject decisions must be bit-exact; delta-MDL values are exact multiples of
+2^-24 on both sides and must be identical (tolerance 0); the whole-blockmodel MDL
+must match the oracle's canonical value within 1e-12 relative and the reference's
+literal float-log value within 1e-9 relative."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+MDL_REL_TOL_CANONICAL = 1e-12
+MDL_REL_TOL_LITERAL = 1e-9
+DELTA_REL_TOL = 1e-10  # spec tolerance; the implementation is exact (0)
+
+
+def same_state(gb, ob):
+    d, o = gb.read(), ob.read()
+    for k in ("assignment", "d_out", "d_in", "d_tot", "sizes", "rows", "cols", "counts"):
+        assert np.array_equal(np.asarray(d[k], np.int64), np.asarray(o[k], np.int64)), k
+
+
+def make_pair(gpu, oracle, n, e, blocks, B, seed, assignment=None):
+    src, dst, planted = gpu.dcsbm.generate(n, e, blocks, seed=seed)
+    rng = np.random.default_rng(seed)
+    a = rng.integers(0, B, n).astype(np.int32) if assignment is None else np.asarray(assignment, np.int32)
+    if assignment is None:
+        a[:B] = np.arange(B)  # every block non-empty
+    G = gpu.Graph(n, src, dst)
+    O = oracle.Graph(n, src, dst)
+    return G, O, gpu.Blockmodel(B, G, 0.5, a), oracle.Blockmodel(O, B, a), a, planted
+
+
+def toy_pair(gpu, oracle, golden, assignment=None, B=None):
+    e = np.array(golden["edges"], np.int32)
+    G = gpu.Graph(11, e[:, 0], e[:, 1])
+    O = oracle.Graph(11, e[:, 0], e[:, 1])
+    a = golden["assignment"] if assignment is None else assignment
+    B = golden["num_blocks"] if B is None else B
+    return G, O, gpu.Blockmodel(B, G, 0.5, a), oracle.Blockmodel(O, B, a)
+
+
+def test_toy_known_answers_on_gpu(gpu, oracle, golden):
+    G, O, gb, ob = toy_pair(gpu, oracle, golden)
+    same_state(gb, ob)
+    d = gb.read()
+    assert d["d_out"].tolist() == golden["block_degrees_out"]
+    assert d["d_in"].tolist() == golden["block_degrees_in"]
+    assert d["d_tot"].tolist() == golden["block_degrees"]
+    mdl = gpu.entropy.mdl(gb)
+    assert abs(np.float32(mdl) - np.float32(golden["mdl"])) <= 4 * np.spacing(np.float32(golden["mdl"]))
+    mv = golden["vertex_move"]
+    dS = gpu.entropy.delta_mdl(gb, [mv["vertex"]], [mv["proposal"]])[0]
+    assert dS == ob.delta_mdl(mv["vertex"], mv["proposal"])[0]
+    sc = golden["special_case"]
+    G2, O2, gb3, ob3 = toy_pair(gpu, oracle, golden, sc["assignment"], sc["num_blocks"])
+    assert gpu.entropy.delta_mdl(gb3, [sc["vertex"]], [sc["proposal"]])[0] == ob3.delta_mdl(sc["vertex"],
+                                                                                           sc["proposal"])[0]
+    bm = golden["block_merge"]
+    assert gpu.entropy.block_merge_delta_mdl(gb, [bm["block"]], [bm["proposal"]])[0] == \
+        ob.merge_delta_mdl(bm["block"], bm["proposal"])[0]
+
+
+@pytest.mark.parametrize("B", [2, 7, 40, 300])
+def test_build_and_mdl(gpu, oracle, B):
+    G, O, gb, ob, a, _ = make_pair(gpu, oracle, 1200, 15000, 9, B, seed=B)
+    same_state(gb, ob)
+    lit, can = ob.mdl()
+    m = gpu.entropy.mdl(gb)
+    assert abs(m - can) <= MDL_REL_TOL_CANONICAL * abs(can)
+    assert abs(m - lit) <= MDL_REL_TOL_LITERAL * abs(lit)
+
+
+@pytest.mark.parametrize("B", [3, 25, 400])
+def test_delta_mdl_batch_exact(gpu, oracle, B):
+    G, O, gb, ob, a, _ = make_pair(gpu, oracle, 1500, 20000, 9, B, seed=10 + B)
+    rng = np.random.default_rng(B)
+    v = rng.integers(0, 1500, 3000).astype(np.int32)
+    s = rng.integers(0, B, 3000).astype(np.int32)
+    got = gpu.entropy.delta_mdl(gb, v, s)
+    for i in range(v.size):
+        lit, fx = ob.delta_mdl(int(v[i]), int(s[i]))
+        assert got[i] == fx / 2**24, (i, v[i], s[i])
+        assert abs(got[i] - lit) <= DELTA_REL_TOL * max(1.0, abs(lit))
+
+
+def test_delta_mdl_high_degree_and_self_loops(gpu, oracle):
+    # hubs (k > 128 takes the CTA path) and vertices with a self-loop
+    n = 800
+    rng = np.random.default_rng(5)
+    src = list(rng.integers(0, n, 12000))
+    dst = list(rng.integers(0, n, 12000))
+    for hub in range(5):
+        src += [hub] * 600 + list(rng.integers(0, n, 300))
+        dst += list(rng.integers(0, n, 600)) + [hub] * 300
+    for v in range(0, n, 7):
+        src.append(v)
+        dst.append(v)
+    src, dst = np.array(src, np.int32), np.array(dst, np.int32)
+    B = 20
+    a = rng.integers(0, B, n).astype(np.int32)
+    a[:B] = np.arange(B)
+    G, O = gpu.Graph(n, src, dst), oracle.Graph(n, src, dst)
+    gb, ob = gpu.Blockmodel(B, G, 0.5, a), oracle.Blockmodel(O, B, a)
+    vs = np.concatenate([np.arange(5), np.arange(0, n, 7)]).astype(np.int32)
+    ss = rng.integers(0, B, vs.size).astype(np.int32)
+    got = gpu.entropy.delta_mdl(gb, vs, ss)
+    for i in range(vs.size):
+        assert got[i] == ob.delta_mdl(int(vs[i]), int(ss[i]))[1] / 2**24
+
+
+@pytest.mark.parametrize("B", [4, 60, 500])
+def test_merge_delta_mdl_exact(gpu, oracle, B):
+    G, O, gb, ob, a, _ = make_pair(gpu, oracle, 1500, 20000, 9, B, seed=20 + B)
+    rng = np.random.default_rng(B)
+    r = rng.integers(0, B, 2000).astype(np.int32)
+    s = rng.integers(0, B, 2000).astype(np.int32)
+    keep = r != s
+    r, s = r[keep], s[keep]
+    got = gpu.entropy.block_merge_delta_mdl(gb, r, s)
+    for i in range(r.size):
+        assert got[i] == ob.merge_delta_mdl(int(r[i]), int(s[i]))[1] / 2**24
+
+
+@pytest.mark.parametrize("B", [5, 80, 700])
+def test_proposals_identical(gpu, oracle, B):
+    G, O, gb, ob, a, _ = make_pair(gpu, oracle, 2000, 25000, 9, B, seed=30 + B)
+    v = np.arange(2000, dtype=np.int32)
+    for c1 in range(3):
+        got = gpu.finetune.propose_new_blocks(gb, v, seed=99, c1=c1, c2=4, c3=1)
+        want = [ob.propose_vertex(int(x), 99, c1, 4, 1) for x in v]
+        assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("B", [6, 50, 900])
+def test_gibbs_batch_identical(gpu, oracle, B):
+    G, O, gb, ob, a, _ = make_pair(gpu, oracle, 2500, 30000, 9, B, seed=40 + B)
+    cfg = oracle.make_config("async_gibbs")
+    verts = np.arange(2500, dtype=np.int32)
+    for it in range(3):
+        mv_g, app_g = gpu.finetune.gibbs_batch(gb, verts, seed=5, iteration=it, step=2)
+        n_o, mv_o, _ = ob.gibbs_batch(verts, 5, it, 2, cfg)
+        assert np.array_equal(mv_g, mv_o)
+        assert app_g == n_o
+        same_state(gb, ob)
+
+
+def test_gibbs_apply_size_one_rule(gpu, oracle):
+    """Many singleton blocks whose only vertex wants to leave: exercises the exact
+    vertex-id-order refusal rule (blockmodel.cpp:437-443) including chains."""
+    n = 3000
+    G, O, gb, ob, a, _ = make_pair(gpu, oracle, n, 24000, 9, 2000, seed=77)
+    cfg = oracle.make_config("async_gibbs")
+    verts = np.arange(n, dtype=np.int32)
+    for it in range(4):
+        mv_g, app_g = gpu.finetune.gibbs_batch(gb, verts, seed=3, iteration=it, step=0)
+        n_o, mv_o, _ = ob.gibbs_batch(verts, 3, it, 0, cfg)
+        assert app_g == n_o
+        same_state(gb, ob)
+
+
+@pytest.mark.parametrize("B", [8, 120, 1500])
+def test_mh_chain_identical(gpu, oracle, B):
+    G, O, gb, ob, a, _ = make_pair(gpu, oracle, 2500, 30000, 9, B, seed=50 + B)
+    order = np.random.default_rng(B).permutation(2500)[:600].astype(np.int32)
+    applied = gpu.finetune.mh_chain(gb, order, seed=8, iteration=1, step=3)
+    want = ob.mh_chain(order, 8, 1, 3, oracle.make_config("hybrid_mcmc"))
+    assert applied == want
+    same_state(gb, ob)
+
+
+@pytest.mark.parametrize("alg", ["async_gibbs", "hybrid_mcmc", "metropolis_hastings"])
+def test_mcmc_identical(gpu, oracle, alg):
+    G, O, gb, ob, a, _ = make_pair(gpu, oracle, 2000, 24000, 9, 150, seed=60)
+    args = gpu.Args(algorithm=alg, seed=13, max_iterations=6)
+    gpu.finetune.mcmc(2, G, gb, True, args)
+    cfg = oracle.make_config(alg, max_iterations=6)
+    ob.mcmc(cfg, seed=13, step=2, golden_ratio_not_reached=True)
+    same_state(gb, ob)
+    assert abs(gb.getOverall_entropy() - ob.mdl()[1]) <= MDL_REL_TOL_CANONICAL * abs(ob.mdl()[1])
+
+
+@pytest.mark.parametrize("B,approx", [(3000, False), (400, False), (60, False), (400, True)])
+def test_merge_blocks_identical(gpu, oracle, B, approx):
+    G, O, gb, ob, a, _ = make_pair(gpu, oracle, 3000, 36000, 9, B, seed=70 + B,
+                                   assignment=None if B < 3000 else np.arange(3000))
+    args = gpu.Args(seed=21, approximate=approx)
+    n = B // 2
+    gpu.block_merge.merge_blocks(gb, G, args=args, step=5, num_blocks_to_merge=n)
+    ob.merge_blocks(oracle.make_config(approximate=approx), seed=21, step=5, num_to_merge=n)
+    assert gb.num_blocks() == B - n == ob.num_blocks
+    same_state(gb, ob)
+
+
+def test_merge_proposals_identical(gpu, oracle):
+    G, O, gb, ob, a, _ = make_pair(gpu, oracle, 2000, 24000, 9, 2000, seed=90, assignment=np.arange(2000))
+    best, dS = gpu.block_merge.merge_proposals(gb, seed=4, step=1)
+    for r in range(0, 2000, 13):
+        props = []
+        vals = []
+        for i in range(10):
+            s = ob.propose_merge(r, 4, 1, i)
+            if s in props:
+                continue
+            props.append(s)
+            vals.append(ob.merge_delta_mdl(r, s)[1] / 2**24)
+        j = int(np.argmin(vals))
+        assert best[r] == props[j] and dS[r] == vals[j]
+
+
+@pytest.mark.parametrize("alg", ["hybrid_mcmc", "async_gibbs"])
+def test_full_sbp_identical_c1(gpu, oracle, alg):
+    src, dst, planted = gpu.dcsbm.generate_config("C1", seed=0)
+    G = gpu.Graph(1000, src, dst)
+    O = oracle.Graph(1000, src, dst)
+    asg, B, mdl, st = gpu.sbp.stochastic_block_partition(G, gpu.Args(algorithm=alg, seed=1))
+    oasg, oB, omdl, ost = oracle.sbp(O, oracle.make_config(alg), seed=1)
+    assert B == oB
+    assert np.array_equal(asg, oasg)
+    assert abs(mdl - omdl) <= MDL_REL_TOL_CANONICAL * abs(omdl)
+    assert st["merges"] == ost.merges and st["mcmc_iterations"] == ost.mcmc_iterations

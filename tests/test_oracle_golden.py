@@ -1,0 +1,202 @@
+"""Pins the CPU oracle to the reference's own known answers (test/toy_example.hpp and
+test/*_test.cpp, extracted into tests/golden/toy_example.json) and checks its internal
+identities.  CPU only."""
+import math
+
+import numpy as np
+import pytest
+
+
+def toy(oracle, golden, assignment=None, num_blocks=None):
+    edges = np.array(golden["edges"], dtype=np.int32)
+    g = oracle.Graph(golden["num_vertices"], edges[:, 0], edges[:, 1])
+    a = golden["assignment"] if assignment is None else assignment
+    B = golden["num_blocks"] if num_blocks is None else num_blocks
+    return g, oracle.Blockmodel(g, B, a)
+
+
+def float_eq(a, b, ulps=4):
+    # gtest EXPECT_FLOAT_EQ: within 4 ULPs in single precision
+    return abs(np.float32(a) - np.float32(b)) <= ulps * np.spacing(np.float32(max(abs(a), abs(b))))
+
+
+def test_philox_known_answers(oracle):
+    # Random123 known-answer vectors for Philox4x32-10.
+    assert oracle.philox([0, 0, 0, 0], [0, 0]).tolist() == [0x6627e8d5, 0xe169c58d, 0xbc57ac4c, 0x9b00dbd8]
+    assert oracle.philox([0xffffffff] * 4, [0xffffffff] * 2).tolist() == [0x408f276d, 0x41c83b0e, 0xa20bc7c6,
+                                                                          0x6d5451fd]
+    assert oracle.philox([0x243f6a88, 0x85a308d3, 0x13198a2e, 0x03707344],
+                         [0xa4093822, 0x299f31d0]).tolist() == [0xd16cfe09, 0x94fdcceb, 0x5001e420, 0x24126ea1]
+
+
+def test_toy_mdl(oracle, golden):
+    # entropy_test.cpp:59-62
+    _, B = toy(oracle, golden)
+    lit, can = B.mdl()
+    assert float_eq(lit, golden["mdl"])
+    assert abs(lit - can) <= 1e-12 * abs(lit)
+
+
+def test_toy_block_degrees(oracle, golden):
+    # blockmodel_test.cpp:25-35
+    _, B = toy(oracle, golden)
+    d = B.read()
+    assert d["d_out"].tolist() == golden["block_degrees_out"]
+    assert d["d_in"].tolist() == golden["block_degrees_in"]
+    assert d["d_tot"].tolist() == golden["block_degrees"]
+
+
+def test_toy_vertex_delta(oracle, golden):
+    # finetune_test.cpp:88-103: six entries, (0,1) and (2,1) absent
+    _, B = toy(oracle, golden)
+    mv = golden["vertex_move"]
+    d = B.vertex_delta(mv["vertex"], mv["proposal"])
+    assert len(d) == mv["delta_entries"]
+    for key, val in mv["delta"].items():
+        r, c = map(int, key.split(","))
+        assert d.get((r, c), 0) == val
+
+
+def test_toy_delta_sums_to_zero(oracle, golden):
+    # finetune_test.cpp:106-127 (vertex 10 has a self edge)
+    _, B = toy(oracle, golden)
+    for v in (7, 10):
+        assert sum(B.vertex_delta(v, 0).values()) == 0
+
+
+def test_toy_delta_mdl_equals_mdl_difference(oracle, golden):
+    # entropy_test.cpp:95-107
+    g, B = toy(oracle, golden)
+    mv = golden["vertex_move"]
+    lit, fx = B.delta_mdl(mv["vertex"], mv["proposal"])
+    assert lit == fx / 2**24
+    after = oracle.Blockmodel(g, 3, mv["after_assignment"])
+    assert float_eq(lit, after.mdl()[0] - B.mdl()[0])
+
+
+def test_toy_special_case(oracle, golden):
+    # finetune_test.cpp:226-239 and entropy_test.cpp:161-186
+    sc = golden["special_case"]
+    g, B3 = toy(oracle, golden, sc["assignment"], sc["num_blocks"])
+    d = B3.vertex_delta(sc["vertex"], sc["proposal"])
+    assert len(d) == 6
+    for key, val in sc["delta"].items():
+        r, c = map(int, key.split(","))
+        assert d[(r, c)] == val
+    lit, fx = B3.delta_mdl(sc["vertex"], sc["proposal"])
+    a2 = list(sc["assignment"])
+    a2[sc["vertex"]] = sc["proposal"]
+    B5 = oracle.Blockmodel(g, sc["num_blocks"], a2)
+    assert float_eq(lit, B5.mdl()[0] - B3.mdl()[0])
+
+
+def test_toy_block_merge(oracle, golden):
+    # block_merge_test.cpp:11-21 and entropy_test.cpp:250-263
+    g, B = toy(oracle, golden)
+    bm = golden["block_merge"]
+    d = B.merge_delta(bm["block"], bm["proposal"])
+    assert len(d) == bm["delta_entries"]
+    for key, val in bm["delta"].items():
+        r, c = map(int, key.split(","))
+        assert d.get((r, c), 0) == val
+    lit, fx = B.merge_delta_mdl(bm["block"], bm["proposal"])
+    assert lit == fx / 2**24
+    B2 = oracle.Blockmodel(g, 3, bm["after_assignment"])
+    assert float_eq(lit, B2.mdl()[0] - B.mdl()[0])
+
+
+def test_null_mdl(oracle, golden):
+    # entropy_test.cpp:198-217
+    nm = golden["null_mdl_v1"]
+    assert float_eq(oracle.null_mdl_v1(nm["num_edges"]), nm["value"])
+
+
+def test_literal_equals_fixed_on_random_moves(oracle):
+    from sbp_gb300 import dcsbm
+    src, dst, planted = dcsbm.generate(600, 6000, 8, seed=3)
+    g = oracle.Graph(600, src, dst)
+    rng = np.random.default_rng(0)
+    B = oracle.Blockmodel(g, 30, rng.integers(0, 30, 600))
+    for _ in range(300):
+        v, s = int(rng.integers(600)), int(rng.integers(30))
+        lit, fx = B.delta_mdl(v, s)
+        assert lit == fx / 2**24  # exact: every term is a multiple of 2^-24
+    for _ in range(100):
+        r, s = rng.choice(30, 2, replace=False)
+        lit, fx = B.merge_delta_mdl(int(r), int(s))
+        assert lit == fx / 2**24
+
+
+def test_delta_mdl_tracks_mdl(oracle):
+    """dS from the table form matches the change of the full MDL (ratio-form logs) up to
+    the float-log rounding the reference itself has (hazard H4)."""
+    from sbp_gb300 import dcsbm
+    src, dst, _ = dcsbm.generate(400, 4000, 6, seed=4)
+    g = oracle.Graph(400, src, dst)
+    rng = np.random.default_rng(1)
+    a = rng.integers(0, 12, 400)
+    B = oracle.Blockmodel(g, 12, a)
+    base = B.mdl()[0]
+    for _ in range(40):
+        v, s = int(rng.integers(400)), int(rng.integers(12))
+        if s == a[v]:
+            continue
+        a2 = a.copy()
+        a2[v] = s
+        if np.bincount(a2, minlength=12).min() == 0:
+            continue
+        lit, _ = B.delta_mdl(v, s)
+        after = oracle.Blockmodel(g, 12, a2).mdl()[0]
+        assert abs(lit - (after - base)) <= 1e-4 * abs(base)
+
+
+def test_sampler_matches_reference_distribution(oracle):
+    """The canonical draw -> block mapping of propose_new_block gives the reference's
+    distribution: P(s) = sum over neighbours u of 1/k * W_{b(u)}[s] / sum(W_{b(u)})."""
+    from sbp_gb300 import dcsbm
+    src, dst, _ = dcsbm.generate(200, 2400, 5, seed=5)
+    g = oracle.Graph(200, src, dst)
+    rng = np.random.default_rng(2)
+    a = rng.integers(0, 8, 200)
+    B = oracle.Blockmodel(g, 8, a)
+    M = np.zeros((8, 8))
+    np.add.at(M, (a[src], a[dst]), 1)
+    v = int(np.argmax(np.bincount(src, minlength=200) + np.bincount(dst, minlength=200)))
+    nbrs = list(dst[src == v]) + [u for u in src[dst == v] if u != v]
+    expect = np.zeros(8)
+    for u in nbrs:
+        nb = a[u]
+        W = M[nb, :] + M[:, nb]
+        W[nb] -= M[nb, nb]
+        expect += W / W.sum() / len(nbrs)
+    n = 20000
+    got = np.bincount([B.propose_vertex(v, 7, i, 0, 1) for i in range(n)], minlength=8)
+    chi2 = ((got - n * expect) ** 2 / np.maximum(n * expect, 1e-9))[expect > 0].sum()
+    assert chi2 < 40  # 7 degrees of freedom; p ~ 1e-6
+    assert got[expect == 0].sum() == 0
+
+
+def test_gibbs_apply_equals_rebuild(oracle):
+    """Applying accepted moves in vertex order (serial loop) leaves the blockmodel equal to
+    a rebuild from the final assignment."""
+    from sbp_gb300 import dcsbm
+    src, dst, _ = dcsbm.generate(500, 5000, 6, seed=6)
+    g = oracle.Graph(500, src, dst)
+    rng = np.random.default_rng(3)
+    B = oracle.Blockmodel(g, 40, rng.integers(0, 40, 500))
+    cfg = oracle.make_config("async_gibbs")
+    n, moves, _ = B.gibbs_batch(np.arange(500), seed=11, iteration=0, step=0, cfg=cfg)
+    d = B.read()
+    R = oracle.Blockmodel(g, 40, d["assignment"]).read()
+    for k in ("d_out", "d_in", "d_tot", "sizes", "rows", "cols", "counts"):
+        assert np.array_equal(d[k], R[k]), k
+
+
+def test_oracle_sbp_recovers_planted_blocks(oracle):
+    from sbp_gb300 import dcsbm, evaluate
+    src, dst, planted = dcsbm.generate_config("C1", seed=0)
+    g = oracle.Graph(1000, src, dst)
+    asg, B, mdl, st = oracle.sbp(g, oracle.make_config("hybrid_mcmc"), seed=1)
+    assert B > 1
+    assert evaluate.nmi(planted, asg) > 0.6
+    assert mdl < oracle.Blockmodel(g, 1, np.zeros(1000, np.int32)).mdl()[0]
