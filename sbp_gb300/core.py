@@ -5,8 +5,10 @@ Names, argument meaning and error behaviour follow vtsynergy/SBP
 lives on the GPU behind the libsbpgpu C ABI.  Invalid arguments raise ValueError /
 IndexError like the reference's std::invalid_argument / IndexOutOfBoundsException.
 """
+import atexit
 import ctypes
 import dataclasses
+import weakref
 
 import numpy as np
 
@@ -53,9 +55,13 @@ class Context:
         if st != 0:
             raise _lib.SbpGpuError(st, "cannot create a CUDA context on device %d" % device)
         self.h = h
+        self._graphs = weakref.WeakSet()
 
     def close(self):
+        """Destroys the context after every graph (and blockmodel) created on it."""
         if getattr(self, "h", None):
+            for g in list(self._graphs):
+                g.close()
             self.lib.sbpgpu_ctx_destroy(self.h)
             self.h = None
 
@@ -86,6 +92,15 @@ def default_context():
     return _default_ctx
 
 
+@atexit.register
+def _close_default_context():
+    # Tear device state down while the CUDA runtime is still alive, children first.
+    global _default_ctx
+    if _default_ctx is not None:
+        _default_ctx.close()
+        _default_ctx = None
+
+
 def _p(a, t):
     return a.ctypes.data_as(t)
 
@@ -107,9 +122,15 @@ class Graph:
         self.ctx.check(self.ctx.lib.sbpgpu_graph_create(self.ctx.h, self._N, int(self.src.size),
                                                         _p(self.src, i32p), _p(self.dst, i32p), ctypes.byref(h)))
         self.h = h
+        self._bms = weakref.WeakSet()
+        self.ctx._graphs.add(self)
 
     def close(self):
+        """Destroys the graph after every blockmodel built on it (finalisers may run in any
+        order when objects are collected together)."""
         if getattr(self, "h", None):
+            for bm in list(self._bms):
+                bm.close()
             self.ctx.lib.sbpgpu_graph_destroy(self.h)
             self.h = None
 
@@ -138,6 +159,7 @@ class Blockmodel:
         self.num_blocks_to_merge = 0
         if _handle is not None:
             self.h = _handle
+            graph._bms.add(self)
             return
         h = ctypes.c_void_p()
         if assignment is None:
@@ -153,6 +175,7 @@ class Blockmodel:
             ptr = _p(a, i32p)
         self.ctx.check(self.ctx.lib.sbpgpu_bm_create(graph.h, int(num_blocks), ptr, ctypes.byref(h)))
         self.h = h
+        graph._bms.add(self)
         self.num_blocks_to_merge = int(num_blocks * block_reduction_rate)
 
     def close(self):

@@ -265,6 +265,8 @@ void chain_init(const DevBM& bm, Work& w, uint64_t extra_keys, cudaStream_t st) 
     w.chain.pool_cap = w.pool_cap;
     w.chain.pool_used = w.d_scalar + 5;
     k_fill_u64<<<grid_for((int64_t)cap), kT, 0, st>>>(w.chain_keys, cap, kEmptyKey);
+    // A key inserted later starts from zero; stale counts of earlier phases must not leak.
+    cudaMemsetAsync(w.chain_vals, 0, sizeof(int32_t) * cap, st);
     cudaMemsetAsync(w.d_scalar + 4, 0, 2 * sizeof(int32_t), st);
     cudaMemsetAsync(w.row_head, 0xff, sizeof(int32_t) * bm.B, st);
     cudaMemsetAsync(w.col_head, 0xff, sizeof(int32_t) * bm.B, st);

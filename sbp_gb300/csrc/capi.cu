@@ -77,6 +77,8 @@ struct TimedSpan {
 
 struct sbpgpu_ctx {
     int device = 0;
+    int refs = 0;          // live graphs
+    bool dead = false;     // destroy requested
     cudaStream_t stream = nullptr;
     std::string err;
     bool timing = false;
@@ -136,6 +138,8 @@ struct Span {
 
 struct sbpgpu_graph {
     sbpgpu_ctx* ctx = nullptr;
+    int refs = 0;          // live blockmodels
+    bool dead = false;     // destroy requested
     int64_t N = 0, E = 0;
     DevGraph dg{};
     std::vector<void*> owned;
@@ -566,6 +570,32 @@ void free_all(std::vector<void*>& owned) {
     owned.clear();
 }
 
+// Destruction is reference counted so that handles may be destroyed in any order: a
+// graph is freed once it was destroyed and its last blockmodel is gone, a context once
+// it was destroyed and its last graph is gone.
+void release_ctx(sbpgpu_ctx* ctx) {
+    if (!ctx->dead || ctx->refs > 0) return;
+    cudaStreamSynchronize(ctx->stream);
+    for (auto& s : ctx->pending) {
+        cudaEventDestroy(s.a);
+        cudaEventDestroy(s.b);
+    }
+    for (auto e : ctx->free_events) cudaEventDestroy(e);
+    cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+void release_graph(sbpgpu_graph* g) {
+    if (!g->dead || g->refs > 0) return;
+    sbpgpu_ctx* ctx = g->ctx;
+    cudaStreamSynchronize(ctx->stream);
+    free_all(g->owned);
+    if (g->flags_host) cudaFreeHost(g->flags_host);
+    delete g;
+    ctx->refs--;
+    release_ctx(ctx);
+}
+
 }  // namespace
 
 // ====================================================================== C ABI
@@ -599,15 +629,9 @@ sbpgpu_status sbpgpu_ctx_create(int32_t device, sbpgpu_ctx** out) {
 }
 
 void sbpgpu_ctx_destroy(sbpgpu_ctx* ctx) {
-    if (!ctx) return;
-    cudaStreamSynchronize(ctx->stream);
-    for (auto& s : ctx->pending) {
-        cudaEventDestroy(s.a);
-        cudaEventDestroy(s.b);
-    }
-    for (auto e : ctx->free_events) cudaEventDestroy(e);
-    cudaStreamDestroy(ctx->stream);
-    delete ctx;
+    if (!ctx || ctx->dead) return;
+    ctx->dead = true;
+    release_ctx(ctx);
 }
 
 const char* sbpgpu_last_error(const sbpgpu_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
@@ -642,6 +666,7 @@ sbpgpu_status sbpgpu_graph_create(sbpgpu_ctx* ctx, int64_t N, int64_t E, const i
         delete g;
         return rc;
     }
+    ctx->refs++;
     *out = g;
     return SBPGPU_OK;
 }
@@ -662,11 +687,9 @@ sbpgpu_status sbpgpu_graph_create_device(sbpgpu_ctx* ctx, int64_t N, int64_t E, 
 }
 
 void sbpgpu_graph_destroy(sbpgpu_graph* g) {
-    if (!g) return;
-    cudaStreamSynchronize(g->ctx->stream);
-    free_all(g->owned);
-    if (g->flags_host) cudaFreeHost(g->flags_host);
-    delete g;
+    if (!g || g->dead) return;
+    g->dead = true;
+    release_graph(g);
 }
 
 int64_t sbpgpu_graph_num_vertices(const sbpgpu_graph* g) { return g ? g->N : 0; }
@@ -701,6 +724,7 @@ sbpgpu_status sbpgpu_bm_create(sbpgpu_graph* g, int64_t B, const int32_t* assign
         }
         return rc;
     }
+    g->refs++;
     *out = bm;
     return SBPGPU_OK;
 }
@@ -742,15 +766,19 @@ sbpgpu_status sbpgpu_bm_copy(const sbpgpu_bm* src, sbpgpu_bm** out) {
         }
         return rc;
     }
+    g->refs++;
     *out = bm;
     return SBPGPU_OK;
 }
 
 void sbpgpu_bm_destroy(sbpgpu_bm* bm) {
     if (!bm) return;
-    cudaStreamSynchronize(bm->g->ctx->stream);
+    sbpgpu_graph* g = bm->g;
+    cudaStreamSynchronize(g->ctx->stream);
     free_all(bm->owned);
     delete bm;
+    g->refs--;
+    release_graph(g);
 }
 
 int64_t sbpgpu_bm_num_blocks(const sbpgpu_bm* bm) { return bm ? bm->d.B : 0; }
