@@ -1,0 +1,299 @@
+"""Benchmark: full SBP (golden-section search, block merges, hybrid MCMC) on the 50k-vertex,
+1M-edge directed DCSBM graph, on one GB300 per rank.
+
+Default (N=1): one JSON line with proposals/s (vertex + merge proposals evaluated per
+second of full-SBP device time), the full-SBP wall time per step, the roofline of the
+dominant kernel, the end-to-end number through the C ABI with host buffers, and a CPU
+baseline (the CPU oracle, timed on a bounded sample of the same workload).
+
+--impl reference: the reference's CPU path for the same workload and metric on the host
+cores.  The reference cannot be built here (it needs MPI, tsl::robin_map, abseil, pcg
+and nlohmann/json, none of which ship with it), so its port in oracle/ runs instead,
+with all host threads, one bounded sample per step.
+
+Multi-GPU: replicas only -- each rank partitions its own copy of the graph; value is
+the proposals of all ranks over the slowest rank's time.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+CONFIG = "C2"
+SEED = 1
+METRIC = "proposals/s"
+
+
+def workload_desc():
+    from sbp_gb300 import dcsbm
+    c = dcsbm.CONFIGS[CONFIG]
+    return {"workload": "full SBP, hybrid MCMC, directed DCSBM N=%d E~%d, %d planted blocks, Dirichlet(%g) sizes, "
+                        "power-law degrees 2.1 in [%d,%d], within:between %g" %
+                        (c["num_vertices"], c["num_edges"], c["num_blocks"], c["alpha"], c["dmin"], c["dmax"],
+                         c["ratio"]),
+            "num_vertices": c["num_vertices"], "num_edges_target": c["num_edges"], "algorithm": "hybrid_mcmc",
+            "graph_seed": 0, "proposal_seed": SEED, "ids": "int32", "counts": "int32",
+            "l2": "flushed between steps (256 MiB write)"}
+
+
+def dist_info():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        self.proc.wait()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                p = [x.strip() for x in line.split(",")]
+                if len(p) < 9:
+                    continue
+                try:
+                    sm.append(float(p[1]))
+                    mx.append(float(p[2]))
+                except ValueError:
+                    continue
+                for n, v in zip(names, p[5:9]):
+                    if v.lower().startswith("active"):
+                        reasons.add(n)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak_hbm():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def ncu_traffic(kind):
+    """Per-launch DRAM bytes of the dominant kernel from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "dram_traffic.json")
+    try:
+        with open(path) as f:
+            return json.load(f).get(kind)
+    except Exception:
+        return None
+
+
+# Algorithmic bytes per launch of each kernel category (formulas stated in the design doc).
+def algorithmic_bytes(kind, stats):
+    if kind == "gibbs_propose":
+        # per vertex proposal: CSR offsets 8 B, neighbour ids + their blocks 8 B per
+        # neighbour, per-neighbour cell lookups and degrees 12 B, sampler + specials 64 B.
+        return 72 * stats["gibbs_proposals"] + 20 * stats["gibbs_edges"]
+    return None
+
+
+def run_cpu_baseline(src, dst, n):
+    """The CPU oracle on a bounded sample of the same workload: the first outer step of the
+    golden-section search (merge pass from B = N to N/2, then the hybrid MCMC finetune)."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_bind as ob
+    ob.build()
+    cores = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+    g = ob.Graph(n, src, dst)
+    bm = ob.Blockmodel(g, n, np.arange(n, dtype=np.int32))
+    cfg = ob.make_config("hybrid_mcmc")
+    t0 = time.perf_counter()
+    s1 = bm.merge_blocks(cfg, seed=SEED, step=0, num_to_merge=n // 2)
+    s2 = bm.mcmc(cfg, seed=SEED, step=0, golden_ratio_not_reached=True)
+    dt = time.perf_counter() - t0
+    props = s1.merge_proposals + s2.proposals
+    return {"value": props / dt, "unit": METRIC, "cores": int(os.environ["OMP_NUM_THREADS"]), "kind": "port",
+            "sample": "first golden-section step of the same SBP (merge pass %d -> %d blocks + hybrid MCMC), "
+                      "%d proposals in %.1f s" % (n, n // 2, props, dt)}
+
+
+def reference_arm(args):
+    ws, rank, local = dist_info()
+    if rank != 0:
+        return
+    from sbp_gb300 import dcsbm
+    src, dst, planted = dcsbm.generate_config(CONFIG, seed=0)
+    n = dcsbm.CONFIGS[CONFIG]["num_vertices"]
+    vals = []
+    last = None
+    for i in range(args.warmup + args.steps):
+        last = run_cpu_baseline(src, dst, n)
+        if i >= args.warmup:
+            vals.append(last["value"])
+    value = float(np.mean(vals))
+    out = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": args.gpus, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "int64+f64", "data": "synthetic (seeded DCSBM)",
+           "config": workload_desc(), "impl": "reference",
+           "cpu_baseline": {"value": value, "unit": METRIC, "cores": last["cores"], "kind": "port",
+                            "sample": last["sample"]},
+           "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return reference_arm(args)
+
+    import torch
+    import sbp_gb300 as sb
+    ws, rank, local = dist_info()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    from sbp_gb300 import build as _b
+    _b.build()
+    src, dst, planted = sb.dcsbm.generate_config(CONFIG, seed=0)
+    n = sb.dcsbm.CONFIGS[CONFIG]["num_vertices"]
+    ctx = sb.Context(local)
+    G = sb.Graph(n, src, dst, ctx=ctx)  # resident in HBM before the timed region
+    sargs = sb.Args(algorithm="hybrid_mcmc", seed=SEED)
+    stream = torch.cuda.ExternalStream(ctx.lib.sbpgpu_ctx_stream(ctx.h), device=local)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=local)
+
+    for _ in range(args.warmup):
+        sb.sbp.stochastic_block_partition(G, sargs)
+    torch.cuda.synchronize()
+
+    ctx.set_timing(True)
+    ctx.read_timing()  # reset accumulators
+    clocks = ClockSampler(local)
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    step_ms, totals, results = [], {}, []
+    t_all0 = time.perf_counter()
+    for _ in range(args.steps):
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        asg, B, mdl, st = sb.sbp.stochastic_block_partition(G, sargs)
+        e1.record(stream)
+        e1.synchronize()
+        step_ms.append(e0.elapsed_time(e1))
+        results.append((asg, B, mdl))
+        for k, v in st.items():
+            totals[k] = totals.get(k, 0) + v
+    torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    wall = time.perf_counter() - t_all0
+    clk = clocks.stop()
+    timing = ctx.read_timing()
+    ctx.set_timing(False)
+    device_s = sum(step_ms) / 1e3
+    proposals = totals["proposals"] + totals["merge_proposals"]
+    local_time = torch.tensor([device_s], dtype=torch.float64, device=local)
+    local_props = torch.tensor([float(proposals)], dtype=torch.float64, device=local)
+    if ws > 1:
+        torch.distributed.all_reduce(local_time, op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.all_reduce(local_props, op=torch.distributed.ReduceOp.SUM)
+    value = local_props.item() / local_time.item()
+
+    # end to end through the C ABI with host buffers: graph upload + partition + result read
+    e2e_s, e2e_props = 0.0, 0
+    for _ in range(max(1, min(args.steps, 2))):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        Gh = sb.Graph(n, src, dst, ctx=ctx)
+        asg_h, B_h, mdl_h, st_h = sb.sbp.stochastic_block_partition(Gh, sargs)
+        Gh.close()
+        torch.cuda.synchronize()
+        e2e_s += time.perf_counter() - t0
+        e2e_props += st_h["proposals"] + st_h["merge_proposals"]
+    E = int(src.size)
+    loops = int(np.sum(src == dst))
+    h2d = 4 * ((n + 1) * 2 + E + (E - loops) + n + E + (E + 2) + n)
+    d2h = 4 * n
+
+    # roofline of the dominant kernel category
+    cats = {k[:-3]: v for k, v in timing.items() if k.endswith("_ms")}
+    dom = max(cats, key=lambda k: cats[k])
+    launches = timing.get(dom + "_launches", 0) or 1
+    peak, peak_kind = measured_peak_hbm()
+    alg_bytes = algorithmic_bytes(dom, totals)
+    roof = {"kernel": dom, "bound": "hbm", "unit": "GB/s", "peak": peak, "peak_source": peak_kind,
+            "launches": launches, "avg_launch_ms": cats[dom] / launches,
+            "time_share": cats[dom] / max(1e-9, sum(step_ms)),
+            "traffic": ncu_traffic(dom)}
+    if alg_bytes:
+        achieved = alg_bytes / launches / (cats[dom] / launches / 1e3) / 1e9
+        roof.update({"achieved": achieved, "frac": achieved / peak})
+    else:
+        roof.update({"achieved": None, "frac": None,
+                     "note": "latency-bound single-CTA sequential phase; no bandwidth roofline applies"})
+    asg, B, mdl = results[-1]
+    out = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": ws, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": float(np.mean(step_ms)), "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "int64+f64", "data": "synthetic (seeded DCSBM)",
+           "config": dict(workload_desc(), parallelism="replicas" if ws > 1 else "single GPU"),
+           "full_sbp_ms": float(np.mean(step_ms)), "wall_s": wall,
+           "num_blocks": int(B), "mdl": mdl, "nmi": sb.evaluate.nmi(planted, asg),
+           "proposals_per_step": proposals / args.steps,
+           "vertex_proposals_per_step": totals["proposals"] / args.steps,
+           "merge_proposals_per_step": totals["merge_proposals"] / args.steps,
+           "edges_swept_per_s": totals["edges_swept"] / device_s,
+           "kernel_ms": cats, "gpu_launches": int(totals["kernel_launches"]),
+           "e2e": {"value": e2e_props / e2e_s, "unit": METRIC, "h2d_bytes_per_step": h2d,
+                   "d2h_bytes_per_step": d2h},
+           "roofline": roof, "clocks": clk}
+    if rank == 0 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = run_cpu_baseline(src, dst, n)
+    if rank == 0:
+        print(json.dumps(out))
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

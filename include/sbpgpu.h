@@ -53,6 +53,8 @@ typedef struct sbpgpu_stats {
     int64_t edges_swept;      /* sum of k_out + k_in over visited vertex proposals */
     int64_t outer_steps;      /* golden-section iterations */
     int64_t kernel_launches;  /* kernels launched by this library for the call */
+    int64_t gibbs_proposals;  /* vertex proposals of the parallel (asynchronous Gibbs) phases */
+    int64_t gibbs_edges;      /* sum of k_out + k_in over those proposals */
 } sbpgpu_stats;
 
 void sbpgpu_default_config(sbpgpu_config* cfg);

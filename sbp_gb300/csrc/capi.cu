@@ -308,7 +308,8 @@ void harvest_counters(sbpgpu_graph* g) {
     check_flags(g);
     const DevFlags& f = *g->flags_host;
     g->st.moves += (int64_t)f.counters[2] + (int64_t)f.counters[5];
-    g->st.edges_swept += (int64_t)f.counters[3];
+    g->st.edges_swept += (int64_t)f.counters[3] + (int64_t)f.counters[4];
+    g->st.gibbs_edges += (int64_t)f.counters[3];
     g->st.merge_proposals += (int64_t)f.counters[6];
     reset_counters(g);
 }
@@ -322,6 +323,7 @@ void gibbs_batch_dev(sbpgpu_bm* bm, const int32_t* list, int32_t n, uint64_t see
     }
     gibbs_apply(bm->d, list, n, g->w, g->ctx->stream);
     g->st.proposals += n;
+    g->st.gibbs_proposals += n;
     do_rebuild(bm);
 }
 

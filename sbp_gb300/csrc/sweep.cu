@@ -338,7 +338,7 @@ __global__ void __launch_bounds__(kChainThreads, 1) k_mh_chain(DevGraph g, DevBM
         __syncthreads();
     }
     if (tid == 0) {
-        atomicAdd(&flags->counters[3], edges);
+        atomicAdd(&flags->counters[4], edges);
         atomicAdd(&flags->counters[5], moved);
         atomicAdd(&flags->counters[7], (unsigned long long)dsum);
     }
