@@ -121,7 +121,7 @@ __global__ void k_mdl(DevBM bm, unsigned long long* __restrict__ out) {
 __global__ void k_vertex_dS_batch(DevGraph g, DevBM bm, const int32_t* __restrict__ vs, const int32_t* __restrict__ ss,
                                   int64_t n, int log2cap, long long* __restrict__ out) {
     extern __shared__ int32_t sh[];
-    __shared__ long long red[32];
+    __shared__ long long red[32][8];
     const int cap = 1 << log2cap;
     int32_t* hk = sh;
     int32_t* hO = sh + cap;
@@ -137,7 +137,7 @@ __global__ void k_vertex_dS_batch(DevGraph g, DevBM bm, const int32_t* __restric
 
 __global__ void k_merge_dS_batch(DevGraph g, DevBM bm, const int32_t* __restrict__ rs, const int32_t* __restrict__ ss,
                                  int64_t n, long long* __restrict__ out) {
-    __shared__ long long red[32];
+    __shared__ long long red[32][8];
     for (int64_t i = blockIdx.x; i < n; i += gridDim.x) {
         const long long d = merge_delta_fixed_csr<kT>(g, bm, rs[i], ss[i], red);
         if (threadIdx.x == 0) out[i] = d;
@@ -159,13 +159,13 @@ __global__ void k_chain_fill(DevBM bm, DevChain ch, DevFlags* flags) {
     for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < bm.nnz; j += (int64_t)gridDim.x * blockDim.x) {
         bool ins;
         const int32_t slot = chain_slot(ch, bm.row_of[j], bm.row_col[j], &ins, flags);
-        if (slot >= 0) ch.vals[slot] = bm.row_cnt[j];
+        if (slot >= 0) *slot_val(ch, slot) = bm.row_cnt[j];
     }
 }
 
-__global__ void k_fill_u64(unsigned long long* p, uint64_t n, unsigned long long v) {
+__global__ void k_fill_slots(ulonglong2* p, uint64_t n) {
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
-        p[i] = v;
+        p[i] = make_ulonglong2(kEmptyKey, 0ull);  // a key inserted later starts from zero
 }
 
 }  // namespace
@@ -254,19 +254,16 @@ void chain_init(const DevBM& bm, Work& w, uint64_t extra_keys, cudaStream_t st) 
     uint64_t need = (uint64_t)bm.nnz + extra_keys + 1024;
     uint64_t cap = 1ull << ceil_log2(need * 2);
     if (cap > w.chain_cap) cap = w.chain_cap;
-    w.chain.keys = w.chain_keys;
-    w.chain.vals = w.chain_vals;
+    w.chain.slots = w.chain_slots;
     w.chain.mask = (uint32_t)(cap - 1);
     w.chain.load_limit = (uint32_t)(cap * 0.85);
     w.chain.n_keys = (uint32_t*)(w.d_scalar + 4);
     w.chain.row_head = w.row_head;
     w.chain.col_head = w.col_head;
     w.chain.pool = w.pool;
-    w.chain.pool_cap = w.pool_cap;
+    w.chain.pool_words = w.pool_words;
     w.chain.pool_used = w.d_scalar + 5;
-    k_fill_u64<<<grid_for((int64_t)cap), kT, 0, st>>>(w.chain_keys, cap, kEmptyKey);
-    // A key inserted later starts from zero; stale counts of earlier phases must not leak.
-    cudaMemsetAsync(w.chain_vals, 0, sizeof(int32_t) * cap, st);
+    k_fill_slots<<<grid_for((int64_t)cap), kT, 0, st>>>(w.chain_slots, cap);
     cudaMemsetAsync(w.d_scalar + 4, 0, 2 * sizeof(int32_t), st);
     cudaMemsetAsync(w.row_head, 0xff, sizeof(int32_t) * bm.B, st);
     cudaMemsetAsync(w.col_head, 0xff, sizeof(int32_t) * bm.B, st);

@@ -233,10 +233,11 @@ void alloc_work(sbpgpu_graph* g) {
     w.list_tmp = dalloc<int32_t>(o, N);
     // chain cell store: capacity for every cell plus the new cells of one phase.
     w.chain_cap = 1ull << ceil_log2((uint64_t)(8 * (uint64_t)E + 4096));
-    w.chain_keys = dalloc<unsigned long long>(o, w.chain_cap);
-    w.chain_vals = dalloc<int32_t>(o, w.chain_cap);
-    w.pool_cap = (int32_t)std::min<int64_t>(2 * N + (8 * E) / kChunkItems + 1024, INT32_MAX / 32);
-    w.pool = dalloc<int32_t>(o, (size_t)w.pool_cap * 32);
+    w.chain_slots = dalloc<ulonglong2>(o, w.chain_cap);
+    // list pool: every list's chunks at most double, so 16 words per block plus three
+    // times the new keys of a phase bound it
+    w.pool_words = std::min<int64_t>(16 * N + 24 * E + 4096, (int64_t)INT32_MAX - (1 << 20));
+    w.pool = dalloc<int32_t>(o, (size_t)w.pool_words);
     w.row_head = dalloc<int32_t>(o, N);
     w.col_head = dalloc<int32_t>(o, N);
     w.best = dalloc<int32_t>(o, N);
@@ -247,6 +248,11 @@ void alloc_work(sbpgpu_graph* g) {
     w.root = dalloc<int32_t>(o, N);
     w.used = dalloc<int32_t>(o, N);
     w.flags_dev = dalloc<DevFlags>(o, 1);
+    w.dense_cap = (int32_t)std::min<int64_t>(N, kDenseGlobalMax);
+    if (w.dense_cap > kDenseMax) {
+        w.dense_M = dalloc<int32_t>(o, (size_t)w.dense_cap * w.dense_cap);
+        w.dense_MT = dalloc<int32_t>(o, (size_t)w.dense_cap * w.dense_cap);
+    }
 }
 
 void ensure_split(sbpgpu_graph* g, float mh_percent) {
@@ -330,9 +336,13 @@ void gibbs_batch_dev(sbpgpu_bm* bm, const int32_t* list, int32_t n, uint64_t see
 void chain_run(sbpgpu_bm* bm, const int32_t* order, int32_t n, int32_t max_k, int64_t k_sum, uint64_t seed,
                uint32_t it, uint32_t step, int greedy) {
     sbpgpu_graph* g = bm->g;
-    if (max_k * 2 > (1 << 13)) throw ApiError(SBPGPU_EUNSUPPORTED, "sequential MH supports vertices with k <= 4096");
-    chain_init(bm->d, g->w, (uint64_t)(2 * k_sum + 4 * (int64_t)n), g->ctx->stream);
-    {
+    if (bm->d.B <= kDenseMax || bm->d.B <= g->w.dense_cap) {
+        Span sp(g->ctx, 1);
+        mh_chain_dense(g->dg, bm->d, order, n, seed, it, step, g->w, g->ctx->stream);
+    } else {
+        if (max_k * 2 > (1 << 13))
+            throw ApiError(SBPGPU_EUNSUPPORTED, "sequential MH supports vertices with k <= 4096");
+        chain_init(bm->d, g->w, (uint64_t)(2 * k_sum + 4 * (int64_t)n), g->ctx->stream);
         Span sp(g->ctx, 1);
         mh_chain(g->dg, bm->d, order, n, max_k, seed, it, step, greedy, g->w, g->ctx->stream);
     }

@@ -1,7 +1,13 @@
 // Single-CTA helpers for the sequential phases (the hybrid MH chain and the merge
 // carry-out).  The current blockmatrix is held in a DevChain: an open-addressing cell
-// hash (exact counts, zero counts kept as keys) plus per-row / per-column key lists made
-// of the snapshot CSR / CSC segment and appended chunks.  A key appears in a list once.
+// table (exact counts; a cell that drops to zero keeps its key) plus per-row /
+// per-column key lists made of the snapshot CSR / CSC segment and appended chunks.  A
+// key appears in a list once.
+//
+// List appends never race: a list that receives keys from many threads of one move
+// (row/column of the target block) is appended in bulk -- keys are staged, one thread
+// reserves room for all of them, every thread copies -- and every other list receives
+// keys from a single owning thread.
 #pragma once
 
 #include "common.cuh"
@@ -10,74 +16,69 @@ namespace sbp {
 
 constexpr int kChainThreads = 512;
 
-// Appends item to list b (one thread per list at a time).
-__device__ __forceinline__ void list_append(int32_t* head, const DevChain& ch, int32_t b, int32_t item,
-                                            DevFlags* flags) {
-    int32_t c = head[b];
-    if (c < 0 || ch.pool[c * 32 + 1] >= kChunkItems) {
-        const int32_t nc = atomicAdd(ch.pool_used, 1);
-        if (nc >= ch.pool_cap) {
-            atomicOr(&flags->err, ERR_POOL_FULL);
-            return;
-        }
-        ch.pool[nc * 32] = c;
-        ch.pool[nc * 32 + 1] = 0;
-        head[b] = nc;
-        c = nc;
-    }
-    const int32_t n = ch.pool[c * 32 + 1];
-    ch.pool[c * 32 + 2 + n] = item;
-    ch.pool[c * 32 + 1] = n + 1;
-}
-
-// Warp 0 appends new cells (rows[i], cols[i]) to the row and column lists.  Lanes that
-// share a list are grouped and their leader appends the group's items in order.
-__device__ __forceinline__ void append_new_keys(const DevChain& ch, const int32_t* rows, const int32_t* cols, int n,
+// Reserves g item slots at the head of list b; returns the pool word index of the first
+// slot or -1 when the pool is full.  One thread per list at a time.
+__device__ __forceinline__ int32_t list_reserve(int32_t* head, const DevChain& ch, int32_t b, int32_t g,
                                                 DevFlags* flags) {
-    if (threadIdx.x >= 32) return;
-    const int lane = threadIdx.x;
-    for (int base = 0; base < n; base += 32) {
-        const int j = base + lane;
-        const bool valid = j < n;
-        for (int pass = 0; pass < 2; ++pass) {
-            const int32_t key = valid ? (pass == 0 ? rows[j] : cols[j]) : -1;
-            const unsigned peers = __match_any_sync(SBP_FULL_MASK, key);
-            if (valid && lane == __ffs(peers) - 1) {
-                int32_t* head = pass == 0 ? ch.row_head : ch.col_head;
-                unsigned m = peers;
-                while (m) {
-                    const int l = __ffs(m) - 1;
-                    m &= m - 1;
-                    const int jj = base + l;
-                    list_append(head, ch, key, pass == 0 ? cols[jj] : rows[jj], flags);
-                }
-            }
-            __syncwarp();
+    const int32_t c = head[b];
+    if (c >= 0) {
+        const int32_t cnt = ch.pool[c + 1], cap = ch.pool[c + 2];
+        if (cnt + g <= cap) {
+            ch.pool[c + 1] = cnt + g;
+            return c + 3 + cnt;
         }
     }
+    int32_t cap = c >= 0 ? min(2 * ch.pool[c + 2], 1 << 16) : 13;
+    if (cap < g) cap = g;
+    const int32_t words = 3 + cap;
+    const int32_t nc = atomicAdd(ch.pool_used, words);
+    if ((int64_t)nc + words > ch.pool_words) {
+        atomicOr(&flags->err, ERR_POOL_FULL);
+        return -1;
+    }
+    ch.pool[nc] = c;
+    ch.pool[nc + 1] = g;
+    ch.pool[nc + 2] = cap;
+    head[b] = nc;
+    return nc + 3;
 }
 
-// Adds d to cell (r, c); new keys are recorded for list appends.
-__device__ __forceinline__ void chain_add(const DevChain& ch, int32_t r, int32_t c, int32_t d, int32_t* new_rows,
-                                          int32_t* new_cols, int* new_n, int new_cap, DevFlags* flags) {
-    if (d == 0) return;
+__device__ __forceinline__ void list_push1(int32_t* head, const DevChain& ch, int32_t b, int32_t item,
+                                           DevFlags* flags) {
+    const int32_t p = list_reserve(head, ch, b, 1, flags);
+    if (p >= 0) ch.pool[p] = item;
+}
+
+// Adds d to cell (r, c); returns true when the key was inserted by this call.
+__device__ __forceinline__ bool chain_add(const DevChain& ch, int32_t r, int32_t c, int32_t d, DevFlags* flags) {
+    if (d == 0) return false;
     bool ins;
     const int32_t slot = chain_slot(ch, r, c, &ins, flags);
-    if (slot < 0) return;
-    atomicAdd(ch.vals + slot, d);
-    if (ins) {
-        const int p = atomicAdd(new_n, 1);
-        if (p < new_cap) {
-            new_rows[p] = r;
-            new_cols[p] = c;
-        } else {
-            atomicOr(&flags->err, ERR_POOL_FULL);
-        }
-    }
+    if (slot < 0) return false;
+    atomicAdd(slot_val(ch, slot), d);
+    return ins;
 }
 
-// Calls f(key) for every key of row (is_row) or column b: snapshot segment
-// [lo, hi) of seg_idx and the appended chunks.  Thread-strided; every thread returns.
+// Stages one item of a bulk-appended list (shared or global staging buffer).
+__device__ __forceinline__ void stage(int32_t* buf, int* count, int cap, int32_t item, DevFlags* flags) {
+    const int p = atomicAdd(count, 1);
+    if (p < cap) buf[p] = item;
+    else atomicOr(&flags->err, ERR_POOL_FULL);
+}
+
+// Thread `leader` reserves room for n staged items in list b (result in *slot); after a
+// barrier every thread copies.  Must be called by the whole CTA.
+__device__ __forceinline__ void bulk_append(int32_t* head, const DevChain& ch, int32_t b, const int32_t* buf, int n,
+                                            int leader, int32_t* slot, DevFlags* flags) {
+    if (threadIdx.x == leader) *slot = n > 0 ? list_reserve(head, ch, b, n, flags) : -1;
+    __syncthreads();
+    const int32_t p = *slot;
+    if (p >= 0)
+        for (int i = threadIdx.x; i < n; i += blockDim.x) ch.pool[p + i] = buf[i];
+}
+
+// Calls f(key) for every key of a row (or column): snapshot segment [lo, hi) of seg_idx
+// and the appended chunks starting at head.  Thread-strided; every thread returns.
 template <typename F>
 __device__ __forceinline__ void chain_for_each(const int32_t* seg_idx, int32_t lo, int32_t hi, int32_t head,
                                                const DevChain& ch, F f) {
@@ -85,11 +86,31 @@ __device__ __forceinline__ void chain_for_each(const int32_t* seg_idx, int32_t l
     int32_t c = head;
     int guard = 0;
     while (c >= 0 && guard < (1 << 26)) {
-        const int32_t n = ((volatile int32_t*)ch.pool)[c * 32 + 1];
-        for (int i = threadIdx.x; i < n; i += blockDim.x) f(((volatile int32_t*)ch.pool)[c * 32 + 2 + i]);
-        c = ((volatile int32_t*)ch.pool)[c * 32];
+        const int32_t n = ((volatile int32_t*)ch.pool)[c + 1];
+        for (int i = threadIdx.x; i < n; i += blockDim.x) f(((volatile int32_t*)ch.pool)[c + 3 + i]);
+        c = ((volatile int32_t*)ch.pool)[c];
         ++guard;
     }
+}
+
+// Block-wide sum of N int64 values (blockDim.x == kChainThreads); every thread gets the totals.
+template <int N>
+__device__ __forceinline__ void cta_sum(long long v[N], long long (*red)[8]) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int j = 0; j < N; ++j) v[j] = warp_sum_ll(v[j]);
+    __syncthreads();
+    if (lane == 0)
+#pragma unroll
+        for (int j = 0; j < N; ++j) red[w][j] = v[j];
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < N; ++j) {
+        long long t = 0;
+        for (int i = 0; i < kChainThreads / 32; ++i) t += red[i][j];
+        v[j] = t;
+    }
+    __syncthreads();
 }
 
 // CTA exclusive scan of 1024 ints in shared memory (blockDim.x == 512); finds the

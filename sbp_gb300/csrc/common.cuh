@@ -71,18 +71,20 @@ struct DevBM {
     int32_t* col_cum;
 };
 
-// Mutable cell store used by the sequential phases (MH chain, merge carry-out).
+// Mutable cell store used by the sequential phases (MH chain, merge carry-out): an
+// open-addressing table of 16-byte slots (.x = key row << 32 | col, .y low word = count;
+// one vector load per probe) and per-row / per-column key lists made of the snapshot
+// CSR / CSC segment plus appended chunks [next, count, capacity, items...] in a pool.
 struct DevChain {
-    unsigned long long* keys;   // EMPTY = ~0ull
-    int32_t* vals;
+    ulonglong2* slots;          // key EMPTY = ~0ull
     uint32_t mask;              // capacity - 1
     uint32_t load_limit;        // maximum number of keys
     uint32_t* n_keys;           // device counter
-    int32_t* row_head;          // [B] first appended chunk of row b or -1
+    int32_t* row_head;          // [B] newest appended chunk of row b or -1
     int32_t* col_head;          // [B]
-    int32_t* pool;              // [pool_cap][32]: [0]=next, [1]=count, [2..31]=items
-    int32_t pool_cap;
-    int32_t* pool_used;         // device counter
+    int32_t* pool;              // int32 words
+    int64_t pool_words;
+    int32_t* pool_used;         // device counter (words)
 };
 
 struct DevFlags {
@@ -92,7 +94,6 @@ struct DevFlags {
 };
 
 constexpr unsigned long long kEmptyKey = ~0ull;
-constexpr int kChunkItems = 30;
 
 // ------------------------------------------------------------------ Philox4x32-10
 __device__ __forceinline__ void philox4x32_10(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3,
@@ -240,13 +241,21 @@ __device__ __forceinline__ unsigned long long cell_key(int32_t r, int32_t c) {
 __device__ __forceinline__ uint32_t cell_slot(unsigned long long k, uint32_t mask) {
     return (uint32_t)((k * 0x9E3779B97F4A7C15ull) >> 32) & mask;
 }
+__device__ __forceinline__ ulonglong2 ld_slot(const ulonglong2* p) {
+    ulonglong2 v;
+    asm volatile("ld.volatile.v2.u64 {%0, %1}, [%2];" : "=l"(v.x), "=l"(v.y) : "l"(p));
+    return v;
+}
+__device__ __forceinline__ int32_t* slot_val(const DevChain& ch, int32_t s) {
+    return reinterpret_cast<int32_t*>(&ch.slots[s].y);
+}
 __device__ __forceinline__ int32_t chain_get(const DevChain& ch, int32_t r, int32_t c) {
     const unsigned long long k = cell_key(r, c);
     uint32_t s = cell_slot(k, ch.mask);
     for (uint32_t probe = 0; probe <= ch.mask; ++probe) {
-        const unsigned long long kk = ((volatile unsigned long long*)ch.keys)[s];
-        if (kk == k) return ((volatile int32_t*)ch.vals)[s];
-        if (kk == kEmptyKey) return 0;
+        const ulonglong2 v = ld_slot(ch.slots + s);
+        if (v.x == k) return (int32_t)(uint32_t)v.y;
+        if (v.x == kEmptyKey) return 0;
         s = (s + 1) & ch.mask;
     }
     return 0;
@@ -258,10 +267,10 @@ __device__ __forceinline__ int32_t chain_slot(const DevChain& ch, int32_t r, int
     uint32_t s = cell_slot(k, ch.mask);
     *inserted = false;
     for (uint32_t probe = 0; probe <= ch.mask; ++probe) {
-        unsigned long long kk = ((volatile unsigned long long*)ch.keys)[s];
+        const unsigned long long kk = ((volatile unsigned long long*)&ch.slots[s].x)[0];
         if (kk == k) return (int32_t)s;
         if (kk == kEmptyKey) {
-            const unsigned long long prev = atomicCAS(ch.keys + s, kEmptyKey, k);
+            const unsigned long long prev = atomicCAS(&ch.slots[s].x, kEmptyKey, k);
             if (prev == kEmptyKey) {
                 *inserted = true;
                 const uint32_t n = atomicAdd(ch.n_keys, 1u);

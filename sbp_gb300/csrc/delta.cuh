@@ -46,18 +46,26 @@ struct Group {
         if (kThreads == 32) __syncwarp();
         else __syncthreads();
     }
-    // Sum over the group; red must hold >= 32 long longs of shared memory (CTA case).
-    __device__ __forceinline__ static long long sum(long long x, long long* red) {
-        x = warp_sum_ll(x);
-        if (kThreads == 32) return x;
+    // Sums N values over the group in one pass; red is [32][8] long longs of shared
+    // memory (unused for a warp).  Every thread receives the totals.
+    template <int N>
+    __device__ __forceinline__ static void sum(long long v[N], long long (*red)[8]) {
+#pragma unroll
+        for (int j = 0; j < N; ++j) v[j] = warp_sum_ll(v[j]);
+        if (kThreads == 32) return;
         const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
         __syncthreads();
-        if (lane == 0) red[w] = x;
+        if (lane == 0)
+#pragma unroll
+            for (int j = 0; j < N; ++j) red[w][j] = v[j];
         __syncthreads();
-        long long t = 0;
-        for (int i = 0; i < kThreads / 32; ++i) t += red[i];
+#pragma unroll
+        for (int j = 0; j < N; ++j) {
+            long long t = 0;
+            for (int i = 0; i < kThreads / 32; ++i) t += red[i][j];
+            v[j] = t;
+        }
         __syncthreads();
-        return t;
     }
 };
 
@@ -162,7 +170,7 @@ struct VertexScalars {
 template <int kThreads, typename Acc>
 __device__ long long vertex_delta_fixed(const DevGraph& g, const int32_t* asg, const int32_t* d_out,
                                         const int32_t* d_in, const Acc& M, int32_t v, int32_t r, int32_t s,
-                                        int32_t* hk, int32_t* hO, int32_t* hI, int log2cap, long long* red) {
+                                        int32_t* hk, int32_t* hO, int32_t* hI, int log2cap, long long (*red)[8]) {
     typedef Group<kThreads> G;
     const int t = G::rank();
     const int cap = 1 << log2cap;
@@ -213,12 +221,16 @@ __device__ long long vertex_delta_fixed(const DevGraph& g, const int32_t* asg, c
             sSi += Mbs;
         }
     }
-    acc = G::sum(acc, red);
-    sRo = G::sum(sRo, red);
-    sSo = G::sum(sSo, red);
-    sRi = G::sum(sRi, red);
-    sSi = G::sum(sSi, red);
-    spec = G::sum(spec, red);
+    {
+        long long v[6] = {acc, sRo, sSo, sRi, sSi, spec};
+        G::template sum<6>(v, red);
+        acc = v[0];
+        sRo = v[1];
+        sSo = v[2];
+        sRi = v[3];
+        sSi = v[4];
+        spec = v[5];
+    }
     // Each count is < 2^16 in this packing only when k < 65536; the callers guarantee it.
     const int32_t Or = (int32_t)((spec >> 48) & 0xffff), Ir = (int32_t)((spec >> 32) & 0xffff);
     const int32_t Os = (int32_t)((spec >> 16) & 0xffff), Is = (int32_t)(spec & 0xffff);
@@ -255,7 +267,8 @@ __device__ long long vertex_delta_fixed(const DevGraph& g, const int32_t* asg, c
 // ------------------------------------------------------------------ merge delta-MDL
 // entropy::block_merge_delta_mdl for merging r into s over the static CSR/CSC.
 template <int kThreads>
-__device__ long long merge_delta_fixed_csr(const DevGraph& g, const DevBM& bm, int32_t r, int32_t s, long long* red) {
+__device__ long long merge_delta_fixed_csr(const DevGraph& g, const DevBM& bm, int32_t r, int32_t s,
+                                        long long (*red)[8]) {
     typedef Group<kThreads> G;
     const int t = G::rank();
     const LogTab Lq{g.Lq, g.E + 1};
@@ -284,9 +297,13 @@ __device__ long long merge_delta_fixed_csr(const DevGraph& g, const DevBM& bm, i
             sCol += Mxs;
         }
     }
-    acc = G::sum(acc, red);
-    sRow = G::sum(sRow, red);
-    sCol = G::sum(sCol, red);
+    {
+        long long v[3] = {acc, sRow, sCol};
+        G::template sum<3>(v, red);
+        acc = v[0];
+        sRow = v[1];
+        sCol = v[2];
+    }
     const int32_t Mrr = csr_get(bm.row_off, bm.row_col, bm.row_cnt, r, r);
     const int32_t Mrs = csr_get(bm.row_off, bm.row_col, bm.row_cnt, r, s);
     const int32_t Msr = csr_get(bm.row_off, bm.row_col, bm.row_cnt, s, r);

@@ -34,11 +34,10 @@ struct Work {
     int ghash_log2 = 0;
     // chain state
     DevChain chain{};
-    unsigned long long* chain_keys = nullptr;
-    int32_t* chain_vals = nullptr;
+    ulonglong2* chain_slots = nullptr;
     uint64_t chain_cap = 0;            // allocated slots (power of two)
     int32_t* pool = nullptr;
-    int32_t pool_cap = 0;
+    int64_t pool_words = 0;
     int32_t* row_head = nullptr;       // [N]
     int32_t* col_head = nullptr;       // [N]
     // merge
@@ -50,6 +49,9 @@ struct Work {
     int32_t* root = nullptr;           // [N]
     int32_t* used = nullptr;           // [N]
     DevFlags* flags_dev = nullptr;
+    int32_t* dense_M = nullptr;        // [kDenseGlobalMax^2] (allocated when N allows)
+    int32_t* dense_MT = nullptr;
+    int32_t dense_cap = 0;             // largest B the dense matrices hold
 };
 
 int ceil_log2(uint64_t x);
@@ -77,6 +79,12 @@ void gibbs_propose(const DevGraph& g, const DevBM& bm, const int32_t* vlist, int
 void gibbs_apply(const DevBM& bm, const int32_t* vlist, int32_t n, Work& w, cudaStream_t st);
 void mh_chain(const DevGraph& g, DevBM& bm, const int32_t* order, int32_t n, int32_t max_k, uint64_t seed,
               uint32_t iter, uint32_t step, int greedy, Work& w, cudaStream_t st);
+// The same chain with the whole blockmatrix in shared memory (B <= kDenseMax).
+constexpr int32_t kDenseMax = 192;
+constexpr int32_t kDenseGlobalMax = 4096;
+size_t mh_chain_dense_smem(int32_t B);
+void mh_chain_dense(const DevGraph& g, DevBM& bm, const int32_t* order, int32_t n, uint64_t seed, uint32_t iter,
+                    uint32_t step, Work& w, cudaStream_t st);
 // order[i] = base[perm(i)] with the canonical shuffle keyed by (i, iter, step, dom).
 void shuffle(const int32_t* base, int32_t n, uint64_t seed, uint32_t iter, uint32_t step, uint32_t dom,
              int32_t* order, Work& w, cudaStream_t st);

@@ -49,7 +49,7 @@ __global__ void k_split_by_degree(DevGraph g, const int32_t* __restrict__ list, 
 template <int kThreads>
 __device__ __forceinline__ int32_t gibbs_one(const DevGraph& g, const DevBM& bm, int32_t v, uint64_t seed,
                                              uint32_t iter, uint32_t step, int32_t* hk, int32_t* hO, int32_t* hI,
-                                             int log2cap, long long* red, DevFlags* flags) {
+                                             int log2cap, long long (*red)[8], DevFlags* flags) {
     const int32_t r = bm.asg[v];
     uint32_t w[4];
     philox4x32_10((uint32_t)v, iter, step, DOM_GIBBS, seed, w);
@@ -93,7 +93,7 @@ __global__ void __launch_bounds__(256) k_gibbs_big(DevGraph g, DevBM bm, const i
                                                    uint32_t step, int log2cap, int32_t* __restrict__ moves,
                                                    DevFlags* flags) {
     extern __shared__ int32_t dyn[];
-    __shared__ long long red[32];
+    __shared__ long long red[32][8];
     const int cap = 1 << log2cap;
     const int32_t n = *d_n;
     for (int32_t i = blockIdx.x; i < n; i += gridDim.x) {
@@ -192,11 +192,11 @@ __global__ void __launch_bounds__(kChainThreads, 1) k_mh_chain(DevGraph g, DevBM
                                                                uint64_t seed, uint32_t iter, uint32_t step,
                                                                int log2cap, int nbits, DevFlags* flags) {
     extern __shared__ int32_t dyn[];
-    __shared__ long long red[32];
+    __shared__ long long red[32][8];
     __shared__ int32_t hist[1024];
     __shared__ int s_bucket;
     __shared__ long long s_t;
-    __shared__ int32_t s_v, s_r, s_go, s_newn, s_Or, s_Ir, s_Os, s_Is, s_cnt;
+    __shared__ int32_t s_v, s_r, s_go, s_nrs, s_ncs, s_p0, s_p1, s_Or, s_Ir, s_Os, s_Is, s_cnt;
     const int cap = 1 << log2cap;
     int32_t* hk = dyn;
     int32_t* hO = dyn + cap;
@@ -284,9 +284,12 @@ __global__ void __launch_bounds__(kChainThreads, 1) k_mh_chain(DevGraph g, DevBM
             __syncthreads();
             continue;
         }
-        // Blockmodel::move_vertex(Vertex, Delta, proposal) (blockmodel.cpp:408-435).
+        // Blockmodel::move_vertex(Vertex, Delta, proposal) (blockmodel.cpp:408-435).  New
+        // keys of row s / column s are staged and appended in bulk; every other list is
+        // appended by the thread that owns its block.
         if (tid == 0) {
-            s_newn = 0;
+            s_nrs = 0;
+            s_ncs = 0;
             s_Or = s_Ir = s_Os = s_Is = 0;
         }
         __syncthreads();
@@ -305,22 +308,51 @@ __global__ void __launch_bounds__(kChainThreads, 1) k_mh_chain(DevGraph g, DevBM
                 continue;
             }
             if (O) {
-                chain_add(ch, r, b, -O, nrows, ncols, &s_newn, ncap, flags);
-                chain_add(ch, s, b, O, nrows, ncols, &s_newn, ncap, flags);
+                chain_add(ch, r, b, -O, flags);
+                if (chain_add(ch, s, b, O, flags)) {
+                    stage(nrows, &s_nrs, ncap, b, flags);
+                    list_push1(ch.col_head, ch, b, s, flags);
+                }
             }
             if (I) {
-                chain_add(ch, b, r, -I, nrows, ncols, &s_newn, ncap, flags);
-                chain_add(ch, b, s, I, nrows, ncols, &s_newn, ncap, flags);
+                chain_add(ch, b, r, -I, flags);
+                if (chain_add(ch, b, s, I, flags)) {
+                    list_push1(ch.row_head, ch, b, s, flags);
+                    stage(ncols, &s_ncs, ncap, b, flags);
+                }
             }
         }
         __syncthreads();
         const int32_t L = __ldg(g.selfcnt + v);
-        if (tid == 0) chain_add(ch, r, r, -s_Or - s_Ir - L, nrows, ncols, &s_newn, ncap, flags);
-        if (tid == 1) chain_add(ch, r, s, s_Ir - s_Os, nrows, ncols, &s_newn, ncap, flags);
-        if (tid == 2) chain_add(ch, s, r, s_Or - s_Is, nrows, ncols, &s_newn, ncap, flags);
-        if (tid == 3) chain_add(ch, s, s, s_Os + s_Is + L, nrows, ncols, &s_newn, ncap, flags);
+        if (tid == 0) {
+            if (chain_add(ch, r, r, -s_Or - s_Ir - L, flags)) {
+                list_push1(ch.row_head, ch, r, r, flags);
+                list_push1(ch.col_head, ch, r, r, flags);
+            }
+            if (chain_add(ch, r, s, s_Ir - s_Os, flags)) {
+                list_push1(ch.row_head, ch, r, s, flags);
+                stage(ncols, &s_ncs, ncap, r, flags);
+            }
+            if (chain_add(ch, s, r, s_Or - s_Is, flags)) {
+                stage(nrows, &s_nrs, ncap, r, flags);
+                list_push1(ch.col_head, ch, r, s, flags);
+            }
+            if (chain_add(ch, s, s, s_Os + s_Is + L, flags)) {
+                stage(nrows, &s_nrs, ncap, s, flags);
+                stage(ncols, &s_ncs, ncap, s, flags);
+            }
+        }
         __syncthreads();
-        append_new_keys(ch, nrows, ncols, min(s_newn, ncap), flags);
+        {
+            const int nr = min(s_nrs, ncap), nc = min(s_ncs, ncap);
+            if (tid == 0) s_p0 = nr > 0 ? list_reserve(ch.row_head, ch, s, nr, flags) : -1;
+            if (tid == 32) s_p1 = nc > 0 ? list_reserve(ch.col_head, ch, s, nc, flags) : -1;
+            __syncthreads();
+            if (s_p0 >= 0)
+                for (int i = tid; i < nr; i += kChainThreads) ch.pool[s_p0 + i] = nrows[i];
+            if (s_p1 >= 0)
+                for (int i = tid; i < nc; i += kChainThreads) ch.pool[s_p1 + i] = ncols[i];
+        }
         if (tid == 0) {
             const int32_t selfw = L > 0 ? 1 : 0;
             bm.d_out[r] -= kout;

@@ -161,19 +161,22 @@ def test_gibbs_apply_size_one_rule(gpu, oracle):
         same_state(gb, ob)
 
 
-@pytest.mark.parametrize("B", [8, 120, 1500])
-def test_mh_chain_identical(gpu, oracle, B):
-    G, O, gb, ob, a, _ = make_pair(gpu, oracle, 2500, 30000, 9, B, seed=50 + B)
-    order = np.random.default_rng(B).permutation(2500)[:600].astype(np.int32)
+@pytest.mark.parametrize("n,B", [(2500, 8), (2500, 120), (2500, 1500), (9000, 5000)])
+def test_mh_chain_identical(gpu, oracle, n, B):
+    """B <= 192: shared-memory dense chain; B <= 4096: global dense chain; larger: the
+    hash-based chain."""
+    G, O, gb, ob, a, _ = make_pair(gpu, oracle, n, 12 * n, 9, B, seed=50 + B)
+    order = np.random.default_rng(B).permutation(n)[:600].astype(np.int32)
     applied = gpu.finetune.mh_chain(gb, order, seed=8, iteration=1, step=3)
     want = ob.mh_chain(order, 8, 1, 3, oracle.make_config("hybrid_mcmc"))
     assert applied == want
     same_state(gb, ob)
 
 
-@pytest.mark.parametrize("alg", ["async_gibbs", "hybrid_mcmc", "metropolis_hastings"])
-def test_mcmc_identical(gpu, oracle, alg):
-    G, O, gb, ob, a, _ = make_pair(gpu, oracle, 2000, 24000, 9, 150, seed=60)
+@pytest.mark.parametrize("alg,B", [("async_gibbs", 150), ("hybrid_mcmc", 150), ("hybrid_mcmc", 900),
+                                   ("metropolis_hastings", 150)])
+def test_mcmc_identical(gpu, oracle, alg, B):
+    G, O, gb, ob, a, _ = make_pair(gpu, oracle, 2000, 24000, 9, B, seed=60)
     args = gpu.Args(algorithm=alg, seed=13, max_iterations=6)
     gpu.finetune.mcmc(2, G, gb, True, args)
     cfg = oracle.make_config(alg, max_iterations=6)
