@@ -64,6 +64,7 @@ SIGNATURES = {
     "sbpgpu_last_error": (ctypes.c_char_p, [vp]),
     "sbpgpu_ctx_synchronize": (ctypes.c_int, [vp]),
     "sbpgpu_ctx_stream": (vp, [vp]),
+    "sbpgpu_ctx_set_cells_budget": (ctypes.c_int, [vp, ctypes.c_int64]),
     "sbpgpu_graph_create": (ctypes.c_int, [vp, ctypes.c_int64, ctypes.c_int64, i32p, i32p, ctypes.POINTER(vp)]),
     "sbpgpu_graph_create_device": (ctypes.c_int, [vp, ctypes.c_int64, ctypes.c_int64, vp, vp, ctypes.POINTER(vp)]),
     "sbpgpu_graph_destroy": (None, [vp]),

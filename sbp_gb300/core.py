@@ -76,6 +76,10 @@ class Context:
     def set_timing(self, enabled):
         self.lib.sbpgpu_set_timing(self.h, int(bool(enabled)))
 
+    def set_cells_budget(self, nbytes):
+        """Device bytes the merge carry-out may use for dense cell counts (0: hashed store)."""
+        self.check(self.lib.sbpgpu_ctx_set_cells_budget(self.h, int(nbytes)))
+
     def read_timing(self):
         t = _lib.KernelTiming()
         self.check(self.lib.sbpgpu_read_timing(self.h, ctypes.byref(t)))

@@ -250,23 +250,27 @@ void launch_propose_batch(const DevGraph& g, const DevBM& bm, const int32_t* v, 
     count_launches(1);
 }
 
-void chain_init(const DevBM& bm, Work& w, uint64_t extra_keys, cudaStream_t st) {
-    uint64_t need = (uint64_t)bm.nnz + extra_keys + 1024;
-    uint64_t cap = 1ull << ceil_log2(need * 2);
-    if (cap > w.chain_cap) cap = w.chain_cap;
+void lists_init(const DevBM& bm, Work& w, cudaStream_t st) {
     w.chain.slots = w.chain_slots;
-    w.chain.mask = (uint32_t)(cap - 1);
-    w.chain.load_limit = (uint32_t)(cap * 0.85);
     w.chain.n_keys = (uint32_t*)(w.d_scalar + 4);
     w.chain.row_head = w.row_head;
     w.chain.col_head = w.col_head;
     w.chain.pool = w.pool;
     w.chain.pool_words = w.pool_words;
     w.chain.pool_used = w.d_scalar + 5;
-    k_fill_slots<<<grid_for((int64_t)cap), kT, 0, st>>>(w.chain_slots, cap);
     cudaMemsetAsync(w.d_scalar + 4, 0, 2 * sizeof(int32_t), st);
     cudaMemsetAsync(w.row_head, 0xff, sizeof(int32_t) * bm.B, st);
     cudaMemsetAsync(w.col_head, 0xff, sizeof(int32_t) * bm.B, st);
+}
+
+void chain_init(const DevBM& bm, Work& w, uint64_t extra_keys, cudaStream_t st) {
+    uint64_t need = (uint64_t)bm.nnz + extra_keys + 1024;
+    uint64_t cap = 1ull << ceil_log2(need * 2);
+    if (cap > w.chain_cap) cap = w.chain_cap;
+    lists_init(bm, w, st);
+    w.chain.mask = (uint32_t)(cap - 1);
+    w.chain.load_limit = (uint32_t)(cap * 0.85);
+    k_fill_slots<<<grid_for((int64_t)cap), kT, 0, st>>>(w.chain_slots, cap);
     k_chain_fill<<<grid_for(bm.nnz), kT, 0, st>>>(bm, w.chain, w.flags_dev);
     count_launches(2);
 }

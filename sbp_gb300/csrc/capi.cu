@@ -82,6 +82,7 @@ struct sbpgpu_ctx {
     cudaStream_t stream = nullptr;
     std::string err;
     bool timing = false;
+    int64_t cells_budget = int64_t(16) << 30;  // dense carry-out cells, bytes
     std::vector<TimedSpan> pending;
     std::vector<cudaEvent_t> free_events;
     sbpgpu_kernel_timing tm{};
@@ -460,6 +461,29 @@ void mcmc_impl(sbpgpu_bm* bm, const sbpgpu_config& cfg, uint64_t seed, int32_t s
     else metropolis_hastings(bm, cfg, seed, step, golden);
 }
 
+// Dense B x B cells for the carry-out when they fit the context's budget; otherwise (or
+// when the allocation fails) the carry-out uses the chain hash.
+void ensure_cells(sbpgpu_graph* g, int32_t B) {
+    Work& w = g->w;
+    const uint64_t need = (uint64_t)B * (uint64_t)B;
+    const bool fits = need * sizeof(int32_t) <= (uint64_t)std::max<int64_t>(g->ctx->cells_budget, 0);
+    if (fits && w.cells_elems >= need) return;
+    if (w.cells) {
+        CK(cudaStreamSynchronize(g->ctx->stream));
+        CK(cudaFree(w.cells));
+        w.cells = nullptr;
+        w.cells_elems = 0;
+    }
+    if (!fits) return;
+    void* p = nullptr;
+    if (cudaMalloc(&p, need * sizeof(int32_t)) != cudaSuccess) {
+        cudaGetLastError();
+        return;
+    }
+    w.cells = static_cast<int32_t*>(p);
+    w.cells_elems = need;
+}
+
 void merge_impl(sbpgpu_bm* bm, const sbpgpu_config& cfg, uint64_t seed, int32_t step, int64_t num_to_merge) {
     sbpgpu_graph* g = bm->g;
     if (num_to_merge <= 0) return;  // nothing is merged; the rebuild would reproduce the same state
@@ -469,6 +493,7 @@ void merge_impl(sbpgpu_bm* bm, const sbpgpu_config& cfg, uint64_t seed, int32_t 
         Span sp(g->ctx, 2);
         merge_propose(g->dg, bm->d, seed, (uint32_t)step, g->w, g->ctx->stream);
     }
+    if (!cfg.approximate) ensure_cells(g, B);
     {
         Span sp(g->ctx, 3);
         carry_out(g->dg, bm->d, num_to_merge, cfg.approximate, g->w, g->ctx->stream);
@@ -602,6 +627,7 @@ void release_graph(sbpgpu_graph* g) {
     sbpgpu_ctx* ctx = g->ctx;
     cudaStreamSynchronize(ctx->stream);
     free_all(g->owned);
+    if (g->w.cells) cudaFree(g->w.cells);
     if (g->flags_host) cudaFreeHost(g->flags_host);
     delete g;
     ctx->refs--;
@@ -656,6 +682,13 @@ sbpgpu_status sbpgpu_ctx_synchronize(sbpgpu_ctx* ctx) {
 }
 
 void* sbpgpu_ctx_stream(sbpgpu_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+sbpgpu_status sbpgpu_ctx_set_cells_budget(sbpgpu_ctx* ctx, int64_t bytes) {
+    if (!ctx) return SBPGPU_EINVAL;
+    if (bytes < 0) return fail(ctx, SBPGPU_EINVAL, "cells budget must be >= 0");
+    ctx->cells_budget = bytes;
+    return SBPGPU_OK;
+}
 
 sbpgpu_status sbpgpu_graph_create(sbpgpu_ctx* ctx, int64_t N, int64_t E, const int32_t* src, const int32_t* dst,
                                   sbpgpu_graph** out) {

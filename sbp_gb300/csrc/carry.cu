@@ -1,0 +1,520 @@
+// Exact block-merge carry-out: block_merge::carry_out_best_merges_advanced (reference
+// src/block_merge.cpp:40-117) on one CTA.
+//
+// The reference pops merges one at a time from a priority queue ordered by delta,
+// recomputes the popped merge's delta against the current blockmodel, puts it back with
+// the recomputed delta when that is larger than the delta now on top of the queue, and
+// merges otherwise.  Between two merges the blockmodel does not change, so the deltas of
+// the next pops do not depend on one another.  Each round here therefore
+//   1. selects the W smallest live queue entries (and the (W+1)-th as a bound),
+//   2. recomputes their deltas at once, one team of warps per entry,
+//   3. replays the reference's pop / put-back / merge rule over those values on one
+//      thread, up to the first merge or the first entry it holds no value for,
+//   4. applies that merge with the whole CTA.
+// Merges, their order and every put-back delta equal those of the one-at-a-time loop;
+// ties of equal delta pop in ascending block order.
+//
+// Queue: the proposals sorted by (delta, block) (P, read through a cursor), put-back
+// entries in a sorted shared-memory buffer (S) that spills into a sorted global run (R)
+// through a parallel merge.  Each block is in the queue at most once.
+//
+// Cell values: a dense B x B int32 matrix when it fits the dense budget (no hashing; a
+// cell of two live blocks is non-zero exactly when its key is in the row / column
+// lists, because the only cells a merge empties are those of the block that dies), else
+// the chain hash.  Keys always come from the chain's row / column lists.
+#include <algorithm>
+#include <cfloat>
+#include <climits>
+
+#include "chain.cuh"
+#include "kernels.cuh"
+
+namespace sbp {
+
+namespace {
+
+constexpr int kCarryThreads = 512;
+constexpr int kCarryWarps = kCarryThreads / 32;
+constexpr int kQS = 1024;   // shared put-back buffer
+constexpr int kMaxW = 16;   // entries evaluated per round (kCarryWarps / warps per team)
+
+struct DenseCells {
+    int32_t* M;
+    int64_t ld;
+    __device__ __forceinline__ int32_t* at(int32_t r, int32_t c) const { return M + (int64_t)r * ld + c; }
+    __device__ __forceinline__ int32_t get(int32_t r, int32_t c) const { return __ldcg(at(r, c)); }
+    // Reads and clears a cell owned by the calling thread.
+    __device__ __forceinline__ int32_t take(int32_t r, int32_t c, DevFlags*) const {
+        int32_t* p = at(r, c);
+        const int32_t v = __ldcg(p);
+        if (v != 0) __stcg(p, 0);
+        return v;
+    }
+    // Adds d > 0; true when the cell was empty (its key is new to the lists).
+    __device__ __forceinline__ bool add(int32_t r, int32_t c, int32_t d, DevFlags*) const {
+        return atomicAdd(at(r, c), d) == 0;
+    }
+};
+
+struct HashCells {
+    DevChain ch;
+    __device__ __forceinline__ int32_t get(int32_t r, int32_t c) const { return chain_get(ch, r, c); }
+    __device__ __forceinline__ int32_t take(int32_t r, int32_t c, DevFlags*) const {
+        const unsigned long long k = cell_key(r, c);
+        uint32_t s = cell_slot(k, ch.mask);
+        for (uint32_t probe = 0; probe <= ch.mask; ++probe) {
+            const ulonglong2 v = ld_slot(ch.slots + s);
+            if (v.x == k) return (int32_t)(uint32_t)v.y == 0 ? 0 : atomicExch(slot_val(ch, (int32_t)s), 0);
+            if (v.x == kEmptyKey) return 0;
+            s = (s + 1) & ch.mask;
+        }
+        return 0;
+    }
+    __device__ __forceinline__ bool add(int32_t r, int32_t c, int32_t d, DevFlags* flags) const {
+        return chain_add(ch, r, c, d, flags);
+    }
+};
+
+__device__ __forceinline__ bool qless(double a, int32_t ab, double b, int32_t bb) {
+    return a < b || (a == b && ab < bb);
+}
+
+// Inverse of the order-preserving key of the proposal sort (k_merge_keys).
+__device__ __forceinline__ double key_to_double(uint64_t k) {
+    const uint64_t u = (k >> 63) ? (k & 0x7fffffffffffffffull) : ~k;
+    return __longlong_as_double((long long)u);
+}
+
+// Number of entries of the sorted list (d[i], b[i]), i < n, ordered before (x, xb).
+__device__ __forceinline__ int count_before(const double* d, const int32_t* b, int n, double x, int32_t xb) {
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (qless(d[mid], b[mid], x, xb)) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// Root of x in the block map (union-find with path halving; concurrent halving only
+// ever links a node to one of its ancestors).
+__device__ __forceinline__ int32_t uf_find(int32_t* parent, int32_t x) {
+    int guard = 0;
+    while (guard++ < (1 << 24)) {
+        const int32_t p = parent[x];
+        if (p == x) return x;
+        const int32_t gp = parent[p];
+        if (gp != p) parent[x] = gp;
+        x = gp;
+    }
+    return x;
+}
+
+// One team's share of entropy::block_merge_delta_mdl (reference src/entropy.cpp:129-182)
+// for merging r into s, in units of 2^-24.  Thread t of nt walks its stride of the row
+// and column key lists of r; the warp sum of the returned values over the team is the
+// delta.  The terms that need no walk are added by the leader warp.
+//
+// Row cell (r, c) with count m moves to (s, c): its term, the change of (s, c) and, for
+// the cells of row s that do not receive anything, the change of their d_out factor
+// collapse into (d_out[s] - M[s][s] - M[s][r] - sum over moved c of M[s][c]) times the
+// log-degree difference; columns likewise.
+template <class Cells>
+__device__ long long merge_delta_part(const DevGraph& g, const DevBM& bm, const DevChain& ch, const Cells& cells,
+                                      int32_t r, int32_t s, int t, int nt, bool leader) {
+    const LogTab Lq{g.Lq, g.E + 1};
+    const int32_t dout_r = bm.d_out[r], din_r = bm.d_in[r], dout_s = bm.d_out[s], din_s = bm.d_in[s];
+    const int32_t dout_s2 = dout_s + dout_r, din_s2 = din_s + din_r;
+    const long long Lout = Lx(Lq, dout_s2) - Lx(Lq, dout_s), Lin = Lx(Lq, din_s2) - Lx(Lq, din_s);
+    long long acc = 0;
+    // is_row: cell (r, key) moving to (s, key), factor d_in[key]; else (key, r) -> (key, s),
+    // factor d_out[key].  Both forms load their three values before using any of them.
+    auto item = [&](int32_t key, bool is_row) {
+        const int32_t m = cells.get(is_row ? r : key, is_row ? key : r);
+        const int32_t o = cells.get(is_row ? s : key, is_row ? key : s);
+        const int32_t deg = (is_row ? bm.d_in : bm.d_out)[key];
+        if (m == 0 || (!is_row && key == r)) return;
+        const int32_t own = is_row ? dout_r : din_r;
+        acc += ce_fixed(Lq, m, deg, own);
+        if (is_row ? (key != r && key != s) : (key != s)) {
+            const int32_t ds = is_row ? dout_s : din_s, ds2 = is_row ? dout_s2 : din_s2;
+            acc += ce_fixed(Lq, o, deg, ds) - ce_fixed(Lq, o + m, deg, ds2) - (long long)o * (is_row ? Lout : Lin);
+        }
+    };
+    // snapshot segments of row r and column r as one index space
+    const int32_t rlo = bm.row_off[r], rn = bm.row_off[r + 1] - rlo;
+    const int32_t clo = bm.col_off[r], cn = bm.col_off[r + 1] - clo;
+    for (int32_t j = t; j < rn + cn; j += nt) {
+        const bool is_row = j < rn;
+        item(is_row ? bm.row_col[rlo + j] : bm.col_row[clo + j - rn], is_row);
+    }
+    chunks_for_each(ch.row_head[r], ch, t, nt, [&](int32_t c) { item(c, true); });
+    chunks_for_each(ch.col_head[r], ch, t, nt, [&](int32_t x) { item(x, false); });
+    acc = warp_sum_ll(acc);
+    if (leader) {
+        const int32_t Mrr = cells.get(r, r), Mrs = cells.get(r, s), Msr = cells.get(s, r), Mss = cells.get(s, s);
+        const int32_t dss = Mrr + Mrs + Msr;
+        if (dss > 0) acc += ce_fixed(Lq, Mss, din_s, dout_s) - ce_fixed(Lq, Mss + dss, din_s2, dout_s2);
+        else acc += ce_delta(Lq, Mss, din_s, dout_s, din_s2, dout_s2);
+        acc += ((long long)dout_s - Msr - Mss) * Lout + ((long long)din_s - Mrs - Mss) * Lin;
+    }
+    return acc;
+}
+
+struct CarryShared {
+    double s_dS[2][kQS];
+    int32_t s_blk[2][kQS];
+    double h_dS[3][32];
+    int32_t h_blk[3][32];
+    double c_dS[kMaxW];
+    int32_t c_blk[kMaxW];
+    int32_t c_src[kMaxW];
+    int32_t c_to[kMaxW];
+    long long part[kCarryWarps];
+    double q_dS[kMaxW];
+    int32_t q_blk[kMaxW];
+    int32_t q_to[kMaxW];
+    double b_dS;
+    int32_t b_blk;
+    int32_t has_bound, ncand, nq, cS;
+    int32_t p, q, nR, rsel, ns, ssel;
+    int32_t mf, mt, nrt, nct, slot_r, slot_c;
+    long long merged, rounds;
+};
+
+// W = kCarryWarps / team_warps entries per round; team_warps in {1, 2, 4, 8}.
+template <class Cells>
+__global__ void __launch_bounds__(kCarryThreads, 1) k_carry_out(
+    DevGraph g, DevBM bm, DevChain ch, Cells cells, const uint64_t* __restrict__ pkeys,
+    const int32_t* __restrict__ pblk, int32_t nP, const int32_t* __restrict__ best, double* r0_dS, int32_t* r0_blk,
+    double* r1_dS, int32_t* r1_blk, int32_t* parent, long long num_to_merge, int team_warps, int32_t* stage_row,
+    int32_t* stage_col, int stage_cap, int32_t* out_merged, DevFlags* flags) {
+    __shared__ CarryShared sh;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int W = min(kMaxW, kCarryWarps / team_warps);
+    if (tid == 0) {
+        sh.p = 0;
+        sh.q = 0;
+        sh.nR = 0;
+        sh.rsel = 0;
+        sh.ns = 0;
+        sh.ssel = 0;
+        sh.merged = 0;
+        sh.rounds = 0;
+    }
+    const long long max_rounds = 64ll * (nP + 1) + 4096;
+    __syncthreads();
+    while (true) {
+        if (sh.merged >= num_to_merge) break;
+        if (sh.rounds >= max_rounds) {
+            if (tid == 0) atomicOr(&flags->err, ERR_STATE);
+            break;
+        }
+        // ---- 1. the W smallest live entries and the bound (warp 0)
+        if (warp == 0) {
+            const int p = sh.p, q = sh.q, nR = sh.nR, ns = sh.ns, ssel = sh.ssel;
+            const double* rd = sh.rsel ? r1_dS : r0_dS;
+            const int32_t* rb = sh.rsel ? r1_blk : r0_blk;
+            const int n0 = max(0, min(W + 1, nP - p)), n1 = max(0, min(W + 1, nR - q)), n2 = min(W + 1, ns);
+            if (lane < n0) {
+                sh.h_dS[0][lane] = key_to_double(pkeys[p + lane]);
+                sh.h_blk[0][lane] = pblk[p + lane];
+            }
+            if (lane < n1) {
+                sh.h_dS[1][lane] = rd[q + lane];
+                sh.h_blk[1][lane] = rb[q + lane];
+            }
+            if (lane < n2) {
+                sh.h_dS[2][lane] = sh.s_dS[ssel][lane];
+                sh.h_blk[2][lane] = sh.s_blk[ssel][lane];
+            }
+            __syncwarp();
+            const int n[3] = {n0, n1, n2};
+#pragma unroll
+            for (int src = 0; src < 3; ++src) {
+                if (lane < n[src]) {
+                    const double d = sh.h_dS[src][lane];
+                    const int32_t b = sh.h_blk[src][lane];
+                    int rank = lane;
+#pragma unroll
+                    for (int o = 0; o < 3; ++o)
+                        if (o != src) rank += count_before(sh.h_dS[o], sh.h_blk[o], n[o], d, b);
+                    if (rank < W) {
+                        sh.c_dS[rank] = d;
+                        sh.c_blk[rank] = b;
+                        sh.c_src[rank] = src;
+                    } else if (rank == W) {
+                        sh.b_dS = d;
+                        sh.b_blk = b;
+                    }
+                }
+            }
+            if (lane == 0) {
+                const int tot = n0 + n1 + n2;
+                sh.ncand = min(W, tot);
+                sh.has_bound = tot > W;
+            }
+        }
+        __syncthreads();
+        const int ncand = sh.ncand;
+        if (ncand == 0) break;
+        // ---- 2. recompute the deltas, one team per entry
+        {
+            const int team = warp / team_warps;
+            if (team < ncand) {
+                const int32_t from = sh.c_blk[team];
+                int32_t to = 0;
+                if (lane == 0) {
+                    const int32_t b = best[from];
+                    to = (b < 0 || b >= bm.B) ? from : uf_find(parent, b);
+                }
+                to = __shfl_sync(SBP_FULL_MASK, to, 0);
+                long long part = 0;
+                if (to != from) {
+                    const int nt = 32 * team_warps, t = tid - team * nt;
+                    part = merge_delta_part(g, bm, ch, cells, from, to, t, nt, (warp % team_warps) == 0);
+                }
+                if (lane == 0) {
+                    sh.part[warp] = part;
+                    if (warp % team_warps == 0) sh.c_to[team] = to;
+                }
+            }
+        }
+        __syncthreads();
+        // ---- 3. replay the queue rule (block_merge.cpp:54-81)
+        if (tid == 0) {
+            int i = 0, nq = 0, cons[3] = {0, 0, 0};
+            int32_t mf = -1, mt = -1;
+            const bool hb = sh.has_bound;
+            while (true) {
+                int pick = -1;
+                double bd = 0.0;
+                int32_t bb = 0;
+                if (i < ncand) {
+                    pick = 0;
+                    bd = sh.c_dS[i];
+                    bb = sh.c_blk[i];
+                }
+                if (nq > 0 && (pick < 0 || qless(sh.q_dS[0], sh.q_blk[0], bd, bb))) {
+                    pick = 1;
+                    bd = sh.q_dS[0];
+                    bb = sh.q_blk[0];
+                }
+                if (pick < 0) break;                                      // queue empty
+                if (hb && qless(sh.b_dS, sh.b_blk, bd, bb)) break;        // next pop not evaluated
+                if (pick == 1) {
+                    // popped again with the delta it was put back with: it is the smallest
+                    // entry, so it merges
+                    mf = sh.q_blk[0];
+                    mt = sh.q_to[0];
+                    for (int k = 1; k < nq; ++k) {
+                        sh.q_dS[k - 1] = sh.q_dS[k];
+                        sh.q_blk[k - 1] = sh.q_blk[k];
+                        sh.q_to[k - 1] = sh.q_to[k];
+                    }
+                    --nq;
+                    break;
+                }
+                const int32_t from = sh.c_blk[i], to = sh.c_to[i];
+                long long aq = 0;
+                for (int k = 0; k < team_warps; ++k) aq += sh.part[i * team_warps + k];
+                ++cons[sh.c_src[i]];
+                ++i;
+                if (to == from) continue;  // already in the same block
+                const double act = fixed_to_double(aq);
+                if (i < ncand || nq > 0 || hb) {
+                    double top = hb ? sh.b_dS : INFINITY;
+                    if (i < ncand) top = fmin(top, sh.c_dS[i]);
+                    if (nq > 0) top = fmin(top, sh.q_dS[0]);
+                    if (act > top) {  // put back with the recomputed delta
+                        int k = nq++;
+                        while (k > 0 && qless(act, from, sh.q_dS[k - 1], sh.q_blk[k - 1])) {
+                            sh.q_dS[k] = sh.q_dS[k - 1];
+                            sh.q_blk[k] = sh.q_blk[k - 1];
+                            sh.q_to[k] = sh.q_to[k - 1];
+                            --k;
+                        }
+                        sh.q_dS[k] = act;
+                        sh.q_blk[k] = from;
+                        sh.q_to[k] = to;
+                        continue;
+                    }
+                }
+                mf = from;
+                mt = to;
+                break;
+            }
+            sh.p += cons[0];
+            sh.q += cons[1];
+            sh.cS = cons[2];
+            sh.nq = nq;
+            sh.mf = mf;
+            sh.mt = mt;
+            sh.nrt = 0;
+            sh.nct = 0;
+            sh.rounds += 1;
+        }
+        __syncthreads();
+        // ---- 4. S := S[cS..ns) merged with the put-back entries
+        {
+            const int cS = sh.cS, nq = sh.nq, ns = sh.ns, ssel = sh.ssel;
+            if (cS > 0 || nq > 0) {
+                const int rest = ns - cS;
+                const double* sd = sh.s_dS[ssel] + cS;
+                const int32_t* sb = sh.s_blk[ssel] + cS;
+                double* od = sh.s_dS[ssel ^ 1];
+                int32_t* ob = sh.s_blk[ssel ^ 1];
+                for (int i = tid; i < rest; i += kCarryThreads) {
+                    int pos = i;
+                    for (int k = 0; k < nq; ++k) pos += qless(sh.q_dS[k], sh.q_blk[k], sd[i], sb[i]);
+                    od[pos] = sd[i];
+                    ob[pos] = sb[i];
+                }
+                for (int j = tid; j < nq; j += kCarryThreads) {
+                    const int pos = j + count_before(sd, sb, rest, sh.q_dS[j], sh.q_blk[j]);
+                    od[pos] = sh.q_dS[j];
+                    ob[pos] = sh.q_blk[j];
+                }
+                __syncthreads();
+                if (tid == 0) {
+                    sh.ns = rest + nq;
+                    sh.ssel = ssel ^ 1;
+                }
+                __syncthreads();
+            }
+        }
+        // ---- spill S into R when it could not take another round's put-backs
+        if (sh.ns > kQS - kMaxW - 1) {
+            const int ns = sh.ns, ssel = sh.ssel, q = sh.q, nr = sh.nR - sh.q;
+            const double* rd = (sh.rsel ? r1_dS : r0_dS) + q;
+            const int32_t* rb = (sh.rsel ? r1_blk : r0_blk) + q;
+            double* od = sh.rsel ? r0_dS : r1_dS;
+            int32_t* ob = sh.rsel ? r0_blk : r1_blk;
+            const double* sd = sh.s_dS[ssel];
+            const int32_t* sb = sh.s_blk[ssel];
+            for (int i = tid; i < nr; i += kCarryThreads) {
+                const double d = rd[i];
+                const int32_t b = rb[i];
+                const int pos = i + count_before(sd, sb, ns, d, b);
+                od[pos] = d;
+                ob[pos] = b;
+            }
+            for (int j = tid; j < ns; j += kCarryThreads) {
+                int lo = 0, hi = nr;
+                while (lo < hi) {
+                    const int mid = (lo + hi) >> 1;
+                    if (qless(rd[mid], rb[mid], sd[j], sb[j])) lo = mid + 1;
+                    else hi = mid;
+                }
+                od[j + lo] = sd[j];
+                ob[j + lo] = sb[j];
+            }
+            __syncthreads();
+            if (tid == 0) {
+                sh.nR = nr + ns;
+                sh.q = 0;
+                sh.rsel ^= 1;
+                sh.ns = 0;
+            }
+            __syncthreads();
+        }
+        // ---- 5. Blockmodel::merge_block (src/blockmodel/blockmodel.cpp:337-363)
+        const int32_t mf = sh.mf, mt = sh.mt;
+        if (mf >= 0) {
+            // Row mf by the first half of the CTA, column mf by the second.  New keys of
+            // row mt and column mt are staged for bulk appends; every other list that
+            // receives a key receives it from one thread.
+            const int half = tid / (kCarryThreads / 2), ht = tid % (kCarryThreads / 2);
+            if (half == 0) {
+                list_for_each(bm.row_col, bm.row_off[mf], bm.row_off[mf + 1], ch.row_head[mf], ch, ht,
+                              kCarryThreads / 2, [&](int32_t c) {
+                                  const int32_t m = cells.take(mf, c, flags);
+                                  if (m == 0) return;
+                                  const int32_t c2 = (c == mf || c == mt) ? mt : c;
+                                  if (cells.add(mt, c2, m, flags)) {
+                                      stage(stage_row, &sh.nrt, stage_cap, c2, flags);
+                                      if (c2 == mt) stage(stage_col, &sh.nct, stage_cap, mt, flags);
+                                      else list_push1(ch.col_head, ch, c2, mt, flags);
+                                  }
+                              });
+            } else {
+                list_for_each(bm.col_row, bm.col_off[mf], bm.col_off[mf + 1], ch.col_head[mf], ch, ht,
+                              kCarryThreads / 2, [&](int32_t x) {
+                                  if (x == mf) return;
+                                  const int32_t m = cells.take(x, mf, flags);
+                                  if (m == 0) return;
+                                  const int32_t x2 = x == mt ? mt : x;
+                                  if (cells.add(x2, mt, m, flags)) {
+                                      stage(stage_col, &sh.nct, stage_cap, x2, flags);
+                                      if (x2 == mt) stage(stage_row, &sh.nrt, stage_cap, mt, flags);
+                                      else list_push1(ch.row_head, ch, x2, mt, flags);
+                                  }
+                              });
+            }
+            __syncthreads();
+            const int nr = min(sh.nrt, stage_cap), nc = min(sh.nct, stage_cap);
+            if (tid == 0) sh.slot_r = nr > 0 ? list_reserve(ch.row_head, ch, mt, nr, flags) : -1;
+            if (tid == 32) sh.slot_c = nc > 0 ? list_reserve(ch.col_head, ch, mt, nc, flags) : -1;
+            __syncthreads();
+            const int32_t pr = sh.slot_r, pc = sh.slot_c;
+            if (pr >= 0)
+                for (int i = tid; i < nr; i += kCarryThreads) ch.pool[pr + i] = stage_row[i];
+            if (pc >= 0)
+                for (int i = tid; i < nc; i += kCarryThreads) ch.pool[pc + i] = stage_col[i];
+            if (tid == 0) {
+                bm.d_out[mt] += bm.d_out[mf];
+                bm.d_in[mt] += bm.d_in[mf];
+                bm.d_out[mf] = 0;
+                bm.d_in[mf] = 0;
+                bm.d_tot[mf] = 0;
+                bm.d_tot[mt] = bm.d_out[mt] + bm.d_in[mt] - cells.get(mt, mt);
+                bm.sizes[mt] += bm.sizes[mf];
+                bm.sizes[mf] = 0;
+                parent[mf] = mt;
+                sh.merged += 1;
+            }
+        }
+        __syncthreads();
+    }
+    if (tid == 0) {
+        *out_merged = (int32_t)sh.merged;
+        atomicAdd(&flags->counters[0], (unsigned long long)sh.rounds);
+    }
+}
+
+__global__ void k_dense_cells_fill(DevBM bm, int32_t* M) {
+    const int64_t B = bm.B;
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < bm.nnz; j += (int64_t)gridDim.x * blockDim.x)
+        M[bm.row_of[j] * B + bm.row_col[j]] = bm.row_cnt[j];
+}
+
+}  // namespace
+
+void carry_out_exact(const DevGraph& g, DevBM& bm, int64_t num_to_merge, Work& w, cudaStream_t st) {
+    const int32_t B = bm.B;
+    const bool dense = w.cells && (uint64_t)B * (uint64_t)B <= w.cells_elems;
+    // team size from the mean number of row + column keys per block
+    const double keys = 2.0 * (double)bm.nnz / (double)(B > 0 ? B : 1);
+    const int team_warps = keys <= 64 ? 1 : keys <= 128 ? 2 : keys <= 256 ? 4 : 8;
+    int32_t* d_merged = w.d_scalar + 1;
+    if (dense) {
+        lists_init(bm, w, st);
+        cudaMemsetAsync(w.cells, 0, sizeof(int32_t) * (size_t)B * (size_t)B, st);
+        const int64_t blocks = std::min<int64_t>((bm.nnz + 255) / 256 + 1, 152 * 16);
+        k_dense_cells_fill<<<(unsigned)blocks, 256, 0, st>>>(bm, w.cells);
+        k_carry_out<DenseCells><<<1, kCarryThreads, 0, st>>>(
+            g, bm, w.chain, DenseCells{w.cells, (int64_t)B}, w.keys, w.vals, B, w.best, w.heap_dS, w.heap_blk,
+            reinterpret_cast<double*>(w.keys_alt), w.vals_alt, w.parent, num_to_merge, team_warps, w.list_small,
+            w.list_big, 2 * g.N, d_merged, w.flags_dev);
+        count_launches(2);
+    } else {
+        chain_init(bm, w, (uint64_t)2 * (uint64_t)bm.nnz, st);
+        k_carry_out<HashCells><<<1, kCarryThreads, 0, st>>>(
+            g, bm, w.chain, HashCells{w.chain}, w.keys, w.vals, B, w.best, w.heap_dS, w.heap_blk,
+            reinterpret_cast<double*>(w.keys_alt), w.vals_alt, w.parent, num_to_merge, team_warps, w.list_small,
+            w.list_big, 2 * g.N, d_merged, w.flags_dev);
+        count_launches(1);
+    }
+}
+
+}  // namespace sbp

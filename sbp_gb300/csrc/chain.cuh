@@ -77,20 +77,34 @@ __device__ __forceinline__ void bulk_append(int32_t* head, const DevChain& ch, i
         for (int i = threadIdx.x; i < n; i += blockDim.x) ch.pool[p + i] = buf[i];
 }
 
-// Calls f(key) for every key of a row (or column): snapshot segment [lo, hi) of seg_idx
-// and the appended chunks starting at head.  Thread-strided; every thread returns.
+// Calls f(key) for every key held in the appended chunks of a list starting at head,
+// strided over threads t = 0..nt-1 of a team.
 template <typename F>
-__device__ __forceinline__ void chain_for_each(const int32_t* seg_idx, int32_t lo, int32_t hi, int32_t head,
-                                               const DevChain& ch, F f) {
-    for (int32_t j = lo + threadIdx.x; j < hi; j += blockDim.x) f(seg_idx[j]);
+__device__ __forceinline__ void chunks_for_each(int32_t head, const DevChain& ch, int t, int nt, F f) {
     int32_t c = head;
     int guard = 0;
     while (c >= 0 && guard < (1 << 26)) {
         const int32_t n = ((volatile int32_t*)ch.pool)[c + 1];
-        for (int i = threadIdx.x; i < n; i += blockDim.x) f(((volatile int32_t*)ch.pool)[c + 3 + i]);
+        for (int i = t; i < n; i += nt) f(((volatile int32_t*)ch.pool)[c + 3 + i]);
         c = ((volatile int32_t*)ch.pool)[c];
         ++guard;
     }
+}
+
+// Calls f(key) for every key of a row (or column): snapshot segment [lo, hi) of seg_idx
+// and the appended chunks starting at head, strided over threads t = 0..nt-1.
+template <typename F>
+__device__ __forceinline__ void list_for_each(const int32_t* seg_idx, int32_t lo, int32_t hi, int32_t head,
+                                              const DevChain& ch, int t, int nt, F f) {
+    for (int32_t j = lo + t; j < hi; j += nt) f(seg_idx[j]);
+    chunks_for_each(head, ch, t, nt, f);
+}
+
+// The same over all threads of the CTA.
+template <typename F>
+__device__ __forceinline__ void chain_for_each(const int32_t* seg_idx, int32_t lo, int32_t hi, int32_t head,
+                                               const DevChain& ch, F f) {
+    list_for_each(seg_idx, lo, hi, head, ch, threadIdx.x, blockDim.x, f);
 }
 
 // Block-wide sum of N int64 values (blockDim.x == kChainThreads); every thread gets the totals.

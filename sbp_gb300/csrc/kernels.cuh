@@ -52,6 +52,9 @@ struct Work {
     int32_t* dense_M = nullptr;        // [kDenseGlobalMax^2] (allocated when N allows)
     int32_t* dense_MT = nullptr;
     int32_t dense_cap = 0;             // largest B the dense matrices hold
+    // dense B x B cell values of the merge carry-out (allocated on demand within a budget)
+    int32_t* cells = nullptr;
+    uint64_t cells_elems = 0;
 };
 
 int ceil_log2(uint64_t x);
@@ -70,6 +73,8 @@ void launch_propose_batch(const DevGraph& g, const DevBM& bm, const int32_t* v, 
                           uint32_t c1, uint32_t c2, uint32_t c3, int32_t* out, cudaStream_t st);
 // Initialises the chain cell store from the current CSR (capacity for extra new keys).
 void chain_init(const DevBM& bm, Work& w, uint64_t extra_keys, cudaStream_t st);
+// Initialises only the chain's row / column key lists (empty appended chunks).
+void lists_init(const DevBM& bm, Work& w, cudaStream_t st);
 
 // ---- sweep.cu
 // Proposals for vlist[0..n) against the current snapshot (moves[v] = s or -1), then the
@@ -94,6 +99,12 @@ void merge_propose(const DevGraph& g, const DevBM& bm, uint64_t seed, uint32_t s
 // Carries out merges; writes the number done to w.d_scalar[1].  Leaves asg relabelled
 // to dense block ids (B - merges blocks); the caller rebuilds.
 void carry_out(const DevGraph& g, DevBM& bm, int64_t num_to_merge, int approximate, Work& w, cudaStream_t st);
+
+// ---- carry.cu
+// carry_out_best_merges_advanced over the queue (w.keys, w.vals) sorted by (delta, block)
+// with the union-find block map in w.parent (identity on entry).  Uses the dense cells
+// w.cells when B * B <= w.cells_elems, the chain hash otherwise.
+void carry_out_exact(const DevGraph& g, DevBM& bm, int64_t num_to_merge, Work& w, cudaStream_t st);
 
 // Launch accounting.
 int64_t kernel_launches();
