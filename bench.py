@@ -29,7 +29,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-CONFIG = "C2"
+CONFIG = "C2"  # --config
 SEED = 1
 METRIC = "proposals/s"
 
@@ -117,12 +117,15 @@ def ncu_traffic(kind):
         return None
 
 
-# Algorithmic bytes per launch of each kernel category (formulas stated in the design doc).
+# Algorithmic bytes of each kernel category over the timed steps.  A vertex proposal
+# reads its CSR offsets (8 B) and, per neighbour, the neighbour id and its block (8 B)
+# and the cell count and block degree it needs (12 B); the sampler and the special
+# cells add 64 B.  The sequential chain does the same work per visited vertex.
 def algorithmic_bytes(kind, stats):
     if kind == "gibbs_propose":
-        # per vertex proposal: CSR offsets 8 B, neighbour ids + their blocks 8 B per
-        # neighbour, per-neighbour cell lookups and degrees 12 B, sampler + specials 64 B.
         return 72 * stats["gibbs_proposals"] + 20 * stats["gibbs_edges"]
+    if kind == "mh_chain":
+        return 72 * (stats["proposals"] - stats["gibbs_proposals"]) + 20 * (stats["edges_swept"] - stats["gibbs_edges"])
     return None
 
 
@@ -171,6 +174,39 @@ def reference_arm(args):
     print(json.dumps(out))
 
 
+def profile_phase(args):
+    """One phase of the same workload at a fixed block count, for profilers: the planted
+    partition with every planted block split at random into sub-blocks (about --blocks
+    blocks in all), then either the merge pass to half as many blocks or --iterations
+    hybrid-MCMC iterations.  Prints a short JSON summary, not a bench line."""
+    import torch
+    import sbp_gb300 as sb
+    from sbp_gb300 import build as _b
+    _b.build()
+    src, dst, planted = sb.dcsbm.generate_config(CONFIG, seed=0)
+    n = sb.dcsbm.CONFIGS[CONFIG]["num_vertices"]
+    rng = np.random.default_rng(3)
+    k = max(1, -(-args.blocks // (int(planted.max()) + 1)))
+    _, a = np.unique(planted.astype(np.int64) * k + rng.integers(0, k, n), return_inverse=True)
+    a = a.astype(np.int32)
+    B = int(a.max()) + 1
+    ctx = sb.Context(0)
+    if args.cells_budget is not None:
+        ctx.set_cells_budget(args.cells_budget)
+    G = sb.Graph(n, src, dst, ctx=ctx)
+    bm = sb.Blockmodel(B, G, 0.5, a)
+    sargs = sb.Args(algorithm="hybrid_mcmc", seed=SEED, max_iterations=args.iterations)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    if args.phase == "merge":
+        _, st = sb.block_merge.merge_blocks(bm, G, args=sargs, step=0, num_blocks_to_merge=B // 2)
+    else:
+        _, st = sb.finetune.mcmc(0, G, bm, True, sargs)
+    ctx.synchronize()
+    print(json.dumps({"phase": args.phase, "config": CONFIG, "blocks_before": B, "blocks_after": bm.num_blocks(),
+                      "seconds": time.perf_counter() - t0, "stats": st}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -178,9 +214,20 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end C ABI run (profiling)")
+    ap.add_argument("--config", default=CONFIG, choices=["C1", "C2", "C3"])
+    ap.add_argument("--cells-budget", type=int, default=None,
+                    help="device bytes for the carry-out's dense cell counts (library default if unset)")
+    ap.add_argument("--phase", default="sbp", choices=["sbp", "merge", "mcmc"],
+                    help="merge / mcmc: one phase at --blocks blocks for profilers (no bench line)")
+    ap.add_argument("--blocks", type=int, default=1500)
+    ap.add_argument("--iterations", type=int, default=2)
     args = ap.parse_args()
+    globals()["CONFIG"] = args.config
     if args.impl == "reference":
         return reference_arm(args)
+    if args.phase != "sbp":
+        return profile_phase(args)
 
     import torch
     import sbp_gb300 as sb
@@ -194,6 +241,8 @@ def main():
     src, dst, planted = sb.dcsbm.generate_config(CONFIG, seed=0)
     n = sb.dcsbm.CONFIGS[CONFIG]["num_vertices"]
     ctx = sb.Context(local)
+    if args.cells_budget is not None:
+        ctx.set_cells_budget(args.cells_budget)
     G = sb.Graph(n, src, dst, ctx=ctx)  # resident in HBM before the timed region
     sargs = sb.Args(algorithm="hybrid_mcmc", seed=SEED)
     stream = torch.cuda.ExternalStream(ctx.lib.sbpgpu_ctx_stream(ctx.h), device=local)
@@ -242,7 +291,7 @@ def main():
 
     # end to end through the C ABI with host buffers: graph upload + partition + result read
     e2e_s, e2e_props = 0.0, 0
-    for _ in range(max(1, min(args.steps, 2))):
+    for _ in range(0 if args.no_e2e else max(1, min(args.steps, 2))):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         Gh = sb.Graph(n, src, dst, ctx=ctx)
@@ -284,8 +333,8 @@ def main():
            "merge_proposals_per_step": totals["merge_proposals"] / args.steps,
            "edges_swept_per_s": totals["edges_swept"] / device_s,
            "kernel_ms": cats, "gpu_launches": int(totals["kernel_launches"]),
-           "e2e": {"value": e2e_props / e2e_s, "unit": METRIC, "h2d_bytes_per_step": h2d,
-                   "d2h_bytes_per_step": d2h},
+           "e2e": {"value": e2e_props / e2e_s if e2e_s > 0 else None, "unit": METRIC,
+                   "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
            "roofline": roof, "clocks": clk}
     if rank == 0 and not args.no_cpu_baseline:
         out["cpu_baseline"] = run_cpu_baseline(src, dst, n)
