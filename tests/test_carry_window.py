@@ -1,0 +1,119 @@
+"""Host model of the windowed merge carry-out (sbp_gb300/csrc/carry.cu) against the
+reference's one-at-a-time queue loop (src/block_merge.cpp:54-95).
+
+The device evaluates the W smallest live entries against one blockmodel state and replays
+the pop / put-back / merge rule over those values.  This model applies the same selection,
+replay and put-back buffering (shared buffer of capacity QS spilling into a sorted run)
+with a stand-in for the recomputed delta that changes whenever a merge changes the state,
+and must produce exactly the sequential loop's merges, in order."""
+import heapq
+import random
+
+import pytest
+
+
+def _instance(seed, B):
+    rng = random.Random(seed)
+    best = [rng.randrange(B) for _ in range(B)]
+    for i in range(B):
+        if best[i] == i:
+            best[i] = (i + 1) % B
+    # integer-valued deltas make ties common
+    d0 = [rng.choice([rng.uniform(-5, 5), float(rng.randrange(-3, 3))]) for _ in range(B)]
+    return best, d0
+
+
+def _recomputed(frm, to, version, seed):
+    r = random.Random(hash((frm, to, version, seed)))
+    return r.choice([r.uniform(-6, 6), float(r.randrange(-3, 4))])
+
+
+def _find(parent, x):
+    while parent[x] != x:
+        x = parent[x]
+    return x
+
+
+def _sequential(best, d0, ntm, seed):
+    q = [(d0[i], i) for i in range(len(best))]
+    heapq.heapify(q)
+    parent = list(range(len(best)))
+    version, merges = 0, []
+    while len(merges) < ntm and q:
+        _, frm = heapq.heappop(q)
+        to = _find(parent, best[frm])
+        if to == frm:
+            continue
+        act = _recomputed(frm, to, version, seed)
+        if q and act > q[0][0]:
+            heapq.heappush(q, (act, frm))
+            continue
+        parent[frm] = to
+        version += 1
+        merges.append((frm, to))
+    return merges
+
+
+def _windowed(best, d0, ntm, seed, W, QS):
+    P = sorted((d0[i], i) for i in range(len(best)))
+    p, R, q, S = 0, [], 0, []
+    parent = list(range(len(best)))
+    version, merges = 0, []
+    while len(merges) < ntm:
+        heads = [P[p:p + W + 1], R[q:q + W + 1], S[:W + 1]]
+        items = sorted((it, src) for src in range(3) for it in heads[src])
+        ncand = min(W, len(items))
+        if ncand == 0:
+            break
+        cands = items[:ncand]
+        bound = items[W][0] if len(items) > W else None
+        evals = []
+        for (_, frm), _src in cands:
+            to = _find(parent, best[frm])
+            evals.append((to, _recomputed(frm, to, version, seed) if to != frm else None))
+        i, Q, cons, mf = 0, [], [0, 0, 0], None
+        while True:
+            pick = None
+            if i < ncand:
+                pick = ("c", cands[i][0])
+            if Q and (pick is None or (Q[0][0], Q[0][1]) < pick[1]):
+                pick = ("q", (Q[0][0], Q[0][1]))
+            if pick is None or (bound is not None and bound < pick[1]):
+                break
+            if pick[0] == "q":
+                mf = (Q[0][1], Q[0][2])
+                Q.pop(0)
+                break
+            (_, frm), src = cands[i]
+            to, act = evals[i]
+            cons[src] += 1
+            i += 1
+            if to == frm:
+                continue
+            heads_left = [x for x in (bound[0] if bound else None, cands[i][0][0] if i < ncand else None,
+                                      Q[0][0] if Q else None) if x is not None]
+            if heads_left and act > min(heads_left):
+                Q.append((act, frm, to))
+                Q.sort()
+                continue
+            mf = (frm, to)
+            break
+        p += cons[0]
+        q += cons[1]
+        S = sorted(S[cons[2]:] + [(a, f) for a, f, _t in Q])
+        if len(S) > QS - W - 1:
+            R, q, S = sorted(R[q:] + S), 0, []
+        if mf:
+            parent[mf[0]] = mf[1]
+            version += 1
+            merges.append(mf)
+    return merges
+
+
+@pytest.mark.parametrize("W,QS", [(1, 8), (3, 12), (16, 40), (16, 1024)])
+def test_windowed_carry_out_matches_sequential_queue(W, QS):
+    for seed in range(150):
+        B = random.Random(seed).randrange(2, 250)
+        best, d0 = _instance(seed, B)
+        ntm = random.Random(seed + 1).randrange(1, B)
+        assert _windowed(best, d0, ntm, seed, W, QS) == _sequential(best, d0, ntm, seed), (seed, B)
