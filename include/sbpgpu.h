@@ -109,6 +109,16 @@ sbpgpu_status sbpgpu_mdl(sbpgpu_bm* bm, double* out);
  * vertex[i] -> proposal[i] against the current blockmodel. */
 sbpgpu_status sbpgpu_delta_mdl_batch(sbpgpu_bm* bm, int64_t n, const int32_t* vertex,
                                      const int32_t* proposal, double* out_delta);
+/* The same as sbpgpu_delta_mdl_batch, for callers that must not allocate device memory
+ * while they score moves (a cudaMalloc can synchronise the device, or fail when the GPU's
+ * memory is committed elsewhere).  No counterpart in the reference.  The ids, proposals
+ * and results are staged in a fixed 1 MiB device array built into the library, so n is at
+ * most 65536; larger batches return SBPGPU_EINVAL.  The first call on a device looks the
+ * array up (cudaGetSymbolAddress); make that first call before any stream capture.
+ * Nothing needs zeroing beforehand.  Calls that overlap in time on the same device, from
+ * any thread or context, share the array and race: serialise them. */
+sbpgpu_status sbpgpu_delta_mdl_batch_noalloc(sbpgpu_bm* bm, int64_t n, const int32_t* vertex,
+                                             const int32_t* proposal, double* out_delta);
 /* entropy::block_merge_delta_mdl (src/entropy.cpp:129-182) for n merges block[i] -> proposal[i]. */
 sbpgpu_status sbpgpu_merge_delta_mdl_batch(sbpgpu_bm* bm, int64_t n, const int32_t* block,
                                            const int32_t* proposal, double* out_delta);

@@ -79,6 +79,7 @@ SIGNATURES = {
     "sbpgpu_bm_entropy": (ctypes.c_double, [vp]),
     "sbpgpu_mdl": (ctypes.c_int, [vp, f64p]),
     "sbpgpu_delta_mdl_batch": (ctypes.c_int, [vp, ctypes.c_int64, i32p, i32p, f64p]),
+    "sbpgpu_delta_mdl_batch_noalloc": (ctypes.c_int, [vp, ctypes.c_int64, i32p, i32p, f64p]),
     "sbpgpu_merge_delta_mdl_batch": (ctypes.c_int, [vp, ctypes.c_int64, i32p, i32p, f64p]),
     "sbpgpu_propose_batch": (ctypes.c_int, [vp, ctypes.c_int64, i32p, ctypes.c_uint64, ctypes.c_uint32,
                                             ctypes.c_uint32, ctypes.c_uint32, i32p]),

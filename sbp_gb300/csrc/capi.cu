@@ -19,6 +19,7 @@
 
 #include "../../include/sbpgpu.h"
 #include "kernels.cuh"
+#include "noalloc.cuh"
 #include "prims.cuh"
 
 using namespace sbp;
@@ -897,6 +898,36 @@ sbpgpu_status sbpgpu_delta_mdl_batch(sbpgpu_bm* bm, int64_t n, const int32_t* ve
         }
         free_all(tmp);
         for (int64_t i = 0; i < n; ++i) out[i] = (double)h[i] * (1.0 / 16777216.0);
+        return SBPGPU_OK;
+    });
+}
+
+sbpgpu_status sbpgpu_delta_mdl_batch_noalloc(sbpgpu_bm* bm, int64_t n, const int32_t* vertex,
+                                             const int32_t* proposal, double* out) {
+    if (!bm || n < 0 || (n && (!vertex || !proposal || !out))) return SBPGPU_EINVAL;
+    sbpgpu_graph* g = bm->g;
+    return guarded(g->ctx, [&] {
+        if (n == 0) return SBPGPU_OK;
+        if (n > kNoAllocMaxBatch)
+            throw ApiError(SBPGPU_EINVAL, "batch of " + std::to_string(n) + " exceeds the allocation-free limit of " +
+                                              std::to_string(kNoAllocMaxBatch) + " entries");
+        int32_t max_k = 0;
+        for (int64_t i = 0; i < n; ++i) {
+            if (vertex[i] < 0 || vertex[i] >= g->N || proposal[i] < 0 || proposal[i] >= bm->d.B)
+                throw ApiError(SBPGPU_EINVAL, "vertex or proposal out of range");
+            max_k = std::max(max_k, g->kdeg[vertex[i]]);
+        }
+        if (max_k > 8192) throw ApiError(SBPGPU_EUNSUPPORTED, "vertex degree above 8192");
+        NoAllocScratch sc{};
+        std::string err;
+        if (!noalloc_scratch(g->ctx->device, &sc, &err)) throw ApiError(SBPGPU_EDEVICE, err);
+        cudaStream_t st = g->ctx->stream;
+        CK(cudaMemcpyAsync(sc.vertex, vertex, n * 4, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(sc.proposal, proposal, n * 4, cudaMemcpyHostToDevice, st));
+        launch_vertex_dS_batch(g->dg, bm->d, sc.vertex, sc.proposal, n, max_k, sc.result, g->w, st);
+        launch_fixed_to_double(sc.result, n, st);
+        CK(cudaMemcpyAsync(out, sc.result, n * 8, cudaMemcpyDeviceToHost, st));
+        check_flags(g);
         return SBPGPU_OK;
     });
 }
