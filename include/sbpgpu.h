@@ -55,6 +55,8 @@ typedef struct sbpgpu_stats {
     int64_t kernel_launches;  /* kernels launched by this library for the call */
     int64_t gibbs_proposals;  /* vertex proposals of the parallel (asynchronous Gibbs) phases */
     int64_t gibbs_edges;      /* sum of k_out + k_in over those proposals */
+    int64_t chain_rounds;     /* windows evaluated by the sequential MH chain */
+    int64_t carry_rounds;     /* windows evaluated by the merge carry-out */
 } sbpgpu_stats;
 
 void sbpgpu_default_config(sbpgpu_config* cfg);

@@ -319,6 +319,8 @@ void harvest_counters(sbpgpu_graph* g) {
     g->st.edges_swept += (int64_t)f.counters[3] + (int64_t)f.counters[4];
     g->st.gibbs_edges += (int64_t)f.counters[3];
     g->st.merge_proposals += (int64_t)f.counters[6];
+    g->st.chain_rounds += (int64_t)f.counters[8];
+    g->st.carry_rounds += (int64_t)f.counters[0];
     reset_counters(g);
 }
 
@@ -338,7 +340,13 @@ void gibbs_batch_dev(sbpgpu_bm* bm, const int32_t* list, int32_t n, uint64_t see
 void chain_run(sbpgpu_bm* bm, const int32_t* order, int32_t n, int32_t max_k, int64_t k_sum, uint64_t seed,
                uint32_t it, uint32_t step, int greedy) {
     sbpgpu_graph* g = bm->g;
-    if (bm->d.B <= kDenseMax || bm->d.B <= g->w.dense_cap) {
+    bool shared_cells = false;
+    int log2cap = 0;
+    const size_t gcells = g->w.dense_M ? (size_t)g->w.dense_cap * (size_t)g->w.dense_cap : 0;
+    if (mh_window_plan(bm->d.B, max_k, gcells, &shared_cells, &log2cap) >= 2) {
+        Span sp(g->ctx, 1);
+        mh_chain_window(g->dg, bm->d, order, n, max_k, seed, it, step, g->w, g->ctx->stream);
+    } else if (bm->d.B <= kDenseMax || bm->d.B <= g->w.dense_cap) {
         Span sp(g->ctx, 1);
         mh_chain_dense(g->dg, bm->d, order, n, seed, it, step, g->w, g->ctx->stream);
     } else {

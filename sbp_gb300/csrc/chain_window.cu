@@ -1,0 +1,591 @@
+// Sequential Metropolis-Hastings chain of hybrid MCMC (reference src/finetune.cpp:589-594;
+// propose_move :842-869, move_vertex :822-840, Blockmodel::move_vertex(Vertex, Delta,
+// proposal) src/blockmodel/blockmodel.cpp:408-435), evaluated in windows.
+//
+// The chain visits vertices in order and applies each accepted move before the next
+// proposal.  A proposal and its delta read only
+//   * the blocks of the vertex's neighbours, r = its block, s = the proposal, nb = the
+//     block of the sampled neighbour,
+//   * cells of rows / columns r and s (and of nb, for the sampler), block degrees and
+//     sizes of those blocks,
+// so a move u: a -> b can change the outcome of a later vertex v only if a or b lies in
+// T(v) = {r, s, nb} + v's neighbour blocks, or nb(v) lies in T(u) (u's neighbours in
+// block nb shift counts of row / column nb between columns / rows a and b).  Each round
+// therefore evaluates the next W vertices of the order at once (one warp each) against
+// the same state; one thread replays them in order and stops before the first vertex
+// that an earlier accepted move of the round may have changed; the accepted moves are
+// then applied together (every update is an addition, so their order does not matter).
+// The result equals the one-vertex-at-a-time chain exactly.
+//
+// Cell counts: B x B dense in shared memory (B <= kWinSharedMax) or dense M and its
+// transpose in global memory (leading dimension a multiple of 4); degrees and sizes in
+// shared memory.  Only the assignment is written back; the caller rebuilds afterwards.
+#include "delta.cuh"
+#include "kernels.cuh"
+
+namespace sbp {
+
+namespace {
+
+constexpr int kWinMaxWarps = 16;
+
+enum : int32_t { ST_SKIP = 0, ST_NOMOVE = 1, ST_REJECT = 2, ST_ACCEPT = 3 };
+
+struct SharedCells {
+    const int32_t* M;
+    int32_t ld;
+    __device__ __forceinline__ int32_t row_get(int32_t r, int32_t c) const { return M[r * ld + c]; }
+    __device__ __forceinline__ int32_t col_get(int32_t c, int32_t r) const { return M[r * ld + c]; }
+};
+
+struct GlobalCells {
+    const int32_t* M;
+    const int32_t* MT;
+    int64_t ld;
+    __device__ __forceinline__ int32_t row_get(int32_t r, int32_t c) const { return __ldcg(M + r * ld + c); }
+    __device__ __forceinline__ int32_t col_get(int32_t c, int32_t r) const { return __ldcg(MT + c * ld + r); }
+};
+
+struct WinResult {
+    long long dS;
+    int32_t v, r, s, nb, status, k, kout, kin, L;
+};
+
+// Entry at cumulative unit t in ascending index order over x(i), i < B, one warp.
+// get(i) returns the weight of index i.  Returns -1 when t is out of range.
+template <typename Get>
+__device__ __forceinline__ int32_t warp_select(int32_t B, long long t, Get get) {
+    const int lane = threadIdx.x & 31;
+    for (int32_t base = 0; base < B; base += 32) {
+        const int32_t i = base + lane;
+        const long long x = i < B ? (long long)get(i) : 0ll;
+        long long incl = x;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const long long y = __shfl_up_sync(SBP_FULL_MASK, incl, o);
+            if (lane >= o) incl += y;
+        }
+        const long long tot = __shfl_sync(SBP_FULL_MASK, incl, 31);
+        if (t < tot) {
+            const unsigned hit = __ballot_sync(SBP_FULL_MASK, incl > t);
+            return base + __ffs(hit) - 1;
+        }
+        t -= tot;
+    }
+    return -1;
+}
+
+// The same over a 16-byte aligned global row (ld a multiple of 4): 128 entries per step.
+__device__ __forceinline__ int32_t warp_select_row4(const int32_t* __restrict__ row, int32_t B, long long t,
+                                                    int32_t skip) {
+    const int lane = threadIdx.x & 31;
+    for (int32_t base = 0; base < B; base += 128) {
+        const int32_t i = base + 4 * lane;
+        int4 q = make_int4(0, 0, 0, 0);
+        if (i < B) q = __ldcg(reinterpret_cast<const int4*>(row + i));
+        int32_t x[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            if (i + j >= B || i + j == skip) x[j] = 0;
+        const long long s4 = (long long)x[0] + x[1] + x[2] + x[3];
+        long long incl = s4;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const long long y = __shfl_up_sync(SBP_FULL_MASK, incl, o);
+            if (lane >= o) incl += y;
+        }
+        const long long tot = __shfl_sync(SBP_FULL_MASK, incl, 31);
+        if (t < tot) {
+            const unsigned hit = __ballot_sync(SBP_FULL_MASK, incl > t);
+            const int src = __ffs(hit) - 1;
+            int32_t pick = -1;
+            if (lane == src) {
+                long long u = t - (incl - s4);
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    if (pick < 0 && u < x[j]) pick = i + j;
+                    u -= x[j];
+                }
+            }
+            return __shfl_sync(SBP_FULL_MASK, pick, src);
+        }
+        t -= tot;
+    }
+    return -1;
+}
+
+__device__ __forceinline__ bool hash_has(const int32_t* hk, int log2cap, int32_t b) {
+    const uint32_t mask = (1u << log2cap) - 1u;
+    uint32_t s = hslot(b, log2cap);
+    for (uint32_t probe = 0; probe <= mask; ++probe) {
+        const int32_t k = hk[s];
+        if (k == b) return true;
+        if (k == -1) return false;
+        s = (s + 1) & mask;
+    }
+    return false;
+}
+
+__device__ __forceinline__ int32_t hash_get(const int32_t* hk, const int32_t* cnt, int log2cap, int32_t b) {
+    const uint32_t mask = (1u << log2cap) - 1u;
+    uint32_t s = hslot(b, log2cap);
+    for (uint32_t probe = 0; probe <= mask; ++probe) {
+        const int32_t k = hk[s];
+        if (k == b) return cnt[s];
+        if (k == -1) return 0;
+        s = (s + 1) & mask;
+    }
+    return 0;
+}
+
+// Two-level select over a 16-byte aligned global row (ld a multiple of 4): the sums of
+// 32 tiles of 128 entries are read with independent coalesced loads, a scan over them
+// finds the tile, and one pass over that tile finds the entry.
+__device__ __forceinline__ int32_t warp_select_row2(const int32_t* __restrict__ row, int32_t B, long long t,
+                                                    int32_t skip) {
+    const int lane = threadIdx.x & 31;
+    const int ntiles = (B + 127) >> 7;
+    for (int tb = 0; tb < ntiles; tb += 32) {
+        long long mine = 0;  // lane q: sum of tile tb + q
+#pragma unroll 8
+        for (int q = 0; q < 32; ++q) {
+            const int32_t i = ((tb + q) << 7) + 4 * lane;
+            long long s4 = 0;
+            if (tb + q < ntiles && i < B) {
+                const int4 x = __ldcg(reinterpret_cast<const int4*>(row + i));
+                s4 = (long long)(i == skip ? 0 : x.x) + (i + 1 >= B || i + 1 == skip ? 0 : x.y) +
+                     (i + 2 >= B || i + 2 == skip ? 0 : x.z) + (i + 3 >= B || i + 3 == skip ? 0 : x.w);
+            }
+            s4 = warp_sum_ll(s4);
+            if (lane == q) mine = s4;
+        }
+        long long incl = mine;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const long long y = __shfl_up_sync(SBP_FULL_MASK, incl, o);
+            if (lane >= o) incl += y;
+        }
+        const long long tot = __shfl_sync(SBP_FULL_MASK, incl, 31);
+        if (t < tot) {
+            const int src = __ffs(__ballot_sync(SBP_FULL_MASK, incl > t)) - 1;
+            const long long before = __shfl_sync(SBP_FULL_MASK, incl - mine, src);
+            const int32_t base = (tb + src) << 7;
+            const int32_t r = warp_select_row4(row + base, min(128, B - base), t - before, skip - base);
+            return r < 0 ? -1 : base + r;
+        }
+        t -= tot;
+    }
+    return -1;
+}
+
+// Neighbour-block counts of v into the warp's hash (edge_weights + the block lookups of
+// blockmodel_delta): out-neighbours except v itself into hO, in-neighbours (self-loops
+// already excluded) into hI.  Neighbour ids, then their blocks, are loaded 8 per lane
+// before any insert.
+__device__ __forceinline__ void warp_gather(const DevGraph& g, const int32_t* asg, int32_t v, int32_t o0,
+                                            int32_t kout, int32_t i0, int32_t k, int32_t* hk, int32_t* hO,
+                                            int32_t* hI, int log2cap) {
+    const int lane = threadIdx.x & 31;
+    const int cap = 1 << log2cap;
+    for (int i = lane; i < cap; i += 32) {
+        hk[i] = -1;
+        hO[i] = 0;
+        hI[i] = 0;
+    }
+    __syncwarp();
+    for (int32_t base = 0; base < k; base += 256) {
+        int32_t u[8], b[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int32_t idx = base + lane + 32 * j;
+            u[j] = idx < k ? (idx < kout ? __ldg(g.out_nbr + o0 + idx) : __ldg(g.inns_nbr + i0 + idx - kout)) : -1;
+        }
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int32_t idx = base + lane + 32 * j;
+            b[j] = (u[j] >= 0 && !(idx < kout && u[j] == v)) ? __ldcg(asg + u[j]) : -1;
+        }
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int32_t idx = base + lane + 32 * j;
+            if (b[j] >= 0) hinsert(hk, idx < kout ? hO : hI, log2cap, b[j]);
+        }
+    }
+    __syncwarp();
+}
+
+// entropy::delta_mdl for moving v from r to s over the gathered neighbour blocks; the same
+// terms as vertex_delta_fixed (exact int64, units of 2^-24), with the occupied hash slots
+// compacted into items[] and every cell of a pass loaded before it is used.
+template <class Cells>
+__device__ long long warp_delta(const DevGraph& g, const int32_t* d_out, const int32_t* d_in, const Cells& M,
+                                int32_t r, int32_t s, int32_t kout, int32_t kin, int32_t L, const int32_t* hk,
+                                const int32_t* hO, const int32_t* hI, int log2cap, int32_t* items) {
+    const int lane = threadIdx.x & 31;
+    const int cap = 1 << log2cap;
+    const LogTab Lq{g.Lq, g.E + 1};
+    int32_t Or = 0, Ir = 0, Os = 0, Is = 0, n = 0;
+    for (int base = 0; base < cap; base += 32) {
+        const int i = base + lane;
+        const int32_t b = hk[i];
+        if (b == r) {
+            Or = hO[i];
+            Ir = hI[i];
+        } else if (b == s) {
+            Os = hO[i];
+            Is = hI[i];
+        }
+        const bool it = b >= 0 && b != r && b != s;
+        const unsigned m = __ballot_sync(SBP_FULL_MASK, it);
+        if (it) items[n + __popc(m & lanemask_lt())] = i;
+        n += __popc(m);
+    }
+    Or = warp_sum_i(Or);
+    Ir = warp_sum_i(Ir);
+    Os = warp_sum_i(Os);
+    Is = warp_sum_i(Is);
+    __syncwarp();
+    const int32_t selfw = L > 0 ? 1 : 0;
+    const int32_t dout_r = d_out[r], dout_s = d_out[s], din_r = d_in[r], din_s = d_in[s];
+    const int32_t dout_r2 = dout_r - kout, dout_s2 = dout_s + kout;
+    const int32_t din_r2 = din_r - (kin + selfw), din_s2 = din_s + (kin + selfw);
+    long long acc = 0, sRo = 0, sSo = 0, sRi = 0, sSi = 0;
+    for (int j0 = 0; j0 < n; j0 += 128) {
+        int32_t b[4], O[4], I[4], Mrb[4], Msb[4], Mbr[4], Mbs[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int jj = j0 + lane + 32 * q;
+            const int sl = jj < n ? items[jj] : -1;
+            b[q] = sl >= 0 ? hk[sl] : -1;
+            O[q] = sl >= 0 ? hO[sl] : 0;
+            I[q] = sl >= 0 ? hI[sl] : 0;
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            Mrb[q] = O[q] > 0 ? M.row_get(r, b[q]) : 0;
+            Msb[q] = O[q] > 0 ? M.row_get(s, b[q]) : 0;
+            Mbr[q] = I[q] > 0 ? M.col_get(r, b[q]) : 0;
+            Mbs[q] = I[q] > 0 ? M.col_get(s, b[q]) : 0;
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            if (b[q] < 0) continue;
+            if (O[q] > 0) {
+                const int32_t dinb = d_in[b[q]];
+                acc += ce_fixed(Lq, Mrb[q], dinb, dout_r) - ce_fixed(Lq, Mrb[q] - O[q], dinb, dout_r2);
+                acc += ce_fixed(Lq, Msb[q], dinb, dout_s) - ce_fixed(Lq, Msb[q] + O[q], dinb, dout_s2);
+                sRo += Mrb[q];
+                sSo += Msb[q];
+            }
+            if (I[q] > 0) {
+                const int32_t doutb = d_out[b[q]];
+                acc += ce_fixed(Lq, Mbr[q], din_r, doutb) - ce_fixed(Lq, Mbr[q] - I[q], din_r2, doutb);
+                acc += ce_fixed(Lq, Mbs[q], din_s, doutb) - ce_fixed(Lq, Mbs[q] + I[q], din_s2, doutb);
+                sRi += Mbr[q];
+                sSi += Mbs[q];
+            }
+        }
+    }
+    acc = warp_sum_ll(acc);
+    sRo = warp_sum_ll(sRo);
+    sSo = warp_sum_ll(sSo);
+    sRi = warp_sum_ll(sRi);
+    sSi = warp_sum_ll(sSi);
+    const int32_t Mrr = M.row_get(r, r), Mrs = M.row_get(r, s), Msr = M.row_get(s, r), Mss = M.row_get(s, s);
+    long long tot = acc;
+    {
+        const int32_t d = -Or - Ir - L;
+        if (Or | Ir | L) tot += ce_fixed(Lq, Mrr, din_r, dout_r) - ce_fixed(Lq, Mrr + d, din_r2, dout_r2);
+        else tot += ce_delta(Lq, Mrr, din_r, dout_r, din_r2, dout_r2);
+    }
+    {
+        const int32_t d = Ir - Os;
+        if (Os | Ir) tot += ce_fixed(Lq, Mrs, din_s, dout_r) - ce_fixed(Lq, Mrs + d, din_s2, dout_r2);
+        if (d == 0) tot += ce_delta(Lq, Mrs, din_s, dout_r, din_s2, dout_r2);
+    }
+    {
+        const int32_t d = Or - Is;
+        if (Or | Is) tot += ce_fixed(Lq, Msr, din_r, dout_s) - ce_fixed(Lq, Msr + d, din_r2, dout_s2);
+        if (d == 0) tot += ce_delta(Lq, Msr, din_r, dout_s, din_r2, dout_s2);
+    }
+    {
+        const int32_t d = Os + Is + L;
+        if (Os | Is | L) tot += ce_fixed(Lq, Mss, din_s, dout_s) - ce_fixed(Lq, Mss + d, din_s2, dout_s2);
+        else tot += ce_delta(Lq, Mss, din_s, dout_s, din_s2, dout_s2);
+    }
+    tot += ((long long)dout_r - Mrr - Mrs - sRo) * (Lx(Lq, dout_r2) - Lx(Lq, dout_r));
+    tot += ((long long)dout_s - Msr - Mss - sSo) * (Lx(Lq, dout_s2) - Lx(Lq, dout_s));
+    tot += ((long long)din_r - Mrr - Msr - sRi) * (Lx(Lq, din_r2) - Lx(Lq, din_r));
+    tot += ((long long)din_s - Mrs - Mss - sSi) * (Lx(Lq, din_s2) - Lx(Lq, din_s));
+    return tot;
+}
+
+// x in T(candidate)?
+__device__ __forceinline__ bool in_touched(const WinResult& c, const int32_t* hk, int log2cap, int32_t x) {
+    if (x == c.r) return true;
+    if (c.status >= ST_NOMOVE && x == c.nb) return true;
+    if (c.status >= ST_REJECT && (x == c.s || hash_has(hk, log2cap, x))) return true;
+    return false;
+}
+
+template <bool kShared>
+__global__ void __launch_bounds__(kWinMaxWarps * 32, 1)
+    k_mh_window(DevGraph g, DevBM bm, const int32_t* __restrict__ order, int32_t n, uint64_t seed, uint32_t iter,
+                uint32_t step, int32_t* gM, int32_t* gMT, int32_t ld, int log2cap, int nwarps, DevFlags* flags) {
+    extern __shared__ int32_t sm[];
+    const int32_t B = bm.B;
+    const int cap = 1 << log2cap;
+    int32_t* dout = sm;
+    int32_t* din = dout + B;
+    int32_t* size = din + B;
+    int32_t* hash = size + B;               // nwarps x (keys, out counts, in counts, items) x cap
+    int32_t* M = hash + 4 * cap * nwarps;  // shared cells (kShared): B rows of ld
+    __shared__ WinResult res[kWinMaxWarps];
+    __shared__ int32_t s_consumed, s_acc_mask;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const int nt = nwarps * 32;
+    int32_t* hk = hash + 4 * cap * wid;
+    int32_t* hO = hk + cap;
+    int32_t* hI = hO + cap;
+    int32_t* items = hI + cap;
+
+    if (kShared) {
+        for (int i = tid; i < B * ld; i += nt) M[i] = 0;
+        __syncthreads();
+        for (int32_t j = tid; j < bm.nnz; j += nt) M[bm.row_of[j] * ld + bm.row_col[j]] = bm.row_cnt[j];
+    }
+    for (int b = tid; b < B; b += nt) {
+        dout[b] = bm.d_out[b];
+        din[b] = bm.d_in[b];
+        size[b] = bm.sizes[b];
+    }
+    __syncthreads();
+    const SharedCells sc{M, ld};
+    const GlobalCells gc{gM, gMT, (int64_t)ld};
+
+    unsigned long long edges = 0, moved = 0, rounds = 0;
+    long long dsum = 0;
+    int32_t it0 = 0;
+    int guard = 0;
+    while (it0 < n && guard++ < (1 << 30)) {
+        const int wn = min(nwarps, n - it0);
+        // ---- evaluate the next wn vertices against the current state, one warp each
+        if (wid < wn) {
+            WinResult c;
+            c.v = order[it0 + wid];
+            c.r = __ldcg(bm.asg + c.v);
+            c.s = -1;
+            c.nb = -1;
+            c.dS = 0;
+            const int32_t o0 = __ldg(g.out_off + c.v), o1 = __ldg(g.out_off + c.v + 1);
+            const int32_t i0 = __ldg(g.inns_off + c.v), i1 = __ldg(g.inns_off + c.v + 1);
+            c.kout = o1 - o0;
+            c.kin = i1 - i0;
+            c.k = c.kout + c.kin;
+            c.L = __ldg(g.selfcnt + c.v);
+            c.status = ST_SKIP;
+            if (size[c.r] != 1) {  // a singleton block never moves (finetune.cpp:845)
+                uint32_t w[4];
+                philox4x32_10((uint32_t)c.v, iter, step, DOM_MH, seed, w);
+                int32_t s;
+                if (c.k == 0) {
+                    s = random_block(c.r, B, w[1]);
+                } else {
+                    // common::propose_new_block: uniform neighbour, then a multinomial over
+                    // nb's row (ascending column) followed by its column without the diagonal
+                    const int32_t idx = (int32_t)u32_below(w[0], (uint32_t)c.k);
+                    const int32_t nbr = idx < c.kout ? __ldg(g.out_nbr + o0 + idx) : __ldg(g.inns_nbr + i0 + idx - c.kout);
+                    const int32_t nb = __ldcg(bm.asg + nbr);
+                    c.nb = nb;
+                    const int32_t dnn = kShared ? sc.row_get(nb, nb) : gc.row_get(nb, nb);
+                    const long long R = dout[nb], C = (long long)din[nb] - dnn;
+                    long long t = (long long)u64_below(w[1], w[2], (uint64_t)(R + C));
+                    if (t < R) {
+                        s = kShared ? warp_select(B, t, [&](int32_t i) { return sc.row_get(nb, i); })
+                                    : warp_select_row2(gM + (int64_t)nb * ld, B, t, -1);
+                    } else {
+                        t -= R;
+                        s = kShared ? warp_select(B, t, [&](int32_t i) { return i == nb ? 0 : sc.row_get(i, nb); })
+                                    : warp_select_row2(gMT + (int64_t)nb * ld, B, t, nb);
+                    }
+                }
+                if (s < 0) {
+                    if (lane == 0) atomicOr(&flags->err, ERR_SELECT);
+                    c.status = ST_SKIP;
+                } else if (s == c.r) {
+                    c.status = ST_NOMOVE;
+                } else {
+                    c.s = s;
+                    warp_gather(g, bm.asg, c.v, o0, c.kout, i0, c.k, hk, hO, hI, log2cap);
+                    c.dS = kShared ? warp_delta(g, dout, din, sc, c.r, s, c.kout, c.kin, c.L, hk, hO, hI, log2cap, items)
+                                   : warp_delta(g, dout, din, gc, c.r, s, c.kout, c.kin, c.L, hk, hO, hI, log2cap, items);
+                    c.status = c.dS < 0 ? ST_ACCEPT : ST_REJECT;  // greedy accept (finetune.cpp:22-25)
+                }
+            }
+            if (lane == 0) res[wid] = c;
+        }
+        __syncthreads();
+        // ---- replay in order; stop before the first vertex an accepted move may change
+        if (tid == 0) {
+            int consumed = 0, acc_mask = 0;
+            for (int j = 0; j < wn; ++j) {
+                const WinResult& cj = res[j];
+                const int32_t* hkj = hash + 4 * cap * j;
+                bool valid = true;
+                for (int u = 0; u < j && valid; ++u) {
+                    if (!((acc_mask >> u) & 1)) continue;
+                    const WinResult& cu = res[u];
+                    const int32_t* hku = hash + 4 * cap * u;
+                    if (in_touched(cj, hkj, log2cap, cu.r) || in_touched(cj, hkj, log2cap, cu.s) ||
+                        (cj.nb >= 0 && in_touched(cu, hku, log2cap, cj.nb)))
+                        valid = false;
+                }
+                if (!valid) break;
+                consumed = j + 1;
+                edges += cj.k;
+                if (cj.status == ST_ACCEPT) {
+                    acc_mask |= 1 << j;
+                    moved++;
+                    dsum += cj.dS;
+                }
+            }
+            s_consumed = consumed;
+            s_acc_mask = acc_mask;
+            ++rounds;
+        }
+        __syncthreads();
+        // ---- apply the accepted moves (Blockmodel::move_vertex, blockmodel.cpp:408-435)
+        if (wid < wn && ((s_acc_mask >> wid) & 1)) {
+            const WinResult c = res[wid];
+            const int32_t r = c.r, s = c.s;
+            for (int i = lane; i < cap; i += 32) {
+                const int32_t b = hk[i];
+                if (b < 0 || b == r || b == s) continue;
+                const int32_t O = hO[i], I = hI[i];
+                if (kShared) {
+                    if (O) {
+                        atomicAdd(M + r * ld + b, -O);
+                        atomicAdd(M + s * ld + b, O);
+                    }
+                    if (I) {
+                        atomicAdd(M + b * ld + r, -I);
+                        atomicAdd(M + b * ld + s, I);
+                    }
+                } else {
+                    if (O) {
+                        atomicAdd(gM + (int64_t)r * ld + b, -O);
+                        atomicAdd(gM + (int64_t)s * ld + b, O);
+                        atomicAdd(gMT + (int64_t)b * ld + r, -O);
+                        atomicAdd(gMT + (int64_t)b * ld + s, O);
+                    }
+                    if (I) {
+                        atomicAdd(gM + (int64_t)b * ld + r, -I);
+                        atomicAdd(gM + (int64_t)b * ld + s, I);
+                        atomicAdd(gMT + (int64_t)r * ld + b, -I);
+                        atomicAdd(gMT + (int64_t)s * ld + b, I);
+                    }
+                }
+            }
+            if (lane == 0) {
+                const int32_t Or = hash_get(hk, hO, log2cap, r), Ir = hash_get(hk, hI, log2cap, r);
+                const int32_t Os = hash_get(hk, hO, log2cap, s), Is = hash_get(hk, hI, log2cap, s);
+                const int32_t L = c.L, selfw = L > 0 ? 1 : 0;
+                const int32_t drr = -Or - Ir - L, drs = Ir - Os, dsr = Or - Is, dss = Os + Is + L;
+                if (kShared) {
+                    atomicAdd(M + r * ld + r, drr);
+                    atomicAdd(M + r * ld + s, drs);
+                    atomicAdd(M + s * ld + r, dsr);
+                    atomicAdd(M + s * ld + s, dss);
+                } else {
+                    atomicAdd(gM + (int64_t)r * ld + r, drr);
+                    atomicAdd(gM + (int64_t)r * ld + s, drs);
+                    atomicAdd(gM + (int64_t)s * ld + r, dsr);
+                    atomicAdd(gM + (int64_t)s * ld + s, dss);
+                    atomicAdd(gMT + (int64_t)r * ld + r, drr);
+                    atomicAdd(gMT + (int64_t)s * ld + r, drs);
+                    atomicAdd(gMT + (int64_t)r * ld + s, dsr);
+                    atomicAdd(gMT + (int64_t)s * ld + s, dss);
+                }
+                atomicAdd(dout + r, -c.kout);
+                atomicAdd(dout + s, c.kout);
+                atomicAdd(din + r, -(c.kin + selfw));
+                atomicAdd(din + s, c.kin + selfw);
+                atomicAdd(size + r, -1);
+                atomicAdd(size + s, 1);
+                bm.asg[c.v] = s;
+            }
+        }
+        it0 += s_consumed;
+        __syncthreads();
+    }
+    if (tid == 0) {
+        atomicAdd(&flags->counters[4], edges);
+        atomicAdd(&flags->counters[5], moved);
+        atomicAdd(&flags->counters[7], (unsigned long long)dsum);
+        atomicAdd(&flags->counters[8], rounds);
+    }
+}
+
+__global__ void k_window_fill(DevBM bm, int32_t* M, int32_t* MT, int64_t ld) {
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < bm.nnz; j += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = bm.row_of[j], c = bm.row_col[j];
+        const int32_t v = bm.row_cnt[j];
+        M[r * ld + c] = v;
+        MT[c * ld + r] = v;
+    }
+}
+
+constexpr size_t kWinSmemBudget = 200 * 1024;
+
+size_t window_smem(int32_t B, bool shared_cells, int log2cap, int nwarps) {
+    const size_t ld = shared_cells ? (size_t)B + 1 : 0;
+    return sizeof(int32_t) * (3 * (size_t)B + 4 * ((size_t)nwarps << log2cap) + (shared_cells ? (size_t)B * ld : 0));
+}
+
+}  // namespace
+
+int mh_window_plan(int32_t B, int32_t max_k, size_t global_cells, bool* shared_cells, int* log2cap) {
+    int l = ceil_log2((uint64_t)(2 * (max_k > 16 ? max_k : 16)));
+    if (l > 13) return 0;
+    *log2cap = l;
+    *shared_cells = B <= kWinSharedMax;
+    if (!*shared_cells) {
+        const uint64_t ld = ((uint64_t)B + 3) & ~3ull;
+        if ((uint64_t)B * ld > global_cells) return 0;
+    }
+    int nw = kWinMaxWarps;
+    while (nw > 0 && window_smem(B, *shared_cells, l, nw) > kWinSmemBudget) --nw;
+    return nw;
+}
+
+void mh_chain_window(const DevGraph& g, DevBM& bm, const int32_t* order, int32_t n, int32_t max_k, uint64_t seed,
+                     uint32_t iter, uint32_t step, Work& w, cudaStream_t st) {
+    if (n <= 0) return;
+    bool shared_cells = false;
+    int log2cap = 0;
+    const size_t gcells = w.dense_M ? (size_t)w.dense_cap * (size_t)w.dense_cap : 0;
+    const int nw = mh_window_plan(bm.B, max_k, gcells, &shared_cells, &log2cap);
+    if (nw <= 0) return;
+    const size_t smem = window_smem(bm.B, shared_cells, log2cap, nw);
+    if (shared_cells) {
+        cudaFuncSetAttribute(k_mh_window<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k_mh_window<true><<<1, 32 * nw, smem, st>>>(g, bm, order, n, seed, iter, step, nullptr, nullptr, bm.B + 1,
+                                                    log2cap, nw, w.flags_dev);
+        count_launches(1);
+        return;
+    }
+    const int64_t ld = ((int64_t)bm.B + 3) & ~3ll;
+    const size_t cells = (size_t)bm.B * (size_t)ld;
+    cudaMemsetAsync(w.dense_M, 0, cells * sizeof(int32_t), st);
+    cudaMemsetAsync(w.dense_MT, 0, cells * sizeof(int32_t), st);
+    int64_t blocks = ((int64_t)bm.nnz + 255) / 256;
+    if (blocks < 1) blocks = 1;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    k_window_fill<<<(unsigned)blocks, 256, 0, st>>>(bm, w.dense_M, w.dense_MT, ld);
+    cudaFuncSetAttribute(k_mh_window<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_mh_window<false><<<1, 32 * nw, smem, st>>>(g, bm, order, n, seed, iter, step, w.dense_M, w.dense_MT, (int32_t)ld,
+                                                 log2cap, nw, w.flags_dev);
+    count_launches(2);
+}
+
+}  // namespace sbp

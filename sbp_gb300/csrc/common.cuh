@@ -90,7 +90,9 @@ struct DevChain {
 struct DevFlags {
     int32_t err;
     int32_t pad;
-    unsigned long long counters[8];
+    // 0 carry-out rounds, 1 Gibbs accepted, 2 Gibbs applied, 3 Gibbs edges, 4 chain edges,
+    // 5 chain moves, 6 merge proposals, 7 chain delta sum (2^-24 units), 8 chain rounds
+    unsigned long long counters[12];
 };
 
 constexpr unsigned long long kEmptyKey = ~0ull;

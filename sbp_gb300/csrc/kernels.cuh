@@ -90,6 +90,14 @@ constexpr int32_t kDenseGlobalMax = 4096;
 size_t mh_chain_dense_smem(int32_t B);
 void mh_chain_dense(const DevGraph& g, DevBM& bm, const int32_t* order, int32_t n, uint64_t seed, uint32_t iter,
                     uint32_t step, Work& w, cudaStream_t st);
+// The chain evaluated in windows of upcoming vertices (chain_window.cu): cells dense in
+// shared memory for B <= kWinSharedMax, else dense M / transpose in w.dense_M / w.dense_MT.
+constexpr int32_t kWinSharedMax = 128;
+// Warps per window for this blockmodel (0 when the windowed chain does not apply: a
+// neighbour hash over 2^13 slots, or a dense matrix larger than global_cells).
+int mh_window_plan(int32_t B, int32_t max_k, size_t global_cells, bool* shared_cells, int* log2cap);
+void mh_chain_window(const DevGraph& g, DevBM& bm, const int32_t* order, int32_t n, int32_t max_k, uint64_t seed,
+                     uint32_t iter, uint32_t step, Work& w, cudaStream_t st);
 // order[i] = base[perm(i)] with the canonical shuffle keyed by (i, iter, step, dom).
 void shuffle(const int32_t* base, int32_t n, uint64_t seed, uint32_t iter, uint32_t step, uint32_t dom,
              int32_t* order, Work& w, cudaStream_t st);
