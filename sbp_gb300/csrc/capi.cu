@@ -337,15 +337,37 @@ void gibbs_batch_dev(sbpgpu_bm* bm, const int32_t* list, int32_t n, uint64_t see
     do_rebuild(bm);
 }
 
+// At least `need` int32 of dense cells (the carry-out's B x B counts, or the windowed
+// chain's matrix and transpose) when they fit the context's budget; otherwise, or when the
+// allocation fails, the callers use the chain hash.
+void ensure_cells(sbpgpu_graph* g, uint64_t need) {
+    Work& w = g->w;
+    const uint64_t budget = (uint64_t)std::max<int64_t>(g->ctx->cells_budget, 0) / sizeof(int32_t);
+    if (w.cells && (w.cells_elems > budget || (need <= budget && w.cells_elems < need))) {
+        CK(cudaStreamSynchronize(g->ctx->stream));
+        CK(cudaFree(w.cells));
+        w.cells = nullptr;
+        w.cells_elems = 0;
+    }
+    if (need > budget || w.cells) return;
+    void* p = nullptr;
+    if (cudaMalloc(&p, need * sizeof(int32_t)) != cudaSuccess) {
+        cudaGetLastError();
+        return;
+    }
+    w.cells = static_cast<int32_t*>(p);
+    w.cells_elems = need;
+}
+
 void chain_run(sbpgpu_bm* bm, const int32_t* order, int32_t n, int32_t max_k, int64_t k_sum, uint64_t seed,
                uint32_t it, uint32_t step, int greedy) {
     sbpgpu_graph* g = bm->g;
-    bool shared_cells = false;
-    int log2cap = 0;
-    const size_t gcells = g->w.dense_M ? (size_t)g->w.dense_cap * (size_t)g->w.dense_cap : 0;
-    if (mh_window_plan(bm->d.B, max_k, gcells, &shared_cells, &log2cap) >= 2) {
+    const int64_t B = bm->d.B;
+    if (B > kWinSharedMax) ensure_cells(g, mh_window_cells((int32_t)B));
+    WindowPlan plan{};
+    if (mh_window_plan(bm->d.B, max_k, g->w, &plan)) {
         Span sp(g->ctx, 1);
-        mh_chain_window(g->dg, bm->d, order, n, max_k, seed, it, step, g->w, g->ctx->stream);
+        mh_chain_window(g->dg, bm->d, order, n, plan, seed, it, step, g->w, g->ctx->stream);
     } else if (bm->d.B <= kDenseMax || bm->d.B <= g->w.dense_cap) {
         Span sp(g->ctx, 1);
         mh_chain_dense(g->dg, bm->d, order, n, seed, it, step, g->w, g->ctx->stream);
@@ -470,29 +492,6 @@ void mcmc_impl(sbpgpu_bm* bm, const sbpgpu_config& cfg, uint64_t seed, int32_t s
     else metropolis_hastings(bm, cfg, seed, step, golden);
 }
 
-// Dense B x B cells for the carry-out when they fit the context's budget; otherwise (or
-// when the allocation fails) the carry-out uses the chain hash.
-void ensure_cells(sbpgpu_graph* g, int32_t B) {
-    Work& w = g->w;
-    const uint64_t need = (uint64_t)B * (uint64_t)B;
-    const bool fits = need * sizeof(int32_t) <= (uint64_t)std::max<int64_t>(g->ctx->cells_budget, 0);
-    if (fits && w.cells_elems >= need) return;
-    if (w.cells) {
-        CK(cudaStreamSynchronize(g->ctx->stream));
-        CK(cudaFree(w.cells));
-        w.cells = nullptr;
-        w.cells_elems = 0;
-    }
-    if (!fits) return;
-    void* p = nullptr;
-    if (cudaMalloc(&p, need * sizeof(int32_t)) != cudaSuccess) {
-        cudaGetLastError();
-        return;
-    }
-    w.cells = static_cast<int32_t*>(p);
-    w.cells_elems = need;
-}
-
 void merge_impl(sbpgpu_bm* bm, const sbpgpu_config& cfg, uint64_t seed, int32_t step, int64_t num_to_merge) {
     sbpgpu_graph* g = bm->g;
     if (num_to_merge <= 0) return;  // nothing is merged; the rebuild would reproduce the same state
@@ -502,7 +501,7 @@ void merge_impl(sbpgpu_bm* bm, const sbpgpu_config& cfg, uint64_t seed, int32_t 
         Span sp(g->ctx, 2);
         merge_propose(g->dg, bm->d, seed, (uint32_t)step, g->w, g->ctx->stream);
     }
-    if (!cfg.approximate) ensure_cells(g, B);
+    if (!cfg.approximate) ensure_cells(g, (uint64_t)B * (uint64_t)B);
     {
         Span sp(g->ctx, 3);
         carry_out(g->dg, bm->d, num_to_merge, cfg.approximate, g->w, g->ctx->stream);

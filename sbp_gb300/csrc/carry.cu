@@ -9,8 +9,13 @@
 //   1. selects the W smallest live queue entries (and the (W+1)-th as a bound),
 //   2. recomputes their deltas at once, one team of warps per entry,
 //   3. replays the reference's pop / put-back / merge rule over those values on one
-//      thread, up to the first merge or the first entry it holds no value for,
-//   4. applies that merge with the whole CTA.
+//      thread, up to the first entry it holds no value for,
+//   4. applies the merges of the round with the whole CTA, one after another.
+// A merge r -> s changes only rows / columns r and s and the degrees of r and s, so an
+// evaluation stays exact after it unless it read one of them: each evaluation records
+// the blocks it read (its two blocks, every key of the moving row and column) in a
+// 2048-bit filter, and the replay continues past a merge only through entries whose
+// filter holds neither block (a false positive merely ends the round early).
 // Merges, their order and every put-back delta equal those of the one-at-a-time loop;
 // ties of equal delta pop in ascending block order.
 //
@@ -37,6 +42,20 @@ constexpr int kCarryThreads = 512;
 constexpr int kCarryWarps = kCarryThreads / 32;
 constexpr int kQS = 1024;   // shared put-back buffer
 constexpr int kMaxW = 16;   // entries evaluated per round (kCarryWarps / warps per team)
+constexpr int kBloomWords = 64;  // 2048-bit filter of the blocks an evaluation read
+
+// Two bits of the 2048-bit filter per block.
+__device__ __forceinline__ void bloom_add(uint32_t* f, int32_t x) {
+    const uint32_t h = (uint32_t)x * 0x9E3779B1u;
+    const uint32_t a = h >> 21, b = (h >> 10) & 2047u;
+    atomicOr(f + (a >> 5), 1u << (a & 31));
+    atomicOr(f + (b >> 5), 1u << (b & 31));
+}
+__device__ __forceinline__ bool bloom_has(const uint32_t* f, int32_t x) {
+    const uint32_t h = (uint32_t)x * 0x9E3779B1u;
+    const uint32_t a = h >> 21, b = (h >> 10) & 2047u;
+    return ((f[a >> 5] >> (a & 31)) & 1u) && ((f[b >> 5] >> (b & 31)) & 1u);
+}
 
 struct DenseCells {
     int32_t* M;
@@ -121,7 +140,7 @@ __device__ __forceinline__ int32_t uf_find(int32_t* parent, int32_t x) {
 // log-degree difference; columns likewise.
 template <class Cells>
 __device__ long long merge_delta_part(const DevGraph& g, const DevBM& bm, const DevChain& ch, const Cells& cells,
-                                      int32_t r, int32_t s, int t, int nt, bool leader) {
+                                      int32_t r, int32_t s, int t, int nt, bool leader, uint32_t* bloom) {
     const LogTab Lq{g.Lq, g.E + 1};
     const int32_t dout_r = bm.d_out[r], din_r = bm.d_in[r], dout_s = bm.d_out[s], din_s = bm.d_in[s];
     const int32_t dout_s2 = dout_s + dout_r, din_s2 = din_s + din_r;
@@ -129,11 +148,9 @@ __device__ long long merge_delta_part(const DevGraph& g, const DevBM& bm, const 
     long long acc = 0;
     // is_row: cell (r, key) moving to (s, key), factor d_in[key]; else (key, r) -> (key, s),
     // factor d_out[key].  Both forms load their three values before using any of them.
-    auto item = [&](int32_t key, bool is_row) {
-        const int32_t m = cells.get(is_row ? r : key, is_row ? key : r);
-        const int32_t o = cells.get(is_row ? s : key, is_row ? key : s);
-        const int32_t deg = (is_row ? bm.d_in : bm.d_out)[key];
+    auto term = [&](int32_t key, bool is_row, int32_t m, int32_t o, int32_t deg) {
         if (m == 0 || (!is_row && key == r)) return;
+        bloom_add(bloom, key);
         const int32_t own = is_row ? dout_r : din_r;
         acc += ce_fixed(Lq, m, deg, own);
         if (is_row ? (key != r && key != s) : (key != s)) {
@@ -141,15 +158,38 @@ __device__ long long merge_delta_part(const DevGraph& g, const DevBM& bm, const 
             acc += ce_fixed(Lq, o, deg, ds) - ce_fixed(Lq, o + m, deg, ds2) - (long long)o * (is_row ? Lout : Lin);
         }
     };
-    // snapshot segments of row r and column r as one index space
+    auto item = [&](int32_t key, bool is_row) {
+        const int32_t m = cells.get(is_row ? r : key, is_row ? key : r);
+        const int32_t o = cells.get(is_row ? s : key, is_row ? key : s);
+        const int32_t deg = (is_row ? bm.d_in : bm.d_out)[key];
+        term(key, is_row, m, o, deg);
+    };
+    // Snapshot segments of row r and column r as one index space, four keys per thread
+    // per pass: the keys, then all their cells and degrees, are loaded before any is used.
     const int32_t rlo = bm.row_off[r], rn = bm.row_off[r + 1] - rlo;
     const int32_t clo = bm.col_off[r], cn = bm.col_off[r + 1] - clo;
-    for (int32_t j = t; j < rn + cn; j += nt) {
-        const bool is_row = j < rn;
-        item(is_row ? bm.row_col[rlo + j] : bm.col_row[clo + j - rn], is_row);
+    const int32_t rhead = ch.row_head[r], chead = ch.col_head[r];
+    for (int32_t j0 = t; j0 < rn + cn; j0 += 4 * nt) {
+        int32_t key[4], m[4], o[4], deg[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int32_t j = j0 + q * nt;
+            key[q] = j < rn ? bm.row_col[rlo + j] : (j < rn + cn ? bm.col_row[clo + j - rn] : -1);
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const bool is_row = j0 + q * nt < rn;
+            const int32_t k = key[q] < 0 ? r : key[q];
+            m[q] = cells.get(is_row ? r : k, is_row ? k : r);
+            o[q] = cells.get(is_row ? s : k, is_row ? k : s);
+            deg[q] = (is_row ? bm.d_in : bm.d_out)[k];
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+            if (key[q] >= 0) term(key[q], j0 + q * nt < rn, m[q], o[q], deg[q]);
     }
-    chunks_for_each(ch.row_head[r], ch, t, nt, [&](int32_t c) { item(c, true); });
-    chunks_for_each(ch.col_head[r], ch, t, nt, [&](int32_t x) { item(x, false); });
+    chunks_for_each(rhead, ch, t, nt, [&](int32_t c) { item(c, true); });
+    chunks_for_each(chead, ch, t, nt, [&](int32_t x) { item(x, false); });
     acc = warp_sum_ll(acc);
     if (leader) {
         const int32_t Mrr = cells.get(r, r), Mrs = cells.get(r, s), Msr = cells.get(s, r), Mss = cells.get(s, s);
@@ -174,11 +214,15 @@ struct CarryShared {
     double q_dS[kMaxW];
     int32_t q_blk[kMaxW];
     int32_t q_to[kMaxW];
+    int32_t q_cand[kMaxW];
+    uint32_t bloom[kMaxW][kBloomWords];
+    int32_t m_from[kMaxW], m_to[kMaxW];
+    int32_t nm;
     double b_dS;
     int32_t b_blk;
     int32_t has_bound, ncand, nq, cS;
     int32_t p, q, nR, rsel, ns, ssel;
-    int32_t mf, mt, nrt, nct, slot_r, slot_c;
+    int32_t nrt, nct, slot_r, slot_c;
     long long merged, rounds;
 };
 
@@ -210,6 +254,7 @@ __global__ void __launch_bounds__(kCarryThreads, 1) k_carry_out(
             if (tid == 0) atomicOr(&flags->err, ERR_STATE);
             break;
         }
+        for (int i = tid; i < kMaxW * kBloomWords; i += kCarryThreads) (&sh.bloom[0][0])[i] = 0u;
         // ---- 1. the W smallest live entries and the bound (warp 0)
         if (warp == 0) {
             const int p = sh.p, q = sh.q, nR = sh.nR, ns = sh.ns, ssel = sh.ssel;
@@ -272,7 +317,8 @@ __global__ void __launch_bounds__(kCarryThreads, 1) k_carry_out(
                 long long part = 0;
                 if (to != from) {
                     const int nt = 32 * team_warps, t = tid - team * nt;
-                    part = merge_delta_part(g, bm, ch, cells, from, to, t, nt, (warp % team_warps) == 0);
+                    part = merge_delta_part(g, bm, ch, cells, from, to, t, nt, (warp % team_warps) == 0,
+                                            sh.bloom[team]);
                 }
                 if (lane == 0) {
                     sh.part[warp] = part;
@@ -281,12 +327,21 @@ __global__ void __launch_bounds__(kCarryThreads, 1) k_carry_out(
             }
         }
         __syncthreads();
-        // ---- 3. replay the queue rule (block_merge.cpp:54-81)
+        // ---- 3. replay the queue rule (block_merge.cpp:54-95)
         if (tid == 0) {
-            int i = 0, nq = 0, cons[3] = {0, 0, 0};
-            int32_t mf = -1, mt = -1;
+            int i = 0, nq = 0, nm = 0, cons[3] = {0, 0, 0};
             const bool hb = sh.has_bound;
-            while (true) {
+            // may a merge of this round have changed the evaluation of candidate ci?
+            auto dirty = [&](int ci) {
+                for (int j = 0; j < nm; ++j) {
+                    const int32_t a = sh.m_from[j], b = sh.m_to[j];
+                    if (a == sh.c_blk[ci] || b == sh.c_blk[ci] || a == sh.c_to[ci] || b == sh.c_to[ci] ||
+                        bloom_has(sh.bloom[ci], a) || bloom_has(sh.bloom[ci], b))
+                        return true;
+                }
+                return false;
+            };
+            while (sh.merged + nm < num_to_merge) {
                 int pick = -1;
                 double bd = 0.0;
                 int32_t bb = 0;
@@ -303,23 +358,27 @@ __global__ void __launch_bounds__(kCarryThreads, 1) k_carry_out(
                 if (pick < 0) break;                                      // queue empty
                 if (hb && qless(sh.b_dS, sh.b_blk, bd, bb)) break;        // next pop not evaluated
                 if (pick == 1) {
-                    // popped again with the delta it was put back with: it is the smallest
-                    // entry, so it merges
-                    mf = sh.q_blk[0];
-                    mt = sh.q_to[0];
+                    // popped again: if no merge since touched what it read, its recomputed
+                    // delta is the one it was put back with, the smallest entry, so it merges
+                    if (dirty(sh.q_cand[0])) break;
+                    sh.m_from[nm] = sh.q_blk[0];
+                    sh.m_to[nm] = sh.q_to[0];
+                    ++nm;
                     for (int k = 1; k < nq; ++k) {
                         sh.q_dS[k - 1] = sh.q_dS[k];
                         sh.q_blk[k - 1] = sh.q_blk[k];
                         sh.q_to[k - 1] = sh.q_to[k];
+                        sh.q_cand[k - 1] = sh.q_cand[k];
                     }
                     --nq;
-                    break;
+                    continue;
                 }
+                if (dirty(i)) break;  // its value is stale: re-evaluate it next round
                 const int32_t from = sh.c_blk[i], to = sh.c_to[i];
                 long long aq = 0;
                 for (int k = 0; k < team_warps; ++k) aq += sh.part[i * team_warps + k];
                 ++cons[sh.c_src[i]];
-                ++i;
+                const int ci = i++;
                 if (to == from) continue;  // already in the same block
                 const double act = fixed_to_double(aq);
                 if (i < ncand || nq > 0 || hb) {
@@ -332,26 +391,25 @@ __global__ void __launch_bounds__(kCarryThreads, 1) k_carry_out(
                             sh.q_dS[k] = sh.q_dS[k - 1];
                             sh.q_blk[k] = sh.q_blk[k - 1];
                             sh.q_to[k] = sh.q_to[k - 1];
+                            sh.q_cand[k] = sh.q_cand[k - 1];
                             --k;
                         }
                         sh.q_dS[k] = act;
                         sh.q_blk[k] = from;
                         sh.q_to[k] = to;
+                        sh.q_cand[k] = ci;
                         continue;
                     }
                 }
-                mf = from;
-                mt = to;
-                break;
+                sh.m_from[nm] = from;
+                sh.m_to[nm] = to;
+                ++nm;
             }
             sh.p += cons[0];
             sh.q += cons[1];
             sh.cS = cons[2];
             sh.nq = nq;
-            sh.mf = mf;
-            sh.mt = mt;
-            sh.nrt = 0;
-            sh.nct = 0;
+            sh.nm = nm;
             sh.rounds += 1;
         }
         __syncthreads();
@@ -418,9 +476,15 @@ __global__ void __launch_bounds__(kCarryThreads, 1) k_carry_out(
             }
             __syncthreads();
         }
-        // ---- 5. Blockmodel::merge_block (src/blockmodel/blockmodel.cpp:337-363)
-        const int32_t mf = sh.mf, mt = sh.mt;
-        if (mf >= 0) {
+        // ---- 5. Blockmodel::merge_block (src/blockmodel/blockmodel.cpp:337-363), in order
+        const int nm = sh.nm;
+        for (int j = 0; j < nm; ++j) {
+            const int32_t mf = sh.m_from[j], mt = sh.m_to[j];
+            if (tid == 0) {
+                sh.nrt = 0;
+                sh.nct = 0;
+            }
+            __syncthreads();
             // Row mf by the first half of the CTA, column mf by the second.  New keys of
             // row mt and column mt are staged for bulk appends; every other list that
             // receives a key receives it from one thread.
@@ -473,6 +537,7 @@ __global__ void __launch_bounds__(kCarryThreads, 1) k_carry_out(
                 parent[mf] = mt;
                 sh.merged += 1;
             }
+            __syncthreads();
         }
         __syncthreads();
     }
@@ -495,7 +560,7 @@ void carry_out_exact(const DevGraph& g, DevBM& bm, int64_t num_to_merge, Work& w
     const bool dense = w.cells && (uint64_t)B * (uint64_t)B <= w.cells_elems;
     // team size from the mean number of row + column keys per block
     const double keys = 2.0 * (double)bm.nnz / (double)(B > 0 ? B : 1);
-    const int team_warps = keys <= 64 ? 1 : keys <= 128 ? 2 : keys <= 256 ? 4 : 8;
+    const int team_warps = keys <= 512 ? 1 : keys <= 1024 ? 2 : keys <= 2048 ? 4 : 8;
     int32_t* d_merged = w.d_scalar + 1;
     if (dense) {
         lists_init(bm, w, st);

@@ -38,18 +38,38 @@ struct SharedCells {
     __device__ __forceinline__ int32_t col_get(int32_t c, int32_t r) const { return M[r * ld + c]; }
 };
 
+// Dense M and its transpose in global memory, each with the sums of its rows' 128-entry
+// tiles (TS for M, TST for the transpose) so that a multinomial draw over a row reads the
+// row's tile sums and one tile instead of the whole row.
 struct GlobalCells {
-    const int32_t* M;
-    const int32_t* MT;
+    int32_t* M;
+    int32_t* MT;
+    int32_t* TS;
+    int32_t* TST;
     int64_t ld;
+    int32_t nt;  // tiles per row
     __device__ __forceinline__ int32_t row_get(int32_t r, int32_t c) const { return __ldcg(M + r * ld + c); }
     __device__ __forceinline__ int32_t col_get(int32_t c, int32_t r) const { return __ldcg(MT + c * ld + r); }
+    // M[r][c] += d, with the transpose and both tile sums
+    __device__ __forceinline__ void add(int32_t r, int32_t c, int32_t d) const {
+        atomicAdd(M + r * ld + c, d);
+        atomicAdd(TS + (int64_t)r * nt + (c >> 7), d);
+        atomicAdd(MT + c * ld + r, d);
+        atomicAdd(TST + (int64_t)c * nt + (r >> 7), d);
+    }
 };
 
 struct WinResult {
     long long dS;
-    int32_t v, r, s, nb, status, k, kout, kin, L;
+    int32_t v, r, s, nb, status, k, kout, kin, L, l2;  // l2: log2 of this vertex's hash size
 };
+
+// log2 of the neighbour-hash size for a vertex of degree k (at least twice k slots).
+__device__ __forceinline__ int hash_log2(int32_t k, int log2max) {
+    const int32_t need = 2 * (k > 16 ? k : 16);
+    const int l = 32 - __clz(need - 1);
+    return l < log2max ? l : log2max;
+}
 
 // Entry at cumulative unit t in ascending index order over x(i), i < B, one warp.
 // get(i) returns the weight of index i.  Returns -1 when t is out of range.
@@ -138,26 +158,23 @@ __device__ __forceinline__ int32_t hash_get(const int32_t* hk, const int32_t* cn
     return 0;
 }
 
-// Two-level select over a 16-byte aligned global row (ld a multiple of 4): the sums of
-// 32 tiles of 128 entries are read with independent coalesced loads, a scan over them
-// finds the tile, and one pass over that tile finds the entry.
-__device__ __forceinline__ int32_t warp_select_row2(const int32_t* __restrict__ row, int32_t B, long long t,
-                                                    int32_t skip) {
+// Entry at cumulative unit t of a global row through its tile sums: lane l takes tiles
+// [8l, 8l + 8) of each group of 256 tiles (one load each), a warp scan over the lanes'
+// totals finds the tile, then one pass over that tile (16-byte loads) finds the entry.
+// Entry `skip` (weight skip_w) is left out.
+__device__ __forceinline__ int32_t warp_select_tiles(const int32_t* __restrict__ row, const int32_t* __restrict__ ts,
+                                                     int32_t B, int32_t nt, long long t, int32_t skip,
+                                                     int32_t skip_w) {
     const int lane = threadIdx.x & 31;
-    const int ntiles = (B + 127) >> 7;
-    for (int tb = 0; tb < ntiles; tb += 32) {
-        long long mine = 0;  // lane q: sum of tile tb + q
-#pragma unroll 8
-        for (int q = 0; q < 32; ++q) {
-            const int32_t i = ((tb + q) << 7) + 4 * lane;
-            long long s4 = 0;
-            if (tb + q < ntiles && i < B) {
-                const int4 x = __ldcg(reinterpret_cast<const int4*>(row + i));
-                s4 = (long long)(i == skip ? 0 : x.x) + (i + 1 >= B || i + 1 == skip ? 0 : x.y) +
-                     (i + 2 >= B || i + 2 == skip ? 0 : x.z) + (i + 3 >= B || i + 3 == skip ? 0 : x.w);
-            }
-            s4 = warp_sum_ll(s4);
-            if (lane == q) mine = s4;
+    const int32_t skip_tile = skip >= 0 ? skip >> 7 : -1;
+    for (int32_t tb = 0; tb < nt; tb += 256) {
+        int32_t x[8];
+        long long mine = 0;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int32_t tile = tb + 8 * lane + j;
+            x[j] = tile < nt ? __ldcg(ts + tile) - (tile == skip_tile ? skip_w : 0) : 0;
+            mine += x[j];
         }
         long long incl = mine;
 #pragma unroll
@@ -168,8 +185,21 @@ __device__ __forceinline__ int32_t warp_select_row2(const int32_t* __restrict__ 
         const long long tot = __shfl_sync(SBP_FULL_MASK, incl, 31);
         if (t < tot) {
             const int src = __ffs(__ballot_sync(SBP_FULL_MASK, incl > t)) - 1;
-            const long long before = __shfl_sync(SBP_FULL_MASK, incl - mine, src);
-            const int32_t base = (tb + src) << 7;
+            int32_t tile = -1;
+            long long before = 0;
+            if (lane == src) {
+                long long u = t - (incl - mine);
+#pragma unroll
+                for (int j = 0; j < 8; ++j) {
+                    if (tile < 0 && u < x[j]) tile = tb + 8 * lane + j;
+                    else if (tile < 0) u -= x[j];
+                }
+                before = t - u;
+            }
+            tile = __shfl_sync(SBP_FULL_MASK, tile, src);
+            before = __shfl_sync(SBP_FULL_MASK, before, src);
+            if (tile < 0) return -1;
+            const int32_t base = tile << 7;
             const int32_t r = warp_select_row4(row + base, min(128, B - base), t - before, skip - base);
             return r < 0 ? -1 : base + r;
         }
@@ -321,25 +351,29 @@ __device__ long long warp_delta(const DevGraph& g, const int32_t* d_out, const i
 }
 
 // x in T(candidate)?
-__device__ __forceinline__ bool in_touched(const WinResult& c, const int32_t* hk, int log2cap, int32_t x) {
+__device__ __forceinline__ bool in_touched(const WinResult& c, const int32_t* hk, int32_t x) {
     if (x == c.r) return true;
     if (c.status >= ST_NOMOVE && x == c.nb) return true;
-    if (c.status >= ST_REJECT && (x == c.s || hash_has(hk, log2cap, x))) return true;
+    if (c.status >= ST_REJECT && (x == c.s || hash_has(hk, c.l2, x))) return true;
     return false;
 }
 
-template <bool kShared>
+// kMode 0: cells, degrees and sizes in shared memory; 1: cells dense in global memory,
+// degrees and sizes in shared memory; 2: all of them in global memory (large B).
+template <int kMode>
 __global__ void __launch_bounds__(kWinMaxWarps * 32, 1)
     k_mh_window(DevGraph g, DevBM bm, const int32_t* __restrict__ order, int32_t n, uint64_t seed, uint32_t iter,
-                uint32_t step, int32_t* gM, int32_t* gMT, int32_t ld, int log2cap, int nwarps, DevFlags* flags) {
+                uint32_t step, GlobalCells gc, int32_t ld, int log2cap, int nwarps, DevFlags* flags) {
+    constexpr bool kShared = kMode == 0;
+    constexpr bool kGlobalDeg = kMode == 2;
     extern __shared__ int32_t sm[];
     const int32_t B = bm.B;
     const int cap = 1 << log2cap;
-    int32_t* dout = sm;
-    int32_t* din = dout + B;
-    int32_t* size = din + B;
-    int32_t* hash = size + B;               // nwarps x (keys, out counts, in counts, items) x cap
-    int32_t* M = hash + 4 * cap * nwarps;  // shared cells (kShared): B rows of ld
+    int32_t* dout = kGlobalDeg ? bm.d_out : sm;
+    int32_t* din = kGlobalDeg ? bm.d_in : dout + B;
+    int32_t* size = kGlobalDeg ? bm.sizes : din + B;
+    int32_t* hash = kGlobalDeg ? sm : size + B;  // nwarps x (keys, out counts, in counts, items) x cap
+    int32_t* M = hash + 4 * cap * nwarps;       // shared cells (kShared): B rows of ld
     __shared__ WinResult res[kWinMaxWarps];
     __shared__ int32_t s_consumed, s_acc_mask;
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
@@ -354,14 +388,15 @@ __global__ void __launch_bounds__(kWinMaxWarps * 32, 1)
         __syncthreads();
         for (int32_t j = tid; j < bm.nnz; j += nt) M[bm.row_of[j] * ld + bm.row_col[j]] = bm.row_cnt[j];
     }
-    for (int b = tid; b < B; b += nt) {
-        dout[b] = bm.d_out[b];
-        din[b] = bm.d_in[b];
-        size[b] = bm.sizes[b];
+    if (!kGlobalDeg) {
+        for (int b = tid; b < B; b += nt) {
+            dout[b] = bm.d_out[b];
+            din[b] = bm.d_in[b];
+            size[b] = bm.sizes[b];
+        }
     }
     __syncthreads();
     const SharedCells sc{M, ld};
-    const GlobalCells gc{gM, gMT, (int64_t)ld};
 
     unsigned long long edges = 0, moved = 0, rounds = 0;
     long long dsum = 0;
@@ -383,6 +418,7 @@ __global__ void __launch_bounds__(kWinMaxWarps * 32, 1)
             c.kin = i1 - i0;
             c.k = c.kout + c.kin;
             c.L = __ldg(g.selfcnt + c.v);
+            c.l2 = hash_log2(c.k, log2cap);
             c.status = ST_SKIP;
             if (size[c.r] != 1) {  // a singleton block never moves (finetune.cpp:845)
                 uint32_t w[4];
@@ -402,11 +438,13 @@ __global__ void __launch_bounds__(kWinMaxWarps * 32, 1)
                     long long t = (long long)u64_below(w[1], w[2], (uint64_t)(R + C));
                     if (t < R) {
                         s = kShared ? warp_select(B, t, [&](int32_t i) { return sc.row_get(nb, i); })
-                                    : warp_select_row2(gM + (int64_t)nb * ld, B, t, -1);
+                                    : warp_select_tiles(gc.M + (int64_t)nb * ld, gc.TS + (int64_t)nb * gc.nt, B,
+                                                        gc.nt, t, -1, 0);
                     } else {
                         t -= R;
                         s = kShared ? warp_select(B, t, [&](int32_t i) { return i == nb ? 0 : sc.row_get(i, nb); })
-                                    : warp_select_row2(gMT + (int64_t)nb * ld, B, t, nb);
+                                    : warp_select_tiles(gc.MT + (int64_t)nb * ld, gc.TST + (int64_t)nb * gc.nt, B,
+                                                        gc.nt, t, nb, dnn);
                     }
                 }
                 if (s < 0) {
@@ -416,9 +454,9 @@ __global__ void __launch_bounds__(kWinMaxWarps * 32, 1)
                     c.status = ST_NOMOVE;
                 } else {
                     c.s = s;
-                    warp_gather(g, bm.asg, c.v, o0, c.kout, i0, c.k, hk, hO, hI, log2cap);
-                    c.dS = kShared ? warp_delta(g, dout, din, sc, c.r, s, c.kout, c.kin, c.L, hk, hO, hI, log2cap, items)
-                                   : warp_delta(g, dout, din, gc, c.r, s, c.kout, c.kin, c.L, hk, hO, hI, log2cap, items);
+                    warp_gather(g, bm.asg, c.v, o0, c.kout, i0, c.k, hk, hO, hI, c.l2);
+                    c.dS = kShared ? warp_delta(g, dout, din, sc, c.r, s, c.kout, c.kin, c.L, hk, hO, hI, c.l2, items)
+                                   : warp_delta(g, dout, din, gc, c.r, s, c.kout, c.kin, c.L, hk, hO, hI, c.l2, items);
                     c.status = c.dS < 0 ? ST_ACCEPT : ST_REJECT;  // greedy accept (finetune.cpp:22-25)
                 }
             }
@@ -436,8 +474,8 @@ __global__ void __launch_bounds__(kWinMaxWarps * 32, 1)
                     if (!((acc_mask >> u) & 1)) continue;
                     const WinResult& cu = res[u];
                     const int32_t* hku = hash + 4 * cap * u;
-                    if (in_touched(cj, hkj, log2cap, cu.r) || in_touched(cj, hkj, log2cap, cu.s) ||
-                        (cj.nb >= 0 && in_touched(cu, hku, log2cap, cj.nb)))
+                    if (in_touched(cj, hkj, cu.r) || in_touched(cj, hkj, cu.s) ||
+                        (cj.nb >= 0 && in_touched(cu, hku, cj.nb)))
                         valid = false;
                 }
                 if (!valid) break;
@@ -458,7 +496,7 @@ __global__ void __launch_bounds__(kWinMaxWarps * 32, 1)
         if (wid < wn && ((s_acc_mask >> wid) & 1)) {
             const WinResult c = res[wid];
             const int32_t r = c.r, s = c.s;
-            for (int i = lane; i < cap; i += 32) {
+            for (int i = lane; i < (1 << c.l2); i += 32) {
                 const int32_t b = hk[i];
                 if (b < 0 || b == r || b == s) continue;
                 const int32_t O = hO[i], I = hI[i];
@@ -473,22 +511,18 @@ __global__ void __launch_bounds__(kWinMaxWarps * 32, 1)
                     }
                 } else {
                     if (O) {
-                        atomicAdd(gM + (int64_t)r * ld + b, -O);
-                        atomicAdd(gM + (int64_t)s * ld + b, O);
-                        atomicAdd(gMT + (int64_t)b * ld + r, -O);
-                        atomicAdd(gMT + (int64_t)b * ld + s, O);
+                        gc.add(r, b, -O);
+                        gc.add(s, b, O);
                     }
                     if (I) {
-                        atomicAdd(gM + (int64_t)b * ld + r, -I);
-                        atomicAdd(gM + (int64_t)b * ld + s, I);
-                        atomicAdd(gMT + (int64_t)r * ld + b, -I);
-                        atomicAdd(gMT + (int64_t)s * ld + b, I);
+                        gc.add(b, r, -I);
+                        gc.add(b, s, I);
                     }
                 }
             }
             if (lane == 0) {
-                const int32_t Or = hash_get(hk, hO, log2cap, r), Ir = hash_get(hk, hI, log2cap, r);
-                const int32_t Os = hash_get(hk, hO, log2cap, s), Is = hash_get(hk, hI, log2cap, s);
+                const int32_t Or = hash_get(hk, hO, c.l2, r), Ir = hash_get(hk, hI, c.l2, r);
+                const int32_t Os = hash_get(hk, hO, c.l2, s), Is = hash_get(hk, hI, c.l2, s);
                 const int32_t L = c.L, selfw = L > 0 ? 1 : 0;
                 const int32_t drr = -Or - Ir - L, drs = Ir - Os, dsr = Or - Is, dss = Os + Is + L;
                 if (kShared) {
@@ -497,14 +531,10 @@ __global__ void __launch_bounds__(kWinMaxWarps * 32, 1)
                     atomicAdd(M + s * ld + r, dsr);
                     atomicAdd(M + s * ld + s, dss);
                 } else {
-                    atomicAdd(gM + (int64_t)r * ld + r, drr);
-                    atomicAdd(gM + (int64_t)r * ld + s, drs);
-                    atomicAdd(gM + (int64_t)s * ld + r, dsr);
-                    atomicAdd(gM + (int64_t)s * ld + s, dss);
-                    atomicAdd(gMT + (int64_t)r * ld + r, drr);
-                    atomicAdd(gMT + (int64_t)s * ld + r, drs);
-                    atomicAdd(gMT + (int64_t)r * ld + s, dsr);
-                    atomicAdd(gMT + (int64_t)s * ld + s, dss);
+                    gc.add(r, r, drr);
+                    gc.add(r, s, drs);
+                    gc.add(s, r, dsr);
+                    gc.add(s, s, dss);
                 }
                 atomicAdd(dout + r, -c.kout);
                 atomicAdd(dout + s, c.kout);
@@ -526,65 +556,83 @@ __global__ void __launch_bounds__(kWinMaxWarps * 32, 1)
     }
 }
 
-__global__ void k_window_fill(DevBM bm, int32_t* M, int32_t* MT, int64_t ld) {
+// The snapshot's cells into the zeroed dense matrices and tile sums.
+__global__ void k_window_fill(DevBM bm, GlobalCells gc) {
     for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < bm.nnz; j += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t r = bm.row_of[j], c = bm.row_col[j];
-        const int32_t v = bm.row_cnt[j];
-        M[r * ld + c] = v;
-        MT[c * ld + r] = v;
+        const int32_t r = bm.row_of[j], c = bm.row_col[j], v = bm.row_cnt[j];
+        gc.M[r * gc.ld + c] = v;
+        gc.MT[c * gc.ld + r] = v;
+        atomicAdd(gc.TS + (int64_t)r * gc.nt + (c >> 7), v);
+        atomicAdd(gc.TST + (int64_t)c * gc.nt + (r >> 7), v);
     }
 }
 
 constexpr size_t kWinSmemBudget = 200 * 1024;
 
-size_t window_smem(int32_t B, bool shared_cells, int log2cap, int nwarps) {
-    const size_t ld = shared_cells ? (size_t)B + 1 : 0;
-    return sizeof(int32_t) * (3 * (size_t)B + 4 * ((size_t)nwarps << log2cap) + (shared_cells ? (size_t)B * ld : 0));
+size_t window_smem(int32_t B, int mode, int log2cap, int nwarps) {
+    const size_t deg = mode == 2 ? 0 : 3 * (size_t)B;
+    const size_t cells = mode == 0 ? (size_t)B * ((size_t)B + 1) : 0;
+    return sizeof(int32_t) * (deg + 4 * ((size_t)nwarps << log2cap) + cells);
 }
 
 }  // namespace
 
-int mh_window_plan(int32_t B, int32_t max_k, size_t global_cells, bool* shared_cells, int* log2cap) {
-    int l = ceil_log2((uint64_t)(2 * (max_k > 16 ? max_k : 16)));
-    if (l > 13) return 0;
-    *log2cap = l;
-    *shared_cells = B <= kWinSharedMax;
-    if (!*shared_cells) {
-        const uint64_t ld = ((uint64_t)B + 3) & ~3ull;
-        if ((uint64_t)B * ld > global_cells) return 0;
-    }
-    int nw = kWinMaxWarps;
-    while (nw > 0 && window_smem(B, *shared_cells, l, nw) > kWinSmemBudget) --nw;
-    return nw;
+uint64_t mh_window_cells(int32_t B) {
+    const uint64_t ld = ((uint64_t)B + 3) & ~3ull, nt = ((uint64_t)B + 127) >> 7;
+    return 2 * (uint64_t)B * ld + 2 * (uint64_t)B * nt;
 }
 
-void mh_chain_window(const DevGraph& g, DevBM& bm, const int32_t* order, int32_t n, int32_t max_k, uint64_t seed,
-                     uint32_t iter, uint32_t step, Work& w, cudaStream_t st) {
+bool mh_window_plan(int32_t B, int32_t max_k, const Work& w, WindowPlan* p) {
+    const int l = ceil_log2((uint64_t)(2 * (max_k > 16 ? max_k : 16)));
+    if (l > 13) return false;
+    p->log2cap = l;
+    if (B <= kWinSharedMax) {
+        p->mode = 0;
+        p->ld = B + 1;
+    } else {
+        if (!w.cells || mh_window_cells(B) > w.cells_elems) return false;
+        p->ld = ((int64_t)B + 3) & ~3ll;
+        p->mode = window_smem(B, 1, l, 8) <= kWinSmemBudget ? 1 : 2;
+    }
+    int nw = kWinMaxWarps;
+    while (nw > 0 && window_smem(B, p->mode, l, nw) > kWinSmemBudget) --nw;
+    p->nw = nw;
+    return nw >= 2;
+}
+
+void mh_chain_window(const DevGraph& g, DevBM& bm, const int32_t* order, int32_t n, const WindowPlan& p,
+                     uint64_t seed, uint32_t iter, uint32_t step, Work& w, cudaStream_t st) {
     if (n <= 0) return;
-    bool shared_cells = false;
-    int log2cap = 0;
-    const size_t gcells = w.dense_M ? (size_t)w.dense_cap * (size_t)w.dense_cap : 0;
-    const int nw = mh_window_plan(bm.B, max_k, gcells, &shared_cells, &log2cap);
-    if (nw <= 0) return;
-    const size_t smem = window_smem(bm.B, shared_cells, log2cap, nw);
-    if (shared_cells) {
-        cudaFuncSetAttribute(k_mh_window<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_mh_window<true><<<1, 32 * nw, smem, st>>>(g, bm, order, n, seed, iter, step, nullptr, nullptr, bm.B + 1,
-                                                    log2cap, nw, w.flags_dev);
+    const size_t smem = window_smem(bm.B, p.mode, p.log2cap, p.nw);
+    if (p.mode == 0) {
+        cudaFuncSetAttribute(k_mh_window<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k_mh_window<0><<<1, 32 * p.nw, smem, st>>>(g, bm, order, n, seed, iter, step, GlobalCells{}, (int32_t)p.ld,
+                                                   p.log2cap, p.nw, w.flags_dev);
         count_launches(1);
         return;
     }
-    const int64_t ld = ((int64_t)bm.B + 3) & ~3ll;
-    const size_t cells = (size_t)bm.B * (size_t)ld;
-    cudaMemsetAsync(w.dense_M, 0, cells * sizeof(int32_t), st);
-    cudaMemsetAsync(w.dense_MT, 0, cells * sizeof(int32_t), st);
+    const int64_t B = bm.B, nt = (B + 127) >> 7;
+    GlobalCells gc;
+    gc.ld = p.ld;
+    gc.nt = (int32_t)nt;
+    gc.M = w.cells;
+    gc.MT = gc.M + B * p.ld;
+    gc.TS = gc.MT + B * p.ld;
+    gc.TST = gc.TS + B * nt;
+    cudaMemsetAsync(w.cells, 0, sizeof(int32_t) * mh_window_cells(bm.B), st);
     int64_t blocks = ((int64_t)bm.nnz + 255) / 256;
     if (blocks < 1) blocks = 1;
     if (blocks > 152 * 16) blocks = 152 * 16;
-    k_window_fill<<<(unsigned)blocks, 256, 0, st>>>(bm, w.dense_M, w.dense_MT, ld);
-    cudaFuncSetAttribute(k_mh_window<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_mh_window<false><<<1, 32 * nw, smem, st>>>(g, bm, order, n, seed, iter, step, w.dense_M, w.dense_MT, (int32_t)ld,
-                                                 log2cap, nw, w.flags_dev);
+    k_window_fill<<<(unsigned)blocks, 256, 0, st>>>(bm, gc);
+    if (p.mode == 1) {
+        cudaFuncSetAttribute(k_mh_window<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k_mh_window<1><<<1, 32 * p.nw, smem, st>>>(g, bm, order, n, seed, iter, step, gc, (int32_t)p.ld, p.log2cap,
+                                                   p.nw, w.flags_dev);
+    } else {
+        cudaFuncSetAttribute(k_mh_window<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k_mh_window<2><<<1, 32 * p.nw, smem, st>>>(g, bm, order, n, seed, iter, step, gc, (int32_t)p.ld, p.log2cap,
+                                                   p.nw, w.flags_dev);
+    }
     count_launches(2);
 }
 

@@ -91,13 +91,21 @@ size_t mh_chain_dense_smem(int32_t B);
 void mh_chain_dense(const DevGraph& g, DevBM& bm, const int32_t* order, int32_t n, uint64_t seed, uint32_t iter,
                     uint32_t step, Work& w, cudaStream_t st);
 // The chain evaluated in windows of upcoming vertices (chain_window.cu): cells dense in
-// shared memory for B <= kWinSharedMax, else dense M / transpose in w.dense_M / w.dense_MT.
+// shared memory for B <= kWinSharedMax, else dense M, its transpose and their row tile
+// sums in w.cells (mh_window_cells(B) int32).
 constexpr int32_t kWinSharedMax = 128;
-// Warps per window for this blockmodel (0 when the windowed chain does not apply: a
-// neighbour hash over 2^13 slots, or a dense matrix larger than global_cells).
-int mh_window_plan(int32_t B, int32_t max_k, size_t global_cells, bool* shared_cells, int* log2cap);
-void mh_chain_window(const DevGraph& g, DevBM& bm, const int32_t* order, int32_t n, int32_t max_k, uint64_t seed,
-                     uint32_t iter, uint32_t step, Work& w, cudaStream_t st);
+struct WindowPlan {
+    int nw;        // warps, one window entry each
+    int mode;      // 0 shared cells; 1 global cells, shared degrees; 2 all global
+    int log2cap;   // neighbour-hash size for the largest vertex
+    int64_t ld;    // leading dimension of the dense cells
+};
+uint64_t mh_window_cells(int32_t B);
+// False when the windowed chain does not apply (a vertex needs a hash over 2^13 slots, or
+// no dense buffer holds the matrices).
+bool mh_window_plan(int32_t B, int32_t max_k, const Work& w, WindowPlan* p);
+void mh_chain_window(const DevGraph& g, DevBM& bm, const int32_t* order, int32_t n, const WindowPlan& p,
+                     uint64_t seed, uint32_t iter, uint32_t step, Work& w, cudaStream_t st);
 // order[i] = base[perm(i)] with the canonical shuffle keyed by (i, iter, step, dom).
 void shuffle(const int32_t* base, int32_t n, uint64_t seed, uint32_t iter, uint32_t step, uint32_t dom,
              int32_t* order, Work& w, cudaStream_t st);

@@ -161,10 +161,21 @@ def test_gibbs_apply_size_one_rule(gpu, oracle):
         same_state(gb, ob)
 
 
-@pytest.mark.parametrize("n,B", [(2500, 8), (2500, 120), (2500, 1500), (9000, 5000)])
-def test_mh_chain_identical(gpu, oracle, n, B):
-    """B <= 192: shared-memory dense chain; B <= 4096: global dense chain; larger: the
-    hash-based chain."""
+@pytest.mark.parametrize("n,B,cells", [(2500, 8, "dense"), (2500, 120, "dense"), (2500, 1500, "dense"),
+                                       (9000, 5000, "dense"), (24000, 16000, "dense"), (9000, 5000, "hash")])
+def test_mh_chain_identical(gpu, oracle, n, B, cells):
+    """The windowed chain with cells in shared memory (B <= 128), dense in global memory
+    with degrees in shared memory, and with degrees in global memory (B = 16000); with a
+    zero dense budget, B > 4096 runs the one-vertex-at-a-time hashed chain."""
+    ctx = gpu.core.default_context()
+    ctx.set_cells_budget(0 if cells == "hash" else 16 << 30)
+    try:
+        _mh_chain_case(gpu, oracle, n, B)
+    finally:
+        ctx.set_cells_budget(16 << 30)
+
+
+def _mh_chain_case(gpu, oracle, n, B):
     G, O, gb, ob, a, _ = make_pair(gpu, oracle, n, 12 * n, 9, B, seed=50 + B)
     order = np.random.default_rng(B).permutation(n)[:600].astype(np.int32)
     applied = gpu.finetune.mh_chain(gb, order, seed=8, iteration=1, step=3)
