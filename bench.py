@@ -126,6 +126,10 @@ def algorithmic_bytes(kind, stats):
         return 72 * stats["gibbs_proposals"] + 20 * stats["gibbs_edges"]
     if kind == "mh_chain":
         return 72 * (stats["proposals"] - stats["gibbs_proposals"]) + 20 * (stats["edges_swept"] - stats["gibbs_edges"])
+    if kind == "carry_out":
+        # per recomputed merge delta: the 4 special cells, degrees and the block map (64 B);
+        # per walked key: the key, its two cells and its block degree (16 B)
+        return 64 * stats["carry_evaluations"] + 16 * stats["carry_keys"]
     return None
 
 

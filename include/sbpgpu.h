@@ -57,6 +57,8 @@ typedef struct sbpgpu_stats {
     int64_t gibbs_edges;      /* sum of k_out + k_in over those proposals */
     int64_t chain_rounds;     /* windows evaluated by the sequential MH chain */
     int64_t carry_rounds;     /* windows evaluated by the merge carry-out */
+    int64_t carry_evaluations;  /* merge deltas recomputed by the carry-out */
+    int64_t carry_keys;       /* row + column keys walked by those recomputations */
 } sbpgpu_stats;
 
 void sbpgpu_default_config(sbpgpu_config* cfg);

@@ -35,7 +35,8 @@ class Config(ctypes.Structure):
 class Stats(ctypes.Structure):
     _fields_ = [(n, ctypes.c_int64) for n in (
         "proposals", "merge_proposals", "moves", "mcmc_iterations", "merges", "edges_swept", "outer_steps",
-        "kernel_launches", "gibbs_proposals", "gibbs_edges", "chain_rounds", "carry_rounds")]
+        "kernel_launches", "gibbs_proposals", "gibbs_edges", "chain_rounds", "carry_rounds", "carry_evaluations",
+        "carry_keys")]
 
     def as_dict(self):
         return {n: int(getattr(self, n)) for n, _ in self._fields_}

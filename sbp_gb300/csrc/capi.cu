@@ -321,6 +321,8 @@ void harvest_counters(sbpgpu_graph* g) {
     g->st.merge_proposals += (int64_t)f.counters[6];
     g->st.chain_rounds += (int64_t)f.counters[8];
     g->st.carry_rounds += (int64_t)f.counters[0];
+    g->st.carry_evaluations += (int64_t)f.counters[10];
+    g->st.carry_keys += (int64_t)f.counters[9];
     reset_counters(g);
 }
 

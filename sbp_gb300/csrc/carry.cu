@@ -140,7 +140,8 @@ __device__ __forceinline__ int32_t uf_find(int32_t* parent, int32_t x) {
 // log-degree difference; columns likewise.
 template <class Cells>
 __device__ long long merge_delta_part(const DevGraph& g, const DevBM& bm, const DevChain& ch, const Cells& cells,
-                                      int32_t r, int32_t s, int t, int nt, bool leader, uint32_t* bloom) {
+                                      int32_t r, int32_t s, int t, int nt, bool leader, uint32_t* bloom,
+                                      unsigned long long& keys_seen) {
     const LogTab Lq{g.Lq, g.E + 1};
     const int32_t dout_r = bm.d_out[r], din_r = bm.d_in[r], dout_s = bm.d_out[s], din_s = bm.d_in[s];
     const int32_t dout_s2 = dout_s + dout_r, din_s2 = din_s + din_r;
@@ -159,6 +160,7 @@ __device__ long long merge_delta_part(const DevGraph& g, const DevBM& bm, const 
         }
     };
     auto item = [&](int32_t key, bool is_row) {
+        ++keys_seen;
         const int32_t m = cells.get(is_row ? r : key, is_row ? key : r);
         const int32_t o = cells.get(is_row ? s : key, is_row ? key : s);
         const int32_t deg = (is_row ? bm.d_in : bm.d_out)[key];
@@ -186,7 +188,10 @@ __device__ long long merge_delta_part(const DevGraph& g, const DevBM& bm, const 
         }
 #pragma unroll
         for (int q = 0; q < 4; ++q)
-            if (key[q] >= 0) term(key[q], j0 + q * nt < rn, m[q], o[q], deg[q]);
+            if (key[q] >= 0) {
+                ++keys_seen;
+                term(key[q], j0 + q * nt < rn, m[q], o[q], deg[q]);
+            }
     }
     chunks_for_each(rhead, ch, t, nt, [&](int32_t c) { item(c, true); });
     chunks_for_each(chead, ch, t, nt, [&](int32_t x) { item(x, false); });
@@ -247,6 +252,7 @@ __global__ void __launch_bounds__(kCarryThreads, 1) k_carry_out(
         sh.rounds = 0;
     }
     const long long max_rounds = 64ll * (nP + 1) + 4096;
+    unsigned long long keys_seen = 0, evals = 0;  // this thread's share of the work counters
     __syncthreads();
     while (true) {
         if (sh.merged >= num_to_merge) break;
@@ -318,7 +324,8 @@ __global__ void __launch_bounds__(kCarryThreads, 1) k_carry_out(
                 if (to != from) {
                     const int nt = 32 * team_warps, t = tid - team * nt;
                     part = merge_delta_part(g, bm, ch, cells, from, to, t, nt, (warp % team_warps) == 0,
-                                            sh.bloom[team]);
+                                            sh.bloom[team], keys_seen);
+                    if (lane == 0 && warp % team_warps == 0) ++evals;
                 }
                 if (lane == 0) {
                     sh.part[warp] = part;
@@ -540,6 +547,12 @@ __global__ void __launch_bounds__(kCarryThreads, 1) k_carry_out(
             __syncthreads();
         }
         __syncthreads();
+    }
+    keys_seen = warp_sum_ll((long long)keys_seen);
+    evals = warp_sum_ll((long long)evals);
+    if (lane == 0) {
+        atomicAdd(&flags->counters[9], keys_seen);
+        atomicAdd(&flags->counters[10], evals);
     }
     if (tid == 0) {
         *out_merged = (int32_t)sh.merged;

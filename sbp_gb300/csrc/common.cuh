@@ -91,7 +91,8 @@ struct DevFlags {
     int32_t err;
     int32_t pad;
     // 0 carry-out rounds, 1 Gibbs accepted, 2 Gibbs applied, 3 Gibbs edges, 4 chain edges,
-    // 5 chain moves, 6 merge proposals, 7 chain delta sum (2^-24 units), 8 chain rounds
+    // 5 chain moves, 6 merge proposals, 7 chain delta sum (2^-24 units), 8 chain rounds,
+    // 9 carry-out keys walked, 10 carry-out evaluations
     unsigned long long counters[12];
 };
 
