@@ -10,15 +10,22 @@
 //   2. recomputes their deltas at once, one team of warps per entry,
 //   3. replays the reference's pop / put-back / merge rule over those values on one
 //      thread, up to the first entry it holds no value for,
-//   4. applies the merges of the round with the whole CTA, one after another.
+//   4. applies the merges of the round together, a team of warps each (up to 8 at once).
 // A merge r -> s changes only rows / columns r and s and the degrees of r and s, so an
 // evaluation stays exact after it unless it read one of them: each evaluation records
 // the blocks it read (its two blocks, every key of the moving row and column) in a
 // 2048-bit filter, and the replay continues past a merge only through entries whose
-// filter holds neither block (a false positive merely ends the round early).
+// filter holds neither block (a false positive merely ends the round early).  The same
+// property lets the round's merges run concurrently: they move disjoint rows and columns
+// into distinct targets, so they share only the key lists of third blocks, which take
+// their keys through list_push1_shared; each merge stages the new keys of its target's row
+// and column in its own slice of the staging buffers, sized from the keys its evaluation
+// walked.
 // Merges, their order and every put-back delta equal those of the one-at-a-time loop;
 // ties of equal delta pop in ascending block order.
 //
+// Deltas are handled as exact int64 multiples of 2^-24 (the reference's doubles compare
+// the same way), which keeps the single-thread queue logic off the slow FP64 pipe.
 // Queue: the proposals sorted by (delta, block) (P, read through a cursor), put-back
 // entries in a sorted shared-memory buffer (S) that spills into a sorted global run (R)
 // through a parallel merge.  Each block is in the queue at most once.
@@ -94,18 +101,16 @@ struct HashCells {
     }
 };
 
-__device__ __forceinline__ bool qless(double a, int32_t ab, double b, int32_t bb) {
+__device__ __forceinline__ bool qless(long long a, int32_t ab, long long b, int32_t bb) {
     return a < b || (a == b && ab < bb);
 }
 
-// Inverse of the order-preserving key of the proposal sort (k_merge_keys).
-__device__ __forceinline__ double key_to_double(uint64_t k) {
-    const uint64_t u = (k >> 63) ? (k & 0x7fffffffffffffffull) : ~k;
-    return __longlong_as_double((long long)u);
-}
+// Inverse of the order-preserving key of the proposal sort (k_merge_keys): the delta in
+// units of 2^-24.
+__device__ __forceinline__ long long key_to_fixed(uint64_t k) { return (long long)(k ^ 0x8000000000000000ull); }
 
 // Number of entries of the sorted list (d[i], b[i]), i < n, ordered before (x, xb).
-__device__ __forceinline__ int count_before(const double* d, const int32_t* b, int n, double x, int32_t xb) {
+__device__ __forceinline__ int count_before(const long long* d, const int32_t* b, int n, long long x, int32_t xb) {
     int lo = 0, hi = n;
     while (lo < hi) {
         const int mid = (lo + hi) >> 1;
@@ -207,23 +212,27 @@ __device__ long long merge_delta_part(const DevGraph& g, const DevBM& bm, const 
 }
 
 struct CarryShared {
-    double s_dS[2][kQS];
+    long long s_dS[2][kQS];
     int32_t s_blk[2][kQS];
-    double h_dS[3][32];
+    long long h_dS[3][32];
     int32_t h_blk[3][32];
-    double c_dS[kMaxW];
+    long long c_dS[kMaxW];
     int32_t c_blk[kMaxW];
     int32_t c_src[kMaxW];
     int32_t c_to[kMaxW];
     long long part[kCarryWarps];
-    double q_dS[kMaxW];
+    long long q_dS[kMaxW];
     int32_t q_blk[kMaxW];
     int32_t q_to[kMaxW];
     int32_t q_cand[kMaxW];
     uint32_t bloom[kMaxW][kBloomWords];
-    int32_t m_from[kMaxW], m_to[kMaxW];
-    int32_t nm;
-    double b_dS;
+    int32_t m_from[kMaxW], m_to[kMaxW], m_keys[kMaxW];
+    int32_t m_off[kMaxW], m_nrt[kMaxW], m_nct[kMaxW], m_slot_r[kMaxW], m_slot_c[kMaxW];
+    int32_t c_keys[kMaxW];
+    uint32_t conf[kMaxW];    // bit i of conf[j]: a merge of candidate i would change j's value
+    long long c_act[kMaxW];  // recomputed delta of candidate i
+    int32_t nm, np;
+    long long b_dS;
     int32_t b_blk;
     int32_t has_bound, ncand, nq, cS;
     int32_t p, q, nR, rsel, ns, ssel;
@@ -235,8 +244,8 @@ struct CarryShared {
 template <class Cells>
 __global__ void __launch_bounds__(kCarryThreads, 1) k_carry_out(
     DevGraph g, DevBM bm, DevChain ch, Cells cells, const uint64_t* __restrict__ pkeys,
-    const int32_t* __restrict__ pblk, int32_t nP, const int32_t* __restrict__ best, double* r0_dS, int32_t* r0_blk,
-    double* r1_dS, int32_t* r1_blk, int32_t* parent, long long num_to_merge, int team_warps, int32_t* stage_row,
+    const int32_t* __restrict__ pblk, int32_t nP, const int32_t* __restrict__ best, long long* r0_dS, int32_t* r0_blk,
+    long long* r1_dS, int32_t* r1_blk, int32_t* parent, long long num_to_merge, int team_warps, int32_t* stage_row,
     int32_t* stage_col, int stage_cap, int32_t* out_merged, DevFlags* flags) {
     __shared__ CarryShared sh;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -261,14 +270,18 @@ __global__ void __launch_bounds__(kCarryThreads, 1) k_carry_out(
             break;
         }
         for (int i = tid; i < kMaxW * kBloomWords; i += kCarryThreads) (&sh.bloom[0][0])[i] = 0u;
+        if (tid < kMaxW) {
+            sh.c_keys[tid] = 0;
+            sh.conf[tid] = 0u;
+        }
         // ---- 1. the W smallest live entries and the bound (warp 0)
         if (warp == 0) {
             const int p = sh.p, q = sh.q, nR = sh.nR, ns = sh.ns, ssel = sh.ssel;
-            const double* rd = sh.rsel ? r1_dS : r0_dS;
+            const long long* rd = sh.rsel ? r1_dS : r0_dS;
             const int32_t* rb = sh.rsel ? r1_blk : r0_blk;
             const int n0 = max(0, min(W + 1, nP - p)), n1 = max(0, min(W + 1, nR - q)), n2 = min(W + 1, ns);
             if (lane < n0) {
-                sh.h_dS[0][lane] = key_to_double(pkeys[p + lane]);
+                sh.h_dS[0][lane] = key_to_fixed(pkeys[p + lane]);
                 sh.h_blk[0][lane] = pblk[p + lane];
             }
             if (lane < n1) {
@@ -284,7 +297,7 @@ __global__ void __launch_bounds__(kCarryThreads, 1) k_carry_out(
 #pragma unroll
             for (int src = 0; src < 3; ++src) {
                 if (lane < n[src]) {
-                    const double d = sh.h_dS[src][lane];
+                    const long long d = sh.h_dS[src][lane];
                     const int32_t b = sh.h_blk[src][lane];
                     int rank = lane;
 #pragma unroll
@@ -323,8 +336,11 @@ __global__ void __launch_bounds__(kCarryThreads, 1) k_carry_out(
                 long long part = 0;
                 if (to != from) {
                     const int nt = 32 * team_warps, t = tid - team * nt;
+                    const unsigned long long before = keys_seen;
                     part = merge_delta_part(g, bm, ch, cells, from, to, t, nt, (warp % team_warps) == 0,
                                             sh.bloom[team], keys_seen);
+                    const int kc = warp_sum_i((int)(keys_seen - before));
+                    if (lane == 0) atomicAdd(&sh.c_keys[team], kc);
                     if (lane == 0 && warp % team_warps == 0) ++evals;
                 }
                 if (lane == 0) {
@@ -334,23 +350,32 @@ __global__ void __launch_bounds__(kCarryThreads, 1) k_carry_out(
             }
         }
         __syncthreads();
+        // ---- which candidate's merge would change which evaluation, all pairs at once
+        if (tid < ncand * ncand) {
+            const int i = tid / ncand, j = tid % ncand;
+            if (i != j) {
+                const int32_t a = sh.c_blk[i], b = sh.c_to[i];
+                if (a == sh.c_blk[j] || b == sh.c_blk[j] || a == sh.c_to[j] || b == sh.c_to[j] ||
+                    bloom_has(sh.bloom[j], a) || bloom_has(sh.bloom[j], b))
+                    atomicOr(&sh.conf[j], 1u << i);
+            }
+        }
+        if (tid < ncand) {
+            long long aq = 0;
+            for (int k = 0; k < team_warps; ++k) aq += sh.part[tid * team_warps + k];
+            sh.c_act[tid] = aq;
+        }
+        __syncthreads();
         // ---- 3. replay the queue rule (block_merge.cpp:54-95)
         if (tid == 0) {
             int i = 0, nq = 0, nm = 0, cons[3] = {0, 0, 0};
+            uint32_t merged_mask = 0u;  // candidates merged in this round
             const bool hb = sh.has_bound;
             // may a merge of this round have changed the evaluation of candidate ci?
-            auto dirty = [&](int ci) {
-                for (int j = 0; j < nm; ++j) {
-                    const int32_t a = sh.m_from[j], b = sh.m_to[j];
-                    if (a == sh.c_blk[ci] || b == sh.c_blk[ci] || a == sh.c_to[ci] || b == sh.c_to[ci] ||
-                        bloom_has(sh.bloom[ci], a) || bloom_has(sh.bloom[ci], b))
-                        return true;
-                }
-                return false;
-            };
+            auto dirty = [&](int ci) { return (sh.conf[ci] & merged_mask) != 0u; };
             while (sh.merged + nm < num_to_merge) {
                 int pick = -1;
-                double bd = 0.0;
+                long long bd = 0;
                 int32_t bb = 0;
                 if (i < ncand) {
                     pick = 0;
@@ -370,6 +395,8 @@ __global__ void __launch_bounds__(kCarryThreads, 1) k_carry_out(
                     if (dirty(sh.q_cand[0])) break;
                     sh.m_from[nm] = sh.q_blk[0];
                     sh.m_to[nm] = sh.q_to[0];
+                    sh.m_keys[nm] = sh.c_keys[sh.q_cand[0]];
+                    merged_mask |= 1u << sh.q_cand[0];
                     ++nm;
                     for (int k = 1; k < nq; ++k) {
                         sh.q_dS[k - 1] = sh.q_dS[k];
@@ -382,16 +409,14 @@ __global__ void __launch_bounds__(kCarryThreads, 1) k_carry_out(
                 }
                 if (dirty(i)) break;  // its value is stale: re-evaluate it next round
                 const int32_t from = sh.c_blk[i], to = sh.c_to[i];
-                long long aq = 0;
-                for (int k = 0; k < team_warps; ++k) aq += sh.part[i * team_warps + k];
                 ++cons[sh.c_src[i]];
                 const int ci = i++;
                 if (to == from) continue;  // already in the same block
-                const double act = fixed_to_double(aq);
+                const long long act = sh.c_act[ci];
                 if (i < ncand || nq > 0 || hb) {
-                    double top = hb ? sh.b_dS : INFINITY;
-                    if (i < ncand) top = fmin(top, sh.c_dS[i]);
-                    if (nq > 0) top = fmin(top, sh.q_dS[0]);
+                    long long top = hb ? sh.b_dS : LLONG_MAX;
+                    if (i < ncand) top = min(top, sh.c_dS[i]);
+                    if (nq > 0) top = min(top, sh.q_dS[0]);
                     if (act > top) {  // put back with the recomputed delta
                         int k = nq++;
                         while (k > 0 && qless(act, from, sh.q_dS[k - 1], sh.q_blk[k - 1])) {
@@ -410,6 +435,8 @@ __global__ void __launch_bounds__(kCarryThreads, 1) k_carry_out(
                 }
                 sh.m_from[nm] = from;
                 sh.m_to[nm] = to;
+                sh.m_keys[nm] = sh.c_keys[ci];
+                merged_mask |= 1u << ci;
                 ++nm;
             }
             sh.p += cons[0];
@@ -425,9 +452,9 @@ __global__ void __launch_bounds__(kCarryThreads, 1) k_carry_out(
             const int cS = sh.cS, nq = sh.nq, ns = sh.ns, ssel = sh.ssel;
             if (cS > 0 || nq > 0) {
                 const int rest = ns - cS;
-                const double* sd = sh.s_dS[ssel] + cS;
+                const long long* sd = sh.s_dS[ssel] + cS;
                 const int32_t* sb = sh.s_blk[ssel] + cS;
-                double* od = sh.s_dS[ssel ^ 1];
+                long long* od = sh.s_dS[ssel ^ 1];
                 int32_t* ob = sh.s_blk[ssel ^ 1];
                 for (int i = tid; i < rest; i += kCarryThreads) {
                     int pos = i;
@@ -451,14 +478,14 @@ __global__ void __launch_bounds__(kCarryThreads, 1) k_carry_out(
         // ---- spill S into R when it could not take another round's put-backs
         if (sh.ns > kQS - kMaxW - 1) {
             const int ns = sh.ns, ssel = sh.ssel, q = sh.q, nr = sh.nR - sh.q;
-            const double* rd = (sh.rsel ? r1_dS : r0_dS) + q;
+            const long long* rd = (sh.rsel ? r1_dS : r0_dS) + q;
             const int32_t* rb = (sh.rsel ? r1_blk : r0_blk) + q;
-            double* od = sh.rsel ? r0_dS : r1_dS;
+            long long* od = sh.rsel ? r0_dS : r1_dS;
             int32_t* ob = sh.rsel ? r0_blk : r1_blk;
-            const double* sd = sh.s_dS[ssel];
+            const long long* sd = sh.s_dS[ssel];
             const int32_t* sb = sh.s_blk[ssel];
             for (int i = tid; i < nr; i += kCarryThreads) {
-                const double d = rd[i];
+                const long long d = rd[i];
                 const int32_t b = rb[i];
                 const int pos = i + count_before(sd, sb, ns, d, b);
                 od[pos] = d;
@@ -483,56 +510,90 @@ __global__ void __launch_bounds__(kCarryThreads, 1) k_carry_out(
             }
             __syncthreads();
         }
-        // ---- 5. Blockmodel::merge_block (src/blockmodel/blockmodel.cpp:337-363), in order
+        // ---- 5. Blockmodel::merge_block (src/blockmodel/blockmodel.cpp:337-363) for the
+        // round's merges, up to 8 at once: merge j of a pass gets wpm warps, the first half
+        // moving row mf, the second half column mf.
         const int nm = sh.nm;
-        for (int j = 0; j < nm; ++j) {
-            const int32_t mf = sh.m_from[j], mt = sh.m_to[j];
+        for (int j0 = 0; j0 < nm; j0 += sh.np) {
+            __syncthreads();  // every thread has read sh.np of the previous pass
             if (tid == 0) {
-                sh.nrt = 0;
-                sh.nct = 0;
+                // as many merges (up to 8) as the staging buffers hold
+                int off = 0, np = 0;
+                while (np < 8 && j0 + np < nm && (np == 0 || off + sh.m_keys[j0 + np] + 2 <= stage_cap)) {
+                    sh.m_off[np] = off;
+                    off += sh.m_keys[j0 + np] + 2;
+                    sh.m_nrt[np] = 0;
+                    sh.m_nct[np] = 0;
+                    ++np;
+                }
+                sh.np = np;
             }
             __syncthreads();
-            // Row mf by the first half of the CTA, column mf by the second.  New keys of
-            // row mt and column mt are staged for bulk appends; every other list that
-            // receives a key receives it from one thread.
-            const int half = tid / (kCarryThreads / 2), ht = tid % (kCarryThreads / 2);
-            if (half == 0) {
-                list_for_each(bm.row_col, bm.row_off[mf], bm.row_off[mf + 1], ch.row_head[mf], ch, ht,
-                              kCarryThreads / 2, [&](int32_t c) {
-                                  const int32_t m = cells.take(mf, c, flags);
-                                  if (m == 0) return;
-                                  const int32_t c2 = (c == mf || c == mt) ? mt : c;
-                                  if (cells.add(mt, c2, m, flags)) {
-                                      stage(stage_row, &sh.nrt, stage_cap, c2, flags);
-                                      if (c2 == mt) stage(stage_col, &sh.nct, stage_cap, mt, flags);
-                                      else list_push1(ch.col_head, ch, c2, mt, flags);
-                                  }
-                              });
-            } else {
-                list_for_each(bm.col_row, bm.col_off[mf], bm.col_off[mf + 1], ch.col_head[mf], ch, ht,
-                              kCarryThreads / 2, [&](int32_t x) {
-                                  if (x == mf) return;
-                                  const int32_t m = cells.take(x, mf, flags);
-                                  if (m == 0) return;
-                                  const int32_t x2 = x == mt ? mt : x;
-                                  if (cells.add(x2, mt, m, flags)) {
-                                      stage(stage_col, &sh.nct, stage_cap, x2, flags);
-                                      if (x2 == mt) stage(stage_row, &sh.nrt, stage_cap, mt, flags);
-                                      else list_push1(ch.row_head, ch, x2, mt, flags);
-                                  }
-                              });
+            const int np = sh.np;
+            const int wpm = np <= 1 ? 16 : np <= 2 ? 8 : np <= 4 ? 4 : 2;
+            const int j = warp / wpm;
+            if (j < np) {
+                const int32_t mf = sh.m_from[j0 + j], mt = sh.m_to[j0 + j];
+                const int half = (warp % wpm) >= wpm / 2;
+                const int nth = 32 * wpm / 2, ht = tid - (j * wpm + half * wpm / 2) * 32;
+                const int slice = sh.m_keys[j0 + j] + 2;
+                int32_t* srow = stage_row + sh.m_off[j];
+                int32_t* scol = stage_col + sh.m_off[j];
+                const bool solo = np == 1;
+                if (half == 0) {
+                    list_for_each(bm.row_col, bm.row_off[mf], bm.row_off[mf + 1], ch.row_head[mf], ch, ht, nth,
+                                  [&](int32_t c) {
+                                      const int32_t m = cells.take(mf, c, flags);
+                                      if (m == 0) return;
+                                      const int32_t c2 = (c == mf || c == mt) ? mt : c;
+                                      if (cells.add(mt, c2, m, flags)) {
+                                          stage(srow, &sh.m_nrt[j], slice, c2, flags);
+                                          if (c2 == mt) stage(scol, &sh.m_nct[j], slice, mt, flags);
+                                          else if (solo) list_push1(ch.col_head, ch, c2, mt, flags);
+                                          else list_push1_shared(ch.col_head, ch, c2, mt, flags);
+                                      }
+                                  });
+                } else {
+                    list_for_each(bm.col_row, bm.col_off[mf], bm.col_off[mf + 1], ch.col_head[mf], ch, ht, nth,
+                                  [&](int32_t x) {
+                                      if (x == mf) return;
+                                      const int32_t m = cells.take(x, mf, flags);
+                                      if (m == 0) return;
+                                      const int32_t x2 = x == mt ? mt : x;
+                                      if (cells.add(x2, mt, m, flags)) {
+                                          stage(scol, &sh.m_nct[j], slice, x2, flags);
+                                          if (x2 == mt) stage(srow, &sh.m_nrt[j], slice, mt, flags);
+                                          else if (solo) list_push1(ch.row_head, ch, x2, mt, flags);
+                                          else list_push1_shared(ch.row_head, ch, x2, mt, flags);
+                                      }
+                                  });
+                }
             }
             __syncthreads();
-            const int nr = min(sh.nrt, stage_cap), nc = min(sh.nct, stage_cap);
-            if (tid == 0) sh.slot_r = nr > 0 ? list_reserve(ch.row_head, ch, mt, nr, flags) : -1;
-            if (tid == 32) sh.slot_c = nc > 0 ? list_reserve(ch.col_head, ch, mt, nc, flags) : -1;
+            if (tid < np) {
+                const int32_t mt = sh.m_to[j0 + tid];
+                const int nr = min(sh.m_nrt[tid], sh.m_keys[j0 + tid] + 2);
+                sh.m_slot_r[tid] = nr > 0 ? list_reserve(ch.row_head, ch, mt, nr, flags) : -1;
+            } else if (tid >= 64 && tid < 64 + np) {
+                const int q = tid - 64;
+                const int32_t mt = sh.m_to[j0 + q];
+                const int nc = min(sh.m_nct[q], sh.m_keys[j0 + q] + 2);
+                sh.m_slot_c[q] = nc > 0 ? list_reserve(ch.col_head, ch, mt, nc, flags) : -1;
+            }
             __syncthreads();
-            const int32_t pr = sh.slot_r, pc = sh.slot_c;
-            if (pr >= 0)
-                for (int i = tid; i < nr; i += kCarryThreads) ch.pool[pr + i] = stage_row[i];
-            if (pc >= 0)
-                for (int i = tid; i < nc; i += kCarryThreads) ch.pool[pc + i] = stage_col[i];
-            if (tid == 0) {
+            for (int q = 0; q < np; ++q) {
+                const int slice = sh.m_keys[j0 + q] + 2;
+                const int nr = min(sh.m_nrt[q], slice), nc = min(sh.m_nct[q], slice);
+                const int32_t pr = sh.m_slot_r[q], pc = sh.m_slot_c[q];
+                const int32_t* srow = stage_row + sh.m_off[q];
+                const int32_t* scol = stage_col + sh.m_off[q];
+                if (pr >= 0)
+                    for (int i = tid; i < nr; i += kCarryThreads) ch.pool[pr + i] = srow[i];
+                if (pc >= 0)
+                    for (int i = tid; i < nc; i += kCarryThreads) ch.pool[pc + i] = scol[i];
+            }
+            if (tid < np) {
+                const int32_t mf = sh.m_from[j0 + tid], mt = sh.m_to[j0 + tid];
                 bm.d_out[mt] += bm.d_out[mf];
                 bm.d_in[mt] += bm.d_in[mf];
                 bm.d_out[mf] = 0;
@@ -542,10 +603,10 @@ __global__ void __launch_bounds__(kCarryThreads, 1) k_carry_out(
                 bm.sizes[mt] += bm.sizes[mf];
                 bm.sizes[mf] = 0;
                 parent[mf] = mt;
-                sh.merged += 1;
             }
             __syncthreads();
         }
+        if (tid == 0) sh.merged += nm;
         __syncthreads();
     }
     keys_seen = warp_sum_ll((long long)keys_seen);
@@ -581,15 +642,15 @@ void carry_out_exact(const DevGraph& g, DevBM& bm, int64_t num_to_merge, Work& w
         const int64_t blocks = std::min<int64_t>((bm.nnz + 255) / 256 + 1, 152 * 16);
         k_dense_cells_fill<<<(unsigned)blocks, 256, 0, st>>>(bm, w.cells);
         k_carry_out<DenseCells><<<1, kCarryThreads, 0, st>>>(
-            g, bm, w.chain, DenseCells{w.cells, (int64_t)B}, w.keys, w.vals, B, w.best, w.heap_dS, w.heap_blk,
-            reinterpret_cast<double*>(w.keys_alt), w.vals_alt, w.parent, num_to_merge, team_warps, w.list_small,
+            g, bm, w.chain, DenseCells{w.cells, (int64_t)B}, w.keys, w.vals, B, w.best, reinterpret_cast<long long*>(w.heap_dS), w.heap_blk,
+            reinterpret_cast<long long*>(w.keys_alt), w.vals_alt, w.parent, num_to_merge, team_warps, w.list_small,
             w.list_big, 2 * g.N, d_merged, w.flags_dev);
         count_launches(2);
     } else {
         chain_init(bm, w, (uint64_t)2 * (uint64_t)bm.nnz, st);
         k_carry_out<HashCells><<<1, kCarryThreads, 0, st>>>(
-            g, bm, w.chain, HashCells{w.chain}, w.keys, w.vals, B, w.best, w.heap_dS, w.heap_blk,
-            reinterpret_cast<double*>(w.keys_alt), w.vals_alt, w.parent, num_to_merge, team_warps, w.list_small,
+            g, bm, w.chain, HashCells{w.chain}, w.keys, w.vals, B, w.best, reinterpret_cast<long long*>(w.heap_dS), w.heap_blk,
+            reinterpret_cast<long long*>(w.keys_alt), w.vals_alt, w.parent, num_to_merge, team_warps, w.list_small,
             w.list_big, 2 * g.N, d_merged, w.flags_dev);
         count_launches(1);
     }

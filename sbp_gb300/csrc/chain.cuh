@@ -4,10 +4,11 @@
 // per-column key lists made of the snapshot CSR / CSC segment and appended chunks.  A
 // key appears in a list once.
 //
-// List appends never race: a list that receives keys from many threads of one move
-// (row/column of the target block) is appended in bulk -- keys are staged, one thread
-// reserves room for all of them, every thread copies -- and every other list receives
-// keys from a single owning thread.
+// A list that receives keys from many threads of one move or merge (row / column of the
+// target block) is appended in bulk -- keys are staged, one thread reserves room for all
+// of them, every thread copies.  Any other list receives keys from a single owning thread
+// (list_push1) or, when several merges are applied together, through list_push1_shared.
+// Lists are never read while they are appended to.
 #pragma once
 
 #include "common.cuh"
@@ -49,6 +50,39 @@ __device__ __forceinline__ void list_push1(int32_t* head, const DevChain& ch, in
     if (p >= 0) ch.pool[p] = item;
 }
 
+// Appends one item to list b when other threads may append to the same list at the same
+// time: a slot of the head chunk is claimed with an atomic increment of its count (a count
+// past the capacity means the chunk is full; readers clamp it), and a full or missing head
+// is replaced by a new chunk published with a compare-and-swap.  A chunk whose publication
+// loses the race is left unused.  No thread may read the list concurrently.
+__device__ __forceinline__ void list_push1_shared(int32_t* head, const DevChain& ch, int32_t b, int32_t item,
+                                                  DevFlags* flags) {
+    volatile int32_t* vpool = ch.pool;
+    for (int tries = 0; tries < 64; ++tries) {
+        const int32_t c = ((volatile int32_t*)head)[b];
+        if (c >= 0) {
+            const int32_t pos = atomicAdd(ch.pool + c + 1, 1);
+            if (pos < vpool[c + 2]) {
+                ch.pool[c + 3 + pos] = item;
+                return;
+            }
+        }
+        const int32_t cap = c >= 0 ? min(2 * vpool[c + 2], 1 << 16) : 13;
+        const int32_t nc = atomicAdd(ch.pool_used, 3 + cap);
+        if ((int64_t)nc + 3 + cap > ch.pool_words) {
+            atomicOr(&flags->err, ERR_POOL_FULL);
+            return;
+        }
+        ch.pool[nc] = c;
+        ch.pool[nc + 1] = 1;
+        ch.pool[nc + 2] = cap;
+        ch.pool[nc + 3] = item;
+        __threadfence_block();
+        if (atomicCAS(head + b, c, nc) == c) return;
+    }
+    atomicOr(&flags->err, ERR_STATE);
+}
+
 // Adds d to cell (r, c); returns true when the key was inserted by this call.
 __device__ __forceinline__ bool chain_add(const DevChain& ch, int32_t r, int32_t c, int32_t d, DevFlags* flags) {
     if (d == 0) return false;
@@ -84,7 +118,7 @@ __device__ __forceinline__ void chunks_for_each(int32_t head, const DevChain& ch
     int32_t c = head;
     int guard = 0;
     while (c >= 0 && guard < (1 << 26)) {
-        const int32_t n = ((volatile int32_t*)ch.pool)[c + 1];
+        const int32_t n = min(((volatile int32_t*)ch.pool)[c + 1], ((volatile int32_t*)ch.pool)[c + 2]);
         for (int i = t; i < n; i += nt) f(((volatile int32_t*)ch.pool)[c + 3 + i]);
         c = ((volatile int32_t*)ch.pool)[c];
         ++guard;

@@ -376,6 +376,7 @@ __global__ void __launch_bounds__(kWinMaxWarps * 32, 1)
     int32_t* M = hash + 4 * cap * nwarps;       // shared cells (kShared): B rows of ld
     __shared__ WinResult res[kWinMaxWarps];
     __shared__ int32_t s_consumed, s_acc_mask;
+    __shared__ uint32_t s_conf[kWinMaxWarps];
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const int nt = nwarps * 32;
     int32_t* hk = hash + 4 * cap * wid;
@@ -463,22 +464,26 @@ __global__ void __launch_bounds__(kWinMaxWarps * 32, 1)
             if (lane == 0) res[wid] = c;
         }
         __syncthreads();
+        // ---- bit u of s_conf[j]: an accepted move of window entry u would change entry j
+        if (tid < kWinMaxWarps) s_conf[tid] = 0u;
+        __syncthreads();
+        if (tid < wn * wn) {
+            const int u = tid / wn, j = tid % wn;
+            if (u < j && res[u].status == ST_ACCEPT) {
+                const WinResult& cj = res[j];
+                const WinResult& cu = res[u];
+                if (in_touched(cj, hash + 4 * cap * j, cu.r) || in_touched(cj, hash + 4 * cap * j, cu.s) ||
+                    (cj.nb >= 0 && in_touched(cu, hash + 4 * cap * u, cj.nb)))
+                    atomicOr(&s_conf[j], 1u << u);
+            }
+        }
+        __syncthreads();
         // ---- replay in order; stop before the first vertex an accepted move may change
         if (tid == 0) {
             int consumed = 0, acc_mask = 0;
             for (int j = 0; j < wn; ++j) {
                 const WinResult& cj = res[j];
-                const int32_t* hkj = hash + 4 * cap * j;
-                bool valid = true;
-                for (int u = 0; u < j && valid; ++u) {
-                    if (!((acc_mask >> u) & 1)) continue;
-                    const WinResult& cu = res[u];
-                    const int32_t* hku = hash + 4 * cap * u;
-                    if (in_touched(cj, hkj, cu.r) || in_touched(cj, hkj, cu.s) ||
-                        (cj.nb >= 0 && in_touched(cu, hku, cj.nb)))
-                        valid = false;
-                }
-                if (!valid) break;
+                if (s_conf[j] & (uint32_t)acc_mask) break;
                 consumed = j + 1;
                 edges += cj.k;
                 if (cj.status == ST_ACCEPT) {

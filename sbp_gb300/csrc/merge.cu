@@ -68,12 +68,15 @@ __global__ void __launch_bounds__(256) k_merge_propose(DevGraph g, DevBM bm, uin
     if (lane == 0) atomicAdd(&flags->counters[6], evaluated);
 }
 
-// Order keys of doubles: ascending unsigned order == ascending double order.
+// Sort keys of the best deltas: each is an exact multiple of 2^-24 (a block without a
+// proposal has DBL_MAX), turned into its int64 count of 2^-24 units with the sign bit
+// flipped, so ascending unsigned order is ascending delta order.
 __global__ void k_merge_keys(const double* __restrict__ dS, int32_t B, uint64_t* __restrict__ keys,
                              int32_t* __restrict__ vals) {
     for (int32_t b = blockIdx.x * blockDim.x + threadIdx.x; b < B; b += gridDim.x * blockDim.x) {
-        const uint64_t u = (uint64_t)__double_as_longlong(dS[b]);
-        keys[b] = (u >> 63) ? ~u : (u | 0x8000000000000000ull);
+        const double d = dS[b];
+        const long long q = d == DBL_MAX ? LLONG_MAX : __double2ll_rn(d * 16777216.0);
+        keys[b] = (uint64_t)q ^ 0x8000000000000000ull;
         vals[b] = b;
     }
 }
