@@ -1,0 +1,407 @@
+/*
+ * sbp_gb300.hpp -- C++ host interface over the sbpgpu C ABI (sbpgpu.h), mirroring the
+ * hot-path API of vtsynergy/SBP so that callers of the reference can switch:
+ *
+ *   Args / args                 include/args.hpp:14-213, src/globals.cpp:5
+ *   Graph                       include/graph.hpp:29-127
+ *   Blockmodel                  include/blockmodel/blockmodel.hpp:46-219
+ *   entropy::mdl, delta_mdl, block_merge_delta_mdl, null_mdl_v1, normalize_mdl_v1
+ *                               include/entropy.hpp:33-81
+ *   finetune::mcmc, asynchronous_gibbs, hybrid_mcmc, metropolis_hastings
+ *                               include/finetune.hpp:36-157
+ *   block_merge::merge_blocks   include/block_merge.hpp:32-56
+ *   sbp::stochastic_block_partition
+ *                               include/sbp.hpp:18
+ *
+ * Header-only; link with libsbpgpu.so.  All state of a Graph and a Blockmodel lives on
+ * the GPU; host vectors returned by the accessors are copies read back on demand and
+ * refreshed after every operation that changes the blockmodel.
+ *
+ * Differences from the reference, by design:
+ *   - randomness comes from the seeded Philox stream (Args::seed), so runs repeat;
+ *   - finetune::mcmc takes the golden-ratio flag directly instead of a
+ *     BlockmodelTriplet, and block_merge::merge_blocks takes an optional step number
+ *     that keys its proposal stream;
+ *   - delta_mdl / block_merge_delta_mdl take (block or vertex, proposal) instead of a
+ *     Delta; batched forms score many moves per call.
+ * Errors: invalid arguments throw std::invalid_argument (as the reference); device
+ * errors and unsupported configurations throw sbp_gb300::Error.
+ */
+#ifndef SBP_GB300_HPP
+#define SBP_GB300_HPP
+
+#include <climits>
+#include <cmath>
+#include <cstdint>
+#include <limits>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <tuple>
+#include <utility>
+#include <vector>
+
+#include "sbpgpu.h"
+
+namespace sbp_gb300 {
+
+class Error : public std::runtime_error {
+  public:
+    Error(sbpgpu_status s, const std::string& what) : std::runtime_error(what), status(s) {}
+    sbpgpu_status status;
+};
+
+inline void check(sbpgpu_status s, const sbpgpu_ctx* ctx) {
+    if (s == SBPGPU_OK) return;
+    const std::string m = ctx ? sbpgpu_last_error(ctx) : "sbpgpu call failed";
+    if (s == SBPGPU_EINVAL) throw std::invalid_argument(m);
+    throw Error(s, m);
+}
+
+/// One CUDA device and stream.  Context::global() is the process-wide default on device 0.
+class Context {
+  public:
+    explicit Context(int device = 0) { check(sbpgpu_ctx_create(device, &h_), nullptr); }
+    ~Context() {
+        if (h_) sbpgpu_ctx_destroy(h_);  // device memory is released after its last graph
+    }
+    Context(const Context&) = delete;
+    Context& operator=(const Context&) = delete;
+    sbpgpu_ctx* get() const { return h_; }
+    static Context& global() {
+        static Context c(0);
+        return c;
+    }
+
+  private:
+    sbpgpu_ctx* h_ = nullptr;
+};
+
+/// The hot-path subset of the reference's Args.
+struct Args {
+    std::string algorithm = "hybrid_mcmc";  // async_gibbs | hybrid_mcmc | metropolis_hastings
+    int batches = 1;
+    float mh_percent = 0.075f;
+    bool greedy = true;
+    bool ordered = false;
+    bool approximate = false;
+    int asynciterations = INT_MAX;
+    bool nonparametric = false;
+    int threads = 1;                  // accepted for compatibility; the device uses every SM
+    uint64_t seed = 0;                // seeds the proposal stream
+    int max_iterations = 100;         // MAX_NUM_ITERATIONS (include/finetune.hpp:34)
+};
+
+/// The global arguments, as the reference's `args`.
+inline Args args;
+
+inline sbpgpu_config to_config(const Args& a) {
+    sbpgpu_config c;
+    sbpgpu_default_config(&c);
+    if (a.algorithm == "async_gibbs") c.algorithm = 0;
+    else if (a.algorithm == "hybrid_mcmc") c.algorithm = 1;
+    else if (a.algorithm == "metropolis_hastings") c.algorithm = 2;
+    else throw std::invalid_argument("unknown algorithm: " + a.algorithm);
+    if (a.nonparametric) throw Error(SBPGPU_EUNSUPPORTED, "nonparametric entropy is not implemented on the device");
+    if (a.batches < 1) throw std::invalid_argument("batches must be >= 1");
+    c.batches = a.batches;
+    c.mh_percent = a.mh_percent;
+    c.greedy = a.greedy ? 1 : 0;
+    c.ordered = a.ordered ? 1 : 0;
+    c.approximate = a.approximate ? 1 : 0;
+    c.asynciterations = a.asynciterations;
+    c.max_iterations = a.max_iterations;
+    return c;
+}
+
+using NeighborList = std::vector<std::vector<long>>;
+
+/// A directed graph resident on the device.  Edges keep their insertion order
+/// (Graph::add_edge, src/graph.cpp:10-18); self-loops and duplicates are kept.
+class Graph {
+  public:
+    Graph(long num_vertices, const std::vector<std::pair<long, long>>& edges, Context& ctx = Context::global())
+        : ctx_(&ctx), n_(num_vertices), out_(num_vertices), in_(num_vertices) {
+        std::vector<int32_t> src, dst;
+        src.reserve(edges.size());
+        dst.reserve(edges.size());
+        for (const auto& e : edges) {
+            if (e.first < 0 || e.first >= num_vertices || e.second < 0 || e.second >= num_vertices)
+                throw std::invalid_argument("edge endpoint out of range");
+            src.push_back((int32_t)e.first);
+            dst.push_back((int32_t)e.second);
+            out_[e.first].push_back(e.second);
+            in_[e.second].push_back(e.first);
+        }
+        upload(src, dst);
+    }
+    /// From neighbour lists (Graph(out, in, N, E)): the edges are taken from the
+    /// out-neighbour lists in vertex order.
+    Graph(const NeighborList& out_neighbors, const NeighborList& in_neighbors, long num_vertices, long num_edges,
+          Context& ctx = Context::global())
+        : ctx_(&ctx), n_(num_vertices), out_(out_neighbors), in_(in_neighbors) {
+        std::vector<int32_t> src, dst;
+        src.reserve(num_edges);
+        dst.reserve(num_edges);
+        for (long v = 0; v < (long)out_neighbors.size(); ++v)
+            for (long u : out_neighbors[v]) {
+                src.push_back((int32_t)v);
+                dst.push_back((int32_t)u);
+            }
+        upload(src, dst);
+    }
+    Graph(const Graph&) = delete;
+    Graph& operator=(const Graph&) = delete;
+    ~Graph() {
+        if (h_) sbpgpu_graph_destroy(h_);
+    }
+    long num_vertices() const { return n_; }
+    long num_edges() const { return e_; }
+    const NeighborList& out_neighbors() const { return out_; }
+    const NeighborList& in_neighbors() const { return in_; }
+    const std::vector<long>& out_neighbors(long v) const { return out_[v]; }
+    const std::vector<long>& in_neighbors(long v) const { return in_[v]; }
+    sbpgpu_graph* handle() const { return h_; }
+    Context& context() const { return *ctx_; }
+
+  private:
+    void upload(const std::vector<int32_t>& src, const std::vector<int32_t>& dst) {
+        e_ = (long)src.size();
+        check(sbpgpu_graph_create(ctx_->get(), n_, e_, src.data(), dst.data(), &h_), ctx_->get());
+    }
+    Context* ctx_;
+    long n_ = 0, e_ = 0;
+    NeighborList out_, in_;
+    sbpgpu_graph* h_ = nullptr;
+};
+
+/// The blockmodel: assignment, block degrees and sizes, and the block-edge-count matrix,
+/// all on the device (Blockmodel::initialize_edge_counts, src/blockmodel/blockmodel.cpp:193-276).
+class Blockmodel {
+  public:
+    Blockmodel(long num_blocks, const Graph& graph, double block_reduction_rate,
+               const std::vector<long>& block_assignment)
+        : graph_(&graph), rate_(block_reduction_rate) {
+        if ((long)block_assignment.size() != graph.num_vertices())
+            throw std::invalid_argument("assignment must have one block per vertex");
+        std::vector<int32_t> a(block_assignment.begin(), block_assignment.end());
+        sbpgpu_bm* h = nullptr;
+        check(sbpgpu_bm_create(graph.handle(), num_blocks, a.data(), &h), ctx());
+        h_.reset(h);
+        num_blocks_to_merge_ = (long)(num_blocks * rate_);
+    }
+    /// Every vertex in its own block is the reference's starting point (src/sbp.cpp:23);
+    /// here num_blocks must equal the number of vertices.
+    Blockmodel(long num_blocks, const Graph& graph, double block_reduction_rate)
+        : Blockmodel(num_blocks, graph, block_reduction_rate, range(graph.num_vertices())) {}
+    Blockmodel(Blockmodel&&) = default;
+    Blockmodel& operator=(Blockmodel&&) = default;
+
+    /// Blockmodel::copy (src/blockmodel/blockmodel.cpp:139-153), device to device.
+    Blockmodel copy() const {
+        sbpgpu_bm* h = nullptr;
+        check(sbpgpu_bm_copy(h_.get(), &h), ctx());
+        Blockmodel b(graph_, rate_, h);
+        b.entropy_ = entropy_;
+        b.num_blocks_to_merge_ = num_blocks_to_merge_;
+        return b;
+    }
+
+    long num_blocks() const { return (long)sbpgpu_bm_num_blocks(h_.get()); }
+    const std::vector<long>& block_assignment() const { return view().assignment; }
+    long block_assignment(long vertex) const { return view().assignment.at(vertex); }
+    const std::vector<long>& degrees_out() const { return view().d_out; }
+    const std::vector<long>& degrees_in() const { return view().d_in; }
+    const std::vector<long>& degrees() const { return view().d_tot; }
+    long degrees_out(long b) const { return view().d_out.at(b); }
+    long degrees_in(long b) const { return view().d_in.at(b); }
+    long degrees(long b) const { return view().d_tot.at(b); }
+    long block_size(long b) const { return view().sizes.at(b); }
+    /// The non-zero cells of the blockmatrix, row-major ascending: (row, col, count).
+    std::vector<std::tuple<long, long, long>> blockmatrix_cells() const {
+        const int64_t nnz = sbpgpu_bm_nnz(h_.get());
+        std::vector<int32_t> r(nnz), c(nnz);
+        std::vector<int64_t> v(nnz);
+        check(sbpgpu_bm_read(h_.get(), nullptr, nullptr, nullptr, nullptr, nullptr, r.data(), c.data(), v.data()),
+              ctx());
+        std::vector<std::tuple<long, long, long>> out(nnz);
+        for (int64_t i = 0; i < nnz; ++i) out[i] = std::make_tuple((long)r[i], (long)c[i], (long)v[i]);
+        return out;
+    }
+    double getOverall_entropy() const { return entropy_; }
+    void setOverall_entropy(double e) { entropy_ = e; }
+    long getNum_blocks_to_merge() const { return num_blocks_to_merge_; }
+    void setNum_blocks_to_merge(long n) { num_blocks_to_merge_ = n; }
+    double getBlock_reduction_rate() const { return rate_; }
+
+    sbpgpu_bm* handle() const { return h_.get(); }
+    const Graph& graph() const { return *graph_; }
+    /// Marks the host copies stale (every device-side mutation calls it).
+    void invalidate() { view_.reset(); }
+
+  private:
+    struct View {
+        std::vector<long> assignment, d_out, d_in, d_tot, sizes;
+    };
+    struct Deleter {
+        void operator()(sbpgpu_bm* b) const { sbpgpu_bm_destroy(b); }
+    };
+    Blockmodel(const Graph* g, double rate, sbpgpu_bm* h) : graph_(g), rate_(rate), h_(h) {}
+    static std::vector<long> range(long n) {
+        std::vector<long> a(n);
+        for (long i = 0; i < n; ++i) a[i] = i;
+        return a;
+    }
+    sbpgpu_ctx* ctx() const { return graph_->context().get(); }
+    const View& view() const {
+        if (!view_) {
+            const long n = graph_->num_vertices(), B = num_blocks();
+            std::vector<int32_t> a(n);
+            std::vector<int64_t> o(B), i(B), t(B), s(B);
+            check(sbpgpu_bm_read(h_.get(), a.data(), o.data(), i.data(), t.data(), s.data(), nullptr, nullptr, nullptr),
+                  ctx());
+            auto v = std::make_shared<View>();
+            v->assignment.assign(a.begin(), a.end());
+            v->d_out.assign(o.begin(), o.end());
+            v->d_in.assign(i.begin(), i.end());
+            v->d_tot.assign(t.begin(), t.end());
+            v->sizes.assign(s.begin(), s.end());
+            view_ = v;
+        }
+        return *view_;
+    }
+
+    const Graph* graph_;
+    double rate_ = 0.5;
+    std::unique_ptr<sbpgpu_bm, Deleter> h_;
+    double entropy_ = std::numeric_limits<double>::max();
+    long num_blocks_to_merge_ = 0;
+    mutable std::shared_ptr<View> view_;
+};
+
+namespace entropy {
+
+/// entropy::mdl (src/entropy.cpp:597-604).
+inline double mdl(const Blockmodel& blockmodel, const Graph& graph) {
+    double out = 0.0;
+    check(sbpgpu_mdl(blockmodel.handle(), &out), graph.context().get());
+    return out;
+}
+
+/// entropy::delta_mdl (src/entropy.cpp:298-403) for the moves vertices[i] -> proposals[i].
+inline std::vector<double> delta_mdl(const Blockmodel& blockmodel, const std::vector<long>& vertices,
+                                     const std::vector<long>& proposals) {
+    if (vertices.size() != proposals.size()) throw std::invalid_argument("vertices and proposals differ in length");
+    std::vector<int32_t> v(vertices.begin(), vertices.end()), s(proposals.begin(), proposals.end());
+    std::vector<double> out(v.size());
+    check(sbpgpu_delta_mdl_batch(blockmodel.handle(), (int64_t)v.size(), v.data(), s.data(), out.data()),
+          blockmodel.graph().context().get());
+    return out;
+}
+inline double delta_mdl(const Blockmodel& blockmodel, long vertex, long proposal) {
+    return delta_mdl(blockmodel, std::vector<long>{vertex}, std::vector<long>{proposal})[0];
+}
+
+/// entropy::block_merge_delta_mdl (src/entropy.cpp:129-182) for merging blocks[i] into proposals[i].
+inline std::vector<double> block_merge_delta_mdl(const Blockmodel& blockmodel, const std::vector<long>& blocks,
+                                                 const std::vector<long>& proposals) {
+    if (blocks.size() != proposals.size()) throw std::invalid_argument("blocks and proposals differ in length");
+    std::vector<int32_t> r(blocks.begin(), blocks.end()), s(proposals.begin(), proposals.end());
+    std::vector<double> out(r.size());
+    check(sbpgpu_merge_delta_mdl_batch(blockmodel.handle(), (int64_t)r.size(), r.data(), s.data(), out.data()),
+          blockmodel.graph().context().get());
+    return out;
+}
+inline double block_merge_delta_mdl(const Blockmodel& blockmodel, long block, long proposal) {
+    return block_merge_delta_mdl(blockmodel, std::vector<long>{block}, std::vector<long>{proposal})[0];
+}
+
+/// entropy::null_mdl_v1 (src/entropy.cpp:571-585): the one-block model's description length.
+inline double null_mdl_v1(const Graph& graph) {
+    const double E = (double)graph.num_edges();
+    const double log_posterior_p = E * std::log(1.0 / E);
+    const double x = 1.0 / E;
+    const double h = ((1 + x) * std::log(1 + x)) - (x * std::log(x));
+    return (E * h) - log_posterior_p;
+}
+/// entropy::normalize_mdl_v1 (src/entropy.cpp:563-565).
+inline double normalize_mdl_v1(double mdl, const Graph& graph) { return mdl / null_mdl_v1(graph); }
+
+}  // namespace entropy
+
+namespace finetune {
+
+/// finetune::mcmc (src/finetune.cpp:754-771) with the algorithm of sbp_gb300::args.
+inline Blockmodel& mcmc(int iteration, const Graph& graph, Blockmodel& blockmodel, bool golden_ratio_not_reached,
+                        const Args& a = args) {
+    const sbpgpu_config cfg = to_config(a);
+    sbpgpu_stats st;
+    check(sbpgpu_mcmc(blockmodel.handle(), &cfg, a.seed, iteration, golden_ratio_not_reached ? 1 : 0, &st),
+          graph.context().get());
+    blockmodel.invalidate();
+    blockmodel.setOverall_entropy(sbpgpu_bm_entropy(blockmodel.handle()));
+    return blockmodel;
+}
+namespace detail {
+inline Blockmodel& run(const char* algorithm, Blockmodel& bm, const Graph& g, bool golden, int iteration) {
+    Args a = args;
+    a.algorithm = algorithm;
+    return mcmc(iteration, g, bm, golden, a);
+}
+}  // namespace detail
+/// finetune::asynchronous_gibbs (src/finetune.cpp:34-107).
+inline Blockmodel& asynchronous_gibbs(Blockmodel& bm, const Graph& g, bool golden_ratio_not_reached, int iteration = 0) {
+    return detail::run("async_gibbs", bm, g, golden_ratio_not_reached, iteration);
+}
+/// finetune::hybrid_mcmc (src/finetune.cpp:563-646).
+inline Blockmodel& hybrid_mcmc(Blockmodel& bm, const Graph& g, bool golden_ratio_not_reached, int iteration = 0) {
+    return detail::run("hybrid_mcmc", bm, g, golden_ratio_not_reached, iteration);
+}
+/// finetune::metropolis_hastings (src/finetune.cpp:773-820).
+inline Blockmodel& metropolis_hastings(Blockmodel& bm, const Graph& g, bool golden_ratio_not_reached,
+                                       int iteration = 0) {
+    return detail::run("metropolis_hastings", bm, g, golden_ratio_not_reached, iteration);
+}
+
+}  // namespace finetune
+
+namespace block_merge {
+
+/// block_merge::merge_blocks (src/block_merge.cpp:178-228): merges
+/// blockmodel.getNum_blocks_to_merge() blocks; `step` keys the proposal stream.
+inline Blockmodel& merge_blocks(Blockmodel& blockmodel, const Graph& graph, long /*num_edges*/, int step = 0,
+                                const Args& a = args) {
+    const sbpgpu_config cfg = to_config(a);
+    sbpgpu_stats st;
+    check(sbpgpu_merge_blocks(blockmodel.handle(), &cfg, a.seed, step, blockmodel.getNum_blocks_to_merge(), &st),
+          graph.context().get());
+    blockmodel.invalidate();
+    blockmodel.setNum_blocks_to_merge((long)(blockmodel.num_blocks() * blockmodel.getBlock_reduction_rate()));
+    return blockmodel;
+}
+
+}  // namespace block_merge
+
+namespace sbp {
+
+/// sbp::stochastic_block_partition (src/sbp.cpp:16-72): the golden-section search over
+/// block counts with merge passes and MCMC, all on the device.
+inline Blockmodel stochastic_block_partition(Graph& graph, Args& a, bool divide_and_conquer = false) {
+    if (divide_and_conquer)
+        throw Error(SBPGPU_EUNSUPPORTED, "divide-and-conquer SBP is outside the device hot path");
+    const sbpgpu_config cfg = to_config(a);
+    std::vector<int32_t> out(graph.num_vertices());
+    int64_t B = 0;
+    double mdl = 0.0;
+    sbpgpu_stats st;
+    check(sbpgpu_sbp(graph.handle(), &cfg, a.seed, out.data(), &B, &mdl, &st), graph.context().get());
+    Blockmodel bm(B, graph, 0.5, std::vector<long>(out.begin(), out.end()));
+    bm.setOverall_entropy(mdl);
+    return bm;
+}
+
+}  // namespace sbp
+
+}  // namespace sbp_gb300
+
+#endif
