@@ -99,6 +99,19 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def combine_ranks(device_s, proposals, device):
+    """Replicas: the slowest rank's time and the proposals of all ranks (max / sum over the
+    process group when one is initialised)."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(device_s)], dtype=torch.float64, device=device)
+    p = torch.tensor([float(proposals)], dtype=torch.float64, device=device)
+    if dist.is_available() and dist.is_initialized() and dist.get_world_size() > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dist.all_reduce(p, op=dist.ReduceOp.SUM)
+    return t.item(), p.item()
+
+
 def measured_peak_hbm():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -286,12 +299,8 @@ def main():
     ctx.set_timing(False)
     device_s = sum(step_ms) / 1e3
     proposals = totals["proposals"] + totals["merge_proposals"]
-    local_time = torch.tensor([device_s], dtype=torch.float64, device=local)
-    local_props = torch.tensor([float(proposals)], dtype=torch.float64, device=local)
-    if ws > 1:
-        torch.distributed.all_reduce(local_time, op=torch.distributed.ReduceOp.MAX)
-        torch.distributed.all_reduce(local_props, op=torch.distributed.ReduceOp.SUM)
-    value = local_props.item() / local_time.item()
+    slowest_s, all_props = combine_ranks(device_s, proposals, local)
+    value = all_props / slowest_s
 
     # end to end through the C ABI with host buffers: graph upload + partition + result read
     e2e_s, e2e_props = 0.0, 0
