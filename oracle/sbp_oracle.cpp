@@ -362,7 +362,30 @@ int64_t merge_dS_fixed(const ora_bm* bm, int64_t r, int64_t s) {
     return merge_delta_mdl_generic<int64_t>(bm, r, s, d, ce_fixed);
 }
 
-/* entropy::hastings_correction(vertex, ...) (entropy.cpp:497-561). */
+/* A non-negative double as an integer count of 2^-64 units (truncated): every term of the
+ * Hastings sums goes through this, so the sums are exact integers and do not depend on the
+ * order in which the neighbour blocks are visited (the device sums them in parallel). */
+inline __int128 to_fix64(double x) {
+    uint64_t bits;
+    std::memcpy(&bits, &x, 8);
+    const int e = (int)((bits >> 52) & 0x7ff);
+    if (e == 0 || (bits >> 63)) return 0;
+    const uint64_t mant = (bits & ((1ull << 52) - 1)) | (1ull << 52);
+    const int sh = e - 1075 + 64;
+    if (sh >= 0) return (__int128)mant << sh;
+    if (sh <= -64) return 0;
+    return (__int128)(mant >> (-sh));
+}
+inline double fix64_to_double(__int128 q) {
+    const int64_t hi = (int64_t)(q >> 64);
+    const uint64_t lo = (uint64_t)q;
+    return (double)hi * 18446744073709551616.0 + (double)lo;
+}
+
+/* entropy::hastings_correction(vertex, ...) (entropy.cpp:497-561).  The reference sums
+ * counts * weights / degrees over the distinct neighbour blocks in hash-map order; here each
+ * term is the same double, accumulated exactly in 2^-64 units, and the ratio is taken of
+ * the two sums converted back to double. */
 double hastings(const ora_bm* bm, int64_t v, int64_t s, const DeltaMap& d, int64_t num_neighbor_edges,
                 const ora_config* cfg) {
     if (num_neighbor_edges == 0 || cfg->greedy) return 1.0;
@@ -372,7 +395,7 @@ double hastings(const ora_bm* bm, int64_t v, int64_t s, const DeltaMap& d, int64
     std::map<int32_t, int64_t> counts;
     for (int32_t u : g->out[v]) counts[bm->asg[u]] += 1;
     for (int32_t w : g->inns[v]) counts[bm->asg[w]] += 1;
-    double pf = 0.0, pb = 0.0;
+    __int128 pf = 0, pb = 0;
     const double B = (double)bm->B;
     for (const auto& e : counts) {
         const int64_t b = e.first;
@@ -388,10 +411,10 @@ double hastings(const ora_bm* bm, int64_t v, int64_t s, const DeltaMap& d, int64
             const int64_t self = bm->get(s, s) + delta_get(d, s, s);
             nd = (bm->dout[s] + vi.kout) + (bm->din[s] + vi.kin) - self;
         }
-        pf += cnt * pw / bd;
-        pb += cnt * bw / ((double)nd + B);
+        pf += to_fix64(cnt * pw / bd);
+        pb += to_fix64(cnt * bw / ((double)nd + B));
     }
-    return pb / pf;
+    return fix64_to_double(pb) / fix64_to_double(pf);
 }
 
 /* finetune::accept (finetune.cpp:22-32). */

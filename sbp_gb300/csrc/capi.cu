@@ -369,7 +369,11 @@ void chain_run(sbpgpu_bm* bm, const int32_t* order, int32_t n, int32_t max_k, in
     WindowPlan plan{};
     if (mh_window_plan(bm->d.B, max_k, g->w, &plan)) {
         Span sp(g->ctx, 1);
-        mh_chain_window(g->dg, bm->d, order, n, plan, seed, it, step, g->w, g->ctx->stream);
+        mh_chain_window(g->dg, bm->d, order, n, plan, seed, it, step, greedy, g->w, g->ctx->stream);
+    } else if (!greedy) {
+        throw ApiError(SBPGPU_EUNSUPPORTED,
+                       "non-greedy acceptance needs the windowed chain (vertex degree <= 4096 and the dense "
+                       "cell budget holding the blockmodel)");
     } else if (bm->d.B <= kDenseMax || bm->d.B <= g->w.dense_cap) {
         Span sp(g->ctx, 1);
         mh_chain_dense(g->dg, bm->d, order, n, seed, it, step, g->w, g->ctx->stream);
@@ -384,15 +388,9 @@ void chain_run(sbpgpu_bm* bm, const int32_t* order, int32_t n, int32_t max_k, in
     do_rebuild(bm);
 }
 
-void require_greedy(const sbpgpu_config& cfg) {
-    if (!cfg.greedy)
-        throw ApiError(SBPGPU_EUNSUPPORTED, "non-greedy acceptance (--greedy switch set) is not implemented on the device");
-}
-
 void async_gibbs(sbpgpu_bm* bm, const sbpgpu_config& cfg, uint64_t seed, int32_t step, bool golden) {
     sbpgpu_graph* g = bm->g;
     if (bm->d.B == 1) return;
-    require_greedy(cfg);
     std::vector<double> deltas;
     const double initial = do_mdl(bm);
     bm->entropy = initial;
@@ -423,7 +421,6 @@ void async_gibbs(sbpgpu_bm* bm, const sbpgpu_config& cfg, uint64_t seed, int32_t
 void hybrid_mcmc(sbpgpu_bm* bm, const sbpgpu_config& cfg, uint64_t seed, int32_t step, bool golden) {
     sbpgpu_graph* g = bm->g;
     if (bm->d.B == 1) return;
-    require_greedy(cfg);
     ensure_split(g, cfg.mh_percent);
     std::vector<double> deltas;
     const double initial = do_mdl(bm);
@@ -464,7 +461,6 @@ void hybrid_mcmc(sbpgpu_bm* bm, const sbpgpu_config& cfg, uint64_t seed, int32_t
 void metropolis_hastings(sbpgpu_bm* bm, const sbpgpu_config& cfg, uint64_t seed, int32_t step, bool golden) {
     sbpgpu_graph* g = bm->g;
     if (bm->d.B == 1) return;
-    require_greedy(cfg);
     std::vector<double> deltas;
     bm->entropy = do_mdl(bm);
     int64_t ksum = 0;
@@ -1006,7 +1002,6 @@ sbpgpu_status sbpgpu_gibbs_batch(sbpgpu_bm* bm, const sbpgpu_config* cfg, int64_
     if (!bm || !cfg || n < 0 || (n && !vertex)) return SBPGPU_EINVAL;
     sbpgpu_graph* g = bm->g;
     return guarded(g->ctx, [&] {
-        require_greedy(*cfg);
         if (bm->d.B < 2) throw ApiError(SBPGPU_EINVAL, "proposals need at least two blocks");
         for (int64_t i = 0; i < n; ++i)
             if (vertex[i] < 0 || vertex[i] >= g->N) throw ApiError(SBPGPU_EINVAL, "vertex out of range");
@@ -1033,7 +1028,6 @@ sbpgpu_status sbpgpu_mh_chain(sbpgpu_bm* bm, const sbpgpu_config* cfg, int64_t n
     if (!bm || !cfg || n < 0 || (n && !vertex)) return SBPGPU_EINVAL;
     sbpgpu_graph* g = bm->g;
     return guarded(g->ctx, [&] {
-        require_greedy(*cfg);
         if (bm->d.B < 2) throw ApiError(SBPGPU_EINVAL, "proposals need at least two blocks");
         int32_t max_k = 0;
         int64_t ksum = 0;
@@ -1109,7 +1103,6 @@ sbpgpu_status sbpgpu_sbp(sbpgpu_graph* g, const sbpgpu_config* cfg_in, uint64_t 
     std::vector<void*> slots_mem;
     const sbpgpu_status rc = guarded(ctx, [&] {
         const sbpgpu_config cfg = *cfg_in;
-        require_greedy(cfg);
         g->st = sbpgpu_stats{};
         const int64_t l0 = kernel_launches();
         reset_counters(g);

@@ -363,7 +363,7 @@ __device__ __forceinline__ bool in_touched(const WinResult& c, const int32_t* hk
 template <int kMode>
 __global__ void __launch_bounds__(kWinMaxWarps * 32, 1)
     k_mh_window(DevGraph g, DevBM bm, const int32_t* __restrict__ order, int32_t n, uint64_t seed, uint32_t iter,
-                uint32_t step, GlobalCells gc, int32_t ld, int log2cap, int nwarps, DevFlags* flags) {
+                uint32_t step, GlobalCells gc, int32_t ld, int log2cap, int nwarps, bool greedy, DevFlags* flags) {
     constexpr bool kShared = kMode == 0;
     constexpr bool kGlobalDeg = kMode == 2;
     extern __shared__ int32_t sm[];
@@ -458,7 +458,17 @@ __global__ void __launch_bounds__(kWinMaxWarps * 32, 1)
                     warp_gather(g, bm.asg, c.v, o0, c.kout, i0, c.k, hk, hO, hI, c.l2);
                     c.dS = kShared ? warp_delta(g, dout, din, sc, c.r, s, c.kout, c.kin, c.L, hk, hO, hI, c.l2, items)
                                    : warp_delta(g, dout, din, gc, c.r, s, c.kout, c.kin, c.L, hk, hO, hI, c.l2, items);
-                    c.status = c.dS < 0 ? ST_ACCEPT : ST_REJECT;  // greedy accept (finetune.cpp:22-25)
+                    double H = 1.0;
+                    if (!greedy && c.k > 0) {  // entropy::hastings_correction (entropy.cpp:497-561)
+                        H = kShared ? hastings_fixed<32>(sc, [&](int32_t b) { return dout[b] + din[b] - sc.row_get(b, b); },
+                                                         dout, din, B, c.r, s, c.kout, c.kin, c.L, hk, hO, hI, c.l2,
+                                                         nullptr)
+                                    : hastings_fixed<32>(gc, [&](int32_t b) { return dout[b] + din[b] - gc.row_get(b, b); },
+                                                         dout, din, B, c.r, s, c.kout, c.kin, c.L, hk, hO, hI, c.l2,
+                                                         nullptr);
+                    }
+                    // finetune::accept (finetune.cpp:22-32)
+                    c.status = accept_move(c.dS, H, greedy, w[3]) ? ST_ACCEPT : ST_REJECT;
                 }
             }
             if (lane == 0) res[wid] = c;
@@ -606,13 +616,13 @@ bool mh_window_plan(int32_t B, int32_t max_k, const Work& w, WindowPlan* p) {
 }
 
 void mh_chain_window(const DevGraph& g, DevBM& bm, const int32_t* order, int32_t n, const WindowPlan& p,
-                     uint64_t seed, uint32_t iter, uint32_t step, Work& w, cudaStream_t st) {
+                     uint64_t seed, uint32_t iter, uint32_t step, int greedy, Work& w, cudaStream_t st) {
     if (n <= 0) return;
     const size_t smem = window_smem(bm.B, p.mode, p.log2cap, p.nw);
     if (p.mode == 0) {
         cudaFuncSetAttribute(k_mh_window<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         k_mh_window<0><<<1, 32 * p.nw, smem, st>>>(g, bm, order, n, seed, iter, step, GlobalCells{}, (int32_t)p.ld,
-                                                   p.log2cap, p.nw, w.flags_dev);
+                                                   p.log2cap, p.nw, greedy != 0, w.flags_dev);
         count_launches(1);
         return;
     }
@@ -632,11 +642,11 @@ void mh_chain_window(const DevGraph& g, DevBM& bm, const int32_t* order, int32_t
     if (p.mode == 1) {
         cudaFuncSetAttribute(k_mh_window<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         k_mh_window<1><<<1, 32 * p.nw, smem, st>>>(g, bm, order, n, seed, iter, step, gc, (int32_t)p.ld, p.log2cap,
-                                                   p.nw, w.flags_dev);
+                                                   p.nw, greedy != 0, w.flags_dev);
     } else {
         cudaFuncSetAttribute(k_mh_window<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         k_mh_window<2><<<1, 32 * p.nw, smem, st>>>(g, bm, order, n, seed, iter, step, gc, (int32_t)p.ld, p.log2cap,
-                                                   p.nw, w.flags_dev);
+                                                   p.nw, greedy != 0, w.flags_dev);
     }
     count_launches(2);
 }

@@ -264,6 +264,148 @@ __device__ long long vertex_delta_fixed(const DevGraph& g, const int32_t* asg, c
     return tot;
 }
 
+// ------------------------------------------------------------------ Hastings correction
+// entropy::hastings_correction (reference src/entropy.cpp:497-561) for the non-greedy
+// acceptance.  Each term counts * weights / degrees is the same IEEE double as on the
+// host; the two sums are accumulated exactly as integers of 2^-64 units (truncated), so
+// they do not depend on the order in which the neighbour blocks are visited, and the
+// ratio is taken of the sums converted back to double.
+__device__ __forceinline__ __int128 to_fix64(double x) {
+    const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
+    const int e = (int)((bits >> 52) & 0x7ff);
+    if (e == 0 || (bits >> 63)) return 0;
+    const unsigned long long mant = (bits & ((1ull << 52) - 1)) | (1ull << 52);
+    const int sh = e - 1075 + 64;
+    if (sh >= 0) return (__int128)mant << sh;
+    if (sh <= -64) return 0;
+    return (__int128)(mant >> (-sh));
+}
+__device__ __forceinline__ double fix64_to_double(__int128 q) {
+    const long long hi = (long long)(q >> 64);
+    const unsigned long long lo = (unsigned long long)q;
+    return __dadd_rn(__dmul_rn((double)hi, 18446744073709551616.0), (double)lo);
+}
+__device__ __forceinline__ __int128 warp_sum_i128(__int128 x) {
+    unsigned long long lo = (unsigned long long)x;
+    long long hi = (long long)(x >> 64);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long lo2 = __shfl_xor_sync(SBP_FULL_MASK, lo, o);
+        const long long hi2 = __shfl_xor_sync(SBP_FULL_MASK, hi, o);
+        const unsigned long long sum = lo + lo2;
+        hi = hi + hi2 + (sum < lo ? 1 : 0);
+        lo = sum;
+    }
+    return ((__int128)hi << 64) | (__int128)lo;
+}
+
+// One neighbour block's terms of the forward and backward proposal sums.
+struct HastingsTerm {
+    __int128 pf, pb;
+};
+
+// Sums over the group's neighbour hash (blocks b with out / in neighbour counts O, I of v)
+// for moving v from r to s.  M: cells before the move; dtot(b): block total degree before
+// the move.  kout counts v's out-edges including self-loops, kin its in-edges without them,
+// L its self-loops (they count toward block r).
+template <int kThreads, typename Acc, typename DTot>
+__device__ double hastings_fixed(const Acc& M, DTot dtot, const int32_t* d_out, const int32_t* d_in, int32_t B,
+                                 int32_t r, int32_t s, int32_t kout, int32_t kin, int32_t L, const int32_t* hk,
+                                 const int32_t* hO, const int32_t* hI, int log2cap, long long (*red)[8]) {
+    typedef Group<kThreads> G;
+    const int t = G::rank();
+    const int cap = 1 << log2cap;
+    const double Bd = (double)B;
+    // cells of the move's own rows / columns before and after (blockmodel_delta, finetune.cpp:201-235)
+    int32_t Or = 0, Ir = 0, Os = 0, Is = 0, has_r = 0;
+    for (int i = t; i < cap; i += kThreads) {
+        const int32_t b = hk[i];
+        if (b == r) {
+            Or = hO[i];
+            Ir = hI[i];
+            has_r = 1;
+        } else if (b == s) {
+            Os = hO[i];
+            Is = hI[i];
+        }
+    }
+    {
+        long long v[5] = {Or, Ir, Os, Is, has_r};
+        G::template sum<5>(v, red);
+        Or = (int32_t)v[0];
+        Ir = (int32_t)v[1];
+        Os = (int32_t)v[2];
+        Is = (int32_t)v[3];
+        has_r = (int32_t)v[4];
+    }
+    const int32_t Mrr = M.row_get(r, r), Mrs = M.row_get(r, s), Msr = M.row_get(s, r), Mss = M.row_get(s, s);
+    const int32_t drr = -Or - Ir - L, drs = Ir - Os, dsr = Or - Is, dss = Os + Is + L;
+    auto term = [&](int32_t b, int32_t cntO, int32_t cntI) {
+        const int32_t cnt = cntO + cntI + (b == r ? L : 0);
+        const double pw = (double)(M.row_get(s, b) + M.col_get(s, b)) + 1.0;
+        const double bd = (double)dtot(b) + Bd;
+        long long bw, nd;
+        if (b == r) {
+            bw = 2ll * (Mrr + drr);
+            nd = ((long long)d_out[r] - kout) + ((long long)d_in[r] - kin) - (Mrr + drr);
+        } else if (b == s) {
+            bw = (long long)(Mrs + drs) + (Msr + dsr);
+            nd = ((long long)d_out[s] + kout) + ((long long)d_in[s] + kin) - (Mss + dss);
+        } else {
+            bw = (long long)(M.row_get(r, b) - cntO) + (M.col_get(r, b) - cntI);
+            nd = dtot(b);
+        }
+        HastingsTerm h;
+        h.pf = to_fix64(__ddiv_rn(__dmul_rn((double)cnt, pw), bd));
+        h.pb = to_fix64(__ddiv_rn(__dmul_rn((double)cnt, (double)bw + 1.0), (double)nd + Bd));
+        return h;
+    };
+    __int128 pf = 0, pb = 0;
+    for (int i = t; i < cap; i += kThreads) {
+        const int32_t b = hk[i];
+        if (b < 0) continue;
+        const HastingsTerm h = term(b, hO[i], hI[i]);
+        pf += h.pf;
+        pb += h.pb;
+    }
+    if (t == 0 && L > 0 && !has_r) {  // block r reached only through self-loops
+        const HastingsTerm h = term(r, 0, 0);
+        pf += h.pf;
+        pb += h.pb;
+    }
+    pf = warp_sum_i128(pf);
+    pb = warp_sum_i128(pb);
+    if (kThreads > 32) {
+        const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+        __syncthreads();
+        if (lane == 0) {
+            red[w][0] = (long long)(unsigned long long)pf;
+            red[w][1] = (long long)(pf >> 64);
+            red[w][2] = (long long)(unsigned long long)pb;
+            red[w][3] = (long long)(pb >> 64);
+        }
+        __syncthreads();
+        pf = 0;
+        pb = 0;
+        for (int i = 0; i < kThreads / 32; ++i) {
+            pf += ((__int128)red[i][1] << 64) | (__int128)(unsigned long long)red[i][0];
+            pb += ((__int128)red[i][3] << 64) | (__int128)(unsigned long long)red[i][2];
+        }
+        __syncthreads();
+    }
+    return __ddiv_rn(fix64_to_double(pb), fix64_to_double(pf));
+}
+
+// finetune::accept (reference src/finetune.cpp:22-32): greedy takes dS < 0; otherwise the
+// uniform draw u = w3 / 2^32 of the proposal's counter against min(1, e^(-3 dS) H).
+__device__ __forceinline__ bool accept_move(long long dS_fixed, double H, bool greedy, uint32_t w3) {
+    if (greedy) return dS_fixed < 0;
+    const double u = (double)w3 * (1.0 / 4294967296.0);
+    double p = exp(-3.0 * fixed_to_double(dS_fixed)) * H;
+    p = p >= 1.0 ? 1.0 : p;
+    return u <= p;
+}
+
 // ------------------------------------------------------------------ merge delta-MDL
 // entropy::block_merge_delta_mdl for merging r into s over the static CSR/CSC.
 template <int kThreads>

@@ -105,7 +105,7 @@ uint64_t mh_window_cells(int32_t B);
 // no dense buffer holds the matrices).
 bool mh_window_plan(int32_t B, int32_t max_k, const Work& w, WindowPlan* p);
 void mh_chain_window(const DevGraph& g, DevBM& bm, const int32_t* order, int32_t n, const WindowPlan& p,
-                     uint64_t seed, uint32_t iter, uint32_t step, Work& w, cudaStream_t st);
+                     uint64_t seed, uint32_t iter, uint32_t step, int greedy, Work& w, cudaStream_t st);
 // order[i] = base[perm(i)] with the canonical shuffle keyed by (i, iter, step, dom).
 void shuffle(const int32_t* base, int32_t n, uint64_t seed, uint32_t iter, uint32_t step, uint32_t dom,
              int32_t* order, Work& w, cudaStream_t st);

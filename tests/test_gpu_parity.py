@@ -263,3 +263,55 @@ def test_full_sbp_identical_c1(gpu, oracle, alg):
     assert np.array_equal(asg, oasg)
     assert abs(mdl - omdl) <= MDL_REL_TOL_CANONICAL * abs(omdl)
     assert st["merges"] == ost.merges and st["mcmc_iterations"] == ost.mcmc_iterations
+
+
+# ---- non-greedy acceptance: min(1, e^(-3 dS) H) against the proposal's uniform draw,
+# H the Hastings correction (entropy.cpp:497-561, finetune.cpp:22-32).  Decisions are
+# bit-exact with the oracle: both sides form the same IEEE terms and sum them exactly
+# as 2^-64 fixed point; only e^x may differ in its last bit, which changes a decision
+# only when the draw falls within one ulp of the acceptance probability.
+
+@pytest.mark.parametrize("B", [6, 900])
+def test_gibbs_batch_identical_non_greedy(gpu, oracle, B):
+    G, O, gb, ob, a, _ = make_pair(gpu, oracle, 2500, 30000, 9, B, seed=140 + B)
+    cfg = oracle.make_config("async_gibbs", greedy=False)
+    args = gpu.Args(algorithm="async_gibbs", greedy=False)
+    verts = np.arange(2500, dtype=np.int32)
+    for it in range(3):
+        mv_g, app_g = gpu.finetune.gibbs_batch(gb, verts, seed=5, iteration=it, step=2, args=args)
+        n_o, mv_o, _ = ob.gibbs_batch(verts, 5, it, 2, cfg)
+        assert np.array_equal(mv_g, mv_o)
+        assert app_g == n_o
+        same_state(gb, ob)
+
+
+@pytest.mark.parametrize("n,B", [(2500, 120), (2500, 1500), (24000, 16000)])
+def test_mh_chain_identical_non_greedy(gpu, oracle, n, B):
+    """The three cell stores of the windowed chain with the Hastings-corrected rule."""
+    G, O, gb, ob, a, _ = make_pair(gpu, oracle, n, 12 * n, 9, B, seed=150 + B)
+    order = np.random.default_rng(B).permutation(n)[:600].astype(np.int32)
+    applied = gpu.finetune.mh_chain(gb, order, seed=8, iteration=1, step=3,
+                                    args=gpu.Args(algorithm="hybrid_mcmc", greedy=False))
+    want = ob.mh_chain(order, 8, 1, 3, oracle.make_config("hybrid_mcmc", greedy=False))
+    assert applied == want
+    same_state(gb, ob)
+
+
+@pytest.mark.parametrize("alg", ["async_gibbs", "hybrid_mcmc", "metropolis_hastings"])
+def test_mcmc_identical_non_greedy(gpu, oracle, alg):
+    G, O, gb, ob, a, _ = make_pair(gpu, oracle, 2000, 24000, 9, 150, seed=160)
+    gpu.finetune.mcmc(2, G, gb, True, gpu.Args(algorithm=alg, seed=13, max_iterations=6, greedy=False))
+    ob.mcmc(oracle.make_config(alg, max_iterations=6, greedy=False), seed=13, step=2, golden_ratio_not_reached=True)
+    same_state(gb, ob)
+
+
+def test_full_sbp_identical_c1_non_greedy(gpu, oracle):
+    src, dst, planted = gpu.dcsbm.generate_config("C1", seed=0)
+    G = gpu.Graph(1000, src, dst)
+    a_g, B_g, mdl_g, _ = gpu.sbp.stochastic_block_partition(G, gpu.Args(algorithm="hybrid_mcmc", seed=3,
+                                                                        greedy=False))
+    O = oracle.Graph(1000, src, dst)
+    a_o, B_o, mdl_o, _ = oracle.sbp(O, oracle.make_config("hybrid_mcmc", greedy=False), seed=3)
+    assert B_g == B_o
+    assert np.array_equal(a_g, a_o)
+    assert abs(mdl_g - mdl_o) <= MDL_REL_TOL_CANONICAL * abs(mdl_o)
