@@ -250,6 +250,7 @@ void alloc_work(sbpgpu_graph* g) {
     w.root = dalloc<int32_t>(o, N);
     w.used = dalloc<int32_t>(o, N);
     w.flags_dev = dalloc<DevFlags>(o, 1);
+    w.win_hash = dalloc<int32_t>(o, (size_t)16 * 4 * 8192);
     w.dense_cap = (int32_t)std::min<int64_t>(N, kDenseGlobalMax);
     if (w.dense_cap > kDenseMax) {
         w.dense_M = dalloc<int32_t>(o, (size_t)w.dense_cap * w.dense_cap);

@@ -19,7 +19,9 @@
 //
 // Cell counts: B x B dense in shared memory (B <= kWinSharedMax) or dense M and its
 // transpose in global memory (leading dimension a multiple of 4); degrees and sizes in
-// shared memory.  Only the assignment is written back; the caller rebuilds afterwards.
+// shared memory unless B is large.  Each warp's neighbour hash lives in shared memory (up
+// to 512 slots) or, for vertices of degree above 256, in a per-warp global region.  Only
+// the assignment is written back; the caller rebuilds afterwards.
 #include "delta.cuh"
 #include "kernels.cuh"
 
@@ -28,6 +30,9 @@ namespace sbp {
 namespace {
 
 constexpr int kWinMaxWarps = 16;
+constexpr int kSmemHashL2 = 9;     // neighbour hashes up to 512 slots live in shared memory
+constexpr int kGlobalHashL2 = 13;  // larger ones (degree > 256) in a per-warp global region
+constexpr int kLqCache = 2048;     // log-table entries copied into shared memory
 
 enum : int32_t { ST_SKIP = 0, ST_NOMOVE = 1, ST_REJECT = 2, ST_ACCEPT = 3 };
 
@@ -211,12 +216,14 @@ __device__ __forceinline__ int32_t warp_select_tiles(const int32_t* __restrict__
 // Neighbour-block counts of v into the warp's hash (edge_weights + the block lookups of
 // blockmodel_delta): out-neighbours except v itself into hO, in-neighbours (self-loops
 // already excluded) into hI.  Neighbour ids, then their blocks, are loaded 8 per lane
-// before any insert.
-__device__ __forceinline__ void warp_gather(const DevGraph& g, const int32_t* asg, int32_t v, int32_t o0,
-                                            int32_t kout, int32_t i0, int32_t k, int32_t* hk, int32_t* hO,
-                                            int32_t* hI, int log2cap) {
+// before any insert.  Returns the block of neighbour number `pick` (the proposal's
+// sampled neighbour), or -1 when pick is out of range.
+__device__ __forceinline__ int32_t warp_gather(const DevGraph& g, const int32_t* asg, int32_t v, int32_t r,
+                                               int32_t o0, int32_t kout, int32_t i0, int32_t k, int32_t pick,
+                                               int32_t* hk, int32_t* hO, int32_t* hI, int log2cap) {
     const int lane = threadIdx.x & 31;
     const int cap = 1 << log2cap;
+    int32_t nb = -1;
     for (int i = lane; i < cap; i += 32) {
         hk[i] = -1;
         hO[i] = 0;
@@ -235,6 +242,17 @@ __device__ __forceinline__ void warp_gather(const DevGraph& g, const int32_t* as
             const int32_t idx = base + lane + 32 * j;
             b[j] = (u[j] >= 0 && !(idx < kout && u[j] == v)) ? __ldcg(asg + u[j]) : -1;
         }
+        if (pick >= base && pick < base + 256) {  // the sampled neighbour's block (its own block for a self-loop)
+            const int q = (pick - base) >> 5, owner = (pick - base) & 31;
+            int32_t bq = b[0], uq = u[0];
+#pragma unroll
+            for (int j = 1; j < 8; ++j)
+                if (j == q) {
+                    bq = b[j];
+                    uq = u[j];
+                }
+            nb = __shfl_sync(SBP_FULL_MASK, uq == v ? r : bq, owner);
+        }
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
             const int32_t idx = base + lane + 32 * j;
@@ -242,6 +260,7 @@ __device__ __forceinline__ void warp_gather(const DevGraph& g, const int32_t* as
         }
     }
     __syncwarp();
+    return nb;
 }
 
 // entropy::delta_mdl for moving v from r to s over the gathered neighbour blocks; the same
@@ -250,10 +269,11 @@ __device__ __forceinline__ void warp_gather(const DevGraph& g, const int32_t* as
 template <class Cells>
 __device__ long long warp_delta(const DevGraph& g, const int32_t* d_out, const int32_t* d_in, const Cells& M,
                                 int32_t r, int32_t s, int32_t kout, int32_t kin, int32_t L, const int32_t* hk,
-                                const int32_t* hO, const int32_t* hI, int log2cap, int32_t* items) {
+                                const int32_t* hO, const int32_t* hI, int log2cap, int32_t* items,
+                                const int32_t* lq_cache) {
     const int lane = threadIdx.x & 31;
     const int cap = 1 << log2cap;
-    const LogTab Lq{g.Lq, g.E + 1};
+    const LogTab Lq{g.Lq, g.E + 1, lq_cache, kLqCache};
     int32_t Or = 0, Ir = 0, Os = 0, Is = 0, n = 0;
     for (int base = 0; base < cap; base += 32) {
         const int i = base + lane;
@@ -363,7 +383,8 @@ __device__ __forceinline__ bool in_touched(const WinResult& c, const int32_t* hk
 template <int kMode>
 __global__ void __launch_bounds__(kWinMaxWarps * 32, 1)
     k_mh_window(DevGraph g, DevBM bm, const int32_t* __restrict__ order, int32_t n, uint64_t seed, uint32_t iter,
-                uint32_t step, GlobalCells gc, int32_t ld, int log2cap, int nwarps, bool greedy, DevFlags* flags) {
+                uint32_t step, GlobalCells gc, int32_t ld, int log2cap, int nwarps, bool greedy, int32_t* ghash,
+                DevFlags* flags) {
     constexpr bool kShared = kMode == 0;
     constexpr bool kGlobalDeg = kMode == 2;
     extern __shared__ int32_t sm[];
@@ -372,18 +393,21 @@ __global__ void __launch_bounds__(kWinMaxWarps * 32, 1)
     int32_t* dout = kGlobalDeg ? bm.d_out : sm;
     int32_t* din = kGlobalDeg ? bm.d_in : dout + B;
     int32_t* size = kGlobalDeg ? bm.sizes : din + B;
-    int32_t* hash = kGlobalDeg ? sm : size + B;  // nwarps x (keys, out counts, in counts, items) x cap
-    int32_t* M = hash + 4 * cap * nwarps;       // shared cells (kShared): B rows of ld
+    int32_t* hash = kGlobalDeg ? sm : size + B;  // nwarps x (keys, out counts, in counts, items) x 512
+    int32_t* lq = hash + (4 << kSmemHashL2) * nwarps;  // the first kLqCache log-table entries
+    int32_t* M = lq + kLqCache;                        // shared cells (kShared): B rows of ld
+    // a vertex's hash: shared memory up to 2^kSmemHashL2 slots, else the warp's global region
+    auto hash_of = [&](int w, int l2) {
+        return l2 <= kSmemHashL2 ? hash + (4 << kSmemHashL2) * w : ghash + ((int64_t)4 << kGlobalHashL2) * w;
+    };
     __shared__ WinResult res[kWinMaxWarps];
     __shared__ int32_t s_consumed, s_acc_mask;
     __shared__ uint32_t s_conf[kWinMaxWarps];
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const int nt = nwarps * 32;
-    int32_t* hk = hash + 4 * cap * wid;
-    int32_t* hO = hk + cap;
-    int32_t* hI = hO + cap;
-    int32_t* items = hI + cap;
+    (void)cap;
 
+    for (int i = tid; i < kLqCache; i += nt) lq[i] = __ldg(g.Lq + min(i, g.E + 1));
     if (kShared) {
         for (int i = tid; i < B * ld; i += nt) M[i] = 0;
         __syncthreads();
@@ -421,18 +445,23 @@ __global__ void __launch_bounds__(kWinMaxWarps * 32, 1)
             c.L = __ldg(g.selfcnt + c.v);
             c.l2 = hash_log2(c.k, log2cap);
             c.status = ST_SKIP;
+            int32_t* hk = hash_of(wid, c.l2);
+            int32_t* hO = hk + (1 << c.l2);
+            int32_t* hI = hO + (1 << c.l2);
+            int32_t* items = hI + (1 << c.l2);
             if (size[c.r] != 1) {  // a singleton block never moves (finetune.cpp:845)
                 uint32_t w[4];
                 philox4x32_10((uint32_t)c.v, iter, step, DOM_MH, seed, w);
+                // the neighbour blocks first; the proposal's sampled neighbour is among them
+                const int32_t idx = c.k > 0 ? (int32_t)u32_below(w[0], (uint32_t)c.k) : -1;
+                const int32_t nbg = warp_gather(g, bm.asg, c.v, c.r, o0, c.kout, i0, c.k, idx, hk, hO, hI, c.l2);
                 int32_t s;
                 if (c.k == 0) {
                     s = random_block(c.r, B, w[1]);
                 } else {
                     // common::propose_new_block: uniform neighbour, then a multinomial over
                     // nb's row (ascending column) followed by its column without the diagonal
-                    const int32_t idx = (int32_t)u32_below(w[0], (uint32_t)c.k);
-                    const int32_t nbr = idx < c.kout ? __ldg(g.out_nbr + o0 + idx) : __ldg(g.inns_nbr + i0 + idx - c.kout);
-                    const int32_t nb = __ldcg(bm.asg + nbr);
+                    const int32_t nb = nbg;
                     c.nb = nb;
                     const int32_t dnn = kShared ? sc.row_get(nb, nb) : gc.row_get(nb, nb);
                     const long long R = dout[nb], C = (long long)din[nb] - dnn;
@@ -455,9 +484,8 @@ __global__ void __launch_bounds__(kWinMaxWarps * 32, 1)
                     c.status = ST_NOMOVE;
                 } else {
                     c.s = s;
-                    warp_gather(g, bm.asg, c.v, o0, c.kout, i0, c.k, hk, hO, hI, c.l2);
-                    c.dS = kShared ? warp_delta(g, dout, din, sc, c.r, s, c.kout, c.kin, c.L, hk, hO, hI, c.l2, items)
-                                   : warp_delta(g, dout, din, gc, c.r, s, c.kout, c.kin, c.L, hk, hO, hI, c.l2, items);
+                    c.dS = kShared ? warp_delta(g, dout, din, sc, c.r, s, c.kout, c.kin, c.L, hk, hO, hI, c.l2, items, lq)
+                                   : warp_delta(g, dout, din, gc, c.r, s, c.kout, c.kin, c.L, hk, hO, hI, c.l2, items, lq);
                     double H = 1.0;
                     if (!greedy && c.k > 0) {  // entropy::hastings_correction (entropy.cpp:497-561)
                         H = kShared ? hastings_fixed<32>(sc, [&](int32_t b) { return dout[b] + din[b] - sc.row_get(b, b); },
@@ -482,8 +510,9 @@ __global__ void __launch_bounds__(kWinMaxWarps * 32, 1)
             if (u < j && res[u].status == ST_ACCEPT) {
                 const WinResult& cj = res[j];
                 const WinResult& cu = res[u];
-                if (in_touched(cj, hash + 4 * cap * j, cu.r) || in_touched(cj, hash + 4 * cap * j, cu.s) ||
-                    (cj.nb >= 0 && in_touched(cu, hash + 4 * cap * u, cj.nb)))
+                const int32_t* hj = hash_of(j, cj.l2);
+                if (in_touched(cj, hj, cu.r) || in_touched(cj, hj, cu.s) ||
+                    (cj.nb >= 0 && in_touched(cu, hash_of(u, cu.l2), cj.nb)))
                     atomicOr(&s_conf[j], 1u << u);
             }
         }
@@ -511,6 +540,9 @@ __global__ void __launch_bounds__(kWinMaxWarps * 32, 1)
         if (wid < wn && ((s_acc_mask >> wid) & 1)) {
             const WinResult c = res[wid];
             const int32_t r = c.r, s = c.s;
+            const int32_t* hk = hash_of(wid, c.l2);
+            const int32_t* hO = hk + (1 << c.l2);
+            const int32_t* hI = hO + (1 << c.l2);
             for (int i = lane; i < (1 << c.l2); i += 32) {
                 const int32_t b = hk[i];
                 if (b < 0 || b == r || b == s) continue;
@@ -582,12 +614,13 @@ __global__ void k_window_fill(DevBM bm, GlobalCells gc) {
     }
 }
 
-constexpr size_t kWinSmemBudget = 200 * 1024;
+constexpr size_t kWinSmemBudget = 220 * 1024;
 
 size_t window_smem(int32_t B, int mode, int log2cap, int nwarps) {
+    (void)log2cap;
     const size_t deg = mode == 2 ? 0 : 3 * (size_t)B;
     const size_t cells = mode == 0 ? (size_t)B * ((size_t)B + 1) : 0;
-    return sizeof(int32_t) * (deg + 4 * ((size_t)nwarps << log2cap) + cells);
+    return sizeof(int32_t) * (deg + ((size_t)nwarps << (kSmemHashL2 + 2)) + kLqCache + cells);
 }
 
 }  // namespace
@@ -599,7 +632,7 @@ uint64_t mh_window_cells(int32_t B) {
 
 bool mh_window_plan(int32_t B, int32_t max_k, const Work& w, WindowPlan* p) {
     const int l = ceil_log2((uint64_t)(2 * (max_k > 16 ? max_k : 16)));
-    if (l > 13) return false;
+    if (l > kGlobalHashL2 || (l > kSmemHashL2 && !w.win_hash)) return false;
     p->log2cap = l;
     if (B <= kWinSharedMax) {
         p->mode = 0;
@@ -607,7 +640,7 @@ bool mh_window_plan(int32_t B, int32_t max_k, const Work& w, WindowPlan* p) {
     } else {
         if (!w.cells || mh_window_cells(B) > w.cells_elems) return false;
         p->ld = ((int64_t)B + 3) & ~3ll;
-        p->mode = window_smem(B, 1, l, 8) <= kWinSmemBudget ? 1 : 2;
+        p->mode = window_smem(B, 1, l, kWinMaxWarps) <= kWinSmemBudget ? 1 : 2;
     }
     int nw = kWinMaxWarps;
     while (nw > 0 && window_smem(B, p->mode, l, nw) > kWinSmemBudget) --nw;
@@ -622,7 +655,7 @@ void mh_chain_window(const DevGraph& g, DevBM& bm, const int32_t* order, int32_t
     if (p.mode == 0) {
         cudaFuncSetAttribute(k_mh_window<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         k_mh_window<0><<<1, 32 * p.nw, smem, st>>>(g, bm, order, n, seed, iter, step, GlobalCells{}, (int32_t)p.ld,
-                                                   p.log2cap, p.nw, greedy != 0, w.flags_dev);
+                                                   p.log2cap, p.nw, greedy != 0, w.win_hash, w.flags_dev);
         count_launches(1);
         return;
     }
@@ -642,11 +675,11 @@ void mh_chain_window(const DevGraph& g, DevBM& bm, const int32_t* order, int32_t
     if (p.mode == 1) {
         cudaFuncSetAttribute(k_mh_window<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         k_mh_window<1><<<1, 32 * p.nw, smem, st>>>(g, bm, order, n, seed, iter, step, gc, (int32_t)p.ld, p.log2cap,
-                                                   p.nw, greedy != 0, w.flags_dev);
+                                                   p.nw, greedy != 0, w.win_hash, w.flags_dev);
     } else {
         cudaFuncSetAttribute(k_mh_window<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         k_mh_window<2><<<1, 32 * p.nw, smem, st>>>(g, bm, order, n, seed, iter, step, gc, (int32_t)p.ld, p.log2cap,
-                                                   p.nw, greedy != 0, w.flags_dev);
+                                                   p.nw, greedy != 0, w.win_hash, w.flags_dev);
     }
     count_launches(2);
 }

@@ -139,12 +139,16 @@ __device__ __forceinline__ int32_t random_block(int32_t current, int32_t B, uint
 // ------------------------------------------------------------------ entropy terms
 // fastlog table in units of 2^-24 with its last valid index; indices are clamped so
 // an inconsistent state can never read outside the table.
+// sq / sn: optional copy of the first sn entries in shared memory.
 struct LogTab {
     const int32_t* q;
     int32_t hi;
+    const int32_t* sq = nullptr;
+    int32_t sn = 0;
 };
 __device__ __forceinline__ long long Lx(const LogTab& t, long long x) {
     x = x < 0 ? 0 : (x > t.hi ? t.hi : x);
+    if (x < t.sn) return (long long)t.sq[x];
     return (long long)__ldg(t.q + x);
 }
 // common::cell_entropy (reference include/common.hpp:39-50) in units of 2^-24:

@@ -52,6 +52,8 @@ struct Work {
     int32_t* dense_M = nullptr;        // [kDenseGlobalMax^2] (allocated when N allows)
     int32_t* dense_MT = nullptr;
     int32_t dense_cap = 0;             // largest B the dense matrices hold
+    // neighbour hashes of the windowed chain's high-degree vertices [16 warps x 4 x 8192]
+    int32_t* win_hash = nullptr;
     // dense B x B cell values of the merge carry-out (allocated on demand within a budget)
     int32_t* cells = nullptr;
     uint64_t cells_elems = 0;
