@@ -273,7 +273,7 @@ __device__ long long warp_delta(const DevGraph& g, const int32_t* d_out, const i
                                 const int32_t* lq_cache) {
     const int lane = threadIdx.x & 31;
     const int cap = 1 << log2cap;
-    const LogTab Lq{g.Lq, g.E + 1, lq_cache, kLqCache};
+    const LogTabCached Lq{g.Lq, g.E + 1, lq_cache, kLqCache};
     int32_t Or = 0, Ir = 0, Os = 0, Is = 0, n = 0;
     for (int base = 0; base < cap; base += 32) {
         const int i = base + lane;

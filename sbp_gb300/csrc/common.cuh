@@ -139,26 +139,36 @@ __device__ __forceinline__ int32_t random_block(int32_t current, int32_t B, uint
 // ------------------------------------------------------------------ entropy terms
 // fastlog table in units of 2^-24 with its last valid index; indices are clamped so
 // an inconsistent state can never read outside the table.
-// sq / sn: optional copy of the first sn entries in shared memory.
 struct LogTab {
     const int32_t* q;
     int32_t hi;
-    const int32_t* sq = nullptr;
-    int32_t sn = 0;
 };
 __device__ __forceinline__ long long Lx(const LogTab& t, long long x) {
+    x = x < 0 ? 0 : (x > t.hi ? t.hi : x);
+    return (long long)__ldg(t.q + x);
+}
+// The same table with its first sn entries also in shared memory (sq).
+struct LogTabCached {
+    const int32_t* q;
+    int32_t hi;
+    const int32_t* sq;
+    int32_t sn;
+};
+__device__ __forceinline__ long long Lx(const LogTabCached& t, long long x) {
     x = x < 0 ? 0 : (x > t.hi ? t.hi : x);
     if (x < t.sn) return (long long)t.sq[x];
     return (long long)__ldg(t.q + x);
 }
 // common::cell_entropy (reference include/common.hpp:39-50) in units of 2^-24:
 // v * (L[v] - L[d_in] - L[d_out]); zero for an empty cell; L[0] = 0 (fastlog(0)).
-__device__ __forceinline__ long long ce_fixed(const LogTab& L, long long v, long long din, long long dout) {
+template <class Tab>
+__device__ __forceinline__ long long ce_fixed(const Tab& L, long long v, long long din, long long dout) {
     if (v == 0) return 0;
     return v * (Lx(L, v) - Lx(L, din) - Lx(L, dout));
 }
 // Change of an unchanged cell's term when only degrees move: old - new.
-__device__ __forceinline__ long long ce_delta(const LogTab& L, long long v, long long din, long long dout,
+template <class Tab>
+__device__ __forceinline__ long long ce_delta(const Tab& L, long long v, long long din, long long dout,
                                               long long din2, long long dout2) {
     if (v == 0) return 0;
     return v * (Lx(L, din2) - Lx(L, din) + Lx(L, dout2) - Lx(L, dout));

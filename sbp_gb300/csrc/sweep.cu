@@ -46,10 +46,11 @@ __global__ void k_split_by_degree(DevGraph g, const int32_t* __restrict__ list, 
     }
 }
 
-template <int kThreads>
+// kGreedy: compiled without the Hastings correction (the default configuration).
+template <int kThreads, bool kGreedy>
 __device__ __forceinline__ int32_t gibbs_one(const DevGraph& g, const DevBM& bm, int32_t v, uint64_t seed,
                                              uint32_t iter, uint32_t step, int32_t* hk, int32_t* hO, int32_t* hI,
-                                             int log2cap, long long (*red)[8], bool greedy, DevFlags* flags) {
+                                             int log2cap, long long (*red)[8], DevFlags* flags) {
     const int32_t r = bm.asg[v];
     uint32_t w[4];
     philox4x32_10((uint32_t)v, iter, step, DOM_GIBBS, seed, w);
@@ -61,19 +62,20 @@ __device__ __forceinline__ int32_t gibbs_one(const DevGraph& g, const DevBM& bm,
     if (s == r) return -1;
     const long long dS =
         vertex_delta_fixed<kThreads>(g, bm.asg, bm.d_out, bm.d_in, CsrAcc{bm}, v, r, s, hk, hO, hI, log2cap, red);
+    if (kGreedy) return dS < 0 ? s : -1;  // finetune::accept with greedy (finetune.cpp:22-25)
     double H = 1.0;
     const int32_t o0 = __ldg(g.out_off + v), i0 = __ldg(g.inns_off + v);
     const int32_t kout = __ldg(g.out_off + v + 1) - o0, kin = __ldg(g.inns_off + v + 1) - i0;
-    if (!greedy && kout + kin > 0)
+    if (kout + kin > 0)
         H = hastings_fixed<kThreads>(CsrAcc{bm}, [&](int32_t b) { return bm.d_tot[b]; }, bm.d_out, bm.d_in, bm.B, r,
                                      s, kout, kin, __ldg(g.selfcnt + v), hk, hO, hI, log2cap, red);
-    return accept_move(dS, H, greedy, w[3]) ? s : -1;  // finetune::accept (finetune.cpp:22-32)
+    return accept_move(dS, H, false, w[3]) ? s : -1;  // finetune::accept (finetune.cpp:26-31)
 }
 
+template <bool kGreedy>
 __global__ void __launch_bounds__(256) k_gibbs_small(DevGraph g, DevBM bm, const int32_t* __restrict__ list,
                                                      const int32_t* __restrict__ d_n, uint64_t seed, uint32_t iter,
-                                                     uint32_t step, int32_t* __restrict__ moves, int greedy,
-                                                     DevFlags* flags) {
+                                                     uint32_t step, int32_t* __restrict__ moves, DevFlags* flags) {
     __shared__ int32_t hk[kGibbsWarps][1 << kSmallLog2];
     __shared__ int32_t hO[kGibbsWarps][1 << kSmallLog2];
     __shared__ int32_t hI[kGibbsWarps][1 << kSmallLog2];
@@ -82,8 +84,8 @@ __global__ void __launch_bounds__(256) k_gibbs_small(DevGraph g, DevBM bm, const
     unsigned long long edges = 0, accepted = 0;
     for (int32_t i = blockIdx.x * kGibbsWarps + wid; i < n; i += gridDim.x * kGibbsWarps) {
         const int32_t v = list[i];
-        const int32_t mv = gibbs_one<32>(g, bm, v, seed, iter, step, hk[wid], hO[wid], hI[wid], kSmallLog2, nullptr,
-                                         greedy != 0, flags);
+        const int32_t mv = gibbs_one<32, kGreedy>(g, bm, v, seed, iter, step, hk[wid], hO[wid], hI[wid], kSmallLog2,
+                                                  nullptr, flags);
         if (lane == 0) {
             moves[v] = mv;
             edges += (__ldg(g.out_off + v + 1) - __ldg(g.out_off + v)) + (__ldg(g.inns_off + v + 1) - __ldg(g.inns_off + v));
@@ -96,10 +98,11 @@ __global__ void __launch_bounds__(256) k_gibbs_small(DevGraph g, DevBM bm, const
     }
 }
 
+template <bool kGreedy>
 __global__ void __launch_bounds__(256) k_gibbs_big(DevGraph g, DevBM bm, const int32_t* __restrict__ list,
                                                    const int32_t* __restrict__ d_n, uint64_t seed, uint32_t iter,
                                                    uint32_t step, int log2cap, int32_t* __restrict__ moves,
-                                                   int greedy, DevFlags* flags) {
+                                                   DevFlags* flags) {
     extern __shared__ int32_t dyn[];
     __shared__ long long red[32][8];
     const int cap = 1 << log2cap;
@@ -111,7 +114,7 @@ __global__ void __launch_bounds__(256) k_gibbs_big(DevGraph g, DevBM bm, const i
         if (2 * k > cap) {
             if (threadIdx.x == 0) atomicOr(&flags->err, ERR_DEGREE);
         } else {
-            mv = gibbs_one<256>(g, bm, v, seed, iter, step, dyn, dyn + cap, dyn + 2 * cap, log2cap, red, greedy != 0, flags);
+            mv = gibbs_one<256, kGreedy>(g, bm, v, seed, iter, step, dyn, dyn + cap, dyn + 2 * cap, log2cap, red, flags);
         }
         if (threadIdx.x == 0) {
             moves[v] = mv;
@@ -403,16 +406,26 @@ void gibbs_propose(const DevGraph& g, const DevBM& bm, const int32_t* vlist, int
     cudaMemsetAsync(counts, 0, 2 * sizeof(int32_t), st);
     k_split_by_degree<<<grid_cap(n, 256, 152 * 16), 256, 0, st>>>(g, vlist, n, 1 << (kSmallLog2 - 1), w.list_small,
                                                                   w.list_big, counts);
-    k_gibbs_small<<<grid_cap(n, kGibbsWarps, 152 * 8), 256, 0, st>>>(g, bm, w.list_small, counts, seed, iter, step,
-                                                                     w.moves, greedy, w.flags_dev);
+    if (greedy)
+        k_gibbs_small<true><<<grid_cap(n, kGibbsWarps, 152 * 8), 256, 0, st>>>(g, bm, w.list_small, counts, seed, iter,
+                                                                               step, w.moves, w.flags_dev);
+    else
+        k_gibbs_small<false><<<grid_cap(n, kGibbsWarps, 152 * 8), 256, 0, st>>>(g, bm, w.list_small, counts, seed,
+                                                                                iter, step, w.moves, w.flags_dev);
     count_launches(2);
     if (max_k > (1 << (kSmallLog2 - 1))) {
         int log2cap = ceil_log2((uint64_t)(2 * max_k));
         if (log2cap > 14) log2cap = 14;
         const size_t smem = (size_t)(3 * sizeof(int32_t)) << log2cap;
-        cudaFuncSetAttribute(k_gibbs_big, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_gibbs_big<<<152 * 2, 256, smem, st>>>(g, bm, w.list_big, counts + 1, seed, iter, step, log2cap, w.moves,
-                                               greedy, w.flags_dev);
+        if (greedy) {
+            cudaFuncSetAttribute(k_gibbs_big<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            k_gibbs_big<true><<<152 * 2, 256, smem, st>>>(g, bm, w.list_big, counts + 1, seed, iter, step, log2cap,
+                                                          w.moves, w.flags_dev);
+        } else {
+            cudaFuncSetAttribute(k_gibbs_big<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            k_gibbs_big<false><<<152 * 2, 256, smem, st>>>(g, bm, w.list_big, counts + 1, seed, iter, step, log2cap,
+                                                           w.moves, w.flags_dev);
+        }
         count_launches(1);
     }
     (void)greedy;
