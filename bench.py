@@ -224,6 +224,123 @@ def profile_phase(args):
                       "seconds": time.perf_counter() - t0, "stats": st}))
 
 
+def mixed_graphs(count, n_lo, n_hi, seed_base=0):
+    """Independent directed DCSBM graphs: N log-uniform in [n_lo, n_hi], about 20 N edges,
+    floor(sqrt(N) / 4) + 2 planted blocks, within:between ratio uniform in [1.5, 3.0], degree
+    propensities power-law 2.1 in [5, 100]; graph i uses seed seed_base + i."""
+    from sbp_gb300 import dcsbm
+    rng = np.random.default_rng(20240 + seed_base)
+    sizes = np.exp(rng.uniform(np.log(n_lo), np.log(n_hi), count)).astype(np.int64)
+    out = []
+    for i, n in enumerate(sizes):
+        r = np.random.default_rng(seed_base + i)
+        src, dst, planted = dcsbm.generate(int(n), 20 * int(n), int(np.sqrt(n) / 4) + 2, dmin=5, dmax=100,
+                                           ratio=float(r.uniform(1.5, 3.0)), seed=seed_base + i)
+        out.append((int(n), src, dst, planted))
+    return out
+
+
+def plain_one_at_a_time(graphs, sargs):
+    """The plain path: each graph uploaded, partitioned and read back in turn on one context."""
+    import torch
+    import sbp_gb300 as sb
+    ctx = sb.Context(0)
+    ctx.set_cells_budget(256 << 20)
+    results, service = [], []
+    for i, (n, src, dst, _) in enumerate(graphs):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        G = sb.Graph(n, src, dst, ctx=ctx)
+        a, B, mdl, _ = sb.sbp.stochastic_block_partition(G, sb.Args(algorithm=sargs.algorithm, seed=i))
+        G.close()
+        service.append(time.perf_counter() - t0)
+        results.append((a, B, mdl))
+    ctx.close()
+    return results, service
+
+
+def batched_workload(args):
+    """Many mixed-size graphs partitioned concurrently on one GPU (the batched
+    configuration) against the same graphs partitioned one at a time; both produce the
+    same partitions, so NMI is equal by construction (checked)."""
+    import sbp_gb300 as sb
+    from sbp_gb300 import build as _b
+    _b.build()
+    graphs = mixed_graphs(args.jobs, 500, 20000)
+    sargs = sb.Args(algorithm="hybrid_mcmc")
+    plain, service = plain_one_at_a_time(graphs, sargs)
+    t0 = time.perf_counter()
+    res = sb.serve.partition_batch([(n, s, d) for n, s, d, _ in graphs], sargs, seeds=list(range(len(graphs))),
+                                   workers=args.workers, hbm_budget=args.hbm_budget, cells_budget=256 << 20)
+    t_batch = time.perf_counter() - t0
+    same = all(np.array_equal(p[0], r[0]) and p[1] == r[1] for p, r in zip(plain, res))
+    nmis = [sb.evaluate.nmi(g[3], r[0]) for g, r in zip(graphs, res)]
+    t_plain = float(np.sum(service))
+    print(json.dumps({"workload": "batched", "metric": "jobs/s", "value": len(graphs) / t_batch, "unit": "jobs/s",
+                      "jobs": len(graphs), "workers": args.workers, "batched_s": t_batch, "plain_s": t_plain,
+                      "plain_jobs_per_s": len(graphs) / t_plain, "speedup_vs_plain": t_plain / t_batch,
+                      "identical_to_plain": bool(same), "mean_nmi": float(np.mean(nmis)),
+                      "total_vertices": int(sum(g[0] for g in graphs)),
+                      "total_edges": int(sum(g[1].size for g in graphs)),
+                      "config": {"workload": "%d directed DCSBM graphs, N log-uniform in [500, 20000], ~20 N edges, "
+                                             "floor(sqrt(N)/4)+2 planted blocks, ratio U[1.5, 3], degrees 2.1 in "
+                                             "[5, 100], seeds 0..%d, hybrid MCMC" % (len(graphs), len(graphs) - 1),
+                                 "data": "synthetic (seeded DCSBM)"}}))
+
+
+def served_workload(args):
+    """A Poisson stream of partition requests served concurrently, against the same stream
+    served one request at a time on the plain path (its latencies follow from each
+    request's measured plain service time: a single FIFO server)."""
+    import concurrent.futures as cf
+    import sbp_gb300 as sb
+    from sbp_gb300 import build as _b
+    _b.build()
+    graphs = mixed_graphs(args.jobs, 1000, args.max_vertices, seed_base=10000)
+    sargs = sb.Args(algorithm="hybrid_mcmc")
+    plain, service = plain_one_at_a_time(graphs, sargs)
+    plain_rate = len(graphs) / float(np.sum(service))
+    rate = args.rate if args.rate else 0.8 * plain_rate  # 0.8 of the plain path's throughput
+    arrivals = np.cumsum(np.random.default_rng(77).exponential(1.0 / rate, len(graphs)))
+    finish_plain, t_free = [], 0.0
+    for a_t, s_t in zip(arrivals, service):
+        t_free = max(a_t, t_free) + s_t
+        finish_plain.append(t_free)
+    lat_plain = np.array(finish_plain) - arrivals
+    done = [None] * len(graphs)
+    with sb.serve.Server(workers=args.workers, hbm_budget=args.hbm_budget, cells_budget=256 << 20) as srv, \
+            cf.ThreadPoolExecutor(max_workers=64) as pool:
+        t0 = time.perf_counter()
+        futures = []
+        for i, (n, src, dst, _) in enumerate(graphs):
+            delay = arrivals[i] - (time.perf_counter() - t0)
+            if delay > 0:
+                time.sleep(delay)
+            tk = srv.submit(n, src, dst, sargs, seed=i)
+
+            def finish(tk=tk, i=i):
+                out = srv.wait(tk)
+                done[i] = (time.perf_counter() - t0, out)
+            futures.append(pool.submit(finish))
+        for f in futures:
+            f.result()
+        makespan = time.perf_counter() - t0
+    lat = np.array([done[i][0] - arrivals[i] for i in range(len(graphs))])
+    same = all(np.array_equal(plain[i][0], done[i][1][0]) for i in range(len(graphs)))
+    print(json.dumps({"workload": "served", "metric": "jobs/s", "value": len(graphs) / makespan, "unit": "jobs/s",
+                      "requests": len(graphs), "offered_rate_per_s": rate, "workers": args.workers,
+                      "p50_ms": 1e3 * float(np.percentile(lat, 50)), "p99_ms": 1e3 * float(np.percentile(lat, 99)),
+                      "plain_p50_ms": 1e3 * float(np.percentile(lat_plain, 50)),
+                      "plain_p99_ms": 1e3 * float(np.percentile(lat_plain, 99)),
+                      "plain_jobs_per_s": plain_rate, "identical_to_plain": bool(same),
+                      "mean_nmi": float(np.mean([sb.evaluate.nmi(graphs[i][3], done[i][1][0])
+                                                 for i in range(len(graphs))])),
+                      "config": {"workload": "%d requests, Poisson arrivals at %.2f/s, N log-uniform in [1000, %d], "
+                                             "~20 N edges, floor(sqrt(N)/4)+2 planted blocks, ratio U[1.5, 3], "
+                                             "hybrid MCMC" % (len(graphs), rate, args.max_vertices),
+                                 "data": "synthetic (seeded DCSBM)"}}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -239,12 +356,23 @@ def main():
                     help="merge / mcmc: one phase at --blocks blocks for profilers (no bench line)")
     ap.add_argument("--blocks", type=int, default=1500)
     ap.add_argument("--iterations", type=int, default=2)
+    ap.add_argument("--workload", default="sbp", choices=["sbp", "batched", "served"],
+                    help="batched / served: many graphs through the partition server (own JSON line)")
+    ap.add_argument("--jobs", type=int, default=64)
+    ap.add_argument("--workers", type=int, default=32)
+    ap.add_argument("--hbm-budget", type=int, default=64 << 30)
+    ap.add_argument("--rate", type=float, default=0.0, help="served: offered requests/s (0: derived)")
+    ap.add_argument("--max-vertices", type=int, default=50000)
     args = ap.parse_args()
     globals()["CONFIG"] = args.config
     if args.impl == "reference":
         return reference_arm(args)
     if args.phase != "sbp":
         return profile_phase(args)
+    if args.workload == "batched":
+        return batched_workload(args)
+    if args.workload == "served":
+        return served_workload(args)
 
     import torch
     import sbp_gb300 as sb

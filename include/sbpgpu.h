@@ -167,6 +167,49 @@ sbpgpu_status sbpgpu_merge_proposals(sbpgpu_bm* bm, uint64_t seed, int32_t step,
 sbpgpu_status sbpgpu_sbp(sbpgpu_graph* g, const sbpgpu_config* cfg, uint64_t seed, int32_t* out_assignment,
                          int64_t* num_blocks, double* out_mdl, sbpgpu_stats* stats);
 
+/* ---- batched and served partitioning ----------------------------------------------
+ * No counterpart in the reference (its plain driver partitions one graph per process).  A
+ * server partitions many independent graphs at once on one device: `workers` host threads,
+ * each with its own context and stream, take jobs in submission order and run
+ * sbpgpu_sbp on them concurrently.  A job is admitted while the estimated device footprint
+ * (sbpgpu_job_footprint) of the jobs in flight plus its own stays within hbm_budget_bytes;
+ * the first job in flight is always admitted.  Each worker's context uses
+ * cells_budget_bytes for dense cell counts (sbpgpu_ctx_set_cells_budget).  A job's result
+ * equals sbpgpu_sbp of the same graph, configuration and seed run alone.  The job's host
+ * arrays must stay valid until sbpgpu_server_wait returns for it. */
+typedef struct sbpgpu_server sbpgpu_server;
+typedef struct sbpgpu_job {
+    int64_t num_vertices;
+    int64_t num_edges;
+    const int32_t* src;          /* host edge arrays, as sbpgpu_graph_create */
+    const int32_t* dst;
+    sbpgpu_config config;
+    uint64_t seed;
+    int32_t* out_assignment;     /* host, num_vertices entries, written by the job */
+} sbpgpu_job;
+typedef struct sbpgpu_job_result {
+    sbpgpu_status status;
+    int64_t num_blocks;
+    double mdl;
+    double queued_ms;            /* submission to start */
+    double run_ms;               /* start to finish (graph upload, partition, result read) */
+    sbpgpu_stats stats;
+    char error[256];             /* message of a failed job */
+} sbpgpu_job_result;
+
+/* Estimated device bytes of one job (graph, work buffers, blockmodels, dense cells). */
+int64_t sbpgpu_job_footprint(int64_t num_vertices, int64_t num_edges, int64_t cells_budget_bytes);
+sbpgpu_status sbpgpu_server_create(int32_t device, int32_t workers, int64_t hbm_budget_bytes,
+                                   int64_t cells_budget_bytes, sbpgpu_server** out);
+sbpgpu_status sbpgpu_server_submit(sbpgpu_server* server, const sbpgpu_job* job, int64_t* ticket);
+/* Blocks until the job is done and returns its result (once per ticket). */
+sbpgpu_status sbpgpu_server_wait(sbpgpu_server* server, int64_t ticket, sbpgpu_job_result* result);
+/* Finishes every submitted job, then stops the workers. */
+void sbpgpu_server_destroy(sbpgpu_server* server);
+/* The batched form: n jobs through a server, results in job order. */
+sbpgpu_status sbpgpu_sbp_batch(int32_t device, int32_t workers, int64_t hbm_budget_bytes, int64_t cells_budget_bytes,
+                               int64_t n, const sbpgpu_job* jobs, sbpgpu_job_result* results);
+
 /* ---- timing of the dominant kernels (CUDA events on the context's stream) --------- */
 typedef struct sbpgpu_kernel_timing {
     double gibbs_propose_ms;  int64_t gibbs_propose_launches;  int64_t gibbs_propose_bytes;

@@ -58,6 +58,22 @@ class KernelTiming(ctypes.Structure):
 
 
 # name -> (restype, argtypes); every symbol declared in include/sbpgpu.h.
+class Job(ctypes.Structure):
+    _fields_ = [
+        ("num_vertices", ctypes.c_int64), ("num_edges", ctypes.c_int64),
+        ("src", ctypes.POINTER(ctypes.c_int32)), ("dst", ctypes.POINTER(ctypes.c_int32)),
+        ("config", Config), ("seed", ctypes.c_uint64), ("out_assignment", ctypes.POINTER(ctypes.c_int32)),
+    ]
+
+
+class JobResult(ctypes.Structure):
+    _fields_ = [
+        ("status", ctypes.c_int), ("num_blocks", ctypes.c_int64), ("mdl", ctypes.c_double),
+        ("queued_ms", ctypes.c_double), ("run_ms", ctypes.c_double), ("stats", Stats),
+        ("error", ctypes.c_char * 256),
+    ]
+
+
 SIGNATURES = {
     "sbpgpu_default_config": (None, [ctypes.POINTER(Config)]),
     "sbpgpu_ctx_create": (ctypes.c_int, [ctypes.c_int32, ctypes.POINTER(vp)]),
@@ -95,6 +111,14 @@ SIGNATURES = {
     "sbpgpu_merge_proposals": (ctypes.c_int, [vp, ctypes.c_uint64, ctypes.c_int32, i32p, f64p]),
     "sbpgpu_sbp": (ctypes.c_int, [vp, ctypes.POINTER(Config), ctypes.c_uint64, i32p, i64p, f64p,
                                   ctypes.POINTER(Stats)]),
+    "sbpgpu_job_footprint": (ctypes.c_int64, [ctypes.c_int64, ctypes.c_int64, ctypes.c_int64]),
+    "sbpgpu_server_create": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int64, ctypes.c_int64,
+                                            ctypes.POINTER(vp)]),
+    "sbpgpu_server_submit": (ctypes.c_int, [vp, ctypes.POINTER(Job), i64p]),
+    "sbpgpu_server_wait": (ctypes.c_int, [vp, ctypes.c_int64, ctypes.POINTER(JobResult)]),
+    "sbpgpu_server_destroy": (None, [vp]),
+    "sbpgpu_sbp_batch": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64,
+                                        ctypes.POINTER(Job), ctypes.POINTER(JobResult)]),
     "sbpgpu_set_timing": (None, [vp, ctypes.c_int32]),
     "sbpgpu_read_timing": (ctypes.c_int, [vp, ctypes.POINTER(KernelTiming)]),
 }

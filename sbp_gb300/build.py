@@ -66,7 +66,7 @@ def build(force=False, verbose=False, extra_flags=()):
     with cf.ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 4)) as ex:
         objs = list(ex.map(compile_one, sources()))
     tmp = LIB + ".tmp"
-    cmd = [exe] + ARCH + ["-shared", "-o", tmp] + objs
+    cmd = [exe] + ARCH + ["-shared", "-o", tmp] + objs + ["-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (r.stdout, r.stderr))

@@ -13,7 +13,7 @@
 namespace sbp {
 
 namespace {
-int64_t g_launch_count = 0;
+thread_local int64_t g_launch_count = 0;  // per host thread: each thread drives its own context
 constexpr int kT = 256;
 
 inline unsigned grid_for(int64_t n, int per = kT) {
@@ -173,6 +173,26 @@ __global__ void k_fill_slots(ulonglong2* p, uint64_t n) {
 int64_t kernel_launches() { return g_launch_count + prims_launch_count(); }
 void count_launches(int64_t n) { g_launch_count += n; }
 
+void host_wait(cudaStream_t st) {
+    thread_local cudaEvent_t ev = nullptr;
+    thread_local int ev_dev = -1;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (!ev || ev_dev != dev) {
+        if (ev) cudaEventDestroy(ev);
+        cudaEventCreateWithFlags(&ev, cudaEventBlockingSync | cudaEventDisableTiming);
+        ev_dev = dev;
+    }
+    cudaEventRecord(ev, st);
+    cudaEventSynchronize(ev);
+}
+
+void* host_scratch() {
+    thread_local void* p = nullptr;
+    if (!p && cudaMallocHost(&p, 256) != cudaSuccess) p = nullptr;
+    return p;
+}
+
 int ceil_log2(uint64_t x) {
     int l = 0;
     while ((1ull << l) < x) ++l;
@@ -200,10 +220,11 @@ void rebuild(const DevGraph& g, DevBM& bm, Work& w, cudaStream_t st) {
     radix_sort_u64(w.keys, w.keys_alt, nullptr, nullptr, E, 2 * nb, w.temp, st);
     k_head_flags<<<grid_for(E), kT, 0, st>>>(w.keys, E, w.flags);
     scan_i32(w.flags, w.flags, E, false, w.d_scalar, w.temp, st);
-    int32_t nnz = 0;
-    cudaMemcpyAsync(&nnz, w.d_scalar, sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+    int32_t* h_nnz = static_cast<int32_t*>(host_scratch());
+    cudaMemcpyAsync(h_nnz, w.d_scalar, sizeof(int32_t), cudaMemcpyDeviceToHost, st);
     k_compact_heads<<<grid_for(E), kT, 0, st>>>(w.keys, E, w.flags, w.keys_alt, w.vals);
-    cudaStreamSynchronize(st);
+    host_wait(st);
+    const int32_t nnz = *h_nnz;
     bm.nnz = nnz;
     k_fill_segments<<<grid_for(nnz), kT, 0, st>>>(w.keys_alt, w.vals, nnz, (int32_t)E, nb, bm.B, bm.row_off, bm.row_col,
                                                    bm.row_cnt, bm.row_of);

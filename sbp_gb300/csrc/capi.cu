@@ -44,14 +44,26 @@ struct ApiError : std::runtime_error {
         }                                                                                 \
     } while (0)
 
+// Device memory is allocated and freed in stream order on the stream of the context whose
+// call is in progress on this thread (cudaMallocAsync / cudaFreeAsync from the device's
+// pool): freeing does not wait for the whole device, so contexts that run concurrently
+// (the partition server's workers) do not stall one another.
+thread_local cudaStream_t tls_stream = nullptr;
+
+struct StreamScope {
+    cudaStream_t prev;
+    explicit StreamScope(cudaStream_t s) : prev(tls_stream) { tls_stream = s; }
+    ~StreamScope() { tls_stream = prev; }
+};
+
 template <typename T>
 T* dalloc(std::vector<void*>& owned, size_t n) {
     void* p = nullptr;
     const size_t bytes = (n ? n : 1) * sizeof(T);
-    const cudaError_t e = cudaMalloc(&p, bytes);
+    const cudaError_t e = cudaMallocAsync(&p, bytes, tls_stream);
     if (e != cudaSuccess) {
         cudaGetLastError();
-        throw ApiError(SBPGPU_ENOMEM, "cudaMalloc of " + std::to_string(bytes) + " bytes failed");
+        throw ApiError(SBPGPU_ENOMEM, "device allocation of " + std::to_string(bytes) + " bytes failed");
     }
     owned.push_back(p);
     return static_cast<T*>(p);
@@ -84,6 +96,7 @@ struct sbpgpu_ctx {
     std::string err;
     bool timing = false;
     int64_t cells_budget = int64_t(16) << 30;  // dense carry-out cells, bytes
+    DevFlags* flags_host = nullptr;            // pinned staging of the device flags
     std::vector<TimedSpan> pending;
     std::vector<cudaEvent_t> free_events;
     sbpgpu_kernel_timing tm{};
@@ -179,6 +192,7 @@ sbpgpu_status fail(sbpgpu_ctx* ctx, sbpgpu_status code, const std::string& msg) 
 
 template <typename F>
 sbpgpu_status guarded(sbpgpu_ctx* ctx, F f) {
+    StreamScope scope(ctx ? ctx->stream : nullptr);
     try {
         return f();
     } catch (const ApiError& e) {
@@ -194,13 +208,13 @@ sbpgpu_status guarded(sbpgpu_ctx* ctx, F f) {
 
 void check_flags(sbpgpu_graph* g) {
     CK(cudaMemcpyAsync(g->flags_host, g->w.flags_dev, sizeof(DevFlags), cudaMemcpyDeviceToHost, g->ctx->stream));
-    CK(cudaStreamSynchronize(g->ctx->stream));
+    host_wait(g->ctx->stream);
     CK(cudaGetLastError());
     const int32_t err = g->flags_host->err;
     if (err) {
         g->flags_host->err = 0;
         CK(cudaMemsetAsync(g->w.flags_dev, 0, sizeof(DevFlags), g->ctx->stream));
-        CK(cudaStreamSynchronize(g->ctx->stream));
+        host_wait(g->ctx->stream);
         std::string m = "device check failed (flags 0x" + std::to_string(err) + "):";
         if (err & ERR_DEGREE) m += " a vertex or block row exceeds the supported neighbour count;";
         if (err & ERR_HASH_FULL) m += " chain cell store full;";
@@ -251,11 +265,8 @@ void alloc_work(sbpgpu_graph* g) {
     w.used = dalloc<int32_t>(o, N);
     w.flags_dev = dalloc<DevFlags>(o, 1);
     w.win_hash = dalloc<int32_t>(o, (size_t)16 * 4 * 8192);
+    // dense M / transpose of the one-vertex-at-a-time chain: allocated when first needed
     w.dense_cap = (int32_t)std::min<int64_t>(N, kDenseGlobalMax);
-    if (w.dense_cap > kDenseMax) {
-        w.dense_M = dalloc<int32_t>(o, (size_t)w.dense_cap * w.dense_cap);
-        w.dense_MT = dalloc<int32_t>(o, (size_t)w.dense_cap * w.dense_cap);
-    }
 }
 
 void ensure_split(sbpgpu_graph* g, float mh_percent) {
@@ -282,7 +293,7 @@ void ensure_split(sbpgpu_graph* g, float mh_percent) {
         CK(cudaMemcpyAsync(g->d_hdv, hdv.data(), hdv.size() * 4, cudaMemcpyHostToDevice, g->ctx->stream));
     if (!ldv.empty())
         CK(cudaMemcpyAsync(g->d_ldv, ldv.data(), ldv.size() * 4, cudaMemcpyHostToDevice, g->ctx->stream));
-    CK(cudaStreamSynchronize(g->ctx->stream));
+    host_wait(g->ctx->stream);
     g->split_mh = mh_percent;
 }
 
@@ -295,9 +306,10 @@ void do_rebuild(sbpgpu_bm* bm) {
 double do_mdl(sbpgpu_bm* bm) {
     sbpgpu_graph* g = bm->g;
     launch_mdl(g->dg, bm->d, g->w, g->ctx->stream);
-    unsigned long long acc = 0;
-    CK(cudaMemcpyAsync(&acc, g->w.d_acc, sizeof(acc), cudaMemcpyDeviceToHost, g->ctx->stream));
+    unsigned long long* h_acc = static_cast<unsigned long long*>(host_scratch());
+    CK(cudaMemcpyAsync(h_acc, g->w.d_acc, sizeof(*h_acc), cudaMemcpyDeviceToHost, g->ctx->stream));
     check_flags(g);
+    const unsigned long long acc = *h_acc;
     g->ctx->collect();
     const long long lpq = (long long)acc;
     const double E = (double)g->E;
@@ -347,14 +359,13 @@ void ensure_cells(sbpgpu_graph* g, uint64_t need) {
     Work& w = g->w;
     const uint64_t budget = (uint64_t)std::max<int64_t>(g->ctx->cells_budget, 0) / sizeof(int32_t);
     if (w.cells && (w.cells_elems > budget || (need <= budget && w.cells_elems < need))) {
-        CK(cudaStreamSynchronize(g->ctx->stream));
-        CK(cudaFree(w.cells));
+        CK(cudaFreeAsync(w.cells, g->ctx->stream));
         w.cells = nullptr;
         w.cells_elems = 0;
     }
     if (need > budget || w.cells) return;
     void* p = nullptr;
-    if (cudaMalloc(&p, need * sizeof(int32_t)) != cudaSuccess) {
+    if (cudaMallocAsync(&p, need * sizeof(int32_t), g->ctx->stream) != cudaSuccess) {
         cudaGetLastError();
         return;
     }
@@ -376,6 +387,10 @@ void chain_run(sbpgpu_bm* bm, const int32_t* order, int32_t n, int32_t max_k, in
                        "non-greedy acceptance needs the windowed chain (vertex degree <= 4096 and the dense "
                        "cell budget holding the blockmodel)");
     } else if (bm->d.B <= kDenseMax || bm->d.B <= g->w.dense_cap) {
+        if (bm->d.B > kDenseMax && !g->w.dense_M) {
+            g->w.dense_M = dalloc<int32_t>(g->owned, (size_t)g->w.dense_cap * g->w.dense_cap);
+            g->w.dense_MT = dalloc<int32_t>(g->owned, (size_t)g->w.dense_cap * g->w.dense_cap);
+        }
         Span sp(g->ctx, 1);
         mh_chain_dense(g->dg, bm->d, order, n, seed, it, step, g->w, g->ctx->stream);
     } else {
@@ -578,10 +593,9 @@ void upload_graph(sbpgpu_graph* g, const int32_t* src, const int32_t* dst) {
     g->d_order = dalloc<int32_t>(o, N);
     g->d_order2 = dalloc<int32_t>(o, N);
     CK(cudaMemcpyAsync(g->d_all, iota.data(), N * 4, cudaMemcpyHostToDevice, st));
-    CK(cudaMallocHost(&g->flags_host, sizeof(DevFlags)));
-    memset(g->flags_host, 0, sizeof(DevFlags));
+    g->flags_host = g->ctx->flags_host;
     reset_counters(g);
-    CK(cudaStreamSynchronize(st));
+    host_wait(st);
 }
 
 sbpgpu_bm* new_bm(sbpgpu_graph* g, int64_t B) {
@@ -609,8 +623,8 @@ sbpgpu_bm* new_bm(sbpgpu_graph* g, int64_t B) {
     return bm;
 }
 
-void free_all(std::vector<void*>& owned) {
-    for (void* p : owned) cudaFree(p);
+void free_all(std::vector<void*>& owned, cudaStream_t st) {
+    for (void* p : owned) cudaFreeAsync(p, st);
     owned.clear();
 }
 
@@ -625,6 +639,7 @@ void release_ctx(sbpgpu_ctx* ctx) {
         cudaEventDestroy(s.b);
     }
     for (auto e : ctx->free_events) cudaEventDestroy(e);
+    if (ctx->flags_host) cudaFreeHost(ctx->flags_host);
     cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
@@ -632,10 +647,8 @@ void release_ctx(sbpgpu_ctx* ctx) {
 void release_graph(sbpgpu_graph* g) {
     if (!g->dead || g->refs > 0) return;
     sbpgpu_ctx* ctx = g->ctx;
-    cudaStreamSynchronize(ctx->stream);
-    free_all(g->owned);
-    if (g->w.cells) cudaFree(g->w.cells);
-    if (g->flags_host) cudaFreeHost(g->flags_host);
+    free_all(g->owned, ctx->stream);
+    if (g->w.cells) cudaFreeAsync(g->w.cells, ctx->stream);
     delete g;
     ctx->refs--;
     release_ctx(ctx);
@@ -664,7 +677,19 @@ sbpgpu_status sbpgpu_ctx_create(int32_t device, sbpgpu_ctx** out) {
     ctx->device = device;
     cudaError_t e = cudaSetDevice(device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMallocHost(&ctx->flags_host, sizeof(DevFlags));
+    if (e == cudaSuccess) {
+        memset(ctx->flags_host, 0, sizeof(DevFlags));
+        // keep memory freed by one partition in the device pool for the next one
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+            uint64_t keep = UINT64_MAX;
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        }
+    }
     if (e != cudaSuccess) {
+        if (ctx->flags_host) cudaFreeHost(ctx->flags_host);
+        if (ctx->stream) cudaStreamDestroy(ctx->stream);
         delete ctx;
         cudaGetLastError();
         return SBPGPU_EDEVICE;
@@ -683,7 +708,7 @@ const char* sbpgpu_last_error(const sbpgpu_ctx* ctx) { return ctx ? ctx->err.c_s
 
 sbpgpu_status sbpgpu_ctx_synchronize(sbpgpu_ctx* ctx) {
     return guarded(ctx, [&] {
-        CK(cudaStreamSynchronize(ctx->stream));
+        host_wait(ctx->stream);
         return SBPGPU_OK;
     });
 }
@@ -713,8 +738,7 @@ sbpgpu_status sbpgpu_graph_create(sbpgpu_ctx* ctx, int64_t N, int64_t E, const i
         return SBPGPU_OK;
     });
     if (rc != SBPGPU_OK) {
-        free_all(g->owned);
-        if (g->flags_host) cudaFreeHost(g->flags_host);
+        free_all(g->owned, ctx->stream);
         delete g;
         return rc;
     }
@@ -771,7 +795,7 @@ sbpgpu_status sbpgpu_bm_create(sbpgpu_graph* g, int64_t B, const int32_t* assign
     });
     if (rc != SBPGPU_OK) {
         if (bm) {
-            free_all(bm->owned);
+            free_all(bm->owned, bm->g->ctx->stream);
             delete bm;
         }
         return rc;
@@ -808,12 +832,12 @@ sbpgpu_status sbpgpu_bm_copy(const sbpgpu_bm* src, sbpgpu_bm** out) {
         b.nnz = a.nnz;
         bm->entropy = src->entropy;
         bm->num_blocks_to_merge = 0;  // Blockmodel::copy (blockmodel.cpp:151)
-        CK(cudaStreamSynchronize(st));
+        host_wait(st);
         return SBPGPU_OK;
     });
     if (rc != SBPGPU_OK) {
         if (bm) {
-            free_all(bm->owned);
+            free_all(bm->owned, bm->g->ctx->stream);
             delete bm;
         }
         return rc;
@@ -826,8 +850,8 @@ sbpgpu_status sbpgpu_bm_copy(const sbpgpu_bm* src, sbpgpu_bm** out) {
 void sbpgpu_bm_destroy(sbpgpu_bm* bm) {
     if (!bm) return;
     sbpgpu_graph* g = bm->g;
-    cudaStreamSynchronize(g->ctx->stream);
-    free_all(bm->owned);
+    host_wait(g->ctx->stream);
+    free_all(bm->owned, bm->g->ctx->stream);
     delete bm;
     g->refs--;
     release_graph(g);
@@ -850,7 +874,7 @@ sbpgpu_status sbpgpu_bm_read(const sbpgpu_bm* bm, int32_t* assignment, int64_t* 
             if (!dst) return;
             tmp.resize(n);
             CK(cudaMemcpyAsync(tmp.data(), src, n * 4, cudaMemcpyDeviceToHost, st));
-            CK(cudaStreamSynchronize(st));
+            host_wait(st);
             for (int64_t i = 0; i < n; ++i) dst[i] = tmp[i];
         };
         widen(bm->d.d_out, d_out, B);
@@ -860,7 +884,7 @@ sbpgpu_status sbpgpu_bm_read(const sbpgpu_bm* bm, int32_t* assignment, int64_t* 
         if (rows) CK(cudaMemcpyAsync(rows, bm->d.row_of, nnz * 4, cudaMemcpyDeviceToHost, st));
         if (cols) CK(cudaMemcpyAsync(cols, bm->d.row_col, nnz * 4, cudaMemcpyDeviceToHost, st));
         widen(bm->d.row_cnt, counts, nnz);
-        CK(cudaStreamSynchronize(st));
+        host_wait(st);
         return SBPGPU_OK;
     });
 }
@@ -899,10 +923,10 @@ sbpgpu_status sbpgpu_delta_mdl_batch(sbpgpu_bm* bm, int64_t n, const int32_t* ve
             CK(cudaMemcpyAsync(h.data(), dout, n * 8, cudaMemcpyDeviceToHost, st));
             check_flags(g);
         } catch (...) {
-            free_all(tmp);
+            free_all(tmp, g->ctx->stream);
             throw;
         }
-        free_all(tmp);
+        free_all(tmp, g->ctx->stream);
         for (int64_t i = 0; i < n; ++i) out[i] = (double)h[i] * (1.0 / 16777216.0);
         return SBPGPU_OK;
     });
@@ -961,10 +985,10 @@ sbpgpu_status sbpgpu_merge_delta_mdl_batch(sbpgpu_bm* bm, int64_t n, const int32
             CK(cudaMemcpyAsync(h.data(), dout, n * 8, cudaMemcpyDeviceToHost, st));
             check_flags(g);
         } catch (...) {
-            free_all(tmp);
+            free_all(tmp, g->ctx->stream);
             throw;
         }
-        free_all(tmp);
+        free_all(tmp, g->ctx->stream);
         for (int64_t i = 0; i < n; ++i) out[i] = (double)h[i] * (1.0 / 16777216.0);
         return SBPGPU_OK;
     });
@@ -989,10 +1013,10 @@ sbpgpu_status sbpgpu_propose_batch(sbpgpu_bm* bm, int64_t n, const int32_t* vert
             CK(cudaMemcpyAsync(out, dout, n * 4, cudaMemcpyDeviceToHost, st));
             check_flags(g);
         } catch (...) {
-            free_all(tmp);
+            free_all(tmp, g->ctx->stream);
             throw;
         }
-        free_all(tmp);
+        free_all(tmp, g->ctx->stream);
         return SBPGPU_OK;
     });
 }
@@ -1013,7 +1037,7 @@ sbpgpu_status sbpgpu_gibbs_batch(sbpgpu_bm* bm, const sbpgpu_config* cfg, int64_
         if (out_moves) {
             std::vector<int32_t> mv(g->N);
             CK(cudaMemcpyAsync(mv.data(), g->w.moves, g->N * 4, cudaMemcpyDeviceToHost, st));
-            CK(cudaStreamSynchronize(st));
+            host_wait(st);
             for (int64_t i = 0; i < n; ++i) out_moves[i] = mv[vertex[i]];
         }
         CK(cudaMemcpyAsync(g->flags_host, g->w.flags_dev, sizeof(DevFlags), cudaMemcpyDeviceToHost, st));
@@ -1181,9 +1205,9 @@ sbpgpu_status sbpgpu_sbp(sbpgpu_graph* g, const sbpgpu_config* cfg_in, uint64_t 
         if (stats) *stats = g->st;
         return SBPGPU_OK;
     });
-    free_all(slots_mem);
+    free_all(slots_mem, ctx->stream);
     if (bm) {
-        free_all(bm->owned);
+        free_all(bm->owned, bm->g->ctx->stream);
         delete bm;
     }
     return rc;

@@ -124,6 +124,12 @@ void carry_out(const DevGraph& g, DevBM& bm, int64_t num_to_merge, int approxima
 // w.cells when B * B <= w.cells_elems, the chain hash otherwise.
 void carry_out_exact(const DevGraph& g, DevBM& bm, int64_t num_to_merge, Work& w, cudaStream_t st);
 
+// Blocks the calling thread, sleeping rather than spinning, until the work queued on st so
+// far is done (many host threads may each drive a context of their own).
+void host_wait(cudaStream_t st);
+// 256 bytes of pinned host memory belonging to the calling thread, for scalar read-backs.
+void* host_scratch();
+
 // Launch accounting.
 int64_t kernel_launches();
 void count_launches(int64_t n);

@@ -16,7 +16,7 @@ constexpr int kSortItems = 16;
 constexpr int kSortTile = kSortThreads * kSortItems;  // 4096 keys per tile
 constexpr int kWarps = kSortThreads / 32;
 
-int64_t g_launches = 0;
+thread_local int64_t g_launches = 0;
 
 // Block-wide exclusive scan of one int per thread; returns the block total.
 __device__ __forceinline__ int block_exclusive_scan(int x, int* warp_tot, int* total) {

@@ -1,0 +1,67 @@
+"""Batched and served partitioning: every job's result in the mix equals the same
+partition run alone (same graph, arguments and seed), with the kernels of many jobs
+sharing the device."""
+import numpy as np
+import pytest
+
+from sbp_gb300 import _lib
+
+
+def test_footprint_grows_with_the_graph():
+    from sbp_gb300 import serve
+    a = serve.footprint(1000, 20000, 0)
+    b = serve.footprint(2000, 40000, 0)
+    assert 0 < a < b
+    assert serve.footprint(1000, 20000, 1 << 20) == a + (1 << 20)
+
+
+def _graphs(gpu, count, seed0):
+    out = []
+    rng = np.random.default_rng(seed0)
+    for i in range(count):
+        n = int(rng.integers(300, 2500))
+        src, dst, planted = gpu.dcsbm.generate(n, 15 * n, int(np.sqrt(n) / 4) + 2, dmin=5, dmax=60,
+                                               ratio=float(rng.uniform(1.5, 3.0)), seed=seed0 + i)
+        out.append((n, src, dst, planted))
+    return out
+
+
+@pytest.mark.gpu
+def test_server_results_equal_alone(gpu):
+    graphs = _graphs(gpu, 12, 400)
+    args = gpu.Args(algorithm="hybrid_mcmc")
+    alone = []
+    for i, (n, src, dst, _) in enumerate(graphs):
+        G = gpu.Graph(n, src, dst)
+        a, B, mdl, _ = gpu.sbp.stochastic_block_partition(G, gpu.Args(algorithm="hybrid_mcmc", seed=i))
+        alone.append((a, B, mdl))
+        G.close()
+    # a small HBM budget forces queueing behind admission; 6 workers run jobs concurrently
+    budget = 3 * gpu.serve.footprint(2500, 37500, 64 << 20)
+    with gpu.serve.Server(workers=6, hbm_budget=budget, cells_budget=64 << 20) as srv:
+        tickets = [srv.submit(n, src, dst, args, seed=i) for i, (n, src, dst, _) in enumerate(graphs)]
+        mixed = [srv.wait(t) for t in tickets]
+    for (a, B, mdl), (a2, B2, mdl2, info) in zip(alone, mixed):
+        assert B == B2
+        assert np.array_equal(a, a2)
+        assert mdl == mdl2
+        assert info["run_ms"] > 0
+
+
+@pytest.mark.gpu
+def test_batch_matches_server_and_reports_errors(gpu):
+    graphs = _graphs(gpu, 5, 700)
+    res = gpu.serve.partition_batch([(n, s, d) for n, s, d, _ in graphs], gpu.Args(algorithm="async_gibbs"),
+                                    seeds=list(range(5)), workers=3)
+    for i, (n, src, dst, _) in enumerate(graphs):
+        G = gpu.Graph(n, src, dst)
+        a, B, mdl, _ = gpu.sbp.stochastic_block_partition(G, gpu.Args(algorithm="async_gibbs", seed=i))
+        assert np.array_equal(a, res[i][0]) and B == res[i][1]
+        G.close()
+    # a job whose edges leave the vertex range fails alone; the server keeps serving
+    with gpu.serve.Server(workers=2, hbm_budget=1 << 34) as srv:
+        bad = srv.submit(10, np.array([0, 50], np.int32), np.array([1, 2], np.int32))
+        good = srv.submit(graphs[0][0], graphs[0][1], graphs[0][2], gpu.Args(algorithm="async_gibbs"), seed=0)
+        with pytest.raises(_lib.SbpGpuError):
+            srv.wait(bad)
+        assert np.array_equal(srv.wait(good)[0], res[0][0])
