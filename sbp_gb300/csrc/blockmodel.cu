@@ -6,6 +6,9 @@
 // radix sort groups equal cells, a head-flag scan compacts them into the sorted CSR
 // (row-major, ascending columns) and the same is done on (col << nb | row) for the CSC.
 // Traffic per rebuild is O(E) and independent of how many vertices moved.
+#include <mutex>
+#include <unordered_set>
+
 #include "kernels.cuh"
 #include "delta.cuh"
 #include "prims.cuh"
@@ -187,6 +190,22 @@ void host_wait(cudaStream_t st) {
     cudaEventSynchronize(ev);
 }
 
+void allow_max_dynamic_smem(const void* func) {
+    static std::mutex mu;
+    static std::unordered_set<const void*> done;
+    std::lock_guard<std::mutex> lk(mu);
+    if (done.count(func)) return;
+    cudaFuncAttributes a;
+    int dev = 0, optin = 0;
+    if (cudaFuncGetAttributes(&a, func) != cudaSuccess || cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) {
+        cudaGetLastError();
+        return;
+    }
+    cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)a.sharedSizeBytes);
+    done.insert(func);
+}
+
 void* host_scratch() {
     thread_local void* p = nullptr;
     if (!p && cudaMallocHost(&p, 256) != cudaSuccess) p = nullptr;
@@ -252,7 +271,7 @@ void launch_vertex_dS_batch(const DevGraph& g, const DevBM& bm, const int32_t* v
     int log2cap = ceil_log2((uint64_t)(2 * (max_k > 16 ? max_k : 16)));
     const size_t smem = (size_t)3 * sizeof(int32_t) << log2cap;
     if (smem > 200 * 1024) return;  // callers check the degree limit first
-    cudaFuncSetAttribute(k_vertex_dS_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    allow_max_dynamic_smem((const void*)k_vertex_dS_batch);
     k_vertex_dS_batch<<<grid_for(n, 1), kT, smem, st>>>(g, bm, v, s, n, log2cap, out);
     count_launches(1);
 }

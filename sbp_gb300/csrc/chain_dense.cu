@@ -294,7 +294,7 @@ void mh_chain_dense(const DevGraph& g, DevBM& bm, const int32_t* order, int32_t 
     if (n <= 0) return;
     const size_t smem = mh_chain_dense_smem(bm.B);
     if (bm.B <= kDenseMax) {
-        cudaFuncSetAttribute(k_mh_chain_dense<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        allow_max_dynamic_smem((const void*)k_mh_chain_dense<false>);
         k_mh_chain_dense<false><<<1, kT, smem, st>>>(g, bm, order, n, seed, iter, step, nullptr, nullptr, w.flags_dev);
         count_launches(1);
         return;
@@ -306,7 +306,7 @@ void mh_chain_dense(const DevGraph& g, DevBM& bm, const int32_t* order, int32_t 
     if (blocks < 1) blocks = 1;
     if (blocks > 152 * 16) blocks = 152 * 16;
     k_dense_fill<<<(unsigned)blocks, 256, 0, st>>>(bm, w.dense_M, w.dense_MT);
-    cudaFuncSetAttribute(k_mh_chain_dense<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    allow_max_dynamic_smem((const void*)k_mh_chain_dense<true>);
     k_mh_chain_dense<true><<<1, kT, smem, st>>>(g, bm, order, n, seed, iter, step, w.dense_M, w.dense_MT,
                                                w.flags_dev);
     count_launches(2);

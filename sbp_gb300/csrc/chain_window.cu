@@ -653,7 +653,7 @@ void mh_chain_window(const DevGraph& g, DevBM& bm, const int32_t* order, int32_t
     if (n <= 0) return;
     const size_t smem = window_smem(bm.B, p.mode, p.log2cap, p.nw);
     if (p.mode == 0) {
-        cudaFuncSetAttribute(k_mh_window<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        allow_max_dynamic_smem((const void*)k_mh_window<0>);
         k_mh_window<0><<<1, 32 * p.nw, smem, st>>>(g, bm, order, n, seed, iter, step, GlobalCells{}, (int32_t)p.ld,
                                                    p.log2cap, p.nw, greedy != 0, w.win_hash, w.flags_dev);
         count_launches(1);
@@ -673,11 +673,11 @@ void mh_chain_window(const DevGraph& g, DevBM& bm, const int32_t* order, int32_t
     if (blocks > 152 * 16) blocks = 152 * 16;
     k_window_fill<<<(unsigned)blocks, 256, 0, st>>>(bm, gc);
     if (p.mode == 1) {
-        cudaFuncSetAttribute(k_mh_window<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        allow_max_dynamic_smem((const void*)k_mh_window<1>);
         k_mh_window<1><<<1, 32 * p.nw, smem, st>>>(g, bm, order, n, seed, iter, step, gc, (int32_t)p.ld, p.log2cap,
                                                    p.nw, greedy != 0, w.win_hash, w.flags_dev);
     } else {
-        cudaFuncSetAttribute(k_mh_window<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        allow_max_dynamic_smem((const void*)k_mh_window<2>);
         k_mh_window<2><<<1, 32 * p.nw, smem, st>>>(g, bm, order, n, seed, iter, step, gc, (int32_t)p.ld, p.log2cap,
                                                    p.nw, greedy != 0, w.win_hash, w.flags_dev);
     }

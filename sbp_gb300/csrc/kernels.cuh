@@ -130,6 +130,11 @@ void host_wait(cudaStream_t st);
 // 256 bytes of pinned host memory belonging to the calling thread, for scalar read-backs.
 void* host_scratch();
 
+// Raises `func`'s dynamic shared-memory limit to the most the device allows, once per
+// kernel.  Every launcher uses the same limit, so host threads that launch concurrently
+// (the partition server's workers) never lower it under one another.
+void allow_max_dynamic_smem(const void* func);
+
 // Launch accounting.
 int64_t kernel_launches();
 void count_launches(int64_t n);

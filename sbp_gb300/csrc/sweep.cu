@@ -418,11 +418,11 @@ void gibbs_propose(const DevGraph& g, const DevBM& bm, const int32_t* vlist, int
         if (log2cap > 14) log2cap = 14;
         const size_t smem = (size_t)(3 * sizeof(int32_t)) << log2cap;
         if (greedy) {
-            cudaFuncSetAttribute(k_gibbs_big<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            allow_max_dynamic_smem((const void*)k_gibbs_big<true>);
             k_gibbs_big<true><<<152 * 2, 256, smem, st>>>(g, bm, w.list_big, counts + 1, seed, iter, step, log2cap,
                                                           w.moves, w.flags_dev);
         } else {
-            cudaFuncSetAttribute(k_gibbs_big<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            allow_max_dynamic_smem((const void*)k_gibbs_big<false>);
             k_gibbs_big<false><<<152 * 2, 256, smem, st>>>(g, bm, w.list_big, counts + 1, seed, iter, step, log2cap,
                                                            w.moves, w.flags_dev);
         }
@@ -452,7 +452,7 @@ void mh_chain(const DevGraph& g, DevBM& bm, const int32_t* order, int32_t n, int
     int log2cap = ceil_log2((uint64_t)(2 * (max_k > 64 ? max_k : 64)));
     if (log2cap > 13) log2cap = 13;
     const size_t smem = (size_t)(3 * sizeof(int32_t) << log2cap) + 2 * sizeof(int32_t) * ((1 << log2cap) + 8);
-    cudaFuncSetAttribute(k_mh_chain, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    allow_max_dynamic_smem((const void*)k_mh_chain);
     const int nbits = ceil_log2((uint64_t)(bm.B > 1 ? bm.B : 2));
     k_mh_chain<<<1, kChainThreads, smem, st>>>(g, bm, w.chain, order, n, seed, iter, step, log2cap, nbits, w.flags_dev);
     count_launches(1);
