@@ -259,10 +259,18 @@ def plain_one_at_a_time(graphs, sargs):
     return results, service
 
 
+def many_streams():
+    """Concurrent jobs run on many streams; without this the process maps all streams onto
+    8 hardware queues and kernels of unrelated jobs wait behind one another.  Must be set
+    before CUDA starts in this process."""
+    os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+
+
 def batched_workload(args):
     """Many mixed-size graphs partitioned concurrently on one GPU (the batched
     configuration) against the same graphs partitioned one at a time; both produce the
     same partitions, so NMI is equal by construction (checked)."""
+    many_streams()
     import sbp_gb300 as sb
     from sbp_gb300 import build as _b
     _b.build()
@@ -277,7 +285,8 @@ def batched_workload(args):
     nmis = [sb.evaluate.nmi(g[3], r[0]) for g, r in zip(graphs, res)]
     t_plain = float(np.sum(service))
     print(json.dumps({"workload": "batched", "metric": "jobs/s", "value": len(graphs) / t_batch, "unit": "jobs/s",
-                      "jobs": len(graphs), "workers": args.workers, "batched_s": t_batch, "plain_s": t_plain,
+                      "jobs": len(graphs), "workers": args.workers,
+                      "cuda_device_max_connections": os.environ.get("CUDA_DEVICE_MAX_CONNECTIONS"), "batched_s": t_batch, "plain_s": t_plain,
                       "plain_jobs_per_s": len(graphs) / t_plain, "speedup_vs_plain": t_plain / t_batch,
                       "identical_to_plain": bool(same), "mean_nmi": float(np.mean(nmis)),
                       "total_vertices": int(sum(g[0] for g in graphs)),
@@ -293,6 +302,7 @@ def served_workload(args):
     served one request at a time on the plain path (its latencies follow from each
     request's measured plain service time: a single FIFO server)."""
     import concurrent.futures as cf
+    many_streams()
     import sbp_gb300 as sb
     from sbp_gb300 import build as _b
     _b.build()
@@ -329,6 +339,7 @@ def served_workload(args):
     same = all(np.array_equal(plain[i][0], done[i][1][0]) for i in range(len(graphs)))
     print(json.dumps({"workload": "served", "metric": "jobs/s", "value": len(graphs) / makespan, "unit": "jobs/s",
                       "requests": len(graphs), "offered_rate_per_s": rate, "workers": args.workers,
+                      "cuda_device_max_connections": os.environ.get("CUDA_DEVICE_MAX_CONNECTIONS"),
                       "p50_ms": 1e3 * float(np.percentile(lat, 50)), "p99_ms": 1e3 * float(np.percentile(lat, 99)),
                       "plain_p50_ms": 1e3 * float(np.percentile(lat_plain, 50)),
                       "plain_p99_ms": 1e3 * float(np.percentile(lat_plain, 99)),
@@ -359,7 +370,7 @@ def main():
     ap.add_argument("--workload", default="sbp", choices=["sbp", "batched", "served"],
                     help="batched / served: many graphs through the partition server (own JSON line)")
     ap.add_argument("--jobs", type=int, default=64)
-    ap.add_argument("--workers", type=int, default=32)
+    ap.add_argument("--workers", type=int, default=16)
     ap.add_argument("--hbm-budget", type=int, default=64 << 30)
     ap.add_argument("--rate", type=float, default=0.0, help="served: offered requests/s (0: derived)")
     ap.add_argument("--max-vertices", type=int, default=50000)

@@ -176,7 +176,9 @@ sbpgpu_status sbpgpu_sbp(sbpgpu_graph* g, const sbpgpu_config* cfg, uint64_t see
  * the first job in flight is always admitted.  Each worker's context uses
  * cells_budget_bytes for dense cell counts (sbpgpu_ctx_set_cells_budget).  A job's result
  * equals sbpgpu_sbp of the same graph, configuration and seed run alone.  The job's host
- * arrays must stay valid until sbpgpu_server_wait returns for it. */
+ * arrays must stay valid until sbpgpu_server_wait returns for it.  Set the environment
+ * variable CUDA_DEVICE_MAX_CONNECTIONS=32 before CUDA starts in the process: with the
+ * default 8 hardware queues the workers' streams share queues and wait on one another. */
 typedef struct sbpgpu_server sbpgpu_server;
 typedef struct sbpgpu_job {
     int64_t num_vertices;

@@ -4,6 +4,10 @@ A Server partitions many independent graphs concurrently on one GPU: worker thre
 library, each with its own context and stream, admit jobs in submission order while the
 estimated device footprint of the jobs in flight fits the HBM budget.  Every job's result
 equals stochastic_block_partition of the same graph, arguments and seed run alone.
+
+Set CUDA_DEVICE_MAX_CONNECTIONS=32 in the environment before CUDA starts in the process:
+with the default of 8 hardware queues the workers' streams share queues and their kernels
+wait behind one another (about 3x lower throughput measured with 16 workers).
 """
 import ctypes
 
@@ -24,7 +28,7 @@ class Server:
     """Partition server on one device.  submit() returns a ticket; wait(ticket) returns
     (assignment, num_blocks, mdl, info) with info holding queued_ms, run_ms and the stats."""
 
-    def __init__(self, device=0, workers=32, hbm_budget=64 << 30, cells_budget=256 << 20):
+    def __init__(self, device=0, workers=16, hbm_budget=64 << 30, cells_budget=256 << 20):
         self.lib = _lib.load()
         h = ctypes.c_void_p()
         st = self.lib.sbpgpu_server_create(int(device), int(workers), int(hbm_budget), int(cells_budget),
@@ -73,7 +77,7 @@ class Server:
         self.close()
 
 
-def partition_batch(graphs, args=None, seeds=None, workers=32, hbm_budget=64 << 30, cells_budget=256 << 20,
+def partition_batch(graphs, args=None, seeds=None, workers=16, hbm_budget=64 << 30, cells_budget=256 << 20,
                     device=0):
     """The batched form: graphs is a list of (num_vertices, src, dst); returns one
     (assignment, num_blocks, mdl, info) per graph, in order."""
