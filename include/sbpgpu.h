@@ -84,6 +84,14 @@ sbpgpu_status sbpgpu_graph_create(sbpgpu_ctx* ctx, int64_t num_vertices, int64_t
 /* Same, with src/dst already resident in device memory. */
 sbpgpu_status sbpgpu_graph_create_device(sbpgpu_ctx* ctx, int64_t num_vertices, int64_t num_edges,
                                          const int32_t* d_src, const int32_t* d_dst, sbpgpu_graph** out);
+/* Graph::load (src/graph.cpp:33-233): a TSV edge list ("from to [weight]" per line, 1-based
+ * ids; tabs, spaces or commas; lines starting with '%' or '#' skipped) or a Matrix Market
+ * coordinate file (a "symmetric" one is read as undirected), parsed on the device.  With
+ * `undirected`, or for symmetric Matrix Market, each edge u-v (u != v) is followed by v-u,
+ * as the reference inserts it, so neighbour lists keep the reference's order.  The vertex
+ * count is the largest id (at least the Matrix Market size).  num_edges counts directed
+ * edges, also for undirected TSV input, where the reference's Graph reports half of them. */
+sbpgpu_status sbpgpu_graph_load(sbpgpu_ctx* ctx, const char* path, int32_t undirected, sbpgpu_graph** out);
 void sbpgpu_graph_destroy(sbpgpu_graph* g);
 int64_t sbpgpu_graph_num_vertices(const sbpgpu_graph* g);
 int64_t sbpgpu_graph_num_edges(const sbpgpu_graph* g);

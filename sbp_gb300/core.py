@@ -7,6 +7,7 @@ IndexError like the reference's std::invalid_argument / IndexOutOfBoundsExceptio
 """
 import atexit
 import ctypes
+import os
 import dataclasses
 import weakref
 
@@ -105,6 +106,18 @@ def _close_default_context():
         _default_ctx = None
 
 
+def load_partition(path, num_vertices):
+    """The true partition of Graph::load (src/graph.cpp:54-69): "vertex block" per line,
+    1-based; vertices without a line get -1."""
+    a = np.full(int(num_vertices), -1, np.int32)
+    with open(path) as f:
+        for line in f:
+            p = line.replace(",", " ").split()
+            if len(p) >= 2 and not line.lstrip().startswith(("%", "#")):
+                a[int(p[0]) - 1] = int(p[1]) - 1
+    return a
+
+
 def _p(a, t):
     return a.ctypes.data_as(t)
 
@@ -129,6 +142,24 @@ class Graph:
         self._bms = weakref.WeakSet()
         self.ctx._graphs.add(self)
 
+    @classmethod
+    def load(cls, path, undirected=False, ctx=None):
+        """Graph::load (src/graph.cpp:33-233): a TSV edge list or a Matrix Market file parsed
+        on the device (include/sbpgpu.h, sbpgpu_graph_load).  The edge arrays are not kept
+        on the host."""
+        self = cls.__new__(cls)
+        self.ctx = ctx or default_context()
+        h = ctypes.c_void_p()
+        self.ctx.check(self.ctx.lib.sbpgpu_graph_load(self.ctx.h, os.fsencode(path), int(bool(undirected)),
+                                                      ctypes.byref(h)))
+        self.h = h
+        self._N = int(self.ctx.lib.sbpgpu_graph_num_vertices(h))
+        self.src = self.dst = None
+        self._E = int(self.ctx.lib.sbpgpu_graph_num_edges(h))
+        self._bms = weakref.WeakSet()
+        self.ctx._graphs.add(self)
+        return self
+
     def close(self):
         """Destroys the graph after every blockmodel built on it (finalisers may run in any
         order when objects are collected together)."""
@@ -144,7 +175,7 @@ class Graph:
         return self._N
 
     def num_edges(self):
-        return int(self.src.size)
+        return self._E if self.src is None else int(self.src.size)
 
     def out_neighbors(self, v):
         return self.dst[self.src == v]

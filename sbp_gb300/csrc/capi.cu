@@ -762,6 +762,80 @@ sbpgpu_status sbpgpu_graph_create_device(sbpgpu_ctx* ctx, int64_t N, int64_t E, 
     return sbpgpu_graph_create(ctx, N, E, src.data(), dst.data(), out);
 }
 
+sbpgpu_status sbpgpu_graph_load(sbpgpu_ctx* ctx, const char* path, int32_t undirected, sbpgpu_graph** out) {
+    if (!ctx || !path || !out) return SBPGPU_EINVAL;
+    *out = nullptr;
+    std::string data;
+    {
+        FILE* f = std::fopen(path, "rb");
+        if (!f) return fail(ctx, SBPGPU_EINVAL, std::string("cannot open ") + path);
+        char buf[1 << 16];
+        size_t got;
+        while ((got = std::fread(buf, 1, sizeof(buf), f)) > 0) data.append(buf, got);
+        std::fclose(f);
+    }
+    // Matrix Market: banner, comment lines, then "rows cols entries" (graph.cpp:75-103)
+    size_t offset = 0;
+    int64_t header_n = 0;
+    bool symmetric = false;
+    auto next_line = [&](size_t at) {
+        const size_t e = data.find('\n', at);
+        return e == std::string::npos ? data.size() : e + 1;
+    };
+    if (data.compare(0, 14, "%%MatrixMarket") == 0) {
+        const size_t e = next_line(0);
+        std::vector<std::string> tok;
+        {
+            std::string cur;
+            for (size_t i = 0; i < e; ++i) {
+                const char c = data[i];
+                if (c == ' ' || c == '\t' || c == '\n' || c == '\r') {
+                    if (!cur.empty()) tok.push_back(cur);
+                    cur.clear();
+                } else {
+                    cur += c;
+                }
+            }
+            if (!cur.empty()) tok.push_back(cur);
+        }
+        if (tok.size() < 5 || tok[2] != "coordinate")
+            return fail(ctx, SBPGPU_EINVAL, "only coordinate Matrix Market files hold graphs");
+        symmetric = tok[4] == "symmetric";
+        size_t at = e;
+        while (at < data.size() && data[at] == '%') at = next_line(at);
+        long long rows = 0, cols = 0, nnz = 0;
+        if (std::sscanf(data.c_str() + at, "%lld %lld %lld", &rows, &cols, &nnz) != 3)
+            return fail(ctx, SBPGPU_EINVAL, "missing Matrix Market size line");
+        if (rows != cols) return fail(ctx, SBPGPU_EINVAL, "rectangular matrices are not graphs");
+        header_n = rows;
+        offset = next_line(at);
+    }
+    const int un = (undirected || symmetric) ? 1 : 0;
+    int32_t *d_src = nullptr, *d_dst = nullptr;
+    int64_t E = 0, max_id = 0;
+    const sbpgpu_status rc = guarded(ctx, [&] {
+        CK(cudaSetDevice(ctx->device));
+        const int64_t n = (int64_t)(data.size() - offset);
+        char* d_text = nullptr;
+        if (n > 0) {
+            CK(cudaMallocAsync(&d_text, (size_t)n, ctx->stream));
+            CK(cudaMemcpyAsync(d_text, data.data() + offset, (size_t)n, cudaMemcpyHostToDevice, ctx->stream));
+        }
+        std::string err;
+        const bool ok = parse_edges_device(d_text, n, un, &d_src, &d_dst, &E, &max_id, &err, ctx->stream);
+        if (d_text) cudaFreeAsync(d_text, ctx->stream);
+        if (!ok) throw ApiError(SBPGPU_EINVAL, err);
+        return SBPGPU_OK;
+    });
+    if (rc != SBPGPU_OK) return rc;
+    const int64_t N = std::max<int64_t>(max_id, header_n);
+    sbpgpu_status rc2 = N > 0 ? sbpgpu_graph_create_device(ctx, N, E, d_src, d_dst, out)
+                              : fail(ctx, SBPGPU_EINVAL, "the file holds no vertices");
+    if (d_src) cudaFreeAsync(d_src, ctx->stream);
+    if (d_dst) cudaFreeAsync(d_dst, ctx->stream);
+    return rc2;
+}
+
 void sbpgpu_graph_destroy(sbpgpu_graph* g) {
     if (!g || g->dead) return;
     g->dead = true;

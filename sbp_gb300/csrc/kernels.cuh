@@ -2,6 +2,8 @@
 // merge.cu).  All work is issued on the given stream.
 #pragma once
 
+#include <string>
+
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -134,6 +136,13 @@ void* host_scratch();
 // kernel.  Every launcher uses the same limit, so host threads that launch concurrently
 // (the partition server's workers) never lower it under one another.
 void allow_max_dynamic_smem(const void* func);
+
+// ---- ingest.cu
+// Parses edge lines ("from to [weight]", 1-based) held in device memory into 0-based device
+// edge arrays in file order, with each reverse edge right after its edge when undirected.
+// *max_id is the largest 1-based id seen.  The arrays are allocated on st (cudaMallocAsync).
+bool parse_edges_device(const char* d_text, int64_t n, int undirected, int32_t** d_src, int32_t** d_dst, int64_t* E,
+                        int64_t* max_id, std::string* err, cudaStream_t st);
 
 // Launch accounting.
 int64_t kernel_launches();
