@@ -175,6 +175,19 @@ sbpgpu_status sbpgpu_merge_proposals(sbpgpu_bm* bm, uint64_t seed, int32_t step,
 sbpgpu_status sbpgpu_sbp(sbpgpu_graph* g, const sbpgpu_config* cfg, uint64_t seed, int32_t* out_assignment,
                          int64_t* num_blocks, double* out_mdl, sbpgpu_stats* stats);
 
+/* ---- evaluation ------------------------------------------------------------------ */
+/* evaluate::evaluate_blockmodel (src/evaluate.cpp:9-180) against a true partition: the
+ * contingency table is counted on the device; NMI (float-log marginal entropies as the
+ * reference), pair-counting F1 / precision / recall / Rand index and the accuracy of the
+ * best one-to-one matching of communities follow on the host.  truth[i] < 0 marks an
+ * unlabelled vertex (left out of the table); assignment values are blocks >= 0. */
+typedef struct sbpgpu_eval {
+    double nmi, f1, precision, recall, rand_index, accuracy;
+    int64_t true_blocks, found_blocks;
+} sbpgpu_eval;
+sbpgpu_status sbpgpu_evaluate(sbpgpu_ctx* ctx, int64_t n, const int32_t* truth, const int32_t* assignment,
+                              sbpgpu_eval* out);
+
 /* ---- batched and served partitioning ----------------------------------------------
  * No counterpart in the reference (its plain driver partitions one graph per process).  A
  * server partitions many independent graphs at once on one device: `workers` host threads,

@@ -58,6 +58,14 @@ class KernelTiming(ctypes.Structure):
 
 
 # name -> (restype, argtypes); every symbol declared in include/sbpgpu.h.
+class Eval(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_double) for n in ("nmi", "f1", "precision", "recall", "rand_index", "accuracy")] + \
+        [("true_blocks", ctypes.c_int64), ("found_blocks", ctypes.c_int64)]
+
+    def as_dict(self):
+        return {n: (float if t is ctypes.c_double else int)(getattr(self, n)) for n, t in self._fields_}
+
+
 class Job(ctypes.Structure):
     _fields_ = [
         ("num_vertices", ctypes.c_int64), ("num_edges", ctypes.c_int64),
@@ -112,6 +120,7 @@ SIGNATURES = {
     "sbpgpu_merge_proposals": (ctypes.c_int, [vp, ctypes.c_uint64, ctypes.c_int32, i32p, f64p]),
     "sbpgpu_sbp": (ctypes.c_int, [vp, ctypes.POINTER(Config), ctypes.c_uint64, i32p, i64p, f64p,
                                   ctypes.POINTER(Stats)]),
+    "sbpgpu_evaluate": (ctypes.c_int, [vp, ctypes.c_int64, i32p, i32p, ctypes.POINTER(Eval)]),
     "sbpgpu_job_footprint": (ctypes.c_int64, [ctypes.c_int64, ctypes.c_int64, ctypes.c_int64]),
     "sbpgpu_server_create": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int64, ctypes.c_int64,
                                             ctypes.POINTER(vp)]),

@@ -15,6 +15,7 @@
 #include <new>
 #include <stdexcept>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "../../include/sbpgpu.h"
@@ -834,6 +835,53 @@ sbpgpu_status sbpgpu_graph_load(sbpgpu_ctx* ctx, const char* path, int32_t undir
     if (d_src) cudaFreeAsync(d_src, ctx->stream);
     if (d_dst) cudaFreeAsync(d_dst, ctx->stream);
     return rc2;
+}
+
+sbpgpu_status sbpgpu_evaluate(sbpgpu_ctx* ctx, int64_t n, const int32_t* truth, const int32_t* assignment,
+                              sbpgpu_eval* out) {
+    if (!ctx || !out || n <= 0 || !truth || !assignment) return SBPGPU_EINVAL;
+    return guarded(ctx, [&] {
+        // true communities renumbered in order of first appearance (evaluate.cpp:103-113)
+        std::unordered_map<int32_t, int32_t> ids;
+        std::vector<int32_t> t(n);
+        int64_t nb = 0;
+        for (int64_t i = 0; i < n; ++i) {
+            if (assignment[i] < 0) throw ApiError(SBPGPU_EINVAL, "negative block in the assignment");
+            nb = std::max<int64_t>(nb, (int64_t)assignment[i] + 1);
+            if (truth[i] < 0) {
+                t[i] = -1;
+                continue;
+            }
+            auto it = ids.emplace(truth[i], (int32_t)ids.size()).first;
+            t[i] = it->second;
+        }
+        const int64_t nt = (int64_t)ids.size();
+        if (nt == 0) throw ApiError(SBPGPU_EINVAL, "no vertex of the true partition is labelled");
+        if (nt * nb > (int64_t(1) << 28)) throw ApiError(SBPGPU_EINVAL, "contingency table above 2^28 cells");
+        cudaStream_t st = ctx->stream;
+        std::vector<void*> tmp;
+        int32_t* dt = dalloc<int32_t>(tmp, n);
+        int32_t* da = dalloc<int32_t>(tmp, n);
+        auto* table = dalloc<unsigned long long>(tmp, (size_t)(nt * nb));
+        std::vector<unsigned long long> h((size_t)(nt * nb));
+        try {
+            CK(cudaMemcpyAsync(dt, t.data(), n * 4, cudaMemcpyHostToDevice, st));
+            CK(cudaMemcpyAsync(da, assignment, n * 4, cudaMemcpyHostToDevice, st));
+            CK(cudaMemsetAsync(table, 0, h.size() * sizeof(unsigned long long), st));
+            launch_contingency(dt, da, n, (int32_t)nb, table, st);
+            CK(cudaMemcpyAsync(h.data(), table, h.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+            host_wait(st);
+            CK(cudaGetLastError());
+        } catch (...) {
+            free_all(tmp, st);
+            throw;
+        }
+        free_all(tmp, st);
+        const PartitionQuality q = quality_from_table(h, nt, nb, n);
+        *out = sbpgpu_eval{q.nmi, q.f1, q.precision, q.recall, q.rand_index, q.accuracy, q.true_blocks,
+                           q.found_blocks};
+        return SBPGPU_OK;
+    });
 }
 
 void sbpgpu_graph_destroy(sbpgpu_graph* g) {

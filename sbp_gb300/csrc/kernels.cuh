@@ -3,6 +3,7 @@
 #pragma once
 
 #include <string>
+#include <vector>
 
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -143,6 +144,18 @@ void allow_max_dynamic_smem(const void* func);
 // *max_id is the largest 1-based id seen.  The arrays are allocated on st (cudaMallocAsync).
 bool parse_edges_device(const char* d_text, int64_t n, int undirected, int32_t** d_src, int32_t** d_dst, int64_t* E,
                         int64_t* max_id, std::string* err, cudaStream_t st);
+
+// ---- evaluate.cu
+struct PartitionQuality {
+    double nmi, f1, precision, recall, rand_index, accuracy;
+    int64_t true_blocks, found_blocks;
+};
+// table[t * ncols + f] += 1 for every vertex with truth t >= 0 and found block f.
+void launch_contingency(const int32_t* truth, const int32_t* found, int64_t n, int32_t ncols,
+                        unsigned long long* table, cudaStream_t st);
+// Metrics of evaluate::evaluate_blockmodel from the nt x nb table (rows = true).
+PartitionQuality quality_from_table(const std::vector<unsigned long long>& table, int64_t nt, int64_t nb,
+                                    int64_t num_vertices);
 
 // Launch accounting.
 int64_t kernel_launches();

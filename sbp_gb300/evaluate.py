@@ -1,10 +1,29 @@
-"""Partition quality against a planted partition: normalised mutual information.
+"""Partition quality against a true partition.
 
-Follows evaluate::calculate_nmi (reference src/evaluate.cpp:63-98): contingency table
-of (true block, found block), joint and marginal entropies in natural log,
-NMI = I / sqrt(H_true * H_found).
+evaluate() is evaluate::evaluate_blockmodel (reference src/evaluate.cpp:9-180) through the
+device (sbpgpu_evaluate): contingency table on the GPU; NMI, pair-counting F1 / precision /
+recall / Rand index and the matched accuracy on the host.  nmi() is a host restatement of
+calculate_nmi (evaluate.cpp:63-98) used where no context is wanted.
 """
+import ctypes
+
 import numpy as np
+
+
+def evaluate(true_assignment, assignment, ctx=None):
+    """Returns a dict with nmi, f1, precision, recall, rand_index, accuracy, true_blocks and
+    found_blocks; true_assignment < 0 marks unlabelled vertices."""
+    from . import _lib
+    from .core import default_context
+    c = ctx or default_context()
+    t = np.ascontiguousarray(true_assignment, dtype=np.int32)
+    a = np.ascontiguousarray(assignment, dtype=np.int32)
+    if t.shape != a.shape:
+        raise ValueError("assignments differ in length")
+    out = _lib.Eval()
+    c.check(c.lib.sbpgpu_evaluate(c.h, t.size, t.ctypes.data_as(_lib.i32p), a.ctypes.data_as(_lib.i32p),
+                                  ctypes.byref(out)))
+    return out.as_dict()
 
 
 def nmi(true_assignment, assignment):

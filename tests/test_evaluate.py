@@ -1,0 +1,80 @@
+"""Partition quality (sbpgpu_evaluate) against a numpy restatement of the reference's
+evaluate::evaluate_blockmodel (src/evaluate.cpp:9-180): the contingency table counted on the
+device gives the same pair-counting F1 / precision / recall / Rand index (exact formulas,
+tolerance 1e-12), the same NMI (the reference takes the marginal entropies with float logs;
+tolerance 1e-6 covers a last-bit difference between float log implementations) and the
+accuracy of the best one-to-one matching (exact, against scipy's assignment solver)."""
+import numpy as np
+import pytest
+
+from sbp_gb300.evaluate import evaluate
+
+
+def _reference_metrics(truth, found):
+    """evaluate.cpp:103-140 (translator, orientation) then :9-98 on rows = found blocks."""
+    ids = {}
+    t = np.empty_like(truth)
+    for i, x in enumerate(truth.tolist()):
+        t[i] = -1 if x < 0 else ids.setdefault(x, len(ids))
+    nt, nb, V = len(ids), int(found.max()) + 1, truth.size
+    m = np.zeros((nb, nt), np.int64)
+    keep = t >= 0
+    np.add.at(m, (found[keep], t[keep]), 1)
+    x = m.astype(np.float64)
+    cell_pairs = (x * (x - 1)).sum() / 2.0
+    rows, cols = x.sum(1), x.sum(0)
+    row_pairs, col_pairs = (rows * (rows - 1)).sum() / 2.0, (cols * (cols - 1)).sum() / 2.0
+    agree_diff = (V * V + (x * x).sum() - ((rows * rows).sum() + (cols * cols).sum())) / 2.0
+    recall, precision = cell_pairs / row_pairs, cell_pairs / col_pairs
+    p = x / V
+    p1, p2 = p.sum(1), p.sum(0)
+    h1 = -(p1 * np.log(p1.astype(np.float32)).astype(np.float64)).sum()
+    h2 = -(p2 * np.log(p2.astype(np.float32)).astype(np.float64)).sum()
+    nz = p > 0
+    mi = (p[nz] * np.log(p[nz] / np.outer(p1, p2)[nz])).sum()
+    sp = pytest.importorskip("scipy.optimize")
+    r, c = sp.linear_sum_assignment(m, maximize=True)
+    return dict(nmi=mi / np.sqrt(h1 * h2), f1=2 * precision * recall / (precision + recall), precision=precision,
+                recall=recall, rand_index=(cell_pairs + agree_diff) / (V * (V - 1.0) / 2.0),
+                accuracy=m[r, c].sum() / V, true_blocks=nt, found_blocks=nb)
+
+
+def _planted(rng, n, nt, nb, noise, unlabelled):
+    truth = rng.integers(0, nt, n).astype(np.int32) * 7 + 3  # sparse community labels, renumbered
+    found = ((truth // 7) % nb).astype(np.int32)
+    if noise > 0:
+        found = np.where(rng.random(n) < noise, rng.integers(0, nb, n), found).astype(np.int32)
+        found[:nb] = np.arange(nb)  # every found block non-empty
+    truth[rng.random(n) < unlabelled] = -1
+    return truth, found
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n,nt,nb,noise,unlabelled", [
+    (200, 5, 5, 0.0, 0.0),      # identical up to relabelling
+    (5000, 12, 20, 0.2, 0.0),   # more found blocks than communities
+    (5000, 30, 9, 0.3, 0.05),   # fewer found blocks, some vertices unlabelled
+    (200000, 64, 64, 0.5, 0.1),
+])
+def test_evaluate_matches_reference_formulas(n, nt, nb, noise, unlabelled):
+    rng = np.random.default_rng(n + nt + nb)
+    truth, found = _planted(rng, n, nt, nb, noise, unlabelled)
+    got = evaluate(truth, found)
+    want = _reference_metrics(truth, found)
+    assert got["true_blocks"] == want["true_blocks"] and got["found_blocks"] == want["found_blocks"]
+    for k in ("f1", "precision", "recall", "rand_index", "accuracy"):
+        assert got[k] == pytest.approx(want[k], rel=1e-12, abs=1e-14), k
+    assert got["nmi"] == pytest.approx(want["nmi"], rel=1e-6), "nmi"
+    if noise == 0.0 and unlabelled == 0.0:
+        assert got["accuracy"] == 1.0 and got["f1"] == pytest.approx(1.0) and got["nmi"] == pytest.approx(1.0)
+
+
+@pytest.mark.gpu
+def test_evaluate_rejects_bad_input():
+    from sbp_gb300._lib import SbpGpuError
+    with pytest.raises((SbpGpuError, ValueError)):
+        evaluate(np.zeros(4, np.int32), np.array([0, 1, -1, 0], np.int32))
+    with pytest.raises((SbpGpuError, ValueError)):
+        evaluate(np.full(4, -1, np.int32), np.zeros(4, np.int32))
+    with pytest.raises(ValueError):
+        evaluate(np.zeros(4, np.int32), np.zeros(5, np.int32))
