@@ -90,6 +90,7 @@ struct ora_graph {
     std::vector<int32_t> selfcnt;
     std::vector<double> Ld;     // fastlog table: logf((float)x) (fastlog.hpp:21-30)
     std::vector<int64_t> Lq;    // the same values in units of 2^-24 (exact)
+    std::vector<int64_t> LG;    // lgamma(x + 1) rounded to units of 2^-24 (nonparametric terms)
 };
 
 namespace {
@@ -98,9 +99,10 @@ const double kFix = 16777216.0;  // 2^24
 const double kInvFix = 1.0 / 16777216.0;
 
 void build_log_tables(ora_graph* g) {
-    const int64_t n = g->E + 2;
+    const int64_t n = std::max(g->E, g->N) + 2;  // edge counts, degrees and block sizes
     g->Ld.resize(n);
     g->Lq.resize(n);
+    g->LG.resize(n);
     g->Ld[0] = 0.0;
     g->Lq[0] = 0;
     for (int64_t x = 1; x < n; ++x) {
@@ -108,6 +110,7 @@ void build_log_tables(ora_graph* g) {
         g->Ld[x] = v;
         g->Lq[x] = (int64_t)(v * kFix);
     }
+    for (int64_t x = 0; x < n; ++x) g->LG[x] = llrint(lgamma((double)(x + 1)) * kFix);
 }
 
 }  // namespace
@@ -147,6 +150,7 @@ struct ora_bm {
     std::vector<std::map<int32_t, int64_t>> row, col;  // matrix and transpose
     double entropy = DBL_MAX;
     int64_t num_blocks_to_merge = 0;
+    int64_t nonempty = 0;  // Blockmodel::_num_nonempty_blocks
     bool empty = false;
 
     int64_t get(int64_t r, int64_t c) const {
@@ -194,6 +198,8 @@ void build(ora_bm* bm) {
             if (b != nb) bm->dtot[b] += 1;
         }
     }
+    bm->nonempty = 0;  // blockmodel.cpp:194, :231
+    for (int64_t b = 0; b < B; ++b) bm->nonempty += bm->sizes[b] > 0;
 }
 
 /* common::cell_entropy (common.hpp:39-50) in the reference's double arithmetic. */
@@ -362,6 +368,126 @@ int64_t merge_dS_fixed(const ora_bm* bm, int64_t r, int64_t s) {
     return merge_delta_mdl_generic<int64_t>(bm, r, s, d, ce_fixed);
 }
 
+// ---------------------------------------------------------------- nonparametric entropy
+/* entropy::nonparametric (entropy.cpp:617-1225, entropy.hpp:101-190) for a directed graph
+ * without degree correction (args.undirected = args.degreecorrected = false).
+ * fastlgamma(x) = lgamma((double)x) (fastlgamma.hpp:19-27, fastlgamma.cpp:11-20);
+ * fastlog(x) = logf(x) (fastlog.hpp:21-30).  Canonical arithmetic, shared with the device:
+ * every lgamma(x + 1) term is rounded to units of 2^-24 (LG), the vterm products use the
+ * exact fastlog table, and the partition / edge-count terms that depend on the number of
+ * non-empty blocks enter as one rounded value per change of that number. */
+
+/* fastlbinom (entropy.hpp:144-148). */
+inline double np_lbinom(int64_t N, int64_t k) {
+    if (N == 0 || k == 0 || k > N) return 0.0;
+    return (lgamma((double)(N + 1)) - lgamma((double)(k + 1))) - lgamma((double)(N - k + 1));
+}
+/* get_edges_dl (entropy.cpp:745-749), directed: NB = B * B. */
+inline double np_edges_dl(int64_t b, int64_t E) { return np_lbinom(b * b + E - 1, E); }
+/* Change of lbinom(N - 1, B - 1) (get_delta_partition_dl, entropy.cpp:933-940) plus
+ * get_delta_edges_dl (:1111-1143) when the non-empty block count goes from b to b + dB. */
+inline int64_t np_dl_step(const ora_graph* g, int64_t b, int dB) {
+    const double part = np_lbinom(g->N - 1, b + dB - 1) - np_lbinom(g->N - 1, b - 1);
+    const double edges = np_edges_dl(b + dB, g->E) - np_edges_dl(b, g->E);
+    return llrint((part + edges) * kFix);
+}
+/* vterm_exact (entropy.hpp:117-133), directed, not degree-corrected. */
+inline int64_t np_vterm(const ora_graph* g, int64_t dout, int64_t din, int64_t w) {
+    return w == 0 ? 0 : (dout + din) * g->Lq[w];
+}
+/* The block terms of virtual_move_sparse (entropy.cpp:822-889), the lgamma terms of
+ * get_delta_partition_dl (:892-1000) and the non-empty-count terms for moving `weight`
+ * vertices with kout / kin edges from r to s. */
+int64_t np_block_terms(const ora_bm* bm, int64_t r, int64_t s, int64_t kout, int64_t kin, int64_t weight) {
+    const ora_graph* g = bm->g;
+    const int64_t sr = bm->sizes[r], ss = bm->sizes[s];
+    int64_t t = np_vterm(g, bm->dout[r] - kout, bm->din[r] - kin, sr - weight) - np_vterm(g, bm->dout[r], bm->din[r], sr);
+    t += np_vterm(g, bm->dout[s] + kout, bm->din[s] + kin, ss + weight) - np_vterm(g, bm->dout[s], bm->din[s], ss);
+    t += g->LG[sr] + g->LG[ss] - g->LG[sr - weight] - g->LG[ss + weight];
+    const int dB = (sr == weight ? -1 : 0) + (ss == 0 ? 1 : 0);
+    if (dB != 0) t += np_dl_step(g, bm->nonempty, dB);
+    return t;
+}
+/* entries_dS (entropy.cpp:782-809): eterm_exact(M + change) - eterm_exact(M) per entry. */
+inline int64_t np_entries(const ora_bm* bm, const DeltaMap& d) {
+    int64_t t = 0;
+    for (const auto& e : d) {
+        const int64_t m = bm->get(e.first.first, e.first.second);
+        t += bm->g->LG[m] - bm->g->LG[m + e.second];
+    }
+    return t;
+}
+/* nonparametric::delta_mdl (entropy.cpp:1146-1178), units of 2^-24. */
+int64_t np_vertex_dS(const ora_bm* bm, int64_t v, int64_t s, const DeltaMap& d) {
+    const int64_t r = bm->asg[v];
+    if (r == s) return 0;
+    const VertexInfo vi = vinfo(bm->g, v);
+    return np_entries(bm, d) + np_block_terms(bm, r, s, vi.kout, vi.kin, 1);
+}
+/* nonparametric::block_merge_delta_mdl (entropy.cpp:1198-1223), units of 2^-24. */
+int64_t np_merge_dS(const ora_bm* bm, int64_t r, int64_t s, const DeltaMap& d) {
+    if (r == s || bm->sizes[r] == 0 || bm->sizes[s] == 0) return 0;
+    int64_t kout = 0, kin = 0;
+    for (const auto& e : bm->row[r]) kout += e.second;
+    for (const auto& e : bm->col[r]) kin += e.second;
+    return np_entries(bm, d) + np_block_terms(bm, r, s, kout, kin, bm->sizes[r]);
+}
+/* The reference's double arithmetic of the same two deltas (for the known-answer checks). */
+double np_dS_literal(const ora_bm* bm, int64_t r, int64_t s, const DeltaMap& d, int64_t kout, int64_t kin,
+                     int64_t weight) {
+    const ora_graph* g = bm->g;
+    auto lg = [](int64_t x) { return lgamma((double)x); };
+    auto vt = [&](int64_t o, int64_t i, int64_t w) { return w == 0 ? 0.0 : (double)(o + i) * g->Ld[w]; };
+    double dS = 0.0;
+    for (const auto& e : d) {
+        const int64_t m = bm->get(e.first.first, e.first.second);
+        dS += -lg(m + e.second + 1) - (-lg(m + 1));
+    }
+    const int64_t sr = bm->sizes[r], ss = bm->sizes[s];
+    dS += vt(bm->dout[r] - kout, bm->din[r] - kin, sr - weight);
+    dS -= vt(bm->dout[r], bm->din[r], sr);
+    dS += vt(bm->dout[s] + kout, bm->din[s] + kin, ss + weight);
+    dS -= vt(bm->dout[s], bm->din[s], ss);
+    double Sb = -lg(sr + 1) - lg(ss + 1), Sa = -lg(sr - weight + 1) - lg(ss + weight + 1);
+    const int dB = (sr == weight ? -1 : 0) + (ss == 0 ? 1 : 0);
+    double edges = 0.0;
+    if (dB != 0) {
+        Sb += np_lbinom(g->N - 1, bm->nonempty - 1);
+        Sa += np_lbinom(g->N - 1, bm->nonempty + dB - 1);
+        edges = np_edges_dl(bm->nonempty + dB, g->E) - np_edges_dl(bm->nonempty, g->E);
+    }
+    return dS + ((Sa - Sb) + 0.0 + edges);
+}
+/* nonparametric::mdl (entropy.cpp:751-779), canonical: exact sum of the table terms, then
+ * the two terms of the non-empty block count. */
+double np_mdl_canonical(const ora_bm* bm) {
+    const ora_graph* g = bm->g;
+    int64_t fixed = 0;
+    for (int64_t r = 0; r < bm->B; ++r)
+        for (const auto& e : bm->row[r]) fixed -= g->LG[e.second];
+    for (int64_t b = 0; b < bm->B; ++b) fixed += np_vterm(g, bm->dout[b], bm->din[b], bm->sizes[b]) - g->LG[bm->sizes[b]];
+    fixed += g->LG[g->N] + g->Lq[g->N];
+    return (double)fixed * kInvFix + (np_lbinom(g->N - 1, bm->nonempty - 1) + np_edges_dl(bm->nonempty, g->E));
+}
+/* The four parts in the reference's arithmetic. */
+void np_terms_literal(const ora_bm* bm, double out[4]) {
+    const ora_graph* g = bm->g;
+    double S = 0.0;
+    for (int64_t r = 0; r < bm->B; ++r)
+        for (const auto& e : bm->row[r]) S += -lgamma((double)(e.second + 1));
+    for (int64_t b = 0; b < bm->B; ++b)
+        if (bm->sizes[b] != 0) S += (double)(bm->dout[b] + bm->din[b]) * g->Ld[bm->sizes[b]];
+    double P = 0.0;
+    P += np_lbinom(g->N - 1, bm->nonempty - 1);
+    P += lgamma((double)(g->N + 1));
+    for (int64_t b = 0; b < bm->B; ++b) P -= lgamma((double)(bm->sizes[b] + 1));
+    P += g->Ld[g->N];
+    out[0] = S;
+    out[1] = P;
+    out[2] = 0.0;
+    out[3] = np_edges_dl(bm->nonempty, g->E);
+}
+
 /* A non-negative double as an integer count of 2^-64 units (truncated): every term of the
  * Hastings sums goes through this, so the sums are exact integers and do not depend on the
  * order in which the neighbour blocks are visited (the device sums them in parallel). */
@@ -388,7 +514,7 @@ inline double fix64_to_double(__int128 q) {
  * the two sums converted back to double. */
 double hastings(const ora_bm* bm, int64_t v, int64_t s, const DeltaMap& d, int64_t num_neighbor_edges,
                 const ora_config* cfg) {
-    if (num_neighbor_edges == 0 || cfg->greedy) return 1.0;
+    if (num_neighbor_edges == 0 || cfg->greedy || cfg->nonparametric) return 1.0;  // entropy.cpp:499
     const ora_graph* g = bm->g;
     const int64_t r = bm->asg[v];
     const VertexInfo vi = vinfo(g, v);
@@ -419,7 +545,7 @@ double hastings(const ora_bm* bm, int64_t v, int64_t s, const DeltaMap& d, int64
 
 /* finetune::accept (finetune.cpp:22-32). */
 inline bool accept(double dS, double H, const ora_config* cfg, uint32_t w) {
-    if (cfg->greedy) return dS < 0.0;
+    if (cfg->greedy && !cfg->nonparametric) return dS < 0.0;  // --nonparametric sets greedy off
     const double u = (double)w * (1.0 / 4294967296.0);
     double p = exp(-3.0 * dS) * H;
     p = p >= 1.0 ? 1.0 : p;
@@ -509,6 +635,9 @@ bool apply_v3(ora_bm* bm, int64_t v, int64_t s) {
     bm->asg[v] = (int32_t)s;
     bm->sizes[r]--;
     bm->sizes[s]++;
+    // the count of non-empty blocks as a recount gives it (a move that would empty its
+    // block is rejected above, so only a move into an empty block changes it)
+    if (bm->sizes[s] == 1) bm->nonempty++;
     return true;
 }
 
@@ -532,6 +661,8 @@ void apply_delta_move(ora_bm* bm, int64_t v, int64_t s, const DeltaMap& d) {
     bm->dtot[s] = bm->dout[s] + bm->din[s] - bm->get(s, s);
     bm->sizes[r]--;
     bm->sizes[s]++;
+    if (bm->sizes[r] == 0) bm->nonempty--;  // blockmodel.cpp:429-430
+    if (bm->sizes[s] == 1) bm->nonempty++;
 }
 
 /* Canonical MDL log term: round-to-float(log(x)) in units of 2^-24 (see sbp_oracle.h). */
@@ -565,6 +696,11 @@ double mdl_canonical(const ora_bm* bm) {
     double c;
     mdl_both(bm, nullptr, &c);
     return c;
+}
+
+/* entropy::mdl (entropy.cpp:597-604): the nonparametric form under --nonparametric. */
+double mdl_for(const ora_bm* bm, const ora_config* cfg) {
+    return cfg->nonparametric ? np_mdl_canonical(bm) : mdl_canonical(bm);
 }
 
 /* finetune::early_stop (finetune.cpp:265-283). */
@@ -626,7 +762,8 @@ Proposal gibbs_proposal(const ora_bm* bm, int64_t v, uint64_t seed, uint32_t ite
     const int64_t s = propose_vertex(bm, v, w);
     if (s == r) return {-1, 0.0, false};
     const DeltaMap d = vertex_delta(bm, v, s);
-    const double dS = (double)delta_mdl_generic<int64_t>(bm, v, s, d, ce_fixed) * kInvFix;
+    const double dS = (double)(cfg->nonparametric ? np_vertex_dS(bm, v, s, d)
+                                                  : delta_mdl_generic<int64_t>(bm, v, s, d, ce_fixed)) * kInvFix;
     const VertexInfo vi = vinfo(bm->g, v);
     const double H = hastings(bm, v, s, d, vi.kout + vi.kin, cfg);
     if (accept(dS, H, cfg, w[3])) return {(int32_t)s, dS, true};
@@ -643,7 +780,8 @@ bool mh_step(ora_bm* bm, int64_t v, uint64_t seed, uint32_t iteration, uint32_t 
     const int64_t s = propose_vertex(bm, v, w);
     if (s == r) return false;
     const DeltaMap d = vertex_delta(bm, v, s);
-    const double dS = (double)delta_mdl_generic<int64_t>(bm, v, s, d, ce_fixed) * kInvFix;
+    const double dS = (double)(cfg->nonparametric ? np_vertex_dS(bm, v, s, d)
+                                                  : delta_mdl_generic<int64_t>(bm, v, s, d, ce_fixed)) * kInvFix;
     const VertexInfo vi = vinfo(bm->g, v);
     const double H = hastings(bm, v, s, d, vi.kout + vi.kin, cfg);
     if (!accept(dS, H, cfg, w[3])) return false;
@@ -692,7 +830,7 @@ void async_gibbs(ora_bm* bm, const ora_config* cfg, uint64_t seed, uint32_t step
     const ora_graph* g = bm->g;
     if (bm->B == 1) return;
     std::vector<double> deltas;
-    const double initial = mdl_canonical(bm);
+    const double initial = mdl_for(bm, cfg);
     bm->entropy = initial;
     double last = initial;
     std::vector<int32_t> base(g->N), order;
@@ -708,13 +846,13 @@ void async_gibbs(ora_bm* bm, const ora_config* cfg, uint64_t seed, uint32_t step
             const int64_t end = std::min(g->N, (batch + 1) * batch_size);
             gibbs_batch(bm, vs.data() + start, end - start, seed, (uint32_t)it, step, cfg, nullptr, nullptr, st);
         }
-        const double e = mdl_canonical(bm);
+        const double e = mdl_for(bm, cfg);
         deltas.push_back(e - last);
         last = e;
         if (st) st->mcmc_iterations++;
         if (early_stop(it, golden, initial, deltas)) break;
     }
-    bm->entropy = mdl_canonical(bm);
+    bm->entropy = mdl_for(bm, cfg);
 }
 
 /* finetune::hybrid_mcmc (finetune.cpp:563-646). */
@@ -722,7 +860,7 @@ void hybrid_mcmc(ora_bm* bm, const ora_config* cfg, uint64_t seed, uint32_t step
     const ora_graph* g = bm->g;
     if (bm->B == 1) return;
     std::vector<double> deltas;
-    const double initial = mdl_canonical(bm);
+    const double initial = mdl_for(bm, cfg);
     bm->entropy = initial;
     double last = initial;
     std::vector<int32_t> hdv0, ldv0, hdv, ldv;
@@ -747,13 +885,13 @@ void hybrid_mcmc(ora_bm* bm, const ora_config* cfg, uint64_t seed, uint32_t step
             const int64_t end = std::min(nlow, (batch + 1) * batch_size);
             gibbs_batch(bm, ldv.data() + start, end - start, seed, (uint32_t)it, step, cfg, nullptr, nullptr, st);
         }
-        const double e = mdl_canonical(bm);
+        const double e = mdl_for(bm, cfg);
         deltas.push_back(e - last);
         last = e;
         if (st) st->mcmc_iterations++;
         if (early_stop(it, golden, initial, deltas)) break;
     }
-    bm->entropy = mdl_canonical(bm);
+    bm->entropy = mdl_for(bm, cfg);
 }
 
 /* finetune::metropolis_hastings (finetune.cpp:773-820). */
@@ -762,7 +900,7 @@ void metropolis_hastings(ora_bm* bm, const ora_config* cfg, uint64_t seed, uint3
     const ora_graph* g = bm->g;
     if (bm->B == 1) return;
     std::vector<double> deltas;
-    bm->entropy = mdl_canonical(bm);
+    bm->entropy = mdl_for(bm, cfg);
     std::vector<int32_t> base(g->N), order;
     for (int64_t v = 0; v < g->N; ++v) base[v] = (int32_t)v;
     for (int it = 0; it < cfg->max_iterations; ++it) {
@@ -781,7 +919,7 @@ void metropolis_hastings(ora_bm* bm, const ora_config* cfg, uint64_t seed, uint3
         if (st) st->mcmc_iterations++;
         if (early_stop(it, golden, bm->entropy, deltas)) break;
     }
-    bm->entropy = mdl_canonical(bm);
+    bm->entropy = mdl_for(bm, cfg);
 }
 
 /* Blockmodel::build_mapping (blockmodel.cpp:34-46) + relabel. */
@@ -810,6 +948,7 @@ void merge_block(ora_bm* bm, int64_t from, int64_t to, const DeltaMap& d) {
     bm->dtot[to] = bm->dout[to] + bm->din[to] - self;
     bm->sizes[to] += bm->sizes[from];
     bm->sizes[from] = 0;
+    bm->nonempty--;  // blockmodel.cpp:356, also when `from` was empty
 }
 
 int64_t uf_find(std::vector<int64_t>& parent, int64_t x) {
@@ -827,7 +966,7 @@ int64_t uf_find(std::vector<int64_t>& parent, int64_t x) {
  * ordered by (delta entropy, block); the reference's std::priority_queue leaves ties in
  * an implementation-defined order. */
 int carry_out_advanced(ora_bm* bm, const std::vector<double>& dS, const std::vector<int64_t>& best,
-                       int64_t num_to_merge, ora_stats* st) {
+                       int64_t num_to_merge, bool nonparametric, ora_stats* st) {
     std::set<std::pair<double, int64_t>> queue;
     std::vector<int64_t> prop(best);
     for (int64_t i = 0; i < (int64_t)dS.size(); ++i) queue.insert({dS[i], i});
@@ -841,7 +980,9 @@ int carry_out_advanced(ora_bm* bm, const std::vector<double>& dS, const std::vec
         const int64_t to = uf_find(parent, prop[from]);
         if (from == to) continue;
         const DeltaMap d = merge_delta(bm, from, to);
-        const double actual = (double)merge_delta_mdl_generic<int64_t>(bm, from, to, d, ce_fixed) * kInvFix;
+        const double actual = (double)(nonparametric ? np_merge_dS(bm, from, to, d)
+                                                     : merge_delta_mdl_generic<int64_t>(bm, from, to, d, ce_fixed)) *
+                              kInvFix;
         if (!queue.empty() && actual > queue.begin()->first) {
             queue.insert({actual, from});
             continue;
@@ -900,7 +1041,8 @@ int merge_blocks(ora_bm* bm, const ora_config* cfg, uint64_t seed, uint32_t step
             const int64_t s = propose_merge(bm, r, w);
             double dS = DBL_MAX;
             if (!past.count(s)) {
-                dS = (double)merge_dS_fixed(bm, r, s) * kInvFix;
+                dS = (double)(cfg->nonparametric ? np_merge_dS(bm, r, s, merge_delta(bm, r, s))
+                                                 : merge_dS_fixed(bm, r, s)) * kInvFix;
                 past.insert(s);
             }
             if (dS < best_dS[r]) {
@@ -911,7 +1053,7 @@ int merge_blocks(ora_bm* bm, const ora_config* cfg, uint64_t seed, uint32_t step
     }
     if (st) st->merge_proposals += 10 * B;
     int rc = cfg->approximate ? carry_out_approximate(bm, best_dS, best, num_to_merge, st)
-                              : carry_out_advanced(bm, best_dS, best, num_to_merge, st);
+                              : carry_out_advanced(bm, best_dS, best, num_to_merge, cfg->nonparametric != 0, st);
     if (rc) return rc;
     bm->B = B - num_to_merge;
     int32_t mx = -1;
@@ -1140,6 +1282,39 @@ extern "C" int64_t ora_sbp(const ora_graph* g, const ora_config* cfg, uint64_t s
     delete bm;
     return B;
 }
+
+extern "C" void ora_np_mdl(const ora_bm* bm, double* literal, double* canonical) {
+    if (literal) {
+        double t[4];
+        np_terms_literal(bm, t);
+        *literal = t[0] + (((0.0 + t[1]) + t[2]) + t[3]) * 1.0;  // S + S_dl * BETA_DL (entropy.cpp:751-779)
+    }
+    if (canonical) *canonical = np_mdl_canonical(bm);
+}
+
+extern "C" void ora_np_terms(const ora_bm* bm, double out[4]) { np_terms_literal(bm, out); }
+
+extern "C" void ora_np_delta_mdl(const ora_bm* bm, int64_t v, int64_t s, double* literal, int64_t* fixed) {
+    const DeltaMap d = vertex_delta(bm, v, s);
+    const VertexInfo vi = vinfo(bm->g, v);
+    const int64_t r = bm->asg[v];
+    if (literal) *literal = r == s ? 0.0 : np_dS_literal(bm, r, s, d, vi.kout, vi.kin, 1);
+    if (fixed) *fixed = np_vertex_dS(bm, v, s, d);
+}
+
+extern "C" void ora_np_merge_delta_mdl(const ora_bm* bm, int64_t r, int64_t s, double* literal, int64_t* fixed) {
+    const DeltaMap d = merge_delta(bm, r, s);
+    if (literal) {
+        int64_t kout = 0, kin = 0;
+        for (const auto& e : bm->row[r]) kout += e.second;
+        for (const auto& e : bm->col[r]) kin += e.second;
+        *literal = (r == s || bm->sizes[r] == 0 || bm->sizes[s] == 0) ? 0.0
+                                                                       : np_dS_literal(bm, r, s, d, kout, kin, bm->sizes[r]);
+    }
+    if (fixed) *fixed = np_merge_dS(bm, r, s, d);
+}
+
+extern "C" int64_t ora_bm_nonempty(const ora_bm* bm) { return bm->nonempty; }
 
 extern "C" double ora_null_mdl_v1(double E) {
     const double log_posterior_p = E * log(1.0 / E);

@@ -35,6 +35,7 @@ typedef struct ora_config {
     int32_t approximate;      /* --approximate */
     int32_t asynciterations;  /* --asynciterations */
     int32_t max_iterations;   /* MAX_NUM_ITERATIONS (finetune.hpp:34) = 100 */
+    int32_t nonparametric;    /* --nonparametric: entropy::nonparametric::*, greedy forced off (args.hpp:204-207) */
 } ora_config;
 
 typedef struct ora_stats {
@@ -116,6 +117,20 @@ int ora_merge_blocks(ora_bm* bm, const ora_config* cfg, uint64_t seed, int32_t s
  * returns the number of blocks (<0 on error). */
 int64_t ora_sbp(const ora_graph* g, const ora_config* cfg, uint64_t seed,
                 int32_t* out_assignment, double* out_mdl, ora_stats* stats);
+
+/* entropy::nonparametric::mdl (entropy.cpp:751-779), directed and not degree-corrected.
+ * literal = the reference's double arithmetic; canonical = the value the device computes
+ * (lgamma terms rounded to 2^-24, exact integer sums). */
+void ora_np_mdl(const ora_bm* bm, double* literal, double* canonical);
+/* Its parts in the reference's arithmetic: sparse_entropy (:623-654), get_partition_dl
+ * (:656-667), get_deg_dl_dist (:709-743, 0 without degree correction), get_edges_dl (:745-749). */
+void ora_np_terms(const ora_bm* bm, double out[4]);
+/* entropy::nonparametric::delta_mdl (entropy.cpp:1146-1178) and block_merge_delta_mdl
+ * (:1198-1223); fixed = canonical value in units of 2^-24. */
+void ora_np_delta_mdl(const ora_bm* bm, int64_t vertex, int64_t proposal, double* literal, int64_t* fixed);
+void ora_np_merge_delta_mdl(const ora_bm* bm, int64_t block, int64_t proposal, double* literal, int64_t* fixed);
+/* Blockmodel::num_nonempty_blocks as the oracle tracks it. */
+int64_t ora_bm_nonempty(const ora_bm* bm);
 
 /* entropy::null_mdl_v1 (entropy.cpp:571-585) for a graph with `num_edges` edges. */
 double ora_null_mdl_v1(double num_edges);

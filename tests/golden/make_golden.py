@@ -57,6 +57,9 @@ def main(root):
     null_mdl = float(re.search(r"hand_calculated_mdl = ([0-9.E+e]+);", et).group(1))
     big_E = float(re.search(r"const long E = ([0-9.E+e]+);", et).group(1))
 
+    npt = read(root, "test/nonparametric_entropy_test.cpp")
+    npc = {name: float(val) for name, val in re.findall(r"const double ([A-Z_0-9]+) = ([0-9.]+);", npt)}
+
     out = {
         "source": "vtsynergy/SBP test/toy_example.hpp, test/*_test.cpp",
         "num_vertices": 11,
@@ -75,6 +78,12 @@ def main(root):
         "block_merge": {"block": 0, "proposal": 1, "delta": mdelta, "delta_entries": mdelta_size,
                         "after_assignment": merge_assignment},
         "null_mdl_v1": {"num_edges": big_E, "value": null_mdl},
+        # nonparametric_entropy_test.cpp:19-27 on the toy blockmodel above (not degree-corrected)
+        "nonparametric": {"mdl": npc["SIMPLE_NONPARAMETRIC_ENTROPY"], "sparse_entropy": npc["SIMPLE_SPARSE_ENTROPY"],
+                          "partition_dl": npc["PARTITION_DL"], "edges_dl": npc["EDGES_DL"],
+                          "degree_corrected": {"mdl": npc["NONPARAMETRIC_ENTROPY"],
+                                               "sparse_entropy": npc["SPARSE_ENTROPY"],
+                                               "degree_dl": npc["DEGREE_DL"]}},
     }
     dst = os.path.join(os.path.dirname(os.path.abspath(__file__)), "toy_example.json")
     with open(dst, "w") as f:

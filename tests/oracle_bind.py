@@ -29,6 +29,7 @@ class OraConfig(ctypes.Structure):
         ("approximate", ctypes.c_int32),
         ("asynciterations", ctypes.c_int32),
         ("max_iterations", ctypes.c_int32),
+        ("nonparametric", ctypes.c_int32),
     ]
 
 
@@ -41,9 +42,9 @@ ALGORITHMS = {"async_gibbs": 0, "hybrid_mcmc": 1, "metropolis_hastings": 2}
 
 
 def make_config(algorithm="hybrid_mcmc", batches=1, mh_percent=0.075, greedy=True, ordered=False,
-                approximate=False, asynciterations=2**31 - 1, max_iterations=100):
+                approximate=False, asynciterations=2**31 - 1, max_iterations=100, nonparametric=False):
     return OraConfig(ALGORITHMS[algorithm], batches, mh_percent, int(greedy), int(ordered),
-                     int(approximate), asynciterations, max_iterations)
+                     int(approximate), asynciterations, max_iterations, int(nonparametric))
 
 
 _lib = None
@@ -104,6 +105,12 @@ def lib():
         L.ora_sbp.restype = ctypes.c_int64
         L.ora_sbp.argtypes = [ctypes.c_void_p, ctypes.POINTER(OraConfig), ctypes.c_uint64, i32p, f64p,
                               ctypes.POINTER(OraStats)]
+        L.ora_np_mdl.argtypes = [ctypes.c_void_p, f64p, f64p]
+        L.ora_np_terms.argtypes = [ctypes.c_void_p, f64p]
+        L.ora_np_delta_mdl.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, f64p, i64p]
+        L.ora_np_merge_delta_mdl.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, f64p, i64p]
+        L.ora_bm_nonempty.restype = ctypes.c_int64
+        L.ora_bm_nonempty.argtypes = [ctypes.c_void_p]
         L.ora_null_mdl_v1.restype = ctypes.c_double
         L.ora_null_mdl_v1.argtypes = [ctypes.c_double]
         _lib = L
@@ -185,6 +192,29 @@ class Blockmodel:
         lit, fx = ctypes.c_double(), ctypes.c_int64()
         lib().ora_merge_delta_mdl(self.h, block, proposal, ctypes.byref(lit), ctypes.byref(fx))
         return lit.value, fx.value
+
+    def np_mdl(self):
+        lit, can = ctypes.c_double(), ctypes.c_double()
+        lib().ora_np_mdl(self.h, ctypes.byref(lit), ctypes.byref(can))
+        return lit.value, can.value
+
+    def np_terms(self):
+        out = np.zeros(4, np.float64)
+        lib().ora_np_terms(self.h, _p(out, f64p))
+        return dict(sparse_entropy=out[0], partition_dl=out[1], degree_dl=out[2], edges_dl=out[3])
+
+    def np_delta_mdl(self, vertex, proposal):
+        lit, fx = ctypes.c_double(), ctypes.c_int64()
+        lib().ora_np_delta_mdl(self.h, vertex, proposal, ctypes.byref(lit), ctypes.byref(fx))
+        return lit.value, fx.value
+
+    def np_merge_delta_mdl(self, block, proposal):
+        lit, fx = ctypes.c_double(), ctypes.c_int64()
+        lib().ora_np_merge_delta_mdl(self.h, block, proposal, ctypes.byref(lit), ctypes.byref(fx))
+        return lit.value, fx.value
+
+    def nonempty(self):
+        return int(lib().ora_bm_nonempty(self.h))
 
     def _delta(self, fn, a, b):
         cap = 4096

@@ -200,3 +200,85 @@ def test_oracle_sbp_recovers_planted_blocks(oracle):
     assert B > 1
     assert evaluate.nmi(planted, asg) > 0.6
     assert mdl < oracle.Blockmodel(g, 1, np.zeros(1000, np.int32)).mdl()[0]
+
+
+# ---- nonparametric entropy (entropy::nonparametric, entropy.cpp:617-1225)
+
+def test_np_toy_terms(oracle, golden):
+    # nonparametric_entropy_test.cpp:57-67, :81-85, :95-99, :111-115 on the toy blockmodel
+    _, B = toy(oracle, golden)
+    npg = golden["nonparametric"]
+    t = B.np_terms()
+    assert float_eq(t["sparse_entropy"], npg["sparse_entropy"])
+    assert float_eq(t["partition_dl"], npg["partition_dl"])
+    assert t["degree_dl"] == 0.0
+    assert float_eq(t["edges_dl"], npg["edges_dl"])
+    lit, can = B.np_mdl()
+    assert float_eq(lit, npg["mdl"])
+    assert abs(lit - can) <= 1e-6  # lgamma terms rounded to 2^-24 each
+
+
+def test_np_toy_delta_mdl_equals_mdl_difference(oracle, golden):
+    # nonparametric_entropy_test.cpp:118-133 (vertex 7 to block 0)
+    g, B = toy(oracle, golden)
+    mv = golden["vertex_move"]
+    lit, fx = B.np_delta_mdl(mv["vertex"], mv["proposal"])
+    after = oracle.Blockmodel(g, 3, mv["after_assignment"])
+    assert float_eq(lit, after.np_mdl()[0] - B.np_mdl()[0])
+    assert abs(lit - fx / 2**24) <= 1e-6
+
+
+def test_np_delta_tracks_mdl_on_random_moves(oracle):
+    """Vertex moves and merges, including moves that empty or occupy a block: the canonical
+    delta equals the change of the canonical MDL exactly, and the reference's double
+    arithmetic to within its rounding.  For a vertex with a self-loop the reference's vterm
+    moves the in-degree by its in-edges without the loop (entropy.cpp:826-827, :861-875)
+    while the blockmodel moves it by one more, so there only delta and literal agree."""
+    from sbp_gb300 import dcsbm
+    src, dst, _ = dcsbm.generate(300, 3000, 6, seed=9)
+    loops = set(src[src == dst].tolist())
+    g = oracle.Graph(300, src, dst)
+    rng = np.random.default_rng(4)
+    a = rng.integers(0, 20, 300)
+    a[a == 19] = 18  # block 19 starts empty
+    a[a == 17] = 16
+    a[7] = 17        # block 17 holds one vertex
+    B = oracle.Blockmodel(g, 20, a)
+    assert B.nonempty() == 19
+    base_lit, base_can = B.np_mdl()
+    cases = [(7, 3), (int(np.flatnonzero(a == 2)[0]), 19)] + [
+        (int(rng.integers(300)), int(rng.integers(20))) for _ in range(80)]
+    checked = 0
+    for v, s in cases:
+        if s == a[v]:
+            continue
+        lit, fx = B.np_delta_mdl(v, s)
+        assert abs(lit - fx / 2**24) <= 1e-6
+        if v in loops:
+            continue
+        a2 = a.copy()
+        a2[v] = s
+        after_lit, after_can = oracle.Blockmodel(g, 20, a2).np_mdl()
+        assert fx == round((after_can - base_can) * 2**24), (v, s)
+        assert abs(lit - (after_lit - base_lit)) <= 1e-7 * abs(base_lit)
+        checked += 1
+    assert checked > 40
+    sizes = np.bincount(a, minlength=20)
+    for _ in range(40):
+        r, s = (int(x) for x in rng.choice(20, 2, replace=False))
+        lit, fx = B.np_merge_delta_mdl(r, s)
+        assert abs(lit - fx / 2**24) <= 1e-6
+        if sizes[r] == 0 or sizes[s] == 0:
+            assert fx == 0 and lit == 0.0  # block_merge_delta_mdl returns 0 (entropy.cpp:1203-1204)
+            continue
+        after_can = oracle.Blockmodel(g, 20, np.where(a == r, s, a)).np_mdl()[1]
+        assert fx == round((after_can - base_can) * 2**24), (r, s)
+
+
+def test_np_sbp_recovers_planted_blocks(oracle):
+    from sbp_gb300 import dcsbm, evaluate
+    src, dst, planted = dcsbm.generate(1000, 8000, 11, seed=2)
+    g = oracle.Graph(1000, src, dst)
+    asg, B, mdl, st = oracle.sbp(g, oracle.make_config("hybrid_mcmc", nonparametric=True), seed=1)
+    assert B > 1
+    assert evaluate.nmi(planted, asg) > 0.6
