@@ -86,7 +86,7 @@ struct Args {
     bool ordered = false;
     bool approximate = false;
     int asynciterations = INT_MAX;
-    bool nonparametric = false;
+    bool nonparametric = false;       // entropy::nonparametric, directed, not degree-corrected
     int threads = 1;                  // accepted for compatibility; the device uses every SM
     uint64_t seed = 0;                // seeds the proposal stream
     int max_iterations = 100;         // MAX_NUM_ITERATIONS (include/finetune.hpp:34)
@@ -102,11 +102,11 @@ inline sbpgpu_config to_config(const Args& a) {
     else if (a.algorithm == "hybrid_mcmc") c.algorithm = 1;
     else if (a.algorithm == "metropolis_hastings") c.algorithm = 2;
     else throw std::invalid_argument("unknown algorithm: " + a.algorithm);
-    if (a.nonparametric) throw Error(SBPGPU_EUNSUPPORTED, "nonparametric entropy is not implemented on the device");
     if (a.batches < 1) throw std::invalid_argument("batches must be >= 1");
     c.batches = a.batches;
     c.mh_percent = a.mh_percent;
-    c.greedy = a.greedy ? 1 : 0;
+    c.greedy = a.greedy && !a.nonparametric ? 1 : 0;  // --nonparametric sets greedy off (args.hpp:204-207)
+    c.nonparametric = a.nonparametric ? 1 : 0;
     c.ordered = a.ordered ? 1 : 0;
     c.approximate = a.approximate ? 1 : 0;
     c.asynciterations = a.asynciterations;
@@ -281,8 +281,42 @@ class Blockmodel {
 
 namespace entropy {
 
-/// entropy::mdl (src/entropy.cpp:597-604).
+namespace nonparametric {
+
+/// nonparametric::mdl (src/entropy.cpp:751-779), directed, not degree-corrected.
 inline double mdl(const Blockmodel& blockmodel, const Graph& graph) {
+    double out = 0.0;
+    check(sbpgpu_np_mdl(blockmodel.handle(), &out), graph.context().get());
+    return out;
+}
+
+/// nonparametric::delta_mdl (src/entropy.cpp:1146-1178) for the moves vertices[i] -> proposals[i].
+inline std::vector<double> delta_mdl(const Blockmodel& blockmodel, const std::vector<long>& vertices,
+                                     const std::vector<long>& proposals) {
+    if (vertices.size() != proposals.size()) throw std::invalid_argument("vertices and proposals differ in length");
+    std::vector<int32_t> v(vertices.begin(), vertices.end()), s(proposals.begin(), proposals.end());
+    std::vector<double> out(v.size());
+    check(sbpgpu_np_delta_mdl_batch(blockmodel.handle(), (int64_t)v.size(), v.data(), s.data(), out.data()),
+          blockmodel.graph().context().get());
+    return out;
+}
+
+/// nonparametric::block_merge_delta_mdl (src/entropy.cpp:1198-1223).
+inline std::vector<double> block_merge_delta_mdl(const Blockmodel& blockmodel, const std::vector<long>& blocks,
+                                                 const std::vector<long>& proposals) {
+    if (blocks.size() != proposals.size()) throw std::invalid_argument("blocks and proposals differ in length");
+    std::vector<int32_t> r(blocks.begin(), blocks.end()), s(proposals.begin(), proposals.end());
+    std::vector<double> out(r.size());
+    check(sbpgpu_np_merge_delta_mdl_batch(blockmodel.handle(), (int64_t)r.size(), r.data(), s.data(), out.data()),
+          blockmodel.graph().context().get());
+    return out;
+}
+
+}  // namespace nonparametric
+
+/// entropy::mdl (src/entropy.cpp:597-604): the nonparametric form under args.nonparametric.
+inline double mdl(const Blockmodel& blockmodel, const Graph& graph) {
+    if (args.nonparametric) return nonparametric::mdl(blockmodel, graph);
     double out = 0.0;
     check(sbpgpu_mdl(blockmodel.handle(), &out), graph.context().get());
     return out;

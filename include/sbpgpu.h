@@ -42,6 +42,10 @@ typedef struct sbpgpu_config {
     int32_t approximate;      /* --approximate (default 0) */
     int32_t asynciterations;  /* --asynciterations (default INT32_MAX) */
     int32_t max_iterations;   /* MAX_NUM_ITERATIONS, include/finetune.hpp:34 (default 100) */
+    int32_t nonparametric;    /* --nonparametric (default 0): entropy::nonparametric::* for every delta and
+                                 MDL, directed, without degree correction; acceptance is then non-greedy
+                                 without the Hastings correction (include/args.hpp:204-207,
+                                 src/entropy.cpp:499) whatever `greedy` says */
 } sbpgpu_config;
 
 typedef struct sbpgpu_stats {
@@ -134,6 +138,17 @@ sbpgpu_status sbpgpu_delta_mdl_batch_noalloc(sbpgpu_bm* bm, int64_t n, const int
 /* entropy::block_merge_delta_mdl (src/entropy.cpp:129-182) for n merges block[i] -> proposal[i]. */
 sbpgpu_status sbpgpu_merge_delta_mdl_batch(sbpgpu_bm* bm, int64_t n, const int32_t* block,
                                            const int32_t* proposal, double* out_delta);
+/* entropy::nonparametric (src/entropy.cpp:617-1225), directed, without degree correction:
+ * mdl (:751-779), delta_mdl (:1146-1178) and block_merge_delta_mdl (:1198-1223).  The
+ * lgamma(x + 1) terms are rounded to multiples of 2^-24 and summed exactly, so a delta
+ * equals the difference of the two MDLs it connects up to one rounding of the terms that
+ * depend on the number of non-empty blocks.  The graph's lgamma table is built on the
+ * first call. */
+sbpgpu_status sbpgpu_np_mdl(sbpgpu_bm* bm, double* out);
+sbpgpu_status sbpgpu_np_delta_mdl_batch(sbpgpu_bm* bm, int64_t n, const int32_t* vertex,
+                                        const int32_t* proposal, double* out_delta);
+sbpgpu_status sbpgpu_np_merge_delta_mdl_batch(sbpgpu_bm* bm, int64_t n, const int32_t* block,
+                                              const int32_t* proposal, double* out_delta);
 
 /* ---- finetune ------------------------------------------------------------------ */
 /* common::propose_new_block under the canonical seeded stream (src/common.cpp:138-198):

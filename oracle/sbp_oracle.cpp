@@ -1055,10 +1055,12 @@ int merge_blocks(ora_bm* bm, const ora_config* cfg, uint64_t seed, uint32_t step
     int rc = cfg->approximate ? carry_out_approximate(bm, best_dS, best, num_to_merge, st)
                               : carry_out_advanced(bm, best_dS, best, num_to_merge, cfg->nonparametric != 0, st);
     if (rc) return rc;
+    // blockmodel.num_blocks(num_blocks - num_blocks_to_merge) (block_merge.cpp:115): blocks
+    // that were empty before the pass become empty trailing blocks
     bm->B = B - num_to_merge;
     int32_t mx = -1;
     for (int32_t b : bm->asg) mx = std::max(mx, b);
-    if (mx + 1 != bm->B) return -2;  // fewer merges than requested: inconsistent labels
+    if (mx + 1 > bm->B) return -2;  // fewer merges than requested: inconsistent labels
     build(bm);
     return 0;
 }

@@ -29,6 +29,7 @@ class Config(ctypes.Structure):
         ("approximate", ctypes.c_int32),
         ("asynciterations", ctypes.c_int32),
         ("max_iterations", ctypes.c_int32),
+        ("nonparametric", ctypes.c_int32),
     ]
 
 
@@ -107,6 +108,9 @@ SIGNATURES = {
     "sbpgpu_delta_mdl_batch": (ctypes.c_int, [vp, ctypes.c_int64, i32p, i32p, f64p]),
     "sbpgpu_delta_mdl_batch_noalloc": (ctypes.c_int, [vp, ctypes.c_int64, i32p, i32p, f64p]),
     "sbpgpu_merge_delta_mdl_batch": (ctypes.c_int, [vp, ctypes.c_int64, i32p, i32p, f64p]),
+    "sbpgpu_np_mdl": (ctypes.c_int, [vp, f64p]),
+    "sbpgpu_np_delta_mdl_batch": (ctypes.c_int, [vp, ctypes.c_int64, i32p, i32p, f64p]),
+    "sbpgpu_np_merge_delta_mdl_batch": (ctypes.c_int, [vp, ctypes.c_int64, i32p, i32p, f64p]),
     "sbpgpu_propose_batch": (ctypes.c_int, [vp, ctypes.c_int64, i32p, ctypes.c_uint64, ctypes.c_uint32,
                                             ctypes.c_uint32, ctypes.c_uint32, i32p]),
     "sbpgpu_gibbs_batch": (ctypes.c_int, [vp, ctypes.POINTER(Config), ctypes.c_int64, i32p, ctypes.c_uint64,

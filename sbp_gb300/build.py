@@ -17,8 +17,10 @@ OUT = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libsbpgpu.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
-              "-Xptxas", "-warn-spills"]
+# host code: no floating-point contraction, so host-side entropy tables round the same on
+# x86_64 and aarch64 hosts
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+              "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]
 
 
 def nvcc():

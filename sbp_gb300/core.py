@@ -30,20 +30,20 @@ class Args:
     approximate: bool = False
     asynciterations: int = 2**31 - 1
     threads: int = 1               # accepted for compatibility; the device uses all SMs
-    nonparametric: bool = False
+    nonparametric: bool = False    # entropy::nonparametric (directed, not degree-corrected)
     seed: int = 0                  # seeds the canonical proposal stream
     max_iterations: int = 100      # MAX_NUM_ITERATIONS (include/finetune.hpp:34)
 
     def config(self):
         if self.algorithm not in ALGORITHMS:
             raise ValueError("algorithm must be one of %s" % sorted(ALGORITHMS))
-        if self.nonparametric:
-            raise NotImplementedError("--nonparametric entropy is not implemented on the device")
         if self.batches < 1:
             raise ValueError("batches must be >= 1")
-        return Config(ALGORITHMS[self.algorithm], int(self.batches), float(self.mh_percent), int(bool(self.greedy)),
+        # --nonparametric sets greedy off (include/args.hpp:204-207)
+        greedy = bool(self.greedy) and not self.nonparametric
+        return Config(ALGORITHMS[self.algorithm], int(self.batches), float(self.mh_percent), int(greedy),
                       int(bool(self.ordered)), int(bool(self.approximate)), int(self.asynciterations),
-                      int(self.max_iterations))
+                      int(self.max_iterations), int(bool(self.nonparametric)))
 
 
 class Context:

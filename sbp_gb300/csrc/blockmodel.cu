@@ -9,6 +9,8 @@
 #include <mutex>
 #include <unordered_set>
 
+#include <stdexcept>
+
 #include "kernels.cuh"
 #include "delta.cuh"
 #include "prims.cuh"
@@ -85,8 +87,10 @@ __global__ void k_csc_keys(const int32_t* __restrict__ row_of, const int32_t* __
     }
 }
 
-__global__ void k_degrees(DevBM bm) {
+__global__ void k_degrees(DevBM bm, bool with_cells) {
     for (int32_t b = blockIdx.x * blockDim.x + threadIdx.x; b < bm.B; b += gridDim.x * blockDim.x) {
+        if (bm.sizes[b] > 0) atomicAdd(bm.nonempty, 1);  // blockmodel.cpp:194, :231
+        if (!with_cells) continue;
         const int32_t dout = (int32_t)(cum_before(bm.row_cum, bm.row_off[b + 1]) - cum_before(bm.row_cum, bm.row_off[b]));
         const int32_t din = (int32_t)(cum_before(bm.col_cum, bm.col_off[b + 1]) - cum_before(bm.col_cum, bm.col_off[b]));
         const int32_t dg = csr_get(bm.row_off, bm.row_col, bm.row_cnt, b, b);
@@ -121,6 +125,25 @@ __global__ void k_mdl(DevBM bm, unsigned long long* __restrict__ out) {
     }
 }
 
+__global__ void k_np_mdl(DevGraph g, DevBM bm, unsigned long long* __restrict__ out) {
+    long long acc = 0;
+    const int64_t n = bm.nnz > bm.B ? bm.nnz : bm.B;
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
+        if (j < bm.nnz) acc -= np_lg(g, bm.row_cnt[j]);  // eterm_exact (entropy.hpp:103-113)
+        if (j < bm.B) acc += np_vterm(g, bm.d_out[j], bm.d_in[j], bm.sizes[j]) - np_lg(g, bm.sizes[j]);
+    }
+    acc = warp_sum_ll(acc);
+    __shared__ long long ws[kT / 32];
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        long long t = 0;
+        for (int i = 0; i < kT / 32; ++i) t += ws[i];
+        atomicAdd(out, (unsigned long long)t);
+    }
+}
+
+template <bool kNP>
 __global__ void k_vertex_dS_batch(DevGraph g, DevBM bm, const int32_t* __restrict__ vs, const int32_t* __restrict__ ss,
                                   int64_t n, int log2cap, long long* __restrict__ out) {
     extern __shared__ int32_t sh[];
@@ -132,17 +155,21 @@ __global__ void k_vertex_dS_batch(DevGraph g, DevBM bm, const int32_t* __restric
     for (int64_t i = blockIdx.x; i < n; i += gridDim.x) {
         const int32_t v = vs[i], s = ss[i], r = bm.asg[v];
         long long d = 0;
-        if (s != r) d = vertex_delta_fixed<kT>(g, bm.asg, bm.d_out, bm.d_in, CsrAcc{bm}, v, r, s, hk, hO, hI, log2cap, red);
+        if (s != r)
+            d = vertex_delta_fixed<kT, CsrAcc, kNP>(g, bm.asg, bm.d_out, bm.d_in, CsrAcc{bm}, v, r, s, hk, hO, hI,
+                                                    log2cap, red, bm.sizes, kNP ? *bm.nonempty : 0);
         if (threadIdx.x == 0) out[i] = d;
         __syncthreads();
     }
 }
 
+template <bool kNP>
 __global__ void k_merge_dS_batch(DevGraph g, DevBM bm, const int32_t* __restrict__ rs, const int32_t* __restrict__ ss,
                                  int64_t n, long long* __restrict__ out) {
     __shared__ long long red[32][8];
     for (int64_t i = blockIdx.x; i < n; i += gridDim.x) {
-        const long long d = merge_delta_fixed_csr<kT>(g, bm, rs[i], ss[i], red);
+        const long long d = kNP ? np_merge_delta_csr<kT>(g, bm, rs[i], ss[i], *bm.nonempty, red)
+                                : merge_delta_fixed_csr<kT>(g, bm, rs[i], ss[i], red);
         if (threadIdx.x == 0) out[i] = d;
         __syncthreads();
     }
@@ -222,6 +249,7 @@ void rebuild(const DevGraph& g, DevBM& bm, Work& w, cudaStream_t st) {
     const int nb = ceil_log2((uint64_t)(bm.B > 1 ? bm.B : 2));
     const int64_t E = g.E;
     cudaMemsetAsync(bm.sizes, 0, sizeof(int32_t) * bm.B, st);
+    cudaMemsetAsync(bm.nonempty, 0, sizeof(int32_t), st);
     k_sizes<<<grid_for(g.N), kT, 0, st>>>(bm.asg, g.N, bm.sizes);
     count_launches(1);
     if (E == 0) {
@@ -231,6 +259,8 @@ void rebuild(const DevGraph& g, DevBM& bm, Work& w, cudaStream_t st) {
         cudaMemsetAsync(bm.d_in, 0, sizeof(int32_t) * bm.B, st);
         cudaMemsetAsync(bm.d_tot, 0, sizeof(int32_t) * bm.B, st);
         cudaMemsetAsync(bm.diag, 0, sizeof(int32_t) * bm.B, st);
+        k_degrees<<<grid_for(bm.B), kT, 0, st>>>(bm, false);
+        count_launches(1);
         bm.nnz = 0;
         return;
     }
@@ -255,7 +285,7 @@ void rebuild(const DevGraph& g, DevBM& bm, Work& w, cudaStream_t st) {
                                                    nullptr);
     k_cnt_from_vals<<<grid_for(nnz), kT, 0, st>>>(w.vals, nnz, bm.col_cnt);
     scan_i32(bm.col_cnt, bm.col_cum, nnz, true, nullptr, w.temp, st);
-    k_degrees<<<grid_for(bm.B), kT, 0, st>>>(bm);
+    k_degrees<<<grid_for(bm.B), kT, 0, st>>>(bm, true);
     count_launches(8);
 }
 
@@ -265,21 +295,36 @@ void launch_mdl(const DevGraph& g, const DevBM& bm, Work& w, cudaStream_t st) {
     count_launches(1);
 }
 
+void launch_np_mdl(const DevGraph& g, const DevBM& bm, Work& w, cudaStream_t st) {
+    if (true && (!g.LG || !g.Dm || !g.Dp)) throw std::logic_error("nonparametric tables missing");
+    cudaMemsetAsync(w.d_acc, 0, sizeof(unsigned long long), st);
+    k_np_mdl<<<grid_for(bm.nnz > bm.B ? bm.nnz : bm.B), kT, 0, st>>>(g, bm, w.d_acc);
+    count_launches(1);
+}
+
 void launch_vertex_dS_batch(const DevGraph& g, const DevBM& bm, const int32_t* v, const int32_t* s, int64_t n,
-                            int32_t max_k, long long* out, Work& w, cudaStream_t st) {
+                            int32_t max_k, long long* out, Work& w, cudaStream_t st, bool np) {
     if (n <= 0) return;
+    if (np && (!g.LG || !g.Dm || !g.Dp)) throw std::logic_error("nonparametric tables missing");
     int log2cap = ceil_log2((uint64_t)(2 * (max_k > 16 ? max_k : 16)));
     const size_t smem = (size_t)3 * sizeof(int32_t) << log2cap;
     if (smem > 200 * 1024) return;  // callers check the degree limit first
-    allow_max_dynamic_smem((const void*)k_vertex_dS_batch);
-    k_vertex_dS_batch<<<grid_for(n, 1), kT, smem, st>>>(g, bm, v, s, n, log2cap, out);
+    if (np) {
+        allow_max_dynamic_smem((const void*)k_vertex_dS_batch<true>);
+        k_vertex_dS_batch<true><<<grid_for(n, 1), kT, smem, st>>>(g, bm, v, s, n, log2cap, out);
+    } else {
+        allow_max_dynamic_smem((const void*)k_vertex_dS_batch<false>);
+        k_vertex_dS_batch<false><<<grid_for(n, 1), kT, smem, st>>>(g, bm, v, s, n, log2cap, out);
+    }
     count_launches(1);
 }
 
 void launch_merge_dS_batch(const DevGraph& g, const DevBM& bm, const int32_t* r, const int32_t* s, int64_t n,
-                           long long* out, Work& w, cudaStream_t st) {
+                           long long* out, Work& w, cudaStream_t st, bool np) {
     if (n <= 0) return;
-    k_merge_dS_batch<<<grid_for(n, 1), kT, 0, st>>>(g, bm, r, s, n, out);
+    if (np && (!g.LG || !g.Dm || !g.Dp)) throw std::logic_error("nonparametric tables missing");
+    if (np) k_merge_dS_batch<true><<<grid_for(n, 1), kT, 0, st>>>(g, bm, r, s, n, out);
+    else k_merge_dS_batch<false><<<grid_for(n, 1), kT, 0, st>>>(g, bm, r, s, n, out);
     count_launches(1);
 }
 

@@ -15,6 +15,7 @@
 #include <new>
 #include <stdexcept>
 #include <string>
+#include <thread>
 #include <unordered_map>
 #include <vector>
 
@@ -173,6 +174,7 @@ struct sbpgpu_graph {
     int32_t* d_ldv = nullptr;
     int32_t n_hdv = 0, n_ldv = 0, max_k_hdv = 0;
     int64_t hdv_k_sum = 0;
+    long long np_lg_N = 0;  // lgamma(N + 1) in units of 2^-24 (nonparametric partition term)
     sbpgpu_stats st{};
 };
 
@@ -270,6 +272,65 @@ void alloc_work(sbpgpu_graph* g) {
     w.dense_cap = (int32_t)std::min<int64_t>(N, kDenseGlobalMax);
 }
 
+// fastlbinom (include/entropy.hpp:144-148) with fastlgamma(x) = lgamma((double)x)
+// (include/fastlgamma.hpp:19-27).
+double np_lbinom(int64_t n, int64_t k) {
+    if (n == 0 || k == 0 || k > n) return 0.0;
+    return (std::lgamma((double)(n + 1)) - std::lgamma((double)(k + 1))) - std::lgamma((double)(n - k + 1));
+}
+// get_edges_dl (entropy.cpp:745-749) for a directed graph: NB = B * B.
+double np_edges_dl(int64_t b, int64_t E) { return np_lbinom(b * b + E - 1, E); }
+
+// Runs f(i) for i in [lo, hi) on the host's cores.
+template <class F>
+void parallel_for(int64_t lo, int64_t hi, F f) {
+    const int64_t n = hi - lo;
+    const int64_t nt = std::max<int64_t>(1, std::min<int64_t>(std::thread::hardware_concurrency(), n / 65536));
+    if (nt <= 1) {
+        for (int64_t i = lo; i < hi; ++i) f(i);
+        return;
+    }
+    std::vector<std::thread> ts;
+    for (int64_t t = 0; t < nt; ++t)
+        ts.emplace_back([=] {
+            for (int64_t i = lo + n * t / nt; i < lo + n * (t + 1) / nt; ++i) f(i);
+        });
+    for (auto& t : ts) t.join();
+}
+
+// The nonparametric tables (entropy::nonparametric), built on first use: LG[x] =
+// lgamma(x + 1) in units of 2^-24 over the range of Lq, and the rounded change of
+// lbinom(N - 1, b - 1) + edges_dl(b) (get_delta_partition_dl, entropy.cpp:933-940;
+// get_delta_edges_dl, :1111-1143) when the non-empty block count steps from b to b - 1
+// (Dm) or b + 1 (Dp).
+void ensure_np(sbpgpu_graph* g) {
+    if (g->dg.LG) return;
+    const int64_t n = (int64_t)g->dg.nlq + 1, N = g->N, E = g->E;
+    std::vector<long long> LG(n), Dm(N + 2, 0), Dp(N + 2, 0);
+    parallel_for(0, n, [&](int64_t x) { LG[x] = std::llrint(std::lgamma((double)(x + 1)) * 16777216.0); });
+    auto step = [&](int64_t b, int dB) {
+        const double part = np_lbinom(N - 1, b + dB - 1) - np_lbinom(N - 1, b - 1);
+        const double edges = np_edges_dl(b + dB, E) - np_edges_dl(b, E);
+        return std::llrint((part + edges) * 16777216.0);
+    };
+    parallel_for(1, N + 2, [&](int64_t b) {
+        if (b >= 2) Dm[b] = step(b, -1);
+        if (b <= N) Dp[b] = step(b, +1);
+    });
+    cudaStream_t st = g->ctx->stream;
+    long long* d_LG = dalloc<long long>(g->owned, n);
+    long long* d_Dm = dalloc<long long>(g->owned, N + 2);
+    long long* d_Dp = dalloc<long long>(g->owned, N + 2);
+    CK(cudaMemcpyAsync(d_LG, LG.data(), n * sizeof(long long), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(d_Dm, Dm.data(), (N + 2) * sizeof(long long), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(d_Dp, Dp.data(), (N + 2) * sizeof(long long), cudaMemcpyHostToDevice, st));
+    host_wait(st);
+    g->dg.LG = d_LG;
+    g->dg.Dm = d_Dm;
+    g->dg.Dp = d_Dp;
+    g->np_lg_N = LG[N];
+}
+
 void ensure_split(sbpgpu_graph* g, float mh_percent) {
     if (g->split_mh == mh_percent) return;
     std::vector<int32_t> idx(g->N);
@@ -304,14 +365,29 @@ void do_rebuild(sbpgpu_bm* bm) {
     rebuild(g->dg, bm->d, g->w, g->ctx->stream);
 }
 
-double do_mdl(sbpgpu_bm* bm) {
+// How a configuration scores and accepts vertex moves.
+int accept_mode(const sbpgpu_config& c) { return c.nonparametric ? ACC_NP : c.greedy ? ACC_GREEDY : ACC_HASTINGS; }
+
+double do_mdl(sbpgpu_bm* bm, bool np = false) {
     sbpgpu_graph* g = bm->g;
-    launch_mdl(g->dg, bm->d, g->w, g->ctx->stream);
+    if (np) ensure_np(g);
+    if (np) launch_np_mdl(g->dg, bm->d, g->w, g->ctx->stream);
+    else launch_mdl(g->dg, bm->d, g->w, g->ctx->stream);
     unsigned long long* h_acc = static_cast<unsigned long long*>(host_scratch());
+    int32_t* h_ne = reinterpret_cast<int32_t*>(h_acc + 1);
     CK(cudaMemcpyAsync(h_acc, g->w.d_acc, sizeof(*h_acc), cudaMemcpyDeviceToHost, g->ctx->stream));
+    if (np) CK(cudaMemcpyAsync(h_ne, bm->d.nonempty, sizeof(int32_t), cudaMemcpyDeviceToHost, g->ctx->stream));
     check_flags(g);
     const unsigned long long acc = *h_acc;
     g->ctx->collect();
+    if (np) {
+        // nonparametric::mdl (entropy.cpp:751-779): the table terms, lgamma(N + 1) and
+        // fastlog(N) of get_partition_dl, then the two terms of the non-empty block count
+        const int64_t N = g->N, E = g->E, ne = *h_ne;
+        const long long lqN = (long long)(int32_t)((double)logf((float)N) * 16777216.0);
+        const long long fixed = (long long)acc + g->np_lg_N + lqN;
+        return (double)fixed * (1.0 / 16777216.0) + (np_lbinom(N - 1, ne - 1) + np_edges_dl(ne, E));
+    }
     const long long lpq = (long long)acc;
     const double E = (double)g->E;
     const double B = (double)bm->d.B;
@@ -341,11 +417,12 @@ void harvest_counters(sbpgpu_graph* g) {
 }
 
 void gibbs_batch_dev(sbpgpu_bm* bm, const int32_t* list, int32_t n, uint64_t seed, uint32_t it, uint32_t step,
-                     int greedy) {
+                     int mode) {
     sbpgpu_graph* g = bm->g;
+    if (mode == ACC_NP) ensure_np(g);
     {
         Span sp(g->ctx, 0);
-        gibbs_propose(g->dg, bm->d, list, n, g->max_k, seed, it, step, greedy, g->w, g->ctx->stream);
+        gibbs_propose(g->dg, bm->d, list, n, g->max_k, seed, it, step, mode, g->w, g->ctx->stream);
     }
     gibbs_apply(bm->d, list, n, g->w, g->ctx->stream);
     g->st.proposals += n;
@@ -375,17 +452,18 @@ void ensure_cells(sbpgpu_graph* g, uint64_t need) {
 }
 
 void chain_run(sbpgpu_bm* bm, const int32_t* order, int32_t n, int32_t max_k, int64_t k_sum, uint64_t seed,
-               uint32_t it, uint32_t step, int greedy) {
+               uint32_t it, uint32_t step, int mode) {
     sbpgpu_graph* g = bm->g;
+    if (mode == ACC_NP) ensure_np(g);
     const int64_t B = bm->d.B;
     if (B > kWinSharedMax) ensure_cells(g, mh_window_cells((int32_t)B));
     WindowPlan plan{};
     if (mh_window_plan(bm->d.B, max_k, g->w, &plan)) {
         Span sp(g->ctx, 1);
-        mh_chain_window(g->dg, bm->d, order, n, plan, seed, it, step, greedy, g->w, g->ctx->stream);
-    } else if (!greedy) {
+        mh_chain_window(g->dg, bm->d, order, n, plan, seed, it, step, mode, g->w, g->ctx->stream);
+    } else if (mode != ACC_GREEDY) {
         throw ApiError(SBPGPU_EUNSUPPORTED,
-                       "non-greedy acceptance needs the windowed chain (vertex degree <= 4096 and the dense "
+                       "non-greedy or nonparametric acceptance needs the windowed chain (vertex degree <= 4096 and the dense "
                        "cell budget holding the blockmodel)");
     } else if (bm->d.B <= kDenseMax || bm->d.B <= g->w.dense_cap) {
         if (bm->d.B > kDenseMax && !g->w.dense_M) {
@@ -399,7 +477,7 @@ void chain_run(sbpgpu_bm* bm, const int32_t* order, int32_t n, int32_t max_k, in
             throw ApiError(SBPGPU_EUNSUPPORTED, "sequential MH supports vertices with k <= 4096");
         chain_init(bm->d, g->w, (uint64_t)(2 * k_sum + 4 * (int64_t)n), g->ctx->stream);
         Span sp(g->ctx, 1);
-        mh_chain(g->dg, bm->d, order, n, max_k, seed, it, step, greedy, g->w, g->ctx->stream);
+        mh_chain(g->dg, bm->d, order, n, max_k, seed, it, step, 1, g->w, g->ctx->stream);
     }
     g->st.proposals += n;
     do_rebuild(bm);
@@ -409,7 +487,7 @@ void async_gibbs(sbpgpu_bm* bm, const sbpgpu_config& cfg, uint64_t seed, int32_t
     sbpgpu_graph* g = bm->g;
     if (bm->d.B == 1) return;
     std::vector<double> deltas;
-    const double initial = do_mdl(bm);
+    const double initial = do_mdl(bm, cfg.nonparametric != 0);
     bm->entropy = initial;
     double last = initial;
     const int64_t N = g->N;
@@ -423,9 +501,9 @@ void async_gibbs(sbpgpu_bm* bm, const sbpgpu_config& cfg, uint64_t seed, int32_t
         }
         for (int64_t b = 0; batch_size > 0 && b < N / batch_size; ++b) {
             const int64_t s0 = b * batch_size, s1 = std::min(N, (b + 1) * batch_size);
-            gibbs_batch_dev(bm, list + s0, (int32_t)(s1 - s0), seed, (uint32_t)it, (uint32_t)step, cfg.greedy);
+            gibbs_batch_dev(bm, list + s0, (int32_t)(s1 - s0), seed, (uint32_t)it, (uint32_t)step, accept_mode(cfg));
         }
-        const double e = do_mdl(bm);
+        const double e = do_mdl(bm, cfg.nonparametric != 0);
         harvest_counters(g);
         deltas.push_back(e - last);
         last = e;
@@ -440,7 +518,7 @@ void hybrid_mcmc(sbpgpu_bm* bm, const sbpgpu_config& cfg, uint64_t seed, int32_t
     if (bm->d.B == 1) return;
     ensure_split(g, cfg.mh_percent);
     std::vector<double> deltas;
-    const double initial = do_mdl(bm);
+    const double initial = do_mdl(bm, cfg.nonparametric != 0);
     bm->entropy = initial;
     double last = initial;
     const int64_t nlow = g->n_ldv;
@@ -453,7 +531,7 @@ void hybrid_mcmc(sbpgpu_bm* bm, const sbpgpu_config& cfg, uint64_t seed, int32_t
                         g->ctx->stream);
                 order = g->d_order;
             }
-            chain_run(bm, order, g->n_hdv, g->max_k_hdv, g->hdv_k_sum, seed, (uint32_t)it, (uint32_t)step, cfg.greedy);
+            chain_run(bm, order, g->n_hdv, g->max_k_hdv, g->hdv_k_sum, seed, (uint32_t)it, (uint32_t)step, accept_mode(cfg));
         }
         const int32_t* list = g->d_ldv;
         if (!cfg.ordered && cfg.batches > 1) {
@@ -463,9 +541,9 @@ void hybrid_mcmc(sbpgpu_bm* bm, const sbpgpu_config& cfg, uint64_t seed, int32_t
         }
         for (int64_t b = 0; batch_size > 0 && b < nlow / batch_size; ++b) {
             const int64_t s0 = b * batch_size, s1 = std::min(nlow, (b + 1) * batch_size);
-            gibbs_batch_dev(bm, list + s0, (int32_t)(s1 - s0), seed, (uint32_t)it, (uint32_t)step, cfg.greedy);
+            gibbs_batch_dev(bm, list + s0, (int32_t)(s1 - s0), seed, (uint32_t)it, (uint32_t)step, accept_mode(cfg));
         }
-        const double e = do_mdl(bm);
+        const double e = do_mdl(bm, cfg.nonparametric != 0);
         harvest_counters(g);
         deltas.push_back(e - last);
         last = e;
@@ -479,7 +557,7 @@ void metropolis_hastings(sbpgpu_bm* bm, const sbpgpu_config& cfg, uint64_t seed,
     sbpgpu_graph* g = bm->g;
     if (bm->d.B == 1) return;
     std::vector<double> deltas;
-    bm->entropy = do_mdl(bm);
+    bm->entropy = do_mdl(bm, cfg.nonparametric != 0);
     int64_t ksum = 0;
     for (int64_t v = 0; v < g->N; ++v) ksum += g->kdeg[v];
     for (int it = 0; it < cfg.max_iterations; ++it) {
@@ -489,7 +567,7 @@ void metropolis_hastings(sbpgpu_bm* bm, const sbpgpu_config& cfg, uint64_t seed,
                     g->ctx->stream);
             order = g->d_order;
         }
-        chain_run(bm, order, (int32_t)g->N, g->max_k, ksum, seed, (uint32_t)it, (uint32_t)step, cfg.greedy);
+        chain_run(bm, order, (int32_t)g->N, g->max_k, ksum, seed, (uint32_t)it, (uint32_t)step, accept_mode(cfg));
         CK(cudaMemcpyAsync(g->flags_host, g->w.flags_dev, sizeof(DevFlags), cudaMemcpyDeviceToHost, g->ctx->stream));
         check_flags(g);
         const double dsum = (double)(long long)g->flags_host->counters[7] * (1.0 / 16777216.0);
@@ -498,10 +576,11 @@ void metropolis_hastings(sbpgpu_bm* bm, const sbpgpu_config& cfg, uint64_t seed,
         g->st.mcmc_iterations++;
         if (early_stop(it, golden, bm->entropy, deltas)) break;
     }
-    bm->entropy = do_mdl(bm);
+    bm->entropy = do_mdl(bm, cfg.nonparametric != 0);
 }
 
 void mcmc_impl(sbpgpu_bm* bm, const sbpgpu_config& cfg, uint64_t seed, int32_t step, bool golden) {
+    if (cfg.nonparametric) ensure_np(bm->g);
     if (cfg.algorithm == 0 && step < cfg.asynciterations) async_gibbs(bm, cfg, seed, step, golden);
     else if (cfg.algorithm == 1) hybrid_mcmc(bm, cfg, seed, step, golden);
     else metropolis_hastings(bm, cfg, seed, step, golden);
@@ -514,22 +593,26 @@ void merge_impl(sbpgpu_bm* bm, const sbpgpu_config& cfg, uint64_t seed, int32_t 
     if (num_to_merge >= B) throw ApiError(SBPGPU_EINVAL, "num_blocks_to_merge must be < num_blocks");
     {
         Span sp(g->ctx, 2);
-        merge_propose(g->dg, bm->d, seed, (uint32_t)step, g->w, g->ctx->stream);
+        if (cfg.nonparametric) ensure_np(g);
+        merge_propose(g->dg, bm->d, seed, (uint32_t)step, g->w, g->ctx->stream, cfg.nonparametric != 0);
     }
     if (!cfg.approximate) ensure_cells(g, (uint64_t)B * (uint64_t)B);
     {
         Span sp(g->ctx, 3);
-        carry_out(g->dg, bm->d, num_to_merge, cfg.approximate, g->w, g->ctx->stream);
+        carry_out(g->dg, bm->d, num_to_merge, cfg.approximate, g->w, g->ctx->stream, cfg.nonparametric != 0);
     }
     int32_t sc[3] = {0, 0, 0};
     CK(cudaMemcpyAsync(sc, g->w.d_scalar, sizeof(sc), cudaMemcpyDeviceToHost, g->ctx->stream));
     harvest_counters(g);
-    if (sc[1] != num_to_merge || sc[2] != B - num_to_merge)
+    // build_mapping numbers the blocks that still hold vertices densely and the blockmodel
+    // keeps B - num_to_merge blocks (block_merge.cpp:109-115), so blocks that were empty
+    // before the pass end up as empty trailing blocks
+    if (sc[1] != num_to_merge || sc[2] > B - num_to_merge)
         throw ApiError(SBPGPU_EDEVICE, "merge pass carried out " + std::to_string(sc[1]) + " of " +
                                            std::to_string(num_to_merge) + " merges (" + std::to_string(sc[2]) +
                                            " blocks left)");
     g->st.merges += sc[1];
-    bm->d.B = sc[2];
+    bm->d.B = (int32_t)(B - num_to_merge);
     do_rebuild(bm);
 }
 
@@ -565,10 +648,12 @@ void upload_graph(sbpgpu_graph* g, const int32_t* src, const int32_t* dst) {
         g->kdeg[v] = outd + (inns_off[v + 1] - inns_off[v]);
         g->max_k = std::max(g->max_k, g->kdeg[v]);
     }
-    // fastlog table (fastlog.hpp:21-30): logf((float)x) is a multiple of 2^-24 for x >= 1.
-    std::vector<int32_t> Lq(E + 2);
+    // fastlog table (fastlog.hpp:21-30): logf((float)x) is a multiple of 2^-24 for x >= 1;
+    // up to max(E, N) + 1 so that block sizes index it too (nonparametric vterm)
+    const int64_t nlq = std::max(E, N) + 2;
+    std::vector<int32_t> Lq(nlq);
     Lq[0] = 0;
-    for (int64_t x = 1; x < E + 2; ++x) Lq[x] = (int32_t)((double)logf((float)x) * 16777216.0);
+    for (int64_t x = 1; x < nlq; ++x) Lq[x] = (int32_t)((double)logf((float)x) * 16777216.0);
     cudaStream_t st = g->ctx->stream;
     auto& o = g->owned;
     int32_t* d_out_off = dalloc<int32_t>(o, N + 1);
@@ -577,7 +662,7 @@ void upload_graph(sbpgpu_graph* g, const int32_t* src, const int32_t* dst) {
     int32_t* d_inns_nbr = dalloc<int32_t>(o, inns_nbr.size());
     int32_t* d_self = dalloc<int32_t>(o, N);
     int32_t* d_esrc = dalloc<int32_t>(o, E);
-    int32_t* d_Lq = dalloc<int32_t>(o, E + 2);
+    int32_t* d_Lq = dalloc<int32_t>(o, nlq);
     CK(cudaMemcpyAsync(d_out_off, out_off.data(), (N + 1) * 4, cudaMemcpyHostToDevice, st));
     if (E) CK(cudaMemcpyAsync(d_out_nbr, out_nbr.data(), E * 4, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(d_inns_off, inns_off.data(), (N + 1) * 4, cudaMemcpyHostToDevice, st));
@@ -585,8 +670,9 @@ void upload_graph(sbpgpu_graph* g, const int32_t* src, const int32_t* dst) {
         CK(cudaMemcpyAsync(d_inns_nbr, inns_nbr.data(), inns_nbr.size() * 4, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(d_self, selfcnt.data(), N * 4, cudaMemcpyHostToDevice, st));
     if (E) CK(cudaMemcpyAsync(d_esrc, esrc.data(), E * 4, cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(d_Lq, Lq.data(), (E + 2) * 4, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(d_Lq, Lq.data(), nlq * 4, cudaMemcpyHostToDevice, st));
     g->dg = DevGraph{(int32_t)N, (int32_t)E, d_out_off, d_out_nbr, d_inns_off, d_inns_nbr, d_self, d_esrc, d_Lq};
+    g->dg.nlq = (int32_t)(nlq - 1);
     alloc_work(g);
     std::vector<int32_t> iota(N);
     for (int64_t v = 0; v < N; ++v) iota[v] = (int32_t)v;
@@ -621,6 +707,7 @@ sbpgpu_bm* new_bm(sbpgpu_graph* g, int64_t B) {
     d.col_row = dalloc<int32_t>(o, E);
     d.col_cnt = dalloc<int32_t>(o, E);
     d.col_cum = dalloc<int32_t>(o, E);
+    d.nonempty = dalloc<int32_t>(o, 1);
     return bm;
 }
 
@@ -655,6 +742,75 @@ void release_graph(sbpgpu_graph* g) {
     release_ctx(ctx);
 }
 
+sbpgpu_status delta_batch_impl(sbpgpu_bm* bm, int64_t n, const int32_t* vertex, const int32_t* proposal, double* out,
+                               bool np) {
+    if (!bm || n < 0 || (n && (!vertex || !proposal || !out))) return SBPGPU_EINVAL;
+    sbpgpu_graph* g = bm->g;
+    return guarded(g->ctx, [&] {
+        if (n == 0) return SBPGPU_OK;
+        int32_t max_k = 0;
+        for (int64_t i = 0; i < n; ++i) {
+            if (vertex[i] < 0 || vertex[i] >= g->N || proposal[i] < 0 || proposal[i] >= bm->d.B)
+                throw ApiError(SBPGPU_EINVAL, "vertex or proposal out of range");
+            max_k = std::max(max_k, g->kdeg[vertex[i]]);
+        }
+        if (max_k > 8192) throw ApiError(SBPGPU_EUNSUPPORTED, "vertex degree above 8192");
+        if (np) ensure_np(g);
+        std::vector<void*> tmp;
+        int32_t* dv = dalloc<int32_t>(tmp, n);
+        int32_t* ds = dalloc<int32_t>(tmp, n);
+        long long* dout = dalloc<long long>(tmp, n);
+        cudaStream_t st = g->ctx->stream;
+        std::vector<long long> h(n);
+        try {
+            CK(cudaMemcpyAsync(dv, vertex, n * 4, cudaMemcpyHostToDevice, st));
+            CK(cudaMemcpyAsync(ds, proposal, n * 4, cudaMemcpyHostToDevice, st));
+            launch_vertex_dS_batch(g->dg, bm->d, dv, ds, n, max_k, dout, g->w, st, np);
+            CK(cudaMemcpyAsync(h.data(), dout, n * 8, cudaMemcpyDeviceToHost, st));
+            check_flags(g);
+        } catch (...) {
+            free_all(tmp, g->ctx->stream);
+            throw;
+        }
+        free_all(tmp, g->ctx->stream);
+        for (int64_t i = 0; i < n; ++i) out[i] = (double)h[i] * (1.0 / 16777216.0);
+        return SBPGPU_OK;
+    });
+}
+
+sbpgpu_status merge_delta_batch_impl(sbpgpu_bm* bm, int64_t n, const int32_t* block, const int32_t* proposal,
+                                     double* out, bool np) {
+    if (!bm || n < 0 || (n && (!block || !proposal || !out))) return SBPGPU_EINVAL;
+    sbpgpu_graph* g = bm->g;
+    return guarded(g->ctx, [&] {
+        if (n == 0) return SBPGPU_OK;
+        for (int64_t i = 0; i < n; ++i)
+            if (block[i] < 0 || block[i] >= bm->d.B || proposal[i] < 0 || proposal[i] >= bm->d.B ||
+                block[i] == proposal[i])
+                throw ApiError(SBPGPU_EINVAL, "block or proposal out of range");
+        if (np) ensure_np(g);
+        std::vector<void*> tmp;
+        int32_t* dr = dalloc<int32_t>(tmp, n);
+        int32_t* ds = dalloc<int32_t>(tmp, n);
+        long long* dout = dalloc<long long>(tmp, n);
+        cudaStream_t st = g->ctx->stream;
+        std::vector<long long> h(n);
+        try {
+            CK(cudaMemcpyAsync(dr, block, n * 4, cudaMemcpyHostToDevice, st));
+            CK(cudaMemcpyAsync(ds, proposal, n * 4, cudaMemcpyHostToDevice, st));
+            launch_merge_dS_batch(g->dg, bm->d, dr, ds, n, dout, g->w, st, np);
+            CK(cudaMemcpyAsync(h.data(), dout, n * 8, cudaMemcpyDeviceToHost, st));
+            check_flags(g);
+        } catch (...) {
+            free_all(tmp, g->ctx->stream);
+            throw;
+        }
+        free_all(tmp, g->ctx->stream);
+        for (int64_t i = 0; i < n; ++i) out[i] = (double)h[i] * (1.0 / 16777216.0);
+        return SBPGPU_OK;
+    });
+}
+
 }  // namespace
 
 // ====================================================================== C ABI
@@ -669,6 +825,7 @@ void sbpgpu_default_config(sbpgpu_config* cfg) {
     cfg->approximate = 0;
     cfg->asynciterations = INT32_MAX;
     cfg->max_iterations = 100;
+    cfg->nonparametric = 0;
 }
 
 sbpgpu_status sbpgpu_ctx_create(int32_t device, sbpgpu_ctx** out) {
@@ -951,6 +1108,7 @@ sbpgpu_status sbpgpu_bm_copy(const sbpgpu_bm* src, sbpgpu_bm** out) {
                             std::make_pair(b.col_row, a.col_row), std::make_pair(b.col_cnt, a.col_cnt),
                             std::make_pair(b.col_cum, a.col_cum)})
                 CK(cudaMemcpyAsync(pr.first, pr.second, nnz * 4, cudaMemcpyDeviceToDevice, st));
+        CK(cudaMemcpyAsync(b.nonempty, a.nonempty, 4, cudaMemcpyDeviceToDevice, st));
         b.nnz = a.nnz;
         bm->entropy = src->entropy;
         bm->num_blocks_to_merge = 0;  // Blockmodel::copy (blockmodel.cpp:151)
@@ -1019,40 +1177,34 @@ sbpgpu_status sbpgpu_mdl(sbpgpu_bm* bm, double* out) {
     });
 }
 
-sbpgpu_status sbpgpu_delta_mdl_batch(sbpgpu_bm* bm, int64_t n, const int32_t* vertex, const int32_t* proposal,
-                                     double* out) {
-    if (!bm || n < 0 || (n && (!vertex || !proposal || !out))) return SBPGPU_EINVAL;
-    sbpgpu_graph* g = bm->g;
-    return guarded(g->ctx, [&] {
-        if (n == 0) return SBPGPU_OK;
-        int32_t max_k = 0;
-        for (int64_t i = 0; i < n; ++i) {
-            if (vertex[i] < 0 || vertex[i] >= g->N || proposal[i] < 0 || proposal[i] >= bm->d.B)
-                throw ApiError(SBPGPU_EINVAL, "vertex or proposal out of range");
-            max_k = std::max(max_k, g->kdeg[vertex[i]]);
-        }
-        if (max_k > 8192) throw ApiError(SBPGPU_EUNSUPPORTED, "vertex degree above 8192");
-        std::vector<void*> tmp;
-        int32_t* dv = dalloc<int32_t>(tmp, n);
-        int32_t* ds = dalloc<int32_t>(tmp, n);
-        long long* dout = dalloc<long long>(tmp, n);
-        cudaStream_t st = g->ctx->stream;
-        std::vector<long long> h(n);
-        try {
-            CK(cudaMemcpyAsync(dv, vertex, n * 4, cudaMemcpyHostToDevice, st));
-            CK(cudaMemcpyAsync(ds, proposal, n * 4, cudaMemcpyHostToDevice, st));
-            launch_vertex_dS_batch(g->dg, bm->d, dv, ds, n, max_k, dout, g->w, st);
-            CK(cudaMemcpyAsync(h.data(), dout, n * 8, cudaMemcpyDeviceToHost, st));
-            check_flags(g);
-        } catch (...) {
-            free_all(tmp, g->ctx->stream);
-            throw;
-        }
-        free_all(tmp, g->ctx->stream);
-        for (int64_t i = 0; i < n; ++i) out[i] = (double)h[i] * (1.0 / 16777216.0);
+sbpgpu_status sbpgpu_np_mdl(sbpgpu_bm* bm, double* out) {
+    if (!bm || !out) return SBPGPU_EINVAL;
+    return guarded(bm->g->ctx, [&] {
+        *out = do_mdl(bm, true);
         return SBPGPU_OK;
     });
 }
+
+sbpgpu_status sbpgpu_delta_mdl_batch(sbpgpu_bm* bm, int64_t n, const int32_t* vertex, const int32_t* proposal,
+                                     double* out) {
+    return delta_batch_impl(bm, n, vertex, proposal, out, false);
+}
+
+sbpgpu_status sbpgpu_np_delta_mdl_batch(sbpgpu_bm* bm, int64_t n, const int32_t* vertex, const int32_t* proposal,
+                                        double* out) {
+    return delta_batch_impl(bm, n, vertex, proposal, out, true);
+}
+
+sbpgpu_status sbpgpu_merge_delta_mdl_batch(sbpgpu_bm* bm, int64_t n, const int32_t* block, const int32_t* proposal,
+                                           double* out) {
+    return merge_delta_batch_impl(bm, n, block, proposal, out, false);
+}
+
+sbpgpu_status sbpgpu_np_merge_delta_mdl_batch(sbpgpu_bm* bm, int64_t n, const int32_t* block,
+                                              const int32_t* proposal, double* out) {
+    return merge_delta_batch_impl(bm, n, block, proposal, out, true);
+}
+
 
 sbpgpu_status sbpgpu_delta_mdl_batch_noalloc(sbpgpu_bm* bm, int64_t n, const int32_t* vertex,
                                              const int32_t* proposal, double* out) {
@@ -1084,37 +1236,6 @@ sbpgpu_status sbpgpu_delta_mdl_batch_noalloc(sbpgpu_bm* bm, int64_t n, const int
     });
 }
 
-sbpgpu_status sbpgpu_merge_delta_mdl_batch(sbpgpu_bm* bm, int64_t n, const int32_t* block, const int32_t* proposal,
-                                           double* out) {
-    if (!bm || n < 0 || (n && (!block || !proposal || !out))) return SBPGPU_EINVAL;
-    sbpgpu_graph* g = bm->g;
-    return guarded(g->ctx, [&] {
-        if (n == 0) return SBPGPU_OK;
-        for (int64_t i = 0; i < n; ++i)
-            if (block[i] < 0 || block[i] >= bm->d.B || proposal[i] < 0 || proposal[i] >= bm->d.B ||
-                block[i] == proposal[i])
-                throw ApiError(SBPGPU_EINVAL, "block or proposal out of range");
-        std::vector<void*> tmp;
-        int32_t* dr = dalloc<int32_t>(tmp, n);
-        int32_t* ds = dalloc<int32_t>(tmp, n);
-        long long* dout = dalloc<long long>(tmp, n);
-        cudaStream_t st = g->ctx->stream;
-        std::vector<long long> h(n);
-        try {
-            CK(cudaMemcpyAsync(dr, block, n * 4, cudaMemcpyHostToDevice, st));
-            CK(cudaMemcpyAsync(ds, proposal, n * 4, cudaMemcpyHostToDevice, st));
-            launch_merge_dS_batch(g->dg, bm->d, dr, ds, n, dout, g->w, st);
-            CK(cudaMemcpyAsync(h.data(), dout, n * 8, cudaMemcpyDeviceToHost, st));
-            check_flags(g);
-        } catch (...) {
-            free_all(tmp, g->ctx->stream);
-            throw;
-        }
-        free_all(tmp, g->ctx->stream);
-        for (int64_t i = 0; i < n; ++i) out[i] = (double)h[i] * (1.0 / 16777216.0);
-        return SBPGPU_OK;
-    });
-}
 
 sbpgpu_status sbpgpu_propose_batch(sbpgpu_bm* bm, int64_t n, const int32_t* vertex, uint64_t seed, uint32_t c1,
                                    uint32_t c2, uint32_t c3, int32_t* out) {
@@ -1155,7 +1276,7 @@ sbpgpu_status sbpgpu_gibbs_batch(sbpgpu_bm* bm, const sbpgpu_config* cfg, int64_
         cudaStream_t st = g->ctx->stream;
         CK(cudaMemcpyAsync(g->w.list_tmp, vertex, n * 4, cudaMemcpyHostToDevice, st));
         reset_counters(g);
-        gibbs_batch_dev(bm, g->w.list_tmp, (int32_t)n, seed, iteration, step, cfg->greedy);
+        gibbs_batch_dev(bm, g->w.list_tmp, (int32_t)n, seed, iteration, step, accept_mode(*cfg));
         if (out_moves) {
             std::vector<int32_t> mv(g->N);
             CK(cudaMemcpyAsync(mv.data(), g->w.moves, g->N * 4, cudaMemcpyDeviceToHost, st));
@@ -1186,7 +1307,7 @@ sbpgpu_status sbpgpu_mh_chain(sbpgpu_bm* bm, const sbpgpu_config* cfg, int64_t n
         cudaStream_t st = g->ctx->stream;
         CK(cudaMemcpyAsync(g->w.list_tmp, vertex, n * 4, cudaMemcpyHostToDevice, st));
         reset_counters(g);
-        chain_run(bm, g->w.list_tmp, (int32_t)n, max_k, ksum, seed, iteration, step, cfg->greedy);
+        chain_run(bm, g->w.list_tmp, (int32_t)n, max_k, ksum, seed, iteration, step, accept_mode(*cfg));
         CK(cudaMemcpyAsync(g->flags_host, g->w.flags_dev, sizeof(DevFlags), cudaMemcpyDeviceToHost, st));
         check_flags(g);
         if (applied) *applied = (int64_t)g->flags_host->counters[5];

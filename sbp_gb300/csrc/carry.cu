@@ -26,6 +26,12 @@
 //
 // Deltas are handled as exact int64 multiples of 2^-24 (the reference's doubles compare
 // the same way), which keeps the single-thread queue logic off the slow FP64 pipe.
+//
+// Nonparametric entropy (kNP): every merge lowers the number of non-empty blocks by one
+// (blockmodel.cpp:356), which changes the partition and edge-count terms of every later
+// merge by the same amount.  An evaluation therefore leaves that term out and the replay
+// adds it for the count at the moment of the pop, so evaluations stay exact across the
+// round's merges; a put-back entry popped again is re-scored the same way.
 // Queue: the proposals sorted by (delta, block) (P, read through a cursor), put-back
 // entries in a sorted shared-memory buffer (S) that spills into a sorted global run (R)
 // through a parallel merge.  Each block is in the queue at most once.
@@ -38,8 +44,11 @@
 #include <cfloat>
 #include <climits>
 
+#include <stdexcept>
+
 #include "chain.cuh"
 #include "kernels.cuh"
+#include "np.cuh"
 
 namespace sbp {
 
@@ -143,7 +152,9 @@ __device__ __forceinline__ int32_t uf_find(int32_t* parent, int32_t x) {
 // the cells of row s that do not receive anything, the change of their d_out factor
 // collapse into (d_out[s] - M[s][s] - M[s][r] - sum over moved c of M[s][c]) times the
 // log-degree difference; columns likewise.
-template <class Cells>
+// kNP: nonparametric::block_merge_delta_mdl (src/entropy.cpp:1198-1223) without its
+// non-empty-count term; both blocks are non-empty (the caller checks).
+template <class Cells, bool kNP>
 __device__ long long merge_delta_part(const DevGraph& g, const DevBM& bm, const DevChain& ch, const Cells& cells,
                                       int32_t r, int32_t s, int t, int nt, bool leader, uint32_t* bloom,
                                       unsigned long long& keys_seen) {
@@ -157,6 +168,11 @@ __device__ long long merge_delta_part(const DevGraph& g, const DevBM& bm, const 
     auto term = [&](int32_t key, bool is_row, int32_t m, int32_t o, int32_t deg) {
         if (m == 0 || (!is_row && key == r)) return;
         bloom_add(bloom, key);
+        if constexpr (kNP) {  // the cell empties; a third block's cell adds into row / column s
+            acc += np_lg(g, m);
+            if (is_row ? (key != r && key != s) : (key != s)) acc += np_cell(g, o, m);
+            return;
+        }
         const int32_t own = is_row ? dout_r : din_r;
         acc += ce_fixed(Lq, m, deg, own);
         if (is_row ? (key != r && key != s) : (key != s)) {
@@ -201,7 +217,12 @@ __device__ long long merge_delta_part(const DevGraph& g, const DevBM& bm, const 
     chunks_for_each(rhead, ch, t, nt, [&](int32_t c) { item(c, true); });
     chunks_for_each(chead, ch, t, nt, [&](int32_t x) { item(x, false); });
     acc = warp_sum_ll(acc);
-    if (leader) {
+    if (leader && kNP) {
+        const int32_t Mrr = cells.get(r, r), Mrs = cells.get(r, s), Msr = cells.get(s, r), Mss = cells.get(s, s);
+        acc += np_cell(g, Mss, Mrr + Mrs + Msr);
+        acc += np_block_terms(g, dout_r, din_r, bm.sizes[r], dout_s, din_s, bm.sizes[s], dout_r, din_r, bm.sizes[r], 0,
+                              false);
+    } else if (leader) {
         const int32_t Mrr = cells.get(r, r), Mrs = cells.get(r, s), Msr = cells.get(s, r), Mss = cells.get(s, s);
         const int32_t dss = Mrr + Mrs + Msr;
         if (dss > 0) acc += ce_fixed(Lq, Mss, din_s, dout_s) - ce_fixed(Lq, Mss + dss, din_s2, dout_s2);
@@ -231,6 +252,8 @@ struct CarryShared {
     int32_t c_keys[kMaxW];
     uint32_t conf[kMaxW];    // bit i of conf[j]: a merge of candidate i would change j's value
     long long c_act[kMaxW];  // recomputed delta of candidate i
+    int32_t c_count[kMaxW];  // kNP: the candidate's delta takes the non-empty-count term
+    int32_t ne;              // kNP: current number of non-empty blocks
     int32_t nm, np;
     long long b_dS;
     int32_t b_blk;
@@ -241,7 +264,7 @@ struct CarryShared {
 };
 
 // W = kCarryWarps / team_warps entries per round; team_warps in {1, 2, 4, 8}.
-template <class Cells>
+template <class Cells, bool kNP>
 __global__ void __launch_bounds__(kCarryThreads, 1) k_carry_out(
     DevGraph g, DevBM bm, DevChain ch, Cells cells, const uint64_t* __restrict__ pkeys,
     const int32_t* __restrict__ pblk, int32_t nP, const int32_t* __restrict__ best, long long* r0_dS, int32_t* r0_blk,
@@ -259,6 +282,7 @@ __global__ void __launch_bounds__(kCarryThreads, 1) k_carry_out(
         sh.ssel = 0;
         sh.merged = 0;
         sh.rounds = 0;
+        sh.ne = kNP ? *bm.nonempty : 0;
     }
     const long long max_rounds = 64ll * (nP + 1) + 4096;
     unsigned long long keys_seen = 0, evals = 0;  // this thread's share of the work counters
@@ -334,11 +358,14 @@ __global__ void __launch_bounds__(kCarryThreads, 1) k_carry_out(
                 }
                 to = __shfl_sync(SBP_FULL_MASK, to, 0);
                 long long part = 0;
-                if (to != from) {
+                // nonparametric: zero when either block is empty (entropy.cpp:1203-1204)
+                const bool counted = !kNP || (to != from && bm.sizes[from] != 0 && bm.sizes[to] != 0);
+                if (lane == 0 && warp % team_warps == 0) sh.c_count[team] = kNP && counted;
+                if (to != from && counted) {
                     const int nt = 32 * team_warps, t = tid - team * nt;
                     const unsigned long long before = keys_seen;
-                    part = merge_delta_part(g, bm, ch, cells, from, to, t, nt, (warp % team_warps) == 0,
-                                            sh.bloom[team], keys_seen);
+                    part = merge_delta_part<Cells, kNP>(g, bm, ch, cells, from, to, t, nt, (warp % team_warps) == 0,
+                                                        sh.bloom[team], keys_seen);
                     const int kc = warp_sum_i((int)(keys_seen - before));
                     if (lane == 0) atomicAdd(&sh.c_keys[team], kc);
                     if (lane == 0 && warp % team_warps == 0) ++evals;
@@ -389,15 +416,15 @@ __global__ void __launch_bounds__(kCarryThreads, 1) k_carry_out(
                 }
                 if (pick < 0) break;                                      // queue empty
                 if (hb && qless(sh.b_dS, sh.b_blk, bd, bb)) break;        // next pop not evaluated
+                int ci;
+                int32_t from, to;
                 if (pick == 1) {
                     // popped again: if no merge since touched what it read, its recomputed
-                    // delta is the one it was put back with, the smallest entry, so it merges
-                    if (dirty(sh.q_cand[0])) break;
-                    sh.m_from[nm] = sh.q_blk[0];
-                    sh.m_to[nm] = sh.q_to[0];
-                    sh.m_keys[nm] = sh.c_keys[sh.q_cand[0]];
-                    merged_mask |= 1u << sh.q_cand[0];
-                    ++nm;
+                    // delta is the one it was put back with (kNP: up to the count term)
+                    ci = sh.q_cand[0];
+                    if (dirty(ci)) break;
+                    from = sh.q_blk[0];
+                    to = sh.q_to[0];
                     for (int k = 1; k < nq; ++k) {
                         sh.q_dS[k - 1] = sh.q_dS[k];
                         sh.q_blk[k - 1] = sh.q_blk[k];
@@ -405,14 +432,19 @@ __global__ void __launch_bounds__(kCarryThreads, 1) k_carry_out(
                         sh.q_cand[k - 1] = sh.q_cand[k];
                     }
                     --nq;
-                    continue;
+                } else {
+                    if (dirty(i)) break;  // its value is stale: re-evaluate it next round
+                    from = sh.c_blk[i];
+                    to = sh.c_to[i];
+                    ++cons[sh.c_src[i]];
+                    ci = i++;
+                    if (to == from) continue;  // already in the same block
                 }
-                if (dirty(i)) break;  // its value is stale: re-evaluate it next round
-                const int32_t from = sh.c_blk[i], to = sh.c_to[i];
-                ++cons[sh.c_src[i]];
-                const int ci = i++;
-                if (to == from) continue;  // already in the same block
-                const long long act = sh.c_act[ci];
+                long long act = sh.c_act[ci];
+                if (kNP && sh.c_count[ci]) {
+                    const int32_t b = min(max(sh.ne - nm, 0), g.N + 1);
+                    act += __ldg(g.Dm + b);
+                }
                 if (i < ncand || nq > 0 || hb) {
                     long long top = hb ? sh.b_dS : LLONG_MAX;
                     if (i < ncand) top = min(top, sh.c_dS[i]);
@@ -444,6 +476,7 @@ __global__ void __launch_bounds__(kCarryThreads, 1) k_carry_out(
             sh.cS = cons[2];
             sh.nq = nq;
             sh.nm = nm;
+            sh.ne -= nm;  // every merge lowers the count (blockmodel.cpp:356)
             sh.rounds += 1;
         }
         __syncthreads();
@@ -629,7 +662,18 @@ __global__ void k_dense_cells_fill(DevBM bm, int32_t* M) {
 
 }  // namespace
 
-void carry_out_exact(const DevGraph& g, DevBM& bm, int64_t num_to_merge, Work& w, cudaStream_t st) {
+template <class Cells>
+void launch_carry(bool np, const DevGraph& g, DevBM& bm, const Cells& cells, int64_t num_to_merge, int team_warps,
+                  int32_t* d_merged, Work& w, cudaStream_t st) {
+    auto k = np ? k_carry_out<Cells, true> : k_carry_out<Cells, false>;
+    k<<<1, kCarryThreads, 0, st>>>(g, bm, w.chain, cells, w.keys, w.vals, bm.B, w.best,
+                                   reinterpret_cast<long long*>(w.heap_dS), w.heap_blk,
+                                   reinterpret_cast<long long*>(w.keys_alt), w.vals_alt, w.parent, num_to_merge,
+                                   team_warps, w.list_small, w.list_big, 2 * g.N, d_merged, w.flags_dev);
+}
+
+void carry_out_exact(const DevGraph& g, DevBM& bm, int64_t num_to_merge, Work& w, cudaStream_t st, bool np) {
+    if (np && (!g.LG || !g.Dm || !g.Dp)) throw std::logic_error("nonparametric tables missing");
     const int32_t B = bm.B;
     const bool dense = w.cells && (uint64_t)B * (uint64_t)B <= w.cells_elems;
     // team size from the mean number of row + column keys per block
@@ -641,17 +685,11 @@ void carry_out_exact(const DevGraph& g, DevBM& bm, int64_t num_to_merge, Work& w
         cudaMemsetAsync(w.cells, 0, sizeof(int32_t) * (size_t)B * (size_t)B, st);
         const int64_t blocks = std::min<int64_t>((bm.nnz + 255) / 256 + 1, 152 * 16);
         k_dense_cells_fill<<<(unsigned)blocks, 256, 0, st>>>(bm, w.cells);
-        k_carry_out<DenseCells><<<1, kCarryThreads, 0, st>>>(
-            g, bm, w.chain, DenseCells{w.cells, (int64_t)B}, w.keys, w.vals, B, w.best, reinterpret_cast<long long*>(w.heap_dS), w.heap_blk,
-            reinterpret_cast<long long*>(w.keys_alt), w.vals_alt, w.parent, num_to_merge, team_warps, w.list_small,
-            w.list_big, 2 * g.N, d_merged, w.flags_dev);
+        launch_carry(np, g, bm, DenseCells{w.cells, (int64_t)B}, num_to_merge, team_warps, d_merged, w, st);
         count_launches(2);
     } else {
         chain_init(bm, w, (uint64_t)2 * (uint64_t)bm.nnz, st);
-        k_carry_out<HashCells><<<1, kCarryThreads, 0, st>>>(
-            g, bm, w.chain, HashCells{w.chain}, w.keys, w.vals, B, w.best, reinterpret_cast<long long*>(w.heap_dS), w.heap_blk,
-            reinterpret_cast<long long*>(w.keys_alt), w.vals_alt, w.parent, num_to_merge, team_warps, w.list_small,
-            w.list_big, 2 * g.N, d_merged, w.flags_dev);
+        launch_carry(np, g, bm, HashCells{w.chain}, num_to_merge, team_warps, d_merged, w, st);
         count_launches(1);
     }
 }

@@ -17,11 +17,18 @@
 // then applied together (every update is an addition, so their order does not matter).
 // The result equals the one-vertex-at-a-time chain exactly.
 //
+// Nonparametric entropy (kNP): a delta also reads the sizes of r and s (covered by T(v))
+// and, when the move would empty r or fill s, the number of non-empty blocks; an accepted
+// move that changes that number therefore also ends the round before every later entry
+// whose delta read it.
+//
 // Cell counts: B x B dense in shared memory (B <= kWinSharedMax) or dense M and its
 // transpose in global memory (leading dimension a multiple of 4); degrees and sizes in
 // shared memory unless B is large.  Each warp's neighbour hash lives in shared memory (up
 // to 512 slots) or, for vertices of degree above 256, in a per-warp global region.  Only
 // the assignment is written back; the caller rebuilds afterwards.
+#include <stdexcept>
+
 #include "delta.cuh"
 #include "kernels.cuh"
 
@@ -67,6 +74,7 @@ struct GlobalCells {
 struct WinResult {
     long long dS;
     int32_t v, r, s, nb, status, k, kout, kin, L, l2;  // l2: log2 of this vertex's hash size
+    int32_t dB;  // kNP: change of the number of non-empty blocks if the move is applied
 };
 
 // log2 of the neighbour-hash size for a vertex of degree k (at least twice k slots).
@@ -266,11 +274,13 @@ __device__ __forceinline__ int32_t warp_gather(const DevGraph& g, const int32_t*
 // entropy::delta_mdl for moving v from r to s over the gathered neighbour blocks; the same
 // terms as vertex_delta_fixed (exact int64, units of 2^-24), with the occupied hash slots
 // compacted into items[] and every cell of a pass loaded before it is used.
-template <class Cells>
+// kNP: nonparametric::delta_mdl (src/entropy.cpp:1146-1178) with block sizes `size` and
+// `nonempty` non-empty blocks.
+template <class Cells, bool kNP>
 __device__ long long warp_delta(const DevGraph& g, const int32_t* d_out, const int32_t* d_in, const Cells& M,
                                 int32_t r, int32_t s, int32_t kout, int32_t kin, int32_t L, const int32_t* hk,
                                 const int32_t* hO, const int32_t* hI, int log2cap, int32_t* items,
-                                const int32_t* lq_cache) {
+                                const int32_t* lq_cache, const int32_t* size, int32_t nonempty) {
     const int lane = threadIdx.x & 31;
     const int cap = 1 << log2cap;
     const LogTabCached Lq{g.Lq, g.E + 1, lq_cache, kLqCache};
@@ -320,6 +330,11 @@ __device__ long long warp_delta(const DevGraph& g, const int32_t* d_out, const i
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
             if (b[q] < 0) continue;
+            if constexpr (kNP) {
+                if (O[q] > 0) acc += np_cell(g, Mrb[q], -O[q]) + np_cell(g, Msb[q], O[q]);
+                if (I[q] > 0) acc += np_cell(g, Mbr[q], -I[q]) + np_cell(g, Mbs[q], I[q]);
+                continue;
+            }
             if (O[q] > 0) {
                 const int32_t dinb = d_in[b[q]];
                 acc += ce_fixed(Lq, Mrb[q], dinb, dout_r) - ce_fixed(Lq, Mrb[q] - O[q], dinb, dout_r2);
@@ -343,6 +358,11 @@ __device__ long long warp_delta(const DevGraph& g, const int32_t* d_out, const i
     sSi = warp_sum_ll(sSi);
     const int32_t Mrr = M.row_get(r, r), Mrs = M.row_get(r, s), Msr = M.row_get(s, r), Mss = M.row_get(s, s);
     long long tot = acc;
+    if constexpr (kNP) {
+        tot += np_cell(g, Mrr, -Or - Ir - L) + np_cell(g, Mrs, Ir - Os) + np_cell(g, Msr, Or - Is) +
+               np_cell(g, Mss, Os + Is + L);
+        return tot + np_block_terms(g, dout_r, din_r, size[r], dout_s, din_s, size[s], kout, kin, 1, nonempty);
+    }
     {
         const int32_t d = -Or - Ir - L;
         if (Or | Ir | L) tot += ce_fixed(Lq, Mrr, din_r, dout_r) - ce_fixed(Lq, Mrr + d, din_r2, dout_r2);
@@ -380,7 +400,7 @@ __device__ __forceinline__ bool in_touched(const WinResult& c, const int32_t* hk
 
 // kMode 0: cells, degrees and sizes in shared memory; 1: cells dense in global memory,
 // degrees and sizes in shared memory; 2: all of them in global memory (large B).
-template <int kMode>
+template <int kMode, bool kNP>
 __global__ void __launch_bounds__(kWinMaxWarps * 32, 1)
     k_mh_window(DevGraph g, DevBM bm, const int32_t* __restrict__ order, int32_t n, uint64_t seed, uint32_t iter,
                 uint32_t step, GlobalCells gc, int32_t ld, int log2cap, int nwarps, bool greedy, int32_t* ghash,
@@ -401,13 +421,14 @@ __global__ void __launch_bounds__(kWinMaxWarps * 32, 1)
         return l2 <= kSmemHashL2 ? hash + (4 << kSmemHashL2) * w : ghash + ((int64_t)4 << kGlobalHashL2) * w;
     };
     __shared__ WinResult res[kWinMaxWarps];
-    __shared__ int32_t s_consumed, s_acc_mask;
+    __shared__ int32_t s_consumed, s_acc_mask, s_ne;
     __shared__ uint32_t s_conf[kWinMaxWarps];
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const int nt = nwarps * 32;
     (void)cap;
 
     for (int i = tid; i < kLqCache; i += nt) lq[i] = __ldg(g.Lq + min(i, g.E + 1));
+    if (tid == 0) s_ne = kNP ? *bm.nonempty : 0;
     if (kShared) {
         for (int i = tid; i < B * ld; i += nt) M[i] = 0;
         __syncthreads();
@@ -437,6 +458,7 @@ __global__ void __launch_bounds__(kWinMaxWarps * 32, 1)
             c.s = -1;
             c.nb = -1;
             c.dS = 0;
+            c.dB = 0;
             const int32_t o0 = __ldg(g.out_off + c.v), o1 = __ldg(g.out_off + c.v + 1);
             const int32_t i0 = __ldg(g.inns_off + c.v), i1 = __ldg(g.inns_off + c.v + 1);
             c.kout = o1 - o0;
@@ -484,10 +506,13 @@ __global__ void __launch_bounds__(kWinMaxWarps * 32, 1)
                     c.status = ST_NOMOVE;
                 } else {
                     c.s = s;
-                    c.dS = kShared ? warp_delta(g, dout, din, sc, c.r, s, c.kout, c.kin, c.L, hk, hO, hI, c.l2, items, lq)
-                                   : warp_delta(g, dout, din, gc, c.r, s, c.kout, c.kin, c.L, hk, hO, hI, c.l2, items, lq);
+                    if constexpr (kNP) c.dB = np_count_change(size[c.r], size[s], 1);
+                    c.dS = kShared ? warp_delta<SharedCells, kNP>(g, dout, din, sc, c.r, s, c.kout, c.kin, c.L, hk, hO,
+                                                                  hI, c.l2, items, lq, size, s_ne)
+                                   : warp_delta<GlobalCells, kNP>(g, dout, din, gc, c.r, s, c.kout, c.kin, c.L, hk, hO,
+                                                                  hI, c.l2, items, lq, size, s_ne);
                     double H = 1.0;
-                    if (!greedy && c.k > 0) {  // entropy::hastings_correction (entropy.cpp:497-561)
+                    if (!kNP && !greedy && c.k > 0) {  // entropy::hastings_correction (entropy.cpp:497-561)
                         H = kShared ? hastings_fixed<32>(sc, [&](int32_t b) { return dout[b] + din[b] - sc.row_get(b, b); },
                                                          dout, din, B, c.r, s, c.kout, c.kin, c.L, hk, hO, hI, c.l2,
                                                          nullptr)
@@ -496,7 +521,7 @@ __global__ void __launch_bounds__(kWinMaxWarps * 32, 1)
                                                          nullptr);
                     }
                     // finetune::accept (finetune.cpp:22-32)
-                    c.status = accept_move(c.dS, H, greedy, w[3]) ? ST_ACCEPT : ST_REJECT;
+                    c.status = accept_move(c.dS, H, greedy && !kNP, w[3]) ? ST_ACCEPT : ST_REJECT;
                 }
             }
             if (lane == 0) res[wid] = c;
@@ -512,7 +537,8 @@ __global__ void __launch_bounds__(kWinMaxWarps * 32, 1)
                 const WinResult& cu = res[u];
                 const int32_t* hj = hash_of(j, cj.l2);
                 if (in_touched(cj, hj, cu.r) || in_touched(cj, hj, cu.s) ||
-                    (cj.nb >= 0 && in_touched(cu, hash_of(u, cu.l2), cj.nb)))
+                    (cj.nb >= 0 && in_touched(cu, hash_of(u, cu.l2), cj.nb)) ||
+                    (kNP && cu.dB != 0 && cj.dB != 0 && cj.status >= ST_REJECT))
                     atomicOr(&s_conf[j], 1u << u);
             }
         }
@@ -529,6 +555,7 @@ __global__ void __launch_bounds__(kWinMaxWarps * 32, 1)
                     acc_mask |= 1 << j;
                     moved++;
                     dsum += cj.dS;
+                    s_ne += cj.dB;  // blockmodel.cpp:429-430
                 }
             }
             s_consumed = consumed;
@@ -648,14 +675,24 @@ bool mh_window_plan(int32_t B, int32_t max_k, const Work& w, WindowPlan* p) {
     return nw >= 2;
 }
 
+template <int kMode>
+void launch_window(bool np, const DevGraph& g, DevBM& bm, const int32_t* order, int32_t n, const WindowPlan& p,
+                   uint64_t seed, uint32_t iter, uint32_t step, bool greedy, const GlobalCells& gc, size_t smem,
+                   Work& w, cudaStream_t st) {
+    auto k = np ? k_mh_window<kMode, true> : k_mh_window<kMode, false>;
+    allow_max_dynamic_smem((const void*)k);
+    k<<<1, 32 * p.nw, smem, st>>>(g, bm, order, n, seed, iter, step, gc, (int32_t)p.ld, p.log2cap, p.nw, greedy,
+                                  w.win_hash, w.flags_dev);
+}
+
 void mh_chain_window(const DevGraph& g, DevBM& bm, const int32_t* order, int32_t n, const WindowPlan& p,
-                     uint64_t seed, uint32_t iter, uint32_t step, int greedy, Work& w, cudaStream_t st) {
+                     uint64_t seed, uint32_t iter, uint32_t step, int mode, Work& w, cudaStream_t st) {
     if (n <= 0) return;
+    if (mode == ACC_NP && (!g.LG || !g.Dm || !g.Dp)) throw std::logic_error("nonparametric tables missing");
     const size_t smem = window_smem(bm.B, p.mode, p.log2cap, p.nw);
+    const bool np = mode == ACC_NP, greedy = mode == ACC_GREEDY;
     if (p.mode == 0) {
-        allow_max_dynamic_smem((const void*)k_mh_window<0>);
-        k_mh_window<0><<<1, 32 * p.nw, smem, st>>>(g, bm, order, n, seed, iter, step, GlobalCells{}, (int32_t)p.ld,
-                                                   p.log2cap, p.nw, greedy != 0, w.win_hash, w.flags_dev);
+        launch_window<0>(np, g, bm, order, n, p, seed, iter, step, greedy, GlobalCells{}, smem, w, st);
         count_launches(1);
         return;
     }
@@ -672,15 +709,8 @@ void mh_chain_window(const DevGraph& g, DevBM& bm, const int32_t* order, int32_t
     if (blocks < 1) blocks = 1;
     if (blocks > 152 * 16) blocks = 152 * 16;
     k_window_fill<<<(unsigned)blocks, 256, 0, st>>>(bm, gc);
-    if (p.mode == 1) {
-        allow_max_dynamic_smem((const void*)k_mh_window<1>);
-        k_mh_window<1><<<1, 32 * p.nw, smem, st>>>(g, bm, order, n, seed, iter, step, gc, (int32_t)p.ld, p.log2cap,
-                                                   p.nw, greedy != 0, w.win_hash, w.flags_dev);
-    } else {
-        allow_max_dynamic_smem((const void*)k_mh_window<2>);
-        k_mh_window<2><<<1, 32 * p.nw, smem, st>>>(g, bm, order, n, seed, iter, step, gc, (int32_t)p.ld, p.log2cap,
-                                                   p.nw, greedy != 0, w.win_hash, w.flags_dev);
-    }
+    if (p.mode == 1) launch_window<1>(np, g, bm, order, n, p, seed, iter, step, greedy, gc, smem, w, st);
+    else launch_window<2>(np, g, bm, order, n, p, seed, iter, step, greedy, gc, smem, w, st);
     count_launches(2);
 }
 

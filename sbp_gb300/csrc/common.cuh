@@ -3,7 +3,9 @@
 // Data layout in HBM (all int32 unless noted; E < 2^31 so every count fits):
 //   graph   : out CSR (out_off[N+1], out_nbr[E]), in CSR without self-loops
 //             (inns_off[N+1], inns_nbr[E-L]), selfcnt[N], edge source esrc[E]
-//             (the vertex owning each out-CSR slot), Lq[E+2] = logf((float)x) * 2^24.
+//             (the vertex owning each out-CSR slot), Lq[max(E,N)+2] = logf((float)x) * 2^24;
+//             for the nonparametric entropy LG[max(E,N)+2] = lgamma(x+1) * 2^24 (int64) and
+//             the non-empty-block-count steps Dm, Dp [N+2] (int64), built on first use.
 //   blockmodel: asg[N]; d_out, d_in, d_tot, sizes, diag[B];
 //             blockmatrix as sorted CSR (row_off[B+1], row_col/row_cnt/row_cum[nnz])
 //             and sorted CSC (col_off[B+1], col_row/col_cnt/col_cum[nnz]); row_of[nnz].
@@ -49,6 +51,10 @@ struct DevGraph {
     const int32_t* selfcnt;
     const int32_t* esrc;
     const int32_t* Lq;
+    const long long* LG;  // nonparametric tables (null until first used)
+    const long long* Dm;
+    const long long* Dp;
+    int32_t nlq;          // last index of Lq and LG
 };
 
 struct DevBM {
@@ -69,6 +75,7 @@ struct DevBM {
     int32_t* col_row;
     int32_t* col_cnt;
     int32_t* col_cum;
+    int32_t* nonempty;  // device scalar: blocks with at least one vertex (recounted by rebuild)
 };
 
 // Mutable cell store used by the sequential phases (MH chain, merge carry-out): an
@@ -97,6 +104,12 @@ struct DevFlags {
 };
 
 constexpr unsigned long long kEmptyKey = ~0ull;
+
+// How proposals are scored and accepted (finetune::accept, reference src/finetune.cpp:22-32):
+// greedy (dS < 0); Metropolis-Hastings with the Hastings correction; or the nonparametric
+// entropy, which the reference always runs non-greedy and without the correction
+// (include/args.hpp:204-207, src/entropy.cpp:499).
+enum : int { ACC_GREEDY = 0, ACC_HASTINGS = 1, ACC_NP = 2 };
 
 // ------------------------------------------------------------------ Philox4x32-10
 __device__ __forceinline__ void philox4x32_10(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3,

@@ -17,6 +17,7 @@
 #pragma once
 
 #include "common.cuh"
+#include "np.cuh"
 
 namespace sbp {
 
@@ -167,10 +168,13 @@ struct VertexScalars {
 
 // Accumulates the touched-cell terms of moving v from r to s and returns the exact
 // delta-MDL in units of 2^-24.  hk/hO/hI: group hash of 2^log2cap slots (>= 2k).
-template <int kThreads, typename Acc>
+// kNP: nonparametric::delta_mdl (reference src/entropy.cpp:1146-1178) instead, which reads
+// the block sizes and the number of non-empty blocks as well.
+template <int kThreads, typename Acc, bool kNP = false>
 __device__ long long vertex_delta_fixed(const DevGraph& g, const int32_t* asg, const int32_t* d_out,
                                         const int32_t* d_in, const Acc& M, int32_t v, int32_t r, int32_t s,
-                                        int32_t* hk, int32_t* hO, int32_t* hI, int log2cap, long long (*red)[8]) {
+                                        int32_t* hk, int32_t* hO, int32_t* hI, int log2cap, long long (*red)[8],
+                                        const int32_t* sizes = nullptr, int32_t nonempty = 0) {
     typedef Group<kThreads> G;
     const int t = G::rank();
     const int cap = 1 << log2cap;
@@ -206,6 +210,11 @@ __device__ long long vertex_delta_fixed(const DevGraph& g, const int32_t* asg, c
             spec += ((long long)O << 16) | (long long)I;
             continue;
         }
+        if constexpr (kNP) {  // entries_dS: only the cells that change
+            if (O > 0) acc += np_cell(g, M.row_get(r, b), -O) + np_cell(g, M.row_get(s, b), O);
+            if (I > 0) acc += np_cell(g, M.col_get(r, b), -I) + np_cell(g, M.col_get(s, b), I);
+            continue;
+        }
         if (O > 0) {
             const int32_t Mrb = M.row_get(r, b), Msb = M.row_get(s, b), dinb = d_in[b];
             acc += ce_fixed(Lq, Mrb, dinb, dout_r) - ce_fixed(Lq, Mrb - O, dinb, dout_r2);
@@ -236,6 +245,11 @@ __device__ long long vertex_delta_fixed(const DevGraph& g, const int32_t* asg, c
     const int32_t Os = (int32_t)((spec >> 16) & 0xffff), Is = (int32_t)(spec & 0xffff);
     const int32_t Mrr = M.row_get(r, r), Mrs = M.row_get(r, s), Msr = M.row_get(s, r), Mss = M.row_get(s, s);
     long long tot = acc;
+    if constexpr (kNP) {
+        tot += np_cell(g, Mrr, -Or - Ir - L) + np_cell(g, Mrs, Ir - Os) + np_cell(g, Msr, Or - Is) +
+               np_cell(g, Mss, Os + Is + L);
+        return tot + np_block_terms(g, dout_r, din_r, sizes[r], dout_s, din_s, sizes[s], kout, kin, 1, nonempty);
+    }
     {   // (r, r): present iff a neighbour lies in r or a self-loop exists; its change is never zero.
         const int32_t d = -Or - Ir - L;
         if (Or | Ir | L) tot += ce_fixed(Lq, Mrr, din_r, dout_r) - ce_fixed(Lq, Mrr + d, din_r2, dout_r2);
@@ -457,6 +471,46 @@ __device__ long long merge_delta_fixed_csr(const DevGraph& g, const DevBM& bm, i
     tot += ((long long)dout_s - Msr - Mss - sRow) * (Lx(Lq, dout_s2) - Lx(Lq, dout_s));
     tot += ((long long)din_s - Mrs - Mss - sCol) * (Lx(Lq, din_s2) - Lx(Lq, din_s));
     return tot;
+}
+
+// nonparametric::block_merge_delta_mdl (reference src/entropy.cpp:1198-1223) for merging r
+// into s over the static CSR/CSC: every cell of row and column r empties, row / column
+// cells of third blocks add into row / column s, and (r,r), (r,s), (s,r) into (s,s).  Zero
+// when either block is empty (:1203-1204).
+template <int kThreads>
+__device__ long long np_merge_delta_csr(const DevGraph& g, const DevBM& bm, int32_t r, int32_t s, int32_t nonempty,
+                                        long long (*red)[8]) {
+    typedef Group<kThreads> G;
+    const int t = G::rank();
+    const int32_t size_r = bm.sizes[r], size_s = bm.sizes[s];
+    if (r == s || size_r == 0 || size_s == 0) return 0;
+    long long acc = 0;
+    const int32_t ro0 = bm.row_off[r], ro1 = bm.row_off[r + 1];
+    for (int32_t j = ro0 + t; j < ro1; j += kThreads) {
+        const int32_t c = bm.row_col[j], m = bm.row_cnt[j];
+        acc += np_lg(g, m);
+        if (c != r && c != s) acc += np_cell(g, csr_get(bm.row_off, bm.row_col, bm.row_cnt, s, c), m);
+    }
+    const int32_t co0 = bm.col_off[r], co1 = bm.col_off[r + 1];
+    for (int32_t j = co0 + t; j < co1; j += kThreads) {
+        const int32_t x = bm.col_row[j], m = bm.col_cnt[j];
+        if (x == r) continue;
+        acc += np_lg(g, m);
+        if (x != s) acc += np_cell(g, csr_get(bm.col_off, bm.col_row, bm.col_cnt, s, x), m);
+    }
+    {
+        long long v[1] = {acc};
+        G::template sum<1>(v, red);
+        acc = v[0];
+    }
+    const int32_t Mrr = csr_get(bm.row_off, bm.row_col, bm.row_cnt, r, r);
+    const int32_t Mrs = csr_get(bm.row_off, bm.row_col, bm.row_cnt, r, s);
+    const int32_t Msr = csr_get(bm.row_off, bm.row_col, bm.row_cnt, s, r);
+    const int32_t Mss = csr_get(bm.row_off, bm.row_col, bm.row_cnt, s, s);
+    acc += np_cell(g, Mss, Mrr + Mrs + Msr);
+    const int32_t dout_r = bm.d_out[r], din_r = bm.d_in[r];
+    return acc + np_block_terms(g, dout_r, din_r, size_r, bm.d_out[s], bm.d_in[s], size_s, dout_r, din_r, size_r,
+                                nonempty);
 }
 
 }  // namespace sbp

@@ -70,10 +70,14 @@ int ceil_log2(uint64_t x);
 void rebuild(const DevGraph& g, DevBM& bm, Work& w, cudaStream_t st);
 // Sum of v * canonical_log(v / (d_out * d_in)) in units of 2^-24 into w.d_acc[0].
 void launch_mdl(const DevGraph& g, const DevBM& bm, Work& w, cudaStream_t st);
+// The table terms of nonparametric::mdl (entropy.cpp:751-779) in units of 2^-24 into
+// w.d_acc[0]: -sum LG[cell] + sum over blocks (vterm - LG[size]).
+void launch_np_mdl(const DevGraph& g, const DevBM& bm, Work& w, cudaStream_t st);
+// np: nonparametric deltas (the graph's nonparametric tables must exist).
 void launch_vertex_dS_batch(const DevGraph& g, const DevBM& bm, const int32_t* v, const int32_t* s, int64_t n,
-                            int32_t max_k, long long* out, Work& w, cudaStream_t st);
+                            int32_t max_k, long long* out, Work& w, cudaStream_t st, bool np = false);
 void launch_merge_dS_batch(const DevGraph& g, const DevBM& bm, const int32_t* r, const int32_t* s, int64_t n,
-                           long long* out, Work& w, cudaStream_t st);
+                           long long* out, Work& w, cudaStream_t st, bool np = false);
 void launch_propose_batch(const DevGraph& g, const DevBM& bm, const int32_t* v, int64_t n, uint64_t seed,
                           uint32_t c1, uint32_t c2, uint32_t c3, int32_t* out, cudaStream_t st);
 // Initialises the chain cell store from the current CSR (capacity for extra new keys).
@@ -84,8 +88,9 @@ void lists_init(const DevBM& bm, Work& w, cudaStream_t st);
 // ---- sweep.cu
 // Proposals for vlist[0..n) against the current snapshot (moves[v] = s or -1), then the
 // vertex-id-order apply with the block-size-1 rule; asg updated (no rebuild).
+// mode: ACC_GREEDY, ACC_HASTINGS or ACC_NP.
 void gibbs_propose(const DevGraph& g, const DevBM& bm, const int32_t* vlist, int32_t n, int32_t small_k,
-                   uint64_t seed, uint32_t iter, uint32_t step, int greedy, Work& w, cudaStream_t st);
+                   uint64_t seed, uint32_t iter, uint32_t step, int mode, Work& w, cudaStream_t st);
 void gibbs_apply(const DevBM& bm, const int32_t* vlist, int32_t n, Work& w, cudaStream_t st);
 void mh_chain(const DevGraph& g, DevBM& bm, const int32_t* order, int32_t n, int32_t max_k, uint64_t seed,
               uint32_t iter, uint32_t step, int greedy, Work& w, cudaStream_t st);
@@ -110,22 +115,25 @@ uint64_t mh_window_cells(int32_t B);
 // no dense buffer holds the matrices).
 bool mh_window_plan(int32_t B, int32_t max_k, const Work& w, WindowPlan* p);
 void mh_chain_window(const DevGraph& g, DevBM& bm, const int32_t* order, int32_t n, const WindowPlan& p,
-                     uint64_t seed, uint32_t iter, uint32_t step, int greedy, Work& w, cudaStream_t st);
+                     uint64_t seed, uint32_t iter, uint32_t step, int mode, Work& w, cudaStream_t st);
 // order[i] = base[perm(i)] with the canonical shuffle keyed by (i, iter, step, dom).
 void shuffle(const int32_t* base, int32_t n, uint64_t seed, uint32_t iter, uint32_t step, uint32_t dom,
              int32_t* order, Work& w, cudaStream_t st);
 
 // ---- merge.cu
-void merge_propose(const DevGraph& g, const DevBM& bm, uint64_t seed, uint32_t step, Work& w, cudaStream_t st);
+// np: score with nonparametric::block_merge_delta_mdl.
+void merge_propose(const DevGraph& g, const DevBM& bm, uint64_t seed, uint32_t step, Work& w, cudaStream_t st,
+                   bool np = false);
 // Carries out merges; writes the number done to w.d_scalar[1].  Leaves asg relabelled
 // to dense block ids (B - merges blocks); the caller rebuilds.
-void carry_out(const DevGraph& g, DevBM& bm, int64_t num_to_merge, int approximate, Work& w, cudaStream_t st);
+void carry_out(const DevGraph& g, DevBM& bm, int64_t num_to_merge, int approximate, Work& w, cudaStream_t st,
+               bool np = false);
 
 // ---- carry.cu
 // carry_out_best_merges_advanced over the queue (w.keys, w.vals) sorted by (delta, block)
 // with the union-find block map in w.parent (identity on entry).  Uses the dense cells
 // w.cells when B * B <= w.cells_elems, the chain hash otherwise.
-void carry_out_exact(const DevGraph& g, DevBM& bm, int64_t num_to_merge, Work& w, cudaStream_t st);
+void carry_out_exact(const DevGraph& g, DevBM& bm, int64_t num_to_merge, Work& w, cudaStream_t st, bool np = false);
 
 // Blocks the calling thread, sleeping rather than spinning, until the work queued on st so
 // far is done (many host threads may each drive a context of their own).

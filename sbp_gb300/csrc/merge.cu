@@ -12,6 +12,8 @@
 #include <cfloat>
 #include <climits>
 
+#include <stdexcept>
+
 #include "chain.cuh"
 #include "delta.cuh"
 #include "kernels.cuh"
@@ -30,11 +32,13 @@ inline unsigned grid_cap(int64_t n, int64_t per, int64_t cap) {
     return (unsigned)b;
 }
 
+template <bool kNP>
 __global__ void __launch_bounds__(256) k_merge_propose(DevGraph g, DevBM bm, uint64_t seed, uint32_t step,
                                                        int32_t* __restrict__ best, double* __restrict__ best_dS,
                                                        DevFlags* flags) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     unsigned long long evaluated = 0;
+    const int32_t nonempty = kNP ? *bm.nonempty : 0;
     for (int32_t r = blockIdx.x * kMergeWarps + wid; r < bm.B; r += gridDim.x * kMergeWarps) {
         long long bestq = LLONG_MAX;
         int32_t bests = -1;
@@ -53,7 +57,8 @@ __global__ void __launch_bounds__(256) k_merge_propose(DevGraph g, DevBM bm, uin
             for (int j = 0; j < np; ++j) dup |= past[j] == s;
             if (dup) continue;
             past[np++] = s;
-            const long long dS = merge_delta_fixed_csr<32>(g, bm, r, s, nullptr);
+            const long long dS = kNP ? np_merge_delta_csr<32>(g, bm, r, s, nonempty, nullptr)
+                                     : merge_delta_fixed_csr<32>(g, bm, r, s, nullptr);
             ++evaluated;
             if (bests < 0 || dS < bestq) {
                 bestq = dS;
@@ -123,13 +128,20 @@ __global__ void k_relabel(int32_t* __restrict__ asg, int32_t N, const int32_t* _
 
 }  // namespace
 
-void merge_propose(const DevGraph& g, const DevBM& bm, uint64_t seed, uint32_t step, Work& w, cudaStream_t st) {
-    k_merge_propose<<<grid_cap(bm.B, kMergeWarps, 152 * 8), 256, 0, st>>>(g, bm, seed, step, w.best, w.best_dS,
-                                                                          w.flags_dev);
+void merge_propose(const DevGraph& g, const DevBM& bm, uint64_t seed, uint32_t step, Work& w, cudaStream_t st,
+                   bool np) {
+    if (np && (!g.LG || !g.Dm || !g.Dp)) throw std::logic_error("nonparametric tables missing");
+    if (np)
+        k_merge_propose<true><<<grid_cap(bm.B, kMergeWarps, 152 * 8), 256, 0, st>>>(g, bm, seed, step, w.best,
+                                                                                    w.best_dS, w.flags_dev);
+    else
+        k_merge_propose<false><<<grid_cap(bm.B, kMergeWarps, 152 * 8), 256, 0, st>>>(g, bm, seed, step, w.best,
+                                                                                     w.best_dS, w.flags_dev);
     count_launches(1);
 }
 
-void carry_out(const DevGraph& g, DevBM& bm, int64_t num_to_merge, int approximate, Work& w, cudaStream_t st) {
+void carry_out(const DevGraph& g, DevBM& bm, int64_t num_to_merge, int approximate, Work& w, cudaStream_t st,
+               bool np) {
     const int32_t B = bm.B;
     // queue order: stable sort of (delta, block)
     k_merge_keys<<<grid_cap(B, 256, 152 * 16), 256, 0, st>>>(w.best_dS, B, w.keys, w.vals);
@@ -140,7 +152,7 @@ void carry_out(const DevGraph& g, DevBM& bm, int64_t num_to_merge, int approxima
     if (approximate) {
         k_carry_approx<<<1, 32, 0, st>>>(w.vals, B, w.best, w.parent, num_to_merge, d_merged);
     } else {
-        carry_out_exact(g, bm, num_to_merge, w, st);
+        carry_out_exact(g, bm, num_to_merge, w, st, np);
     }
     count_launches(1);
     // union-find roots -> dense labels in ascending root order (build_mapping)

@@ -15,6 +15,8 @@
 //      incremental apply ends in the same state).
 // Hybrid MCMC sequential phase (:589-594): k_mh_chain, one CTA that walks the shuffled
 // high-degree vertices and applies every accepted move before the next proposal.
+#include <stdexcept>
+
 #include "chain.cuh"
 #include "delta.cuh"
 #include "kernels.cuh"
@@ -46,8 +48,9 @@ __global__ void k_split_by_degree(DevGraph g, const int32_t* __restrict__ list, 
     }
 }
 
-// kGreedy: compiled without the Hastings correction (the default configuration).
-template <int kThreads, bool kGreedy>
+// kMode: ACC_GREEDY (the default configuration, compiled without the Hastings
+// correction), ACC_HASTINGS or ACC_NP (nonparametric delta, no correction).
+template <int kThreads, int kMode>
 __device__ __forceinline__ int32_t gibbs_one(const DevGraph& g, const DevBM& bm, int32_t v, uint64_t seed,
                                              uint32_t iter, uint32_t step, int32_t* hk, int32_t* hO, int32_t* hI,
                                              int log2cap, long long (*red)[8], DevFlags* flags) {
@@ -60,9 +63,15 @@ __device__ __forceinline__ int32_t gibbs_one(const DevGraph& g, const DevBM& bm,
         return -1;
     }
     if (s == r) return -1;
+    if constexpr (kMode == ACC_NP) {
+        const long long dS = vertex_delta_fixed<kThreads, CsrAcc, true>(g, bm.asg, bm.d_out, bm.d_in, CsrAcc{bm}, v, r,
+                                                                        s, hk, hO, hI, log2cap, red, bm.sizes,
+                                                                        *bm.nonempty);
+        return accept_move(dS, 1.0, false, w[3]) ? s : -1;
+    }
     const long long dS =
         vertex_delta_fixed<kThreads>(g, bm.asg, bm.d_out, bm.d_in, CsrAcc{bm}, v, r, s, hk, hO, hI, log2cap, red);
-    if (kGreedy) return dS < 0 ? s : -1;  // finetune::accept with greedy (finetune.cpp:22-25)
+    if (kMode == ACC_GREEDY) return dS < 0 ? s : -1;  // finetune::accept with greedy (finetune.cpp:22-25)
     double H = 1.0;
     const int32_t o0 = __ldg(g.out_off + v), i0 = __ldg(g.inns_off + v);
     const int32_t kout = __ldg(g.out_off + v + 1) - o0, kin = __ldg(g.inns_off + v + 1) - i0;
@@ -72,7 +81,7 @@ __device__ __forceinline__ int32_t gibbs_one(const DevGraph& g, const DevBM& bm,
     return accept_move(dS, H, false, w[3]) ? s : -1;  // finetune::accept (finetune.cpp:26-31)
 }
 
-template <bool kGreedy>
+template <int kMode>
 __global__ void __launch_bounds__(256) k_gibbs_small(DevGraph g, DevBM bm, const int32_t* __restrict__ list,
                                                      const int32_t* __restrict__ d_n, uint64_t seed, uint32_t iter,
                                                      uint32_t step, int32_t* __restrict__ moves, DevFlags* flags) {
@@ -84,7 +93,7 @@ __global__ void __launch_bounds__(256) k_gibbs_small(DevGraph g, DevBM bm, const
     unsigned long long edges = 0, accepted = 0;
     for (int32_t i = blockIdx.x * kGibbsWarps + wid; i < n; i += gridDim.x * kGibbsWarps) {
         const int32_t v = list[i];
-        const int32_t mv = gibbs_one<32, kGreedy>(g, bm, v, seed, iter, step, hk[wid], hO[wid], hI[wid], kSmallLog2,
+        const int32_t mv = gibbs_one<32, kMode>(g, bm, v, seed, iter, step, hk[wid], hO[wid], hI[wid], kSmallLog2,
                                                   nullptr, flags);
         if (lane == 0) {
             moves[v] = mv;
@@ -98,7 +107,7 @@ __global__ void __launch_bounds__(256) k_gibbs_small(DevGraph g, DevBM bm, const
     }
 }
 
-template <bool kGreedy>
+template <int kMode>
 __global__ void __launch_bounds__(256) k_gibbs_big(DevGraph g, DevBM bm, const int32_t* __restrict__ list,
                                                    const int32_t* __restrict__ d_n, uint64_t seed, uint32_t iter,
                                                    uint32_t step, int log2cap, int32_t* __restrict__ moves,
@@ -114,7 +123,7 @@ __global__ void __launch_bounds__(256) k_gibbs_big(DevGraph g, DevBM bm, const i
         if (2 * k > cap) {
             if (threadIdx.x == 0) atomicOr(&flags->err, ERR_DEGREE);
         } else {
-            mv = gibbs_one<256, kGreedy>(g, bm, v, seed, iter, step, dyn, dyn + cap, dyn + 2 * cap, log2cap, red, flags);
+            mv = gibbs_one<256, kMode>(g, bm, v, seed, iter, step, dyn, dyn + cap, dyn + 2 * cap, log2cap, red, flags);
         }
         if (threadIdx.x == 0) {
             moves[v] = mv;
@@ -399,36 +408,35 @@ __global__ void k_shuffle_keys(const int32_t* __restrict__ base, int32_t n, uint
 
 }  // namespace
 
-void gibbs_propose(const DevGraph& g, const DevBM& bm, const int32_t* vlist, int32_t n, int32_t max_k, uint64_t seed,
-                   uint32_t iter, uint32_t step, int greedy, Work& w, cudaStream_t st) {
-    if (n <= 0) return;
-    int32_t* counts = w.d_scalar + 6;  // [6], [7]
-    cudaMemsetAsync(counts, 0, 2 * sizeof(int32_t), st);
-    k_split_by_degree<<<grid_cap(n, 256, 152 * 16), 256, 0, st>>>(g, vlist, n, 1 << (kSmallLog2 - 1), w.list_small,
-                                                                  w.list_big, counts);
-    if (greedy)
-        k_gibbs_small<true><<<grid_cap(n, kGibbsWarps, 152 * 8), 256, 0, st>>>(g, bm, w.list_small, counts, seed, iter,
-                                                                               step, w.moves, w.flags_dev);
-    else
-        k_gibbs_small<false><<<grid_cap(n, kGibbsWarps, 152 * 8), 256, 0, st>>>(g, bm, w.list_small, counts, seed,
-                                                                                iter, step, w.moves, w.flags_dev);
-    count_launches(2);
+template <int kMode>
+void gibbs_launch(const DevGraph& g, const DevBM& bm, int32_t n, int32_t max_k, const int32_t* counts, uint64_t seed,
+                  uint32_t iter, uint32_t step, Work& w, cudaStream_t st) {
+    k_gibbs_small<kMode><<<grid_cap(n, kGibbsWarps, 152 * 8), 256, 0, st>>>(g, bm, w.list_small, counts, seed, iter,
+                                                                            step, w.moves, w.flags_dev);
+    count_launches(1);
     if (max_k > (1 << (kSmallLog2 - 1))) {
         int log2cap = ceil_log2((uint64_t)(2 * max_k));
         if (log2cap > 14) log2cap = 14;
         const size_t smem = (size_t)(3 * sizeof(int32_t)) << log2cap;
-        if (greedy) {
-            allow_max_dynamic_smem((const void*)k_gibbs_big<true>);
-            k_gibbs_big<true><<<152 * 2, 256, smem, st>>>(g, bm, w.list_big, counts + 1, seed, iter, step, log2cap,
-                                                          w.moves, w.flags_dev);
-        } else {
-            allow_max_dynamic_smem((const void*)k_gibbs_big<false>);
-            k_gibbs_big<false><<<152 * 2, 256, smem, st>>>(g, bm, w.list_big, counts + 1, seed, iter, step, log2cap,
-                                                           w.moves, w.flags_dev);
-        }
+        allow_max_dynamic_smem((const void*)k_gibbs_big<kMode>);
+        k_gibbs_big<kMode><<<152 * 2, 256, smem, st>>>(g, bm, w.list_big, counts + 1, seed, iter, step, log2cap,
+                                                       w.moves, w.flags_dev);
         count_launches(1);
     }
-    (void)greedy;
+}
+
+void gibbs_propose(const DevGraph& g, const DevBM& bm, const int32_t* vlist, int32_t n, int32_t max_k, uint64_t seed,
+                   uint32_t iter, uint32_t step, int mode, Work& w, cudaStream_t st) {
+    if (n <= 0) return;
+    if (mode == ACC_NP && (!g.LG || !g.Dm || !g.Dp)) throw std::logic_error("nonparametric tables missing");
+    int32_t* counts = w.d_scalar + 6;  // [6], [7]
+    cudaMemsetAsync(counts, 0, 2 * sizeof(int32_t), st);
+    k_split_by_degree<<<grid_cap(n, 256, 152 * 16), 256, 0, st>>>(g, vlist, n, 1 << (kSmallLog2 - 1), w.list_small,
+                                                                  w.list_big, counts);
+    count_launches(1);
+    if (mode == ACC_NP) gibbs_launch<ACC_NP>(g, bm, n, max_k, counts, seed, iter, step, w, st);
+    else if (mode == ACC_HASTINGS) gibbs_launch<ACC_HASTINGS>(g, bm, n, max_k, counts, seed, iter, step, w, st);
+    else gibbs_launch<ACC_GREEDY>(g, bm, n, max_k, counts, seed, iter, step, w, st);
 }
 
 void gibbs_apply(const DevBM& bm, const int32_t* vlist, int32_t n, Work& w, cudaStream_t st) {

@@ -42,6 +42,42 @@ def block_merge_delta_mdl(blockmodel, blocks, proposals):
     return out
 
 
+class nonparametric:
+    """entropy::nonparametric (src/entropy.cpp:617-1225, include/entropy.hpp:101-190) on the
+    device, for a directed graph without degree correction."""
+
+    @staticmethod
+    def mdl(blockmodel, graph=None):
+        """nonparametric::mdl (src/entropy.cpp:751-779)."""
+        out = ctypes.c_double()
+        blockmodel.ctx.check(blockmodel.ctx.lib.sbpgpu_np_mdl(blockmodel.h, ctypes.byref(out)))
+        return out.value
+
+    @staticmethod
+    def delta_mdl(blockmodel, vertices, proposals):
+        """nonparametric::delta_mdl (src/entropy.cpp:1146-1178) for vertices[i] -> proposals[i]."""
+        v = np.ascontiguousarray(np.atleast_1d(vertices), dtype=np.int32)
+        s = np.ascontiguousarray(np.atleast_1d(proposals), dtype=np.int32)
+        if v.shape != s.shape:
+            raise ValueError("vertices and proposals must have the same length")
+        out = np.zeros(v.size, np.float64)
+        blockmodel.ctx.check(blockmodel.ctx.lib.sbpgpu_np_delta_mdl_batch(blockmodel.h, v.size, _p(v, i32p),
+                                                                          _p(s, i32p), _p(out, f64p)))
+        return out
+
+    @staticmethod
+    def block_merge_delta_mdl(blockmodel, blocks, proposals):
+        """nonparametric::block_merge_delta_mdl (src/entropy.cpp:1198-1223)."""
+        r = np.ascontiguousarray(np.atleast_1d(blocks), dtype=np.int32)
+        s = np.ascontiguousarray(np.atleast_1d(proposals), dtype=np.int32)
+        if r.shape != s.shape:
+            raise ValueError("blocks and proposals must have the same length")
+        out = np.zeros(r.size, np.float64)
+        blockmodel.ctx.check(blockmodel.ctx.lib.sbpgpu_np_merge_delta_mdl_batch(blockmodel.h, r.size, _p(r, i32p),
+                                                                                _p(s, i32p), _p(out, f64p)))
+        return out
+
+
 def null_mdl_v1(num_edges):
     """entropy::null_mdl_v1 (src/entropy.cpp:571-585) for the parametric entropy."""
     E = float(num_edges)

@@ -7,7 +7,7 @@
 //   test_api <toy.txt> <graph.txt> <seed> <assignment_out.txt>
 //
 // toy.txt: N E, E edge pairs, B, N assignment entries, MDL, then B out-degrees, B
-// in-degrees and B total degrees.  graph.txt: N E, then E edge pairs.
+// in-degrees, B total degrees and the nonparametric MDL.  graph.txt: N E, then E edge pairs.
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -47,6 +47,7 @@ struct Toy {
     std::vector<std::pair<long, long>> edges;
     std::vector<long> assignment, dout, din, dtot;
     double mdl = 0.0;
+    double np_mdl = 0.0;
 };
 
 static Toy read_toy(const char* path) {
@@ -66,6 +67,7 @@ static Toy read_toy(const char* path) {
         vec->resize(t.B);
         for (auto& x : *vec) f >> x;
     }
+    f >> t.np_mdl;
     if (!f) throw std::runtime_error("cannot read the toy fixture");
     return t;
 }
@@ -127,15 +129,19 @@ static void toy_known_answers(const Toy& t) {
         threw = true;
     }
     EXPECT(threw);
-    threw = false;
-    try {
-        s::Args na;
-        na.nonparametric = true;
-        s::finetune::mcmc(0, graph, c, true, na);
-    } catch (const s::Error& e) {
-        threw = e.status == SBPGPU_EUNSUPPORTED;
-    }
-    EXPECT(threw);
+
+    // nonparametric entropy: the toy blockmodel's known answer (nonparametric_entropy_test.cpp:19-27,
+    // :57-61) and the vertex-7 move against the MDL difference (:118-133)
+    EXPECT(float_eq(s::entropy::nonparametric::mdl(bm, graph), t.np_mdl));
+    const double dN = s::entropy::nonparametric::delta_mdl(bm, std::vector<long>{v}, std::vector<long>{to})[0];
+    EXPECT(std::fabs(dN - (s::entropy::nonparametric::mdl(bm2, graph) - s::entropy::nonparametric::mdl(bm, graph))) <
+           1e-6);
+    s::Args na;
+    na.nonparametric = true;
+    na.seed = 5;
+    s::Blockmodel c2 = bm.copy();
+    s::finetune::mcmc(0, graph, c2, true, na);
+    EXPECT(c2.num_blocks() == t.B);
 
     // normalize_mdl_v1 divides by the one-block model's length
     EXPECT(std::fabs(s::entropy::normalize_mdl_v1(mdl, graph) * s::entropy::null_mdl_v1(graph) - mdl) < 1e-9 * mdl);

@@ -30,6 +30,7 @@ def _write_toy(golden, path):
         f.write(repr(float(golden["mdl"])) + "\n")
         for k in ("block_degrees_out", "block_degrees_in", "block_degrees"):
             f.write(" ".join(str(x) for x in golden[k]) + "\n")
+        f.write(repr(float(golden["nonparametric"]["mdl"])) + "\n")
 
 
 @pytest.mark.gpu

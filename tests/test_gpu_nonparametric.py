@@ -1,0 +1,177 @@
+"""GPU parity of the nonparametric entropy (entropy::nonparametric, reference
+src/entropy.cpp:617-1225; directed, not degree-corrected).
+
+Deltas are exact sums of the same 2^-24 terms on both sides and must be identical to the
+oracle's (tolerance 0).  The MDL is the same exact sum plus the two terms of the non-empty
+block count, which both sides form with the same host arithmetic: it must equal the
+oracle's canonical value within 1e-12 relative, and the reference's known answer within
+EXPECT_FLOAT_EQ.  Sweeps, merges and whole partitions must leave the same integer state.
+The graphs include empty blocks, singleton blocks and vertices without edges, so moves that
+change the number of non-empty blocks occur."""
+import numpy as np
+import pytest
+
+from test_gpu_parity import same_state
+
+pytestmark = pytest.mark.gpu
+
+MDL_REL_TOL_CANONICAL = 1e-12
+
+
+def np_pair(gpu, oracle, n, e, blocks, B, seed, isolated=0, empty=0, assignment=None):
+    """A DC-SBM graph plus `isolated` vertices without edges; the last `empty` blocks start
+    empty and block B - empty - 1 holds a single vertex."""
+    src, dst, _ = gpu.dcsbm.generate(n, e, blocks, seed=seed)
+    N = n + isolated
+    rng = np.random.default_rng(seed)
+    if assignment is None:
+        live = B - empty
+        a = rng.integers(0, live - 1, N).astype(np.int32)
+        a[: live - 1] = np.arange(live - 1)
+        a[N - 1] = live - 1  # the singleton block
+    else:
+        a = np.asarray(assignment, np.int32)
+    G, O = gpu.Graph(N, src, dst), oracle.Graph(N, src, dst)
+    return G, O, gpu.Blockmodel(B, G, 0.5, a), oracle.Blockmodel(O, B, a), a
+
+
+def float_eq(a, b, ulps=4):
+    return abs(np.float32(a) - np.float32(b)) <= ulps * np.spacing(np.float32(max(abs(a), abs(b))))
+
+
+def test_np_toy_known_answers(gpu, oracle, golden):
+    e = np.array(golden["edges"], np.int32)
+    G, O = gpu.Graph(11, e[:, 0], e[:, 1]), oracle.Graph(11, e[:, 0], e[:, 1])
+    gb = gpu.Blockmodel(3, G, 0.5, golden["assignment"])
+    ob = oracle.Blockmodel(O, 3, golden["assignment"])
+    m = gpu.entropy.nonparametric.mdl(gb)
+    assert float_eq(m, golden["nonparametric"]["mdl"])  # nonparametric_entropy_test.cpp:57-61
+    assert abs(m - ob.np_mdl()[1]) <= MDL_REL_TOL_CANONICAL * abs(m)
+    mv = golden["vertex_move"]
+    d = gpu.entropy.nonparametric.delta_mdl(gb, [mv["vertex"]], [mv["proposal"]])[0]
+    assert d == ob.np_delta_mdl(mv["vertex"], mv["proposal"])[1] / 2**24
+    bm = golden["block_merge"]
+    d = gpu.entropy.nonparametric.block_merge_delta_mdl(gb, [bm["block"]], [bm["proposal"]])[0]
+    assert d == ob.np_merge_delta_mdl(bm["block"], bm["proposal"])[1] / 2**24
+
+
+@pytest.mark.parametrize("B", [5, 40, 600])
+def test_np_mdl_and_deltas_exact(gpu, oracle, B):
+    G, O, gb, ob, a = np_pair(gpu, oracle, 1500, 20000, 9, B, seed=200 + B, isolated=30, empty=2)
+    N = a.size
+    m = gpu.entropy.nonparametric.mdl(gb)
+    assert abs(m - ob.np_mdl()[1]) <= MDL_REL_TOL_CANONICAL * abs(m)
+    rng = np.random.default_rng(B)
+    v = np.concatenate([rng.integers(0, N, 2500), [N - 1] * 3, np.arange(N - 30, N)]).astype(np.int32)
+    s = np.concatenate([rng.integers(0, B, 2500), [0, B - 1, B - 2], np.full(30, B - 1)]).astype(np.int32)
+    keep = s != a[v]
+    v, s = v[keep], s[keep]
+    got = gpu.entropy.nonparametric.delta_mdl(gb, v, s)
+    for i in range(v.size):
+        assert got[i] == ob.np_delta_mdl(int(v[i]), int(s[i]))[1] / 2**24, (i, v[i], s[i])
+    r = rng.integers(0, B, 1500).astype(np.int32)
+    t = rng.integers(0, B, 1500).astype(np.int32)
+    keep = r != t
+    r, t = r[keep], t[keep]
+    got = gpu.entropy.nonparametric.block_merge_delta_mdl(gb, r, t)
+    for i in range(r.size):
+        assert got[i] == ob.np_merge_delta_mdl(int(r[i]), int(t[i]))[1] / 2**24, (i, r[i], t[i])
+
+
+def test_np_deltas_high_degree_and_self_loops(gpu, oracle):
+    n, B = 800, 20
+    rng = np.random.default_rng(6)
+    src = list(rng.integers(0, n, 12000))
+    dst = list(rng.integers(0, n, 12000))
+    for hub in range(5):
+        src += [hub] * 600 + list(rng.integers(0, n, 300))
+        dst += list(rng.integers(0, n, 600)) + [hub] * 300
+    for v in range(0, n, 7):
+        src.append(v)
+        dst.append(v)
+    src, dst = np.array(src, np.int32), np.array(dst, np.int32)
+    a = rng.integers(0, B, n).astype(np.int32)
+    a[:B] = np.arange(B)
+    G, O = gpu.Graph(n, src, dst), oracle.Graph(n, src, dst)
+    gb, ob = gpu.Blockmodel(B, G, 0.5, a), oracle.Blockmodel(O, B, a)
+    vs = np.concatenate([np.arange(5), np.arange(0, n, 7)]).astype(np.int32)
+    ss = ((a[vs] + 1 + rng.integers(0, B - 1, vs.size)) % B).astype(np.int32)
+    got = gpu.entropy.nonparametric.delta_mdl(gb, vs, ss)
+    for i in range(vs.size):
+        assert got[i] == ob.np_delta_mdl(int(vs[i]), int(ss[i]))[1] / 2**24
+
+
+@pytest.mark.parametrize("B", [6, 900])
+def test_np_gibbs_batch_identical(gpu, oracle, B):
+    G, O, gb, ob, a = np_pair(gpu, oracle, 2500, 30000, 9, B, seed=240 + B, isolated=40, empty=3)
+    cfg = oracle.make_config("async_gibbs", nonparametric=True)
+    args = gpu.Args(algorithm="async_gibbs", nonparametric=True)
+    verts = np.arange(a.size, dtype=np.int32)
+    for it in range(3):
+        mv_g, app_g = gpu.finetune.gibbs_batch(gb, verts, seed=5, iteration=it, step=2, args=args)
+        n_o, mv_o, _ = ob.gibbs_batch(verts, 5, it, 2, cfg)
+        assert np.array_equal(mv_g, mv_o)
+        assert app_g == n_o
+        same_state(gb, ob)
+        assert abs(gpu.entropy.nonparametric.mdl(gb) - ob.np_mdl()[1]) <= MDL_REL_TOL_CANONICAL * ob.np_mdl()[1]
+
+
+@pytest.mark.parametrize("n,B", [(2500, 8), (2500, 120), (2500, 1500), (24000, 16000)])
+def test_np_mh_chain_identical(gpu, oracle, n, B):
+    """The windowed chain's three cell stores; vertices without edges propose random blocks,
+    some of them empty, so accepted moves change the non-empty block count."""
+    G, O, gb, ob, a = np_pair(gpu, oracle, n, 12 * n, 9, B, seed=250 + B, isolated=200, empty=4)
+    N = a.size
+    rng = np.random.default_rng(B)
+    order = np.concatenate([rng.permutation(n)[:500], np.arange(n, N)])
+    order = rng.permutation(order).astype(np.int32)
+    args = gpu.Args(algorithm="hybrid_mcmc", nonparametric=True)
+    applied = gpu.finetune.mh_chain(gb, order, seed=8, iteration=1, step=3, args=args)
+    want = ob.mh_chain(order, 8, 1, 3, oracle.make_config("hybrid_mcmc", nonparametric=True))
+    assert applied == want
+    same_state(gb, ob)
+
+
+@pytest.mark.parametrize("alg", ["async_gibbs", "hybrid_mcmc", "metropolis_hastings"])
+def test_np_mcmc_identical(gpu, oracle, alg):
+    G, O, gb, ob, a = np_pair(gpu, oracle, 2000, 24000, 9, 150, seed=260, isolated=50, empty=2)
+    gpu.finetune.mcmc(2, G, gb, True, gpu.Args(algorithm=alg, seed=13, max_iterations=6, nonparametric=True))
+    ob.mcmc(oracle.make_config(alg, max_iterations=6, nonparametric=True), seed=13, step=2,
+            golden_ratio_not_reached=True)
+    same_state(gb, ob)
+    assert abs(gb.getOverall_entropy() - ob.np_mdl()[1]) <= MDL_REL_TOL_CANONICAL * ob.np_mdl()[1]
+
+
+@pytest.mark.parametrize("cells", ["dense", "hash"])
+@pytest.mark.parametrize("B,approx", [(3000, False), (400, False), (60, False), (400, True)])
+def test_np_merge_blocks_identical(gpu, oracle, B, approx, cells):
+    """Every merge lowers the non-empty block count, so the carry-out adds that term at each
+    pop; empty blocks score 0 (entropy.cpp:1203-1204)."""
+    if approx and cells == "hash":
+        pytest.skip("the approximate carry-out uses no cell store")
+    ctx = gpu.core.default_context()
+    ctx.set_cells_budget(0 if cells == "hash" else 16 << 30)
+    try:
+        G, O, gb, ob, a = np_pair(gpu, oracle, 3000, 36000, 9, B, seed=270 + B, empty=0 if B == 3000 else 3,
+                                  assignment=np.arange(3000) if B == 3000 else None)
+        args = gpu.Args(seed=21, approximate=approx, nonparametric=True)
+        n = B // 2
+        gpu.block_merge.merge_blocks(gb, G, args=args, step=5, num_blocks_to_merge=n)
+        ob.merge_blocks(oracle.make_config(approximate=approx, nonparametric=True), seed=21, step=5, num_to_merge=n)
+        assert gb.num_blocks() == B - n == ob.num_blocks
+        same_state(gb, ob)
+    finally:
+        ctx.set_cells_budget(16 << 30)
+
+
+def test_np_full_sbp_identical_c1(gpu, oracle):
+    src, dst, planted = gpu.dcsbm.generate_config("C1", seed=0)
+    G = gpu.Graph(1000, src, dst)
+    a_g, B_g, mdl_g, st = gpu.sbp.stochastic_block_partition(G, gpu.Args(algorithm="hybrid_mcmc", seed=3,
+                                                                         nonparametric=True))
+    O = oracle.Graph(1000, src, dst)
+    a_o, B_o, mdl_o, ost = oracle.sbp(O, oracle.make_config("hybrid_mcmc", nonparametric=True), seed=3)
+    assert B_g == B_o
+    assert np.array_equal(a_g, a_o)
+    assert abs(mdl_g - mdl_o) <= MDL_REL_TOL_CANONICAL * abs(mdl_o)
+    assert st["merges"] == ost.merges and st["mcmc_iterations"] == ost.mcmc_iterations

@@ -49,8 +49,8 @@ def test_args_validation():
     import sbp_gb300
     with pytest.raises(ValueError):
         sbp_gb300.Args(algorithm="nope").config()
-    with pytest.raises(NotImplementedError):
-        sbp_gb300.Args(nonparametric=True).config()
+    c = sbp_gb300.Args(nonparametric=True).config()
+    assert (c.nonparametric, c.greedy) == (1, 0)  # --nonparametric sets greedy off (args.hpp:204-207)
 
 
 def test_entry_points_reject_null_handles_without_device():
