@@ -190,6 +190,30 @@ sbpgpu_status sbpgpu_merge_proposals(sbpgpu_bm* bm, uint64_t seed, int32_t step,
 sbpgpu_status sbpgpu_sbp(sbpgpu_graph* g, const sbpgpu_config* cfg, uint64_t seed, int32_t* out_assignment,
                          int64_t* num_blocks, double* out_mdl, sbpgpu_stats* stats);
 
+/* ---- sampling (src/sample.cpp, src/main.cpp:98-140) ------------------------------ */
+/* A vertex sample: algorithm 0 max_degree (sample.cpp:255-270), 1 random (:272-284, the
+ * seeded stream), 2 degree_product (:28-49), 3 detach (:12-26, vertices of degree above 1;
+ * sample_size unused).  mapping[N] receives each vertex's id in the sample or -1;
+ * sample_n the sample's size (long(sample_size * N) vertices, or as the algorithm gives). */
+sbpgpu_status sbpgpu_sample(sbpgpu_graph* g, int32_t algorithm, double sample_size, uint64_t seed,
+                            int32_t* mapping, int64_t* sample_n);
+/* sample::from_vertices (sample.cpp:240-253): the graph of the sampled vertices. */
+sbpgpu_status sbpgpu_graph_subgraph(sbpgpu_graph* g, const int32_t* mapping, int64_t sample_n,
+                                    sbpgpu_graph** out);
+/* sample::extend (sample.cpp:159-199): sampled vertices keep their sample block; the others,
+ * in vertex order, take the block most of their assigned neighbours are in (ties to the
+ * smallest block), or a block drawn from the seeded stream. */
+sbpgpu_status sbpgpu_extend(sbpgpu_graph* g, const int32_t* sample_assignment, int64_t sample_n,
+                            int64_t num_blocks, const int32_t* mapping, uint64_t seed, int32_t* out_assignment);
+/* finetune::finetune_assignment (src/finetune.cpp:903-932). */
+sbpgpu_status sbpgpu_finetune_assignment(sbpgpu_bm* bm, const sbpgpu_config* cfg, uint64_t seed,
+                                         sbpgpu_stats* stats);
+/* The --samplesize < 1 path of main.cpp:98-140: sample, sbpgpu_sbp on the sample, extend,
+ * then finetune_assignment on the full graph. */
+sbpgpu_status sbpgpu_sbp_sampled(sbpgpu_graph* g, const sbpgpu_config* cfg, uint64_t seed, int32_t algorithm,
+                                 double sample_size, int32_t* out_assignment, int64_t* num_blocks,
+                                 double* out_mdl, sbpgpu_stats* stats);
+
 /* ---- evaluation ------------------------------------------------------------------ */
 /* evaluate::evaluate_blockmodel (src/evaluate.cpp:9-180) against a true partition: the
  * contingency table is counted on the device; NMI (float-log marginal entropies as the

@@ -12,6 +12,9 @@
  *   MH vertex proposal    : ctr = (vertex, iteration, step, DOM_MH)
  *   merge proposal i      : ctr = (block, 0, step, DOM_MERGE | i << 8)
  *   shuffles              : ctr = (position, iteration, step, DOM_SHUFFLE_*)
+ *   random sample         : shuffle with ctr = (position, 0, 0, DOM_SAMPLE = 6)
+ *   extend, random block  : ctr = (vertex, 0, 0, DOM_EXTEND = 7), block = u32_below(w[0], B)
+ *   finetune_assignment   : MH draws with step = 0xffffffff
  *   u32_below(w, n) = (w * n) >> 32;  u64_below(hi, lo, n) = ((hi:lo) * n) >> 64.
  *   Multinomials over a block's neighbour weights enumerate the row part (ascending
  *   column) and then the column part (ascending row), the same concatenation the
@@ -39,7 +42,8 @@
 namespace {
 
 enum : uint32_t {
-    DOM_GIBBS = 1, DOM_MH = 2, DOM_MERGE = 3, DOM_SHUFFLE_HDV = 4, DOM_SHUFFLE_ALL = 5,
+    DOM_GIBBS = 1, DOM_MH = 2, DOM_MERGE = 3, DOM_SHUFFLE_HDV = 4, DOM_SHUFFLE_ALL = 5, DOM_SAMPLE = 6,
+    DOM_EXTEND = 7,
 };
 
 // ---------------------------------------------------------------- Philox4x32-10
@@ -1232,6 +1236,199 @@ extern "C" int ora_merge_blocks(ora_bm* bm, const ora_config* cfg, uint64_t seed
     return merge_blocks(bm, cfg, seed, (uint32_t)step, num_to_merge, st);
 }
 
+// ---------------------------------------------------------------- sampling
+namespace {
+
+/* Graph::degrees (graph.cpp:24-31): out + in - (has a self-loop). */
+std::vector<int64_t> graph_degrees(const ora_graph* g) {
+    std::vector<int64_t> d(g->N);
+    for (int64_t v = 0; v < g->N; ++v)
+        d[v] = (int64_t)g->out[v].size() + (int64_t)g->in[v].size() - (g->selfcnt[v] > 0 ? 1 : 0);
+    return d;
+}
+
+/* long(args.samplesize * double(N)) */
+inline int64_t sample_target(const ora_graph* g, double samplesize) { return (int64_t)(samplesize * (double)g->N); }
+
+/* sample::max_degree (sample.cpp:255-270): stable argsort by degree, descending. */
+int64_t sample_max_degree(const ora_graph* g, double samplesize, std::vector<int32_t>& mapping) {
+    const std::vector<int64_t> d = graph_degrees(g);
+    std::vector<int32_t> idx(g->N);
+    for (int64_t v = 0; v < g->N; ++v) idx[v] = (int32_t)v;
+    std::stable_sort(idx.begin(), idx.end(), [&](int32_t a, int32_t b) { return d[a] > d[b]; });
+    const int64_t n = std::min(sample_target(g, samplesize), g->N);
+    for (int64_t i = 0; i < n; ++i) mapping[idx[i]] = (int32_t)i;
+    return n;
+}
+
+/* sample::random (sample.cpp:272-284) with the canonical shuffle. */
+int64_t sample_random(const ora_graph* g, double samplesize, uint64_t seed, std::vector<int32_t>& mapping) {
+    std::vector<int32_t> base(g->N), order;
+    for (int64_t v = 0; v < g->N; ++v) base[v] = (int32_t)v;
+    shuffle(order, base, seed, 0, 0, DOM_SAMPLE);
+    const int64_t n = std::min(sample_target(g, samplesize), g->N);
+    for (int64_t i = 0; i < n; ++i) mapping[order[i]] = (int32_t)i;
+    return n;
+}
+
+/* sample::degree_product (sample.cpp:28-49) over Graph::sorted_edge_list (graph.cpp:302-315):
+ * edges in source order, stable-sorted by degree product, descending. */
+int64_t sample_degree_product(const ora_graph* g, double samplesize, std::vector<int32_t>& mapping) {
+    const std::vector<int64_t> d = graph_degrees(g);
+    std::vector<std::pair<std::pair<int32_t, int32_t>, int64_t>> edges;
+    for (int64_t u = 0; u < g->N; ++u)
+        for (int32_t v : g->out[u]) edges.push_back({{(int32_t)u, v}, d[u] * d[v]});
+    std::stable_sort(edges.begin(), edges.end(), [](const auto& a, const auto& b) { return a.second > b.second; });
+    const int64_t target = sample_target(g, samplesize);
+    int64_t n = 0;
+    for (const auto& e : edges) {
+        if (mapping[e.first.first] == -1) mapping[e.first.first] = (int32_t)n++;
+        if (mapping[e.first.second] == -1) mapping[e.first.second] = (int32_t)n++;
+        if (n >= target) break;
+    }
+    return n;
+}
+
+/* sample::detach (sample.cpp:12-26): vertices of degree above 1. */
+int64_t sample_detach(const ora_graph* g, std::vector<int32_t>& mapping) {
+    const std::vector<int64_t> d = graph_degrees(g);
+    int64_t n = 0;
+    for (int64_t v = 0; v < g->N; ++v)
+        if (d[v] > 1) mapping[v] = (int32_t)n++;
+    return n;
+}
+
+/* sample::from_vertices (sample.cpp:240-253): edges between sampled vertices, by source
+ * vertex in ascending original id, each source's out-neighbours in order. */
+ora_graph* from_vertices(const ora_graph* g, const std::vector<int32_t>& mapping, int64_t n) {
+    std::vector<int32_t> src, dst;
+    for (int64_t u = 0; u < g->N; ++u) {
+        if (mapping[u] < 0) continue;
+        for (int32_t v : g->out[u])
+            if (mapping[v] >= 0) {
+                src.push_back(mapping[u]);
+                dst.push_back(mapping[v]);
+            }
+    }
+    return ora_graph_create(n, (int64_t)src.size(), src.data(), dst.data());
+}
+
+/* sample::extend (sample.cpp:159-199): sampled vertices keep their block; the others, in
+ * vertex order, take the block most of their already-assigned neighbours are in (ties to
+ * the smallest block: the reference iterates a hash map), or a random block. */
+void extend(const ora_graph* g, const std::vector<int32_t>& sample_asg, int64_t B, const std::vector<int32_t>& mapping,
+            uint64_t seed, std::vector<int32_t>& asg) {
+    asg.assign(g->N, -1);
+    for (int64_t v = 0; v < g->N; ++v)
+        if (mapping[v] >= 0) asg[v] = sample_asg[mapping[v]];
+    for (int64_t v = 0; v < g->N; ++v) {
+        if (asg[v] != -1) continue;
+        std::map<int32_t, int64_t> counts;
+        for (int32_t u : g->out[v])
+            if (asg[u] != -1) counts[asg[u]]++;
+        for (int32_t u : g->in[v])
+            if (asg[u] != -1 && u != v) counts[asg[u]]++;
+        if (counts.empty()) {
+            uint32_t w[4];
+            draw(seed, (uint32_t)v, 0, 0, DOM_EXTEND, w);
+            asg[v] = (int32_t)u32_below(w[0], (uint32_t)B);
+            continue;
+        }
+        int64_t best = 0;
+        int32_t block = -1;
+        for (const auto& e : counts)
+            if (e.second > best) {
+                best = e.second;
+                block = e.first;
+            }
+        asg[v] = block;
+    }
+}
+
+/* finetune::early_stop(iteration, initial_entropy, deltas) (finetune.cpp:285-294). */
+bool early_stop3(int64_t iteration, double initial_entropy, const std::vector<double>& d) {
+    if (iteration < 3) return false;
+    const size_t last = d.size() - 1;
+    double average = d[last] + d[last - 1] + d[last - 2];
+    average /= -3.0;
+    return average < 1e-4 * initial_entropy;
+}
+
+constexpr uint32_t kFinetuneStep = 0xffffffffu;
+
+/* finetune::finetune_assignment (finetune.cpp:903-932): sequential MH over every vertex in
+ * id order until the three-iteration average improvement falls below 1e-4 of the entropy. */
+void finetune_assignment(ora_bm* bm, const ora_config* cfg, uint64_t seed, ora_stats* st) {
+    const ora_graph* g = bm->g;
+    bm->entropy = mdl_for(bm, cfg);
+    if (bm->B < 2) return;  // one block: no move can be proposed (as the sweeps, finetune.cpp:567)
+    std::vector<double> deltas;
+    for (int it = 0; it < cfg->max_iterations; ++it) {
+        double dsum = 0.0;
+        for (int64_t v = 0; v < g->N; ++v) {
+            double dS = 0.0;
+            add_stats(st, g, v);
+            if (mh_step(bm, v, seed, (uint32_t)it, kFinetuneStep, cfg, &dS)) {
+                dsum += dS;
+                if (st) st->moves++;
+            }
+        }
+        deltas.push_back(dsum);
+        if (st) st->mcmc_iterations++;
+        if (early_stop3(it, bm->entropy, deltas)) break;
+    }
+    bm->entropy = mdl_for(bm, cfg);
+}
+
+int64_t sample_any(const ora_graph* g, int32_t alg, double samplesize, uint64_t seed, std::vector<int32_t>& mapping) {
+    mapping.assign(g->N, -1);
+    switch (alg) {
+        case 0: return sample_max_degree(g, samplesize, mapping);
+        case 1: return sample_random(g, samplesize, seed, mapping);
+        case 2: return sample_degree_product(g, samplesize, mapping);
+        case 3: return sample_detach(g, mapping);
+        default: return -1;
+    }
+}
+
+}  // namespace
+
+extern "C" int64_t ora_sample(const ora_graph* g, int32_t alg, double samplesize, uint64_t seed, int32_t* mapping) {
+    std::vector<int32_t> m;
+    const int64_t n = sample_any(g, alg, samplesize, seed, m);
+    if (mapping) std::copy(m.begin(), m.end(), mapping);
+    return n;
+}
+
+extern "C" ora_graph* ora_subgraph(const ora_graph* g, const int32_t* mapping, int64_t n) {
+    return from_vertices(g, std::vector<int32_t>(mapping, mapping + g->N), n);
+}
+
+extern "C" void ora_graph_edges(const ora_graph* g, int32_t* src, int32_t* dst) {
+    int64_t i = 0;
+    for (int64_t u = 0; u < g->N; ++u)
+        for (int32_t v : g->out[u]) {
+            src[i] = (int32_t)u;
+            dst[i] = v;
+            ++i;
+        }
+}
+
+extern "C" int64_t ora_graph_num_edges(const ora_graph* g) { return g->E; }
+
+extern "C" void ora_extend(const ora_graph* g, const int32_t* sample_asg, int64_t sample_n, int64_t B,
+                           const int32_t* mapping, uint64_t seed, int32_t* out) {
+    std::vector<int32_t> a;
+    extend(g, std::vector<int32_t>(sample_asg, sample_asg + sample_n), B, std::vector<int32_t>(mapping, mapping + g->N),
+           seed, a);
+    std::copy(a.begin(), a.end(), out);
+}
+
+extern "C" int ora_finetune_assignment(ora_bm* bm, const ora_config* cfg, uint64_t seed, ora_stats* st) {
+    finetune_assignment(bm, cfg, seed, st);
+    return 0;
+}
+
 /* sbp::stochastic_block_partition (sbp.cpp:16-72) with BlockmodelTriplet::get_next_blockmodel
  * (blockmodel_triplet.cpp:4-37). */
 extern "C" int64_t ora_sbp(const ora_graph* g, const ora_config* cfg, uint64_t seed, int32_t* out_asg,
@@ -1317,6 +1514,29 @@ extern "C" void ora_np_merge_delta_mdl(const ora_bm* bm, int64_t r, int64_t s, d
 }
 
 extern "C" int64_t ora_bm_nonempty(const ora_bm* bm) { return bm->nonempty; }
+
+/* The sampled partition of main.cpp:98-140: sample, partition the sample, extend the
+ * sample's blocks to the full graph, then finetune_assignment on the full graph. */
+extern "C" int64_t ora_sbp_sampled(const ora_graph* g, const ora_config* cfg, uint64_t seed, int32_t alg,
+                                   double samplesize, int32_t* out_asg, double* out_mdl, ora_stats* st) {
+    std::vector<int32_t> mapping;
+    const int64_t n = sample_any(g, alg, samplesize, seed, mapping);
+    if (n <= 0) return -1;
+    ora_graph* sg = from_vertices(g, mapping, n);
+    std::vector<int32_t> sasg(n);
+    double smdl = 0.0;
+    const int64_t B = ora_sbp(sg, cfg, seed, sasg.data(), &smdl, st);
+    ora_graph_destroy(sg);
+    if (B <= 0) return -1;
+    std::vector<int32_t> asg;
+    extend(g, sasg, B, mapping, seed, asg);
+    ora_bm* bm = ora_bm_create(g, B, asg.data());
+    finetune_assignment(bm, cfg, seed, st);
+    if (out_asg) std::copy(bm->asg.begin(), bm->asg.end(), out_asg);
+    if (out_mdl) *out_mdl = bm->entropy;
+    delete bm;
+    return B;
+}
 
 extern "C" double ora_null_mdl_v1(double E) {
     const double log_posterior_p = E * log(1.0 / E);

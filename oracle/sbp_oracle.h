@@ -132,6 +132,23 @@ void ora_np_merge_delta_mdl(const ora_bm* bm, int64_t block, int64_t proposal, d
 /* Blockmodel::num_nonempty_blocks as the oracle tracks it. */
 int64_t ora_bm_nonempty(const ora_bm* bm);
 
+/* Sampling (sample.cpp).  alg: 0 max_degree, 1 random, 2 degree_product, 3 detach.
+ * mapping[v] = the vertex's id in the sample or -1; returns the sample's size. */
+int64_t ora_sample(const ora_graph* g, int32_t alg, double samplesize, uint64_t seed, int32_t* mapping);
+/* sample::from_vertices (sample.cpp:240-253). */
+ora_graph* ora_subgraph(const ora_graph* g, const int32_t* mapping, int64_t n);
+int64_t ora_graph_num_edges(const ora_graph* g);
+/* The graph's edges, by source vertex, each source's out-neighbours in order. */
+void ora_graph_edges(const ora_graph* g, int32_t* src, int32_t* dst);
+/* sample::extend (sample.cpp:159-199). */
+void ora_extend(const ora_graph* g, const int32_t* sample_assignment, int64_t sample_n, int64_t num_blocks,
+                const int32_t* mapping, uint64_t seed, int32_t* out_assignment);
+/* finetune::finetune_assignment (finetune.cpp:903-932); mutates bm. */
+int ora_finetune_assignment(ora_bm* bm, const ora_config* cfg, uint64_t seed, ora_stats* stats);
+/* main.cpp:98-140: sample, partition, extend, finetune.  Returns the number of blocks. */
+int64_t ora_sbp_sampled(const ora_graph* g, const ora_config* cfg, uint64_t seed, int32_t alg, double samplesize,
+                        int32_t* out_assignment, double* out_mdl, ora_stats* stats);
+
 /* entropy::null_mdl_v1 (entropy.cpp:571-585) for a graph with `num_edges` edges. */
 double ora_null_mdl_v1(double num_edges);
 

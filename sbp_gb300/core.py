@@ -32,6 +32,8 @@ class Args:
     threads: int = 1               # accepted for compatibility; the device uses all SMs
     nonparametric: bool = False    # entropy::nonparametric (directed, not degree-corrected)
     seed: int = 0                  # seeds the canonical proposal stream
+    samplesize: float = 1.0        # --samplesize: below 1, partition a sample and extend it (main.cpp:98-140)
+    samplingalg: str = "random"    # --samplingalg: random | max_degree | degree_product
     max_iterations: int = 100      # MAX_NUM_ITERATIONS (include/finetune.hpp:34)
 
     def config(self):
@@ -141,6 +143,19 @@ class Graph:
         self.h = h
         self._bms = weakref.WeakSet()
         self.ctx._graphs.add(self)
+
+    @classmethod
+    def _adopt(cls, handle, ctx):
+        """A Graph object for a graph the library built (edge arrays not kept on the host)."""
+        self = cls.__new__(cls)
+        self.ctx = ctx
+        self.h = handle
+        self._N = int(ctx.lib.sbpgpu_graph_num_vertices(handle))
+        self.src = self.dst = None
+        self._E = int(ctx.lib.sbpgpu_graph_num_edges(handle))
+        self._bms = weakref.WeakSet()
+        ctx._graphs.add(self)
+        return self
 
     @classmethod
     def load(cls, path, undirected=False, ctx=None):

@@ -83,6 +83,16 @@ bool early_stop(int64_t iteration, bool golden, double initial, const std::vecto
     return average < early_threshold(golden, initial);
 }
 
+// finetune::early_stop(iteration, initial_entropy, deltas) (finetune.cpp:285-294), used by
+// finetune_assignment: no zero test, threshold 1e-4.
+bool early_stop_finetune(int64_t iteration, double initial, const std::vector<double>& d) {
+    if (iteration < 3) return false;
+    const size_t last = d.size() - 1;
+    double average = d[last] + d[last - 1] + d[last - 2];
+    average /= -3.0;
+    return average < 1e-4 * initial;
+}
+
 }  // namespace
 
 struct TimedSpan {
@@ -579,6 +589,35 @@ void metropolis_hastings(sbpgpu_bm* bm, const sbpgpu_config& cfg, uint64_t seed,
     bm->entropy = do_mdl(bm, cfg.nonparametric != 0);
 }
 
+// finetune::finetune_assignment (finetune.cpp:903-932): the sequential MH chain over every
+// vertex in id order (draws keyed by step 0xffffffff), stopped by the three-iteration
+// average against 1e-4 of the entropy.
+constexpr uint32_t kFinetuneStep = 0xffffffffu;
+
+void finetune_assignment_impl(sbpgpu_bm* bm, const sbpgpu_config& cfg, uint64_t seed) {
+    sbpgpu_graph* g = bm->g;
+    const bool np = cfg.nonparametric != 0;
+    if (bm->d.B < 2) {
+        bm->entropy = do_mdl(bm, np);
+        return;
+    }
+    bm->entropy = do_mdl(bm, np);
+    int64_t ksum = 0;
+    for (int64_t v = 0; v < g->N; ++v) ksum += g->kdeg[v];
+    std::vector<double> deltas;
+    for (int it = 0; it < cfg.max_iterations; ++it) {
+        chain_run(bm, g->d_all, (int32_t)g->N, g->max_k, ksum, seed, (uint32_t)it, kFinetuneStep, accept_mode(cfg));
+        CK(cudaMemcpyAsync(g->flags_host, g->w.flags_dev, sizeof(DevFlags), cudaMemcpyDeviceToHost, g->ctx->stream));
+        check_flags(g);
+        const double dsum = (double)(long long)g->flags_host->counters[7] * (1.0 / 16777216.0);
+        harvest_counters(g);
+        deltas.push_back(dsum);
+        g->st.mcmc_iterations++;
+        if (early_stop_finetune(it, bm->entropy, deltas)) break;
+    }
+    bm->entropy = do_mdl(bm, np);
+}
+
 void mcmc_impl(sbpgpu_bm* bm, const sbpgpu_config& cfg, uint64_t seed, int32_t step, bool golden) {
     if (cfg.nonparametric) ensure_np(bm->g);
     if (cfg.algorithm == 0 && step < cfg.asynciterations) async_gibbs(bm, cfg, seed, step, golden);
@@ -992,6 +1031,183 @@ sbpgpu_status sbpgpu_graph_load(sbpgpu_ctx* ctx, const char* path, int32_t undir
     if (d_src) cudaFreeAsync(d_src, ctx->stream);
     if (d_dst) cudaFreeAsync(d_dst, ctx->stream);
     return rc2;
+}
+
+sbpgpu_status sbpgpu_sample(sbpgpu_graph* g, int32_t algorithm, double sample_size, uint64_t seed, int32_t* mapping,
+                            int64_t* sample_n) {
+    if (!g || !mapping || !sample_n || algorithm < 0 || algorithm > 3 || !(sample_size > 0.0)) return SBPGPU_EINVAL;
+    return guarded(g->ctx, [&] {
+        cudaStream_t st = g->ctx->stream;
+        std::vector<void*> tmp;
+        int32_t* d_map = dalloc<int32_t>(tmp, g->N);
+        try {
+            *sample_n = sample_vertices(g->dg, algorithm, sample_size, seed, d_map, g->w, st);
+            CK(cudaMemcpyAsync(mapping, d_map, g->N * 4, cudaMemcpyDeviceToHost, st));
+            host_wait(st);
+            CK(cudaGetLastError());
+        } catch (...) {
+            free_all(tmp, st);
+            throw;
+        }
+        free_all(tmp, st);
+        return SBPGPU_OK;
+    });
+}
+
+namespace {
+
+// The sampled subgraph of g for the device mapping d_map (n sampled vertices).
+sbpgpu_graph* make_subgraph(sbpgpu_graph* g, const int32_t* d_map, int64_t n) {
+    cudaStream_t st = g->ctx->stream;
+    int32_t *d_src = nullptr, *d_dst = nullptr;
+    int64_t E2 = 0;
+    subgraph_edges(g->dg, d_map, &d_src, &d_dst, &E2, g->w, st);
+    sbpgpu_graph* sub = nullptr;
+    const sbpgpu_status rc = sbpgpu_graph_create_device(g->ctx, n, E2, d_src, d_dst, &sub);
+    if (d_src) cudaFreeAsync(d_src, st);
+    if (d_dst) cudaFreeAsync(d_dst, st);
+    if (rc != SBPGPU_OK) throw ApiError(rc, std::string("sample graph: ") + sbpgpu_last_error(g->ctx));
+    return sub;
+}
+
+// Checks a host mapping: every entry in [-1, n) and each sample id used exactly once.
+void check_mapping(const sbpgpu_graph* g, const int32_t* mapping, int64_t n) {
+    std::vector<char> seen(n, 0);
+    for (int64_t v = 0; v < g->N; ++v) {
+        const int32_t m = mapping[v];
+        if (m < -1 || m >= n || (m >= 0 && seen[m]++)) throw ApiError(SBPGPU_EINVAL, "invalid sample mapping");
+    }
+    for (int64_t i = 0; i < n; ++i)
+        if (!seen[i]) throw ApiError(SBPGPU_EINVAL, "sample mapping misses a sample id");
+}
+
+}  // namespace
+
+sbpgpu_status sbpgpu_graph_subgraph(sbpgpu_graph* g, const int32_t* mapping, int64_t n, sbpgpu_graph** out) {
+    if (!g || !mapping || !out || n <= 0) return SBPGPU_EINVAL;
+    *out = nullptr;
+    return guarded(g->ctx, [&] {
+        check_mapping(g, mapping, n);
+        cudaStream_t st = g->ctx->stream;
+        std::vector<void*> tmp;
+        int32_t* d_map = dalloc<int32_t>(tmp, g->N);
+        try {
+            CK(cudaMemcpyAsync(d_map, mapping, g->N * 4, cudaMemcpyHostToDevice, st));
+            *out = make_subgraph(g, d_map, n);
+        } catch (...) {
+            free_all(tmp, st);
+            throw;
+        }
+        free_all(tmp, st);
+        return SBPGPU_OK;
+    });
+}
+
+sbpgpu_status sbpgpu_extend(sbpgpu_graph* g, const int32_t* sample_assignment, int64_t sample_n, int64_t num_blocks,
+                            const int32_t* mapping, uint64_t seed, int32_t* out) {
+    if (!g || !sample_assignment || !mapping || !out || sample_n <= 0 || num_blocks <= 0) return SBPGPU_EINVAL;
+    return guarded(g->ctx, [&] {
+        check_mapping(g, mapping, sample_n);
+        for (int64_t i = 0; i < sample_n; ++i)
+            if (sample_assignment[i] < 0 || sample_assignment[i] >= num_blocks)
+                throw ApiError(SBPGPU_EINVAL, "sample assignment out of range");
+        cudaStream_t st = g->ctx->stream;
+        std::vector<void*> tmp;
+        int32_t* d_map = dalloc<int32_t>(tmp, g->N);
+        int32_t* d_sasg = dalloc<int32_t>(tmp, sample_n);
+        int32_t* d_asg = dalloc<int32_t>(tmp, g->N);
+        try {
+            CK(cudaMemcpyAsync(d_map, mapping, g->N * 4, cudaMemcpyHostToDevice, st));
+            CK(cudaMemcpyAsync(d_sasg, sample_assignment, sample_n * 4, cudaMemcpyHostToDevice, st));
+            extend_assignment(g->dg, d_map, d_sasg, (int32_t)num_blocks, g->max_k, seed, d_asg, st);
+            CK(cudaMemcpyAsync(out, d_asg, g->N * 4, cudaMemcpyDeviceToHost, st));
+            host_wait(st);
+            CK(cudaGetLastError());
+        } catch (...) {
+            free_all(tmp, st);
+            throw;
+        }
+        free_all(tmp, st);
+        return SBPGPU_OK;
+    });
+}
+
+sbpgpu_status sbpgpu_finetune_assignment(sbpgpu_bm* bm, const sbpgpu_config* cfg, uint64_t seed,
+                                         sbpgpu_stats* stats) {
+    if (!bm || !cfg) return SBPGPU_EINVAL;
+    sbpgpu_graph* g = bm->g;
+    return guarded(g->ctx, [&] {
+        g->st = sbpgpu_stats{};
+        const int64_t l0 = kernel_launches();
+        reset_counters(g);
+        finetune_assignment_impl(bm, *cfg, seed);
+        harvest_counters(g);
+        g->st.kernel_launches = kernel_launches() - l0;
+        if (stats) *stats = g->st;
+        return SBPGPU_OK;
+    });
+}
+
+sbpgpu_status sbpgpu_sbp_sampled(sbpgpu_graph* g, const sbpgpu_config* cfg, uint64_t seed, int32_t algorithm,
+                                 double sample_size, int32_t* out_assignment, int64_t* num_blocks, double* out_mdl,
+                                 sbpgpu_stats* stats) {
+    if (!g || !cfg || algorithm < 0 || algorithm > 3 || !(sample_size > 0.0)) return SBPGPU_EINVAL;
+    sbpgpu_graph* sub = nullptr;
+    sbpgpu_bm* bm = nullptr;
+    const sbpgpu_status rc = guarded(g->ctx, [&] {
+        cudaStream_t st = g->ctx->stream;
+        const int64_t l0 = kernel_launches();
+        std::vector<void*> tmp;
+        int32_t* d_map = dalloc<int32_t>(tmp, g->N);
+        int32_t* d_asg = dalloc<int32_t>(tmp, g->N);
+        sbpgpu_stats st1{};
+        int64_t B = 0;
+        try {
+            // sample, then the partition of the sample (main.cpp:98-121)
+            const int64_t n = sample_vertices(g->dg, algorithm, sample_size, seed, d_map, g->w, st);
+            if (n <= 0) throw ApiError(SBPGPU_EINVAL, "the sample is empty");
+            sub = make_subgraph(g, d_map, n);
+            std::vector<int32_t> sasg(n);
+            double smdl = 0.0;
+            const sbpgpu_status r1 = sbpgpu_sbp(sub, cfg, seed, sasg.data(), &B, &smdl, &st1);
+            if (r1 != SBPGPU_OK) throw ApiError(r1, std::string("sample partition: ") + sbpgpu_last_error(g->ctx));
+            // extend to the full graph, then finetune_assignment (main.cpp:122-140)
+            int32_t* d_sasg = dalloc<int32_t>(tmp, n);
+            CK(cudaMemcpyAsync(d_sasg, sasg.data(), n * 4, cudaMemcpyHostToDevice, st));
+            extend_assignment(g->dg, d_map, d_sasg, (int32_t)B, g->max_k, seed, d_asg, st);
+            std::vector<int32_t> asg(g->N);
+            CK(cudaMemcpyAsync(asg.data(), d_asg, g->N * 4, cudaMemcpyDeviceToHost, st));
+            host_wait(st);
+            const sbpgpu_status r2 = sbpgpu_bm_create(g, B, asg.data(), &bm);
+            if (r2 != SBPGPU_OK) throw ApiError(r2, std::string("extended blockmodel: ") + sbpgpu_last_error(g->ctx));
+        } catch (...) {
+            free_all(tmp, st);
+            throw;
+        }
+        free_all(tmp, st);
+        g->st = sbpgpu_stats{};
+        reset_counters(g);
+        finetune_assignment_impl(bm, *cfg, seed);
+        harvest_counters(g);
+        if (out_assignment) CK(cudaMemcpyAsync(out_assignment, bm->d.asg, g->N * 4, cudaMemcpyDeviceToHost, st));
+        host_wait(st);
+        if (num_blocks) *num_blocks = B;
+        if (out_mdl) *out_mdl = bm->entropy;
+        if (stats) {
+            sbpgpu_stats s = st1;
+            s.proposals += g->st.proposals;
+            s.moves += g->st.moves;
+            s.mcmc_iterations += g->st.mcmc_iterations;
+            s.edges_swept += g->st.edges_swept;
+            s.chain_rounds += g->st.chain_rounds;
+            s.kernel_launches = kernel_launches() - l0;
+            *stats = s;
+        }
+        return SBPGPU_OK;
+    });
+    if (bm) sbpgpu_bm_destroy(bm);
+    if (sub) sbpgpu_graph_destroy(sub);
+    return rc;
 }
 
 sbpgpu_status sbpgpu_evaluate(sbpgpu_ctx* ctx, int64_t n, const int32_t* truth, const int32_t* assignment,

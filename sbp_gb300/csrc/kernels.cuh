@@ -153,6 +153,19 @@ void allow_max_dynamic_smem(const void* func);
 bool parse_edges_device(const char* d_text, int64_t n, int undirected, int32_t** d_src, int32_t** d_dst, int64_t* E,
                         int64_t* max_id, std::string* err, cudaStream_t st);
 
+// ---- sample.cu
+// Vertex sample (alg 0 max_degree, 1 random, 2 degree_product, 3 detach) into the device
+// array mapping[N] (sample id or -1); returns the sample's size.
+int64_t sample_vertices(const DevGraph& g, int alg, double samplesize, uint64_t seed, int32_t* mapping, Work& w,
+                        cudaStream_t st);
+// Edges between sampled vertices, relabelled, in out-CSR order (cudaMallocAsync'd; the
+// caller frees them).
+void subgraph_edges(const DevGraph& g, const int32_t* mapping, int32_t** d_src, int32_t** d_dst, int64_t* E,
+                    Work& w, cudaStream_t st);
+// sample::extend into asg[N] (device), from the sample's assignment (device).
+void extend_assignment(const DevGraph& g, const int32_t* mapping, const int32_t* sample_asg, int32_t B,
+                       int32_t max_k, uint64_t seed, int32_t* asg, cudaStream_t st);
+
 // ---- evaluate.cu
 struct PartitionQuality {
     double nmi, f1, precision, recall, rand_index, accuracy;

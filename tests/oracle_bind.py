@@ -111,6 +111,20 @@ def lib():
         L.ora_np_merge_delta_mdl.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, f64p, i64p]
         L.ora_bm_nonempty.restype = ctypes.c_int64
         L.ora_bm_nonempty.argtypes = [ctypes.c_void_p]
+        L.ora_sample.restype = ctypes.c_int64
+        L.ora_sample.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_double, ctypes.c_uint64, i32p]
+        L.ora_subgraph.restype = ctypes.c_void_p
+        L.ora_subgraph.argtypes = [ctypes.c_void_p, i32p, ctypes.c_int64]
+        L.ora_graph_num_edges.restype = ctypes.c_int64
+        L.ora_graph_num_edges.argtypes = [ctypes.c_void_p]
+        L.ora_graph_edges.argtypes = [ctypes.c_void_p, i32p, i32p]
+        L.ora_extend.argtypes = [ctypes.c_void_p, i32p, ctypes.c_int64, ctypes.c_int64, i32p, ctypes.c_uint64, i32p]
+        L.ora_finetune_assignment.restype = ctypes.c_int
+        L.ora_finetune_assignment.argtypes = [ctypes.c_void_p, ctypes.POINTER(OraConfig), ctypes.c_uint64,
+                                              ctypes.POINTER(OraStats)]
+        L.ora_sbp_sampled.restype = ctypes.c_int64
+        L.ora_sbp_sampled.argtypes = [ctypes.c_void_p, ctypes.POINTER(OraConfig), ctypes.c_uint64, ctypes.c_int32,
+                                      ctypes.c_double, i32p, f64p, ctypes.POINTER(OraStats)]
         L.ora_null_mdl_v1.restype = ctypes.c_double
         L.ora_null_mdl_v1.argtypes = [ctypes.c_double]
         _lib = L
@@ -141,6 +155,44 @@ class Graph:
         if getattr(self, "h", None):
             lib().ora_graph_destroy(self.h)
             self.h = None
+
+
+SAMPLERS = {"max_degree": 0, "random": 1, "degree_product": 2, "detach": 3}
+
+
+def sample(graph, algorithm, sample_size, seed):
+    m = np.zeros(graph.N, np.int32)
+    n = int(lib().ora_sample(graph.h, SAMPLERS[algorithm], float(sample_size), seed, _p(m, i32p)))
+    return m, n
+
+
+def subgraph_edges(graph, mapping):
+    m = np.ascontiguousarray(mapping, dtype=np.int32)
+    n = int((m >= 0).sum())
+    h = lib().ora_subgraph(graph.h, _p(m, i32p), n)
+    E = int(lib().ora_graph_num_edges(h))
+    src, dst = np.zeros(E, np.int32), np.zeros(E, np.int32)
+    lib().ora_graph_edges(h, _p(src, i32p), _p(dst, i32p))
+    lib().ora_graph_destroy(h)
+    return n, src, dst
+
+
+def extend(graph, sample_assignment, num_blocks, mapping, seed):
+    a = np.ascontiguousarray(sample_assignment, dtype=np.int32)
+    m = np.ascontiguousarray(mapping, dtype=np.int32)
+    out = np.zeros(graph.N, np.int32)
+    lib().ora_extend(graph.h, _p(a, i32p), a.size, int(num_blocks), _p(m, i32p), seed, _p(out, i32p))
+    return out
+
+
+def sbp_sampled(graph, cfg, seed, algorithm, sample_size):
+    out = np.zeros(graph.N, np.int32)
+    mdl = ctypes.c_double()
+    st = OraStats()
+    B = lib().ora_sbp_sampled(graph.h, ctypes.byref(cfg), seed, SAMPLERS[algorithm], float(sample_size),
+                              _p(out, i32p), ctypes.byref(mdl), ctypes.byref(st))
+    assert B > 0, B
+    return out, int(B), mdl.value, st
 
 
 class Blockmodel:
@@ -255,6 +307,11 @@ class Blockmodel:
         rc = lib().ora_mcmc(self.h, ctypes.byref(cfg), seed, step, int(golden_ratio_not_reached),
                             ctypes.byref(st))
         assert rc == 0
+        return st
+
+    def finetune_assignment(self, cfg, seed):
+        st = OraStats()
+        assert lib().ora_finetune_assignment(self.h, ctypes.byref(cfg), seed, ctypes.byref(st)) == 0
         return st
 
     def merge_blocks(self, cfg, seed, step, num_to_merge):

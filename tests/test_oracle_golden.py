@@ -282,3 +282,52 @@ def test_np_sbp_recovers_planted_blocks(oracle):
     asg, B, mdl, st = oracle.sbp(g, oracle.make_config("hybrid_mcmc", nonparametric=True), seed=1)
     assert B > 1
     assert evaluate.nmi(planted, asg) > 0.6
+
+
+# ---- sampling (sample.cpp) and the sampled partition (main.cpp:98-140)
+
+def test_oracle_samplers(oracle):
+    from sbp_gb300 import dcsbm
+    src, dst, _ = dcsbm.generate(500, 4000, 5, seed=11)
+    g = oracle.Graph(500, src, dst)
+    deg = np.bincount(src, minlength=500) + np.bincount(dst, minlength=500)
+    deg -= np.bincount(src[src == dst], minlength=500) > 0
+    for alg in ("max_degree", "random", "degree_product"):
+        m, n = oracle.sample(g, alg, 0.3, 5)
+        assert sorted(m[m >= 0].tolist()) == list(range(n))
+        assert n >= 150 if alg == "degree_product" else n == 150
+    m, n = oracle.sample(g, "max_degree", 0.3, 5)
+    order = np.argsort(-deg, kind="stable")  # utils::argsort: stable, descending
+    assert np.array_equal(np.flatnonzero(m >= 0), np.sort(order[:150]))
+    assert all(m[order[i]] == i for i in range(150))
+    m, n = oracle.sample(g, "detach", 1.0, 0)
+    assert np.array_equal(m >= 0, deg > 1)
+    # from_vertices keeps the edges between sampled vertices, each source's out-neighbours
+    # in their original order (the sample graph lists them by sample id)
+    m, n = oracle.sample(g, "random", 0.5, 3)
+    n2, s2, d2 = oracle.subgraph_edges(g, m)
+    keep = np.flatnonzero((m[src] >= 0) & (m[dst] >= 0))
+    keep = keep[np.argsort(m[src[keep]], kind="stable")]
+    want = [(int(m[src[i]]), int(m[dst[i]])) for i in keep]
+    assert n2 == n and list(zip(s2.tolist(), d2.tolist())) == want
+
+
+def test_oracle_extend_rules(oracle):
+    # vertex 2 has neighbours in blocks 1, 1, 0: it takes block 1; vertex 4 then follows
+    # vertex 2 (already assigned, id order); vertex 5 has no neighbours: a drawn block
+    src = np.array([0, 1, 3, 2, 4, 2], np.int32)
+    dst = np.array([2, 2, 2, 4, 0, 0], np.int32)
+    g = oracle.Graph(6, src, dst)
+    mapping = np.array([0, 1, -1, 2, -1, -1], np.int32)
+    asg = oracle.extend(g, [1, 1, 0], 3, mapping, 9)
+    assert asg[:5].tolist() == [1, 1, 1, 0, 1]
+    assert 0 <= asg[5] < 3
+
+
+def test_oracle_sampled_partition(oracle):
+    from sbp_gb300 import dcsbm, evaluate
+    src, dst, planted = dcsbm.generate_config("C1", seed=0)
+    g = oracle.Graph(1000, src, dst)
+    asg, B, mdl, st = oracle.sbp_sampled(g, oracle.make_config("hybrid_mcmc"), 1, "max_degree", 0.5)
+    assert B > 1 and asg.max() < B
+    assert evaluate.nmi(planted, asg) > 0.6
