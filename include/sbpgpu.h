@@ -214,6 +214,20 @@ sbpgpu_status sbpgpu_sbp_sampled(sbpgpu_graph* g, const sbpgpu_config* cfg, uint
                                  double sample_size, int32_t* out_assignment, int64_t* num_blocks,
                                  double* out_mdl, sbpgpu_stats* stats);
 
+/* ---- top-down (divisive) partitioning (src/top_down_sbp.cpp) --------------------- */
+/* divisive::split_communities (top_down_sbp.cpp:472-530) with --split random: every cluster
+ * of at least 0.001 N vertices gets 10 random two-way splits scored by the nonparametric
+ * description length of its subgraph against entropy::null_mdl_v1; the clusters are split
+ * in ascending order of their best delta until the block count reaches the target. */
+sbpgpu_status sbpgpu_split_communities(sbpgpu_bm* bm, const sbpgpu_config* cfg, uint64_t seed, int32_t step,
+                                       int64_t target_num_blocks);
+/* divisive::run (top_down_sbp.cpp:435-470, without --mix): from one block, split toward
+ * ceil(1.5 B) blocks and finetune until the golden-section bracket of
+ * TopDownBlockmodelTriplet closes. */
+sbpgpu_status sbpgpu_sbp_top_down(sbpgpu_graph* g, const sbpgpu_config* cfg, uint64_t seed,
+                                  int32_t* out_assignment, int64_t* num_blocks, double* out_mdl,
+                                  sbpgpu_stats* stats);
+
 /* ---- evaluation ------------------------------------------------------------------ */
 /* evaluate::evaluate_blockmodel (src/evaluate.cpp:9-180) against a true partition: the
  * contingency table is counted on the device; NMI (float-log marginal entropies as the

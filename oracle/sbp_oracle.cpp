@@ -15,6 +15,10 @@
  *   random sample         : shuffle with ctr = (position, 0, 0, DOM_SAMPLE = 6)
  *   extend, random block  : ctr = (vertex, 0, 0, DOM_EXTEND = 7), block = u32_below(w[0], B)
  *   finetune_assignment   : MH draws with step = 0xffffffff
+ *   top-down split size   : ctr = (cluster, proposal, step, DOM_SPLIT_SIZE = 8),
+ *                           size = lo + u64_below(w[0], w[1], hi - lo + 1)
+ *   top-down split side   : ctr = (vertex, proposal, step, DOM_SPLIT_SIDE = 9),
+ *                           side 0 iff w[0] * n < size * 2^32
  *   u32_below(w, n) = (w * n) >> 32;  u64_below(hi, lo, n) = ((hi:lo) * n) >> 64.
  *   Multinomials over a block's neighbour weights enumerate the row part (ascending
  *   column) and then the column part (ascending row), the same concatenation the
@@ -43,7 +47,7 @@ namespace {
 
 enum : uint32_t {
     DOM_GIBBS = 1, DOM_MH = 2, DOM_MERGE = 3, DOM_SHUFFLE_HDV = 4, DOM_SHUFFLE_ALL = 5, DOM_SAMPLE = 6,
-    DOM_EXTEND = 7,
+    DOM_EXTEND = 7, DOM_SPLIT_SIZE = 8, DOM_SPLIT_SIDE = 9,
 };
 
 // ---------------------------------------------------------------- Philox4x32-10
@@ -1536,6 +1540,186 @@ extern "C" int64_t ora_sbp_sampled(const ora_graph* g, const ora_config* cfg, ui
     if (out_mdl) *out_mdl = bm->entropy;
     delete bm;
     return B;
+}
+
+// ---------------------------------------------------------------- top-down (divisive) SBP
+namespace {
+
+/* The random split of a cluster of n vertices (propose_random_split, top_down_sbp.cpp:
+ * 248-260): the size of side 0 uniform in [long(0.2 n), long(0.8 n)], then each vertex on
+ * side 0 with probability size / n. */
+inline int64_t split_size(uint64_t seed, int64_t cluster, int32_t i, uint32_t step, int64_t n) {
+    const int64_t lo = (int64_t)((double)n * 0.2), hi = (int64_t)((double)n * 0.8);
+    uint32_t w[4];
+    draw(seed, (uint32_t)cluster, (uint32_t)i, step, DOM_SPLIT_SIZE, w);
+    return lo + (int64_t)u64_below(w[0], w[1], (uint64_t)(hi - lo + 1));
+}
+inline int split_side(uint64_t seed, int64_t v, int32_t i, uint32_t step, int64_t size, int64_t n) {
+    uint32_t w[4];
+    draw(seed, (uint32_t)v, (uint32_t)i, step, DOM_SPLIT_SIDE, w);
+    return (uint64_t)w[0] * (uint64_t)n < ((uint64_t)size << 32) ? 0 : 1;
+}
+
+/* nonparametric::mdl (entropy.cpp:751-779) of a two-block model of a subgraph with n
+ * vertices and E edges: sizes[2], cells M[2][2] (row-major).  The canonical form. */
+double np_mdl_two_blocks(const ora_graph* g, int64_t n, int64_t E, const int64_t sizes[2], const int64_t M[4]) {
+    int64_t fixed = 0;
+    for (int k = 0; k < 4; ++k) fixed -= g->LG[M[k]];
+    for (int b = 0; b < 2; ++b) {
+        const int64_t dout = M[2 * b] + M[2 * b + 1], din = M[b] + M[2 + b];
+        fixed += np_vterm(g, dout, din, sizes[b]) - g->LG[sizes[b]];
+    }
+    fixed += g->LG[n] + g->Lq[n];
+    const int64_t ne = (sizes[0] > 0) + (sizes[1] > 0);
+    return (double)fixed * kInvFix + (np_lbinom(n - 1, ne - 1) + np_edges_dl(ne, E));
+}
+
+/* entropy::null_mdl_v1 (entropy.cpp:571-585) of a subgraph: the one-block nonparametric
+ * MDL under --nonparametric, else the parametric formula. */
+double split_null_mdl(const ora_graph* g, int64_t n, int64_t E, bool nonparametric) {
+    if (nonparametric) {
+        const int64_t sizes[2] = {n, 0}, M[4] = {E, 0, 0, 0};
+        return np_mdl_two_blocks(g, n, E, sizes, M);
+    }
+    const double e = (double)E;
+    const double log_posterior_p = e * log(1.0 / e);
+    const double x = 1.0 / e;
+    const double h = ((1 + x) * log(1 + x)) - (x * log(x));
+    return (e * h) - log_posterior_p;
+}
+
+/* divisive::split_communities (top_down_sbp.cpp:472-530) with random splits and
+ * apply_best_splits (:30-65). */
+void split_communities(ora_bm* bm, const ora_config* cfg, uint64_t seed, uint32_t step, int64_t target) {
+    const ora_graph* g = bm->g;
+    const int64_t B = bm->B, N = g->N;
+    std::vector<std::vector<int32_t>> members(B);
+    for (int64_t v = 0; v < N; ++v) members[bm->asg[v]].push_back((int32_t)v);
+    std::vector<double> best(B, DBL_MAX);
+    std::vector<int32_t> best_i(B, -1);
+    std::vector<int64_t> split_n(B, INT64_MAX);  // Split::num_vertices; unset splits are skipped
+    std::vector<int64_t> sizes_of(B * 10, 0);
+    for (int64_t c = 0; c < B; ++c) {
+        const int64_t n = (int64_t)members[c].size();
+        if ((double)n < 0.001 * (double)N) continue;  // do not split small clusters
+        int64_t E = 0;
+        for (int32_t u : members[c])
+            for (int32_t v : g->out[u]) E += bm->asg[v] == c;
+        const double old_entropy = split_null_mdl(g, n, E, cfg->nonparametric != 0);
+        for (int32_t i = 0; i < 10; ++i) {  // NUM_AGG_PROPOSALS_PER_BLOCK
+            const int64_t size = n < 2 ? n : split_size(seed, c, i, step, n);
+            int64_t sizes[2] = {0, 0}, M[4] = {0, 0, 0, 0};
+            auto side = [&](int32_t v) { return n < 2 ? 0 : split_side(seed, v, i, step, size, n); };
+            for (int32_t u : members[c]) {
+                sizes[side(u)]++;
+                for (int32_t v : g->out[u])
+                    if (bm->asg[v] == c) M[2 * side(u) + side(v)]++;
+            }
+            const double delta = np_mdl_two_blocks(g, n, E, sizes, M) - old_entropy;
+            if (delta < best[c]) {
+                best[c] = delta;
+                best_i[c] = i;
+                split_n[c] = n;
+            }
+        }
+    }
+    // apply_best_splits: ascending delta (utils::argsort is a stable descending sort, walked
+    // from its end)
+    std::vector<int64_t> order(B);
+    for (int64_t c = 0; c < B; ++c) order[c] = c;
+    std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t b) { return best[a] > best[b]; });
+    int64_t num_blocks = B;
+    for (int64_t k = B - 1; k >= 0; --k) {
+        const int64_t c = order[k];
+        if (split_n[c] > N) continue;
+        const int64_t n = split_n[c];
+        const int32_t i = best_i[c];
+        const int64_t size = n < 2 ? n : split_size(seed, c, i, step, n);
+        for (int32_t v : members[c])
+            if (n >= 2 && split_side(seed, v, i, step, size, n) == 1) bm->asg[v] = (int32_t)num_blocks;
+        num_blocks++;
+        if (num_blocks >= target) break;
+    }
+    bm->B = num_blocks;
+    build(bm);
+}
+
+/* TopDownBlockmodelTriplet (blockmodel_triplet.cpp:107-193). */
+struct TDTriplet {
+    Slot s[3];
+    bool optimal = false;
+    bool golden_ratio_not_reached() const { return s[2].empty; }
+    void update(const ora_bm* bm) {
+        int idx;
+        if (s[1].empty) {
+            idx = 1;
+        } else if (bm->entropy <= s[1].entropy && std::labs(bm->B - s[1].B) > 0.1 * (double)s[1].B) {
+            const int old = s[1].B < bm->B ? 0 : 2;
+            s[old] = s[1];
+            idx = 1;
+        } else {
+            idx = s[1].B < bm->B ? 2 : 0;
+        }
+        s[idx].empty = false;
+        s[idx].B = bm->B;
+        s[idx].entropy = bm->entropy;
+        s[idx].asg = bm->asg;
+    }
+    bool is_done() {
+        if ((!s[0].empty && s[2].B - s[0].B <= 2) || (s[0].empty && s[2].B - s[1].B <= 1)) optimal = true;
+        return optimal;
+    }
+};
+
+}  // namespace
+
+/* divisive::run (top_down_sbp.cpp:435-470) without --mix: from one block, split toward
+ * ceil(1.5 B) blocks until the golden-section bracket closes, finetuning after each split. */
+extern "C" int64_t ora_top_down(const ora_graph* g, const ora_config* cfg, uint64_t seed, int32_t* out_asg,
+                                double* out_mdl, ora_stats* st) {
+    std::vector<int32_t> zeros(g->N, 0);
+    ora_bm* bm = ora_bm_create(g, 1, zeros.data());
+    bm->entropy = DBL_MAX;
+    TDTriplet t;
+    uint32_t step = 0;
+    auto next = [&](ora_bm* cur, int64_t* target) -> const Slot* {
+        t.update(cur);
+        if (t.golden_ratio_not_reached()) {
+            *target = (int64_t)ceil((double)t.s[1].B * 1.5);
+            if (*target == 0 || *target >= g->N) t.optimal = true;
+            return &t.s[1];
+        }
+        if (t.is_done()) return &t.s[1];
+        int index;
+        if (t.s[0].empty && t.s[1].B < t.s[2].B) index = 1;
+        else if ((t.s[1].B - t.s[0].B) <= (t.s[2].B - t.s[1].B)) index = 1;
+        else index = 0;
+        *target = t.s[index + 1].B + (int64_t)((double)(t.s[index].B - t.s[index + 1].B) * 0.618);
+        return &t.s[index];
+    };
+    int64_t target = 0;
+    const Slot* src = next(bm, &target);
+    while (!t.optimal) {
+        delete bm;
+        bm = ora_bm_create(g, src->B, src->asg.data());
+        bm->entropy = src->entropy;
+        split_communities(bm, cfg, seed, step, target);
+        mcmc(bm, cfg, seed, (int32_t)step, t.golden_ratio_not_reached(), st);
+        ++step;
+        if (st) st->outer_steps++;
+        src = next(bm, &target);
+    }
+    const int64_t B = src->B;
+    if (out_asg) std::copy(src->asg.begin(), src->asg.end(), out_asg);
+    if (out_mdl) *out_mdl = src->entropy;
+    delete bm;
+    return B;
+}
+
+extern "C" int ora_split_communities(ora_bm* bm, const ora_config* cfg, uint64_t seed, uint32_t step,
+                                     int64_t target) {
+    split_communities(bm, cfg, seed, step, target);
+    return 0;
 }
 
 extern "C" double ora_null_mdl_v1(double E) {

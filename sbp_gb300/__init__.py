@@ -6,7 +6,7 @@ the reference's API names: Graph, Blockmodel, Args and the entropy / finetune /
 block_merge / sbp namespaces.  The compute path is libsbpgpu.so (hand-written CUDA,
 include/sbpgpu.h); there is no CPU fallback.
 """
-from . import block_merge, dcsbm, entropy, evaluate, finetune, sample, sbp, serve
+from . import block_merge, dcsbm, divisive, entropy, evaluate, finetune, sample, sbp, serve
 from ._lib import SbpGpuError, load
 from .core import Args, Blockmodel, Context, Graph, default_context
 

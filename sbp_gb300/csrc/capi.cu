@@ -185,6 +185,7 @@ struct sbpgpu_graph {
     int32_t n_hdv = 0, n_ldv = 0, max_k_hdv = 0;
     int64_t hdv_k_sum = 0;
     long long np_lg_N = 0;  // lgamma(N + 1) in units of 2^-24 (nonparametric partition term)
+    std::vector<long long> np_lg;  // host copy of the lgamma table
     sbpgpu_stats st{};
 };
 
@@ -339,6 +340,7 @@ void ensure_np(sbpgpu_graph* g) {
     g->dg.Dm = d_Dm;
     g->dg.Dp = d_Dp;
     g->np_lg_N = LG[N];
+    g->np_lg = std::move(LG);
 }
 
 void ensure_split(sbpgpu_graph* g, float mh_percent) {
@@ -618,6 +620,117 @@ void finetune_assignment_impl(sbpgpu_bm* bm, const sbpgpu_config& cfg, uint64_t 
     bm->entropy = do_mdl(bm, np);
 }
 
+void free_all(std::vector<void*>& owned, cudaStream_t st) {
+    for (void* p : owned) cudaFreeAsync(p, st);
+    owned.clear();
+}
+
+// fastlog(x) in units of 2^-24 (the Lq table's values).
+long long lq_of(int64_t x) { return x <= 0 ? 0 : (long long)(int32_t)((double)logf((float)x) * 16777216.0); }
+
+// nonparametric::mdl (entropy.cpp:751-779) of a two-block model of a subgraph of n vertices
+// and E edges (sizes, row-major cells M), in the canonical arithmetic of the device deltas.
+double np_mdl_two_blocks(const sbpgpu_graph* g, int64_t n, int64_t E, const int64_t sizes[2], const int64_t M[4]) {
+    const std::vector<long long>& LG = g->np_lg;
+    long long fixed = 0;
+    for (int k = 0; k < 4; ++k) fixed -= LG[M[k]];
+    for (int b = 0; b < 2; ++b) {
+        const int64_t dout = M[2 * b] + M[2 * b + 1], din = M[b] + M[2 + b];
+        fixed += (sizes[b] == 0 ? 0 : (dout + din) * lq_of(sizes[b])) - LG[sizes[b]];
+    }
+    fixed += LG[n] + lq_of(n);
+    const int64_t ne = (sizes[0] > 0) + (sizes[1] > 0);
+    return (double)fixed * (1.0 / 16777216.0) + (np_lbinom(n - 1, ne - 1) + np_edges_dl(ne, E));
+}
+
+// entropy::null_mdl_v1 (entropy.cpp:571-585) of a subgraph: the one-block nonparametric MDL
+// under --nonparametric, else the parametric formula.
+double split_null_mdl(const sbpgpu_graph* g, int64_t n, int64_t E, bool np) {
+    if (np) {
+        const int64_t sizes[2] = {n, 0}, M[4] = {E, 0, 0, 0};
+        return np_mdl_two_blocks(g, n, E, sizes, M);
+    }
+    const double e = (double)E;
+    const double log_posterior_p = e * log(1.0 / e);
+    const double x = 1.0 / e;
+    const double h = ((1 + x) * log(1 + x)) - (x * log(x));
+    return (e * h) - log_posterior_p;
+}
+
+// divisive::split_communities (top_down_sbp.cpp:472-530) with random splits, then
+// apply_best_splits (:30-65): the clusters in ascending order of their best split's
+// delta are split until the block count reaches `target`.
+void split_impl(sbpgpu_bm* bm, const sbpgpu_config& cfg, uint64_t seed, uint32_t step, int64_t target) {
+    sbpgpu_graph* g = bm->g;
+    ensure_np(g);
+    cudaStream_t st = g->ctx->stream;
+    const int64_t B = bm->d.B, N = g->N, P = 10;
+    std::vector<void*> tmp;
+    SplitBuffers b{};
+    b.split_size = dalloc<long long>(tmp, B * P);
+    b.eligible = dalloc<int32_t>(tmp, B);
+    b.mask = dalloc<uint16_t>(tmp, N);
+    b.n1 = dalloc<int32_t>(tmp, B * P);
+    b.cells = dalloc<int32_t>(tmp, B * P * 4);
+    b.ecount = dalloc<unsigned long long>(tmp, B);
+    b.new_block = dalloc<int32_t>(tmp, B);
+    b.proposal = dalloc<int32_t>(tmp, B);
+    try {
+        split_count(g->dg, bm->d, seed, step, b, st);
+        std::vector<int32_t> n1(B * P), cells(B * P * 4), elig(B), sizes(B);
+        std::vector<unsigned long long> ecount(B);
+        CK(cudaMemcpyAsync(n1.data(), b.n1, n1.size() * 4, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(cells.data(), b.cells, cells.size() * 4, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(elig.data(), b.eligible, B * 4, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(sizes.data(), bm->d.sizes, B * 4, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(ecount.data(), b.ecount, B * 8, cudaMemcpyDeviceToHost, st));
+        host_wait(st);
+        CK(cudaGetLastError());
+        std::vector<double> best(B, DBL_MAX);
+        std::vector<int32_t> best_i(B, -1);
+        for (int64_t c = 0; c < B; ++c) {
+            if (!elig[c]) continue;
+            const int64_t n = sizes[c], E = (int64_t)ecount[c];
+            const double old_entropy = split_null_mdl(g, n, E, cfg.nonparametric != 0);
+            for (int64_t i = 0; i < P; ++i) {
+                const int64_t s2[2] = {n - n1[c * P + i], n1[c * P + i]};
+                int64_t M[4];
+                for (int k = 0; k < 4; ++k) M[k] = cells[(c * P + i) * 4 + k];
+                const double delta = np_mdl_two_blocks(g, n, E, s2, M) - old_entropy;
+                if (delta < best[c]) {
+                    best[c] = delta;
+                    best_i[c] = (int32_t)i;
+                }
+            }
+        }
+        // utils::argsort<double> is a stable descending sort; apply_best_splits walks it from the end
+        std::vector<int64_t> order(B);
+        for (int64_t c = 0; c < B; ++c) order[c] = c;
+        std::stable_sort(order.begin(), order.end(), [&](int64_t x, int64_t y) { return best[x] > best[y]; });
+        std::vector<int32_t> new_block(B, -1), prop(B, 0);
+        int64_t num_blocks = B;
+        for (int64_t k = B - 1; k >= 0; --k) {
+            const int64_t c = order[k];
+            if (best_i[c] < 0) continue;  // no split was proposed (small cluster)
+            new_block[c] = (int32_t)num_blocks;
+            prop[c] = best_i[c];
+            num_blocks++;
+            if (num_blocks >= target) break;
+        }
+        if (num_blocks > N) throw ApiError(SBPGPU_EINVAL, "splits would exceed one block per vertex");
+        CK(cudaMemcpyAsync(b.new_block, new_block.data(), B * 4, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(b.proposal, prop.data(), B * 4, cudaMemcpyHostToDevice, st));
+        split_apply(g->dg, bm->d, b, st);
+        host_wait(st);
+        bm->d.B = (int32_t)num_blocks;
+    } catch (...) {
+        free_all(tmp, st);
+        throw;
+    }
+    free_all(tmp, st);
+    do_rebuild(bm);
+}
+
 void mcmc_impl(sbpgpu_bm* bm, const sbpgpu_config& cfg, uint64_t seed, int32_t step, bool golden) {
     if (cfg.nonparametric) ensure_np(bm->g);
     if (cfg.algorithm == 0 && step < cfg.asynciterations) async_gibbs(bm, cfg, seed, step, golden);
@@ -748,11 +861,6 @@ sbpgpu_bm* new_bm(sbpgpu_graph* g, int64_t B) {
     d.col_cum = dalloc<int32_t>(o, E);
     d.nonempty = dalloc<int32_t>(o, 1);
     return bm;
-}
-
-void free_all(std::vector<void*>& owned, cudaStream_t st) {
-    for (void* p : owned) cudaFreeAsync(p, st);
-    owned.clear();
 }
 
 // Destruction is reference counted so that handles may be destroyed in any order: a
@@ -1660,6 +1768,105 @@ sbpgpu_status sbpgpu_sbp(sbpgpu_graph* g, const sbpgpu_config* cfg_in, uint64_t 
         harvest_counters(g);
         if (num_blocks) *num_blocks = bm->d.B;
         if (out_mdl) *out_mdl = bm->entropy;
+        g->st.kernel_launches = kernel_launches() - l0;
+        if (stats) *stats = g->st;
+        return SBPGPU_OK;
+    });
+    free_all(slots_mem, ctx->stream);
+    if (bm) {
+        free_all(bm->owned, bm->g->ctx->stream);
+        delete bm;
+    }
+    return rc;
+}
+
+sbpgpu_status sbpgpu_split_communities(sbpgpu_bm* bm, const sbpgpu_config* cfg, uint64_t seed, int32_t step,
+                                       int64_t target_num_blocks) {
+    if (!bm || !cfg || target_num_blocks < 1) return SBPGPU_EINVAL;
+    sbpgpu_graph* g = bm->g;
+    return guarded(g->ctx, [&] {
+        if (target_num_blocks > g->N) throw ApiError(SBPGPU_EINVAL, "target above one block per vertex");
+        split_impl(bm, *cfg, seed, (uint32_t)step, target_num_blocks);
+        return SBPGPU_OK;
+    });
+}
+
+sbpgpu_status sbpgpu_sbp_top_down(sbpgpu_graph* g, const sbpgpu_config* cfg_in, uint64_t seed,
+                                  int32_t* out_assignment, int64_t* num_blocks, double* out_mdl,
+                                  sbpgpu_stats* stats) {
+    if (!g || !cfg_in) return SBPGPU_EINVAL;
+    sbpgpu_ctx* ctx = g->ctx;
+    sbpgpu_bm* bm = nullptr;
+    std::vector<void*> slots_mem;
+    const sbpgpu_status rc = guarded(ctx, [&] {
+        const sbpgpu_config cfg = *cfg_in;
+        g->st = sbpgpu_stats{};
+        const int64_t l0 = kernel_launches();
+        reset_counters(g);
+        cudaStream_t st = ctx->stream;
+        const int64_t N = g->N;
+        // Blockmodel(1, graph, 1.5, zeros) (top_down_sbp.cpp:440-442)
+        bm = new_bm(g, N);
+        CK(cudaMemsetAsync(bm->d.asg, 0, N * 4, st));
+        bm->d.B = 1;
+        do_rebuild(bm);
+        bm->entropy = DBL_MAX;
+        struct Slot {
+            bool empty = true;
+            int64_t B = 0;
+            double entropy = DBL_MAX;
+            int32_t* asg = nullptr;
+        } s[3];
+        for (auto& sl : s) sl.asg = dalloc<int32_t>(slots_mem, N);
+        bool optimal = false;
+        // TopDownBlockmodelTriplet::update and get_next_blockmodel (blockmodel_triplet.cpp:107-193)
+        auto next = [&](int64_t* target) -> const Slot* {
+            int idx;
+            if (s[1].empty) {
+                idx = 1;
+            } else if (bm->entropy <= s[1].entropy && std::labs(bm->d.B - s[1].B) > 0.1 * (double)s[1].B) {
+                const int old = s[1].B < bm->d.B ? 0 : 2;
+                std::swap(s[old], s[1]);
+                idx = 1;
+            } else {
+                idx = s[1].B < bm->d.B ? 2 : 0;
+            }
+            s[idx].empty = false;
+            s[idx].B = bm->d.B;
+            s[idx].entropy = bm->entropy;
+            CK(cudaMemcpyAsync(s[idx].asg, bm->d.asg, N * 4, cudaMemcpyDeviceToDevice, st));
+            if (s[2].empty) {
+                *target = (int64_t)ceil((double)s[1].B * 1.5);
+                if (*target == 0 || *target >= N) optimal = true;
+                return &s[1];
+            }
+            if ((!s[0].empty && s[2].B - s[0].B <= 2) || (s[0].empty && s[2].B - s[1].B <= 1)) optimal = true;
+            if (optimal) return &s[1];
+            int index;
+            if (s[0].empty && s[1].B < s[2].B) index = 1;
+            else if ((s[1].B - s[0].B) <= (s[2].B - s[1].B)) index = 1;
+            else index = 0;
+            *target = s[index + 1].B + (int64_t)((double)(s[index].B - s[index + 1].B) * 0.618);
+            return &s[index];
+        };
+        int64_t target = 0;
+        int32_t step = 0;
+        const Slot* src = next(&target);
+        while (!optimal) {
+            CK(cudaMemcpyAsync(bm->d.asg, src->asg, N * 4, cudaMemcpyDeviceToDevice, st));
+            bm->d.B = (int32_t)src->B;
+            bm->entropy = src->entropy;
+            do_rebuild(bm);
+            split_impl(bm, cfg, seed, (uint32_t)step, target);
+            mcmc_impl(bm, cfg, seed, step, s[2].empty);
+            ++step;
+            g->st.outer_steps++;
+            src = next(&target);
+        }
+        if (out_assignment) CK(cudaMemcpyAsync(out_assignment, src->asg, N * 4, cudaMemcpyDeviceToHost, st));
+        harvest_counters(g);
+        if (num_blocks) *num_blocks = src->B;
+        if (out_mdl) *out_mdl = src->entropy;
         g->st.kernel_launches = kernel_launches() - l0;
         if (stats) *stats = g->st;
         return SBPGPU_OK;

@@ -166,6 +166,24 @@ void subgraph_edges(const DevGraph& g, const int32_t* mapping, int32_t** d_src, 
 void extend_assignment(const DevGraph& g, const int32_t* mapping, const int32_t* sample_asg, int32_t B,
                        int32_t max_k, uint64_t seed, int32_t* asg, cudaStream_t st);
 
+// ---- split.cu
+// Buffers of one split pass over B clusters (10 proposals each) and N vertices.
+struct SplitBuffers {
+    long long* split_size;       // [B * 10] side-0 size, or -1 when the cluster is not split
+    int32_t* eligible;           // [B] cluster of at least 0.001 N vertices
+    uint16_t* mask;              // [N] bit i: the vertex's side in proposal i
+    int32_t* n1;                 // [B * 10] vertices on side 1
+    int32_t* cells;              // [B * 10 * 4] 2 x 2 blockmatrix of the cluster's edges
+    unsigned long long* ecount;  // [B] edges inside the cluster
+    int32_t* new_block;          // [B] block receiving the cluster's side 1, or -1
+    int32_t* proposal;           // [B] the proposal applied
+};
+// Counts every cluster's 10 random two-way splits (divisive::split_communities,
+// top_down_sbp.cpp:472-530; propose_random_split :248-260).
+void split_count(const DevGraph& g, const DevBM& bm, uint64_t seed, uint32_t step, SplitBuffers& b, cudaStream_t st);
+// Moves side-1 vertices of the chosen clusters into their new blocks (apply_best_splits).
+void split_apply(const DevGraph& g, DevBM& bm, const SplitBuffers& b, cudaStream_t st);
+
 // ---- evaluate.cu
 struct PartitionQuality {
     double nmi, f1, precision, recall, rand_index, accuracy;

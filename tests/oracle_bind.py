@@ -125,6 +125,12 @@ def lib():
         L.ora_sbp_sampled.restype = ctypes.c_int64
         L.ora_sbp_sampled.argtypes = [ctypes.c_void_p, ctypes.POINTER(OraConfig), ctypes.c_uint64, ctypes.c_int32,
                                       ctypes.c_double, i32p, f64p, ctypes.POINTER(OraStats)]
+        L.ora_split_communities.restype = ctypes.c_int
+        L.ora_split_communities.argtypes = [ctypes.c_void_p, ctypes.POINTER(OraConfig), ctypes.c_uint64,
+                                            ctypes.c_uint32, ctypes.c_int64]
+        L.ora_top_down.restype = ctypes.c_int64
+        L.ora_top_down.argtypes = [ctypes.c_void_p, ctypes.POINTER(OraConfig), ctypes.c_uint64, i32p, f64p,
+                                   ctypes.POINTER(OraStats)]
         L.ora_null_mdl_v1.restype = ctypes.c_double
         L.ora_null_mdl_v1.argtypes = [ctypes.c_double]
         _lib = L
@@ -191,6 +197,15 @@ def sbp_sampled(graph, cfg, seed, algorithm, sample_size):
     st = OraStats()
     B = lib().ora_sbp_sampled(graph.h, ctypes.byref(cfg), seed, SAMPLERS[algorithm], float(sample_size),
                               _p(out, i32p), ctypes.byref(mdl), ctypes.byref(st))
+    assert B > 0, B
+    return out, int(B), mdl.value, st
+
+
+def top_down(graph, cfg, seed):
+    out = np.zeros(graph.N, np.int32)
+    mdl = ctypes.c_double()
+    st = OraStats()
+    B = lib().ora_top_down(graph.h, ctypes.byref(cfg), seed, _p(out, i32p), ctypes.byref(mdl), ctypes.byref(st))
     assert B > 0, B
     return out, int(B), mdl.value, st
 
@@ -313,6 +328,9 @@ class Blockmodel:
         st = OraStats()
         assert lib().ora_finetune_assignment(self.h, ctypes.byref(cfg), seed, ctypes.byref(st)) == 0
         return st
+
+    def split_communities(self, cfg, seed, step, target):
+        assert lib().ora_split_communities(self.h, ctypes.byref(cfg), seed, step, target) == 0
 
     def merge_blocks(self, cfg, seed, step, num_to_merge):
         st = OraStats()
