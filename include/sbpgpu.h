@@ -193,7 +193,8 @@ sbpgpu_status sbpgpu_sbp(sbpgpu_graph* g, const sbpgpu_config* cfg, uint64_t see
 /* ---- sampling (src/sample.cpp, src/main.cpp:98-140) ------------------------------ */
 /* A vertex sample: algorithm 0 max_degree (sample.cpp:255-270), 1 random (:272-284, the
  * seeded stream), 2 degree_product (:28-49), 3 detach (:12-26, vertices of degree above 1;
- * sample_size unused).  mapping[N] receives each vertex's id in the sample or -1;
+ * sample_size unused), 4 expansion_snowball (:125-157), 5 degree_product_snowball (:51-101;
+ * the two snowballs grow one vertex at a time and run on the host).  mapping[N] receives each vertex's id in the sample or -1;
  * sample_n the sample's size (long(sample_size * N) vertices, or as the algorithm gives). */
 sbpgpu_status sbpgpu_sample(sbpgpu_graph* g, int32_t algorithm, double sample_size, uint64_t seed,
                             int32_t* mapping, int64_t* sample_n);
@@ -205,6 +206,11 @@ sbpgpu_status sbpgpu_graph_subgraph(sbpgpu_graph* g, const int32_t* mapping, int
  * smallest block), or a block drawn from the seeded stream. */
 sbpgpu_status sbpgpu_extend(sbpgpu_graph* g, const int32_t* sample_assignment, int64_t sample_n,
                             int64_t num_blocks, const int32_t* mapping, uint64_t seed, int32_t* out_assignment);
+/* sample::reattach (sample.cpp:365-405) after a detach: a detached vertex takes its one
+ * neighbour's block, or (alone, or paired with another detached vertex) a block drawn from
+ * the seeded stream.  Every unsampled vertex must have degree 0 or 1. */
+sbpgpu_status sbpgpu_reattach(sbpgpu_graph* g, const int32_t* sample_assignment, int64_t sample_n,
+                              int64_t num_blocks, const int32_t* mapping, uint64_t seed, int32_t* out_assignment);
 /* finetune::finetune_assignment (src/finetune.cpp:903-932). */
 sbpgpu_status sbpgpu_finetune_assignment(sbpgpu_bm* bm, const sbpgpu_config* cfg, uint64_t seed,
                                          sbpgpu_stats* stats);

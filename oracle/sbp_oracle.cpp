@@ -15,6 +15,9 @@
  *   random sample         : shuffle with ctr = (position, 0, 0, DOM_SAMPLE = 6)
  *   extend, random block  : ctr = (vertex, 0, 0, DOM_EXTEND = 7), block = u32_below(w[0], B)
  *   finetune_assignment   : MH draws with step = 0xffffffff
+ *   reattach, random block: ctr = (vertex, 0, 0, DOM_REATTACH = 10), block = u32_below(w[0], B)
+ *   snowball samplers     : the k-th draw of a run, ctr = (k, 0, 0, DOM_SNOWBALL = 11),
+ *                           random_integer(lo, hi) = lo + u64_below(w[0], w[1], hi - lo + 1)
  *   top-down split size   : ctr = (cluster, proposal, step, DOM_SPLIT_SIZE = 8),
  *                           size = lo + u64_below(w[0], w[1], hi - lo + 1)
  *   top-down split side   : ctr = (vertex, proposal, step, DOM_SPLIT_SIDE = 9),
@@ -35,6 +38,8 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <queue>
+#include <tuple>
 #include <set>
 #include <utility>
 #include <vector>
@@ -47,7 +52,7 @@ namespace {
 
 enum : uint32_t {
     DOM_GIBBS = 1, DOM_MH = 2, DOM_MERGE = 3, DOM_SHUFFLE_HDV = 4, DOM_SHUFFLE_ALL = 5, DOM_SAMPLE = 6,
-    DOM_EXTEND = 7, DOM_SPLIT_SIZE = 8, DOM_SPLIT_SIDE = 9,
+    DOM_EXTEND = 7, DOM_SPLIT_SIZE = 8, DOM_SPLIT_SIDE = 9, DOM_REATTACH = 10, DOM_SNOWBALL = 11,
 };
 
 // ---------------------------------------------------------------- Philox4x32-10
@@ -1384,6 +1389,10 @@ void finetune_assignment(ora_bm* bm, const ora_config* cfg, uint64_t seed, ora_s
     bm->entropy = mdl_for(bm, cfg);
 }
 
+int64_t sample_expansion_snowball(const ora_graph* g, double samplesize, uint64_t seed, std::vector<int32_t>& mapping);
+int64_t sample_degree_product_snowball(const ora_graph* g, double samplesize, uint64_t seed,
+                                       std::vector<int32_t>& mapping);
+
 int64_t sample_any(const ora_graph* g, int32_t alg, double samplesize, uint64_t seed, std::vector<int32_t>& mapping) {
     mapping.assign(g->N, -1);
     switch (alg) {
@@ -1391,11 +1400,166 @@ int64_t sample_any(const ora_graph* g, int32_t alg, double samplesize, uint64_t 
         case 1: return sample_random(g, samplesize, seed, mapping);
         case 2: return sample_degree_product(g, samplesize, mapping);
         case 3: return sample_detach(g, mapping);
+        case 4: return sample_expansion_snowball(g, samplesize, seed, mapping);
+        case 5: return sample_degree_product_snowball(g, samplesize, seed, mapping);
         default: return -1;
     }
 }
 
 }  // namespace
+
+namespace {
+
+/* sample::reattach (sample.cpp:365-405) for the detached vertices (degree 0 or 1): a vertex
+ * whose one neighbour is assigned takes its block; otherwise the vertex (and its unassigned
+ * neighbour) take the vertex's random block. */
+void reattach(const ora_graph* g, const std::vector<int32_t>& sample_asg, int64_t B,
+              const std::vector<int32_t>& mapping, uint64_t seed, std::vector<int32_t>& asg) {
+    asg.assign(g->N, -1);
+    for (int64_t v = 0; v < g->N; ++v)
+        if (mapping[v] >= 0) asg[v] = sample_asg[mapping[v]];
+    for (int64_t v = 0; v < g->N; ++v) {
+        if (asg[v] != -1) continue;
+        uint32_t w[4];
+        draw(seed, (uint32_t)v, 0, 0, DOM_REATTACH, w);
+        const int32_t random_block_v = (int32_t)u32_below(w[0], (uint32_t)B);
+        for (int32_t u : g->out[v]) {
+            if (asg[u] == -1) {
+                asg[v] = random_block_v;
+                asg[u] = random_block_v;
+                break;
+            }
+            asg[v] = asg[u];
+        }
+        for (int32_t u : g->in[v]) {
+            if (asg[u] == -1) {
+                asg[v] = random_block_v;
+                asg[u] = random_block_v;
+                break;
+            }
+            asg[v] = asg[u];
+        }
+        if (asg[v] < 0) asg[v] = random_block_v;
+    }
+}
+
+/* The k-th draw of a snowball run: common::random_integer(lo, hi). */
+struct SeqRng {
+    uint64_t seed;
+    uint32_t k = 0;
+    int64_t operator()(int64_t lo, int64_t hi) {
+        uint32_t w[4];
+        draw(seed, k++, 0, 0, DOM_SNOWBALL, w);
+        return lo + (int64_t)u64_below(w[0], w[1], (uint64_t)(hi - lo + 1));
+    }
+};
+
+/* sample::expansion_snowball (sample.cpp:125-157, es_add_vertex :103-117,
+ * es_update_contribution :119-130): grow the sample by the neighbour that adds the most
+ * new neighbours. */
+int64_t sample_expansion_snowball(const ora_graph* g, double samplesize, uint64_t seed, std::vector<int32_t>& mapping) {
+    const int64_t N = g->N, target = sample_target(g, samplesize);
+    SeqRng rng{seed};
+    std::vector<int64_t> contribution(N, 0);
+    std::vector<char> flag(N, 0);
+    std::set<int64_t> neighbors;
+    int64_t contribution_sum = 0, n = 0;
+    auto update = [&](int64_t vertex) {
+        for (int32_t nb : g->out[vertex]) {
+            if (flag[nb] || mapping[nb] >= 0) continue;
+            contribution[vertex]++;
+            contribution_sum++;
+        }
+        for (int32_t nb : g->in[vertex])
+            if (contribution[nb] > 0) {
+                contribution[nb]--;
+                contribution_sum--;
+            }
+    };
+    auto add = [&](int64_t vertex) {
+        mapping[vertex] = (int32_t)n++;
+        for (int32_t nb : g->out[vertex]) {
+            if (flag[nb] || mapping[nb] >= 0) continue;
+            neighbors.insert(nb);
+            flag[nb] = 1;
+            if (contribution[nb] > 0) continue;
+            update(nb);
+        }
+        neighbors.erase(vertex);
+        flag[vertex] = 0;
+    };
+    add(rng(0, N - 1));
+    while (n < target) {
+        if (neighbors.empty()) {
+            int64_t v;
+            do v = rng(0, N - 1);
+            while (mapping[v] >= 0);
+            add(v);
+            continue;
+        } else if (contribution_sum == 0) {
+            auto it = neighbors.begin();
+            std::advance(it, rng(0, (int64_t)neighbors.size() - 1));
+            add(*it);
+            continue;
+        }
+        int64_t best = 0;
+        for (int64_t v = 1; v < N; ++v)
+            if (contribution[v] > contribution[best]) best = v;
+        add(best);
+    }
+    return n;
+}
+
+/* sample::degree_product_snowball (sample.cpp:51-101): grow the sample along the frontier
+ * edge of the largest degree product (ties: the earliest pushed edge). */
+int64_t sample_degree_product_snowball(const ora_graph* g, double samplesize, uint64_t seed,
+                                       std::vector<int32_t>& mapping) {
+    const int64_t N = g->N;
+    const std::vector<int64_t> d = graph_degrees(g);
+    SeqRng rng{seed};
+    // (degree product, -push sequence, source, destination): the largest product first, then
+    // the earliest push
+    std::priority_queue<std::tuple<int64_t, int64_t, int32_t, int32_t>> frontier;
+    int64_t pushes = 0, n = 0;
+    auto add = [&](int64_t vertex) {
+        mapping[vertex] = (int32_t)n++;
+        for (int32_t nb : g->out[vertex]) {
+            if (mapping[nb] != -1) continue;
+            frontier.push({d[vertex] * d[nb], -(pushes++), (int32_t)vertex, nb});
+        }
+        for (int32_t nb : g->in[vertex]) {
+            if (mapping[nb] != -1) continue;
+            frontier.push({d[nb] * d[vertex], -(pushes++), nb, (int32_t)vertex});
+        }
+    };
+    add(rng(0, N - 1));
+    const int64_t target = (int64_t)((double)N * samplesize);
+    while (n < target) {
+        if (frontier.empty()) {
+            int64_t v;
+            do v = rng(0, N - 1);
+            while (mapping[v] >= 0);
+            add(v);
+            if (frontier.empty()) continue;  // the vertex had no unsampled neighbour
+        }
+        const auto next = frontier.top();
+        frontier.pop();
+        const int32_t src = std::get<2>(next), dst = std::get<3>(next);
+        if (mapping[src] == -1) add(src);
+        if (mapping[dst] == -1) add(dst);
+    }
+    return n;
+}
+
+}  // namespace
+
+extern "C" void ora_reattach(const ora_graph* g, const int32_t* sample_asg, int64_t sample_n, int64_t B,
+                             const int32_t* mapping, uint64_t seed, int32_t* out) {
+    std::vector<int32_t> a;
+    reattach(g, std::vector<int32_t>(sample_asg, sample_asg + sample_n), B,
+             std::vector<int32_t>(mapping, mapping + g->N), seed, a);
+    std::copy(a.begin(), a.end(), out);
+}
 
 extern "C" int64_t ora_sample(const ora_graph* g, int32_t alg, double samplesize, uint64_t seed, int32_t* mapping) {
     std::vector<int32_t> m;

@@ -135,6 +135,10 @@ int64_t ora_bm_nonempty(const ora_bm* bm);
 /* Sampling (sample.cpp).  alg: 0 max_degree, 1 random, 2 degree_product, 3 detach.
  * mapping[v] = the vertex's id in the sample or -1; returns the sample's size. */
 int64_t ora_sample(const ora_graph* g, int32_t alg, double samplesize, uint64_t seed, int32_t* mapping);
+/* alg 4 expansion_snowball, 5 degree_product_snowball (serial, canonical draws). */
+/* sample::reattach (sample.cpp:365-405). */
+void ora_reattach(const ora_graph* g, const int32_t* sample_assignment, int64_t sample_n, int64_t num_blocks,
+                  const int32_t* mapping, uint64_t seed, int32_t* out_assignment);
 /* sample::from_vertices (sample.cpp:240-253). */
 ora_graph* ora_subgraph(const ora_graph* g, const int32_t* mapping, int64_t n);
 int64_t ora_graph_num_edges(const ora_graph* g);

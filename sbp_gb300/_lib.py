@@ -132,6 +132,7 @@ SIGNATURES = {
     "sbpgpu_sample": (ctypes.c_int, [vp, ctypes.c_int32, ctypes.c_double, ctypes.c_uint64, i32p, i64p]),
     "sbpgpu_graph_subgraph": (ctypes.c_int, [vp, i32p, ctypes.c_int64, ctypes.POINTER(vp)]),
     "sbpgpu_extend": (ctypes.c_int, [vp, i32p, ctypes.c_int64, ctypes.c_int64, i32p, ctypes.c_uint64, i32p]),
+    "sbpgpu_reattach": (ctypes.c_int, [vp, i32p, ctypes.c_int64, ctypes.c_int64, i32p, ctypes.c_uint64, i32p]),
     "sbpgpu_finetune_assignment": (ctypes.c_int, [vp, ctypes.POINTER(Config), ctypes.c_uint64, ctypes.POINTER(Stats)]),
     "sbpgpu_sbp_sampled": (ctypes.c_int, [vp, ctypes.POINTER(Config), ctypes.c_uint64, ctypes.c_int32, ctypes.c_double,
                                           i32p, i64p, f64p, ctypes.POINTER(Stats)]),

@@ -33,7 +33,8 @@ class Args:
     nonparametric: bool = False    # entropy::nonparametric (directed, not degree-corrected)
     seed: int = 0                  # seeds the canonical proposal stream
     samplesize: float = 1.0        # --samplesize: below 1, partition a sample and extend it (main.cpp:98-140)
-    samplingalg: str = "random"    # --samplingalg: random | max_degree | degree_product
+    samplingalg: str = "random"    # --samplingalg: random | max_degree | degree_product | *_snowball
+    detach: bool = False           # --detach: set degree-0/1 vertices aside and reattach them
     max_iterations: int = 100      # MAX_NUM_ITERATIONS (include/finetune.hpp:34)
 
     def config(self):

@@ -1143,7 +1143,7 @@ sbpgpu_status sbpgpu_graph_load(sbpgpu_ctx* ctx, const char* path, int32_t undir
 
 sbpgpu_status sbpgpu_sample(sbpgpu_graph* g, int32_t algorithm, double sample_size, uint64_t seed, int32_t* mapping,
                             int64_t* sample_n) {
-    if (!g || !mapping || !sample_n || algorithm < 0 || algorithm > 3 || !(sample_size > 0.0)) return SBPGPU_EINVAL;
+    if (!g || !mapping || !sample_n || algorithm < 0 || algorithm > 5 || !(sample_size > 0.0)) return SBPGPU_EINVAL;
     return guarded(g->ctx, [&] {
         cudaStream_t st = g->ctx->stream;
         std::vector<void*> tmp;
@@ -1240,6 +1240,39 @@ sbpgpu_status sbpgpu_extend(sbpgpu_graph* g, const int32_t* sample_assignment, i
     });
 }
 
+sbpgpu_status sbpgpu_reattach(sbpgpu_graph* g, const int32_t* sample_assignment, int64_t sample_n, int64_t num_blocks,
+                              const int32_t* mapping, uint64_t seed, int32_t* out) {
+    if (!g || !sample_assignment || !mapping || !out || sample_n <= 0 || num_blocks <= 0) return SBPGPU_EINVAL;
+    return guarded(g->ctx, [&] {
+        check_mapping(g, mapping, sample_n);
+        for (int64_t i = 0; i < sample_n; ++i)
+            if (sample_assignment[i] < 0 || sample_assignment[i] >= num_blocks)
+                throw ApiError(SBPGPU_EINVAL, "sample assignment out of range");
+        cudaStream_t st = g->ctx->stream;
+        std::vector<void*> tmp;
+        int32_t* d_map = dalloc<int32_t>(tmp, g->N);
+        int32_t* d_sasg = dalloc<int32_t>(tmp, sample_n);
+        int32_t* d_asg = dalloc<int32_t>(tmp, g->N);
+        try {
+            CK(cudaMemcpyAsync(d_map, mapping, g->N * 4, cudaMemcpyHostToDevice, st));
+            CK(cudaMemcpyAsync(d_sasg, sample_assignment, sample_n * 4, cudaMemcpyHostToDevice, st));
+            try {
+                reattach_assignment(g->dg, d_map, d_sasg, (int32_t)num_blocks, seed, d_asg, st);
+            } catch (const std::invalid_argument& e) {
+                throw ApiError(SBPGPU_EINVAL, e.what());
+            }
+            CK(cudaMemcpyAsync(out, d_asg, g->N * 4, cudaMemcpyDeviceToHost, st));
+            host_wait(st);
+            CK(cudaGetLastError());
+        } catch (...) {
+            free_all(tmp, st);
+            throw;
+        }
+        free_all(tmp, st);
+        return SBPGPU_OK;
+    });
+}
+
 sbpgpu_status sbpgpu_finetune_assignment(sbpgpu_bm* bm, const sbpgpu_config* cfg, uint64_t seed,
                                          sbpgpu_stats* stats) {
     if (!bm || !cfg) return SBPGPU_EINVAL;
@@ -1259,7 +1292,7 @@ sbpgpu_status sbpgpu_finetune_assignment(sbpgpu_bm* bm, const sbpgpu_config* cfg
 sbpgpu_status sbpgpu_sbp_sampled(sbpgpu_graph* g, const sbpgpu_config* cfg, uint64_t seed, int32_t algorithm,
                                  double sample_size, int32_t* out_assignment, int64_t* num_blocks, double* out_mdl,
                                  sbpgpu_stats* stats) {
-    if (!g || !cfg || algorithm < 0 || algorithm > 3 || !(sample_size > 0.0)) return SBPGPU_EINVAL;
+    if (!g || !cfg || algorithm < 0 || algorithm > 5 || !(sample_size > 0.0)) return SBPGPU_EINVAL;
     sbpgpu_graph* sub = nullptr;
     sbpgpu_bm* bm = nullptr;
     const sbpgpu_status rc = guarded(g->ctx, [&] {

@@ -166,6 +166,10 @@ void subgraph_edges(const DevGraph& g, const int32_t* mapping, int32_t** d_src, 
 void extend_assignment(const DevGraph& g, const int32_t* mapping, const int32_t* sample_asg, int32_t B,
                        int32_t max_k, uint64_t seed, int32_t* asg, cudaStream_t st);
 
+// sample::reattach into asg[N] for a mapping whose unsampled vertices have degree <= 1.
+void reattach_assignment(const DevGraph& g, const int32_t* mapping, const int32_t* sample_asg, int32_t B, uint64_t seed,
+                         int32_t* asg, cudaStream_t st);
+
 // ---- split.cu
 // Buffers of one split pass over B clusters (10 proposals each) and N vertices.
 struct SplitBuffers {

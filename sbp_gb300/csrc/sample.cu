@@ -21,9 +21,18 @@
 //    two ready vertices are never neighbours.  Ties go to the smallest block (the
 //    reference iterates a hash map); a vertex without assigned neighbours draws its block
 //    from the canonical stream (domain 7).
+//  * expansion_snowball and degree_product_snowball (:51-157) grow the sample one vertex at
+//    a time from a frontier; they run on the host over a copy of the adjacency, with the
+//    k-th random draw of a run taken from the canonical stream (domain 11).
+//  * reattach (:365-405) for the detached vertices (degree 0 or 1): a vertex with an
+//    assigned neighbour takes its block; a vertex whose one neighbour is detached as well
+//    shares the block drawn for the smaller of the two (domain 10).
 #include <climits>
+#include <queue>
+#include <set>
 #include <stdexcept>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "delta.cuh"
@@ -202,6 +211,204 @@ __global__ void k_extend_assign(DevGraph g, int32_t* __restrict__ asg, const int
     }
 }
 
+// ---- the snowball samplers: serial frontier processes, run on the host over a copy of
+// the adjacency (as the reference runs them serially)
+
+// Philox4x32-10 on the host, the same stream as the device's philox4x32_10.
+void philox_host(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint64_t seed, uint32_t w[4]) {
+    uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+    for (int r = 0; r < 10; ++r) {
+        if (r) {
+            k0 += 0x9E3779B9u;
+            k1 += 0xBB67AE85u;
+        }
+        const uint64_t p0 = (uint64_t)0xD2511F53u * c0, p1 = (uint64_t)0xCD9E8D57u * c2;
+        const uint32_t n0 = (uint32_t)(p1 >> 32) ^ c1 ^ k0, n2 = (uint32_t)(p0 >> 32) ^ c3 ^ k1;
+        c0 = n0;
+        c1 = (uint32_t)p1;
+        c2 = n2;
+        c3 = (uint32_t)p0;
+    }
+    w[0] = c0;
+    w[1] = c1;
+    w[2] = c2;
+    w[3] = c3;
+}
+
+enum : uint32_t { DOM_SNOWBALL = 11 };
+
+// common::random_integer(lo, hi) as the k-th draw of a run.
+struct SnowballRng {
+    uint64_t seed;
+    uint32_t k = 0;
+    int64_t operator()(int64_t lo, int64_t hi) {
+        uint32_t w[4];
+        philox_host(k++, 0, 0, DOM_SNOWBALL, seed, w);
+        const unsigned __int128 x = ((unsigned __int128)(((uint64_t)w[0] << 32) | w[1])) * (uint64_t)(hi - lo + 1);
+        return lo + (int64_t)(uint64_t)(x >> 64);
+    }
+};
+
+struct HostAdjacency {
+    std::vector<int32_t> out_off, out_nbr, in_off, in_nbr, deg;
+};
+
+// Out-lists in input order; in-lists with each self-loop as the vertex itself.
+HostAdjacency host_adjacency(const DevGraph& g, cudaStream_t st) {
+    const int64_t N = g.N, E = g.E;
+    HostAdjacency a;
+    std::vector<int32_t> inns_off(N + 1), self(N), inns;
+    a.out_off.resize(N + 1);
+    a.out_nbr.resize(E);
+    cudaMemcpyAsync(a.out_off.data(), g.out_off, (N + 1) * 4, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(inns_off.data(), g.inns_off, (N + 1) * 4, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(self.data(), g.selfcnt, N * 4, cudaMemcpyDeviceToHost, st);
+    if (E) cudaMemcpyAsync(a.out_nbr.data(), g.out_nbr, E * 4, cudaMemcpyDeviceToHost, st);
+    host_wait(st);
+    inns.resize(inns_off[N]);
+    if (!inns.empty()) cudaMemcpyAsync(inns.data(), g.inns_nbr, inns.size() * 4, cudaMemcpyDeviceToHost, st);
+    host_wait(st);
+    a.in_off.assign(N + 1, 0);
+    for (int64_t v = 0; v < N; ++v) a.in_off[v + 1] = a.in_off[v] + (inns_off[v + 1] - inns_off[v]) + self[v];
+    a.in_nbr.resize(a.in_off[N]);
+    a.deg.resize(N);
+    for (int64_t v = 0; v < N; ++v) {
+        int32_t o = a.in_off[v];
+        for (int32_t j = inns_off[v]; j < inns_off[v + 1]; ++j) a.in_nbr[o++] = inns[j];
+        for (int32_t j = 0; j < self[v]; ++j) a.in_nbr[o++] = (int32_t)v;
+        a.deg[v] = (a.out_off[v + 1] - a.out_off[v]) + (a.in_off[v + 1] - a.in_off[v]) - (self[v] > 0 ? 1 : 0);
+    }
+    return a;
+}
+
+// sample::expansion_snowball (sample.cpp:125-157; es_add_vertex :103-117,
+// es_update_contribution :119-130).
+int64_t expansion_snowball(const HostAdjacency& a, int64_t N, int64_t target, uint64_t seed,
+                           std::vector<int32_t>& mapping) {
+    SnowballRng rng{seed};
+    std::vector<int64_t> contribution(N, 0);
+    std::vector<char> in_hood(N, 0);
+    std::set<int64_t> hood;
+    int64_t contribution_sum = 0, n = 0;
+    auto update = [&](int64_t x) {
+        for (int32_t j = a.out_off[x]; j < a.out_off[x + 1]; ++j) {
+            const int32_t y = a.out_nbr[j];
+            if (in_hood[y] || mapping[y] >= 0) continue;
+            contribution[x]++;
+            contribution_sum++;
+        }
+        for (int32_t j = a.in_off[x]; j < a.in_off[x + 1]; ++j) {
+            const int32_t y = a.in_nbr[j];
+            if (contribution[y] > 0) {
+                contribution[y]--;
+                contribution_sum--;
+            }
+        }
+    };
+    auto add = [&](int64_t x) {
+        mapping[x] = (int32_t)n++;
+        for (int32_t j = a.out_off[x]; j < a.out_off[x + 1]; ++j) {
+            const int32_t y = a.out_nbr[j];
+            if (in_hood[y] || mapping[y] >= 0) continue;
+            hood.insert(y);
+            in_hood[y] = 1;
+            if (contribution[y] > 0) continue;
+            update(y);
+        }
+        hood.erase(x);
+        in_hood[x] = 0;
+    };
+    add(rng(0, N - 1));
+    while (n < target) {
+        if (hood.empty()) {
+            int64_t x;
+            do x = rng(0, N - 1);
+            while (mapping[x] >= 0);
+            add(x);
+        } else if (contribution_sum == 0) {
+            auto it = hood.begin();
+            std::advance(it, rng(0, (int64_t)hood.size() - 1));
+            add(*it);
+        } else {
+            int64_t best = 0;  // utils::argmax: the first largest contribution
+            for (int64_t x = 1; x < N; ++x)
+                if (contribution[x] > contribution[best]) best = x;
+            add(best);
+        }
+    }
+    return n;
+}
+
+// sample::degree_product_snowball (sample.cpp:51-101): the frontier edge of the largest
+// degree product first (ties: the earliest pushed).
+int64_t degree_product_snowball(const HostAdjacency& a, int64_t N, int64_t target, uint64_t seed,
+                                std::vector<int32_t>& mapping) {
+    SnowballRng rng{seed};
+    std::priority_queue<std::tuple<int64_t, int64_t, int32_t, int32_t>> frontier;
+    int64_t pushes = 0, n = 0;
+    auto add = [&](int64_t x) {
+        mapping[x] = (int32_t)n++;
+        for (int32_t j = a.out_off[x]; j < a.out_off[x + 1]; ++j) {
+            const int32_t y = a.out_nbr[j];
+            if (mapping[y] != -1) continue;
+            frontier.push({(int64_t)a.deg[x] * a.deg[y], -(pushes++), (int32_t)x, y});
+        }
+        for (int32_t j = a.in_off[x]; j < a.in_off[x + 1]; ++j) {
+            const int32_t y = a.in_nbr[j];
+            if (mapping[y] != -1) continue;
+            frontier.push({(int64_t)a.deg[y] * a.deg[x], -(pushes++), y, (int32_t)x});
+        }
+    };
+    add(rng(0, N - 1));
+    while (n < target) {
+        if (frontier.empty()) {
+            int64_t x;
+            do x = rng(0, N - 1);
+            while (mapping[x] >= 0);
+            add(x);
+            if (frontier.empty()) continue;
+        }
+        const auto next = frontier.top();
+        frontier.pop();
+        if (mapping[std::get<2>(next)] == -1) add(std::get<2>(next));
+        if (mapping[std::get<3>(next)] == -1) add(std::get<3>(next));
+    }
+    return n;
+}
+
+enum : uint32_t { DOM_REATTACH = 10 };
+
+// sample::reattach for vertices of degree 0 or 1 (the complement of detach).  flags a
+// vertex of larger degree in *bad.
+__global__ void k_reattach(DevGraph g, const int32_t* __restrict__ mapping, const int32_t* __restrict__ sample_asg,
+                           int32_t B, uint64_t seed, int32_t* __restrict__ asg, int32_t* __restrict__ bad) {
+    for (int32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < g.N; v += gridDim.x * blockDim.x) {
+        if (mapping[v] >= 0) {
+            asg[v] = sample_asg[mapping[v]];
+            continue;
+        }
+        if (vertex_degree(g, v) > 1) {
+            atomicAdd(bad, 1);
+            continue;
+        }
+        // the one neighbour other than v itself, if any
+        int32_t u = -1;
+        for (int32_t j = __ldg(g.out_off + v); j < __ldg(g.out_off + v + 1); ++j)
+            if (__ldg(g.out_nbr + j) != v) u = __ldg(g.out_nbr + j);
+        for (int32_t j = __ldg(g.inns_off + v); j < __ldg(g.inns_off + v + 1); ++j) u = __ldg(g.inns_nbr + j);
+        int32_t b;
+        if (u >= 0 && mapping[u] >= 0) {
+            b = sample_asg[mapping[u]];
+        } else {  // alone, or paired with another detached vertex: the smaller one's draw
+            const int32_t x = (u >= 0 && u < v) ? u : v;
+            uint32_t w[4];
+            philox4x32_10((uint32_t)x, 0u, 0u, DOM_REATTACH, seed, w);
+            b = (int32_t)u32_below(w[0], (uint32_t)B);
+        }
+        asg[v] = b;
+    }
+}
+
 template <class T>
 T* talloc(std::vector<void*>& tmp, size_t n, cudaStream_t st) {
     void* p = nullptr;
@@ -290,6 +497,13 @@ int64_t sample_vertices(const DevGraph& g, int alg, double samplesize, uint64_t 
             k_number_flagged<<<grid_of(N), 256, 0, st>>>(flags, pos, (int32_t)N, mapping);
             count_launches(2);
             n = read_i32(total, st);
+        } else if (alg == 4 || alg == 5) {  // expansion_snowball, degree_product_snowball
+            const HostAdjacency a = host_adjacency(g, st);
+            std::vector<int32_t> m(N, -1);
+            const int64_t t = std::min(std::max<int64_t>(target, 1), N);
+            n = alg == 4 ? expansion_snowball(a, N, t, seed, m) : degree_product_snowball(a, N, t, seed, m);
+            cudaMemcpyAsync(mapping, m.data(), N * sizeof(int32_t), cudaMemcpyHostToDevice, st);
+            host_wait(st);
         } else {
             throw std::invalid_argument("unknown sampling algorithm");
         }
@@ -361,6 +575,18 @@ void extend_assignment(const DevGraph& g, const int32_t* mapping, const int32_t*
     }
     host_wait(st);
     free_tmp(tmp, st);
+}
+
+void reattach_assignment(const DevGraph& g, const int32_t* mapping, const int32_t* sample_asg, int32_t B, uint64_t seed,
+                         int32_t* asg, cudaStream_t st) {
+    std::vector<void*> tmp;
+    int32_t* bad = talloc<int32_t>(tmp, 1, st);
+    cudaMemsetAsync(bad, 0, sizeof(int32_t), st);
+    k_reattach<<<grid_of(g.N), 256, 0, st>>>(g, mapping, sample_asg, B, seed, asg, bad);
+    count_launches(1);
+    const int32_t nbad = read_i32(bad, st);
+    free_tmp(tmp, st);
+    if (nbad) throw std::invalid_argument("reattach: an unsampled vertex has degree above 1");
 }
 
 }  // namespace sbp

@@ -9,7 +9,8 @@ from . import _lib
 from ._lib import Stats, i32p, i64p
 from .core import Args, Blockmodel, Graph
 
-ALGORITHMS = {"max_degree": 0, "random": 1, "degree_product": 2, "detach": 3}
+ALGORITHMS = {"max_degree": 0, "random": 1, "degree_product": 2, "detach": 3, "expansion_snowball": 4,
+              "degree_product_snowball": 5}
 
 
 @dataclasses.dataclass
@@ -21,8 +22,7 @@ class Sample:
 
 def _alg(name):
     if name not in ALGORITHMS:
-        raise ValueError("sampling algorithm must be one of %s (expansion_snowball and degree_product_snowball "
-                         "are not available)" % sorted(ALGORITHMS))
+        raise ValueError("sampling algorithm must be one of %s" % sorted(ALGORITHMS))
     return ALGORITHMS[name]
 
 
@@ -65,6 +65,16 @@ def extend(graph, sample_assignment, num_blocks, smp, seed=0):
     return out
 
 
+def reattach(graph, sample_assignment, num_blocks, smp, seed=0):
+    """sample::reattach (src/sample.cpp:365-405): the full graph's assignment after a detach."""
+    a = np.ascontiguousarray(sample_assignment, dtype=np.int32)
+    m = np.ascontiguousarray(smp.mapping, dtype=np.int32)
+    out = np.zeros(graph.num_vertices(), np.int32)
+    graph.ctx.check(graph.ctx.lib.sbpgpu_reattach(graph.h, a.ctypes.data_as(i32p), a.size, int(num_blocks),
+                                                  m.ctypes.data_as(i32p), int(seed), out.ctypes.data_as(i32p)))
+    return out
+
+
 def finetune_assignment(blockmodel, graph=None, args=None):
     """finetune::finetune_assignment (src/finetune.cpp:903-932); returns the stats dict."""
     a = args or Args()
@@ -76,13 +86,23 @@ def finetune_assignment(blockmodel, graph=None, args=None):
 
 
 def partition(graph, args=None):
-    """main.cpp:94-140: sbp::stochastic_block_partition on the whole graph when
-    args.samplesize >= 1, else on a sample of it, extended and finetuned.
+    """main.cpp:82-150: with args.detach, vertices of degree 0 or 1 are set aside first and
+    reattached at the end; the rest is partitioned whole (args.samplesize >= 1) or through
+    a sample, extended and finetuned.
 
     Returns (assignment, num_blocks, mdl, stats dict)."""
     a = args or Args()
     if not a.samplesize > 0:
         raise ValueError("samplesize must be > 0")
+    if a.detach:
+        det = detach(graph)
+        inner = dataclasses.replace(a, detach=False)
+        sub_asg, B, _, st = partition(det.graph, inner)
+        asg = reattach(graph, sub_asg, B, det, a.seed)
+        bm = Blockmodel(B, graph, 0.5, asg)
+        from . import entropy
+        mdl = entropy.nonparametric.mdl(bm) if a.nonparametric else entropy.mdl(bm)
+        return asg, B, mdl, st
     if a.samplesize >= 1.0:
         from .sbp import stochastic_block_partition
         return stochastic_block_partition(graph, a)

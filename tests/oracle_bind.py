@@ -119,6 +119,7 @@ def lib():
         L.ora_graph_num_edges.argtypes = [ctypes.c_void_p]
         L.ora_graph_edges.argtypes = [ctypes.c_void_p, i32p, i32p]
         L.ora_extend.argtypes = [ctypes.c_void_p, i32p, ctypes.c_int64, ctypes.c_int64, i32p, ctypes.c_uint64, i32p]
+        L.ora_reattach.argtypes = [ctypes.c_void_p, i32p, ctypes.c_int64, ctypes.c_int64, i32p, ctypes.c_uint64, i32p]
         L.ora_finetune_assignment.restype = ctypes.c_int
         L.ora_finetune_assignment.argtypes = [ctypes.c_void_p, ctypes.POINTER(OraConfig), ctypes.c_uint64,
                                               ctypes.POINTER(OraStats)]
@@ -163,7 +164,8 @@ class Graph:
             self.h = None
 
 
-SAMPLERS = {"max_degree": 0, "random": 1, "degree_product": 2, "detach": 3}
+SAMPLERS = {"max_degree": 0, "random": 1, "degree_product": 2, "detach": 3, "expansion_snowball": 4,
+            "degree_product_snowball": 5}
 
 
 def sample(graph, algorithm, sample_size, seed):
@@ -188,6 +190,14 @@ def extend(graph, sample_assignment, num_blocks, mapping, seed):
     m = np.ascontiguousarray(mapping, dtype=np.int32)
     out = np.zeros(graph.N, np.int32)
     lib().ora_extend(graph.h, _p(a, i32p), a.size, int(num_blocks), _p(m, i32p), seed, _p(out, i32p))
+    return out
+
+
+def reattach(graph, sample_assignment, num_blocks, mapping, seed):
+    a = np.ascontiguousarray(sample_assignment, dtype=np.int32)
+    m = np.ascontiguousarray(mapping, dtype=np.int32)
+    out = np.zeros(graph.N, np.int32)
+    lib().ora_reattach(graph.h, _p(a, i32p), a.size, int(num_blocks), _p(m, i32p), seed, _p(out, i32p))
     return out
 
 

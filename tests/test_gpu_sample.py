@@ -16,7 +16,8 @@ def graphs(gpu, oracle, n, e, k, seed, isolated=0):
     return gpu.Graph(N, src, dst), oracle.Graph(N, src, dst), src, dst, planted
 
 
-@pytest.mark.parametrize("alg", ["max_degree", "random", "degree_product", "detach"])
+@pytest.mark.parametrize("alg", ["max_degree", "random", "degree_product", "detach", "expansion_snowball",
+                                 "degree_product_snowball"])
 @pytest.mark.parametrize("size", [0.001, 0.3, 0.75])
 def test_sample_mapping_identical(gpu, oracle, alg, size):
     G, O, *_ = graphs(gpu, oracle, 3000, 30000, 9, seed=300, isolated=60)
@@ -98,3 +99,39 @@ def test_sampled_partition_identical_c1(gpu, oracle, alg, size, np_):
     assert B_g == B_o
     assert np.array_equal(a_g, a_o)
     assert abs(mdl_g - mdl_o) <= 1e-12 * abs(mdl_o)
+
+
+def _detach_graph(gpu, oracle):
+    src, dst, planted = gpu.dcsbm.generate(2000, 16000, 6, seed=340)
+    extra_s = [2000, 2002, 2003, 2005, 2006]
+    extra_d = [2001, 2002, 7, 2004, 9]
+    src = np.concatenate([src, extra_s]).astype(np.int32)
+    dst = np.concatenate([dst, extra_d]).astype(np.int32)
+    N = 2010  # 2007..2009 isolated
+    return gpu.Graph(N, src, dst), oracle.Graph(N, src, dst), src, dst, N
+
+
+def test_reattach_identical(gpu, oracle):
+    G, O, src, dst, N = _detach_graph(gpu, oracle)
+    m, n = gpu.sample.sample_mapping(G, "detach", 1.0)
+    m_o, n_o = oracle.sample(O, "detach", 1.0, 0)
+    assert n == n_o and np.array_equal(m, m_o)
+    sa = (np.arange(n) * 7 % 11).astype(np.int32)
+    got = gpu.sample.reattach(G, sa, 11, gpu.sample.Sample(None, m), seed=5)
+    assert np.array_equal(got, oracle.reattach(O, sa, 11, m, 5))
+
+
+def test_detached_partition_identical(gpu, oracle):
+    """main.cpp with --detach: partition the graph of degree > 1 vertices, then reattach."""
+    G, O, src, dst, N = _detach_graph(gpu, oracle)
+    args = gpu.Args(algorithm="hybrid_mcmc", seed=4, detach=True)
+    a_g, B_g, mdl_g, st = gpu.sample.partition(G, args)
+    m, n = oracle.sample(O, "detach", 1.0, 0)
+    n2, s2, d2 = oracle.subgraph_edges(O, m)
+    keep = np.argsort(src, kind="stable")
+    keep = keep[(m[src[keep]] >= 0) & (m[dst[keep]] >= 0)]
+    SO = oracle.Graph(n, m[src[keep]], m[dst[keep]])
+    sa, B_o, _, _ = oracle.sbp(SO, oracle.make_config("hybrid_mcmc"), 4)
+    a_o = oracle.reattach(O, sa, B_o, m, 4)
+    assert B_g == B_o and np.array_equal(a_g, a_o)
+    assert abs(mdl_g - oracle.Blockmodel(O, B_o, a_o).mdl()[1]) <= 1e-12 * abs(mdl_g)

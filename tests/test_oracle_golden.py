@@ -331,3 +331,21 @@ def test_oracle_sampled_partition(oracle):
     asg, B, mdl, st = oracle.sbp_sampled(g, oracle.make_config("hybrid_mcmc"), 1, "max_degree", 0.5)
     assert B > 1 and asg.max() < B
     assert evaluate.nmi(planted, asg) > 0.6
+
+
+def test_oracle_snowball_samplers_and_reattach(oracle):
+    from sbp_gb300 import dcsbm
+    src, dst, _ = dcsbm.generate(800, 6000, 5, seed=12)
+    src = np.concatenate([src, [800, 802, 803]]).astype(np.int32)   # 800 -> 801 pendant pair,
+    dst = np.concatenate([dst, [801, 802, 5]]).astype(np.int32)     # 802 self-loop, 803 -> 5
+    g = oracle.Graph(805, src, dst)                                  # 804 isolated
+    for alg in ("expansion_snowball", "degree_product_snowball"):
+        m, n = oracle.sample(g, alg, 0.25, 4)
+        assert n >= 201 and sorted(m[m >= 0].tolist()) == list(range(n))
+    m, n = oracle.sample(g, "detach", 1.0, 0)
+    assert all(m[v] == -1 for v in (800, 801, 802, 803, 804))
+    sa = np.arange(n, dtype=np.int32) % 7
+    asg = oracle.reattach(g, sa, 7, m, 3)
+    assert asg[803] == sa[m[5]]              # takes its sampled neighbour's block
+    assert asg[800] == asg[801]              # a detached pair shares one draw
+    assert asg.min() >= 0 and asg.max() < 7
