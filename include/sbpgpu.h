@@ -227,10 +227,10 @@ sbpgpu_status sbpgpu_sbp_sampled(sbpgpu_graph* g, const sbpgpu_config* cfg, uint
  * in ascending order of their best delta until the block count reaches the target. */
 sbpgpu_status sbpgpu_split_communities(sbpgpu_bm* bm, const sbpgpu_config* cfg, uint64_t seed, int32_t step,
                                        int64_t target_num_blocks);
-/* divisive::run (top_down_sbp.cpp:435-470, without --mix): from one block, split toward
- * ceil(1.5 B) blocks and finetune until the golden-section bracket of
- * TopDownBlockmodelTriplet closes. */
-sbpgpu_status sbpgpu_sbp_top_down(sbpgpu_graph* g, const sbpgpu_config* cfg, uint64_t seed,
+/* divisive::run (top_down_sbp.cpp:435-470): from one block, split toward ceil(1.5 B)
+ * blocks and finetune until the golden-section bracket of TopDownBlockmodelTriplet closes;
+ * with mix (--mix) until the bracket forms, then continue_agglomerative (:67-98). */
+sbpgpu_status sbpgpu_sbp_top_down(sbpgpu_graph* g, const sbpgpu_config* cfg, uint64_t seed, int32_t mix,
                                   int32_t* out_assignment, int64_t* num_blocks, double* out_mdl,
                                   sbpgpu_stats* stats);
 

@@ -1102,21 +1102,42 @@ struct Triplet {
     Slot s[3];
     bool optimal = false;
     bool golden_ratio_not_reached() const { return s[2].empty; }
-    void update(const ora_bm* bm) {
+    void update(const ora_bm* bm) { update(bm->B, bm->entropy, bm->asg); }
+    void update(int64_t B, double entropy, const std::vector<int32_t>& asg) {
         int idx;
         if (s[1].empty) {
             idx = 1;
-        } else if (bm->entropy <= s[1].entropy) {
-            const int old = (s[1].B > bm->B) ? 0 : 2;
+        } else if (entropy <= s[1].entropy) {
+            const int old = (s[1].B > B) ? 0 : 2;
             s[old] = s[1];
             idx = 1;
         } else {
-            idx = (s[1].B > bm->B) ? 2 : 0;
+            idx = (s[1].B > B) ? 2 : 0;
         }
         s[idx].empty = false;
-        s[idx].B = bm->B;
-        s[idx].entropy = bm->entropy;
-        s[idx].asg = bm->asg;
+        s[idx].B = B;
+        s[idx].entropy = entropy;
+        s[idx].asg = asg;
+    }
+    /* BlockmodelTriplet::get_next_blockmodel (blockmodel_triplet.cpp:4-37) after update. */
+    const Slot* next(int64_t* next_merge) {
+        if (golden_ratio_not_reached()) {
+            *next_merge = (int64_t)((double)s[1].B * 0.5);
+            if (*next_merge == 0) optimal = true;
+            return &s[1];
+        }
+        if (is_done()) {
+            *next_merge = 0;
+            return &s[1];
+        }
+        int index = 1;
+        if (s[0].empty && s[1].B > s[2].B) index = 1;
+        else if ((s[0].B - s[1].B) >= (s[1].B - s[2].B)) index = 0;
+        else index = 1;
+        int64_t next_try = s[index + 1].B;
+        next_try += (int64_t)((double)(s[index].B - s[index + 1].B) * 0.618);
+        *next_merge = s[index].B - next_try;
+        return &s[index];
     }
     bool is_done() {
         if ((!s[0].empty && s[0].B - s[2].B == 2) || (s[0].empty && s[1].B - s[2].B == 1)) optimal = true;
@@ -1839,8 +1860,8 @@ struct TDTriplet {
 
 /* divisive::run (top_down_sbp.cpp:435-470) without --mix: from one block, split toward
  * ceil(1.5 B) blocks until the golden-section bracket closes, finetuning after each split. */
-extern "C" int64_t ora_top_down(const ora_graph* g, const ora_config* cfg, uint64_t seed, int32_t* out_asg,
-                                double* out_mdl, ora_stats* st) {
+extern "C" int64_t ora_top_down(const ora_graph* g, const ora_config* cfg, uint64_t seed, int32_t mix,
+                                int32_t* out_asg, double* out_mdl, ora_stats* st) {
     std::vector<int32_t> zeros(g->N, 0);
     ora_bm* bm = ora_bm_create(g, 1, zeros.data());
     bm->entropy = DBL_MAX;
@@ -1863,7 +1884,8 @@ extern "C" int64_t ora_top_down(const ora_graph* g, const ora_config* cfg, uint6
     };
     int64_t target = 0;
     const Slot* src = next(bm, &target);
-    while (!t.optimal) {
+    // end_condition_not_reached (top_down_sbp.cpp:428-433): with --mix, until the bracket forms
+    while (mix ? t.golden_ratio_not_reached() : !t.optimal) {
         delete bm;
         bm = ora_bm_create(g, src->B, src->asg.data());
         bm->entropy = src->entropy;
@@ -1873,6 +1895,32 @@ extern "C" int64_t ora_top_down(const ora_graph* g, const ora_config* cfg, uint6
         if (st) st->outer_steps++;
         src = next(bm, &target);
     }
+    Slot result = *src;
+    if (mix) {
+        /* continue_agglomerative (top_down_sbp.cpp:67-98): an agglomerative triplet fed the three
+         * top-down blockmodels in slot order, then merges and finetuning until it is done; the
+         * finetuning keeps the top-down triplet's (reached) golden-ratio state. */
+        Triplet gr;
+        const Slot* gs = nullptr;
+        int64_t next_merge = 0;
+        for (int k = 0; k < 3; ++k) {
+            gr.update(t.s[k].B, t.s[k].entropy, t.s[k].asg);
+            gs = gr.next(&next_merge);
+        }
+        while (!gr.optimal) {
+            delete bm;
+            bm = ora_bm_create(g, gs->B, gs->asg.data());
+            bm->entropy = gs->entropy;
+            merge_blocks(bm, cfg, seed, step, next_merge, st);
+            mcmc(bm, cfg, seed, (int32_t)step, t.golden_ratio_not_reached(), st);
+            ++step;
+            if (st) st->outer_steps++;
+            gr.update(bm);
+            gs = gr.next(&next_merge);
+        }
+        result = *gs;
+    }
+    src = &result;
     const int64_t B = src->B;
     if (out_asg) std::copy(src->asg.begin(), src->asg.end(), out_asg);
     if (out_mdl) *out_mdl = src->entropy;

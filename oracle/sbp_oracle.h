@@ -156,8 +156,9 @@ int64_t ora_sbp_sampled(const ora_graph* g, const ora_config* cfg, uint64_t seed
 /* divisive::split_communities (top_down_sbp.cpp:472-530) with random splits toward
  * `target` blocks; mutates bm. */
 int ora_split_communities(ora_bm* bm, const ora_config* cfg, uint64_t seed, uint32_t step, int64_t target);
-/* divisive::run (top_down_sbp.cpp:435-470).  Returns the number of blocks. */
-int64_t ora_top_down(const ora_graph* g, const ora_config* cfg, uint64_t seed, int32_t* out_assignment,
+/* divisive::run (top_down_sbp.cpp:435-470); mix: --mix (continue_agglomerative).  Returns
+ * the number of blocks. */
+int64_t ora_top_down(const ora_graph* g, const ora_config* cfg, uint64_t seed, int32_t mix, int32_t* out_assignment,
                      double* out_mdl, ora_stats* stats);
 
 /* entropy::null_mdl_v1 (entropy.cpp:571-585) for a graph with `num_edges` edges. */

@@ -127,8 +127,8 @@ SIGNATURES = {
     "sbpgpu_evaluate": (ctypes.c_int, [vp, ctypes.c_int64, i32p, i32p, ctypes.POINTER(Eval)]),
     "sbpgpu_split_communities": (ctypes.c_int, [vp, ctypes.POINTER(Config), ctypes.c_uint64, ctypes.c_int32,
                                                 ctypes.c_int64]),
-    "sbpgpu_sbp_top_down": (ctypes.c_int, [vp, ctypes.POINTER(Config), ctypes.c_uint64, i32p, i64p, f64p,
-                                           ctypes.POINTER(Stats)]),
+    "sbpgpu_sbp_top_down": (ctypes.c_int, [vp, ctypes.POINTER(Config), ctypes.c_uint64, ctypes.c_int32, i32p, i64p,
+                                           f64p, ctypes.POINTER(Stats)]),
     "sbpgpu_sample": (ctypes.c_int, [vp, ctypes.c_int32, ctypes.c_double, ctypes.c_uint64, i32p, i64p]),
     "sbpgpu_graph_subgraph": (ctypes.c_int, [vp, i32p, ctypes.c_int64, ctypes.POINTER(vp)]),
     "sbpgpu_extend": (ctypes.c_int, [vp, i32p, ctypes.c_int64, ctypes.c_int64, i32p, ctypes.c_uint64, i32p]),

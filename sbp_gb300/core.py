@@ -35,6 +35,7 @@ class Args:
     samplesize: float = 1.0        # --samplesize: below 1, partition a sample and extend it (main.cpp:98-140)
     samplingalg: str = "random"    # --samplingalg: random | max_degree | degree_product | *_snowball
     detach: bool = False           # --detach: set degree-0/1 vertices aside and reattach them
+    mix: bool = False              # --mix: top-down, then agglomerative once the bracket forms
     max_iterations: int = 100      # MAX_NUM_ITERATIONS (include/finetune.hpp:34)
 
     def config(self):

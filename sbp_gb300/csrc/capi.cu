@@ -1824,7 +1824,7 @@ sbpgpu_status sbpgpu_split_communities(sbpgpu_bm* bm, const sbpgpu_config* cfg, 
     });
 }
 
-sbpgpu_status sbpgpu_sbp_top_down(sbpgpu_graph* g, const sbpgpu_config* cfg_in, uint64_t seed,
+sbpgpu_status sbpgpu_sbp_top_down(sbpgpu_graph* g, const sbpgpu_config* cfg_in, uint64_t seed, int32_t mix,
                                   int32_t* out_assignment, int64_t* num_blocks, double* out_mdl,
                                   sbpgpu_stats* stats) {
     if (!g || !cfg_in) return SBPGPU_EINVAL;
@@ -1885,7 +1885,8 @@ sbpgpu_status sbpgpu_sbp_top_down(sbpgpu_graph* g, const sbpgpu_config* cfg_in, 
         int64_t target = 0;
         int32_t step = 0;
         const Slot* src = next(&target);
-        while (!optimal) {
+        // end_condition_not_reached (top_down_sbp.cpp:428-433): with --mix, until the bracket forms
+        while (mix ? s[2].empty : !optimal) {
             CK(cudaMemcpyAsync(bm->d.asg, src->asg, N * 4, cudaMemcpyDeviceToDevice, st));
             bm->d.B = (int32_t)src->B;
             bm->entropy = src->entropy;
@@ -1895,6 +1896,64 @@ sbpgpu_status sbpgpu_sbp_top_down(sbpgpu_graph* g, const sbpgpu_config* cfg_in, 
             ++step;
             g->st.outer_steps++;
             src = next(&target);
+        }
+        if (mix) {
+            // continue_agglomerative (top_down_sbp.cpp:67-98): an agglomerative triplet fed the
+            // three top-down blockmodels in slot order, then merges and finetuning until done;
+            // the finetuning keeps the top-down triplet's (reached) golden-ratio state
+            Slot gs[3];
+            for (auto& sl : gs) sl.asg = dalloc<int32_t>(slots_mem, N);
+            bool gopt = false;
+            int64_t next_merge = 0;
+            // BlockmodelTriplet::update and get_next_blockmodel (blockmodel_triplet.cpp:4-37, :82-105)
+            auto agg_next = [&](int64_t B, double entropy, const int32_t* asg) -> const Slot* {
+                int idx;
+                if (gs[1].empty) {
+                    idx = 1;
+                } else if (entropy <= gs[1].entropy) {
+                    const int old = (gs[1].B > B) ? 0 : 2;
+                    std::swap(gs[old], gs[1]);
+                    idx = 1;
+                } else {
+                    idx = (gs[1].B > B) ? 2 : 0;
+                }
+                gs[idx].empty = false;
+                gs[idx].B = B;
+                gs[idx].entropy = entropy;
+                CK(cudaMemcpyAsync(gs[idx].asg, asg, N * 4, cudaMemcpyDeviceToDevice, st));
+                if (gs[2].empty) {
+                    next_merge = (int64_t)((double)gs[1].B * 0.5);
+                    if (next_merge == 0) gopt = true;
+                    return &gs[1];
+                }
+                if ((!gs[0].empty && gs[0].B - gs[2].B == 2) || (gs[0].empty && gs[1].B - gs[2].B == 1)) gopt = true;
+                if (gopt) {
+                    next_merge = 0;
+                    return &gs[1];
+                }
+                int index;
+                if (gs[0].empty && gs[1].B > gs[2].B) index = 1;
+                else if ((gs[0].B - gs[1].B) >= (gs[1].B - gs[2].B)) index = 0;
+                else index = 1;
+                int64_t next_try = gs[index + 1].B;
+                next_try += (int64_t)((double)(gs[index].B - gs[index + 1].B) * 0.618);
+                next_merge = gs[index].B - next_try;
+                return &gs[index];
+            };
+            const Slot* gsrc = nullptr;
+            for (int k = 0; k < 3; ++k) gsrc = agg_next(s[k].B, s[k].entropy, s[k].asg);
+            while (!gopt) {
+                CK(cudaMemcpyAsync(bm->d.asg, gsrc->asg, N * 4, cudaMemcpyDeviceToDevice, st));
+                bm->d.B = (int32_t)gsrc->B;
+                bm->entropy = gsrc->entropy;
+                do_rebuild(bm);
+                merge_impl(bm, cfg, seed, step, next_merge);
+                mcmc_impl(bm, cfg, seed, step, s[2].empty);
+                ++step;
+                g->st.outer_steps++;
+                gsrc = agg_next(bm->d.B, bm->entropy, bm->d.asg);
+            }
+            src = gsrc;
         }
         if (out_assignment) CK(cudaMemcpyAsync(out_assignment, src->asg, N * 4, cudaMemcpyDeviceToHost, st));
         harvest_counters(g);

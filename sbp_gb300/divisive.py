@@ -20,7 +20,8 @@ def split_communities(blockmodel, graph=None, target_num_communities=None, args=
 
 
 def run(graph, args=None):
-    """divisive::run (src/top_down_sbp.cpp:435-470, without --mix).
+    """divisive::run (src/top_down_sbp.cpp:435-470); args.mix continues agglomeratively
+    once the bracket forms (continue_agglomerative, :67-98).
 
     Returns (assignment, num_blocks, mdl, stats dict)."""
     a = args or Args()
@@ -29,6 +30,7 @@ def run(graph, args=None):
     B = ctypes.c_int64()
     mdl = ctypes.c_double()
     st = Stats()
-    graph.ctx.check(graph.ctx.lib.sbpgpu_sbp_top_down(graph.h, ctypes.byref(cfg), int(a.seed), out.ctypes.data_as(i32p),
-                                                      ctypes.byref(B), ctypes.byref(mdl), ctypes.byref(st)))
+    graph.ctx.check(graph.ctx.lib.sbpgpu_sbp_top_down(graph.h, ctypes.byref(cfg), int(a.seed), int(bool(a.mix)),
+                                                      out.ctypes.data_as(i32p), ctypes.byref(B), ctypes.byref(mdl),
+                                                      ctypes.byref(st)))
     return out, int(B.value), float(mdl.value), st.as_dict()

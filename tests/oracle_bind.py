@@ -130,8 +130,8 @@ def lib():
         L.ora_split_communities.argtypes = [ctypes.c_void_p, ctypes.POINTER(OraConfig), ctypes.c_uint64,
                                             ctypes.c_uint32, ctypes.c_int64]
         L.ora_top_down.restype = ctypes.c_int64
-        L.ora_top_down.argtypes = [ctypes.c_void_p, ctypes.POINTER(OraConfig), ctypes.c_uint64, i32p, f64p,
-                                   ctypes.POINTER(OraStats)]
+        L.ora_top_down.argtypes = [ctypes.c_void_p, ctypes.POINTER(OraConfig), ctypes.c_uint64, ctypes.c_int32, i32p,
+                                   f64p, ctypes.POINTER(OraStats)]
         L.ora_null_mdl_v1.restype = ctypes.c_double
         L.ora_null_mdl_v1.argtypes = [ctypes.c_double]
         _lib = L
@@ -211,11 +211,12 @@ def sbp_sampled(graph, cfg, seed, algorithm, sample_size):
     return out, int(B), mdl.value, st
 
 
-def top_down(graph, cfg, seed):
+def top_down(graph, cfg, seed, mix=False):
     out = np.zeros(graph.N, np.int32)
     mdl = ctypes.c_double()
     st = OraStats()
-    B = lib().ora_top_down(graph.h, ctypes.byref(cfg), seed, _p(out, i32p), ctypes.byref(mdl), ctypes.byref(st))
+    B = lib().ora_top_down(graph.h, ctypes.byref(cfg), seed, int(mix), _p(out, i32p), ctypes.byref(mdl),
+                           ctypes.byref(st))
     assert B > 0, B
     return out, int(B), mdl.value, st
 

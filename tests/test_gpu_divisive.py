@@ -30,12 +30,12 @@ def test_split_communities_identical(gpu, oracle, n, B, target, np_):
     same_state(gb, ob)
 
 
-@pytest.mark.parametrize("np_", [True, False])
-def test_top_down_identical_c1(gpu, oracle, np_):
+@pytest.mark.parametrize("np_,mix", [(True, False), (False, False), (False, True), (True, True)])
+def test_top_down_identical_c1(gpu, oracle, np_, mix):
     src, dst, planted = gpu.dcsbm.generate_config("C1", seed=0)
     G, O = gpu.Graph(1000, src, dst), oracle.Graph(1000, src, dst)
-    a_g, B_g, mdl_g, st = gpu.divisive.run(G, gpu.Args(algorithm="hybrid_mcmc", seed=1, nonparametric=np_))
-    a_o, B_o, mdl_o, ost = oracle.top_down(O, oracle.make_config("hybrid_mcmc", nonparametric=np_), 1)
+    a_g, B_g, mdl_g, st = gpu.divisive.run(G, gpu.Args(algorithm="hybrid_mcmc", seed=1, nonparametric=np_, mix=mix))
+    a_o, B_o, mdl_o, ost = oracle.top_down(O, oracle.make_config("hybrid_mcmc", nonparametric=np_), 1, mix)
     assert B_g == B_o
     assert np.array_equal(a_g, a_o)
     assert abs(mdl_g - mdl_o) <= 1e-12 * abs(mdl_o)
