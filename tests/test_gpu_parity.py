@@ -315,3 +315,19 @@ def test_full_sbp_identical_c1_non_greedy(gpu, oracle):
     assert B_g == B_o
     assert np.array_equal(a_g, a_o)
     assert abs(mdl_g - mdl_o) <= MDL_REL_TOL_CANONICAL * abs(mdl_o)
+
+
+def test_full_sbp_identical_c2(gpu, oracle):
+    """The benchmark workload itself (C2: N = 50,000, E ~ 1M, 33 planted blocks): the whole
+    golden-section partition on the device equals the oracle's (about a minute of host
+    time on the oracle side)."""
+    src, dst, planted = gpu.dcsbm.generate_config("C2", seed=0)
+    N = gpu.dcsbm.CONFIGS["C2"]["num_vertices"]
+    G = gpu.Graph(N, src, dst)
+    a_g, B_g, mdl_g, st = gpu.sbp.stochastic_block_partition(G, gpu.Args(algorithm="hybrid_mcmc", seed=1))
+    O = oracle.Graph(N, src, dst)
+    a_o, B_o, mdl_o, ost = oracle.sbp(O, oracle.make_config("hybrid_mcmc"), seed=1)
+    assert B_g == B_o
+    assert np.array_equal(a_g, a_o)
+    assert abs(mdl_g - mdl_o) <= MDL_REL_TOL_CANONICAL * abs(mdl_o)
+    assert st["merges"] == ost.merges and st["proposals"] == ost.proposals
