@@ -31,6 +31,7 @@
 #define SBP_GB300_HPP
 
 #include <climits>
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <limits>
@@ -90,6 +91,10 @@ struct Args {
     int threads = 1;                  // accepted for compatibility; the device uses every SM
     uint64_t seed = 0;                // seeds the proposal stream
     int max_iterations = 100;         // MAX_NUM_ITERATIONS (include/finetune.hpp:34)
+    double samplesize = 1.0;          // --samplesize: below 1, partition a sample (src/main.cpp:98-140)
+    std::string samplingalg = "random";  // random | max_degree | degree_product | *_snowball
+    bool detach = false;              // --detach: set degree-0/1 vertices aside, reattach them
+    bool mix = false;                 // --mix: top-down, then agglomerative (top_down_sbp.cpp:67-98)
 };
 
 /// The global arguments, as the reference's `args`.
@@ -161,17 +166,24 @@ class Graph {
     const NeighborList& in_neighbors() const { return in_; }
     const std::vector<long>& out_neighbors(long v) const { return out_[v]; }
     const std::vector<long>& in_neighbors(long v) const { return in_[v]; }
+    /// The true assignment, -1 where unknown (Graph::assignment, include/graph.hpp:74-78).
+    const std::vector<long>& assignment() const { return assignment_; }
+    void assignment(const std::vector<long>& a) { assignment_ = a; }
+    long assignment(long v) const { return assignment_[v]; }
+    void assign(long v, long block) { assignment_[v] = block; }
     sbpgpu_graph* handle() const { return h_; }
     Context& context() const { return *ctx_; }
 
   private:
     void upload(const std::vector<int32_t>& src, const std::vector<int32_t>& dst) {
         e_ = (long)src.size();
+        assignment_.assign(n_, -1);
         check(sbpgpu_graph_create(ctx_->get(), n_, e_, src.data(), dst.data(), &h_), ctx_->get());
     }
     Context* ctx_;
     long n_ = 0, e_ = 0;
     NeighborList out_, in_;
+    std::vector<long> assignment_;
     sbpgpu_graph* h_ = nullptr;
 };
 
@@ -435,6 +447,159 @@ inline Blockmodel stochastic_block_partition(Graph& graph, Args& a, bool divide_
 }
 
 }  // namespace sbp
+
+namespace sample {
+
+/// sample::Sample: the sampled graph and mapping[v] = v's id in it, or -1.
+struct Sample {
+    std::unique_ptr<Graph> graph;
+    std::vector<long> mapping;
+};
+
+namespace detail {
+inline int32_t algorithm(const std::string& name) {
+    if (name == "max_degree") return 0;
+    if (name == "random") return 1;
+    if (name == "degree_product") return 2;
+    if (name == "expansion_snowball") return 4;
+    if (name == "degree_product_snowball") return 5;
+    throw std::invalid_argument(name + " is not a valid sampling algorithm!");
+}
+// sample::from_vertices (src/sample.cpp:240-253) on the host mirror: edges between sampled
+// vertices in source order; the true assignment follows the vertices.
+inline Sample from_mapping(const Graph& graph, std::vector<long> mapping, long n) {
+    NeighborList out(n), in(n);
+    long E = 0;
+    for (long v = 0; v < graph.num_vertices(); ++v) {
+        if (mapping[v] < 0) continue;
+        for (long u : graph.out_neighbors(v))
+            if (mapping[u] >= 0) {
+                out[mapping[v]].push_back(mapping[u]);
+                in[mapping[u]].push_back(mapping[v]);
+                ++E;
+            }
+    }
+    Sample s{std::make_unique<Graph>(out, in, n, E, graph.context()), std::move(mapping)};
+    for (long v = 0; v < graph.num_vertices(); ++v)
+        if (s.mapping[v] >= 0) s.graph->assign(s.mapping[v], graph.assignment(v));
+    return s;
+}
+inline Sample run(const Graph& graph, int32_t alg, double size, uint64_t seed) {
+    std::vector<int32_t> m(graph.num_vertices());
+    int64_t n = 0;
+    check(sbpgpu_sample(graph.handle(), alg, size, seed, m.data(), &n), graph.context().get());
+    return from_mapping(graph, std::vector<long>(m.begin(), m.end()), n);
+}
+inline std::vector<int32_t> narrow(const std::vector<long>& v) { return std::vector<int32_t>(v.begin(), v.end()); }
+}  // namespace detail
+
+/// sample::sample (src/sample.cpp:328-341) with args.samplingalg and args.samplesize.
+inline Sample sample(const Graph& graph, const Args& a = args) {
+    return detail::run(graph, detail::algorithm(a.samplingalg), a.samplesize, a.seed);
+}
+/// sample::detach (src/sample.cpp:12-26): the vertices of degree above 1.
+inline Sample detach(const Graph& graph) { return detail::run(graph, 3, 1.0, 0); }
+
+/// sample::extend (src/sample.cpp:159-199).
+inline std::vector<long> extend(const Graph& graph, const Blockmodel& sample_blockmodel, const Sample& s,
+                                const Args& a = args) {
+    const std::vector<int32_t> sa = detail::narrow(sample_blockmodel.block_assignment());
+    const std::vector<int32_t> m = detail::narrow(s.mapping);
+    std::vector<int32_t> out(graph.num_vertices());
+    check(sbpgpu_extend(graph.handle(), sa.data(), (int64_t)sa.size(), sample_blockmodel.num_blocks(), m.data(), a.seed,
+                        out.data()),
+          graph.context().get());
+    return std::vector<long>(out.begin(), out.end());
+}
+
+/// sample::reattach (src/sample.cpp:365-405).
+inline Blockmodel reattach(const Graph& graph, const Blockmodel& sample_blockmodel, const Sample& s,
+                           const Args& a = args) {
+    const std::vector<int32_t> sa = detail::narrow(sample_blockmodel.block_assignment());
+    const std::vector<int32_t> m = detail::narrow(s.mapping);
+    std::vector<int32_t> out(graph.num_vertices());
+    check(sbpgpu_reattach(graph.handle(), sa.data(), (int64_t)sa.size(), sample_blockmodel.num_blocks(), m.data(),
+                          a.seed, out.data()),
+          graph.context().get());
+    return Blockmodel(sample_blockmodel.num_blocks(), graph, 0.5, std::vector<long>(out.begin(), out.end()));
+}
+
+}  // namespace sample
+
+namespace finetune {
+
+/// finetune::finetune_assignment (src/finetune.cpp:903-932).
+inline Blockmodel& finetune_assignment(Blockmodel& blockmodel, const Graph& graph, const Args& a = args) {
+    const sbpgpu_config cfg = to_config(a);
+    sbpgpu_stats st;
+    check(sbpgpu_finetune_assignment(blockmodel.handle(), &cfg, a.seed, &st), graph.context().get());
+    blockmodel.invalidate();
+    blockmodel.setOverall_entropy(sbpgpu_bm_entropy(blockmodel.handle()));
+    return blockmodel;
+}
+
+}  // namespace finetune
+
+namespace divisive {
+
+/// divisive::split_communities (src/top_down_sbp.cpp:472-530) with --split random.
+inline Blockmodel& split_communities(Blockmodel& blockmodel, const Graph& graph, int target_num_communities,
+                                     int step = 0, const Args& a = args) {
+    const sbpgpu_config cfg = to_config(a);
+    check(sbpgpu_split_communities(blockmodel.handle(), &cfg, a.seed, step, target_num_communities),
+          graph.context().get());
+    blockmodel.invalidate();
+    return blockmodel;
+}
+
+/// divisive::run (src/top_down_sbp.cpp:435-470), with args.mix as --mix.
+inline Blockmodel run(const Graph& graph, const Args& a = args) {
+    const sbpgpu_config cfg = to_config(a);
+    std::vector<int32_t> out(graph.num_vertices());
+    int64_t B = 0;
+    double mdl = 0.0;
+    sbpgpu_stats st;
+    check(sbpgpu_sbp_top_down(graph.handle(), &cfg, a.seed, a.mix ? 1 : 0, out.data(), &B, &mdl, &st),
+          graph.context().get());
+    Blockmodel bm(B, graph, 0.5, std::vector<long>(out.begin(), out.end()));
+    bm.setOverall_entropy(mdl);
+    return bm;
+}
+
+}  // namespace divisive
+
+namespace evaluate {
+
+/// evaluate::Eval (include/evaluate.hpp:15-19), with the other figures the reference prints.
+struct Eval {
+    double f1_score;
+    double nmi;
+    double true_mdl;
+    double precision, recall, rand_index, accuracy;
+};
+
+/// evaluate::evaluate_blockmodel (src/evaluate.cpp:100-110) against graph.assignment().
+inline Eval evaluate_blockmodel(const Graph& graph, Blockmodel& blockmodel) {
+    const std::vector<int32_t> t = sample::detail::narrow(graph.assignment());
+    const std::vector<int32_t> a = sample::detail::narrow(blockmodel.block_assignment());
+    sbpgpu_eval e;
+    check(sbpgpu_evaluate(graph.context().get(), graph.num_vertices(), t.data(), a.data(), &e), graph.context().get());
+    // the true blockmodel's MDL (evaluate.cpp:104-108), when every vertex is labelled
+    long true_blocks = 0;
+    bool labelled = true;
+    for (long x : graph.assignment()) {
+        true_blocks = std::max(true_blocks, x + 1);
+        labelled = labelled && x >= 0;
+    }
+    double true_mdl = std::numeric_limits<double>::quiet_NaN();
+    if (labelled) {
+        Blockmodel truth(true_blocks, graph, 0.5, graph.assignment());
+        true_mdl = entropy::mdl(truth, graph);
+    }
+    return Eval{e.f1, e.nmi, true_mdl, e.precision, e.recall, e.rand_index, e.accuracy};
+}
+
+}  // namespace evaluate
 
 }  // namespace sbp_gb300
 

@@ -161,6 +161,25 @@ static void full_partition(const char* graph_path, uint64_t seed, const char* ou
     s::Blockmodel bm = s::sbp::stochastic_block_partition(graph, a);
     EXPECT(bm.num_blocks() >= 1);
     EXPECT((long)bm.block_assignment().size() == n);
+    // sampling (src/main.cpp:98-140), top-down partitioning and evaluation entry points
+    s::Args sa = a;
+    sa.samplesize = 0.5;
+    sa.samplingalg = "max_degree";
+    s::sample::Sample smp = s::sample::sample(graph, sa);
+    EXPECT(smp.graph->num_vertices() == n / 2);
+    s::Blockmodel sbm = s::sbp::stochastic_block_partition(*smp.graph, sa);
+    const std::vector<long> ext = s::sample::extend(graph, sbm, smp, sa);
+    EXPECT((long)ext.size() == n);
+    s::Blockmodel ebm(sbm.num_blocks(), graph, 0.5, ext);
+    s::finetune::finetune_assignment(ebm, graph, sa);
+    EXPECT(ebm.num_blocks() == sbm.num_blocks());
+    s::Blockmodel td = s::divisive::run(graph, a);
+    EXPECT(td.num_blocks() >= 1);
+    graph.assignment(bm.block_assignment());
+    const s::evaluate::Eval ev = s::evaluate::evaluate_blockmodel(graph, bm);
+    EXPECT(std::fabs(ev.nmi - 1.0) < 1e-6 && ev.f1_score == 1.0 && ev.accuracy == 1.0);
+    EXPECT(std::fabs(ev.true_mdl - bm.getOverall_entropy()) < 1e-6 * bm.getOverall_entropy());
+
     std::ofstream o(out_path);
     o.precision(17);
     o << bm.num_blocks() << " " << bm.getOverall_entropy() << "\n";
