@@ -169,6 +169,8 @@ sbpgpu_status sbpgpu_server_submit(sbpgpu_server* s, const sbpgpu_job* job, int6
     auto st = std::make_unique<JobState>();
     st->job = *job;
     st->footprint = sbpgpu_job_footprint(job->num_vertices, job->num_edges, s->cells_budget);
+    if (job->config.nonparametric)  // lgamma table and the non-empty-count steps (int64)
+        st->footprint += 8 * (std::max(job->num_vertices, job->num_edges) + 2) + 16 * (job->num_vertices + 2);
     st->t_submit = Clock::now();
     {
         std::lock_guard<std::mutex> lk(s->mu);
