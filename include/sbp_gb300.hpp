@@ -95,6 +95,8 @@ struct Args {
     std::string samplingalg = "random";  // random | max_degree | degree_product | *_snowball
     bool detach = false;              // --detach: set degree-0/1 vertices aside, reattach them
     bool mix = false;                 // --mix: top-down, then agglomerative (top_down_sbp.cpp:67-98)
+    std::string split = "random";     // --split: random | snowball | single-snowball | connectivity-snowball
+    std::string splitinit = "random";  // --splitinit: random | degree-weighted | high-degree
 };
 
 /// The global arguments, as the reference's `args`.
@@ -112,6 +114,15 @@ inline sbpgpu_config to_config(const Args& a) {
     c.mh_percent = a.mh_percent;
     c.greedy = a.greedy && !a.nonparametric ? 1 : 0;  // --nonparametric sets greedy off (args.hpp:204-207)
     c.nonparametric = a.nonparametric ? 1 : 0;
+    if (a.split == "random") c.split = 0;
+    else if (a.split == "snowball") c.split = 1;
+    else if (a.split == "single-snowball") c.split = 2;
+    else if (a.split == "connectivity-snowball") c.split = 3;
+    else throw std::invalid_argument("Invalid split type provided.");
+    if (a.splitinit == "random") c.splitinit = 0;
+    else if (a.splitinit == "degree-weighted") c.splitinit = 1;
+    else if (a.splitinit == "high-degree") c.splitinit = 2;
+    else throw std::logic_error("This init split type has not been implemented yet.");
     c.ordered = a.ordered ? 1 : 0;
     c.approximate = a.approximate ? 1 : 0;
     c.asynciterations = a.asynciterations;

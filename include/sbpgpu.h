@@ -46,6 +46,9 @@ typedef struct sbpgpu_config {
                                  MDL, directed, without degree correction; acceptance is then non-greedy
                                  without the Hastings correction (include/args.hpp:204-207,
                                  src/entropy.cpp:499) whatever `greedy` says */
+    int32_t split;            /* --split (top-down): 0 random (default), 1 snowball, 2 single-snowball,
+                                 3 connectivity-snowball */
+    int32_t splitinit;        /* --splitinit: 0 random (default), 1 degree-weighted, 2 high-degree */
 } sbpgpu_config;
 
 typedef struct sbpgpu_stats {

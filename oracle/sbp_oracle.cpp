@@ -22,6 +22,8 @@
  *                           size = lo + u64_below(w[0], w[1], hi - lo + 1)
  *   top-down split side   : ctr = (vertex, proposal, step, DOM_SPLIT_SIDE = 9),
  *                           side 0 iff w[0] * n < size * 2^32
+ *   snowball splits       : the k-th draw of (cluster, proposal, step),
+ *                           ctr = (cluster, proposal | k << 8, step, DOM_SPLIT_SNOWBALL = 12)
  *   u32_below(w, n) = (w * n) >> 32;  u64_below(hi, lo, n) = ((hi:lo) * n) >> 64.
  *   Multinomials over a block's neighbour weights enumerate the row part (ascending
  *   column) and then the column part (ascending row), the same concatenation the
@@ -53,6 +55,7 @@ namespace {
 enum : uint32_t {
     DOM_GIBBS = 1, DOM_MH = 2, DOM_MERGE = 3, DOM_SHUFFLE_HDV = 4, DOM_SHUFFLE_ALL = 5, DOM_SAMPLE = 6,
     DOM_EXTEND = 7, DOM_SPLIT_SIZE = 8, DOM_SPLIT_SIDE = 9, DOM_REATTACH = 10, DOM_SNOWBALL = 11,
+    DOM_SPLIT_SNOWBALL = 12,
 };
 
 // ---------------------------------------------------------------- Philox4x32-10
@@ -1773,8 +1776,197 @@ double split_null_mdl(const ora_graph* g, int64_t n, int64_t E, bool nonparametr
     return (e * h) - log_posterior_p;
 }
 
-/* divisive::split_communities (top_down_sbp.cpp:472-530) with random splits and
- * apply_best_splits (:30-65). */
+/* A cluster's subgraph (extract_subgraph, top_down_sbp.cpp:100-130): local ids in vertex
+ * order, the edges between its vertices; neighbors(v) = out-neighbours then in-neighbours
+ * (Graph::neighbors, graph.cpp:174-183). */
+struct ClusterGraph {
+    int64_t n = 0;
+    std::vector<std::vector<int32_t>> nbrs;
+    std::vector<int64_t> deg;  // Graph::degrees: out + in - (has a self-loop)
+};
+
+ClusterGraph cluster_graph(const ora_graph* g, const std::vector<int32_t>& members, const std::vector<int32_t>& local) {
+    ClusterGraph cg;
+    cg.n = (int64_t)members.size();
+    std::vector<std::vector<int32_t>> out(cg.n), in(cg.n);
+    std::vector<char> self(cg.n, 0);
+    for (int32_t u : members)
+        for (int32_t v : g->out[u])
+            if (local[v] >= 0) {
+                out[local[u]].push_back(local[v]);
+                in[local[v]].push_back(local[u]);
+                if (u == v) self[local[u]] = 1;
+            }
+    cg.nbrs.resize(cg.n);
+    cg.deg.resize(cg.n);
+    for (int64_t x = 0; x < cg.n; ++x) {
+        cg.nbrs[x] = out[x];
+        cg.nbrs[x].insert(cg.nbrs[x].end(), in[x].begin(), in[x].end());
+        cg.deg[x] = (int64_t)out[x].size() + (int64_t)in[x].size() - self[x];
+    }
+    return cg;
+}
+
+/* common::random_integer for the k-th draw of one split proposal. */
+struct SplitRng {
+    uint64_t seed;
+    uint32_t cluster, proposal, step, k = 0;
+    uint32_t word() {
+        uint32_t w[4];
+        draw(seed, cluster, proposal | (k++ << 8), step, DOM_SPLIT_SNOWBALL, w);
+        return w[0];
+    }
+    int64_t operator()(int64_t lo, int64_t hi) {
+        uint32_t w[4];
+        draw(seed, cluster, proposal | (k++ << 8), step, DOM_SPLIT_SNOWBALL, w);
+        return lo + (int64_t)u64_below(w[0], w[1], (uint64_t)(hi - lo + 1));
+    }
+};
+
+/* split_init (top_down_sbp.cpp:532-583): two start vertices.  The reference's nth_element
+ * leaves ties in an unspecified order; here the degree ranking is a stable descending sort.
+ * degree-weighted draws from the top max(n / 10, 2) (the reference's n / 10 = 1 never ends). */
+std::pair<int64_t, int64_t> split_init(const ClusterGraph& cg, int32_t kind, SplitRng& rng) {
+    const int64_t n = cg.n;
+    if (kind == 0 || n < 10) {
+        const int64_t a = rng(0, n - 1);
+        int64_t b = rng(0, n - 1);
+        while (b == a) b = rng(0, n - 1);
+        return {a, b};
+    }
+    std::vector<int64_t> idx(n);
+    for (int64_t x = 0; x < n; ++x) idx[x] = x;
+    std::stable_sort(idx.begin(), idx.end(), [&](int64_t a, int64_t b) { return cg.deg[a] > cg.deg[b]; });
+    if (kind == 2) return {idx[0], idx[1]};
+    const int64_t m = std::max<int64_t>(n / 10, 2);
+    const int64_t a = rng(0, m - 1);
+    int64_t b = rng(0, m - 1);
+    while (b == a) b = rng(0, m - 1);
+    return {idx[a], idx[b]};
+}
+
+/* propose_snowball_split (top_down_sbp.cpp:313-363): two snowballs; each step picks a side
+ * with the split-size odds and takes the smallest vertex of its frontier (or the smallest
+ * unsampled vertex). */
+std::vector<int8_t> snowball_split(const ClusterGraph& cg, int32_t init, SplitRng& rng) {
+    const int64_t n = cg.n;
+    std::vector<int8_t> side(n, -1);
+    std::set<int64_t> unsampled;
+    for (int64_t x = 0; x < n; ++x) unsampled.insert(x);
+    std::set<int64_t> frontier[2];
+    const auto st = split_init(cg, init, rng);
+    const int64_t start[2] = {st.first, st.second};
+    for (int id = 0; id < 2; ++id) {
+        side[start[id]] = (int8_t)id;
+        unsampled.erase(start[id]);
+    }
+    for (int id = 0; id < 2; ++id)
+        for (int32_t y : cg.nbrs[start[id]])
+            if (side[y] == -1) frontier[id].insert(y);
+    const int64_t size = rng((int64_t)((double)n * 0.2), (int64_t)((double)n * 0.8));
+    while (!unsampled.empty()) {
+        const int id = (uint64_t)rng.word() * (uint64_t)n < ((uint64_t)size << 32) ? 0 : 1;
+        const int64_t sel = frontier[id].empty() ? *unsampled.begin() : *frontier[id].begin();
+        side[sel] = (int8_t)id;
+        unsampled.erase(sel);
+        frontier[0].erase(sel);
+        frontier[1].erase(sel);
+        for (int32_t y : cg.nbrs[sel])
+            if (side[y] == -1) frontier[id].insert(y);
+    }
+    return side;
+}
+
+/* propose_single_snowball_split (top_down_sbp.cpp:382-426): one snowball grown level by level
+ * until it holds the target number of vertices.  As in the reference, the membership test
+ * `sampled[vertex]` of a map counts every vertex it looks at. */
+std::vector<int8_t> single_snowball_split(const ClusterGraph& cg, int32_t init, SplitRng& rng) {
+    const int64_t n = cg.n;
+    std::vector<int8_t> side(n, 0);
+    std::map<int64_t, bool> sampled, frontier, next_frontier;
+    const int64_t start = split_init(cg, init, rng).first;
+    side[start] = 1;
+    sampled[start] = true;
+    for (int32_t y : cg.nbrs[start])
+        if (side[y] != 1) frontier[y] = true;
+    const uint64_t target = (uint64_t)rng((int64_t)((double)n * 0.2), (int64_t)((double)n * 0.8));
+    while (sampled.size() < target) {
+        if (frontier.empty() && next_frontier.empty()) break;
+        for (const auto& e : frontier) {
+            const int64_t x = e.first;
+            if (!sampled[x]) {
+                side[x] = 1;
+                sampled[x] = true;
+                for (int32_t y : cg.nbrs[x])
+                    if (side[y] != 1) next_frontier[y] = true;
+            }
+            if (sampled.size() >= target) break;
+        }
+        frontier = std::move(next_frontier);
+        next_frontier.clear();
+    }
+    return side;
+}
+
+/* propose_connectivity_snowball_split (top_down_sbp.cpp:262-311): two seeds, then level by
+ * level every frontier vertex joins the side most of its assigned neighbours are on. */
+std::vector<int8_t> connectivity_snowball_split(const ClusterGraph& cg, int32_t init, SplitRng& rng) {
+    const int64_t n = cg.n;
+    std::vector<int8_t> side(n, -1);
+    std::set<int64_t> unsampled;
+    for (int64_t x = 0; x < n; ++x) unsampled.insert(x);
+    std::map<int64_t, bool> frontier, next_frontier;
+    const auto st = split_init(cg, init, rng);
+    const int64_t start[2] = {st.first, st.second};
+    for (int id = 0; id < 2; ++id) {
+        side[start[id]] = (int8_t)id;
+        unsampled.erase(start[id]);
+    }
+    for (int id = 0; id < 2; ++id)
+        for (int32_t y : cg.nbrs[start[id]])
+            if (side[y] == -1) frontier[y] = true;
+    auto sample_vertex = [&](int64_t x) {
+        int e0 = 0, e1 = 0;
+        for (int32_t y : cg.nbrs[x]) {
+            if (side[y] == 0) e0++;
+            if (side[y] == 1) e1++;
+            if (side[y] != -1) continue;
+            next_frontier[y] = true;
+        }
+        side[x] = e1 > e0 ? 1 : 0;
+        unsampled.erase(x);
+        frontier[x] = false;
+    };
+    while (!unsampled.empty()) {
+        if (frontier.empty()) {
+            sample_vertex(*unsampled.begin());
+            continue;
+        }
+        for (const auto& e : frontier) sample_vertex(e.first);
+        frontier = std::move(next_frontier);
+        next_frontier.clear();
+    }
+    return side;
+}
+
+/* The sides of proposal i of cluster c (local ids): propose_random_split or a snowball. */
+std::vector<int8_t> split_sides(const ora_graph* g, const ora_config* cfg, const std::vector<int32_t>& members,
+                                const ClusterGraph* cg, uint64_t seed, int64_t c, int32_t i, uint32_t step) {
+    const int64_t n = (int64_t)members.size();
+    std::vector<int8_t> side(n, 0);
+    if (n < 2) return side;
+    if (cfg->split == 0) {
+        const int64_t size = split_size(seed, c, i, step, n);
+        for (int64_t x = 0; x < n; ++x) side[x] = (int8_t)split_side(seed, members[x], i, step, size, n);
+        return side;
+    }
+    SplitRng rng{seed, (uint32_t)c, (uint32_t)i, step};
+    if (cfg->split == 1) return snowball_split(*cg, cfg->splitinit, rng);
+    if (cfg->split == 2) return single_snowball_split(*cg, cfg->splitinit, rng);
+    return connectivity_snowball_split(*cg, cfg->splitinit, rng);
+}
+
+/* divisive::split_communities (top_down_sbp.cpp:472-530) and apply_best_splits (:30-65). */
 void split_communities(ora_bm* bm, const ora_config* cfg, uint64_t seed, uint32_t step, int64_t target) {
     const ora_graph* g = bm->g;
     const int64_t B = bm->B, N = g->N;
@@ -1783,22 +1975,24 @@ void split_communities(ora_bm* bm, const ora_config* cfg, uint64_t seed, uint32_
     std::vector<double> best(B, DBL_MAX);
     std::vector<int32_t> best_i(B, -1);
     std::vector<int64_t> split_n(B, INT64_MAX);  // Split::num_vertices; unset splits are skipped
-    std::vector<int64_t> sizes_of(B * 10, 0);
+    std::vector<int32_t> local(N, -1);
     for (int64_t c = 0; c < B; ++c) {
         const int64_t n = (int64_t)members[c].size();
         if ((double)n < 0.001 * (double)N) continue;  // do not split small clusters
+        for (int64_t x = 0; x < n; ++x) local[members[c][x]] = (int32_t)x;
         int64_t E = 0;
         for (int32_t u : members[c])
             for (int32_t v : g->out[u]) E += bm->asg[v] == c;
         const double old_entropy = split_null_mdl(g, n, E, cfg->nonparametric != 0);
+        ClusterGraph cg;
+        if (cfg->split != 0 && n >= 2) cg = cluster_graph(g, members[c], local);
         for (int32_t i = 0; i < 10; ++i) {  // NUM_AGG_PROPOSALS_PER_BLOCK
-            const int64_t size = n < 2 ? n : split_size(seed, c, i, step, n);
+            const std::vector<int8_t> sd = split_sides(g, cfg, members[c], &cg, seed, c, i, step);
             int64_t sizes[2] = {0, 0}, M[4] = {0, 0, 0, 0};
-            auto side = [&](int32_t v) { return n < 2 ? 0 : split_side(seed, v, i, step, size, n); };
             for (int32_t u : members[c]) {
-                sizes[side(u)]++;
+                sizes[sd[local[u]]]++;
                 for (int32_t v : g->out[u])
-                    if (bm->asg[v] == c) M[2 * side(u) + side(v)]++;
+                    if (bm->asg[v] == c) M[2 * sd[local[u]] + sd[local[v]]]++;
             }
             const double delta = np_mdl_two_blocks(g, n, E, sizes, M) - old_entropy;
             if (delta < best[c]) {
@@ -1807,6 +2001,7 @@ void split_communities(ora_bm* bm, const ora_config* cfg, uint64_t seed, uint32_
                 split_n[c] = n;
             }
         }
+        for (int32_t u : members[c]) local[u] = -1;
     }
     // apply_best_splits: ascending delta (utils::argsort is a stable descending sort, walked
     // from its end)
@@ -1817,11 +2012,14 @@ void split_communities(ora_bm* bm, const ora_config* cfg, uint64_t seed, uint32_
     for (int64_t k = B - 1; k >= 0; --k) {
         const int64_t c = order[k];
         if (split_n[c] > N) continue;
-        const int64_t n = split_n[c];
         const int32_t i = best_i[c];
-        const int64_t size = n < 2 ? n : split_size(seed, c, i, step, n);
-        for (int32_t v : members[c])
-            if (n >= 2 && split_side(seed, v, i, step, size, n) == 1) bm->asg[v] = (int32_t)num_blocks;
+        for (int64_t x = 0; x < (int64_t)members[c].size(); ++x) local[members[c][x]] = (int32_t)x;
+        ClusterGraph cg;
+        if (cfg->split != 0 && members[c].size() >= 2) cg = cluster_graph(g, members[c], local);
+        const std::vector<int8_t> sd = split_sides(g, cfg, members[c], &cg, seed, c, i, step);
+        for (int32_t u : members[c]) local[u] = -1;
+        for (int64_t x = 0; x < (int64_t)members[c].size(); ++x)
+            if (sd[x] == 1) bm->asg[members[c][x]] = (int32_t)num_blocks;
         num_blocks++;
         if (num_blocks >= target) break;
     }

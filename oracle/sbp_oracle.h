@@ -36,6 +36,8 @@ typedef struct ora_config {
     int32_t asynciterations;  /* --asynciterations */
     int32_t max_iterations;   /* MAX_NUM_ITERATIONS (finetune.hpp:34) = 100 */
     int32_t nonparametric;    /* --nonparametric: entropy::nonparametric::*, greedy forced off (args.hpp:204-207) */
+    int32_t split;            /* --split: 0 random, 1 snowball, 2 single-snowball, 3 connectivity-snowball */
+    int32_t splitinit;        /* --splitinit: 0 random, 1 degree-weighted, 2 high-degree */
 } ora_config;
 
 typedef struct ora_stats {

@@ -30,6 +30,8 @@ class Config(ctypes.Structure):
         ("asynciterations", ctypes.c_int32),
         ("max_iterations", ctypes.c_int32),
         ("nonparametric", ctypes.c_int32),
+        ("split", ctypes.c_int32),
+        ("splitinit", ctypes.c_int32),
     ]
 
 

@@ -17,6 +17,8 @@ from . import _lib
 from ._lib import Config, Stats, check, i32p, i64p, f64p
 
 ALGORITHMS = {"async_gibbs": 0, "hybrid_mcmc": 1, "metropolis_hastings": 2}
+SPLITS = {"random": 0, "snowball": 1, "single-snowball": 2, "connectivity-snowball": 3}
+SPLIT_INITS = {"random": 0, "degree-weighted": 1, "high-degree": 2}
 
 
 @dataclasses.dataclass
@@ -36,6 +38,8 @@ class Args:
     samplingalg: str = "random"    # --samplingalg: random | max_degree | degree_product | *_snowball
     detach: bool = False           # --detach: set degree-0/1 vertices aside and reattach them
     mix: bool = False              # --mix: top-down, then agglomerative once the bracket forms
+    split: str = "random"          # --split: random | snowball | single-snowball | connectivity-snowball
+    splitinit: str = "random"      # --splitinit: random | degree-weighted | high-degree
     max_iterations: int = 100      # MAX_NUM_ITERATIONS (include/finetune.hpp:34)
 
     def config(self):
@@ -45,9 +49,12 @@ class Args:
             raise ValueError("batches must be >= 1")
         # --nonparametric sets greedy off (include/args.hpp:204-207)
         greedy = bool(self.greedy) and not self.nonparametric
+        if self.split not in SPLITS or self.splitinit not in SPLIT_INITS:
+            raise ValueError("split must be one of %s and splitinit one of %s" % (sorted(SPLITS), sorted(SPLIT_INITS)))
         return Config(ALGORITHMS[self.algorithm], int(self.batches), float(self.mh_percent), int(greedy),
                       int(bool(self.ordered)), int(bool(self.approximate)), int(self.asynciterations),
-                      int(self.max_iterations), int(bool(self.nonparametric)))
+                      int(self.max_iterations), int(bool(self.nonparametric)), SPLITS[self.split],
+                      SPLIT_INITS[self.splitinit])
 
 
 class Context:

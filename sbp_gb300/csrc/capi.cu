@@ -676,7 +676,25 @@ void split_impl(sbpgpu_bm* bm, const sbpgpu_config& cfg, uint64_t seed, uint32_t
     b.new_block = dalloc<int32_t>(tmp, B);
     b.proposal = dalloc<int32_t>(tmp, B);
     try {
-        split_count(g->dg, bm->d, seed, step, b, st);
+        if (cfg.split == 0) {
+            split_count(g->dg, bm->d, seed, step, b, st);
+        } else {
+            // snowball splits: serial frontier processes on the host, counted on the device
+            std::vector<int32_t> asg(N), hsizes(B), helig(B);
+            CK(cudaMemcpyAsync(asg.data(), bm->d.asg, N * 4, cudaMemcpyDeviceToHost, st));
+            CK(cudaMemcpyAsync(hsizes.data(), bm->d.sizes, B * 4, cudaMemcpyDeviceToHost, st));
+            host_wait(st);
+            for (int64_t c = 0; c < B; ++c) helig[c] = (double)hsizes[c] < 0.001 * (double)N ? 0 : 1;
+            std::vector<uint16_t> mask;
+            std::vector<int32_t> hn1;
+            snowball_split_masks(host_adjacency(g->dg, st), asg, hsizes, helig, (int32_t)B, cfg.split, cfg.splitinit, seed,
+                                 step, mask, hn1);
+            CK(cudaMemcpyAsync(b.mask, mask.data(), N * sizeof(uint16_t), cudaMemcpyHostToDevice, st));
+            CK(cudaMemcpyAsync(b.n1, hn1.data(), hn1.size() * 4, cudaMemcpyHostToDevice, st));
+            CK(cudaMemcpyAsync(b.eligible, helig.data(), B * 4, cudaMemcpyHostToDevice, st));
+            split_count_edges(g->dg, bm->d, b, st);
+            host_wait(st);
+        }
         std::vector<int32_t> n1(B * P), cells(B * P * 4), elig(B), sizes(B);
         std::vector<unsigned long long> ecount(B);
         CK(cudaMemcpyAsync(n1.data(), b.n1, n1.size() * 4, cudaMemcpyDeviceToHost, st));
@@ -973,6 +991,8 @@ void sbpgpu_default_config(sbpgpu_config* cfg) {
     cfg->asynciterations = INT32_MAX;
     cfg->max_iterations = 100;
     cfg->nonparametric = 0;
+    cfg->split = 0;
+    cfg->splitinit = 0;
 }
 
 sbpgpu_status sbpgpu_ctx_create(int32_t device, sbpgpu_ctx** out) {
@@ -1815,7 +1835,9 @@ sbpgpu_status sbpgpu_sbp(sbpgpu_graph* g, const sbpgpu_config* cfg_in, uint64_t 
 
 sbpgpu_status sbpgpu_split_communities(sbpgpu_bm* bm, const sbpgpu_config* cfg, uint64_t seed, int32_t step,
                                        int64_t target_num_blocks) {
-    if (!bm || !cfg || target_num_blocks < 1) return SBPGPU_EINVAL;
+    if (!bm || !cfg || target_num_blocks < 1 || cfg->split < 0 || cfg->split > 3 || cfg->splitinit < 0 ||
+        cfg->splitinit > 2)
+        return SBPGPU_EINVAL;
     sbpgpu_graph* g = bm->g;
     return guarded(g->ctx, [&] {
         if (target_num_blocks > g->N) throw ApiError(SBPGPU_EINVAL, "target above one block per vertex");
@@ -1827,7 +1849,8 @@ sbpgpu_status sbpgpu_split_communities(sbpgpu_bm* bm, const sbpgpu_config* cfg, 
 sbpgpu_status sbpgpu_sbp_top_down(sbpgpu_graph* g, const sbpgpu_config* cfg_in, uint64_t seed, int32_t mix,
                                   int32_t* out_assignment, int64_t* num_blocks, double* out_mdl,
                                   sbpgpu_stats* stats) {
-    if (!g || !cfg_in) return SBPGPU_EINVAL;
+    if (!g || !cfg_in || cfg_in->split < 0 || cfg_in->split > 3 || cfg_in->splitinit < 0 || cfg_in->splitinit > 2)
+        return SBPGPU_EINVAL;
     sbpgpu_ctx* ctx = g->ctx;
     sbpgpu_bm* bm = nullptr;
     std::vector<void*> slots_mem;

@@ -154,6 +154,14 @@ bool parse_edges_device(const char* d_text, int64_t n, int undirected, int32_t**
                         int64_t* max_id, std::string* err, cudaStream_t st);
 
 // ---- sample.cu
+// Philox4x32-10 on the host: the device stream's words for the same counter and key.
+void philox_host(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint64_t seed, uint32_t w[4]);
+// A host copy of the adjacency: out-lists in input order, in-lists with each self-loop as
+// the vertex itself, and Graph::degrees (out + in - has a self-loop).
+struct HostAdjacency {
+    std::vector<int32_t> out_off, out_nbr, in_off, in_nbr, deg;
+};
+HostAdjacency host_adjacency(const DevGraph& g, cudaStream_t st);
 // Vertex sample (alg 0 max_degree, 1 random, 2 degree_product, 3 detach) into the device
 // array mapping[N] (sample id or -1); returns the sample's size.
 int64_t sample_vertices(const DevGraph& g, int alg, double samplesize, uint64_t seed, int32_t* mapping, Work& w,
@@ -187,6 +195,16 @@ struct SplitBuffers {
 void split_count(const DevGraph& g, const DevBM& bm, uint64_t seed, uint32_t step, SplitBuffers& b, cudaStream_t st);
 // Moves side-1 vertices of the chosen clusters into their new blocks (apply_best_splits).
 void split_apply(const DevGraph& g, DevBM& bm, const SplitBuffers& b, cudaStream_t st);
+// The edge counts alone, for sides (b.mask) and eligibility (b.eligible) set by the host.
+void split_count_edges(const DevGraph& g, const DevBM& bm, SplitBuffers& b, cudaStream_t st);
+// Snowball splits (propose_snowball_split, propose_single_snowball_split,
+// propose_connectivity_snowball_split, top_down_sbp.cpp:262-426) of every eligible cluster:
+// split 1 snowball, 2 single-snowball, 3 connectivity-snowball; init (split_init) 0 random,
+// 1 degree-weighted, 2 high-degree.  Fills mask[N] (bit i: side in proposal i) and
+// n1[B * 10].
+void snowball_split_masks(const HostAdjacency& a, const std::vector<int32_t>& asg, const std::vector<int32_t>& sizes,
+                          const std::vector<int32_t>& eligible, int32_t B, int split, int init, uint64_t seed,
+                          uint32_t step, std::vector<uint16_t>& mask, std::vector<int32_t>& n1);
 
 // ---- evaluate.cu
 struct PartitionQuality {

@@ -41,6 +41,55 @@
 
 namespace sbp {
 
+// Philox4x32-10 on the host, the same stream as the device's philox4x32_10.
+void philox_host(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint64_t seed, uint32_t w[4]) {
+    uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+    for (int r = 0; r < 10; ++r) {
+        if (r) {
+            k0 += 0x9E3779B9u;
+            k1 += 0xBB67AE85u;
+        }
+        const uint64_t p0 = (uint64_t)0xD2511F53u * c0, p1 = (uint64_t)0xCD9E8D57u * c2;
+        const uint32_t n0 = (uint32_t)(p1 >> 32) ^ c1 ^ k0, n2 = (uint32_t)(p0 >> 32) ^ c3 ^ k1;
+        c0 = n0;
+        c1 = (uint32_t)p1;
+        c2 = n2;
+        c3 = (uint32_t)p0;
+    }
+    w[0] = c0;
+    w[1] = c1;
+    w[2] = c2;
+    w[3] = c3;
+}
+
+// Out-lists in input order; in-lists with each self-loop as the vertex itself.
+HostAdjacency host_adjacency(const DevGraph& g, cudaStream_t st) {
+    const int64_t N = g.N, E = g.E;
+    HostAdjacency a;
+    std::vector<int32_t> inns_off(N + 1), self(N), inns;
+    a.out_off.resize(N + 1);
+    a.out_nbr.resize(E);
+    cudaMemcpyAsync(a.out_off.data(), g.out_off, (N + 1) * 4, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(inns_off.data(), g.inns_off, (N + 1) * 4, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(self.data(), g.selfcnt, N * 4, cudaMemcpyDeviceToHost, st);
+    if (E) cudaMemcpyAsync(a.out_nbr.data(), g.out_nbr, E * 4, cudaMemcpyDeviceToHost, st);
+    host_wait(st);
+    inns.resize(inns_off[N]);
+    if (!inns.empty()) cudaMemcpyAsync(inns.data(), g.inns_nbr, inns.size() * 4, cudaMemcpyDeviceToHost, st);
+    host_wait(st);
+    a.in_off.assign(N + 1, 0);
+    for (int64_t v = 0; v < N; ++v) a.in_off[v + 1] = a.in_off[v] + (inns_off[v + 1] - inns_off[v]) + self[v];
+    a.in_nbr.resize(a.in_off[N]);
+    a.deg.resize(N);
+    for (int64_t v = 0; v < N; ++v) {
+        int32_t o = a.in_off[v];
+        for (int32_t j = inns_off[v]; j < inns_off[v + 1]; ++j) a.in_nbr[o++] = inns[j];
+        for (int32_t j = 0; j < self[v]; ++j) a.in_nbr[o++] = (int32_t)v;
+        a.deg[v] = (a.out_off[v + 1] - a.out_off[v]) + (a.in_off[v + 1] - a.in_off[v]) - (self[v] > 0 ? 1 : 0);
+    }
+    return a;
+}
+
 namespace {
 
 enum : uint32_t { DOM_SAMPLE = 6, DOM_EXTEND = 7 };
@@ -214,27 +263,6 @@ __global__ void k_extend_assign(DevGraph g, int32_t* __restrict__ asg, const int
 // ---- the snowball samplers: serial frontier processes, run on the host over a copy of
 // the adjacency (as the reference runs them serially)
 
-// Philox4x32-10 on the host, the same stream as the device's philox4x32_10.
-void philox_host(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint64_t seed, uint32_t w[4]) {
-    uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
-    for (int r = 0; r < 10; ++r) {
-        if (r) {
-            k0 += 0x9E3779B9u;
-            k1 += 0xBB67AE85u;
-        }
-        const uint64_t p0 = (uint64_t)0xD2511F53u * c0, p1 = (uint64_t)0xCD9E8D57u * c2;
-        const uint32_t n0 = (uint32_t)(p1 >> 32) ^ c1 ^ k0, n2 = (uint32_t)(p0 >> 32) ^ c3 ^ k1;
-        c0 = n0;
-        c1 = (uint32_t)p1;
-        c2 = n2;
-        c3 = (uint32_t)p0;
-    }
-    w[0] = c0;
-    w[1] = c1;
-    w[2] = c2;
-    w[3] = c3;
-}
-
 enum : uint32_t { DOM_SNOWBALL = 11 };
 
 // common::random_integer(lo, hi) as the k-th draw of a run.
@@ -248,38 +276,6 @@ struct SnowballRng {
         return lo + (int64_t)(uint64_t)(x >> 64);
     }
 };
-
-struct HostAdjacency {
-    std::vector<int32_t> out_off, out_nbr, in_off, in_nbr, deg;
-};
-
-// Out-lists in input order; in-lists with each self-loop as the vertex itself.
-HostAdjacency host_adjacency(const DevGraph& g, cudaStream_t st) {
-    const int64_t N = g.N, E = g.E;
-    HostAdjacency a;
-    std::vector<int32_t> inns_off(N + 1), self(N), inns;
-    a.out_off.resize(N + 1);
-    a.out_nbr.resize(E);
-    cudaMemcpyAsync(a.out_off.data(), g.out_off, (N + 1) * 4, cudaMemcpyDeviceToHost, st);
-    cudaMemcpyAsync(inns_off.data(), g.inns_off, (N + 1) * 4, cudaMemcpyDeviceToHost, st);
-    cudaMemcpyAsync(self.data(), g.selfcnt, N * 4, cudaMemcpyDeviceToHost, st);
-    if (E) cudaMemcpyAsync(a.out_nbr.data(), g.out_nbr, E * 4, cudaMemcpyDeviceToHost, st);
-    host_wait(st);
-    inns.resize(inns_off[N]);
-    if (!inns.empty()) cudaMemcpyAsync(inns.data(), g.inns_nbr, inns.size() * 4, cudaMemcpyDeviceToHost, st);
-    host_wait(st);
-    a.in_off.assign(N + 1, 0);
-    for (int64_t v = 0; v < N; ++v) a.in_off[v + 1] = a.in_off[v] + (inns_off[v + 1] - inns_off[v]) + self[v];
-    a.in_nbr.resize(a.in_off[N]);
-    a.deg.resize(N);
-    for (int64_t v = 0; v < N; ++v) {
-        int32_t o = a.in_off[v];
-        for (int32_t j = inns_off[v]; j < inns_off[v + 1]; ++j) a.in_nbr[o++] = inns[j];
-        for (int32_t j = 0; j < self[v]; ++j) a.in_nbr[o++] = (int32_t)v;
-        a.deg[v] = (a.out_off[v + 1] - a.out_off[v]) + (a.in_off[v + 1] - a.in_off[v]) - (self[v] > 0 ? 1 : 0);
-    }
-    return a;
-}
 
 // sample::expansion_snowball (sample.cpp:125-157; es_add_vertex :103-117,
 // es_update_contribution :119-130).

@@ -30,7 +30,13 @@ class OraConfig(ctypes.Structure):
         ("asynciterations", ctypes.c_int32),
         ("max_iterations", ctypes.c_int32),
         ("nonparametric", ctypes.c_int32),
+        ("split", ctypes.c_int32),
+        ("splitinit", ctypes.c_int32),
     ]
+
+
+SPLITS = {"random": 0, "snowball": 1, "single-snowball": 2, "connectivity-snowball": 3}
+SPLIT_INITS = {"random": 0, "degree-weighted": 1, "high-degree": 2}
 
 
 class OraStats(ctypes.Structure):
@@ -42,9 +48,11 @@ ALGORITHMS = {"async_gibbs": 0, "hybrid_mcmc": 1, "metropolis_hastings": 2}
 
 
 def make_config(algorithm="hybrid_mcmc", batches=1, mh_percent=0.075, greedy=True, ordered=False,
-                approximate=False, asynciterations=2**31 - 1, max_iterations=100, nonparametric=False):
+                approximate=False, asynciterations=2**31 - 1, max_iterations=100, nonparametric=False,
+                split="random", splitinit="random"):
     return OraConfig(ALGORITHMS[algorithm], batches, mh_percent, int(greedy), int(ordered),
-                     int(approximate), asynciterations, max_iterations, int(nonparametric))
+                     int(approximate), asynciterations, max_iterations, int(nonparametric), SPLITS[split],
+                     SPLIT_INITS[splitinit])
 
 
 _lib = None

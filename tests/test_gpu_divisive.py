@@ -40,3 +40,20 @@ def test_top_down_identical_c1(gpu, oracle, np_, mix):
     assert np.array_equal(a_g, a_o)
     assert abs(mdl_g - mdl_o) <= 1e-12 * abs(mdl_o)
     assert st["outer_steps"] == ost.outer_steps
+
+
+@pytest.mark.parametrize("split", ["snowball", "single-snowball", "connectivity-snowball"])
+@pytest.mark.parametrize("init", ["random", "degree-weighted", "high-degree"])
+def test_snowball_splits_identical(gpu, oracle, split, init):
+    """The snowball splits (top_down_sbp.cpp:262-426): host frontier processes per cluster,
+    counted and applied on the device, against the oracle."""
+    n, B = 2500, 8
+    src, dst, planted = gpu.dcsbm.generate(n, 10 * n, 6, seed=450)
+    a = (np.arange(n) % B).astype(np.int32)
+    G, O = gpu.Graph(n, src, dst), oracle.Graph(n, src, dst)
+    gb, ob = gpu.Blockmodel(B, G, 0.5, a), oracle.Blockmodel(O, B, a)
+    args = gpu.Args(seed=5, nonparametric=True, split=split, splitinit=init)
+    gpu.divisive.split_communities(gb, G, 13, args, step=2)
+    ob.split_communities(oracle.make_config(nonparametric=True, split=split, splitinit=init), 5, 2, 13)
+    assert gb.num_blocks() == ob.num_blocks == 13
+    same_state(gb, ob)

@@ -349,3 +349,18 @@ def test_oracle_snowball_samplers_and_reattach(oracle):
     assert asg[803] == sa[m[5]]              # takes its sampled neighbour's block
     assert asg[800] == asg[801]              # a detached pair shares one draw
     assert asg.min() >= 0 and asg.max() < 7
+
+
+@pytest.mark.parametrize("split", ["snowball", "single-snowball", "connectivity-snowball"])
+@pytest.mark.parametrize("init", ["random", "degree-weighted", "high-degree"])
+def test_oracle_snowball_splits(oracle, split, init):
+    from sbp_gb300 import dcsbm
+    src, dst, _ = dcsbm.generate(1500, 15000, 6, seed=21)
+    g = oracle.Graph(1500, src, dst)
+    a = (np.arange(1500) % 5).astype(np.int32)
+    b = oracle.Blockmodel(g, 5, a)
+    b.split_communities(oracle.make_config(nonparametric=True, split=split, splitinit=init), 3, 0, 9)
+    d = b.read()
+    assert b.num_blocks == 9 and np.bincount(d["assignment"], minlength=9).min() > 0
+    # every vertex keeps its cluster or moves to one of the new blocks
+    assert all(x == y or x >= 5 for x, y in zip(d["assignment"].tolist(), a.tolist()))
