@@ -180,12 +180,62 @@ __device__ long long merge_delta_part(const DevGraph& g, const DevBM& bm, const 
             acc += ce_fixed(Lq, o, deg, ds) - ce_fixed(Lq, o + m, deg, ds2) - (long long)o * (is_row ? Lout : Lin);
         }
     };
-    auto item = [&](int32_t key, bool is_row) {
-        ++keys_seen;
-        const int32_t m = cells.get(is_row ? r : key, is_row ? key : r);
-        const int32_t o = cells.get(is_row ? s : key, is_row ? key : s);
-        const int32_t deg = (is_row ? bm.d_in : bm.d_out)[key];
-        term(key, is_row, m, o, deg);
+    // The appended chunks of row r and of column r, walked together: each step takes the next
+    // chunk of each list, loads the headers of the chunks after them before using its keys,
+    // and handles the keys four per thread per pass with all their cells loaded first, so the
+    // two list walks overlap their memory latencies.
+    auto walk = [&](int32_t rh, int32_t chd) {
+        const volatile int32_t* vp = ch.pool;
+        int32_t c[2] = {rh, chd}, nxt[2] = {-1, -1}, cnt[2] = {0, 0}, cap[2] = {0, 0};
+#pragma unroll
+        for (int l = 0; l < 2; ++l)
+            if (c[l] >= 0) {
+                nxt[l] = vp[c[l]];
+                cnt[l] = vp[c[l] + 1];
+                cap[l] = vp[c[l] + 2];
+            }
+        int guard = 0;
+        while ((c[0] >= 0 || c[1] >= 0) && guard++ < (1 << 26)) {
+            int32_t nxt2[2] = {-1, -1}, cnt2[2] = {0, 0}, cap2[2] = {0, 0};
+#pragma unroll
+            for (int l = 0; l < 2; ++l)
+                if (nxt[l] >= 0) {
+                    nxt2[l] = vp[nxt[l]];
+                    cnt2[l] = vp[nxt[l] + 1];
+                    cap2[l] = vp[nxt[l] + 2];
+                }
+            const int32_t n0 = c[0] >= 0 ? min(cnt[0], cap[0]) : 0, n1 = c[1] >= 0 ? min(cnt[1], cap[1]) : 0;
+            // one index space over the two chunks: [0, n0) row keys, [n0, n0 + n1) column keys
+            for (int32_t i0 = t; i0 < n0 + n1; i0 += 4 * nt) {
+                int32_t key[4], m[4], o[4], deg[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const int32_t i = i0 + q * nt;
+                    key[q] = i < n0 ? vp[c[0] + 3 + i] : (i < n0 + n1 ? vp[c[1] + 3 + i - n0] : -1);
+                }
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const bool is_row = i0 + q * nt < n0;
+                    const int32_t k = key[q] < 0 ? r : key[q];
+                    m[q] = cells.get(is_row ? r : k, is_row ? k : r);
+                    o[q] = cells.get(is_row ? s : k, is_row ? k : s);
+                    deg[q] = (is_row ? bm.d_in : bm.d_out)[k];
+                }
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                    if (key[q] >= 0) {
+                        ++keys_seen;
+                        term(key[q], i0 + q * nt < n0, m[q], o[q], deg[q]);
+                    }
+            }
+#pragma unroll
+            for (int l = 0; l < 2; ++l) {
+                c[l] = nxt[l];
+                nxt[l] = nxt2[l];
+                cnt[l] = cnt2[l];
+                cap[l] = cap2[l];
+            }
+        }
     };
     // Snapshot segments of row r and column r as one index space, four keys per thread
     // per pass: the keys, then all their cells and degrees, are loaded before any is used.
@@ -214,8 +264,7 @@ __device__ long long merge_delta_part(const DevGraph& g, const DevBM& bm, const 
                 term(key[q], j0 + q * nt < rn, m[q], o[q], deg[q]);
             }
     }
-    chunks_for_each(rhead, ch, t, nt, [&](int32_t c) { item(c, true); });
-    chunks_for_each(chead, ch, t, nt, [&](int32_t x) { item(x, false); });
+    walk(rhead, chead);
     acc = warp_sum_ll(acc);
     if (leader && kNP) {
         const int32_t Mrr = cells.get(r, r), Mrs = cells.get(r, s), Msr = cells.get(s, r), Mss = cells.get(s, s);
