@@ -75,6 +75,7 @@ struct WinResult {
     long long dS;
     int32_t v, r, s, nb, status, k, kout, kin, L, l2;  // l2: log2 of this vertex's hash size
     int32_t dB;  // kNP: change of the number of non-empty blocks if the move is applied
+    int32_t ni;  // slots of the hash taken by the neighbour blocks
 };
 
 // log2 of the neighbour-hash size for a vertex of degree k (at least twice k slots).
@@ -221,23 +222,41 @@ __device__ __forceinline__ int32_t warp_select_tiles(const int32_t* __restrict__
     return -1;
 }
 
+// Adds one to the count of key b, taking a slot for b when it is absent.  Returns the slot
+// when this call took it, else -1.
+__device__ __forceinline__ int32_t hinsert_fresh(int32_t* keys, int32_t* cnt, int log2cap, int32_t b) {
+    const uint32_t mask = (1u << log2cap) - 1u;
+    uint32_t s = hslot(b, log2cap);
+    for (uint32_t probe = 0; probe <= mask; ++probe) {
+        const int32_t k = ((volatile int32_t*)keys)[s];
+        if (k == -1) {
+            const int32_t prev = atomicCAS(keys + s, -1, b);
+            if (prev == -1 || prev == b) {
+                atomicAdd(cnt + s, 1);
+                return prev == -1 ? (int32_t)s : -1;
+            }
+        } else if (k == b) {
+            atomicAdd(cnt + s, 1);
+            return -1;
+        }
+        s = (s + 1) & mask;
+    }
+    return -1;
+}
+
 // Neighbour-block counts of v into the warp's hash (edge_weights + the block lookups of
 // blockmodel_delta): out-neighbours except v itself into hO, in-neighbours (self-loops
-// already excluded) into hI.  Neighbour ids, then their blocks, are loaded 8 per lane
-// before any insert.  Returns the block of neighbour number `pick` (the proposal's
-// sampled neighbour), or -1 when pick is out of range.
+// already excluded) into hI, the slots taken listed in items[] (their number in n, which
+// the caller zeroes).  Neighbour ids, then their blocks, are loaded 8 per lane before any
+// insert; each lane keeps the slots it took and one warp scan places them in the list.
+// The hash must be clean (keys -1, counts 0).  Returns the block of neighbour number
+// `pick` (the proposal's sampled neighbour), or -1 when pick is out of range.
 __device__ __forceinline__ int32_t warp_gather(const DevGraph& g, const int32_t* asg, int32_t v, int32_t r,
                                                int32_t o0, int32_t kout, int32_t i0, int32_t k, int32_t pick,
-                                               int32_t* hk, int32_t* hO, int32_t* hI, int log2cap) {
+                                               int32_t* hk, int32_t* hO, int32_t* hI, int log2cap, int32_t* items,
+                                               int32_t& n) {
     const int lane = threadIdx.x & 31;
-    const int cap = 1 << log2cap;
     int32_t nb = -1;
-    for (int i = lane; i < cap; i += 32) {
-        hk[i] = -1;
-        hO[i] = 0;
-        hI[i] = 0;
-    }
-    __syncwarp();
     for (int32_t base = 0; base < k; base += 256) {
         int32_t u[8], b[8];
 #pragma unroll
@@ -261,57 +280,73 @@ __device__ __forceinline__ int32_t warp_gather(const DevGraph& g, const int32_t*
                 }
             nb = __shfl_sync(SBP_FULL_MASK, uq == v ? r : bq, owner);
         }
+        int32_t fresh[8], nf = 0;
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
             const int32_t idx = base + lane + 32 * j;
-            if (b[j] >= 0) hinsert(hk, idx < kout ? hO : hI, log2cap, b[j]);
+            fresh[j] = b[j] >= 0 ? hinsert_fresh(hk, idx < kout ? hO : hI, log2cap, b[j]) : -1;
+            nf += fresh[j] >= 0;
         }
+        // the slots this lane took, appended after those of the lanes below it
+        int32_t off = nf;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int32_t y = __shfl_up_sync(SBP_FULL_MASK, off, o);
+            if (lane >= o) off += y;
+        }
+        const int32_t tot = __shfl_sync(SBP_FULL_MASK, off, 31);
+        off += n - nf;
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+            if (fresh[j] >= 0) items[off++] = fresh[j];
+        n += tot;
     }
     __syncwarp();
     return nb;
 }
 
 // entropy::delta_mdl for moving v from r to s over the gathered neighbour blocks; the same
-// terms as vertex_delta_fixed (exact int64, units of 2^-24), with the occupied hash slots
-// compacted into items[] and every cell of a pass loaded before it is used.
+// terms as vertex_delta_fixed (exact int64, units of 2^-24) over the n occupied hash slots
+// listed in items[], every cell of a pass loaded before it is used.  Log-table
+// entries are 32-bit and a cell term v * (L[v] - L[d_in] - L[d_out]) is formed without a
+// test for v = 0 (the product is 0 then); the logs of the degrees of r and s before and
+// after the move are looked up once, and the four cells of rows / columns r and s are
+// loaded before the hash is scanned.
 // kNP: nonparametric::delta_mdl (src/entropy.cpp:1146-1178) with block sizes `size` and
 // `nonempty` non-empty blocks.
 template <class Cells, bool kNP>
 __device__ long long warp_delta(const DevGraph& g, const int32_t* d_out, const int32_t* d_in, const Cells& M,
                                 int32_t r, int32_t s, int32_t kout, int32_t kin, int32_t L, const int32_t* hk,
-                                const int32_t* hO, const int32_t* hI, int log2cap, int32_t* items,
+                                const int32_t* hO, const int32_t* hI, const int32_t* items, int32_t n,
                                 const int32_t* lq_cache, const int32_t* size, int32_t nonempty) {
     const int lane = threadIdx.x & 31;
-    const int cap = 1 << log2cap;
-    const LogTabCached Lq{g.Lq, g.E + 1, lq_cache, kLqCache};
-    int32_t Or = 0, Ir = 0, Os = 0, Is = 0, n = 0;
-    for (int base = 0; base < cap; base += 32) {
-        const int i = base + lane;
-        const int32_t b = hk[i];
-        if (b == r) {
-            Or = hO[i];
-            Ir = hI[i];
-        } else if (b == s) {
-            Os = hO[i];
-            Is = hI[i];
-        }
-        const bool it = b >= 0 && b != r && b != s;
-        const unsigned m = __ballot_sync(SBP_FULL_MASK, it);
-        if (it) items[n + __popc(m & lanemask_lt())] = i;
-        n += __popc(m);
-    }
-    Or = warp_sum_i(Or);
-    Ir = warp_sum_i(Ir);
-    Os = warp_sum_i(Os);
-    Is = warp_sum_i(Is);
-    __syncwarp();
+    const int32_t hi = g.E + 1;
+    // fastlog table entry: the first kLqCache entries from shared memory
+    auto L32 = [&](int32_t x) -> int32_t {
+        x = max(0, min(x, hi));
+        return x < kLqCache ? lq_cache[x] : __ldg(g.Lq + x);
+    };
     const int32_t selfw = L > 0 ? 1 : 0;
     const int32_t dout_r = d_out[r], dout_s = d_out[s], din_r = d_in[r], din_s = d_in[s];
+    const int32_t Mrr = M.row_get(r, r), Mrs = M.row_get(r, s), Msr = M.row_get(s, r), Mss = M.row_get(s, s);
     const int32_t dout_r2 = dout_r - kout, dout_s2 = dout_s + kout;
     const int32_t din_r2 = din_r - (kin + selfw), din_s2 = din_s + (kin + selfw);
-    long long acc = 0, sRo = 0, sSo = 0, sRi = 0, sSi = 0;
+    int32_t lo_r = 0, lo_s = 0, li_r = 0, li_s = 0, lo_r2 = 0, lo_s2 = 0, li_r2 = 0, li_s2 = 0;
+    if (!kNP) {
+        lo_r = L32(dout_r);
+        lo_r2 = L32(dout_r2);
+        lo_s = L32(dout_s);
+        lo_s2 = L32(dout_s2);
+        li_r = L32(din_r);
+        li_r2 = L32(din_r2);
+        li_s = L32(din_s);
+        li_s2 = L32(din_s2);
+    }
+    int32_t Or = 0, Ir = 0, Os = 0, Is = 0;
+    long long acc = 0;
+    int32_t sRo = 0, sSo = 0, sRi = 0, sSi = 0;  // row / column sums of cells <= E
     for (int j0 = 0; j0 < n; j0 += 128) {
-        int32_t b[4], O[4], I[4], Mrb[4], Msb[4], Mbr[4], Mbs[4];
+        int32_t b[4], O[4], I[4], Mrb[4], Msb[4], Mbr[4], Mbs[4], dib[4], dob[4];
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
             const int jj = j0 + lane + 32 * q;
@@ -319,6 +354,18 @@ __device__ long long warp_delta(const DevGraph& g, const int32_t* d_out, const i
             b[q] = sl >= 0 ? hk[sl] : -1;
             O[q] = sl >= 0 ? hO[sl] : 0;
             I[q] = sl >= 0 ? hI[sl] : 0;
+            if (b[q] == r || b[q] == s) {  // the cells of r and s are handled after the loop
+                if (b[q] == r) {
+                    Or += O[q];
+                    Ir += I[q];
+                } else {
+                    Os += O[q];
+                    Is += I[q];
+                }
+                b[q] = -1;
+                O[q] = 0;
+                I[q] = 0;
+            }
         }
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
@@ -326,67 +373,70 @@ __device__ long long warp_delta(const DevGraph& g, const int32_t* d_out, const i
             Msb[q] = O[q] > 0 ? M.row_get(s, b[q]) : 0;
             Mbr[q] = I[q] > 0 ? M.col_get(r, b[q]) : 0;
             Mbs[q] = I[q] > 0 ? M.col_get(s, b[q]) : 0;
+            dib[q] = !kNP && O[q] > 0 ? d_in[b[q]] : 0;
+            dob[q] = !kNP && I[q] > 0 ? d_out[b[q]] : 0;
         }
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
-            if (b[q] < 0) continue;
             if constexpr (kNP) {
                 if (O[q] > 0) acc += np_cell(g, Mrb[q], -O[q]) + np_cell(g, Msb[q], O[q]);
                 if (I[q] > 0) acc += np_cell(g, Mbr[q], -I[q]) + np_cell(g, Mbs[q], I[q]);
                 continue;
             }
             if (O[q] > 0) {
-                const int32_t dinb = d_in[b[q]];
-                acc += ce_fixed(Lq, Mrb[q], dinb, dout_r) - ce_fixed(Lq, Mrb[q] - O[q], dinb, dout_r2);
-                acc += ce_fixed(Lq, Msb[q], dinb, dout_s) - ce_fixed(Lq, Msb[q] + O[q], dinb, dout_s2);
+                const int32_t ld = L32(dib[q]);
+                const int32_t a0 = L32(Mrb[q]), a1 = L32(Mrb[q] - O[q]), a2 = L32(Msb[q]), a3 = L32(Msb[q] + O[q]);
+                acc += (long long)Mrb[q] * (a0 - ld - lo_r) - (long long)(Mrb[q] - O[q]) * (a1 - ld - lo_r2) +
+                       (long long)Msb[q] * (a2 - ld - lo_s) - (long long)(Msb[q] + O[q]) * (a3 - ld - lo_s2);
                 sRo += Mrb[q];
                 sSo += Msb[q];
             }
             if (I[q] > 0) {
-                const int32_t doutb = d_out[b[q]];
-                acc += ce_fixed(Lq, Mbr[q], din_r, doutb) - ce_fixed(Lq, Mbr[q] - I[q], din_r2, doutb);
-                acc += ce_fixed(Lq, Mbs[q], din_s, doutb) - ce_fixed(Lq, Mbs[q] + I[q], din_s2, doutb);
+                const int32_t ld = L32(dob[q]);
+                const int32_t a0 = L32(Mbr[q]), a1 = L32(Mbr[q] - I[q]), a2 = L32(Mbs[q]), a3 = L32(Mbs[q] + I[q]);
+                acc += (long long)Mbr[q] * (a0 - li_r - ld) - (long long)(Mbr[q] - I[q]) * (a1 - li_r2 - ld) +
+                       (long long)Mbs[q] * (a2 - li_s - ld) - (long long)(Mbs[q] + I[q]) * (a3 - li_s2 - ld);
                 sRi += Mbr[q];
                 sSi += Mbs[q];
             }
         }
     }
+    Or = warp_sum_i(Or);
+    Ir = warp_sum_i(Ir);
+    Os = warp_sum_i(Os);
+    Is = warp_sum_i(Is);
     acc = warp_sum_ll(acc);
-    sRo = warp_sum_ll(sRo);
-    sSo = warp_sum_ll(sSo);
-    sRi = warp_sum_ll(sRi);
-    sSi = warp_sum_ll(sSi);
-    const int32_t Mrr = M.row_get(r, r), Mrs = M.row_get(r, s), Msr = M.row_get(s, r), Mss = M.row_get(s, s);
+    sRo = warp_sum_i(sRo);
+    sSo = warp_sum_i(sSo);
+    sRi = warp_sum_i(sRi);
+    sSi = warp_sum_i(sSi);
+    const int32_t d_rr = -Or - Ir - L, d_rs = Ir - Os, d_sr = Or - Is, d_ss = Os + Is + L;
     long long tot = acc;
     if constexpr (kNP) {
-        tot += np_cell(g, Mrr, -Or - Ir - L) + np_cell(g, Mrs, Ir - Os) + np_cell(g, Msr, Or - Is) +
-               np_cell(g, Mss, Os + Is + L);
+        tot += np_cell(g, Mrr, d_rr) + np_cell(g, Mrs, d_rs) + np_cell(g, Msr, d_sr) + np_cell(g, Mss, d_ss);
         return tot + np_block_terms(g, dout_r, din_r, size[r], dout_s, din_s, size[s], kout, kin, 1, nonempty);
     }
-    {
-        const int32_t d = -Or - Ir - L;
-        if (Or | Ir | L) tot += ce_fixed(Lq, Mrr, din_r, dout_r) - ce_fixed(Lq, Mrr + d, din_r2, dout_r2);
-        else tot += ce_delta(Lq, Mrr, din_r, dout_r, din_r2, dout_r2);
-    }
-    {
-        const int32_t d = Ir - Os;
-        if (Os | Ir) tot += ce_fixed(Lq, Mrs, din_s, dout_r) - ce_fixed(Lq, Mrs + d, din_s2, dout_r2);
-        if (d == 0) tot += ce_delta(Lq, Mrs, din_s, dout_r, din_s2, dout_r2);
-    }
-    {
-        const int32_t d = Or - Is;
-        if (Or | Is) tot += ce_fixed(Lq, Msr, din_r, dout_s) - ce_fixed(Lq, Msr + d, din_r2, dout_s2);
-        if (d == 0) tot += ce_delta(Lq, Msr, din_r, dout_s, din_r2, dout_s2);
-    }
-    {
-        const int32_t d = Os + Is + L;
-        if (Os | Is | L) tot += ce_fixed(Lq, Mss, din_s, dout_s) - ce_fixed(Lq, Mss + d, din_s2, dout_s2);
-        else tot += ce_delta(Lq, Mss, din_s, dout_s, din_s2, dout_s2);
-    }
-    tot += ((long long)dout_r - Mrr - Mrs - sRo) * (Lx(Lq, dout_r2) - Lx(Lq, dout_r));
-    tot += ((long long)dout_s - Msr - Mss - sSo) * (Lx(Lq, dout_s2) - Lx(Lq, dout_s));
-    tot += ((long long)din_r - Mrr - Msr - sRi) * (Lx(Lq, din_r2) - Lx(Lq, din_r));
-    tot += ((long long)din_s - Mrs - Mss - sSi) * (Lx(Lq, din_s2) - Lx(Lq, din_s));
+    const int32_t c0 = L32(Mrr), c1 = L32(Mrr + d_rr), c2 = L32(Mrs), c3 = L32(Mrs + d_rs);
+    const int32_t c4 = L32(Msr), c5 = L32(Msr + d_sr), c6 = L32(Mss), c7 = L32(Mss + d_ss);
+    // ce_fixed(v, d_in, d_out) - ce_fixed(v + d, d_in', d_out') of a changed cell, and
+    // ce_delta of an unchanged one (its degrees change only)
+    auto changed = [](int32_t v, int32_t d, int32_t lv, int32_t lvd, int32_t li, int32_t lo, int32_t li2,
+                      int32_t lo2) { return (long long)v * (lv - li - lo) - (long long)(v + d) * (lvd - li2 - lo2); };
+    auto unchanged = [](int32_t v, int32_t li, int32_t lo, int32_t li2, int32_t lo2) {
+        return (long long)v * ((li2 - li) + (lo2 - lo));
+    };
+    if (Or | Ir | L) tot += changed(Mrr, d_rr, c0, c1, li_r, lo_r, li_r2, lo_r2);
+    else tot += unchanged(Mrr, li_r, lo_r, li_r2, lo_r2);
+    if (Os | Ir) tot += changed(Mrs, d_rs, c2, c3, li_s, lo_r, li_s2, lo_r2);
+    if (d_rs == 0) tot += unchanged(Mrs, li_s, lo_r, li_s2, lo_r2);
+    if (Or | Is) tot += changed(Msr, d_sr, c4, c5, li_r, lo_s, li_r2, lo_s2);
+    if (d_sr == 0) tot += unchanged(Msr, li_r, lo_s, li_r2, lo_s2);
+    if (Os | Is | L) tot += changed(Mss, d_ss, c6, c7, li_s, lo_s, li_s2, lo_s2);
+    else tot += unchanged(Mss, li_s, lo_s, li_s2, lo_s2);
+    tot += ((long long)dout_r - Mrr - Mrs - sRo) * (lo_r2 - lo_r);
+    tot += ((long long)dout_s - Msr - Mss - sSo) * (lo_s2 - lo_s);
+    tot += ((long long)din_r - Mrr - Msr - sRi) * (li_r2 - li_r);
+    tot += ((long long)din_s - Mrs - Mss - sSi) * (li_s2 - li_s);
     return tot;
 }
 
@@ -417,17 +467,27 @@ __global__ void __launch_bounds__(kWinMaxWarps * 32, 1)
     int32_t* lq = hash + (4 << kSmemHashL2) * nwarps;  // the first kLqCache log-table entries
     int32_t* M = lq + kLqCache;                        // shared cells (kShared): B rows of ld
     // a vertex's hash: shared memory up to 2^kSmemHashL2 slots, else the warp's global region
+    // Each warp's hash: keys, out counts, in counts and the list of taken slots, at a fixed
+    // stride (2^kSmemHashL2 in shared memory, 2^kGlobalHashL2 in the global region) so that
+    // a slot keeps its place whatever the size of the hash that used it last.
     auto hash_of = [&](int w, int l2) {
         return l2 <= kSmemHashL2 ? hash + (4 << kSmemHashL2) * w : ghash + ((int64_t)4 << kGlobalHashL2) * w;
     };
     __shared__ WinResult res[kWinMaxWarps];
     __shared__ int32_t s_consumed, s_acc_mask, s_ne;
     __shared__ uint32_t s_conf[kWinMaxWarps];
+    __shared__ int32_t s_dirty[kWinMaxWarps];   // slots of the shared hash left by the last one
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const int nt = nwarps * 32;
     (void)cap;
 
     for (int i = tid; i < kLqCache; i += nt) lq[i] = __ldg(g.Lq + min(i, g.E + 1));
+    // the shared hashes start clean and are kept clean through their slot lists
+    for (int i = tid; i < nwarps << (kSmemHashL2 + 2); i += nt) {
+        const int part = (i >> kSmemHashL2) & 3;
+        if (part < 3) hash[i] = part == 0 ? -1 : 0;
+    }
+    if (tid < kWinMaxWarps) s_dirty[tid] = 0;
     if (tid == 0) s_ne = kNP ? *bm.nonempty : 0;
     if (kShared) {
         for (int i = tid; i < B * ld; i += nt) M[i] = 0;
@@ -459,6 +519,7 @@ __global__ void __launch_bounds__(kWinMaxWarps * 32, 1)
             c.nb = -1;
             c.dS = 0;
             c.dB = 0;
+            c.ni = 0;
             const int32_t o0 = __ldg(g.out_off + c.v), o1 = __ldg(g.out_off + c.v + 1);
             const int32_t i0 = __ldg(g.inns_off + c.v), i1 = __ldg(g.inns_off + c.v + 1);
             c.kout = o1 - o0;
@@ -467,16 +528,43 @@ __global__ void __launch_bounds__(kWinMaxWarps * 32, 1)
             c.L = __ldg(g.selfcnt + c.v);
             c.l2 = hash_log2(c.k, log2cap);
             c.status = ST_SKIP;
+            const bool in_smem = c.l2 <= kSmemHashL2;
+            const int32_t hs = in_smem ? 1 << kSmemHashL2 : 1 << kGlobalHashL2;
             int32_t* hk = hash_of(wid, c.l2);
-            int32_t* hO = hk + (1 << c.l2);
-            int32_t* hI = hO + (1 << c.l2);
-            int32_t* items = hI + (1 << c.l2);
+            int32_t* hO = hk + hs;
+            int32_t* hI = hO + hs;
+            int32_t* items = hI + hs;
             if (size[c.r] != 1) {  // a singleton block never moves (finetune.cpp:845)
                 uint32_t w[4];
                 philox4x32_10((uint32_t)c.v, iter, step, DOM_MH, seed, w);
+                // a clean hash: the shared one through the slot list of its last use, the
+                // global one (vertices of degree above 256) in full
+                if (in_smem) {
+                    const int32_t nd = s_dirty[wid];
+                    for (int j = lane; j < nd; j += 32) {
+                        const int32_t sl = items[j];
+                        hk[sl] = -1;
+                        hO[sl] = 0;
+                        hI[sl] = 0;
+                    }
+                } else {
+                    for (int i = lane; i < (1 << c.l2); i += 32) {
+                        hk[i] = -1;
+                        hO[i] = 0;
+                        hI[i] = 0;
+                    }
+                }
+                __syncwarp();
                 // the neighbour blocks first; the proposal's sampled neighbour is among them
                 const int32_t idx = c.k > 0 ? (int32_t)u32_below(w[0], (uint32_t)c.k) : -1;
-                const int32_t nbg = warp_gather(g, bm.asg, c.v, c.r, o0, c.kout, i0, c.k, idx, hk, hO, hI, c.l2);
+                // (the shared hash through pointers the compiler sees are shared: its inserts
+                // are then shared-memory atomics)
+                int32_t* sh = hash + (4 << kSmemHashL2) * wid;
+                const int32_t nbg =
+                    in_smem ? warp_gather(g, bm.asg, c.v, c.r, o0, c.kout, i0, c.k, idx, sh, sh + (1 << kSmemHashL2),
+                                          sh + (2 << kSmemHashL2), c.l2, sh + (3 << kSmemHashL2), c.ni)
+                            : warp_gather(g, bm.asg, c.v, c.r, o0, c.kout, i0, c.k, idx, hk, hO, hI, c.l2, items, c.ni);
+                if (in_smem && lane == 0) s_dirty[wid] = c.ni;
                 int32_t s;
                 if (c.k == 0) {
                     s = random_block(c.r, B, w[1]);
@@ -508,9 +596,9 @@ __global__ void __launch_bounds__(kWinMaxWarps * 32, 1)
                     c.s = s;
                     if constexpr (kNP) c.dB = np_count_change(size[c.r], size[s], 1);
                     c.dS = kShared ? warp_delta<SharedCells, kNP>(g, dout, din, sc, c.r, s, c.kout, c.kin, c.L, hk, hO,
-                                                                  hI, c.l2, items, lq, size, s_ne)
+                                                                  hI, items, c.ni, lq, size, s_ne)
                                    : warp_delta<GlobalCells, kNP>(g, dout, din, gc, c.r, s, c.kout, c.kin, c.L, hk, hO,
-                                                                  hI, c.l2, items, lq, size, s_ne);
+                                                                  hI, items, c.ni, lq, size, s_ne);
                     double H = 1.0;
                     if (!kNP && !greedy && c.k > 0) {  // entropy::hastings_correction (entropy.cpp:497-561)
                         H = kShared ? hastings_fixed<32>(sc, [&](int32_t b) { return dout[b] + din[b] - sc.row_get(b, b); },
@@ -526,8 +614,7 @@ __global__ void __launch_bounds__(kWinMaxWarps * 32, 1)
             }
             if (lane == 0) res[wid] = c;
         }
-        __syncthreads();
-        // ---- bit u of s_conf[j]: an accepted move of window entry u would change entry j
+        // bit u of s_conf[j]: an accepted move of window entry u would change entry j
         if (tid < kWinMaxWarps) s_conf[tid] = 0u;
         __syncthreads();
         if (tid < wn * wn) {
@@ -543,36 +630,42 @@ __global__ void __launch_bounds__(kWinMaxWarps * 32, 1)
             }
         }
         __syncthreads();
-        // ---- replay in order; stop before the first vertex an accepted move may change
-        if (tid == 0) {
-            int consumed = 0, acc_mask = 0;
-            for (int j = 0; j < wn; ++j) {
-                const WinResult& cj = res[j];
-                if (s_conf[j] & (uint32_t)acc_mask) break;
-                consumed = j + 1;
-                edges += cj.k;
-                if (cj.status == ST_ACCEPT) {
-                    acc_mask |= 1 << j;
-                    moved++;
-                    dsum += cj.dS;
-                    s_ne += cj.dB;  // blockmodel.cpp:429-430
-                }
+        // ---- replay in order; stop before the first vertex an accepted move may change.
+        // s_conf[j] holds accepted entries before j only, and every entry before the stop
+        // is taken, so the stop is the first entry with a conflict bit: one ballot.
+        if (wid == 0) {
+            const unsigned stop = __ballot_sync(SBP_FULL_MASK, lane < wn && s_conf[lane] != 0u);
+            const int consumed = stop ? __ffs(stop) - 1 : wn;
+            const bool taken = lane < consumed;
+            const bool acc = taken && res[lane].status == ST_ACCEPT;
+            const unsigned acc_mask = __ballot_sync(SBP_FULL_MASK, acc);
+            const int32_t k_sum = warp_sum_i(taken ? res[lane].k : 0);
+            const long long d_sum = warp_sum_ll(acc ? res[lane].dS : 0ll);
+            const int32_t dB_sum = warp_sum_i(acc ? res[lane].dB : 0);
+            if (lane == 0) {
+                edges += (unsigned long long)k_sum;
+                moved += (unsigned long long)__popc(acc_mask);
+                dsum += d_sum;
+                s_ne += dB_sum;  // blockmodel.cpp:429-430
+                s_consumed = consumed;
+                s_acc_mask = (int32_t)acc_mask;
+                ++rounds;
             }
-            s_consumed = consumed;
-            s_acc_mask = acc_mask;
-            ++rounds;
         }
         __syncthreads();
         // ---- apply the accepted moves (Blockmodel::move_vertex, blockmodel.cpp:408-435)
         if (wid < wn && ((s_acc_mask >> wid) & 1)) {
             const WinResult c = res[wid];
             const int32_t r = c.r, s = c.s;
+            const int32_t hs = c.l2 <= kSmemHashL2 ? 1 << kSmemHashL2 : 1 << kGlobalHashL2;
             const int32_t* hk = hash_of(wid, c.l2);
-            const int32_t* hO = hk + (1 << c.l2);
-            const int32_t* hI = hO + (1 << c.l2);
-            for (int i = lane; i < (1 << c.l2); i += 32) {
+            const int32_t* hO = hk + hs;
+            const int32_t* hI = hO + hs;
+            const int32_t* items = hI + hs;
+            for (int j = lane; j < c.ni; j += 32) {
+                const int i = items[j];
                 const int32_t b = hk[i];
-                if (b < 0 || b == r || b == s) continue;
+                if (b == r || b == s) continue;
                 const int32_t O = hO[i], I = hI[i];
                 if (kShared) {
                     if (O) {
