@@ -158,13 +158,18 @@ template <class Cells, bool kNP>
 __device__ long long merge_delta_part(const DevGraph& g, const DevBM& bm, const DevChain& ch, const Cells& cells,
                                       int32_t r, int32_t s, int t, int nt, bool leader, uint32_t* bloom,
                                       unsigned long long& keys_seen) {
-    const LogTab Lq{g.Lq, g.E + 1};
+    const int32_t hi = g.E + 1;
+    // fastlog table entry, 32-bit (cells and degrees are at most E)
+    auto L32 = [&](int32_t x) -> int32_t { return __ldg(g.Lq + max(0, min(x, hi))); };
     const int32_t dout_r = bm.d_out[r], din_r = bm.d_in[r], dout_s = bm.d_out[s], din_s = bm.d_in[s];
     const int32_t dout_s2 = dout_s + dout_r, din_s2 = din_s + din_r;
-    const long long Lout = Lx(Lq, dout_s2) - Lx(Lq, dout_s), Lin = Lx(Lq, din_s2) - Lx(Lq, din_s);
+    const int32_t lo_r = L32(dout_r), li_r = L32(din_r), lo_s = L32(dout_s), li_s = L32(din_s);
+    const int32_t lo_s2 = L32(dout_s2), li_s2 = L32(din_s2);
+    const long long Lout = lo_s2 - lo_s, Lin = li_s2 - li_s;
     long long acc = 0;
     // is_row: cell (r, key) moving to (s, key), factor d_in[key]; else (key, r) -> (key, s),
-    // factor d_out[key].  Both forms load their three values before using any of them.
+    // factor d_out[key].  Both forms load their three values before using any of them; a
+    // cell term v * (L[v] - L[deg] - L[own]) needs no test for v = 0 (the product is 0).
     auto term = [&](int32_t key, bool is_row, int32_t m, int32_t o, int32_t deg) {
         if (m == 0 || (!is_row && key == r)) return;
         bloom_add(bloom, key);
@@ -173,11 +178,13 @@ __device__ long long merge_delta_part(const DevGraph& g, const DevBM& bm, const 
             if (is_row ? (key != r && key != s) : (key != s)) acc += np_cell(g, o, m);
             return;
         }
-        const int32_t own = is_row ? dout_r : din_r;
-        acc += ce_fixed(Lq, m, deg, own);
-        if (is_row ? (key != r && key != s) : (key != s)) {
-            const int32_t ds = is_row ? dout_s : din_s, ds2 = is_row ? dout_s2 : din_s2;
-            acc += ce_fixed(Lq, o, deg, ds) - ce_fixed(Lq, o + m, deg, ds2) - (long long)o * (is_row ? Lout : Lin);
+        const bool third = is_row ? (key != r && key != s) : (key != s);
+        const int32_t ld = L32(deg), lm = L32(m), lo = L32(third ? o : 0), lom = L32(third ? o + m : 0);
+        acc += (long long)m * (lm - ld - (is_row ? lo_r : li_r));
+        if (third) {
+            const int32_t ls = is_row ? lo_s : li_s, ls2 = is_row ? lo_s2 : li_s2;
+            acc += (long long)o * (lo - ld - ls) - (long long)(o + m) * (lom - ld - ls2) -
+                   (long long)o * (is_row ? Lout : Lin);
         }
     };
     // The appended chunks of row r and of column r, walked together: each step takes the next
@@ -274,8 +281,9 @@ __device__ long long merge_delta_part(const DevGraph& g, const DevBM& bm, const 
     } else if (leader) {
         const int32_t Mrr = cells.get(r, r), Mrs = cells.get(r, s), Msr = cells.get(s, r), Mss = cells.get(s, s);
         const int32_t dss = Mrr + Mrs + Msr;
-        if (dss > 0) acc += ce_fixed(Lq, Mss, din_s, dout_s) - ce_fixed(Lq, Mss + dss, din_s2, dout_s2);
-        else acc += ce_delta(Lq, Mss, din_s, dout_s, din_s2, dout_s2);
+        if (dss > 0)
+            acc += (long long)Mss * (L32(Mss) - li_s - lo_s) - (long long)(Mss + dss) * (L32(Mss + dss) - li_s2 - lo_s2);
+        else acc += (long long)Mss * ((li_s2 - li_s) + (lo_s2 - lo_s));
         acc += ((long long)dout_s - Msr - Mss) * Lout + ((long long)din_s - Mrs - Mss) * Lin;
     }
     return acc;

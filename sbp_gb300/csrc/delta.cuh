@@ -192,11 +192,25 @@ __device__ long long vertex_delta_fixed(const DevGraph& g, const int32_t* asg, c
     }
     for (int32_t i = i0 + t; i < i1; i += kThreads) hinsert(hk, hI, log2cap, asg[__ldg(g.inns_nbr + i)]);
     G::sync();
-    const LogTab Lq{g.Lq, g.E + 1};
+    const int32_t hi = g.E + 1;
+    // fastlog table entry, 32-bit (cells and degrees are at most E); a cell term
+    // v * (L[v] - L[d_in] - L[d_out]) is formed without a test for v = 0 (the product is 0)
+    auto L32 = [&](int32_t x) -> int32_t { return __ldg(g.Lq + max(0, min(x, hi))); };
     const int32_t kout = o1 - o0, kin = i1 - i0, L = __ldg(g.selfcnt + v), selfw = L > 0 ? 1 : 0;
     const int32_t dout_r = d_out[r], dout_s = d_out[s], din_r = d_in[r], din_s = d_in[s];
     const int32_t dout_r2 = dout_r - kout, dout_s2 = dout_s + kout;
     const int32_t din_r2 = din_r - (kin + selfw), din_s2 = din_s + (kin + selfw);
+    int32_t lo_r = 0, lo_s = 0, li_r = 0, li_s = 0, lo_r2 = 0, lo_s2 = 0, li_r2 = 0, li_s2 = 0;
+    if (!kNP) {
+        lo_r = L32(dout_r);
+        lo_r2 = L32(dout_r2);
+        lo_s = L32(dout_s);
+        lo_s2 = L32(dout_s2);
+        li_r = L32(din_r);
+        li_r2 = L32(din_r2);
+        li_s = L32(din_s);
+        li_s2 = L32(din_s2);
+    }
     long long acc = 0, sRo = 0, sSo = 0, sRi = 0, sSi = 0, spec = 0;
     for (int i = t; i < cap; i += kThreads) {
         const int32_t b = hk[i];
@@ -216,16 +230,18 @@ __device__ long long vertex_delta_fixed(const DevGraph& g, const int32_t* asg, c
             continue;
         }
         if (O > 0) {
-            const int32_t Mrb = M.row_get(r, b), Msb = M.row_get(s, b), dinb = d_in[b];
-            acc += ce_fixed(Lq, Mrb, dinb, dout_r) - ce_fixed(Lq, Mrb - O, dinb, dout_r2);
-            acc += ce_fixed(Lq, Msb, dinb, dout_s) - ce_fixed(Lq, Msb + O, dinb, dout_s2);
+            const int32_t Mrb = M.row_get(r, b), Msb = M.row_get(s, b), ld = L32(d_in[b]);
+            const int32_t a0 = L32(Mrb), a1 = L32(Mrb - O), a2 = L32(Msb), a3 = L32(Msb + O);
+            acc += (long long)Mrb * (a0 - ld - lo_r) - (long long)(Mrb - O) * (a1 - ld - lo_r2) +
+                   (long long)Msb * (a2 - ld - lo_s) - (long long)(Msb + O) * (a3 - ld - lo_s2);
             sRo += Mrb;
             sSo += Msb;
         }
         if (I > 0) {
-            const int32_t Mbr = M.col_get(r, b), Mbs = M.col_get(s, b), doutb = d_out[b];
-            acc += ce_fixed(Lq, Mbr, din_r, doutb) - ce_fixed(Lq, Mbr - I, din_r2, doutb);
-            acc += ce_fixed(Lq, Mbs, din_s, doutb) - ce_fixed(Lq, Mbs + I, din_s2, doutb);
+            const int32_t Mbr = M.col_get(r, b), Mbs = M.col_get(s, b), ld = L32(d_out[b]);
+            const int32_t a0 = L32(Mbr), a1 = L32(Mbr - I), a2 = L32(Mbs), a3 = L32(Mbs + I);
+            acc += (long long)Mbr * (a0 - li_r - ld) - (long long)(Mbr - I) * (a1 - li_r2 - ld) +
+                   (long long)Mbs * (a2 - li_s - ld) - (long long)(Mbs + I) * (a3 - li_s2 - ld);
             sRi += Mbr;
             sSi += Mbs;
         }
@@ -250,31 +266,33 @@ __device__ long long vertex_delta_fixed(const DevGraph& g, const int32_t* asg, c
                np_cell(g, Mss, Os + Is + L);
         return tot + np_block_terms(g, dout_r, din_r, sizes[r], dout_s, din_s, sizes[s], kout, kin, 1, nonempty);
     }
-    {   // (r, r): present iff a neighbour lies in r or a self-loop exists; its change is never zero.
-        const int32_t d = -Or - Ir - L;
-        if (Or | Ir | L) tot += ce_fixed(Lq, Mrr, din_r, dout_r) - ce_fixed(Lq, Mrr + d, din_r2, dout_r2);
-        else tot += ce_delta(Lq, Mrr, din_r, dout_r, din_r2, dout_r2);
-    }
-    {   // (r, s): may be present with a zero change; then both loops count it.
-        const int32_t d = Ir - Os;
-        if (Os | Ir) tot += ce_fixed(Lq, Mrs, din_s, dout_r) - ce_fixed(Lq, Mrs + d, din_s2, dout_r2);
-        if (d == 0) tot += ce_delta(Lq, Mrs, din_s, dout_r, din_s2, dout_r2);
-    }
-    {   // (s, r)
-        const int32_t d = Or - Is;
-        if (Or | Is) tot += ce_fixed(Lq, Msr, din_r, dout_s) - ce_fixed(Lq, Msr + d, din_r2, dout_s2);
-        if (d == 0) tot += ce_delta(Lq, Msr, din_r, dout_s, din_r2, dout_s2);
-    }
-    {   // (s, s)
-        const int32_t d = Os + Is + L;
-        if (Os | Is | L) tot += ce_fixed(Lq, Mss, din_s, dout_s) - ce_fixed(Lq, Mss + d, din_s2, dout_s2);
-        else tot += ce_delta(Lq, Mss, din_s, dout_s, din_s2, dout_s2);
-    }
+    const int32_t d_rr = -Or - Ir - L, d_rs = Ir - Os, d_sr = Or - Is, d_ss = Os + Is + L;
+    const int32_t c0 = L32(Mrr), c1 = L32(Mrr + d_rr), c2 = L32(Mrs), c3 = L32(Mrs + d_rs);
+    const int32_t c4 = L32(Msr), c5 = L32(Msr + d_sr), c6 = L32(Mss), c7 = L32(Mss + d_ss);
+    // ce_fixed(v, d_in, d_out) - ce_fixed(v + d, d_in', d_out') of a changed cell, and
+    // ce_delta of an unchanged one (its degrees change only)
+    auto changed = [](int32_t x, int32_t d, int32_t lv, int32_t lvd, int32_t li, int32_t lo, int32_t li2,
+                      int32_t lo2) { return (long long)x * (lv - li - lo) - (long long)(x + d) * (lvd - li2 - lo2); };
+    auto unchanged = [](int32_t x, int32_t li, int32_t lo, int32_t li2, int32_t lo2) {
+        return (long long)x * ((li2 - li) + (lo2 - lo));
+    };
+    // (r, r): present iff a neighbour lies in r or a self-loop exists; its change is never zero.
+    if (Or | Ir | L) tot += changed(Mrr, d_rr, c0, c1, li_r, lo_r, li_r2, lo_r2);
+    else tot += unchanged(Mrr, li_r, lo_r, li_r2, lo_r2);
+    // (r, s): may be present with a zero change; then both loops count it.
+    if (Os | Ir) tot += changed(Mrs, d_rs, c2, c3, li_s, lo_r, li_s2, lo_r2);
+    if (d_rs == 0) tot += unchanged(Mrs, li_s, lo_r, li_s2, lo_r2);
+    // (s, r)
+    if (Or | Is) tot += changed(Msr, d_sr, c4, c5, li_r, lo_s, li_r2, lo_s2);
+    if (d_sr == 0) tot += unchanged(Msr, li_r, lo_s, li_r2, lo_s2);
+    // (s, s)
+    if (Os | Is | L) tot += changed(Mss, d_ss, c6, c7, li_s, lo_s, li_s2, lo_s2);
+    else tot += unchanged(Mss, li_s, lo_s, li_s2, lo_s2);
     // Unchanged cells of rows r, s and columns r, s (entropy.cpp:346-401).
-    tot += ((long long)dout_r - Mrr - Mrs - sRo) * (Lx(Lq, dout_r2) - Lx(Lq, dout_r));
-    tot += ((long long)dout_s - Msr - Mss - sSo) * (Lx(Lq, dout_s2) - Lx(Lq, dout_s));
-    tot += ((long long)din_r - Mrr - Msr - sRi) * (Lx(Lq, din_r2) - Lx(Lq, din_r));
-    tot += ((long long)din_s - Mrs - Mss - sSi) * (Lx(Lq, din_s2) - Lx(Lq, din_s));
+    tot += ((long long)dout_r - Mrr - Mrs - sRo) * (lo_r2 - lo_r);
+    tot += ((long long)dout_s - Msr - Mss - sSo) * (lo_s2 - lo_s);
+    tot += ((long long)din_r - Mrr - Msr - sRi) * (li_r2 - li_r);
+    tot += ((long long)din_s - Mrs - Mss - sSi) * (li_s2 - li_s);
     return tot;
 }
 
