@@ -27,6 +27,7 @@
 // shared memory unless B is large.  Each warp's neighbour hash lives in shared memory (up
 // to 512 slots) or, for vertices of degree above 256, in a per-warp global region.  Only
 // the assignment is written back; the caller rebuilds afterwards.
+#include <climits>
 #include <stdexcept>
 
 #include "delta.cuh"
@@ -175,10 +176,11 @@ __device__ __forceinline__ int32_t hash_get(const int32_t* hk, const int32_t* cn
 // Entry at cumulative unit t of a global row through its tile sums: lane l takes tiles
 // [8l, 8l + 8) of each group of 256 tiles (one load each), a warp scan over the lanes'
 // totals finds the tile, then one pass over that tile (16-byte loads) finds the entry.
-// Entry `skip` (weight skip_w) is left out.
+// Entry `skip` (weight skip_w) is left out.  pre, when given, holds this lane's tile sums
+// of the first group, loaded earlier.
 __device__ __forceinline__ int32_t warp_select_tiles(const int32_t* __restrict__ row, const int32_t* __restrict__ ts,
                                                      int32_t B, int32_t nt, long long t, int32_t skip,
-                                                     int32_t skip_w) {
+                                                     int32_t skip_w, const int32_t* pre = nullptr) {
     const int lane = threadIdx.x & 31;
     const int32_t skip_tile = skip >= 0 ? skip >> 7 : -1;
     for (int32_t tb = 0; tb < nt; tb += 256) {
@@ -187,7 +189,7 @@ __device__ __forceinline__ int32_t warp_select_tiles(const int32_t* __restrict__
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
             const int32_t tile = tb + 8 * lane + j;
-            x[j] = tile < nt ? __ldcg(ts + tile) - (tile == skip_tile ? skip_w : 0) : 0;
+            x[j] = tile < nt ? (pre && tb == 0 ? pre[j] : __ldcg(ts + tile)) - (tile == skip_tile ? skip_w : 0) : 0;
             mine += x[j];
         }
         long long incl = mine;
@@ -222,11 +224,10 @@ __device__ __forceinline__ int32_t warp_select_tiles(const int32_t* __restrict__
     return -1;
 }
 
-// Adds one to the count of key b, taking a slot for b when it is absent.  Returns the slot
-// when this call took it, else -1.
-__device__ __forceinline__ int32_t hinsert_fresh(int32_t* keys, int32_t* cnt, int log2cap, int32_t b) {
+// Adds one to the count of key b, taking a slot for b when it is absent, probing from slot
+// s.  Returns the slot when this call took it, else -1.
+__device__ __forceinline__ int32_t hinsert_fresh(int32_t* keys, int32_t* cnt, int log2cap, int32_t b, uint32_t s) {
     const uint32_t mask = (1u << log2cap) - 1u;
-    uint32_t s = hslot(b, log2cap);
     for (uint32_t probe = 0; probe <= mask; ++probe) {
         const int32_t k = ((volatile int32_t*)keys)[s];
         if (k == -1) {
@@ -249,12 +250,14 @@ __device__ __forceinline__ int32_t hinsert_fresh(int32_t* keys, int32_t* cnt, in
 // already excluded) into hI, the slots taken listed in items[] (their number in n, which
 // the caller zeroes).  Neighbour ids, then their blocks, are loaded 8 per lane before any
 // insert; each lane keeps the slots it took and one warp scan places them in the list.
-// The hash must be clean (keys -1, counts 0).  Returns the block of neighbour number
-// `pick` (the proposal's sampled neighbour), or -1 when pick is out of range.
+// on_nb(nb) is called as soon as the block nb of neighbour number `pick` (the proposal's
+// sampled neighbour) is known.  The hash must be clean (keys -1, counts 0).  Returns nb,
+// or -1 when pick is out of range.
+template <class OnNb>
 __device__ __forceinline__ int32_t warp_gather(const DevGraph& g, const int32_t* asg, int32_t v, int32_t r,
                                                int32_t o0, int32_t kout, int32_t i0, int32_t k, int32_t pick,
                                                int32_t* hk, int32_t* hO, int32_t* hI, int log2cap, int32_t* items,
-                                               int32_t& n) {
+                                               int32_t& n, OnNb on_nb) {
     const int lane = threadIdx.x & 31;
     int32_t nb = -1;
     for (int32_t base = 0; base < k; base += 256) {
@@ -279,12 +282,36 @@ __device__ __forceinline__ int32_t warp_gather(const DevGraph& g, const int32_t*
                     uq = u[j];
                 }
             nb = __shfl_sync(SBP_FULL_MASK, uq == v ? r : bq, owner);
+            on_nb(nb);  // loads that need only nb start before the inserts
         }
-        int32_t fresh[8], nf = 0;
+        // The eight inserts of a lane in three batches: the home slots' keys, then a take of
+        // every empty home slot, then the counts; a key whose home slot holds another key
+        // probes on alone.
+        uint32_t sl[8];
+        int32_t kk[8], fresh[8], nf = 0;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            sl[j] = b[j] >= 0 ? hslot(b[j], log2cap) : 0u;
+            kk[j] = b[j] >= 0 ? ((volatile int32_t*)hk)[sl[j]] : 0;
+        }
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+            if (b[j] >= 0 && kk[j] == -1) {
+                const int32_t prev = atomicCAS(hk + sl[j], -1, b[j]);
+                kk[j] = prev == -1 ? INT_MIN : prev;  // INT_MIN: taken by this insert
+            }
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
             const int32_t idx = base + lane + 32 * j;
-            fresh[j] = b[j] >= 0 ? hinsert_fresh(hk, idx < kout ? hO : hI, log2cap, b[j]) : -1;
+            int32_t* cnt = idx < kout ? hO : hI;
+            fresh[j] = -1;
+            if (b[j] < 0) continue;
+            if (kk[j] == INT_MIN || kk[j] == b[j]) {
+                atomicAdd(cnt + sl[j], 1);
+                if (kk[j] == INT_MIN) fresh[j] = (int32_t)sl[j];
+            } else {
+                fresh[j] = hinsert_fresh(hk, cnt, log2cap, b[j], (sl[j] + 1) & ((1u << log2cap) - 1u));
+            }
             nf += fresh[j] >= 0;
         }
         // the slots this lane took, appended after those of the lanes below it
@@ -506,14 +533,14 @@ __global__ void __launch_bounds__(kWinMaxWarps * 32, 1)
 
     unsigned long long edges = 0, moved = 0, rounds = 0;
     long long dsum = 0;
-    int32_t it0 = 0;
+    int32_t it0 = 0, next_pos = -1, next_v = -1;
     int guard = 0;
     while (it0 < n && guard++ < (1 << 30)) {
         const int wn = min(nwarps, n - it0);
         // ---- evaluate the next wn vertices against the current state, one warp each
         if (wid < wn) {
             WinResult c;
-            c.v = order[it0 + wid];
+            c.v = next_pos == it0 + wid ? next_v : order[it0 + wid];
             c.r = __ldcg(bm.asg + c.v);
             c.s = -1;
             c.nb = -1;
@@ -559,11 +586,27 @@ __global__ void __launch_bounds__(kWinMaxWarps * 32, 1)
                 const int32_t idx = c.k > 0 ? (int32_t)u32_below(w[0], (uint32_t)c.k) : -1;
                 // (the shared hash through pointers the compiler sees are shared: its inserts
                 // are then shared-memory atomics)
+                // the sampler's first reads (cell (nb, nb), nb's degrees and the first group
+                // of tile sums of its row and column), issued before the hash inserts
+                int32_t p_dnn = 0, p_R = 0, p_din = 0, p_tr[8], p_tc[8];
+                auto on_nb = [&](int32_t nb) {
+                    if (kShared || nb < 0) return;
+                    p_dnn = gc.row_get(nb, nb);
+                    p_R = dout[nb];
+                    p_din = din[nb];
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) {
+                        const int32_t tile = 8 * lane + j;
+                        p_tr[j] = tile < gc.nt ? __ldcg(gc.TS + (int64_t)nb * gc.nt + tile) : 0;
+                        p_tc[j] = tile < gc.nt ? __ldcg(gc.TST + (int64_t)nb * gc.nt + tile) : 0;
+                    }
+                };
                 int32_t* sh = hash + (4 << kSmemHashL2) * wid;
                 const int32_t nbg =
                     in_smem ? warp_gather(g, bm.asg, c.v, c.r, o0, c.kout, i0, c.k, idx, sh, sh + (1 << kSmemHashL2),
-                                          sh + (2 << kSmemHashL2), c.l2, sh + (3 << kSmemHashL2), c.ni)
-                            : warp_gather(g, bm.asg, c.v, c.r, o0, c.kout, i0, c.k, idx, hk, hO, hI, c.l2, items, c.ni);
+                                          sh + (2 << kSmemHashL2), c.l2, sh + (3 << kSmemHashL2), c.ni, on_nb)
+                            : warp_gather(g, bm.asg, c.v, c.r, o0, c.kout, i0, c.k, idx, hk, hO, hI, c.l2, items, c.ni,
+                                          on_nb);
                 if (in_smem && lane == 0) s_dirty[wid] = c.ni;
                 int32_t s;
                 if (c.k == 0) {
@@ -573,18 +616,18 @@ __global__ void __launch_bounds__(kWinMaxWarps * 32, 1)
                     // nb's row (ascending column) followed by its column without the diagonal
                     const int32_t nb = nbg;
                     c.nb = nb;
-                    const int32_t dnn = kShared ? sc.row_get(nb, nb) : gc.row_get(nb, nb);
-                    const long long R = dout[nb], C = (long long)din[nb] - dnn;
+                    const int32_t dnn = kShared ? sc.row_get(nb, nb) : p_dnn;
+                    const long long R = kShared ? dout[nb] : p_R, C = (long long)(kShared ? din[nb] : p_din) - dnn;
                     long long t = (long long)u64_below(w[1], w[2], (uint64_t)(R + C));
                     if (t < R) {
                         s = kShared ? warp_select(B, t, [&](int32_t i) { return sc.row_get(nb, i); })
                                     : warp_select_tiles(gc.M + (int64_t)nb * ld, gc.TS + (int64_t)nb * gc.nt, B,
-                                                        gc.nt, t, -1, 0);
+                                                        gc.nt, t, -1, 0, p_tr);
                     } else {
                         t -= R;
                         s = kShared ? warp_select(B, t, [&](int32_t i) { return i == nb ? 0 : sc.row_get(i, nb); })
                                     : warp_select_tiles(gc.MT + (int64_t)nb * ld, gc.TST + (int64_t)nb * gc.nt, B,
-                                                        gc.nt, t, nb, dnn);
+                                                        gc.nt, t, nb, dnn, p_tc);
                     }
                 }
                 if (s < 0) {
@@ -653,6 +696,10 @@ __global__ void __launch_bounds__(kWinMaxWarps * 32, 1)
             }
         }
         __syncthreads();
+        // the vertex this warp evaluates next, loaded while the moves are applied
+        next_pos = it0 + s_consumed + wid;
+        if (wid < nwarps && next_pos < n) next_v = __ldg(order + next_pos);
+        else next_pos = -1;
         // ---- apply the accepted moves (Blockmodel::move_vertex, blockmodel.cpp:408-435)
         if (wid < wn && ((s_acc_mask >> wid) & 1)) {
             const WinResult c = res[wid];
