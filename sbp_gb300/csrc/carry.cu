@@ -450,91 +450,121 @@ __global__ void __launch_bounds__(kCarryThreads, 1) k_carry_out(
             sh.c_act[tid] = aq;
         }
         __syncthreads();
-        // ---- 3. replay the queue rule (block_merge.cpp:54-95)
-        if (tid == 0) {
-            int i = 0, nq = 0, nm = 0, cons[3] = {0, 0, 0};
+        // ---- 3. replay the queue rule (block_merge.cpp:54-95) on warp 0.  Lane l holds
+        // candidate l and entry l of the round's put-back list (sorted by delta, block) in
+        // registers: a pop shifts the list down one lane, a put-back finds its place with a
+        // ballot (the list holds each block at most once, so no two keys are equal) and
+        // shifts the entries above it up one lane.
+        if (warp == 0) {
+            const bool lc = lane < ncand;
+            const long long cd = lc ? sh.c_dS[lane] : 0, cact = lc ? sh.c_act[lane] : 0;
+            const int32_t cb = lc ? sh.c_blk[lane] : 0, cto = lc ? sh.c_to[lane] : 0;
+            const int32_t csrc = lc ? sh.c_src[lane] : 0, ckeys = lc ? sh.c_keys[lane] : 0;
+            const int32_t ccount = lc ? sh.c_count[lane] : 0;
+            const uint32_t cconf = lc ? sh.conf[lane] : 0u;
+            long long qd = 0;
+            int32_t qb = 0, qt = 0, qc = 0;
+            int i = 0, nq = 0, nm = 0, cons0 = 0, cons1 = 0, cons2 = 0;
             uint32_t merged_mask = 0u;  // candidates merged in this round
             const bool hb = sh.has_bound;
-            // may a merge of this round have changed the evaluation of candidate ci?
-            auto dirty = [&](int ci) { return (sh.conf[ci] & merged_mask) != 0u; };
-            while (sh.merged + nm < num_to_merge) {
-                int pick = -1;
-                long long bd = 0;
-                int32_t bb = 0;
-                if (i < ncand) {
-                    pick = 0;
-                    bd = sh.c_dS[i];
-                    bb = sh.c_blk[i];
-                }
-                if (nq > 0 && (pick < 0 || qless(sh.q_dS[0], sh.q_blk[0], bd, bb))) {
+            const long long bnd_dS = sh.b_dS, merged0 = sh.merged;
+            const int32_t bnd_blk = sh.b_blk, ne0 = sh.ne;
+            // each candidate is taken once and put back at most once
+            for (int it = 0; it <= 2 * kMaxW + 1 && merged0 + nm < num_to_merge; ++it) {
+                const long long hc_d = __shfl_sync(SBP_FULL_MASK, cd, i & 31);
+                const int32_t hc_b = __shfl_sync(SBP_FULL_MASK, cb, i & 31);
+                const long long hq_d = __shfl_sync(SBP_FULL_MASK, qd, 0);
+                const int32_t hq_b = __shfl_sync(SBP_FULL_MASK, qb, 0);
+                int pick = i < ncand ? 0 : -1;
+                long long bd = hc_d;
+                int32_t bb = hc_b;
+                if (nq > 0 && (pick < 0 || qless(hq_d, hq_b, bd, bb))) {
                     pick = 1;
-                    bd = sh.q_dS[0];
-                    bb = sh.q_blk[0];
+                    bd = hq_d;
+                    bb = hq_b;
                 }
-                if (pick < 0) break;                                      // queue empty
-                if (hb && qless(sh.b_dS, sh.b_blk, bd, bb)) break;        // next pop not evaluated
+                if (pick < 0) break;                                  // queue empty
+                if (hb && qless(bnd_dS, bnd_blk, bd, bb)) break;      // next pop not evaluated
                 int ci;
                 int32_t from, to;
                 if (pick == 1) {
                     // popped again: if no merge since touched what it read, its recomputed
                     // delta is the one it was put back with (kNP: up to the count term)
-                    ci = sh.q_cand[0];
-                    if (dirty(ci)) break;
-                    from = sh.q_blk[0];
-                    to = sh.q_to[0];
-                    for (int k = 1; k < nq; ++k) {
-                        sh.q_dS[k - 1] = sh.q_dS[k];
-                        sh.q_blk[k - 1] = sh.q_blk[k];
-                        sh.q_to[k - 1] = sh.q_to[k];
-                        sh.q_cand[k - 1] = sh.q_cand[k];
-                    }
+                    ci = __shfl_sync(SBP_FULL_MASK, qc, 0);
+                    if (__shfl_sync(SBP_FULL_MASK, cconf, ci) & merged_mask) break;
+                    from = hq_b;
+                    to = __shfl_sync(SBP_FULL_MASK, qt, 0);
+                    qd = __shfl_down_sync(SBP_FULL_MASK, qd, 1);
+                    qb = __shfl_down_sync(SBP_FULL_MASK, qb, 1);
+                    qt = __shfl_down_sync(SBP_FULL_MASK, qt, 1);
+                    qc = __shfl_down_sync(SBP_FULL_MASK, qc, 1);
                     --nq;
                 } else {
-                    if (dirty(i)) break;  // its value is stale: re-evaluate it next round
-                    from = sh.c_blk[i];
-                    to = sh.c_to[i];
-                    ++cons[sh.c_src[i]];
+                    // its value is stale: re-evaluate it next round
+                    if (__shfl_sync(SBP_FULL_MASK, cconf, i) & merged_mask) break;
+                    from = hc_b;
+                    to = __shfl_sync(SBP_FULL_MASK, cto, i);
+                    const int32_t src = __shfl_sync(SBP_FULL_MASK, csrc, i);
+                    cons0 += src == 0;
+                    cons1 += src == 1;
+                    cons2 += src == 2;
                     ci = i++;
                     if (to == from) continue;  // already in the same block
                 }
-                long long act = sh.c_act[ci];
-                if (kNP && sh.c_count[ci]) {
-                    const int32_t b = min(max(sh.ne - nm, 0), g.N + 1);
+                long long act = __shfl_sync(SBP_FULL_MASK, cact, ci);
+                if (kNP && __shfl_sync(SBP_FULL_MASK, ccount, ci)) {
+                    const int32_t b = min(max(ne0 - nm, 0), g.N + 1);
                     act += __ldg(g.Dm + b);
                 }
+                const int32_t keys_ci = __shfl_sync(SBP_FULL_MASK, ckeys, ci);
+                const long long nc_d = __shfl_sync(SBP_FULL_MASK, cd, i & 31);
+                const long long nq_d = __shfl_sync(SBP_FULL_MASK, qd, 0);
                 if (i < ncand || nq > 0 || hb) {
-                    long long top = hb ? sh.b_dS : LLONG_MAX;
-                    if (i < ncand) top = min(top, sh.c_dS[i]);
-                    if (nq > 0) top = min(top, sh.q_dS[0]);
+                    long long top = hb ? bnd_dS : LLONG_MAX;
+                    if (i < ncand) top = min(top, nc_d);
+                    if (nq > 0) top = min(top, nq_d);
                     if (act > top) {  // put back with the recomputed delta
-                        int k = nq++;
-                        while (k > 0 && qless(act, from, sh.q_dS[k - 1], sh.q_blk[k - 1])) {
-                            sh.q_dS[k] = sh.q_dS[k - 1];
-                            sh.q_blk[k] = sh.q_blk[k - 1];
-                            sh.q_to[k] = sh.q_to[k - 1];
-                            sh.q_cand[k] = sh.q_cand[k - 1];
-                            --k;
+                        const int k = __popc(__ballot_sync(SBP_FULL_MASK, lane < nq && qless(qd, qb, act, from)));
+                        const long long ud = __shfl_up_sync(SBP_FULL_MASK, qd, 1);
+                        const int32_t ub = __shfl_up_sync(SBP_FULL_MASK, qb, 1);
+                        const int32_t ut = __shfl_up_sync(SBP_FULL_MASK, qt, 1);
+                        const int32_t uc = __shfl_up_sync(SBP_FULL_MASK, qc, 1);
+                        if (lane > k) {
+                            qd = ud;
+                            qb = ub;
+                            qt = ut;
+                            qc = uc;
+                        } else if (lane == k) {
+                            qd = act;
+                            qb = from;
+                            qt = to;
+                            qc = ci;
                         }
-                        sh.q_dS[k] = act;
-                        sh.q_blk[k] = from;
-                        sh.q_to[k] = to;
-                        sh.q_cand[k] = ci;
+                        ++nq;
                         continue;
                     }
                 }
-                sh.m_from[nm] = from;
-                sh.m_to[nm] = to;
-                sh.m_keys[nm] = sh.c_keys[ci];
+                if (lane == 0) {
+                    sh.m_from[nm] = from;
+                    sh.m_to[nm] = to;
+                    sh.m_keys[nm] = keys_ci;
+                }
                 merged_mask |= 1u << ci;
                 ++nm;
             }
-            sh.p += cons[0];
-            sh.q += cons[1];
-            sh.cS = cons[2];
-            sh.nq = nq;
-            sh.nm = nm;
-            sh.ne -= nm;  // every merge lowers the count (blockmodel.cpp:356)
-            sh.rounds += 1;
+            if (lane < nq) {
+                sh.q_dS[lane] = qd;
+                sh.q_blk[lane] = qb;
+            }
+            if (lane == 0) {
+                sh.p += cons0;
+                sh.q += cons1;
+                sh.cS = cons2;
+                sh.nq = nq;
+                sh.nm = nm;
+                sh.ne -= nm;  // every merge lowers the count (blockmodel.cpp:356)
+                sh.rounds += 1;
+            }
         }
         __syncthreads();
         // ---- 4. S := S[cS..ns) merged with the put-back entries
