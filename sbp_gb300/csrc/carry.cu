@@ -9,7 +9,7 @@
 //   1. selects the W smallest live queue entries (and the (W+1)-th as a bound),
 //   2. recomputes their deltas at once, one team of warps per entry,
 //   3. replays the reference's pop / put-back / merge rule over those values on one
-//      thread, up to the first entry it holds no value for,
+//      warp, up to the first entry it holds no value for,
 //   4. applies the merges of the round together, a team of warps each (up to 8 at once).
 // A merge r -> s changes only rows / columns r and s and the degrees of r and s, so an
 // evaluation stays exact after it unless it read one of them: each evaluation records
@@ -25,7 +25,7 @@
 // ties of equal delta pop in ascending block order.
 //
 // Deltas are handled as exact int64 multiples of 2^-24 (the reference's doubles compare
-// the same way), which keeps the single-thread queue logic off the slow FP64 pipe.
+// the same way), which keeps the sequential queue logic off the slow FP64 pipe.
 //
 // Nonparametric entropy (kNP): every merge lowers the number of non-empty blocks by one
 // (blockmodel.cpp:356), which changes the partition and edge-count terms of every later

@@ -12,9 +12,11 @@
 // T(v) = {r, s, nb} + v's neighbour blocks, or nb(v) lies in T(u) (u's neighbours in
 // block nb shift counts of row / column nb between columns / rows a and b).  Each round
 // therefore evaluates the next W vertices of the order at once (one warp each) against
-// the same state; one thread replays them in order and stops before the first vertex
-// that an earlier accepted move of the round may have changed; the accepted moves are
-// then applied together (every update is an addition, so their order does not matter).
+// the same state; the replay takes them in order and stops before the first vertex
+// that an earlier accepted move of the round may have changed (one ballot: that vertex is
+// the first with a conflict bit, since the bits name accepted earlier entries only); the
+// accepted moves are then applied together (every update is an addition, so their order
+// does not matter).
 // The result equals the one-vertex-at-a-time chain exactly.
 //
 // Nonparametric entropy (kNP): a delta also reads the sizes of r and s (covered by T(v))
