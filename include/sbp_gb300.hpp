@@ -152,7 +152,9 @@ class Graph {
         upload(src, dst);
     }
     /// From neighbour lists (Graph(out, in, N, E)): the edges are taken from the
-    /// out-neighbour lists in vertex order.
+    /// out-neighbour lists in vertex order; num_edges is kept as Graph::num_edges, the count
+    /// the description lengths use (half the stored edges for an undirected edge list,
+    /// src/graph.cpp:145-147).
     Graph(const NeighborList& out_neighbors, const NeighborList& in_neighbors, long num_vertices, long num_edges,
           Context& ctx = Context::global())
         : ctx_(&ctx), n_(num_vertices), out_(out_neighbors), in_(in_neighbors) {
@@ -165,6 +167,10 @@ class Graph {
                 dst.push_back((int32_t)u);
             }
         upload(src, dst);
+        if (num_edges != e_) {
+            check(sbpgpu_graph_set_model_edges(h_, num_edges), ctx_->get());
+            e_ = num_edges;
+        }
     }
     Graph(const Graph&) = delete;
     Graph& operator=(const Graph&) = delete;

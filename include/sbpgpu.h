@@ -96,12 +96,22 @@ sbpgpu_status sbpgpu_graph_create_device(sbpgpu_ctx* ctx, int64_t num_vertices, 
  * coordinate file (a "symmetric" one is read as undirected), parsed on the device.  With
  * `undirected`, or for symmetric Matrix Market, each edge u-v (u != v) is followed by v-u,
  * as the reference inserts it, so neighbour lists keep the reference's order.  The vertex
- * count is the largest id (at least the Matrix Market size).  num_edges counts directed
- * edges, also for undirected TSV input, where the reference's Graph reports half of them. */
+ * count is the largest id (at least the Matrix Market size).  The stored edge count
+ * (sbpgpu_graph_num_edges) is the directed one; the model edge count is half of it for
+ * undirected TSV input, as the reference's Graph reports it (graph.cpp:145-147). */
 sbpgpu_status sbpgpu_graph_load(sbpgpu_ctx* ctx, const char* path, int32_t undirected, sbpgpu_graph** out);
 void sbpgpu_graph_destroy(sbpgpu_graph* g);
 int64_t sbpgpu_graph_num_vertices(const sbpgpu_graph* g);
+/* The directed edges stored (the length of the edge arrays). */
 int64_t sbpgpu_graph_num_edges(const sbpgpu_graph* g);
+/* Graph::num_edges (include/graph.hpp:99) as the description lengths use it: entropy::mdl
+ * (src/entropy.cpp:597-604), null_mdl_v1 and the nonparametric get_edges_dl
+ * (:745-749).  It is the stored count, except for an undirected edge list, whose
+ * reference Graph counts each stored pair once (src/graph.cpp:145-147).  The setter gives
+ * the count of a graph built from arrays that hold both directions of each edge; EINVAL
+ * for a count below 1. */
+int64_t sbpgpu_graph_model_edges(const sbpgpu_graph* g);
+sbpgpu_status sbpgpu_graph_set_model_edges(sbpgpu_graph* g, int64_t num_edges);
 
 /* ---- blockmodel: replaces Blockmodel(num_blocks, graph, rate, assignment) and
  * Blockmodel::initialize_edge_counts (src/blockmodel/blockmodel.cpp:193-276).

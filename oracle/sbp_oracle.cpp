@@ -102,6 +102,9 @@ inline int64_t random_block(int64_t current, int64_t B, uint32_t w) {
 // ---------------------------------------------------------------- graph
 struct ora_graph {
     int64_t N = 0, E = 0;
+    // Graph::num_edges (graph.hpp:99), the count every description length uses: the stored
+    // directed edges, or half of them for an undirected edge list (graph.cpp:145-147)
+    int64_t Em = 0;
     std::vector<std::vector<int32_t>> out, in, inns;  // inns = in-neighbours without self
     std::vector<int32_t> selfcnt;
     std::vector<double> Ld;     // fastlog table: logf((float)x) (fastlog.hpp:21-30)
@@ -139,6 +142,7 @@ extern "C" ora_graph* ora_graph_create(int64_t N, int64_t E, const int32_t* src,
     auto* g = new ora_graph();
     g->N = N;
     g->E = E;
+    g->Em = E;
     g->out.assign(N, {});
     g->in.assign(N, {});
     g->inns.assign(N, {});
@@ -404,7 +408,7 @@ inline double np_edges_dl(int64_t b, int64_t E) { return np_lbinom(b * b + E - 1
  * get_delta_edges_dl (:1111-1143) when the non-empty block count goes from b to b + dB. */
 inline int64_t np_dl_step(const ora_graph* g, int64_t b, int dB) {
     const double part = np_lbinom(g->N - 1, b + dB - 1) - np_lbinom(g->N - 1, b - 1);
-    const double edges = np_edges_dl(b + dB, g->E) - np_edges_dl(b, g->E);
+    const double edges = np_edges_dl(b + dB, g->Em) - np_edges_dl(b, g->Em);
     return llrint((part + edges) * kFix);
 }
 /* vterm_exact (entropy.hpp:117-133), directed, not degree-corrected. */
@@ -470,7 +474,7 @@ double np_dS_literal(const ora_bm* bm, int64_t r, int64_t s, const DeltaMap& d, 
     if (dB != 0) {
         Sb += np_lbinom(g->N - 1, bm->nonempty - 1);
         Sa += np_lbinom(g->N - 1, bm->nonempty + dB - 1);
-        edges = np_edges_dl(bm->nonempty + dB, g->E) - np_edges_dl(bm->nonempty, g->E);
+        edges = np_edges_dl(bm->nonempty + dB, g->Em) - np_edges_dl(bm->nonempty, g->Em);
     }
     return dS + ((Sa - Sb) + 0.0 + edges);
 }
@@ -483,7 +487,7 @@ double np_mdl_canonical(const ora_bm* bm) {
         for (const auto& e : bm->row[r]) fixed -= g->LG[e.second];
     for (int64_t b = 0; b < bm->B; ++b) fixed += np_vterm(g, bm->dout[b], bm->din[b], bm->sizes[b]) - g->LG[bm->sizes[b]];
     fixed += g->LG[g->N] + g->Lq[g->N];
-    return (double)fixed * kInvFix + (np_lbinom(g->N - 1, bm->nonempty - 1) + np_edges_dl(bm->nonempty, g->E));
+    return (double)fixed * kInvFix + (np_lbinom(g->N - 1, bm->nonempty - 1) + np_edges_dl(bm->nonempty, g->Em));
 }
 /* The four parts in the reference's arithmetic. */
 void np_terms_literal(const ora_bm* bm, double out[4]) {
@@ -501,7 +505,7 @@ void np_terms_literal(const ora_bm* bm, double out[4]) {
     out[0] = S;
     out[1] = P;
     out[2] = 0.0;
-    out[3] = np_edges_dl(bm->nonempty, g->E);
+    out[3] = np_edges_dl(bm->nonempty, g->Em);
 }
 
 /* A non-negative double as an integer count of 2^-64 units (truncated): every term of the
@@ -700,7 +704,7 @@ void mdl_both(const ora_bm* bm, double* literal, double* canonical) {
             lpq += (__int128)e.second * canon_log_q(ratio);
         }
     }
-    const double E = (double)g->E;
+    const double E = (double)g->Em;
     const double x = pow((double)bm->B, 2) / E;
     const double h = ((1 + x) * log(1 + x)) - (x * log(x));
     const double model = (E * h) + ((double)g->N * log((double)bm->B));
@@ -1607,6 +1611,8 @@ extern "C" void ora_graph_edges(const ora_graph* g, int32_t* src, int32_t* dst) 
 }
 
 extern "C" int64_t ora_graph_num_edges(const ora_graph* g) { return g->E; }
+extern "C" int64_t ora_graph_model_edges(const ora_graph* g) { return g->Em; }
+extern "C" void ora_graph_set_model_edges(ora_graph* g, int64_t num_edges) { g->Em = num_edges; }
 
 extern "C" void ora_extend(const ora_graph* g, const int32_t* sample_asg, int64_t sample_n, int64_t B,
                            const int32_t* mapping, uint64_t seed, int32_t* out) {

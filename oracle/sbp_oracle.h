@@ -144,6 +144,10 @@ void ora_reattach(const ora_graph* g, const int32_t* sample_assignment, int64_t 
 /* sample::from_vertices (sample.cpp:240-253). */
 ora_graph* ora_subgraph(const ora_graph* g, const int32_t* mapping, int64_t n);
 int64_t ora_graph_num_edges(const ora_graph* g);
+/* Graph::num_edges (graph.hpp:99) as the description lengths use it: the stored directed
+ * edges by default; half of them for an undirected edge list (graph.cpp:145-147). */
+int64_t ora_graph_model_edges(const ora_graph* g);
+void ora_graph_set_model_edges(ora_graph* g, int64_t num_edges);
 /* The graph's edges, by source vertex, each source's out-neighbours in order. */
 void ora_graph_edges(const ora_graph* g, int32_t* src, int32_t* dst);
 /* sample::extend (sample.cpp:159-199). */

@@ -134,9 +134,14 @@ def _p(a, t):
 
 
 class Graph:
-    """Directed multigraph in input edge order (Graph::add_edge, src/graph.cpp:10-18)."""
+    """Directed multigraph in input edge order (Graph::add_edge, src/graph.cpp:10-18).
 
-    def __init__(self, num_vertices, src, dst, ctx=None):
+    num_edges: Graph::num_edges (include/graph.hpp:99), the count the description lengths
+    use; the number of edges given by default.  Pass half of it for arrays that hold both
+    directions of an undirected edge list, as the reference's loader counts them
+    (src/graph.cpp:145-147)."""
+
+    def __init__(self, num_vertices, src, dst, ctx=None, num_edges=None):
         self.ctx = ctx or default_context()
         self.src = np.ascontiguousarray(src, dtype=np.int32)
         self.dst = np.ascontiguousarray(dst, dtype=np.int32)
@@ -152,6 +157,8 @@ class Graph:
         self.h = h
         self._bms = weakref.WeakSet()
         self.ctx._graphs.add(self)
+        if num_edges is not None:
+            self.ctx.check(self.ctx.lib.sbpgpu_graph_set_model_edges(self.h, int(num_edges)))
 
     @classmethod
     def _adopt(cls, handle, ctx):
@@ -199,6 +206,12 @@ class Graph:
         return self._N
 
     def num_edges(self):
+        """Graph::num_edges: the count the description lengths use (half the stored edges
+        for an undirected edge list)."""
+        return int(self.ctx.lib.sbpgpu_graph_model_edges(self.h))
+
+    def num_stored_edges(self):
+        """The directed edges stored (the length of the edge arrays)."""
         return self._E if self.src is None else int(self.src.size)
 
     def out_neighbors(self, v):

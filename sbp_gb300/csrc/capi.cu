@@ -168,6 +168,10 @@ struct sbpgpu_graph {
     int refs = 0;          // live blockmodels
     bool dead = false;     // destroy requested
     int64_t N = 0, E = 0;
+    // Graph::num_edges (graph.hpp:99), the count the description lengths use: the stored
+    // directed edges, or half of them for an undirected edge list (graph.cpp:145-147)
+    int64_t Em = 0;
+    int64_t np_Em = -1;  // the count the nonparametric Dm / Dp tables were built for
     DevGraph dg{};
     std::vector<void*> owned;
     std::vector<int32_t> deg;   // Graph::degrees (graph.cpp:24-31): out + in - self
@@ -313,12 +317,14 @@ void parallel_for(int64_t lo, int64_t hi, F f) {
 // lgamma(x + 1) in units of 2^-24 over the range of Lq, and the rounded change of
 // lbinom(N - 1, b - 1) + edges_dl(b) (get_delta_partition_dl, entropy.cpp:933-940;
 // get_delta_edges_dl, :1111-1143) when the non-empty block count steps from b to b - 1
-// (Dm) or b + 1 (Dp).
+// (Dm) or b + 1 (Dp).  Dm and Dp are rebuilt when the graph's model edge count changes.
 void ensure_np(sbpgpu_graph* g) {
-    if (g->dg.LG) return;
-    const int64_t n = (int64_t)g->dg.nlq + 1, N = g->N, E = g->E;
-    std::vector<long long> LG(n), Dm(N + 2, 0), Dp(N + 2, 0);
-    parallel_for(0, n, [&](int64_t x) { LG[x] = std::llrint(std::lgamma((double)(x + 1)) * 16777216.0); });
+    if (g->dg.LG && g->np_Em == g->Em) return;
+    const int64_t n = (int64_t)g->dg.nlq + 1, N = g->N, E = g->Em;
+    const bool have_lg = g->dg.LG != nullptr;
+    std::vector<long long> LG(have_lg ? 0 : n), Dm(N + 2, 0), Dp(N + 2, 0);
+    if (!have_lg)
+        parallel_for(0, n, [&](int64_t x) { LG[x] = std::llrint(std::lgamma((double)(x + 1)) * 16777216.0); });
     auto step = [&](int64_t b, int dB) {
         const double part = np_lbinom(N - 1, b + dB - 1) - np_lbinom(N - 1, b - 1);
         const double edges = np_edges_dl(b + dB, E) - np_edges_dl(b, E);
@@ -329,18 +335,22 @@ void ensure_np(sbpgpu_graph* g) {
         if (b <= N) Dp[b] = step(b, +1);
     });
     cudaStream_t st = g->ctx->stream;
-    long long* d_LG = dalloc<long long>(g->owned, n);
-    long long* d_Dm = dalloc<long long>(g->owned, N + 2);
-    long long* d_Dp = dalloc<long long>(g->owned, N + 2);
-    CK(cudaMemcpyAsync(d_LG, LG.data(), n * sizeof(long long), cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(d_Dm, Dm.data(), (N + 2) * sizeof(long long), cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(d_Dp, Dp.data(), (N + 2) * sizeof(long long), cudaMemcpyHostToDevice, st));
+    if (!have_lg) {
+        long long* d_LG = dalloc<long long>(g->owned, n);
+        CK(cudaMemcpyAsync(d_LG, LG.data(), n * sizeof(long long), cudaMemcpyHostToDevice, st));
+        g->dg.Dm = dalloc<long long>(g->owned, N + 2);
+        g->dg.Dp = dalloc<long long>(g->owned, N + 2);
+        g->dg.LG = d_LG;
+        g->np_lg_N = LG[N];
+        g->np_lg = std::move(LG);
+    }
+    // the graph owns the tables; the device view holds them read-only
+    CK(cudaMemcpyAsync(const_cast<long long*>(g->dg.Dm), Dm.data(), (N + 2) * sizeof(long long),
+                       cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(const_cast<long long*>(g->dg.Dp), Dp.data(), (N + 2) * sizeof(long long),
+                       cudaMemcpyHostToDevice, st));
     host_wait(st);
-    g->dg.LG = d_LG;
-    g->dg.Dm = d_Dm;
-    g->dg.Dp = d_Dp;
-    g->np_lg_N = LG[N];
-    g->np_lg = std::move(LG);
+    g->np_Em = g->Em;
 }
 
 void ensure_split(sbpgpu_graph* g, float mh_percent) {
@@ -395,13 +405,13 @@ double do_mdl(sbpgpu_bm* bm, bool np = false) {
     if (np) {
         // nonparametric::mdl (entropy.cpp:751-779): the table terms, lgamma(N + 1) and
         // fastlog(N) of get_partition_dl, then the two terms of the non-empty block count
-        const int64_t N = g->N, E = g->E, ne = *h_ne;
+        const int64_t N = g->N, E = g->Em, ne = *h_ne;
         const long long lqN = (long long)(int32_t)((double)logf((float)N) * 16777216.0);
         const long long fixed = (long long)acc + g->np_lg_N + lqN;
         return (double)fixed * (1.0 / 16777216.0) + (np_lbinom(N - 1, ne - 1) + np_edges_dl(ne, E));
     }
     const long long lpq = (long long)acc;
-    const double E = (double)g->E;
+    const double E = (double)g->Em;
     const double B = (double)bm->d.B;
     const double x = pow(B, 2) / E;
     const double h = ((1 + x) * log(1 + x)) - (x * log(x));
@@ -1057,6 +1067,7 @@ sbpgpu_status sbpgpu_graph_create(sbpgpu_ctx* ctx, int64_t N, int64_t E, const i
     g->ctx = ctx;
     g->N = N;
     g->E = E;
+    g->Em = E;
     const sbpgpu_status rc = guarded(ctx, [&] {
         CK(cudaSetDevice(ctx->device));
         upload_graph(g, src, dst);
@@ -1102,12 +1113,13 @@ sbpgpu_status sbpgpu_graph_load(sbpgpu_ctx* ctx, const char* path, int32_t undir
     // Matrix Market: banner, comment lines, then "rows cols entries" (graph.cpp:75-103)
     size_t offset = 0;
     int64_t header_n = 0;
-    bool symmetric = false;
+    bool symmetric = false, matrix_market = false;
     auto next_line = [&](size_t at) {
         const size_t e = data.find('\n', at);
         return e == std::string::npos ? data.size() : e + 1;
     };
     if (data.compare(0, 14, "%%MatrixMarket") == 0) {
+        matrix_market = true;
         const size_t e = next_line(0);
         std::vector<std::string> tok;
         {
@@ -1156,6 +1168,9 @@ sbpgpu_status sbpgpu_graph_load(sbpgpu_ctx* ctx, const char* path, int32_t undir
     const int64_t N = std::max<int64_t>(max_id, header_n);
     sbpgpu_status rc2 = N > 0 ? sbpgpu_graph_create_device(ctx, N, E, d_src, d_dst, out)
                               : fail(ctx, SBPGPU_EINVAL, "the file holds no vertices");
+    // an undirected edge list counts each stored pair once (graph.cpp:145-147); a Matrix
+    // Market file counts its header entries plus the reverse edges added (graph.cpp:96-116)
+    if (rc2 == SBPGPU_OK && un && !matrix_market) (*out)->Em = E / 2;
     if (d_src) cudaFreeAsync(d_src, ctx->stream);
     if (d_dst) cudaFreeAsync(d_dst, ctx->stream);
     return rc2;
@@ -1426,6 +1441,14 @@ void sbpgpu_graph_destroy(sbpgpu_graph* g) {
 
 int64_t sbpgpu_graph_num_vertices(const sbpgpu_graph* g) { return g ? g->N : 0; }
 int64_t sbpgpu_graph_num_edges(const sbpgpu_graph* g) { return g ? g->E : 0; }
+int64_t sbpgpu_graph_model_edges(const sbpgpu_graph* g) { return g ? g->Em : 0; }
+
+sbpgpu_status sbpgpu_graph_set_model_edges(sbpgpu_graph* g, int64_t num_edges) {
+    if (!g) return SBPGPU_EINVAL;
+    if (num_edges <= 0) return fail(g->ctx, SBPGPU_EINVAL, "the model edge count must be positive");
+    g->Em = num_edges;  // the nonparametric tables follow on their next use
+    return SBPGPU_OK;
+}
 
 sbpgpu_status sbpgpu_bm_create(sbpgpu_graph* g, int64_t B, const int32_t* assignment, sbpgpu_bm** out) {
     if (!g || !out) return SBPGPU_EINVAL;

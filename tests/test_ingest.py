@@ -54,8 +54,10 @@ def test_tsv_load_matches_reference_construction(gpu, tmp_path, undirected):
     G = gpu.Graph.load(str(path), undirected=undirected)
     s2, d2 = _edges(undirected, src, dst)
     n = int(max(src.max(), dst.max())) + 1
-    assert G.num_vertices() == n and G.num_edges() == s2.size
-    _same_partition(gpu, G, gpu.Graph(n, s2, d2))
+    # the reference's undirected Graph counts each stored pair once (graph.cpp:145-147)
+    Em = s2.size // 2 if undirected else s2.size
+    assert G.num_vertices() == n and G.num_stored_edges() == s2.size and G.num_edges() == Em
+    _same_partition(gpu, G, gpu.Graph(n, s2, d2, num_edges=Em))
 
 
 @pytest.mark.gpu
@@ -66,7 +68,7 @@ def test_matrix_market_load(gpu, tmp_path, symmetric):
     _write_mtx(path, 750, src, dst, symmetric)  # the size line may exceed the largest id
     G = gpu.Graph.load(str(path))
     s2, d2 = _edges(symmetric, src, dst)
-    assert G.num_vertices() == 750 and G.num_edges() == s2.size
+    assert G.num_vertices() == 750 and G.num_edges() == s2.size == G.num_stored_edges()
     _same_partition(gpu, G, gpu.Graph(750, s2, d2))
 
 
