@@ -112,6 +112,14 @@ int64_t sbpgpu_graph_num_edges(const sbpgpu_graph* g);
  * for a count below 1. */
 int64_t sbpgpu_graph_model_edges(const sbpgpu_graph* g);
 sbpgpu_status sbpgpu_graph_set_model_edges(sbpgpu_graph* g, int64_t num_edges);
+/* args.undirected (include/args.hpp:55) as the nonparametric entropy reads it
+ * (include/entropy.hpp:102-133, src/entropy.cpp:745-749): a diagonal cell's eterm carries
+ * -w log 2, a block's vertex term counts its out-degree only, and get_edges_dl spreads the
+ * edges over B (B + 1) / 2 block pairs.  Set by sbpgpu_graph_load for undirected or
+ * symmetric input and inherited by sampled subgraphs; off for graphs built from arrays
+ * until set.  The parametric entropy does not read it. */
+int32_t sbpgpu_graph_undirected(const sbpgpu_graph* g);
+sbpgpu_status sbpgpu_graph_set_undirected(sbpgpu_graph* g, int32_t undirected);
 
 /* ---- blockmodel: replaces Blockmodel(num_blocks, graph, rate, assignment) and
  * Blockmodel::initialize_edge_counts (src/blockmodel/blockmodel.cpp:193-276).

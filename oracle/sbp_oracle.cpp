@@ -105,6 +105,10 @@ struct ora_graph {
     // Graph::num_edges (graph.hpp:99), the count every description length uses: the stored
     // directed edges, or half of them for an undirected edge list (graph.cpp:145-147)
     int64_t Em = 0;
+    // args.undirected for the nonparametric entropy (entropy.hpp:102-133, entropy.cpp:745):
+    // diagonal cells carry -w log 2, a block's vertex term counts its out-degree only, and
+    // the edge count is spread over B (B + 1) / 2 block pairs
+    bool und = false;
     std::vector<std::vector<int32_t>> out, in, inns;  // inns = in-neighbours without self
     std::vector<int32_t> selfcnt;
     std::vector<double> Ld;     // fastlog table: logf((float)x) (fastlog.hpp:21-30)
@@ -402,18 +406,28 @@ inline double np_lbinom(int64_t N, int64_t k) {
     if (N == 0 || k == 0 || k > N) return 0.0;
     return (lgamma((double)(N + 1)) - lgamma((double)(k + 1))) - lgamma((double)(N - k + 1));
 }
-/* get_edges_dl (entropy.cpp:745-749), directed: NB = B * B. */
-inline double np_edges_dl(int64_t b, int64_t E) { return np_lbinom(b * b + E - 1, E); }
+/* get_edges_dl (entropy.cpp:745-749): NB = B * B, or B (B + 1) / 2 when undirected. */
+inline double np_edges_dl(int64_t b, int64_t E, bool und = false) {
+    return np_lbinom((und ? b * (b + 1) / 2 : b * b) + E - 1, E);
+}
+/* log 2 in units of 2^-24, rounded: the undirected diagonal term w log 2 of eterm_exact
+ * (entropy.hpp:102-111) is w times this constant in the canonical arithmetic. */
+const int64_t kLn2Fix = llrint(0.69314718055994530942 * 16777216.0);
+/* eterm_exact(r, s, M + d) - eterm_exact(r, s, M), canonical. */
+inline int64_t np_cell(const ora_graph* g, bool diag, int64_t m, int64_t d) {
+    return g->LG[m] - g->LG[m + d] - (g->und && diag ? d * kLn2Fix : 0);
+}
 /* Change of lbinom(N - 1, B - 1) (get_delta_partition_dl, entropy.cpp:933-940) plus
  * get_delta_edges_dl (:1111-1143) when the non-empty block count goes from b to b + dB. */
 inline int64_t np_dl_step(const ora_graph* g, int64_t b, int dB) {
     const double part = np_lbinom(g->N - 1, b + dB - 1) - np_lbinom(g->N - 1, b - 1);
-    const double edges = np_edges_dl(b + dB, g->Em) - np_edges_dl(b, g->Em);
+    const double edges = np_edges_dl(b + dB, g->Em, g->und) - np_edges_dl(b, g->Em, g->und);
     return llrint((part + edges) * kFix);
 }
-/* vterm_exact (entropy.hpp:117-133), directed, not degree-corrected. */
+/* vterm_exact (entropy.hpp:117-133), not degree-corrected: (d_out + d_in) log w, or
+ * d_out log w when undirected. */
 inline int64_t np_vterm(const ora_graph* g, int64_t dout, int64_t din, int64_t w) {
-    return w == 0 ? 0 : (dout + din) * g->Lq[w];
+    return w == 0 ? 0 : (g->und ? dout : dout + din) * g->Lq[w];
 }
 /* The block terms of virtual_move_sparse (entropy.cpp:822-889), the lgamma terms of
  * get_delta_partition_dl (:892-1000) and the non-empty-count terms for moving `weight`
@@ -433,7 +447,7 @@ inline int64_t np_entries(const ora_bm* bm, const DeltaMap& d) {
     int64_t t = 0;
     for (const auto& e : d) {
         const int64_t m = bm->get(e.first.first, e.first.second);
-        t += bm->g->LG[m] - bm->g->LG[m + e.second];
+        t += np_cell(bm->g, e.first.first == e.first.second, m, e.second);
     }
     return t;
 }
@@ -457,11 +471,14 @@ double np_dS_literal(const ora_bm* bm, int64_t r, int64_t s, const DeltaMap& d, 
                      int64_t weight) {
     const ora_graph* g = bm->g;
     auto lg = [](int64_t x) { return lgamma((double)x); };
-    auto vt = [&](int64_t o, int64_t i, int64_t w) { return w == 0 ? 0.0 : (double)(o + i) * g->Ld[w]; };
+    auto vt = [&](int64_t o, int64_t i, int64_t w) { return w == 0 ? 0.0 : (double)(g->und ? o : o + i) * g->Ld[w]; };
+    const double log_2 = log(2.0);
+    auto et = [&](bool diag, int64_t w) { return -lg(w + 1) - (g->und && diag ? (double)w * log_2 : 0.0); };
     double dS = 0.0;
     for (const auto& e : d) {
         const int64_t m = bm->get(e.first.first, e.first.second);
-        dS += -lg(m + e.second + 1) - (-lg(m + 1));
+        const bool diag = e.first.first == e.first.second;
+        dS += et(diag, m + e.second) - et(diag, m);
     }
     const int64_t sr = bm->sizes[r], ss = bm->sizes[s];
     dS += vt(bm->dout[r] - kout, bm->din[r] - kin, sr - weight);
@@ -474,7 +491,7 @@ double np_dS_literal(const ora_bm* bm, int64_t r, int64_t s, const DeltaMap& d, 
     if (dB != 0) {
         Sb += np_lbinom(g->N - 1, bm->nonempty - 1);
         Sa += np_lbinom(g->N - 1, bm->nonempty + dB - 1);
-        edges = np_edges_dl(bm->nonempty + dB, g->Em) - np_edges_dl(bm->nonempty, g->Em);
+        edges = np_edges_dl(bm->nonempty + dB, g->Em, g->und) - np_edges_dl(bm->nonempty, g->Em, g->und);
     }
     return dS + ((Sa - Sb) + 0.0 + edges);
 }
@@ -484,19 +501,22 @@ double np_mdl_canonical(const ora_bm* bm) {
     const ora_graph* g = bm->g;
     int64_t fixed = 0;
     for (int64_t r = 0; r < bm->B; ++r)
-        for (const auto& e : bm->row[r]) fixed -= g->LG[e.second];
+        for (const auto& e : bm->row[r]) fixed -= np_cell(g, e.first == r, e.second, -e.second);  // + eterm
     for (int64_t b = 0; b < bm->B; ++b) fixed += np_vterm(g, bm->dout[b], bm->din[b], bm->sizes[b]) - g->LG[bm->sizes[b]];
     fixed += g->LG[g->N] + g->Lq[g->N];
-    return (double)fixed * kInvFix + (np_lbinom(g->N - 1, bm->nonempty - 1) + np_edges_dl(bm->nonempty, g->Em));
+    return (double)fixed * kInvFix +
+           (np_lbinom(g->N - 1, bm->nonempty - 1) + np_edges_dl(bm->nonempty, g->Em, g->und));
 }
 /* The four parts in the reference's arithmetic. */
 void np_terms_literal(const ora_bm* bm, double out[4]) {
     const ora_graph* g = bm->g;
     double S = 0.0;
+    const double log_2 = log(2.0);
     for (int64_t r = 0; r < bm->B; ++r)
-        for (const auto& e : bm->row[r]) S += -lgamma((double)(e.second + 1));
+        for (const auto& e : bm->row[r])
+            S += -lgamma((double)(e.second + 1)) - (g->und && e.first == r ? (double)e.second * log_2 : 0.0);
     for (int64_t b = 0; b < bm->B; ++b)
-        if (bm->sizes[b] != 0) S += (double)(bm->dout[b] + bm->din[b]) * g->Ld[bm->sizes[b]];
+        if (bm->sizes[b] != 0) S += (double)(g->und ? bm->dout[b] : bm->dout[b] + bm->din[b]) * g->Ld[bm->sizes[b]];
     double P = 0.0;
     P += np_lbinom(g->N - 1, bm->nonempty - 1);
     P += lgamma((double)(g->N + 1));
@@ -505,7 +525,7 @@ void np_terms_literal(const ora_bm* bm, double out[4]) {
     out[0] = S;
     out[1] = P;
     out[2] = 0.0;
-    out[3] = np_edges_dl(bm->nonempty, g->Em);
+    out[3] = np_edges_dl(bm->nonempty, g->Em, g->und);
 }
 
 /* A non-negative double as an integer count of 2^-64 units (truncated): every term of the
@@ -1347,7 +1367,9 @@ ora_graph* from_vertices(const ora_graph* g, const std::vector<int32_t>& mapping
                 dst.push_back(mapping[v]);
             }
     }
-    return ora_graph_create(n, (int64_t)src.size(), src.data(), dst.data());
+    ora_graph* sub = ora_graph_create(n, (int64_t)src.size(), src.data(), dst.data());
+    sub->und = g->und;  // args.undirected is global in the reference
+    return sub;
 }
 
 /* sample::extend (sample.cpp:159-199): sampled vertices keep their block; the others, in
@@ -1613,6 +1635,7 @@ extern "C" void ora_graph_edges(const ora_graph* g, int32_t* src, int32_t* dst) 
 extern "C" int64_t ora_graph_num_edges(const ora_graph* g) { return g->E; }
 extern "C" int64_t ora_graph_model_edges(const ora_graph* g) { return g->Em; }
 extern "C" void ora_graph_set_model_edges(ora_graph* g, int64_t num_edges) { g->Em = num_edges; }
+extern "C" void ora_graph_set_undirected(ora_graph* g, int32_t undirected) { g->und = undirected != 0; }
 
 extern "C" void ora_extend(const ora_graph* g, const int32_t* sample_asg, int64_t sample_n, int64_t B,
                            const int32_t* mapping, uint64_t seed, int32_t* out) {
@@ -1758,14 +1781,14 @@ inline int split_side(uint64_t seed, int64_t v, int32_t i, uint32_t step, int64_
  * vertices and E edges: sizes[2], cells M[2][2] (row-major).  The canonical form. */
 double np_mdl_two_blocks(const ora_graph* g, int64_t n, int64_t E, const int64_t sizes[2], const int64_t M[4]) {
     int64_t fixed = 0;
-    for (int k = 0; k < 4; ++k) fixed -= g->LG[M[k]];
+    for (int k = 0; k < 4; ++k) fixed -= np_cell(g, k == 0 || k == 3, M[k], -M[k]);  // + eterm
     for (int b = 0; b < 2; ++b) {
         const int64_t dout = M[2 * b] + M[2 * b + 1], din = M[b] + M[2 + b];
         fixed += np_vterm(g, dout, din, sizes[b]) - g->LG[sizes[b]];
     }
     fixed += g->LG[n] + g->Lq[n];
     const int64_t ne = (sizes[0] > 0) + (sizes[1] > 0);
-    return (double)fixed * kInvFix + (np_lbinom(n - 1, ne - 1) + np_edges_dl(ne, E));
+    return (double)fixed * kInvFix + (np_lbinom(n - 1, ne - 1) + np_edges_dl(ne, E, g->und));
 }
 
 /* entropy::null_mdl_v1 (entropy.cpp:571-585) of a subgraph: the one-block nonparametric

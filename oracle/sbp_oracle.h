@@ -148,6 +148,8 @@ int64_t ora_graph_num_edges(const ora_graph* g);
  * edges by default; half of them for an undirected edge list (graph.cpp:145-147). */
 int64_t ora_graph_model_edges(const ora_graph* g);
 void ora_graph_set_model_edges(ora_graph* g, int64_t num_edges);
+/* args.undirected for the nonparametric entropy (entropy.hpp:102-133, entropy.cpp:745). */
+void ora_graph_set_undirected(ora_graph* g, int32_t undirected);
 /* The graph's edges, by source vertex, each source's out-neighbours in order. */
 void ora_graph_edges(const ora_graph* g, int32_t* src, int32_t* dst);
 /* sample::extend (sample.cpp:159-199). */

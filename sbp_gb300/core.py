@@ -139,9 +139,10 @@ class Graph:
     num_edges: Graph::num_edges (include/graph.hpp:99), the count the description lengths
     use; the number of edges given by default.  Pass half of it for arrays that hold both
     directions of an undirected edge list, as the reference's loader counts them
-    (src/graph.cpp:145-147)."""
+    (src/graph.cpp:145-147).  undirected: args.undirected for the nonparametric entropy
+    (include/sbpgpu.h, sbpgpu_graph_set_undirected)."""
 
-    def __init__(self, num_vertices, src, dst, ctx=None, num_edges=None):
+    def __init__(self, num_vertices, src, dst, ctx=None, num_edges=None, undirected=False):
         self.ctx = ctx or default_context()
         self.src = np.ascontiguousarray(src, dtype=np.int32)
         self.dst = np.ascontiguousarray(dst, dtype=np.int32)
@@ -159,6 +160,8 @@ class Graph:
         self.ctx._graphs.add(self)
         if num_edges is not None:
             self.ctx.check(self.ctx.lib.sbpgpu_graph_set_model_edges(self.h, int(num_edges)))
+        if undirected:
+            self.ctx.check(self.ctx.lib.sbpgpu_graph_set_undirected(self.h, 1))
 
     @classmethod
     def _adopt(cls, handle, ctx):
@@ -209,6 +212,10 @@ class Graph:
         """Graph::num_edges: the count the description lengths use (half the stored edges
         for an undirected edge list)."""
         return int(self.ctx.lib.sbpgpu_graph_model_edges(self.h))
+
+    def undirected(self):
+        """args.undirected as the nonparametric entropy reads it."""
+        return bool(self.ctx.lib.sbpgpu_graph_undirected(self.h))
 
     def num_stored_edges(self):
         """The directed edges stored (the length of the edge arrays)."""

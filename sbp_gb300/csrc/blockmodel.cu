@@ -129,7 +129,9 @@ __global__ void k_np_mdl(DevGraph g, DevBM bm, unsigned long long* __restrict__ 
     long long acc = 0;
     const int64_t n = bm.nnz > bm.B ? bm.nnz : bm.B;
     for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
-        if (j < bm.nnz) acc -= np_lg(g, bm.row_cnt[j]);  // eterm_exact (entropy.hpp:103-113)
+        if (j < bm.nnz)  // eterm_exact (entropy.hpp:103-113)
+            acc += bm.row_of[j] == bm.row_col[j] ? -np_cell_diag(g, bm.row_cnt[j], -bm.row_cnt[j])
+                                                 : -np_lg(g, bm.row_cnt[j]);
         if (j < bm.B) acc += np_vterm(g, bm.d_out[j], bm.d_in[j], bm.sizes[j]) - np_lg(g, bm.sizes[j]);
     }
     acc = warp_sum_ll(acc);

@@ -171,7 +171,10 @@ struct sbpgpu_graph {
     // Graph::num_edges (graph.hpp:99), the count the description lengths use: the stored
     // directed edges, or half of them for an undirected edge list (graph.cpp:145-147)
     int64_t Em = 0;
-    int64_t np_Em = -1;  // the count the nonparametric Dm / Dp tables were built for
+    // args.undirected for the nonparametric entropy (entropy.hpp:102-133, entropy.cpp:745)
+    int32_t und = 0;
+    int64_t np_Em = -1;   // the count the nonparametric Dm / Dp tables were built for
+    int32_t np_und = -1;  // and the form
     DevGraph dg{};
     std::vector<void*> owned;
     std::vector<int32_t> deg;   // Graph::degrees (graph.cpp:24-31): out + in - self
@@ -294,7 +297,10 @@ double np_lbinom(int64_t n, int64_t k) {
     return (std::lgamma((double)(n + 1)) - std::lgamma((double)(k + 1))) - std::lgamma((double)(n - k + 1));
 }
 // get_edges_dl (entropy.cpp:745-749) for a directed graph: NB = B * B.
-double np_edges_dl(int64_t b, int64_t E) { return np_lbinom(b * b + E - 1, E); }
+// get_edges_dl (entropy.cpp:745-749): NB = B * B, or B (B + 1) / 2 when undirected.
+double np_edges_dl(int64_t b, int64_t E, bool und) { return np_lbinom((und ? b * (b + 1) / 2 : b * b) + E - 1, E); }
+// log 2 in units of 2^-24, rounded: the undirected diagonal eterm's w log 2 is w times this.
+const long long kLn2Fix = std::llrint(0.69314718055994530942 * 16777216.0);
 
 // Runs f(i) for i in [lo, hi) on the host's cores.
 template <class F>
@@ -319,7 +325,8 @@ void parallel_for(int64_t lo, int64_t hi, F f) {
 // get_delta_edges_dl, :1111-1143) when the non-empty block count steps from b to b - 1
 // (Dm) or b + 1 (Dp).  Dm and Dp are rebuilt when the graph's model edge count changes.
 void ensure_np(sbpgpu_graph* g) {
-    if (g->dg.LG && g->np_Em == g->Em) return;
+    if (g->dg.LG && g->np_Em == g->Em && g->np_und == g->und) return;
+    const bool und = g->und != 0;
     const int64_t n = (int64_t)g->dg.nlq + 1, N = g->N, E = g->Em;
     const bool have_lg = g->dg.LG != nullptr;
     std::vector<long long> LG(have_lg ? 0 : n), Dm(N + 2, 0), Dp(N + 2, 0);
@@ -327,7 +334,7 @@ void ensure_np(sbpgpu_graph* g) {
         parallel_for(0, n, [&](int64_t x) { LG[x] = std::llrint(std::lgamma((double)(x + 1)) * 16777216.0); });
     auto step = [&](int64_t b, int dB) {
         const double part = np_lbinom(N - 1, b + dB - 1) - np_lbinom(N - 1, b - 1);
-        const double edges = np_edges_dl(b + dB, E) - np_edges_dl(b, E);
+        const double edges = np_edges_dl(b + dB, E, und) - np_edges_dl(b, E, und);
         return std::llrint((part + edges) * 16777216.0);
     };
     parallel_for(1, N + 2, [&](int64_t b) {
@@ -351,6 +358,9 @@ void ensure_np(sbpgpu_graph* g) {
                        cudaMemcpyHostToDevice, st));
     host_wait(st);
     g->np_Em = g->Em;
+    g->np_und = g->und;
+    g->dg.np_und = g->und;
+    g->dg.ln2q = kLn2Fix;
 }
 
 void ensure_split(sbpgpu_graph* g, float mh_percent) {
@@ -408,7 +418,7 @@ double do_mdl(sbpgpu_bm* bm, bool np = false) {
         const int64_t N = g->N, E = g->Em, ne = *h_ne;
         const long long lqN = (long long)(int32_t)((double)logf((float)N) * 16777216.0);
         const long long fixed = (long long)acc + g->np_lg_N + lqN;
-        return (double)fixed * (1.0 / 16777216.0) + (np_lbinom(N - 1, ne - 1) + np_edges_dl(ne, E));
+        return (double)fixed * (1.0 / 16777216.0) + (np_lbinom(N - 1, ne - 1) + np_edges_dl(ne, E, g->und != 0));
     }
     const long long lpq = (long long)acc;
     const double E = (double)g->Em;
@@ -642,15 +652,16 @@ long long lq_of(int64_t x) { return x <= 0 ? 0 : (long long)(int32_t)((double)lo
 // and E edges (sizes, row-major cells M), in the canonical arithmetic of the device deltas.
 double np_mdl_two_blocks(const sbpgpu_graph* g, int64_t n, int64_t E, const int64_t sizes[2], const int64_t M[4]) {
     const std::vector<long long>& LG = g->np_lg;
+    const bool und = g->und != 0;
     long long fixed = 0;
-    for (int k = 0; k < 4; ++k) fixed -= LG[M[k]];
+    for (int k = 0; k < 4; ++k) fixed -= LG[M[k]] + (und && (k == 0 || k == 3) ? M[k] * kLn2Fix : 0);
     for (int b = 0; b < 2; ++b) {
         const int64_t dout = M[2 * b] + M[2 * b + 1], din = M[b] + M[2 + b];
-        fixed += (sizes[b] == 0 ? 0 : (dout + din) * lq_of(sizes[b])) - LG[sizes[b]];
+        fixed += (sizes[b] == 0 ? 0 : (und ? dout : dout + din) * lq_of(sizes[b])) - LG[sizes[b]];
     }
     fixed += LG[n] + lq_of(n);
     const int64_t ne = (sizes[0] > 0) + (sizes[1] > 0);
-    return (double)fixed * (1.0 / 16777216.0) + (np_lbinom(n - 1, ne - 1) + np_edges_dl(ne, E));
+    return (double)fixed * (1.0 / 16777216.0) + (np_lbinom(n - 1, ne - 1) + np_edges_dl(ne, E, und));
 }
 
 // entropy::null_mdl_v1 (entropy.cpp:571-585) of a subgraph: the one-block nonparametric MDL
@@ -1171,6 +1182,7 @@ sbpgpu_status sbpgpu_graph_load(sbpgpu_ctx* ctx, const char* path, int32_t undir
     // an undirected edge list counts each stored pair once (graph.cpp:145-147); a Matrix
     // Market file counts its header entries plus the reverse edges added (graph.cpp:96-116)
     if (rc2 == SBPGPU_OK && un && !matrix_market) (*out)->Em = E / 2;
+    if (rc2 == SBPGPU_OK) (*out)->und = un;
     if (d_src) cudaFreeAsync(d_src, ctx->stream);
     if (d_dst) cudaFreeAsync(d_dst, ctx->stream);
     return rc2;
@@ -1210,6 +1222,7 @@ sbpgpu_graph* make_subgraph(sbpgpu_graph* g, const int32_t* d_map, int64_t n) {
     if (d_src) cudaFreeAsync(d_src, st);
     if (d_dst) cudaFreeAsync(d_dst, st);
     if (rc != SBPGPU_OK) throw ApiError(rc, std::string("sample graph: ") + sbpgpu_last_error(g->ctx));
+    sub->und = g->und;  // args.undirected is global in the reference
     return sub;
 }
 
@@ -1442,6 +1455,14 @@ void sbpgpu_graph_destroy(sbpgpu_graph* g) {
 int64_t sbpgpu_graph_num_vertices(const sbpgpu_graph* g) { return g ? g->N : 0; }
 int64_t sbpgpu_graph_num_edges(const sbpgpu_graph* g) { return g ? g->E : 0; }
 int64_t sbpgpu_graph_model_edges(const sbpgpu_graph* g) { return g ? g->Em : 0; }
+
+int32_t sbpgpu_graph_undirected(const sbpgpu_graph* g) { return g ? g->und : 0; }
+
+sbpgpu_status sbpgpu_graph_set_undirected(sbpgpu_graph* g, int32_t undirected) {
+    if (!g) return SBPGPU_EINVAL;
+    g->und = undirected ? 1 : 0;  // the nonparametric tables follow on their next use
+    return SBPGPU_OK;
+}
 
 sbpgpu_status sbpgpu_graph_set_model_edges(sbpgpu_graph* g, int64_t num_edges) {
     if (!g) return SBPGPU_EINVAL;

@@ -174,7 +174,7 @@ __device__ long long merge_delta_part(const DevGraph& g, const DevBM& bm, const 
         if (m == 0 || (!is_row && key == r)) return;
         bloom_add(bloom, key);
         if constexpr (kNP) {  // the cell empties; a third block's cell adds into row / column s
-            acc += np_lg(g, m);
+            acc += is_row && key == r ? np_cell_diag(g, m, -m) : np_lg(g, m);
             if (is_row ? (key != r && key != s) : (key != s)) acc += np_cell(g, o, m);
             return;
         }
@@ -275,7 +275,7 @@ __device__ long long merge_delta_part(const DevGraph& g, const DevBM& bm, const 
     acc = warp_sum_ll(acc);
     if (leader && kNP) {
         const int32_t Mrr = cells.get(r, r), Mrs = cells.get(r, s), Msr = cells.get(s, r), Mss = cells.get(s, s);
-        acc += np_cell(g, Mss, Mrr + Mrs + Msr);
+        acc += np_cell_diag(g, Mss, Mrr + Mrs + Msr);
         acc += np_block_terms(g, dout_r, din_r, bm.sizes[r], dout_s, din_s, bm.sizes[s], dout_r, din_r, bm.sizes[r], 0,
                               false);
     } else if (leader) {

@@ -442,7 +442,7 @@ __device__ long long warp_delta(const DevGraph& g, const int32_t* d_out, const i
     const int32_t d_rr = -Or - Ir - L, d_rs = Ir - Os, d_sr = Or - Is, d_ss = Os + Is + L;
     long long tot = acc;
     if constexpr (kNP) {
-        tot += np_cell(g, Mrr, d_rr) + np_cell(g, Mrs, d_rs) + np_cell(g, Msr, d_sr) + np_cell(g, Mss, d_ss);
+        tot += np_cell_diag(g, Mrr, d_rr) + np_cell(g, Mrs, d_rs) + np_cell(g, Msr, d_sr) + np_cell_diag(g, Mss, d_ss);
         return tot + np_block_terms(g, dout_r, din_r, size[r], dout_s, din_s, size[s], kout, kin, 1, nonempty);
     }
     const int32_t c0 = L32(Mrr), c1 = L32(Mrr + d_rr), c2 = L32(Mrs), c3 = L32(Mrs + d_rs);

@@ -55,6 +55,10 @@ struct DevGraph {
     const long long* Dm;
     const long long* Dp;
     int32_t nlq;          // last index of Lq and LG
+    // args.undirected for the nonparametric entropy: diagonal cells carry -w log 2 (ln2q =
+    // log 2 in units of 2^-24, rounded), vertex terms count out-degrees only
+    int32_t np_und;
+    long long ln2q;
 };
 
 struct DevBM {

@@ -262,8 +262,8 @@ __device__ long long vertex_delta_fixed(const DevGraph& g, const int32_t* asg, c
     const int32_t Mrr = M.row_get(r, r), Mrs = M.row_get(r, s), Msr = M.row_get(s, r), Mss = M.row_get(s, s);
     long long tot = acc;
     if constexpr (kNP) {
-        tot += np_cell(g, Mrr, -Or - Ir - L) + np_cell(g, Mrs, Ir - Os) + np_cell(g, Msr, Or - Is) +
-               np_cell(g, Mss, Os + Is + L);
+        tot += np_cell_diag(g, Mrr, -Or - Ir - L) + np_cell(g, Mrs, Ir - Os) + np_cell(g, Msr, Or - Is) +
+               np_cell_diag(g, Mss, Os + Is + L);
         return tot + np_block_terms(g, dout_r, din_r, sizes[r], dout_s, din_s, sizes[s], kout, kin, 1, nonempty);
     }
     const int32_t d_rr = -Or - Ir - L, d_rs = Ir - Os, d_sr = Or - Is, d_ss = Os + Is + L;
@@ -506,7 +506,7 @@ __device__ long long np_merge_delta_csr(const DevGraph& g, const DevBM& bm, int3
     const int32_t ro0 = bm.row_off[r], ro1 = bm.row_off[r + 1];
     for (int32_t j = ro0 + t; j < ro1; j += kThreads) {
         const int32_t c = bm.row_col[j], m = bm.row_cnt[j];
-        acc += np_lg(g, m);
+        acc += c == r ? np_cell_diag(g, m, -m) : np_lg(g, m);  // the cell empties
         if (c != r && c != s) acc += np_cell(g, csr_get(bm.row_off, bm.row_col, bm.row_cnt, s, c), m);
     }
     const int32_t co0 = bm.col_off[r], co1 = bm.col_off[r + 1];
@@ -525,7 +525,7 @@ __device__ long long np_merge_delta_csr(const DevGraph& g, const DevBM& bm, int3
     const int32_t Mrs = csr_get(bm.row_off, bm.row_col, bm.row_cnt, r, s);
     const int32_t Msr = csr_get(bm.row_off, bm.row_col, bm.row_cnt, s, r);
     const int32_t Mss = csr_get(bm.row_off, bm.row_col, bm.row_cnt, s, s);
-    acc += np_cell(g, Mss, Mrr + Mrs + Msr);
+    acc += np_cell_diag(g, Mss, Mrr + Mrs + Msr);
     const int32_t dout_r = bm.d_out[r], din_r = bm.d_in[r];
     return acc + np_block_terms(g, dout_r, din_r, size_r, bm.d_out[s], bm.d_in[s], size_s, dout_r, din_r, size_r,
                                 nonempty);

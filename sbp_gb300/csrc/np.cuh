@@ -33,13 +33,19 @@ __device__ __forceinline__ long long np_log(const DevGraph& g, long long x) {
     x = x < 0 ? 0 : (x > g.nlq ? g.nlq : x);
     return (long long)__ldg(g.Lq + x);
 }
-// vterm_exact (include/entropy.hpp:117-133), directed, not degree-corrected.
+// vterm_exact (include/entropy.hpp:117-133), not degree-corrected: (d_out + d_in) log w,
+// or d_out log w for an undirected graph.
 __device__ __forceinline__ long long np_vterm(const DevGraph& g, long long dout, long long din, long long w) {
-    return w == 0 ? 0 : (dout + din) * np_log(g, w);
+    return w == 0 ? 0 : (g.np_und ? dout : dout + din) * np_log(g, w);
 }
-// One changed cell of entries_dS: eterm(M + d) - eterm(M).
+// One changed cell of entries_dS: eterm(M + d) - eterm(M), off the diagonal.
 __device__ __forceinline__ long long np_cell(const DevGraph& g, long long m, long long d) {
     return np_lg(g, m) - np_lg(g, m + d);
+}
+// The same for a diagonal cell: eterm_exact(r, r, w) carries -w log 2 more when the graph
+// is undirected (include/entropy.hpp:102-111).
+__device__ __forceinline__ long long np_cell_diag(const DevGraph& g, long long m, long long d) {
+    return np_cell(g, m, d) - (g.np_und ? d * g.ln2q : 0);
 }
 // The block, partition and edge-count terms of moving `w` vertices with kout / kin edges
 // from r to s; nonempty = the current number of non-empty blocks.  The terms that depend

@@ -128,6 +128,7 @@ def lib():
         L.ora_graph_model_edges.restype = ctypes.c_int64
         L.ora_graph_model_edges.argtypes = [ctypes.c_void_p]
         L.ora_graph_set_model_edges.argtypes = [ctypes.c_void_p, ctypes.c_int64]
+        L.ora_graph_set_undirected.argtypes = [ctypes.c_void_p, ctypes.c_int32]
         L.ora_graph_edges.argtypes = [ctypes.c_void_p, i32p, i32p]
         L.ora_extend.argtypes = [ctypes.c_void_p, i32p, ctypes.c_int64, ctypes.c_int64, i32p, ctypes.c_uint64, i32p]
         L.ora_reattach.argtypes = [ctypes.c_void_p, i32p, ctypes.c_int64, ctypes.c_int64, i32p, ctypes.c_uint64, i32p]
@@ -163,9 +164,10 @@ def philox(ctr, key):
 
 class Graph:
     """num_edges: the count the description lengths use (Graph::num_edges); the stored
-    directed edges by default, half of them for an undirected edge list."""
+    directed edges by default, half of them for an undirected edge list.  undirected:
+    args.undirected for the nonparametric entropy."""
 
-    def __init__(self, num_vertices, src, dst, num_edges=None):
+    def __init__(self, num_vertices, src, dst, num_edges=None, undirected=False):
         self.src = np.ascontiguousarray(src, dtype=np.int32)
         self.dst = np.ascontiguousarray(dst, dtype=np.int32)
         self.N = int(num_vertices)
@@ -173,6 +175,8 @@ class Graph:
         self.h = lib().ora_graph_create(self.N, self.E, _p(self.src, i32p), _p(self.dst, i32p))
         if num_edges is not None:
             lib().ora_graph_set_model_edges(self.h, int(num_edges))
+        if undirected:
+            lib().ora_graph_set_undirected(self.h, 1)
 
     def model_edges(self):
         return int(lib().ora_graph_model_edges(self.h))
