@@ -298,7 +298,7 @@ void launch_mdl(const DevGraph& g, const DevBM& bm, Work& w, cudaStream_t st) {
 }
 
 void launch_np_mdl(const DevGraph& g, const DevBM& bm, Work& w, cudaStream_t st) {
-    if (true && (!g.LG || !g.Dm || !g.Dp)) throw std::logic_error("nonparametric tables missing");
+    if (!g.LG || !g.Dm || !g.Dp) throw std::logic_error("nonparametric tables missing");
     cudaMemsetAsync(w.d_acc, 0, sizeof(unsigned long long), st);
     k_np_mdl<<<grid_for(bm.nnz > bm.B ? bm.nnz : bm.B), kT, 0, st>>>(g, bm, w.d_acc);
     count_launches(1);
