@@ -87,7 +87,10 @@ struct Args {
     bool ordered = false;
     bool approximate = false;
     int asynciterations = INT_MAX;
-    bool nonparametric = false;       // entropy::nonparametric, directed, not degree-corrected
+    bool nonparametric = false;       // entropy::nonparametric, not degree-corrected
+    bool undirected = false;          // args.undirected (include/args.hpp:55): the nonparametric
+                                      // entropy's undirected form; graphs built while it is set
+                                      // take it, and stochastic_block_partition applies it
     int threads = 1;                  // accepted for compatibility; the device uses every SM
     uint64_t seed = 0;                // seeds the proposal stream
     int max_iterations = 100;         // MAX_NUM_ITERATIONS (include/finetune.hpp:34)
@@ -196,6 +199,7 @@ class Graph {
         e_ = (long)src.size();
         assignment_.assign(n_, -1);
         check(sbpgpu_graph_create(ctx_->get(), n_, e_, src.data(), dst.data(), &h_), ctx_->get());
+        if (args.undirected) check(sbpgpu_graph_set_undirected(h_, 1), ctx_->get());
     }
     Context* ctx_;
     long n_ = 0, e_ = 0;
@@ -453,6 +457,7 @@ inline Blockmodel stochastic_block_partition(Graph& graph, Args& a, bool divide_
     if (divide_and_conquer)
         throw Error(SBPGPU_EUNSUPPORTED, "divide-and-conquer SBP is outside the device hot path");
     const sbpgpu_config cfg = to_config(a);
+    check(sbpgpu_graph_set_undirected(graph.handle(), a.undirected ? 1 : 0), graph.context().get());
     std::vector<int32_t> out(graph.num_vertices());
     int64_t B = 0;
     double mdl = 0.0;
