@@ -117,3 +117,64 @@ def test_windowed_carry_out_matches_sequential_queue(W, QS):
         best, d0 = _instance(seed, B)
         ntm = random.Random(seed + 1).randrange(1, B)
         assert _windowed(best, d0, ntm, seed, W, QS) == _sequential(best, d0, ntm, seed), (seed, B)
+
+
+# ---- the carry-out's replay on one warp (carry.cu, step 3): the round's put-back list
+# lives in lane registers, entry l in lane l.  These model the warp primitives with the
+# kernel's own lane arithmetic and check them against the sorted list the single-thread
+# replay kept (an insertion sort on (delta, block), pops from the front).
+
+def _qless(a, b):
+    return a[0] < b[0] or (a[0] == b[0] and a[1] < b[1])
+
+
+def _shfl_down(lanes, delta):
+    return [lanes[l + delta] if l + delta < 32 else lanes[l] for l in range(32)]
+
+
+def _shfl_up(lanes, delta):
+    return [lanes[l - delta] if l - delta >= 0 else lanes[l] for l in range(32)]
+
+
+def _warp_pop(lanes):
+    return _shfl_down(lanes, 1)
+
+
+def _warp_insert(lanes, nq, new):
+    """k = popc(ballot(lane < nq && qless(q[lane], new))); lanes above k take their lower
+    neighbour's entry, lane k the new one."""
+    k = sum(1 for l in range(32) if l < nq and _qless(lanes[l], new))
+    up = _shfl_up(lanes, 1)
+    return [up[l] if l > k else (new if l == k else lanes[l]) for l in range(32)]
+
+
+def _thread_insert(q, new):
+    q = list(q)
+    k = len(q)
+    q.append(None)
+    while k > 0 and _qless(new, q[k - 1]):
+        q[k] = q[k - 1]
+        k -= 1
+    q[k] = new
+    return q
+
+
+@pytest.mark.parametrize("seed", range(40))
+def test_warp_put_back_list_matches_insertion_sort(seed):
+    rng = random.Random(seed)
+    lanes = [(0, -1)] * 32
+    ref, nq = [], 0
+    blocks = rng.sample(range(1000), 64)  # a block is in the list at most once
+    for step in range(200):
+        if nq > 0 and (nq == 16 or rng.random() < 0.45):
+            assert lanes[0] == ref[0]
+            lanes = _warp_pop(lanes)
+            ref.pop(0)
+            nq -= 1
+        else:
+            free = [b for b in blocks if all(b != e[1] for e in ref)]
+            new = (rng.choice([rng.randrange(-3, 3), rng.uniform(-3, 3)]), rng.choice(free))
+            lanes = _warp_insert(lanes, nq, new)
+            ref = _thread_insert(ref, new)
+            nq += 1
+        assert lanes[:nq] == ref, (seed, step)
