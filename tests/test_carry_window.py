@@ -178,3 +178,37 @@ def test_warp_put_back_list_matches_insertion_sort(seed):
             ref = _thread_insert(ref, new)
             nq += 1
         assert lanes[:nq] == ref, (seed, step)
+
+
+# ---- the MH chain window's replay (chain_window.cu): bit u of conf[j] is set only for an
+# accepted entry u < j whose move may change entry j.  The single-thread replay walked the
+# entries, keeping each while no accepted earlier entry conflicts with it; the warp replay
+# stops at the first entry with any bit set (one ballot).  Both keep the same entries.
+
+def _serial_stop(conf, accepted, wn):
+    consumed, acc_mask = 0, 0
+    for j in range(wn):
+        if conf[j] & acc_mask:
+            break
+        consumed = j + 1
+        if accepted[j]:
+            acc_mask |= 1 << j
+    return consumed, acc_mask
+
+
+def _ballot_stop(conf, accepted, wn):
+    stop = [j for j in range(wn) if conf[j] != 0]
+    consumed = stop[0] if stop else wn
+    acc_mask = sum(1 << j for j in range(consumed) if accepted[j])
+    return consumed, acc_mask
+
+
+@pytest.mark.parametrize("seed", range(20))
+def test_chain_window_ballot_stop_matches_serial_replay(seed):
+    rng = random.Random(seed)
+    for _ in range(500):
+        wn = rng.randrange(1, 17)
+        accepted = [rng.random() < rng.choice([0.1, 0.5, 0.9]) for _ in range(wn)]
+        p = rng.choice([0.05, 0.3, 0.8])
+        conf = [sum(1 << u for u in range(j) if accepted[u] and rng.random() < p) for j in range(wn)]
+        assert _ballot_stop(conf, accepted, wn) == _serial_stop(conf, accepted, wn)
