@@ -5,7 +5,11 @@ The device evaluates the W smallest live entries against one blockmodel state an
 the pop / put-back / merge rule over those values.  This model applies the same selection,
 replay and put-back buffering (shared buffer of capacity QS spilling into a sorted run)
 with a stand-in for the recomputed delta that changes whenever a merge changes the state,
-and must produce exactly the sequential loop's merges, in order."""
+and must produce exactly the sequential loop's merges, in order.
+
+Two models of the warp-level replays follow: the carry-out's put-back list in lane
+registers against the single-thread insertion sort, and the MH chain window's one-ballot
+stop (sbp_gb300/csrc/chain_window.cu) against the serial replay."""
 import heapq
 import random
 
