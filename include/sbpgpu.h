@@ -267,6 +267,13 @@ typedef struct sbpgpu_eval {
 } sbpgpu_eval;
 sbpgpu_status sbpgpu_evaluate(sbpgpu_ctx* ctx, int64_t n, const int32_t* truth, const int32_t* assignment,
                               sbpgpu_eval* out);
+/* evaluate::calculate_f1_score and evaluate::calculate_nmi (src/evaluate.cpp:9-98) of a
+ * contingency table given row-major, nrows x ncols, as the reference's Hungarian::Matrix:
+ * F1, precision, recall and Rand index by pair counting and NMI, over num_vertices.  A host
+ * computation that needs no device; accuracy is left 0, true_blocks = ncols and
+ * found_blocks = nrows. */
+sbpgpu_status sbpgpu_partition_scores(int64_t num_vertices, int64_t nrows, int64_t ncols, const int64_t* table,
+                                      sbpgpu_eval* out);
 
 /* ---- batched and served partitioning ----------------------------------------------
  * No counterpart in the reference (its plain driver partitions one graph per process).  A

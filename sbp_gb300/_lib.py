@@ -131,6 +131,8 @@ SIGNATURES = {
     "sbpgpu_sbp": (ctypes.c_int, [vp, ctypes.POINTER(Config), ctypes.c_uint64, i32p, i64p, f64p,
                                   ctypes.POINTER(Stats)]),
     "sbpgpu_evaluate": (ctypes.c_int, [vp, ctypes.c_int64, i32p, i32p, ctypes.POINTER(Eval)]),
+    "sbpgpu_partition_scores": (ctypes.c_int, [ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, i64p,
+                                               ctypes.POINTER(Eval)]),
     "sbpgpu_split_communities": (ctypes.c_int, [vp, ctypes.POINTER(Config), ctypes.c_uint64, ctypes.c_int32,
                                                 ctypes.c_int64]),
     "sbpgpu_sbp_top_down": (ctypes.c_int, [vp, ctypes.POINTER(Config), ctypes.c_uint64, ctypes.c_int32, i32p, i64p,

@@ -7,6 +7,7 @@
 // (row-major, ascending columns) and the same is done on (col << nb | row) for the CSC.
 // Traffic per rebuild is O(E) and independent of how many vertices moved.
 #include <mutex>
+#include <unordered_map>
 #include <unordered_set>
 
 #include <stdexcept>
@@ -24,7 +25,7 @@ constexpr int kT = 256;
 inline unsigned grid_for(int64_t n, int per = kT) {
     int64_t b = (n + per - 1) / per;
     if (b < 1) b = 1;
-    if (b > 152 * 64) b = 152 * 64;
+    if (b > (int64_t)device_sms() * 64) b = (int64_t)device_sms() * 64;
     return (unsigned)b;
 }
 
@@ -235,6 +236,23 @@ void allow_max_dynamic_smem(const void* func) {
     done.insert(func);
 }
 
+int device_sms() {
+    static std::mutex mu;
+    static std::unordered_map<int, int> cache;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = cache.find(dev);
+    if (it != cache.end()) return it->second;
+    int n = 0;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) {
+        cudaGetLastError();
+        n = 1;
+    }
+    cache[dev] = n;
+    return n;
+}
+
 void* host_scratch() {
     thread_local void* p = nullptr;
     if (!p && cudaMallocHost(&p, 256) != cudaSuccess) p = nullptr;
@@ -310,7 +328,9 @@ void launch_vertex_dS_batch(const DevGraph& g, const DevBM& bm, const int32_t* v
     if (np && (!g.LG || !g.Dm || !g.Dp)) throw std::logic_error("nonparametric tables missing");
     int log2cap = ceil_log2((uint64_t)(2 * (max_k > 16 ? max_k : 16)));
     const size_t smem = (size_t)3 * sizeof(int32_t) << log2cap;
-    if (smem > 200 * 1024) return;  // callers check the degree limit first
+    if (smem > 200 * 1024)
+        throw std::invalid_argument("a vertex of degree " + std::to_string(max_k) +
+                                    " needs more shared memory for its neighbour hash than a block has");
     if (np) {
         allow_max_dynamic_smem((const void*)k_vertex_dS_batch<true>);
         k_vertex_dS_batch<true><<<grid_for(n, 1), kT, smem, st>>>(g, bm, v, s, n, log2cap, out);

@@ -222,6 +222,8 @@ sbpgpu_status guarded(sbpgpu_ctx* ctx, F f) {
         return fail(ctx, SBPGPU_EDEVICE, e.what());
     } catch (const std::bad_alloc&) {
         return fail(ctx, SBPGPU_ENOMEM, "host allocation failed");
+    } catch (const std::invalid_argument& e) {
+        return fail(ctx, SBPGPU_EINVAL, e.what());
     } catch (const std::exception& e) {
         return fail(ctx, SBPGPU_EDEVICE, e.what());
     }
@@ -1397,6 +1399,22 @@ sbpgpu_status sbpgpu_sbp_sampled(sbpgpu_graph* g, const sbpgpu_config* cfg, uint
     if (bm) sbpgpu_bm_destroy(bm);
     if (sub) sbpgpu_graph_destroy(sub);
     return rc;
+}
+
+sbpgpu_status sbpgpu_partition_scores(int64_t num_vertices, int64_t nrows, int64_t ncols, const int64_t* table,
+                                      sbpgpu_eval* out) {
+    if (!table || !out || num_vertices < 2 || nrows <= 0 || ncols <= 0 || nrows * ncols > (int64_t(1) << 28))
+        return SBPGPU_EINVAL;
+    try {
+        std::vector<std::vector<long long>> m(nrows, std::vector<long long>(ncols));
+        for (int64_t r = 0; r < nrows; ++r)
+            for (int64_t c = 0; c < ncols; ++c) m[r][c] = table[r * ncols + c];
+        const PartitionQuality q = scores_from_matrix(m, num_vertices, false);
+        *out = sbpgpu_eval{q.nmi, q.f1, q.precision, q.recall, q.rand_index, 0.0, q.true_blocks, q.found_blocks};
+    } catch (const std::bad_alloc&) {
+        return SBPGPU_ENOMEM;
+    }
+    return SBPGPU_OK;
 }
 
 sbpgpu_status sbpgpu_evaluate(sbpgpu_ctx* ctx, int64_t n, const int32_t* truth, const int32_t* assignment,

@@ -770,7 +770,7 @@ void carry_out_exact(const DevGraph& g, DevBM& bm, int64_t num_to_merge, Work& w
     if (dense) {
         lists_init(bm, w, st);
         cudaMemsetAsync(w.cells, 0, sizeof(int32_t) * (size_t)B * (size_t)B, st);
-        const int64_t blocks = std::min<int64_t>((bm.nnz + 255) / 256 + 1, 152 * 16);
+        const int64_t blocks = std::min<int64_t>((bm.nnz + 255) / 256 + 1, (int64_t)device_sms() * 16);
         k_dense_cells_fill<<<(unsigned)blocks, 256, 0, st>>>(bm, w.cells);
         launch_carry(np, g, bm, DenseCells{w.cells, (int64_t)B}, num_to_merge, team_warps, d_merged, w, st);
         count_launches(2);

@@ -304,7 +304,7 @@ void mh_chain_dense(const DevGraph& g, DevBM& bm, const int32_t* order, int32_t 
     cudaMemsetAsync(w.dense_MT, 0, cells * sizeof(int32_t), st);
     int64_t blocks = ((int64_t)bm.nnz + 255) / 256;
     if (blocks < 1) blocks = 1;
-    if (blocks > 152 * 16) blocks = 152 * 16;
+    if (blocks > (int64_t)device_sms() * 16) blocks = (int64_t)device_sms() * 16;
     k_dense_fill<<<(unsigned)blocks, 256, 0, st>>>(bm, w.dense_M, w.dense_MT);
     allow_max_dynamic_smem((const void*)k_mh_chain_dense<true>);
     k_mh_chain_dense<true><<<1, kT, smem, st>>>(g, bm, order, n, seed, iter, step, w.dense_M, w.dense_MT,

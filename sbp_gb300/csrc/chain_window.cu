@@ -849,7 +849,7 @@ void mh_chain_window(const DevGraph& g, DevBM& bm, const int32_t* order, int32_t
     cudaMemsetAsync(w.cells, 0, sizeof(int32_t) * mh_window_cells(bm.B), st);
     int64_t blocks = ((int64_t)bm.nnz + 255) / 256;
     if (blocks < 1) blocks = 1;
-    if (blocks > 152 * 16) blocks = 152 * 16;
+    if (blocks > (int64_t)device_sms() * 16) blocks = (int64_t)device_sms() * 16;
     k_window_fill<<<(unsigned)blocks, 256, 0, st>>>(bm, gc);
     if (p.mode == 1) launch_window<1>(np, g, bm, order, n, p, seed, iter, step, greedy, gc, smem, w, st);
     else launch_window<2>(np, g, bm, order, n, p, seed, iter, step, greedy, gc, smem, w, st);

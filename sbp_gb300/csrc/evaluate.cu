@@ -81,7 +81,7 @@ void launch_contingency(const int32_t* truth, const int32_t* found, int64_t n, i
                         unsigned long long* table, cudaStream_t st) {
     if (n <= 0) return;
     int64_t blocks = (n + 255) / 256;
-    if (blocks > 152 * 16) blocks = 152 * 16;
+    if (blocks > (int64_t)device_sms() * 16) blocks = (int64_t)device_sms() * 16;
     k_contingency<<<(unsigned)blocks, 256, 0, st>>>(truth, found, n, ncols, table);
     count_launches(1);
 }
@@ -92,10 +92,18 @@ PartitionQuality quality_from_table(const std::vector<unsigned long long>& t, in
     std::vector<std::vector<long long>> m(nb, std::vector<long long>(nt, 0));
     for (int64_t i = 0; i < nt; ++i)
         for (int64_t j = 0; j < nb; ++j) m[j][i] = (long long)t[i * nb + j];
-    const int64_t nrows = nb, ncols = nt;
-    PartitionQuality q{};
+    PartitionQuality q = scores_from_matrix(m, num_vertices, true);
     q.true_blocks = nt;
     q.found_blocks = nb;
+    return q;
+}
+
+PartitionQuality scores_from_matrix(const std::vector<std::vector<long long>>& m, int64_t num_vertices,
+                                    bool with_accuracy) {
+    const int64_t nrows = (int64_t)m.size(), ncols = nrows ? (int64_t)m[0].size() : 0;
+    PartitionQuality q{};
+    q.true_blocks = ncols;
+    q.found_blocks = nrows;
     // F1 (calculate_f1_score, evaluate.cpp:9-61): pair counts from the table
     const double V = (double)num_vertices;
     const double num_pairs = (V * (V - 1.0)) / 2.0;
@@ -148,6 +156,7 @@ PartitionQuality quality_from_table(const std::vector<unsigned long long>& t, in
             mi += p * std::log(p / (p1[r] * p2[c]));
         }
     q.nmi = mi / std::sqrt(h1 * h2);
+    if (!with_accuracy) return q;
     // accuracy: the best one-to-one matching of the smaller side into the larger
     const bool by_rows = nrows <= ncols;
     const int64_t a = by_rows ? nrows : ncols, b = by_rows ? ncols : nrows;

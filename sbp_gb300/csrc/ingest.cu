@@ -98,7 +98,7 @@ __global__ void k_emit_edges(const int32_t* __restrict__ from, const int32_t* __
 unsigned grid_of(int64_t n) {
     int64_t b = (n + 255) / 256;
     if (b < 1) b = 1;
-    if (b > 152 * 16) b = 152 * 16;
+    if (b > (int64_t)device_sms() * 16) b = (int64_t)device_sms() * 16;
     return (unsigned)b;
 }
 

@@ -217,6 +217,15 @@ void launch_contingency(const int32_t* truth, const int32_t* found, int64_t n, i
 // Metrics of evaluate::evaluate_blockmodel from the nt x nb table (rows = true).
 PartitionQuality quality_from_table(const std::vector<unsigned long long>& table, int64_t nt, int64_t nb,
                                     int64_t num_vertices);
+// calculate_f1_score and calculate_nmi (evaluate.cpp:9-98) of a contingency table given as
+// the reference passes it (rows x columns), and the best one-to-one matching's accuracy
+// when with_accuracy is set.
+PartitionQuality scores_from_matrix(const std::vector<std::vector<long long>>& m, int64_t num_vertices,
+                                    bool with_accuracy);
+
+// Streaming multiprocessors of the current device (queried once per device and cached);
+// grids of grid-stride kernels are capped at a multiple of it.
+int device_sms();
 
 // Launch accounting.
 int64_t kernel_launches();

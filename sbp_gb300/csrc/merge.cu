@@ -132,10 +132,10 @@ void merge_propose(const DevGraph& g, const DevBM& bm, uint64_t seed, uint32_t s
                    bool np) {
     if (np && (!g.LG || !g.Dm || !g.Dp)) throw std::logic_error("nonparametric tables missing");
     if (np)
-        k_merge_propose<true><<<grid_cap(bm.B, kMergeWarps, 152 * 8), 256, 0, st>>>(g, bm, seed, step, w.best,
+        k_merge_propose<true><<<grid_cap(bm.B, kMergeWarps, device_sms() * 8), 256, 0, st>>>(g, bm, seed, step, w.best,
                                                                                     w.best_dS, w.flags_dev);
     else
-        k_merge_propose<false><<<grid_cap(bm.B, kMergeWarps, 152 * 8), 256, 0, st>>>(g, bm, seed, step, w.best,
+        k_merge_propose<false><<<grid_cap(bm.B, kMergeWarps, device_sms() * 8), 256, 0, st>>>(g, bm, seed, step, w.best,
                                                                                      w.best_dS, w.flags_dev);
     count_launches(1);
 }
@@ -144,9 +144,9 @@ void carry_out(const DevGraph& g, DevBM& bm, int64_t num_to_merge, int approxima
                bool np) {
     const int32_t B = bm.B;
     // queue order: stable sort of (delta, block)
-    k_merge_keys<<<grid_cap(B, 256, 152 * 16), 256, 0, st>>>(w.best_dS, B, w.keys, w.vals);
+    k_merge_keys<<<grid_cap(B, 256, device_sms() * 16), 256, 0, st>>>(w.best_dS, B, w.keys, w.vals);
     radix_sort_u64(w.keys, w.keys_alt, w.vals, w.vals_alt, B, 64, w.temp, st);
-    k_iota<<<grid_cap(B, 256, 152 * 16), 256, 0, st>>>(w.parent, B);
+    k_iota<<<grid_cap(B, 256, device_sms() * 16), 256, 0, st>>>(w.parent, B);
     count_launches(2);
     int32_t* d_merged = w.d_scalar + 1;
     if (approximate) {
@@ -156,11 +156,11 @@ void carry_out(const DevGraph& g, DevBM& bm, int64_t num_to_merge, int approxima
     }
     count_launches(1);
     // union-find roots -> dense labels in ascending root order (build_mapping)
-    k_roots<<<grid_cap(B, 256, 152 * 16), 256, 0, st>>>(w.parent, B, w.root);
+    k_roots<<<grid_cap(B, 256, device_sms() * 16), 256, 0, st>>>(w.parent, B, w.root);
     cudaMemsetAsync(w.used, 0, sizeof(int32_t) * B, st);
-    k_mark_used<<<grid_cap(g.N, 256, 152 * 16), 256, 0, st>>>(bm.asg, g.N, w.root, w.used);
+    k_mark_used<<<grid_cap(g.N, 256, device_sms() * 16), 256, 0, st>>>(bm.asg, g.N, w.root, w.used);
     scan_i32(w.used, w.used, B, false, w.d_scalar + 2, w.temp, st);
-    k_relabel<<<grid_cap(g.N, 256, 152 * 16), 256, 0, st>>>(bm.asg, g.N, w.root, w.used);
+    k_relabel<<<grid_cap(g.N, 256, device_sms() * 16), 256, 0, st>>>(bm.asg, g.N, w.root, w.used);
     count_launches(3);
 }
 

@@ -63,7 +63,7 @@ bool noalloc_scratch(int device, NoAllocScratch* out, std::string* err) {
 
 void launch_fixed_to_double(long long* v, int64_t n, cudaStream_t st) {
     if (n <= 0) return;
-    const int64_t blocks = std::min<int64_t>((n + 255) / 256, 152 * 8);
+    const int64_t blocks = std::min<int64_t>((n + 255) / 256, device_sms() * 8);
     k_fixed_to_double<<<(unsigned)blocks, 256, 0, st>>>(v, n);
     count_launches(1);
 }

@@ -97,7 +97,7 @@ enum : uint32_t { DOM_SAMPLE = 6, DOM_EXTEND = 7 };
 unsigned grid_of(int64_t n, int per = 256) {
     int64_t b = (n + per - 1) / per;
     if (b < 1) b = 1;
-    if (b > 152 * 16) b = 152 * 16;
+    if (b > (int64_t)device_sms() * 16) b = (int64_t)device_sms() * 16;
     return (unsigned)b;
 }
 

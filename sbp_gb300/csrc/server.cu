@@ -2,7 +2,7 @@
 //
 // A plain partition spends most of its time in the sequential phases (the hybrid MH chain
 // and the merge carry-out), each a single CTA on one SM, so one graph at a time leaves most
-// of the 152 SMs idle.  A server runs several partitions concurrently: worker threads, each
+// of the GPU's SMs idle.  A server runs several partitions concurrently: worker threads, each
 // with its own context and stream, take jobs in submission order and run the same host
 // loop as sbpgpu_sbp; their kernels share the device.  A job is admitted only while the
 // estimated device footprint of the jobs in flight plus its own stays within the server's

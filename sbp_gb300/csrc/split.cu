@@ -31,7 +31,7 @@ constexpr int kProposals = 10;  // NUM_AGG_PROPOSALS_PER_BLOCK (top_down_sbp.hpp
 unsigned grid_of(int64_t n) {
     int64_t b = (n + 255) / 256;
     if (b < 1) b = 1;
-    if (b > 152 * 16) b = 152 * 16;
+    if (b > (int64_t)device_sms() * 16) b = (int64_t)device_sms() * 16;
     return (unsigned)b;
 }
 

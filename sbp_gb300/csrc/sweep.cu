@@ -411,7 +411,7 @@ __global__ void k_shuffle_keys(const int32_t* __restrict__ base, int32_t n, uint
 template <int kMode>
 void gibbs_launch(const DevGraph& g, const DevBM& bm, int32_t n, int32_t max_k, const int32_t* counts, uint64_t seed,
                   uint32_t iter, uint32_t step, Work& w, cudaStream_t st) {
-    k_gibbs_small<kMode><<<grid_cap(n, kGibbsWarps, 152 * 8), 256, 0, st>>>(g, bm, w.list_small, counts, seed, iter,
+    k_gibbs_small<kMode><<<grid_cap(n, kGibbsWarps, device_sms() * 8), 256, 0, st>>>(g, bm, w.list_small, counts, seed, iter,
                                                                             step, w.moves, w.flags_dev);
     count_launches(1);
     if (max_k > (1 << (kSmallLog2 - 1))) {
@@ -419,7 +419,7 @@ void gibbs_launch(const DevGraph& g, const DevBM& bm, int32_t n, int32_t max_k, 
         if (log2cap > 14) log2cap = 14;
         const size_t smem = (size_t)(3 * sizeof(int32_t)) << log2cap;
         allow_max_dynamic_smem((const void*)k_gibbs_big<kMode>);
-        k_gibbs_big<kMode><<<152 * 2, 256, smem, st>>>(g, bm, w.list_big, counts + 1, seed, iter, step, log2cap,
+        k_gibbs_big<kMode><<<device_sms() * 2, 256, smem, st>>>(g, bm, w.list_big, counts + 1, seed, iter, step, log2cap,
                                                        w.moves, w.flags_dev);
         count_launches(1);
     }
@@ -431,7 +431,7 @@ void gibbs_propose(const DevGraph& g, const DevBM& bm, const int32_t* vlist, int
     if (mode == ACC_NP && (!g.LG || !g.Dm || !g.Dp)) throw std::logic_error("nonparametric tables missing");
     int32_t* counts = w.d_scalar + 6;  // [6], [7]
     cudaMemsetAsync(counts, 0, 2 * sizeof(int32_t), st);
-    k_split_by_degree<<<grid_cap(n, 256, 152 * 16), 256, 0, st>>>(g, vlist, n, 1 << (kSmallLog2 - 1), w.list_small,
+    k_split_by_degree<<<grid_cap(n, 256, device_sms() * 16), 256, 0, st>>>(g, vlist, n, 1 << (kSmallLog2 - 1), w.list_small,
                                                                   w.list_big, counts);
     count_launches(1);
     if (mode == ACC_NP) gibbs_launch<ACC_NP>(g, bm, n, max_k, counts, seed, iter, step, w, st);
@@ -446,7 +446,7 @@ void gibbs_apply(const DevBM& bm, const int32_t* vlist, int32_t n, Work& w, cuda
     cudaMemsetAsync(w.last, 0xff, sizeof(int32_t) * bm.B, st);
     cudaMemsetAsync(w.acc, 0, sizeof(int32_t) * bm.B, st);
     cudaMemsetAsync(ndep, 0, sizeof(int32_t), st);
-    const unsigned grid = grid_cap(n, 256, 152 * 16);
+    const unsigned grid = grid_cap(n, 256, device_sms() * 16);
     k_apply_count<<<grid, 256, 0, st>>>(vlist, n, bm.asg, w.moves, w.m_out, w.last);
     k_apply_saved<<<grid, 256, 0, st>>>(vlist, n, bm.asg, w.moves, bm.sizes, w.m_out, w.last, w.acc, w.dep, ndep);
     k_resolve<<<1, 1024, 0, st>>>(w.dep, ndep, w.acc, w.flags_dev);
@@ -470,7 +470,7 @@ void mh_chain(const DevGraph& g, DevBM& bm, const int32_t* order, int32_t n, int
 void shuffle(const int32_t* base, int32_t n, uint64_t seed, uint32_t iter, uint32_t step, uint32_t dom,
              int32_t* order, Work& w, cudaStream_t st) {
     if (n <= 0) return;
-    k_shuffle_keys<<<grid_cap(n, 256, 152 * 16), 256, 0, st>>>(base, n, seed, iter, step, dom, w.keys, w.vals);
+    k_shuffle_keys<<<grid_cap(n, 256, device_sms() * 16), 256, 0, st>>>(base, n, seed, iter, step, dom, w.keys, w.vals);
     radix_sort_u64(w.keys, w.keys_alt, w.vals, w.vals_alt, n, 64, w.temp, st);
     cudaMemcpyAsync(order, w.vals, sizeof(int32_t) * n, cudaMemcpyDeviceToDevice, st);
     count_launches(1);

@@ -26,6 +26,28 @@ def evaluate(true_assignment, assignment, ctx=None):
     return out.as_dict()
 
 
+def partition_scores(num_vertices, contingency_table):
+    """calculate_f1_score and calculate_nmi (reference src/evaluate.cpp:9-98) of a contingency
+    table given as the reference passes it (a rows x columns matrix of counts): a dict with
+    f1, precision, recall, rand_index and nmi.  Host arithmetic in the library; no device."""
+    from . import _lib
+    m = np.ascontiguousarray(contingency_table, dtype=np.int64)
+    if m.ndim != 2 or m.size == 0:
+        raise ValueError("the contingency table must be a non-empty matrix")
+    out = _lib.Eval()
+    st = _lib.load().sbpgpu_partition_scores(int(num_vertices), m.shape[0], m.shape[1], m.ctypes.data_as(_lib.i64p),
+                                             ctypes.byref(out))
+    if st != 0:
+        raise ValueError("invalid contingency table or vertex count")
+    d = out.as_dict()
+    return {k: d[k] for k in ("f1", "precision", "recall", "rand_index", "nmi")}
+
+
+def calculate_f1_score(num_vertices, contingency_table):
+    """evaluate::calculate_f1_score (reference src/evaluate.cpp:9-61)."""
+    return partition_scores(num_vertices, contingency_table)["f1"]
+
+
 def nmi(true_assignment, assignment):
     t = np.asarray(true_assignment, dtype=np.int64)
     a = np.asarray(assignment, dtype=np.int64)

@@ -60,6 +60,14 @@ def main(root):
     npt = read(root, "test/nonparametric_entropy_test.cpp")
     npc = {name: float(val) for name, val in re.findall(r"const double ([A-Z_0-9]+) = ([0-9.]+);", npt)}
 
+    evt = read(root, "test/evaluate_test.cpp")
+
+    def matrix(name):
+        block = re.search(name + r" = \{(.*?)\};", evt, re.S).group(1)
+        return [ints(row) for row in re.findall(r"\{([^{}]*)\}", block)]
+
+    evc = {name: float(val) for name, val in re.findall(r"\b([A-Z][A-Za-z0-9]*) = ([0-9.]+);", evt)}
+
     out = {
         "source": "vtsynergy/SBP test/toy_example.hpp, test/*_test.cpp",
         "num_vertices": 11,
@@ -85,6 +93,10 @@ def main(root):
                                                "sparse_entropy": npc["SPARSE_ENTROPY"],
                                                "degree_dl": npc["DEGREE_DL"]}},
     }
+    # evaluate_test.cpp:17-44: calculate_f1_score on two contingency tables (EXPECT_FLOAT_EQ)
+    out["evaluate"] = {"matrix": matrix("Matrix"), "num_vertices": int(evc["N"]), "f1": evc["F1"],
+                       "rand_index": evc["RandIndex"], "recall": evc["Recall"], "precision": evc["Precision"],
+                       "matrix2": matrix("Matrix2"), "num_vertices2": int(evc["N2"]), "f1_2": evc["F12"]}
     dst = os.path.join(os.path.dirname(os.path.abspath(__file__)), "toy_example.json")
     with open(dst, "w") as f:
         json.dump(out, f, indent=1)
@@ -92,4 +104,6 @@ def main(root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python make_golden.py <path to the reference checkout>")
+    main(sys.argv[1])

@@ -78,3 +78,30 @@ def test_evaluate_rejects_bad_input():
         evaluate(np.full(4, -1, np.int32), np.zeros(4, np.int32))
     with pytest.raises(ValueError):
         evaluate(np.zeros(4, np.int32), np.zeros(5, np.int32))
+
+
+def _float_eq(a, b, ulps=4):
+    """EXPECT_FLOAT_EQ: both values as float32, at most 4 units in the last place apart."""
+    fa, fb = np.float32(a), np.float32(b)
+    ia, ib = (np.array([x], np.float32).view(np.int32)[0] for x in (fa, fb))
+    return abs(int(ia) - int(ib)) <= ulps
+
+
+def test_f1_known_answers_of_the_reference():
+    """calculate_f1_score on the reference's two contingency tables
+    (test/evaluate_test.cpp:17-61, fixtures in tests/golden): F1 0.620835 and 0.26938562,
+    and the Rand index, recall and precision the first test states, each as the reference
+    checks them (EXPECT_FLOAT_EQ).  The library's host scoring needs no device."""
+    import json
+    import os
+    from sbp_gb300.evaluate import calculate_f1_score, partition_scores
+    with open(os.path.join(os.path.dirname(__file__), "golden", "toy_example.json")) as f:
+        ev = json.load(f)["evaluate"]
+    s = partition_scores(ev["num_vertices"], ev["matrix"])
+    assert _float_eq(s["f1"], ev["f1"]), s
+    # the remaining figures are stated to 6 digits in the test's set-up
+    for k in ("rand_index", "recall", "precision"):
+        assert abs(s[k] - ev[k]) <= 5e-7, (k, s[k], ev[k])
+    assert _float_eq(calculate_f1_score(ev["num_vertices2"], ev["matrix2"]), ev["f1_2"])
+    with pytest.raises(ValueError):
+        partition_scores(1, ev["matrix"])
