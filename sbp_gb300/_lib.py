@@ -93,6 +93,7 @@ SIGNATURES = {
     "sbpgpu_ctx_synchronize": (ctypes.c_int, [vp]),
     "sbpgpu_ctx_stream": (vp, [vp]),
     "sbpgpu_ctx_set_cells_budget": (ctypes.c_int, [vp, ctypes.c_int64]),
+    "sbpgpu_ctx_set_cluster_blocks": (ctypes.c_int, [vp, ctypes.c_int64]),
     "sbpgpu_graph_create": (ctypes.c_int, [vp, ctypes.c_int64, ctypes.c_int64, i32p, i32p, ctypes.POINTER(vp)]),
     "sbpgpu_graph_create_device": (ctypes.c_int, [vp, ctypes.c_int64, ctypes.c_int64, vp, vp, ctypes.POINTER(vp)]),
     "sbpgpu_graph_load": (ctypes.c_int, [vp, ctypes.c_char_p, ctypes.c_int32, ctypes.POINTER(vp)]),

@@ -92,6 +92,11 @@ class Context:
         """Device bytes the merge carry-out may use for dense cell counts (0: hashed store)."""
         self.check(self.lib.sbpgpu_ctx_set_cells_budget(self.h, int(nbytes)))
 
+    def set_cluster_blocks(self, min_blocks):
+        """Smallest block count at which the MH chain runs on a thread-block cluster
+        (0: whenever there are more than 128 blocks); results do not depend on it."""
+        self.check(self.lib.sbpgpu_ctx_set_cluster_blocks(self.h, int(min_blocks)))
+
     def read_timing(self):
         t = _lib.KernelTiming()
         self.check(self.lib.sbpgpu_read_timing(self.h, ctypes.byref(t)))

@@ -108,6 +108,7 @@ struct sbpgpu_ctx {
     std::string err;
     bool timing = false;
     int64_t cells_budget = int64_t(16) << 30;  // dense carry-out cells, bytes
+    int64_t cluster_blocks = 8192;              // smallest B whose MH chain runs on a cluster
     DevFlags* flags_host = nullptr;            // pinned staging of the device flags
     std::vector<TimedSpan> pending;
     std::vector<cudaEvent_t> free_events;
@@ -485,12 +486,36 @@ void ensure_cells(sbpgpu_graph* g, uint64_t need) {
     w.cells_elems = need;
 }
 
+// The cluster chain's buffers (per-warp neighbour hashes and row scratch), allocated on
+// first use.  False when the device holds no cluster.
+bool ensure_cluster(sbpgpu_graph* g) {
+    const int cs = mh_cluster_size();
+    if (cs <= 0) return false;
+    Work& w = g->w;
+    if (!w.cl_hash) w.cl_hash = dalloc<int32_t>(g->owned, mh_cluster_hash_ints(cs));
+    if (!w.cl_scratch) w.cl_scratch = dalloc<int32_t>(g->owned, mh_cluster_scratch_ints(cs));
+    return true;
+}
+
 void chain_run(sbpgpu_bm* bm, const int32_t* order, int32_t n, int32_t max_k, int64_t k_sum, uint64_t seed,
                uint32_t it, uint32_t step, int mode) {
     sbpgpu_graph* g = bm->g;
     if (mode == ACC_NP) ensure_np(g);
     const int64_t B = bm->d.B;
     if (B > kWinSharedMax) ensure_cells(g, mh_window_cells((int32_t)B));
+    // Many blocks: the window spread over a thread-block cluster, cells dense when the
+    // budget holds them, else hashed.
+    if (B >= g->ctx->cluster_blocks && B > kWinSharedMax && max_k <= 4096 && ensure_cluster(g)) {
+        const bool hashed = !g->w.cells || mh_window_cells((int32_t)B) > g->w.cells_elems;
+        if (hashed) chain_init(bm->d, g->w, (uint64_t)(2 * k_sum + 4 * (int64_t)n), g->ctx->stream);
+        {
+            Span sp(g->ctx, 1);
+            mh_chain_cluster(g->dg, bm->d, order, n, max_k, hashed, seed, it, step, mode, g->w, g->ctx->stream);
+        }
+        g->st.proposals += n;
+        do_rebuild(bm);
+        return;
+    }
     WindowPlan plan{};
     if (mh_window_plan(bm->d.B, max_k, g->w, &plan)) {
         Span sp(g->ctx, 1);
@@ -1062,6 +1087,12 @@ sbpgpu_status sbpgpu_ctx_synchronize(sbpgpu_ctx* ctx) {
 }
 
 void* sbpgpu_ctx_stream(sbpgpu_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+sbpgpu_status sbpgpu_ctx_set_cluster_blocks(sbpgpu_ctx* ctx, int64_t min_blocks) {
+    if (!ctx || min_blocks < 0) return SBPGPU_EINVAL;
+    ctx->cluster_blocks = min_blocks;
+    return SBPGPU_OK;
+}
 
 sbpgpu_status sbpgpu_ctx_set_cells_budget(sbpgpu_ctx* ctx, int64_t bytes) {
     if (!ctx) return SBPGPU_EINVAL;
@@ -1710,6 +1741,7 @@ sbpgpu_status sbpgpu_gibbs_batch(sbpgpu_bm* bm, const sbpgpu_config* cfg, int64_
     sbpgpu_graph* g = bm->g;
     return guarded(g->ctx, [&] {
         if (bm->d.B < 2) throw ApiError(SBPGPU_EINVAL, "proposals need at least two blocks");
+        if (n > g->N) throw ApiError(SBPGPU_EINVAL, "a batch holds at most num_vertices vertices");
         for (int64_t i = 0; i < n; ++i)
             if (vertex[i] < 0 || vertex[i] >= g->N) throw ApiError(SBPGPU_EINVAL, "vertex out of range");
         cudaStream_t st = g->ctx->stream;
@@ -1736,6 +1768,7 @@ sbpgpu_status sbpgpu_mh_chain(sbpgpu_bm* bm, const sbpgpu_config* cfg, int64_t n
     sbpgpu_graph* g = bm->g;
     return guarded(g->ctx, [&] {
         if (bm->d.B < 2) throw ApiError(SBPGPU_EINVAL, "proposals need at least two blocks");
+        if (n > g->N) throw ApiError(SBPGPU_EINVAL, "the chain visits at most num_vertices vertices per call");
         int32_t max_k = 0;
         int64_t ksum = 0;
         for (int64_t i = 0; i < n; ++i) {

@@ -57,6 +57,9 @@ struct Work {
     int32_t dense_cap = 0;             // largest B the dense matrices hold
     // neighbour hashes of the windowed chain's high-degree vertices [16 warps x 4 x 8192]
     int32_t* win_hash = nullptr;
+    // the cluster chain's per-warp neighbour hashes and row scratch (allocated on first use)
+    int32_t* cl_hash = nullptr;
+    int32_t* cl_scratch = nullptr;
     // dense B x B cell values of the merge carry-out (allocated on demand within a budget)
     int32_t* cells = nullptr;
     uint64_t cells_elems = 0;
@@ -116,6 +119,16 @@ uint64_t mh_window_cells(int32_t B);
 bool mh_window_plan(int32_t B, int32_t max_k, const Work& w, WindowPlan* p);
 void mh_chain_window(const DevGraph& g, DevBM& bm, const int32_t* order, int32_t n, const WindowPlan& p,
                      uint64_t seed, uint32_t iter, uint32_t step, int mode, Work& w, cudaStream_t st);
+// The chain evaluated in windows spread over a thread-block cluster (chain_cluster.cu), for
+// blockmodels with many blocks: cells dense in w.cells (as the windowed chain's global mode)
+// or, when hashed is set, in the chain hash (chain_init first).  mh_cluster_size() is the
+// cluster size the device holds (0: none); the buffers w.cl_hash and w.cl_scratch hold
+// mh_cluster_hash_ints / mh_cluster_scratch_ints int32 for it.
+int mh_cluster_size();
+size_t mh_cluster_hash_ints(int cs);
+size_t mh_cluster_scratch_ints(int cs);
+void mh_chain_cluster(const DevGraph& g, DevBM& bm, const int32_t* order, int32_t n, int32_t max_k, bool hashed,
+                      uint64_t seed, uint32_t iter, uint32_t step, int mode, Work& w, cudaStream_t st);
 // order[i] = base[perm(i)] with the canonical shuffle keyed by (i, iter, step, dom).
 void shuffle(const int32_t* base, int32_t n, uint64_t seed, uint32_t iter, uint32_t step, uint32_t dom,
              int32_t* order, Work& w, cudaStream_t st);
