@@ -1,17 +1,24 @@
-"""Benchmark: full SBP (golden-section search, block merges, hybrid MCMC) on the 50k-vertex,
-1M-edge directed DCSBM graph, on one GB300 per rank.
+"""Benchmark: the first golden-section step of SBP on the 1M-vertex, 20M-edge directed DCSBM
+graph (the large high-overlap configuration), on one GB300 per rank.
 
-Default (N=1): one JSON line with proposals/s (vertex + merge proposals evaluated per
-second of full-SBP device time), the full-SBP wall time per step, the roofline of the
-dominant kernel, the end-to-end number through the C ABI with host buffers, and a CPU
-baseline (the CPU oracle, timed on a bounded sample of the same workload).
+The step is what sbp::stochastic_block_partition does first (src/sbp.cpp:23-35): from the
+N-block identity partition, the block-merge pass to N/2 blocks (10 merge proposals per
+block, the sequential carry-out) and then the hybrid-MCMC finetune until its early stop.
+Metric: proposals/s, counting the merge proposals drawn (10 per block, repeats included, as
+the reference's loop does) plus the vertex proposals visited.
 
---impl reference: the reference's CPU path for the same workload and metric on the host
-cores.  The reference cannot be built here (it needs MPI, tsl::robin_map, abseil, pcg
-and nlohmann/json, none of which ship with it), so its port in oracle/ runs instead,
-with all host threads, one bounded sample per step.
+Default (N=1): one JSON line with `value` (the step timed on the device with the graph
+resident), the end-to-end number through the C ABI with host buffers (graph upload, the
+step, the assignment read back), the roofline of the dominant kernel, the whole SBP's wall
+time, NMI and block count as extra keys, and a CPU baseline: the CPU oracle on a bounded
+sample of the same step.
 
-Multi-GPU: replicas only -- each rank partitions its own copy of the graph; value is
+--impl reference: the reference's CPU path for the same step and metric on all host
+cores.  The reference cannot be built here (it needs MPI, tsl::robin_map, abseil, pcg and
+nlohmann/json, none of which ship with it), so its line-cited port in oracle/ runs, one
+bounded sample of the step per bench step (see cpu_sample).
+
+Multi-GPU: replicas only -- each rank runs the step on its own copy of the graph; value is
 the proposals of all ranks over the slowest rank's time.
 """
 import argparse
@@ -29,20 +36,24 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-CONFIG = "C2"  # --config
+CONFIG = "C3"  # --config
 SEED = 1
 METRIC = "proposals/s"
+SAMPLE_DIV = 32        # the CPU sample: the merge proposals of 1/32 of the blocks
 
 
 def workload_desc():
     from sbp_gb300 import dcsbm
     c = dcsbm.CONFIGS[CONFIG]
-    return {"workload": "full SBP, hybrid MCMC, directed DCSBM N=%d E~%d, %d planted blocks, Dirichlet(%g) sizes, "
+    return {"workload": "first golden-section step of SBP (merge pass N -> N/2 blocks, then hybrid MCMC until its "
+                        "early stop) on the directed DCSBM graph N=%d E~%d, %d planted blocks, Dirichlet(%g) sizes, "
                         "power-law degrees 2.1 in [%d,%d], within:between %g" %
                         (c["num_vertices"], c["num_edges"], c["num_blocks"], c["alpha"], c["dmin"], c["dmax"],
                          c["ratio"]),
             "num_vertices": c["num_vertices"], "num_edges_target": c["num_edges"], "algorithm": "hybrid_mcmc",
-            "graph_seed": 0, "proposal_seed": SEED, "ids": "int32", "counts": "int32",
+            "graph_seed": 0, "proposal_seed": SEED, "ids": "int32",
+            "counts": "int32 block-edge counts (exact: every count is at most E < 2^31)",
+            "proposals": "merge proposals drawn (10 per block) + vertex proposals visited",
             "l2": "flushed between steps (256 MiB write)"}
 
 
@@ -146,25 +157,58 @@ def algorithmic_bytes(kind, stats):
     return None
 
 
-def run_cpu_baseline(src, dst, n):
-    """The CPU oracle on a bounded sample of the same workload: the first outer step of the
-    golden-section search (merge pass from B = N to N/2, then the hybrid MCMC finetune)."""
-    sys.path.insert(0, os.path.join(ROOT, "tests"))
-    import oracle_bind as ob
-    ob.build()
-    cores = os.cpu_count() or 1
-    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
-    g = ob.Graph(n, src, dst)
-    bm = ob.Blockmodel(g, n, np.arange(n, dtype=np.int32))
-    cfg = ob.make_config("hybrid_mcmc")
-    t0 = time.perf_counter()
-    s1 = bm.merge_blocks(cfg, seed=SEED, step=0, num_to_merge=n // 2)
-    s2 = bm.mcmc(cfg, seed=SEED, step=0, golden_ratio_not_reached=True)
-    dt = time.perf_counter() - t0
-    props = s1.merge_proposals + s2.proposals
-    return {"value": props / dt, "unit": METRIC, "cores": int(os.environ["OMP_NUM_THREADS"]), "kind": "port",
-            "sample": "first golden-section step of the same SBP (merge pass %d -> %d blocks + hybrid MCMC), "
-                      "%d proposals in %.1f s" % (n, n // 2, props, dt)}
+def hub_mask(n, src, dst, mh_percent=0.075):
+    """Graph::sort_vertices (src/graph.cpp:235-268): the top mh_percent of the vertices by
+    degree (out + in - has a self-loop), stable in vertex order, are the high-degree
+    vertices the hybrid MCMC walks as a sequential chain."""
+    deg = np.bincount(src, minlength=n) + np.bincount(dst, minlength=n)
+    deg -= np.bincount(src[src == dst], minlength=n) > 0
+    order = np.argsort(-deg, kind="stable")
+    mask = np.zeros(n, bool)
+    limit = np.float32(mh_percent) * np.float32(n)  # float arithmetic as graph.cpp:252
+    mask[order[:int(np.count_nonzero(np.arange(n, dtype=np.float32) < limit))]] = True
+    return mask
+
+
+def split_planted(planted, n, target_blocks, seed=3):
+    """The planted partition with every planted block split at random into sub-blocks,
+    about target_blocks blocks in all, numbered densely."""
+    rng = np.random.default_rng(seed)
+    k = max(1, -(-target_blocks // (int(planted.max()) + 1)))
+    _, a = np.unique(planted.astype(np.int64) * k + rng.integers(0, k, n), return_inverse=True)
+    return a.astype(np.int32)
+
+
+class CpuSample:
+    """The oracle (the reference's hot path restated, OpenMP over all host cores) on a bounded
+    sample of the bench step: the merge pass's proposal loop (block_merge.cpp:188-217; 10
+    draws per block, repeats skipped, each scored by block_merge_delta_mdl) over a random
+    1/SAMPLE_DIV of the blocks of the N-block identity partition the step starts from.  That
+    phase carries 10 N of the step's proposals and is the CPU's fastest per proposal: the
+    sample leaves out the sequential carry-out and the hybrid MCMC (whose high-degree chain
+    is sequential), which favours the CPU."""
+
+    def __init__(self, src, dst, n):
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        import oracle_bind as ob
+        ob.build()
+        self.cores = os.cpu_count() or 1
+        os.environ.setdefault("OMP_NUM_THREADS", str(self.cores))
+        self.n = n
+        self.g = ob.Graph(n, src, dst)
+        self.bm = ob.Blockmodel(self.g, n, np.arange(n, dtype=np.int32))
+
+    def run(self, index):
+        rng = np.random.default_rng(1000 + index)
+        m = max(1, self.n // SAMPLE_DIV)
+        blocks = np.sort(rng.choice(self.n, m, replace=False)).astype(np.int32)
+        t0 = time.perf_counter()
+        _, _, draws = self.bm.merge_proposals(blocks, SEED, 0)
+        dt = time.perf_counter() - t0
+        return {"value": draws / dt, "unit": METRIC, "cores": int(os.environ["OMP_NUM_THREADS"]), "kind": "port",
+                "sample": "first golden-section step, its merge-proposal phase on a random 1/%d of the blocks "
+                          "(%d blocks, %d proposals drawn) in %.2f s; the carry-out and the MCMC are not sampled"
+                          % (SAMPLE_DIV, m, draws, dt)}
 
 
 def reference_arm(args):
@@ -174,10 +218,10 @@ def reference_arm(args):
     from sbp_gb300 import dcsbm
     src, dst, planted = dcsbm.generate_config(CONFIG, seed=0)
     n = dcsbm.CONFIGS[CONFIG]["num_vertices"]
-    vals = []
-    last = None
+    cpu = CpuSample(src, dst, n)
+    vals, last = [], None
     for i in range(args.warmup + args.steps):
-        last = run_cpu_baseline(src, dst, n)
+        last = cpu.run(i)
         if i >= args.warmup:
             vals.append(last["value"])
     value = float(np.mean(vals))
@@ -202,10 +246,7 @@ def profile_phase(args):
     _b.build()
     src, dst, planted = sb.dcsbm.generate_config(CONFIG, seed=0)
     n = sb.dcsbm.CONFIGS[CONFIG]["num_vertices"]
-    rng = np.random.default_rng(3)
-    k = max(1, -(-args.blocks // (int(planted.max()) + 1)))
-    _, a = np.unique(planted.astype(np.int64) * k + rng.integers(0, k, n), return_inverse=True)
-    a = a.astype(np.int32)
+    a = split_planted(planted, n, args.blocks)
     B = int(a.max()) + 1
     ctx = sb.Context(0)
     if args.cells_budget is not None:
@@ -360,6 +401,7 @@ def main():
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end C ABI run (profiling)")
+    ap.add_argument("--no-full-sbp", action="store_true", help="skip the whole-SBP run after the timed steps")
     ap.add_argument("--config", default=CONFIG, choices=["C1", "C2", "C3"])
     ap.add_argument("--cells-budget", type=int, default=None,
                     help="device bytes for the carry-out's dense cell counts (library default if unset)")
@@ -396,6 +438,7 @@ def main():
     _b.build()
     src, dst, planted = sb.dcsbm.generate_config(CONFIG, seed=0)
     n = sb.dcsbm.CONFIGS[CONFIG]["num_vertices"]
+    ident = np.arange(n, dtype=np.int32)
     ctx = sb.Context(local)
     if args.cells_budget is not None:
         ctx.set_cells_budget(args.cells_budget)
@@ -404,8 +447,23 @@ def main():
     stream = torch.cuda.ExternalStream(ctx.lib.sbpgpu_ctx_stream(ctx.h), device=local)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=local)
 
+    def first_step(graph):
+        """Blockmodel(N, graph, 0.5) on the identity partition (sbp.cpp:23), built before
+        the caller's timing starts."""
+        return sb.Blockmodel(n, graph, 0.5, ident)
+
+    def run_step(bm):
+        """The golden-section step (sbp.cpp:27-35): merge_blocks to N/2 blocks, then the
+        hybrid-MCMC finetune with the pre-bracket early stop.  Returns (proposals drawn,
+        merge stats, mcmc stats)."""
+        _, s1 = sb.block_merge.merge_blocks(bm, bm.graph, args=sargs, step=0, num_blocks_to_merge=n // 2)
+        _, s2 = sb.finetune.mcmc(0, bm.graph, bm, True, sargs)
+        return 10 * n + s2["proposals"], s1, s2
+
     for _ in range(args.warmup):
-        sb.sbp.stochastic_block_partition(G, sargs)
+        bm = first_step(G)
+        run_step(bm)
+        bm.close()
     torch.cuda.synchronize()
 
     ctx.set_timing(True)
@@ -415,20 +473,25 @@ def main():
         torch.distributed.barrier()
     torch.cuda.synchronize()
     clocks.start()
-    step_ms, totals, results = [], {}, []
+    step_ms, totals, proposals, iters = [], {}, 0, []
     t_all0 = time.perf_counter()
     for _ in range(args.steps):
+        bm = first_step(G)
         flush.fill_(1)
+        ctx.synchronize()
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        asg, B, mdl, st = sb.sbp.stochastic_block_partition(G, sargs)
+        p, s1, s2 = run_step(bm)
         e1.record(stream)
         e1.synchronize()
         step_ms.append(e0.elapsed_time(e1))
-        results.append((asg, B, mdl))
-        for k, v in st.items():
-            totals[k] = totals.get(k, 0) + v
+        proposals += p
+        iters.append(s2["mcmc_iterations"])
+        for st in (s1, s2):
+            for k, v in st.items():
+                totals[k] = totals.get(k, 0) + v
+        last_bm = bm
     torch.cuda.synchronize()
     if ws > 1:
         torch.distributed.barrier()
@@ -436,26 +499,43 @@ def main():
     clk = clocks.stop()
     timing = ctx.read_timing()
     ctx.set_timing(False)
+    step_blocks = last_bm.num_blocks()
+    step_mdl = last_bm.getOverall_entropy()
+    last_bm.close()
     device_s = sum(step_ms) / 1e3
-    proposals = totals["proposals"] + totals["merge_proposals"]
     slowest_s, all_props = combine_ranks(device_s, proposals, local)
     value = all_props / slowest_s
 
-    # end to end through the C ABI with host buffers: graph upload + partition + result read
+    # end to end through the C ABI with host buffers: graph upload, the step, the
+    # assignment read back
     e2e_s, e2e_props = 0.0, 0
     for _ in range(0 if args.no_e2e else max(1, min(args.steps, 2))):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         Gh = sb.Graph(n, src, dst, ctx=ctx)
-        asg_h, B_h, mdl_h, st_h = sb.sbp.stochastic_block_partition(Gh, sargs)
+        bm = first_step(Gh)
+        p, _, _ = run_step(bm)
+        asg_h = bm.block_assignment()
+        bm.close()
         Gh.close()
         torch.cuda.synchronize()
         e2e_s += time.perf_counter() - t0
-        e2e_props += st_h["proposals"] + st_h["merge_proposals"]
+        e2e_props += p
     E = int(src.size)
     loops = int(np.sum(src == dst))
-    h2d = 4 * ((n + 1) * 2 + E + (E - loops) + n + E + (E + 2) + n)
+    h2d = 4 * ((n + 1) * 2 + E + (E - loops) + n + E + (E + 2) + n) + 4 * n
     d2h = 4 * n
+
+    # the whole SBP once, for the full-SBP wall time and quality beside the step rate
+    full = {}
+    if not args.no_full_sbp:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        asg, B, mdl, st = sb.sbp.stochastic_block_partition(G, sargs)
+        torch.cuda.synchronize()
+        full = {"full_sbp_s": time.perf_counter() - t0, "full_sbp_blocks": int(B), "full_sbp_mdl": mdl,
+                "full_sbp_nmi": sb.evaluate.nmi(planted, asg), "full_sbp_outer_steps": st["outer_steps"],
+                "full_sbp_proposals": st["proposals"] + st["merge_proposals"]}
 
     # roofline of the dominant kernel category
     cats = {k[:-3]: v for k, v in timing.items() if k.endswith("_ms")}
@@ -472,24 +552,25 @@ def main():
         roof.update({"achieved": achieved, "frac": achieved / peak})
     else:
         roof.update({"achieved": None, "frac": None,
-                     "note": "latency-bound single-CTA sequential phase; no bandwidth roofline applies"})
-    asg, B, mdl = results[-1]
+                     "note": "latency-bound sequential phase; no bandwidth roofline applies"})
     out = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": ws, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": float(np.mean(step_ms)), "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "int64+f64", "data": "synthetic (seeded DCSBM)",
            "config": dict(workload_desc(), parallelism="replicas" if ws > 1 else "single GPU"),
-           "full_sbp_ms": float(np.mean(step_ms)), "wall_s": wall,
-           "num_blocks": int(B), "mdl": mdl, "nmi": sb.evaluate.nmi(planted, asg),
+           "wall_s": wall, "step_blocks": int(step_blocks), "step_mdl": step_mdl,
+           "step_mcmc_iterations": iters[-1] if iters else None,
            "proposals_per_step": proposals / args.steps,
-           "vertex_proposals_per_step": totals["proposals"] / args.steps,
-           "merge_proposals_per_step": totals["merge_proposals"] / args.steps,
-           "edges_swept_per_s": totals["edges_swept"] / device_s,
-           "kernel_ms": cats, "gpu_launches": int(totals["kernel_launches"]),
+           "merge_proposals_drawn_per_step": 10.0 * n,
+           "vertex_proposals_per_step": totals.get("proposals", 0) / args.steps,
+           "merges_per_step": totals.get("merges", 0) / args.steps,
+           "edges_swept_per_s": totals.get("edges_swept", 0) / device_s,
+           "kernel_ms": cats, "gpu_launches": int(totals.get("kernel_launches", 0)),
            "e2e": {"value": e2e_props / e2e_s if e2e_s > 0 else None, "unit": METRIC,
                    "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
            "roofline": roof, "clocks": clk}
+    out.update(full)
     if rank == 0 and not args.no_cpu_baseline:
-        out["cpu_baseline"] = run_cpu_baseline(src, dst, n)
+        out["cpu_baseline"] = CpuSample(src, dst, n).run(0)
     if rank == 0:
         print(json.dumps(out))
     if ws > 1:

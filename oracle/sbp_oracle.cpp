@@ -1262,6 +1262,39 @@ extern "C" int64_t ora_propose_merge(const ora_bm* bm, int64_t r, uint64_t seed,
     return propose_merge(bm, r, w);
 }
 
+/* The proposal loop of block_merge::merge_blocks (block_merge.cpp:188-217) over the blocks
+ * blocks[0..n) only: 10 draws per block, repeats skipped, the best proposal and its delta
+ * per listed block.  OpenMP over blocks as the reference.  Returns the draws made. */
+extern "C" int64_t ora_merge_proposals(const ora_bm* bm, const int32_t* blocks, int64_t n, uint64_t seed,
+                                       uint32_t step, int32_t nonparametric, int32_t* best_out,
+                                       double* dS_out) {
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int64_t k = 0; k < n; ++k) {
+        const int64_t r = blocks[k];
+        std::set<int64_t> past;
+        int64_t best = -1;
+        double best_dS = DBL_MAX;
+        for (int i = 0; i < 10; ++i) {
+            uint32_t w[4];
+            draw(seed, (uint32_t)r, 0, step, DOM_MERGE | ((uint32_t)i << 8), w);
+            const int64_t s = propose_merge(bm, r, w);
+            double dS = DBL_MAX;
+            if (!past.count(s)) {
+                dS = (double)(nonparametric ? np_merge_dS(bm, r, s, merge_delta(bm, r, s)) : merge_dS_fixed(bm, r, s)) *
+                     kInvFix;
+                past.insert(s);
+            }
+            if (dS < best_dS) {
+                best_dS = dS;
+                best = s;
+            }
+        }
+        best_out[k] = (int32_t)best;
+        dS_out[k] = best_dS;
+    }
+    return 10 * n;
+}
+
 extern "C" int64_t ora_gibbs_batch(ora_bm* bm, const int32_t* vertices, int64_t n, uint64_t seed,
                                    uint32_t iteration, uint32_t step, const ora_config* cfg, int32_t* out_moves,
                                    double* out_dS) {

@@ -94,6 +94,11 @@ int64_t ora_propose_vertex(const ora_bm* bm, int64_t vertex, uint64_t seed,
 int64_t ora_propose_merge(const ora_bm* bm, int64_t block, uint64_t seed,
                           uint32_t c2, int32_t proposal_index);
 
+/* The proposal loop of block_merge::merge_blocks (block_merge.cpp:188-217) restricted to
+ * blocks[0..n): best proposal and delta per listed block; returns the draws made (10 n). */
+int64_t ora_merge_proposals(const ora_bm* bm, const int32_t* blocks, int64_t n, uint64_t seed,
+                            uint32_t step, int32_t nonparametric, int32_t* best_out, double* dS_out);
+
 /* One parallel-propose + serial-apply batch over vertices[0..n) (finetune.cpp:65-86):
  * proposals against the same snapshot, applied in vertex-id order with the
  * block-size-1 rejection of blockmodel.cpp:437-443. out_moves[i] = proposal or -1. */

@@ -297,7 +297,9 @@ class Blockmodel:
 
     # accessors named as in blockmodel.hpp
     def block_assignment(self):
-        return self.read()["assignment"]
+        a = np.zeros(self.graph.num_vertices(), np.int32)
+        self.ctx.check(self.ctx.lib.sbpgpu_bm_read(self.h, _p(a, i32p), None, None, None, None, None, None, None))
+        return a
 
     def degrees_out(self):
         return self.read()["d_out"]

@@ -101,6 +101,9 @@ def lib():
                                       ctypes.c_uint32, ctypes.POINTER(OraConfig), i32p, f64p]
         L.ora_apply_moves.restype = ctypes.c_int64
         L.ora_apply_moves.argtypes = [ctypes.c_void_p, i32p]
+        L.ora_merge_proposals.restype = ctypes.c_int64
+        L.ora_merge_proposals.argtypes = [ctypes.c_void_p, i32p, ctypes.c_int64, ctypes.c_uint64, ctypes.c_uint32,
+                                          ctypes.c_int32, i32p, f64p]
         L.ora_mh_chain.restype = ctypes.c_int64
         L.ora_mh_chain.argtypes = [ctypes.c_void_p, i32p, ctypes.c_int64, ctypes.c_uint64, ctypes.c_uint32,
                                    ctypes.c_uint32, ctypes.POINTER(OraConfig)]
@@ -342,6 +345,16 @@ class Blockmodel:
         n = lib().ora_gibbs_batch(self.h, _p(v, i32p), v.size, seed, iteration, step, ctypes.byref(cfg),
                                   _p(moves, i32p), _p(dS, f64p))
         return int(n), moves, dS
+
+    def merge_proposals(self, blocks, seed, step, nonparametric=False):
+        """Best merge proposal and delta of each listed block (the merge pass's proposal
+        loop); returns (best, dS, draws)."""
+        b = np.ascontiguousarray(blocks, np.int32)
+        best = np.zeros(b.size, np.int32)
+        dS = np.zeros(b.size, np.float64)
+        draws = lib().ora_merge_proposals(self.h, _p(b, i32p), b.size, int(seed), int(step), int(bool(nonparametric)),
+                                          _p(best, i32p), _p(dS, f64p))
+        return best, dS, int(draws)
 
     def apply_moves(self, moves_per_vertex):
         m = np.ascontiguousarray(moves_per_vertex, dtype=np.int32)
