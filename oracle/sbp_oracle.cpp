@@ -1295,6 +1295,59 @@ extern "C" int64_t ora_merge_proposals(const ora_bm* bm, const int32_t* blocks, 
     return 10 * n;
 }
 
+/* A bounded sample of one golden-section step (sbp.cpp:27-35), for timing: the merge pass's
+ * proposal loop over blocks[0..n) (block_merge.cpp:188-217), the carry-out
+ * (block_merge.cpp:40-117) of their queue until n / 2 merges, and `sweeps` hybrid-MCMC
+ * sweeps (finetune.cpp:563-646) over the vertices of the blocks that received a merge:
+ * those flagged in hub[] as the sequential chain, the rest as one asynchronous-Gibbs batch.
+ * Mutates bm (its blocks keep their ids; merged-away blocks stay empty).  counts[0..2] =
+ * proposals drawn, merges, vertex proposals. */
+extern "C" void ora_step_sample(ora_bm* bm, const int32_t* blocks, int64_t n, const uint8_t* hub, uint64_t seed,
+                                uint32_t step, const ora_config* cfg, int32_t sweeps, int64_t* counts) {
+    std::vector<int32_t> best(n);
+    std::vector<double> dS(n);
+    counts[0] = ora_merge_proposals(bm, blocks, n, seed, step, cfg->nonparametric, best.data(), dS.data());
+    std::set<std::pair<double, int64_t>> queue;
+    std::vector<int64_t> parent(bm->B), prop(bm->B, -1);
+    for (int64_t i = 0; i < bm->B; ++i) parent[i] = i;
+    for (int64_t k = 0; k < n; ++k) {
+        if (best[k] < 0) continue;
+        queue.insert({dS[k], (int64_t)blocks[k]});
+        prop[blocks[k]] = best[k];
+    }
+    std::vector<uint8_t> target(bm->B, 0);
+    int64_t merged = 0;
+    while (merged < n / 2 && !queue.empty()) {
+        const auto top = *queue.begin();
+        queue.erase(queue.begin());
+        const int64_t from = top.second;
+        const int64_t to = uf_find(parent, prop[from]);
+        if (from == to) continue;
+        const DeltaMap d = merge_delta(bm, from, to);
+        const double actual = (double)(cfg->nonparametric ? np_merge_dS(bm, from, to, d)
+                                                          : merge_delta_mdl_generic<int64_t>(bm, from, to, d, ce_fixed)) *
+                              kInvFix;
+        if (!queue.empty() && actual > queue.begin()->first) {
+            queue.insert({actual, from});
+            continue;
+        }
+        merge_block(bm, from, to, d);
+        parent[from] = to;
+        target[to] = 1;
+        merged++;
+    }
+    for (auto& b : bm->asg) b = (int32_t)uf_find(parent, b);
+    counts[1] = merged;
+    std::vector<int32_t> chain, rest;
+    for (int64_t v = 0; v < bm->g->N; ++v)
+        if (target[bm->asg[v]]) (hub[v] ? chain : rest).push_back((int32_t)v);
+    for (int32_t it = 0; it < sweeps; ++it) {
+        for (int32_t v : chain) mh_step(bm, v, seed, (uint32_t)it, step, cfg, nullptr);
+        gibbs_batch(bm, rest.data(), (int64_t)rest.size(), seed, (uint32_t)it, step, cfg, nullptr, nullptr, nullptr);
+    }
+    counts[2] = (int64_t)sweeps * (int64_t)(chain.size() + rest.size());
+}
+
 extern "C" int64_t ora_gibbs_batch(ora_bm* bm, const int32_t* vertices, int64_t n, uint64_t seed,
                                    uint32_t iteration, uint32_t step, const ora_config* cfg, int32_t* out_moves,
                                    double* out_dS) {

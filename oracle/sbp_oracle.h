@@ -99,6 +99,13 @@ int64_t ora_propose_merge(const ora_bm* bm, int64_t block, uint64_t seed,
 int64_t ora_merge_proposals(const ora_bm* bm, const int32_t* blocks, int64_t n, uint64_t seed,
                             uint32_t step, int32_t nonparametric, int32_t* best_out, double* dS_out);
 
+/* A bounded sample of one golden-section step for timing: the merge proposals of
+ * blocks[0..n), the carry-out of their queue to n / 2 merges, then `sweeps` hybrid sweeps
+ * over the vertices of the merged blocks (hub[v]: chain, else one Gibbs batch).  Mutates
+ * bm.  counts[0..2] = proposals drawn, merges, vertex proposals. */
+void ora_step_sample(ora_bm* bm, const int32_t* blocks, int64_t n, const uint8_t* hub, uint64_t seed,
+                     uint32_t step, const ora_config* cfg, int32_t sweeps, int64_t* counts);
+
 /* One parallel-propose + serial-apply batch over vertices[0..n) (finetune.cpp:65-86):
  * proposals against the same snapshot, applied in vertex-id order with the
  * block-size-1 rejection of blockmodel.cpp:437-443. out_moves[i] = proposal or -1. */

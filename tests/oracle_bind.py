@@ -101,6 +101,9 @@ def lib():
                                       ctypes.c_uint32, ctypes.POINTER(OraConfig), i32p, f64p]
         L.ora_apply_moves.restype = ctypes.c_int64
         L.ora_apply_moves.argtypes = [ctypes.c_void_p, i32p]
+        L.ora_step_sample.argtypes = [ctypes.c_void_p, i32p, ctypes.c_int64, ctypes.POINTER(ctypes.c_uint8),
+                                      ctypes.c_uint64, ctypes.c_uint32, ctypes.POINTER(OraConfig), ctypes.c_int32,
+                                      i64p]
         L.ora_merge_proposals.restype = ctypes.c_int64
         L.ora_merge_proposals.argtypes = [ctypes.c_void_p, i32p, ctypes.c_int64, ctypes.c_uint64, ctypes.c_uint32,
                                           ctypes.c_int32, i32p, f64p]
@@ -355,6 +358,17 @@ class Blockmodel:
         draws = lib().ora_merge_proposals(self.h, _p(b, i32p), b.size, int(seed), int(step), int(bool(nonparametric)),
                                           _p(best, i32p), _p(dS, f64p))
         return best, dS, int(draws)
+
+    def step_sample(self, blocks, hub, seed, step, cfg, sweeps):
+        """A bounded sample of a golden-section step (merge proposals of the listed blocks,
+        their carry-out to half as many merges, hybrid sweeps over the merged blocks'
+        vertices); returns (proposals drawn, merges, vertex proposals)."""
+        b = np.ascontiguousarray(blocks, np.int32)
+        h = np.ascontiguousarray(hub, np.uint8)
+        c = np.zeros(3, np.int64)
+        lib().ora_step_sample(self.h, _p(b, i32p), b.size, h.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)),
+                              int(seed), int(step), ctypes.byref(cfg), int(sweeps), _p(c, i64p))
+        return int(c[0]), int(c[1]), int(c[2])
 
     def apply_moves(self, moves_per_vertex):
         m = np.ascontiguousarray(moves_per_vertex, dtype=np.int32)
