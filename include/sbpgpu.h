@@ -82,10 +82,11 @@ void* sbpgpu_ctx_stream(sbpgpu_ctx* ctx);
  * of cell counts; larger blockmodels use the hashed cell store.  Default 16 GiB; 0
  * always uses the hash.  Results do not depend on it.  No counterpart in the reference. */
 sbpgpu_status sbpgpu_ctx_set_cells_budget(sbpgpu_ctx* ctx, int64_t bytes);
-/* Smallest block count at which the sequential Metropolis-Hastings chain is evaluated in
- * windows spread over a thread-block cluster instead of one CTA (default 8192; 0: whenever
- * the blockmodel has more than 128 blocks).  Results do not depend on it.  No counterpart
- * in the reference. */
+/* Smallest block count at which the sequential phases -- the Metropolis-Hastings chain and
+ * the exact merge carry-out -- are evaluated in wide windows spread over a thread-block
+ * cluster instead of one CTA (default 8192; 0: always, for the chain once the blockmodel
+ * has more than 128 blocks).  Results do not depend on it.  No counterpart in the
+ * reference. */
 sbpgpu_status sbpgpu_ctx_set_cluster_blocks(sbpgpu_ctx* ctx, int64_t min_blocks);
 
 /* ---- graph: replaces Graph(out_neighbors, in_neighbors, ...) (include/graph.hpp:29-60)

@@ -108,7 +108,7 @@ struct sbpgpu_ctx {
     std::string err;
     bool timing = false;
     int64_t cells_budget = int64_t(16) << 30;  // dense carry-out cells, bytes
-    int64_t cluster_blocks = 8192;              // smallest B whose MH chain runs on a cluster
+    int64_t cluster_blocks = 8192;              // smallest B whose sequential phases run on a cluster
     DevFlags* flags_host = nullptr;            // pinned staging of the device flags
     std::vector<TimedSpan> pending;
     std::vector<cudaEvent_t> free_events;
@@ -497,6 +497,20 @@ bool ensure_cluster(sbpgpu_graph* g) {
     return true;
 }
 
+// The cluster carry-out's reader lists, allocated on first use.  False when the device
+// holds no cluster.
+bool ensure_cluster_carry(sbpgpu_graph* g) {
+    if (carry_cluster_size() <= 0) return false;
+    Work& w = g->w;
+    if (!w.cc_head) {
+        w.cc_node_cap = (int32_t)std::min<int64_t>(std::max<int64_t>(2 * g->E, 1 << 20), int64_t(1) << 24);
+        w.cc_head = dalloc<int32_t>(g->owned, g->N);
+        w.cc_nodes = dalloc<int32_t>(g->owned, 3 * (size_t)w.cc_node_cap);
+        w.cc_used = dalloc<int32_t>(g->owned, 1);
+    }
+    return true;
+}
+
 void chain_run(sbpgpu_bm* bm, const int32_t* order, int32_t n, int32_t max_k, int64_t k_sum, uint64_t seed,
                uint32_t it, uint32_t step, int mode) {
     sbpgpu_graph* g = bm->g;
@@ -815,9 +829,11 @@ void merge_impl(sbpgpu_bm* bm, const sbpgpu_config& cfg, uint64_t seed, int32_t 
         merge_propose(g->dg, bm->d, seed, (uint32_t)step, g->w, g->ctx->stream, cfg.nonparametric != 0);
     }
     if (!cfg.approximate) ensure_cells(g, (uint64_t)B * (uint64_t)B);
+    const bool cluster = !cfg.approximate && B >= g->ctx->cluster_blocks && ensure_cluster_carry(g);
     {
         Span sp(g->ctx, 3);
-        carry_out(g->dg, bm->d, num_to_merge, cfg.approximate, g->w, g->ctx->stream, cfg.nonparametric != 0);
+        carry_out(g->dg, bm->d, num_to_merge, cfg.approximate, g->w, g->ctx->stream, cfg.nonparametric != 0,
+                  cluster);
     }
     int32_t sc[3] = {0, 0, 0};
     CK(cudaMemcpyAsync(sc, g->w.d_scalar, sizeof(sc), cudaMemcpyDeviceToHost, g->ctx->stream));

@@ -1,0 +1,570 @@
+// Exact block-merge carry-out (block_merge::carry_out_best_merges_advanced, reference
+// src/block_merge.cpp:40-117) on a thread-block cluster, for blockmodels with many blocks.
+//
+// The round structure is the one of carry.cu (the W smallest live queue entries are
+// re-scored against one state, the reference's pop / put-back / merge rule is replayed over
+// those values up to the first entry whose value a merge of the round has changed, and the
+// round's merges are applied together), with a window of 16 entries per CTA of the cluster
+// (up to 256) so that the many independent merges of a large blockmodel are found in few
+// rounds.  CTA 0 keeps the queue and replays the rule; the cluster's distributed shared
+// memory and hardware barriers carry the rest:
+//   1. CTA 0 selects the candidates (the W smallest entries of the sorted proposals, the
+//      global put-back runs and its shared put-back buffer) and the bound (the next entry);
+//   2. each warp re-scores one candidate and registers, in a per-block reader list, every
+//      block its value depends on (its two blocks and the third blocks of its row and
+//      column);
+//   3. each warp walks the reader lists of its candidate's two blocks and marks, in the
+//      readers' conflict masks, that a merge of this candidate changes their values;
+//   4. CTA 0 collects the values and masks and replays the rule on one thread (a pop of a
+//      candidate or put-back entry whose mask meets a merge of the round ends the round),
+//      then folds the round's put-backs into its buffer;
+//   5. the round's merges (disjoint rows, columns and targets, by the conflict rule) are
+//      applied by all CTAs at once, and the reader lists are cleared.
+// Merges, their order and every put-back delta equal those of the one-at-a-time loop; ties
+// of equal delta pop in ascending block order.
+#include <cooperative_groups.h>
+
+#include <algorithm>
+#include <stdexcept>
+
+#include "carry.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace sbp {
+
+namespace {
+
+constexpr int kCcWarps = 16;
+constexpr int kCcThreads = kCcWarps * 32;
+constexpr int kCcMaxCluster = 16;
+constexpr int kCcMaxW = kCcWarps * kCcMaxCluster;  // candidates per round
+constexpr int kCcWords = kCcMaxW / 32;              // words of a conflict mask
+constexpr int kCcQS = 4096;                         // CTA 0's sorted put-back buffer
+
+// Shared memory of every CTA (dynamic); the queue parts are used by CTA 0 only.
+struct CcShared {
+    long long s_dS[2][kCcQS];
+    int32_t s_blk[2][kCcQS];
+    long long hs_dS[3][kCcMaxW + 1];
+    int32_t hs_blk[3][kCcMaxW + 1];
+    long long c_dS[kCcMaxW];
+    int32_t c_blk[kCcMaxW];
+    int32_t c_src[kCcMaxW];
+    int32_t c_to[kCcMaxW];
+    long long c_act[kCcMaxW];
+    int32_t c_count[kCcMaxW];
+    uint32_t conf[kCcMaxW][kCcWords];  // bit i of conf[j]: a merge of candidate i changes j's value
+    int32_t m_from[kCcMaxW], m_to[kCcMaxW];
+    long long h_d[kCcMaxW];  // replay's put-back heap
+    int32_t h_b[kCcMaxW], h_c[kCcMaxW];
+    long long q_dS[kCcMaxW];  // the round's remaining put-backs, sorted
+    int32_t q_blk[kCcMaxW];
+    uint32_t mm[kCcWords];  // candidates merged in the round
+    // this CTA's own candidates
+    int32_t my_to[kCcWarps];
+    long long my_act[kCcWarps];
+    int32_t my_count[kCcWarps];
+    uint32_t my_conf[kCcWarps][kCcWords];
+    long long b_dS, merged, rounds;
+    int32_t b_blk;
+    int32_t p, q, nR, rsel, ns, ssel, ne;
+    int32_t ncand, has_bound, done, nm, cS, nq;
+};
+
+// Per-block reader lists of a round: head[b] (or -1) and nodes (block, candidate, next).
+struct Readers {
+    int32_t* head;
+    int32_t* node;
+    int32_t cap;
+    int32_t* used;
+    __device__ __forceinline__ bool add(int32_t b, int32_t cand) const {
+        const int32_t k = atomicAdd(used, 1);
+        if (k >= cap) return false;
+        node[3 * k] = b;
+        node[3 * k + 1] = cand;
+        node[3 * k + 2] = atomicExch(head + b, k);
+        return true;
+    }
+};
+
+__device__ __forceinline__ void heap_push(CcShared& sh, int& n, long long d, int32_t b, int32_t c) {
+    int i = n++;
+    while (i > 0) {
+        const int p = (i - 1) >> 1;
+        if (!qless(d, b, sh.h_d[p], sh.h_b[p])) break;
+        sh.h_d[i] = sh.h_d[p];
+        sh.h_b[i] = sh.h_b[p];
+        sh.h_c[i] = sh.h_c[p];
+        i = p;
+    }
+    sh.h_d[i] = d;
+    sh.h_b[i] = b;
+    sh.h_c[i] = c;
+}
+
+__device__ __forceinline__ void heap_pop(CcShared& sh, int& n) {
+    const int m = --n;
+    const long long d = sh.h_d[m];
+    const int32_t b = sh.h_b[m], c = sh.h_c[m];
+    int i = 0;
+    while (true) {
+        int k = 2 * i + 1;
+        if (k >= m) break;
+        if (k + 1 < m && qless(sh.h_d[k + 1], sh.h_b[k + 1], sh.h_d[k], sh.h_b[k])) ++k;
+        if (!qless(sh.h_d[k], sh.h_b[k], d, b)) break;
+        sh.h_d[i] = sh.h_d[k];
+        sh.h_b[i] = sh.h_b[k];
+        sh.h_c[i] = sh.h_c[k];
+        i = k;
+    }
+    if (m > 0) {
+        sh.h_d[i] = d;
+        sh.h_b[i] = b;
+        sh.h_c[i] = c;
+    }
+}
+
+template <class Cells, bool kNP>
+__global__ void __launch_bounds__(kCcThreads, 1) k_carry_cluster(
+    DevGraph g, DevBM bm, DevChain ch, Cells cells, const uint64_t* __restrict__ pkeys,
+    const int32_t* __restrict__ pblk, int32_t nP, const int32_t* __restrict__ best, long long* r0_dS, int32_t* r0_blk,
+    long long* r1_dS, int32_t* r1_blk, int32_t* parent, long long num_to_merge, Readers rd, int32_t* out_merged,
+    DevFlags* flags) {
+    cg::cluster_group cluster = cg::this_cluster();
+    const int rank = (int)cluster.block_rank(), cs = (int)cluster.num_blocks();
+    const int W = kCcWarps * cs;
+    extern __shared__ __align__(16) unsigned char cc_raw[];
+    CcShared& sh = *reinterpret_cast<CcShared*>(cc_raw);
+    CcShared& ctl = *cluster.map_shared_rank(&sh, 0);  // CTA 0's queue and round results
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const bool controller = rank == 0;
+    if (controller && tid == 0) {
+        sh.p = sh.q = sh.nR = sh.rsel = sh.ns = sh.ssel = 0;
+        sh.merged = 0;
+        sh.rounds = 0;
+        sh.ne = kNP ? *bm.nonempty : 0;
+    }
+    const long long max_rounds = 64ll * (nP + 1) + 4096;
+    unsigned long long keys_seen = 0, evals = 0;
+    cluster.sync();
+    while (true) {
+        // ---- 1. CTA 0: stop test, the candidates and the bound
+        if (controller) {
+            if (tid == 0) {
+                sh.done = sh.merged >= num_to_merge;
+                if (!sh.done && sh.rounds >= max_rounds) {
+                    atomicOr(&flags->err, ERR_STATE);
+                    sh.done = 1;
+                }
+                *rd.used = 0;
+            }
+            __syncthreads();
+            if (!sh.done) {
+                const int p = sh.p, q = sh.q, nR = sh.nR, ns = sh.ns, ssel = sh.ssel;
+                const long long* rdS = sh.rsel ? r1_dS : r0_dS;
+                const int32_t* rb = sh.rsel ? r1_blk : r0_blk;
+                const int n0 = max(0, min(W + 1, nP - p)), n1 = max(0, min(W + 1, nR - q)), n2 = min(W + 1, ns);
+                for (int k = tid; k < n0; k += kCcThreads) {
+                    sh.hs_dS[0][k] = key_to_fixed(pkeys[p + k]);
+                    sh.hs_blk[0][k] = pblk[p + k];
+                }
+                for (int k = tid; k < n1; k += kCcThreads) {
+                    sh.hs_dS[1][k] = rdS[q + k];
+                    sh.hs_blk[1][k] = rb[q + k];
+                }
+                for (int k = tid; k < n2; k += kCcThreads) {
+                    sh.hs_dS[2][k] = sh.s_dS[ssel][k];
+                    sh.hs_blk[2][k] = sh.s_blk[ssel][k];
+                }
+                __syncthreads();
+                const int n[3] = {n0, n1, n2};
+                for (int e = tid; e < n0 + n1 + n2; e += kCcThreads) {
+                    const int src = e < n0 ? 0 : (e < n0 + n1 ? 1 : 2);
+                    const int k = e - (src == 0 ? 0 : (src == 1 ? n0 : n0 + n1));
+                    const long long d = sh.hs_dS[src][k];
+                    const int32_t b = sh.hs_blk[src][k];
+                    int r = k;
+                    for (int o = 0; o < 3; ++o)
+                        if (o != src) r += count_before(sh.hs_dS[o], sh.hs_blk[o], n[o], d, b);
+                    if (r < W) {
+                        sh.c_dS[r] = d;
+                        sh.c_blk[r] = b;
+                        sh.c_src[r] = src;
+                    } else if (r == W) {
+                        sh.b_dS = d;
+                        sh.b_blk = b;
+                    }
+                }
+                if (tid == 0) {
+                    const int tot = n0 + n1 + n2;
+                    sh.ncand = min(W, tot);
+                    sh.has_bound = tot > W;
+                    if (sh.ncand == 0) sh.done = 1;
+                }
+            }
+        }
+        cluster.sync();
+        if (ctl.done) break;
+        const int ncand = ctl.ncand;
+        // ---- 2. re-score this warp's candidate; register the blocks its value reads
+        for (int i = tid; i < kCcWarps * kCcWords; i += kCcThreads) (&sh.my_conf[0][0])[i] = 0u;
+        __syncthreads();
+        const int j = rank * kCcWarps + warp;
+        if (j < ncand) {
+            const int32_t from = ctl.c_blk[j];
+            int32_t to = 0;
+            bool ok = true;
+            if (lane == 0) {
+                const int32_t b = best[from];
+                to = (b < 0 || b >= bm.B) ? from : uf_find(parent, b);
+                ok = rd.add(from, j) && rd.add(to, j);
+            }
+            to = __shfl_sync(SBP_FULL_MASK, to, 0);
+            long long part = 0;
+            // nonparametric: zero when either block is empty (entropy.cpp:1203-1204)
+            const bool counted = !kNP || (to != from && bm.sizes[from] != 0 && bm.sizes[to] != 0);
+            if (to != from && counted) {
+                part = merge_delta_part<Cells, kNP>(g, bm, ch, cells, from, to, lane, 32, true,
+                                                    [&](int32_t x) { ok = rd.add(x, j) && ok; }, keys_seen);
+                if (lane == 0) ++evals;
+            }
+            ok = __all_sync(SBP_FULL_MASK, ok);
+            if (lane == 0) {
+                sh.my_to[warp] = to;
+                sh.my_act[warp] = part;
+                sh.my_count[warp] = kNP && counted;
+            }
+            // a full reader pool: every merge of the round counts as changing this value
+            if (!ok && lane < kCcWords) sh.my_conf[warp][lane] = ~0u;
+        }
+        cluster.sync();
+        // ---- 3. mark the readers of this candidate's two blocks
+        if (j < ncand && lane == 0) {
+            const int32_t a = ctl.c_blk[j], b = sh.my_to[warp];
+            for (int h = 0; h < 2; ++h) {
+                if (h == 1 && b == a) break;
+                int32_t k = ((volatile int32_t*)rd.head)[h == 0 ? a : b];
+                int guard = 0;
+                while (k >= 0 && k < rd.cap && guard++ < (1 << 22)) {
+                    const int32_t r = rd.node[3 * k + 1];
+                    if (r != j && r >= 0 && r < ncand) {
+                        uint32_t* c = cluster.map_shared_rank(&sh.my_conf[r % kCcWarps][j >> 5], r / kCcWarps);
+                        atomicOr(c, 1u << (j & 31));
+                    }
+                    k = rd.node[3 * k + 2];
+                }
+            }
+        }
+        cluster.sync();
+        // ---- 4. CTA 0: collect, replay the queue rule (block_merge.cpp:54-95), fold put-backs
+        if (controller) {
+            for (int k = tid; k < ncand; k += kCcThreads) {
+                const CcShared& o = *cluster.map_shared_rank(&sh, k / kCcWarps);
+                sh.c_to[k] = o.my_to[k % kCcWarps];
+                sh.c_act[k] = o.my_act[k % kCcWarps];
+                sh.c_count[k] = o.my_count[k % kCcWarps];
+            }
+            for (int e = tid; e < ncand * kCcWords; e += kCcThreads) {
+                const int k = e / kCcWords, w = e % kCcWords;
+                sh.conf[k][w] = cluster.map_shared_rank(&sh, k / kCcWarps)->my_conf[k % kCcWarps][w];
+            }
+            if (tid < kCcWords) sh.mm[tid] = 0u;
+            __syncthreads();
+            if (tid == 0) {
+                const bool hb = sh.has_bound;
+                const long long bnd_dS = sh.b_dS, merged0 = sh.merged;
+                const int32_t bnd_blk = sh.b_blk, ne0 = sh.ne;
+                int i = 0, nq = 0, nm = 0, cons[3] = {0, 0, 0};
+                auto stale = [&](int ci) {
+                    uint32_t x = 0;
+                    for (int w = 0; w < kCcWords; ++w) x |= sh.conf[ci][w] & sh.mm[w];
+                    return x != 0u;
+                };
+                while (merged0 + nm < num_to_merge) {
+                    const bool hc = i < ncand, hq = nq > 0;
+                    if (!hc && !hq) break;  // queue empty
+                    const bool fromq = hq && (!hc || qless(sh.h_d[0], sh.h_b[0], sh.c_dS[i], sh.c_blk[i]));
+                    const long long kd = fromq ? sh.h_d[0] : sh.c_dS[i];
+                    const int32_t kb = fromq ? sh.h_b[0] : sh.c_blk[i];
+                    if (hb && qless(bnd_dS, bnd_blk, kd, kb)) break;  // next pop not evaluated
+                    int ci;
+                    if (fromq) {
+                        // popped again: unless a merge since touched what it read, its value is
+                        // the one it was put back with (kNP: up to the count term)
+                        ci = sh.h_c[0];
+                        if (stale(ci)) break;
+                        heap_pop(sh, nq);
+                    } else {
+                        if (stale(i)) break;  // its value is stale: re-score it next round
+                        ci = i++;
+                        cons[sh.c_src[ci]]++;
+                        if (sh.c_to[ci] == kb) continue;  // already in the same block
+                    }
+                    const int32_t from = kb, to = sh.c_to[ci];
+                    long long act = sh.c_act[ci];
+                    if (kNP && sh.c_count[ci]) act += __ldg(g.Dm + min(max(ne0 - nm, 0), g.N + 1));
+                    const bool hc2 = i < ncand, hq2 = nq > 0;
+                    if (hc2 || hq2 || hb) {
+                        long long top = hb ? bnd_dS : LLONG_MAX;
+                        if (hc2) top = min(top, sh.c_dS[i]);
+                        if (hq2) top = min(top, sh.h_d[0]);
+                        if (act > top) {  // put back with the recomputed delta
+                            heap_push(sh, nq, act, from, ci);
+                            continue;
+                        }
+                    }
+                    sh.m_from[nm] = from;
+                    sh.m_to[nm] = to;
+                    sh.mm[ci >> 5] |= 1u << (ci & 31);
+                    ++nm;
+                }
+                int k = 0;
+                while (nq > 0) {
+                    sh.q_dS[k] = sh.h_d[0];
+                    sh.q_blk[k] = sh.h_b[0];
+                    ++k;
+                    heap_pop(sh, nq);
+                }
+                sh.nq = k;
+                sh.p += cons[0];
+                sh.q += cons[1];
+                sh.cS = cons[2];
+                sh.nm = nm;
+                sh.merged += nm;
+                sh.ne -= nm;  // every merge lowers the count (blockmodel.cpp:356)
+                sh.rounds += 1;
+            }
+            __syncthreads();
+            // S := S[cS..ns) merged with the round's put-backs
+            {
+                const int cS = sh.cS, nq = sh.nq, ns = sh.ns, ssel = sh.ssel;
+                if (cS > 0 || nq > 0) {
+                    const int rest = ns - cS;
+                    const long long* sd = sh.s_dS[ssel] + cS;
+                    const int32_t* sb = sh.s_blk[ssel] + cS;
+                    long long* od = sh.s_dS[ssel ^ 1];
+                    int32_t* ob = sh.s_blk[ssel ^ 1];
+                    for (int i = tid; i < rest; i += kCcThreads) {
+                        const int pos = i + count_before(sh.q_dS, sh.q_blk, nq, sd[i], sb[i]);
+                        od[pos] = sd[i];
+                        ob[pos] = sb[i];
+                    }
+                    for (int k = tid; k < nq; k += kCcThreads) {
+                        const int pos = k + count_before(sd, sb, rest, sh.q_dS[k], sh.q_blk[k]);
+                        od[pos] = sh.q_dS[k];
+                        ob[pos] = sh.q_blk[k];
+                    }
+                    __syncthreads();
+                    if (tid == 0) {
+                        sh.ns = rest + nq;
+                        sh.ssel = ssel ^ 1;
+                    }
+                    __syncthreads();
+                }
+            }
+            // spill S into the global run when it could not take another round's put-backs
+            if (sh.ns > kCcQS - kCcMaxW - 1) {
+                const int ns = sh.ns, ssel = sh.ssel, q = sh.q, nr = sh.nR - sh.q;
+                const long long* rdS = (sh.rsel ? r1_dS : r0_dS) + q;
+                const int32_t* rb = (sh.rsel ? r1_blk : r0_blk) + q;
+                long long* od = sh.rsel ? r0_dS : r1_dS;
+                int32_t* ob = sh.rsel ? r0_blk : r1_blk;
+                const long long* sd = sh.s_dS[ssel];
+                const int32_t* sb = sh.s_blk[ssel];
+                for (int i = tid; i < nr; i += kCcThreads) {
+                    const int pos = i + count_before(sd, sb, ns, rdS[i], rb[i]);
+                    od[pos] = rdS[i];
+                    ob[pos] = rb[i];
+                }
+                for (int k = tid; k < ns; k += kCcThreads) {
+                    int lo = 0, hi = nr;
+                    while (lo < hi) {
+                        const int mid = (lo + hi) >> 1;
+                        if (qless(rdS[mid], rb[mid], sd[k], sb[k])) lo = mid + 1;
+                        else hi = mid;
+                    }
+                    od[k + lo] = sd[k];
+                    ob[k + lo] = sb[k];
+                }
+                __syncthreads();
+                if (tid == 0) {
+                    sh.nR = nr + ns;
+                    sh.q = 0;
+                    sh.rsel ^= 1;
+                    sh.ns = 0;
+                }
+                __syncthreads();
+            }
+        }
+        cluster.sync();
+        // ---- 5. Blockmodel::merge_block (blockmodel.cpp:337-363) for the round's merges:
+        // merge k goes to CTA k % cs; a CTA's merges share its warps (row walk and column
+        // walk on separate warps when there are few)
+        {
+            const int nm = ctl.nm;
+            const int mine = nm > rank ? (nm - rank + cs - 1) / cs : 0;
+            for (int base = 0; base < mine; base += kCcWarps / 2) {
+                const int here = min(kCcWarps / 2, mine - base);
+                const int wpm = here == 1 ? 16 : here == 2 ? 8 : here <= 4 ? 4 : 2;
+                const int slot = warp / wpm;
+                if (slot < here) {
+                    const int k = rank + cs * (base + slot);
+                    const int32_t mf = ctl.m_from[k], mt = ctl.m_to[k];
+                    const int half = (warp % wpm) >= wpm / 2;
+                    const int nth = 32 * wpm / 2, ht = tid - (slot * wpm + half * wpm / 2) * 32;
+                    if (half == 0) {
+                        list_for_each(bm.row_col, bm.row_off[mf], bm.row_off[mf + 1], ch.row_head[mf], ch, ht, nth,
+                                      [&](int32_t c) {
+                                          const int32_t m = cells.take(mf, c, flags);
+                                          if (m == 0) return;
+                                          const int32_t c2 = (c == mf || c == mt) ? mt : c;
+                                          if (cells.add(mt, c2, m, flags)) {
+                                              list_push1_shared(ch.row_head, ch, mt, c2, flags);
+                                              list_push1_shared(ch.col_head, ch, c2, mt, flags);
+                                          }
+                                      });
+                    } else {
+                        list_for_each(bm.col_row, bm.col_off[mf], bm.col_off[mf + 1], ch.col_head[mf], ch, ht, nth,
+                                      [&](int32_t x) {
+                                          if (x == mf) return;
+                                          const int32_t m = cells.take(x, mf, flags);
+                                          if (m == 0) return;
+                                          const int32_t x2 = x == mt ? mt : x;
+                                          if (cells.add(x2, mt, m, flags)) {
+                                              list_push1_shared(ch.col_head, ch, mt, x2, flags);
+                                              list_push1_shared(ch.row_head, ch, x2, mt, flags);
+                                          }
+                                      });
+                    }
+                }
+                __syncthreads();
+                if (tid < here) {
+                    const int k = rank + cs * (base + tid);
+                    const int32_t mf = ctl.m_from[k], mt = ctl.m_to[k];
+                    bm.d_out[mt] += bm.d_out[mf];
+                    bm.d_in[mt] += bm.d_in[mf];
+                    bm.d_out[mf] = 0;
+                    bm.d_in[mf] = 0;
+                    bm.d_tot[mf] = 0;
+                    bm.d_tot[mt] = bm.d_out[mt] + bm.d_in[mt] - cells.get(mt, mt);
+                    bm.sizes[mt] += bm.sizes[mf];
+                    bm.sizes[mf] = 0;
+                    parent[mf] = mt;
+                }
+                __syncthreads();
+            }
+            // clear the round's reader lists
+            const int32_t used = min(*(volatile int32_t*)rd.used, rd.cap);
+            for (int32_t k = rank * kCcThreads + tid; k < used; k += cs * kCcThreads) rd.head[rd.node[3 * k]] = -1;
+        }
+        cluster.sync();
+    }
+    keys_seen = warp_sum_ll((long long)keys_seen);
+    evals = warp_sum_ll((long long)evals);
+    if (lane == 0) {
+        atomicAdd(&flags->counters[9], keys_seen);
+        atomicAdd(&flags->counters[10], evals);
+    }
+    if (controller && tid == 0) {
+        *out_merged = (int32_t)sh.merged;
+        atomicAdd(&flags->counters[0], (unsigned long long)sh.rounds);
+    }
+}
+
+// Largest cluster (16, else 8, else 4) the device holds for this kernel.
+template <class K>
+int carry_cluster_pick(K kernel) {
+    static int cached = -1;
+    if (cached >= 0) return cached;
+    const int smem = (int)sizeof(CcShared);
+    cudaFuncSetAttribute((const void*)kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    cudaFuncSetAttribute((const void*)kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    for (int cs = kCcMaxCluster; cs >= 4; cs /= 2) {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(cs);
+        cfg.blockDim = dim3(kCcThreads);
+        cfg.dynamicSmemBytes = smem;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = cs;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        int nc = 0;
+        if (cudaOccupancyMaxActiveClusters(&nc, (const void*)kernel, &cfg) == cudaSuccess && nc >= 1) {
+            cached = cs;
+            return cs;
+        }
+        cudaGetLastError();
+    }
+    cached = 0;
+    return 0;
+}
+
+template <class Cells, bool kNP>
+void launch_carry_cluster(const DevGraph& g, DevBM& bm, const Cells& cells, int64_t num_to_merge, int cs,
+                          int32_t* d_merged, Work& w, cudaStream_t st) {
+    auto kernel = k_carry_cluster<Cells, kNP>;
+    const int smem = (int)sizeof(CcShared);
+    cudaFuncSetAttribute((const void*)kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    cudaFuncSetAttribute((const void*)kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(cs);
+    cfg.blockDim = dim3(kCcThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = cs;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    Readers rd{w.cc_head, w.cc_nodes, w.cc_node_cap, w.cc_used};
+    const cudaError_t e = cudaLaunchKernelEx(
+        &cfg, kernel, g, bm, w.chain, cells, (const uint64_t*)w.keys, (const int32_t*)w.vals, bm.B,
+        (const int32_t*)w.best, reinterpret_cast<long long*>(w.heap_dS), w.heap_blk,
+        reinterpret_cast<long long*>(w.keys_alt), w.vals_alt, w.parent, (long long)num_to_merge, rd, d_merged,
+        w.flags_dev);
+    if (e != cudaSuccess) throw std::runtime_error(std::string("cluster carry-out launch: ") + cudaGetErrorString(e));
+}
+
+__global__ void k_cc_dense_fill(DevBM bm, int32_t* M) {
+    const int64_t B = bm.B;
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < bm.nnz; j += (int64_t)gridDim.x * blockDim.x)
+        M[bm.row_of[j] * B + bm.row_col[j]] = bm.row_cnt[j];
+}
+
+}  // namespace
+
+int carry_cluster_size() { return carry_cluster_pick(k_carry_cluster<HashCells, false>); }
+
+void carry_out_cluster(const DevGraph& g, DevBM& bm, int64_t num_to_merge, Work& w, cudaStream_t st, bool np) {
+    if (np && (!g.LG || !g.Dm || !g.Dp)) throw std::logic_error("nonparametric tables missing");
+    const int cs = carry_cluster_size();
+    if (cs <= 0 || !w.cc_head || !w.cc_nodes) throw std::logic_error("cluster carry-out buffers missing");
+    const int32_t B = bm.B;
+    const bool dense = w.cells && (uint64_t)B * (uint64_t)B <= w.cells_elems;
+    int32_t* d_merged = w.d_scalar + 1;
+    cudaMemsetAsync(w.cc_head, 0xff, sizeof(int32_t) * (size_t)B, st);
+    if (dense) {
+        lists_init(bm, w, st);
+        cudaMemsetAsync(w.cells, 0, sizeof(int32_t) * (size_t)B * (size_t)B, st);
+        const int64_t blocks = std::min<int64_t>((bm.nnz + 255) / 256 + 1, (int64_t)device_sms() * 16);
+        k_cc_dense_fill<<<(unsigned)blocks, 256, 0, st>>>(bm, w.cells);
+        const DenseCells dc{w.cells, (int64_t)B};
+        if (np) launch_carry_cluster<DenseCells, true>(g, bm, dc, num_to_merge, cs, d_merged, w, st);
+        else launch_carry_cluster<DenseCells, false>(g, bm, dc, num_to_merge, cs, d_merged, w, st);
+        count_launches(2);
+    } else {
+        chain_init(bm, w, (uint64_t)2 * (uint64_t)bm.nnz, st);
+        const HashCells hc{w.chain};
+        if (np) launch_carry_cluster<HashCells, true>(g, bm, hc, num_to_merge, cs, d_merged, w, st);
+        else launch_carry_cluster<HashCells, false>(g, bm, hc, num_to_merge, cs, d_merged, w, st);
+        count_launches(1);
+    }
+}
+
+}  // namespace sbp

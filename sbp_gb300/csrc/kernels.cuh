@@ -60,6 +60,11 @@ struct Work {
     // the cluster chain's per-warp neighbour hashes and row scratch (allocated on first use)
     int32_t* cl_hash = nullptr;
     int32_t* cl_scratch = nullptr;
+    // the cluster carry-out's per-block reader lists (allocated on first use)
+    int32_t* cc_head = nullptr;        // [N]
+    int32_t* cc_nodes = nullptr;       // [3 * cc_node_cap]
+    int32_t cc_node_cap = 0;
+    int32_t* cc_used = nullptr;        // device counter
     // dense B x B cell values of the merge carry-out (allocated on demand within a budget)
     int32_t* cells = nullptr;
     uint64_t cells_elems = 0;
@@ -139,14 +144,19 @@ void merge_propose(const DevGraph& g, const DevBM& bm, uint64_t seed, uint32_t s
                    bool np = false);
 // Carries out merges; writes the number done to w.d_scalar[1].  Leaves asg relabelled
 // to dense block ids (B - merges blocks); the caller rebuilds.
+// cluster: the exact carry-out on a thread-block cluster (carry_cluster.cu).
 void carry_out(const DevGraph& g, DevBM& bm, int64_t num_to_merge, int approximate, Work& w, cudaStream_t st,
-               bool np = false);
+               bool np = false, bool cluster = false);
 
 // ---- carry.cu
 // carry_out_best_merges_advanced over the queue (w.keys, w.vals) sorted by (delta, block)
 // with the union-find block map in w.parent (identity on entry).  Uses the dense cells
 // w.cells when B * B <= w.cells_elems, the chain hash otherwise.
 void carry_out_exact(const DevGraph& g, DevBM& bm, int64_t num_to_merge, Work& w, cudaStream_t st, bool np = false);
+// The same on a thread-block cluster of carry_cluster_size() CTAs (0: the device holds
+// none); needs w.cc_head / w.cc_nodes / w.cc_used.
+int carry_cluster_size();
+void carry_out_cluster(const DevGraph& g, DevBM& bm, int64_t num_to_merge, Work& w, cudaStream_t st, bool np);
 
 // Blocks the calling thread, sleeping rather than spinning, until the work queued on st so
 // far is done (many host threads may each drive a context of their own).

@@ -141,7 +141,7 @@ void merge_propose(const DevGraph& g, const DevBM& bm, uint64_t seed, uint32_t s
 }
 
 void carry_out(const DevGraph& g, DevBM& bm, int64_t num_to_merge, int approximate, Work& w, cudaStream_t st,
-               bool np) {
+               bool np, bool cluster) {
     const int32_t B = bm.B;
     // queue order: stable sort of (delta, block)
     k_merge_keys<<<grid_cap(B, 256, device_sms() * 16), 256, 0, st>>>(w.best_dS, B, w.keys, w.vals);
@@ -151,6 +151,8 @@ void carry_out(const DevGraph& g, DevBM& bm, int64_t num_to_merge, int approxima
     int32_t* d_merged = w.d_scalar + 1;
     if (approximate) {
         k_carry_approx<<<1, 32, 0, st>>>(w.vals, B, w.best, w.parent, num_to_merge, d_merged);
+    } else if (cluster) {
+        carry_out_cluster(g, bm, num_to_merge, w, st, np);
     } else {
         carry_out_exact(g, bm, num_to_merge, w, st, np);
     }
