@@ -507,6 +507,7 @@ bool ensure_cluster_carry(sbpgpu_graph* g) {
         w.cc_head = dalloc<int32_t>(g->owned, g->N);
         w.cc_nodes = dalloc<int32_t>(g->owned, 3 * (size_t)w.cc_node_cap);
         w.cc_used = dalloc<int32_t>(g->owned, 1);
+        w.cc_stage = dalloc<int32_t>(g->owned, carry_cluster_stage_ints(carry_cluster_size()));
     }
     return true;
 }

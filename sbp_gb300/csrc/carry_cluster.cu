@@ -41,6 +41,7 @@ constexpr int kCcMaxCluster = 16;
 constexpr int kCcMaxW = kCcWarps * kCcMaxCluster;  // candidates per round
 constexpr int kCcWords = kCcMaxW / 32;              // words of a conflict mask
 constexpr int kCcQS = 4096;                         // CTA 0's sorted put-back buffer
+constexpr int kCcStage = 1 << 15;                   // staged new keys per merge and list
 
 // Shared memory of every CTA (dynamic); the queue parts are used by CTA 0 only.
 struct CcShared {
@@ -66,6 +67,9 @@ struct CcShared {
     long long my_act[kCcWarps];
     int32_t my_count[kCcWarps];
     uint32_t my_conf[kCcWarps][kCcWords];
+    // new keys of the row / column of each merge's target, staged, then appended in bulk
+    int32_t st_n[kCcWarps / 2][2];
+    int32_t st_slot[kCcWarps / 2][2];
     long long b_dS, merged, rounds;
     int32_t b_blk;
     int32_t p, q, nR, rsel, ns, ssel, ne;
@@ -400,19 +404,32 @@ __global__ void __launch_bounds__(kCcThreads, 1) k_carry_cluster(
         cluster.sync();
         // ---- 5. Blockmodel::merge_block (blockmodel.cpp:337-363) for the round's merges:
         // merge k goes to CTA k % cs; a CTA's merges share its warps (row walk and column
-        // walk on separate warps when there are few)
+        // walk on separate warps when there are few).  The target's own row and column
+        // receive their new keys through a staging slice and one bulk append; the lists of
+        // third blocks, which several merges may extend at once, take single keys.
         {
             const int nm = ctl.nm;
             const int mine = nm > rank ? (nm - rank + cs - 1) / cs : 0;
+            int32_t* my_stage = stage_buf + (int64_t)rank * (kCcWarps / 2) * 2 * kCcStage;
             for (int base = 0; base < mine; base += kCcWarps / 2) {
                 const int here = min(kCcWarps / 2, mine - base);
                 const int wpm = here == 1 ? 16 : here == 2 ? 8 : here <= 4 ? 4 : 2;
                 const int slot = warp / wpm;
+                if (tid < kCcWarps) (&sh.st_n[0][0])[tid] = 0;
+                __syncthreads();
                 if (slot < here) {
                     const int k = rank + cs * (base + slot);
                     const int32_t mf = ctl.m_from[k], mt = ctl.m_to[k];
                     const int half = (warp % wpm) >= wpm / 2;
                     const int nth = 32 * wpm / 2, ht = tid - (slot * wpm + half * wpm / 2) * 32;
+                    int32_t* srow = my_stage + (int64_t)(2 * slot) * kCcStage;
+                    int32_t* scol = srow + kCcStage;
+                    // a new key of the target's row (which 0) or column (which 1)
+                    auto stage_key = [&](int which, int32_t key) {
+                        const int p = atomicAdd(&sh.st_n[slot][which], 1);
+                        if (p < kCcStage) (which ? scol : srow)[p] = key;
+                        else list_push1_shared(which ? ch.col_head : ch.row_head, ch, mt, key, flags);
+                    };
                     if (half == 0) {
                         list_for_each(bm.row_col, bm.row_off[mf], bm.row_off[mf + 1], ch.row_head[mf], ch, ht, nth,
                                       [&](int32_t c) {
@@ -420,8 +437,9 @@ __global__ void __launch_bounds__(kCcThreads, 1) k_carry_cluster(
                                           if (m == 0) return;
                                           const int32_t c2 = (c == mf || c == mt) ? mt : c;
                                           if (cells.add(mt, c2, m, flags)) {
-                                              list_push1_shared(ch.row_head, ch, mt, c2, flags);
-                                              list_push1_shared(ch.col_head, ch, c2, mt, flags);
+                                              stage_key(0, c2);
+                                              if (c2 == mt) stage_key(1, mt);
+                                              else list_push1_shared(ch.col_head, ch, c2, mt, flags);
                                           }
                                       });
                     } else {
@@ -432,13 +450,29 @@ __global__ void __launch_bounds__(kCcThreads, 1) k_carry_cluster(
                                           if (m == 0) return;
                                           const int32_t x2 = x == mt ? mt : x;
                                           if (cells.add(x2, mt, m, flags)) {
-                                              list_push1_shared(ch.col_head, ch, mt, x2, flags);
-                                              list_push1_shared(ch.row_head, ch, x2, mt, flags);
+                                              stage_key(1, x2);
+                                              if (x2 == mt) stage_key(0, mt);
+                                              else list_push1_shared(ch.row_head, ch, x2, mt, flags);
                                           }
                                       });
                     }
                 }
                 __syncthreads();
+                if (tid < 2 * here) {
+                    const int sl = tid >> 1, which = tid & 1;
+                    const int32_t mt = ctl.m_to[rank + cs * (base + sl)];
+                    const int n = min(sh.st_n[sl][which], kCcStage);
+                    sh.st_slot[sl][which] = n > 0 ? list_reserve(which ? ch.col_head : ch.row_head, ch, mt, n, flags) : -1;
+                }
+                __syncthreads();
+                for (int sl = 0; sl < here; ++sl)
+                    for (int which = 0; which < 2; ++which) {
+                        const int n = min(sh.st_n[sl][which], kCcStage);
+                        const int32_t at = sh.st_slot[sl][which];
+                        const int32_t* src = my_stage + (int64_t)(2 * sl + which) * kCcStage;
+                        if (at >= 0)
+                            for (int i = tid; i < n; i += kCcThreads) ch.pool[at + i] = src[i];
+                    }
                 if (tid < here) {
                     const int k = rank + cs * (base + tid);
                     const int32_t mf = ctl.m_from[k], mt = ctl.m_to[k];
@@ -526,8 +560,8 @@ void launch_carry_cluster(const DevGraph& g, DevBM& bm, const Cells& cells, int6
     const cudaError_t e = cudaLaunchKernelEx(
         &cfg, kernel, g, bm, w.chain, cells, (const uint64_t*)w.keys, (const int32_t*)w.vals, bm.B,
         (const int32_t*)w.best, reinterpret_cast<long long*>(w.heap_dS), w.heap_blk,
-        reinterpret_cast<long long*>(w.keys_alt), w.vals_alt, w.parent, (long long)num_to_merge, rd, d_merged,
-        w.flags_dev);
+        reinterpret_cast<long long*>(w.keys_alt), w.vals_alt, w.parent, (long long)num_to_merge, rd, w.cc_stage,
+        d_merged, w.flags_dev);
     if (e != cudaSuccess) throw std::runtime_error(std::string("cluster carry-out launch: ") + cudaGetErrorString(e));
 }
 
@@ -541,10 +575,13 @@ __global__ void k_cc_dense_fill(DevBM bm, int32_t* M) {
 
 int carry_cluster_size() { return carry_cluster_pick(k_carry_cluster<HashCells, false>); }
 
+size_t carry_cluster_stage_ints(int cs) { return (size_t)cs * (kCcWarps / 2) * 2 * kCcStage; }
+
 void carry_out_cluster(const DevGraph& g, DevBM& bm, int64_t num_to_merge, Work& w, cudaStream_t st, bool np) {
     if (np && (!g.LG || !g.Dm || !g.Dp)) throw std::logic_error("nonparametric tables missing");
     const int cs = carry_cluster_size();
-    if (cs <= 0 || !w.cc_head || !w.cc_nodes) throw std::logic_error("cluster carry-out buffers missing");
+    if (cs <= 0 || !w.cc_head || !w.cc_nodes || !w.cc_stage)
+        throw std::logic_error("cluster carry-out buffers missing");
     const int32_t B = bm.B;
     const bool dense = w.cells && (uint64_t)B * (uint64_t)B <= w.cells_elems;
     int32_t* d_merged = w.d_scalar + 1;

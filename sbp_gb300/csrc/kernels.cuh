@@ -65,6 +65,7 @@ struct Work {
     int32_t* cc_nodes = nullptr;       // [3 * cc_node_cap]
     int32_t cc_node_cap = 0;
     int32_t* cc_used = nullptr;        // device counter
+    int32_t* cc_stage = nullptr;       // staged new keys of the merges' targets
     // dense B x B cell values of the merge carry-out (allocated on demand within a budget)
     int32_t* cells = nullptr;
     uint64_t cells_elems = 0;
@@ -156,6 +157,7 @@ void carry_out_exact(const DevGraph& g, DevBM& bm, int64_t num_to_merge, Work& w
 // The same on a thread-block cluster of carry_cluster_size() CTAs (0: the device holds
 // none); needs w.cc_head / w.cc_nodes / w.cc_used.
 int carry_cluster_size();
+size_t carry_cluster_stage_ints(int cs);
 void carry_out_cluster(const DevGraph& g, DevBM& bm, int64_t num_to_merge, Work& w, cudaStream_t st, bool np);
 
 // Blocks the calling thread, sleeping rather than spinning, until the work queued on st so
