@@ -133,8 +133,8 @@ template <class Cells, bool kNP>
 __global__ void __launch_bounds__(kCcThreads, 1) k_carry_cluster(
     DevGraph g, DevBM bm, DevChain ch, Cells cells, const uint64_t* __restrict__ pkeys,
     const int32_t* __restrict__ pblk, int32_t nP, const int32_t* __restrict__ best, long long* r0_dS, int32_t* r0_blk,
-    long long* r1_dS, int32_t* r1_blk, int32_t* parent, long long num_to_merge, Readers rd, int32_t* out_merged,
-    DevFlags* flags) {
+    long long* r1_dS, int32_t* r1_blk, int32_t* parent, long long num_to_merge, Readers rd, int32_t* stage_buf,
+    int32_t* out_merged, DevFlags* flags) {
     cg::cluster_group cluster = cg::this_cluster();
     const int rank = (int)cluster.block_rank(), cs = (int)cluster.num_blocks();
     const int W = kCcWarps * cs;
