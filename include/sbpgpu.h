@@ -84,7 +84,7 @@ void* sbpgpu_ctx_stream(sbpgpu_ctx* ctx);
 sbpgpu_status sbpgpu_ctx_set_cells_budget(sbpgpu_ctx* ctx, int64_t bytes);
 /* Smallest block count at which the sequential phases -- the Metropolis-Hastings chain and
  * the exact merge carry-out -- are evaluated in wide windows spread over a thread-block
- * cluster instead of one CTA (default 8192; 0: always, for the chain once the blockmodel
+ * cluster instead of one CTA (default 65536; 0: always, for the chain once the blockmodel
  * has more than 128 blocks).  Results do not depend on it.  No counterpart in the
  * reference. */
 sbpgpu_status sbpgpu_ctx_set_cluster_blocks(sbpgpu_ctx* ctx, int64_t min_blocks);

@@ -13,11 +13,11 @@
 //   2. each warp re-scores one candidate and registers, in a per-block reader list, every
 //      block its value depends on (its two blocks and the third blocks of its row and
 //      column);
-//   3. each warp walks the reader lists of its candidate's two blocks and marks, in the
-//      readers' conflict masks, that a merge of this candidate changes their values;
-//   4. CTA 0 collects the values and masks and replays the rule on one thread (a pop of a
-//      candidate or put-back entry whose mask meets a merge of the round ends the round),
-//      then folds the round's put-backs into its buffer;
+//   3. each warp walks the reader lists of its candidate's two blocks: the readers are the
+//      candidates a merge of this one would change;
+//   4. CTA 0 collects the values and those sets and replays the rule on one thread (a merge
+//      marks the candidates it changes; popping a marked candidate or put-back entry ends
+//      the round), then folds the round's put-backs into its buffer;
 //   5. the round's merges (disjoint rows, columns and targets, by the conflict rule) are
 //      applied by all CTAs at once, and the reader lists are cleared.
 // Merges, their order and every put-back delta equal those of the one-at-a-time loop; ties
@@ -55,18 +55,20 @@ struct CcShared {
     int32_t c_to[kCcMaxW];
     long long c_act[kCcMaxW];
     int32_t c_count[kCcMaxW];
-    uint32_t conf[kCcMaxW][kCcWords];  // bit i of conf[j]: a merge of candidate i changes j's value
+    uint32_t inv[kCcMaxW][kCcWords];  // bit j of inv[i]: a merge of candidate i changes j's value
+    int32_t fragile[kCcMaxW];         // its readers are not all listed: any merge changes it
     int32_t m_from[kCcMaxW], m_to[kCcMaxW];
     long long h_d[kCcMaxW];  // replay's put-back heap
     int32_t h_b[kCcMaxW], h_c[kCcMaxW];
     long long q_dS[kCcMaxW];  // the round's remaining put-backs, sorted
     int32_t q_blk[kCcMaxW];
-    uint32_t mm[kCcWords];  // candidates merged in the round
+    uint32_t smask[kCcWords];  // candidates whose value a merge of the round has changed
     // this CTA's own candidates
     int32_t my_to[kCcWarps];
     long long my_act[kCcWarps];
     int32_t my_count[kCcWarps];
-    uint32_t my_conf[kCcWarps][kCcWords];
+    uint32_t my_inv[kCcWarps][kCcWords];
+    int32_t my_fragile[kCcWarps];
     // new keys of the row / column of each merge's target, staged, then appended in bulk
     int32_t st_n[kCcWarps / 2][2];
     int32_t st_slot[kCcWarps / 2][2];
@@ -212,7 +214,7 @@ __global__ void __launch_bounds__(kCcThreads, 1) k_carry_cluster(
         if (ctl.done) break;
         const int ncand = ctl.ncand;
         // ---- 2. re-score this warp's candidate; register the blocks its value reads
-        for (int i = tid; i < kCcWarps * kCcWords; i += kCcThreads) (&sh.my_conf[0][0])[i] = 0u;
+        for (int i = tid; i < kCcWarps * kCcWords; i += kCcThreads) (&sh.my_inv[0][0])[i] = 0u;
         __syncthreads();
         const int j = rank * kCcWarps + warp;
         if (j < ncand) {
@@ -240,10 +242,10 @@ __global__ void __launch_bounds__(kCcThreads, 1) k_carry_cluster(
                 sh.my_count[warp] = kNP && counted;
             }
             // a full reader pool: every merge of the round counts as changing this value
-            if (!ok && lane < kCcWords) sh.my_conf[warp][lane] = ~0u;
+            if (lane == 0) sh.my_fragile[warp] = !ok;
         }
         cluster.sync();
-        // ---- 3. mark the readers of this candidate's two blocks
+        // ---- 3. the candidates a merge of this one would change: the readers of its blocks
         if (j < ncand && lane == 0) {
             const int32_t a = ctl.c_blk[j], b = sh.my_to[warp];
             for (int h = 0; h < 2; ++h) {
@@ -252,10 +254,7 @@ __global__ void __launch_bounds__(kCcThreads, 1) k_carry_cluster(
                 int guard = 0;
                 while (k >= 0 && k < rd.cap && guard++ < (1 << 22)) {
                     const int32_t r = rd.node[3 * k + 1];
-                    if (r != j && r >= 0 && r < ncand) {
-                        uint32_t* c = cluster.map_shared_rank(&sh.my_conf[r % kCcWarps][j >> 5], r / kCcWarps);
-                        atomicOr(c, 1u << (j & 31));
-                    }
+                    if (r != j && r >= 0 && r < ncand) sh.my_inv[warp][r >> 5] |= 1u << (r & 31);
                     k = rd.node[3 * k + 2];
                 }
             }
@@ -271,9 +270,11 @@ __global__ void __launch_bounds__(kCcThreads, 1) k_carry_cluster(
             }
             for (int e = tid; e < ncand * kCcWords; e += kCcThreads) {
                 const int k = e / kCcWords, w = e % kCcWords;
-                sh.conf[k][w] = cluster.map_shared_rank(&sh, k / kCcWarps)->my_conf[k % kCcWarps][w];
+                sh.inv[k][w] = cluster.map_shared_rank(&sh, k / kCcWarps)->my_inv[k % kCcWarps][w];
             }
-            if (tid < kCcWords) sh.mm[tid] = 0u;
+            for (int k = tid; k < ncand; k += kCcThreads)
+                sh.fragile[k] = cluster.map_shared_rank(&sh, k / kCcWarps)->my_fragile[k % kCcWarps];
+            if (tid < kCcWords) sh.smask[tid] = 0u;
             __syncthreads();
             if (tid == 0) {
                 const bool hb = sh.has_bound;
@@ -281,9 +282,7 @@ __global__ void __launch_bounds__(kCcThreads, 1) k_carry_cluster(
                 const int32_t bnd_blk = sh.b_blk, ne0 = sh.ne;
                 int i = 0, nq = 0, nm = 0, cons[3] = {0, 0, 0};
                 auto stale = [&](int ci) {
-                    uint32_t x = 0;
-                    for (int w = 0; w < kCcWords; ++w) x |= sh.conf[ci][w] & sh.mm[w];
-                    return x != 0u;
+                    return ((sh.smask[ci >> 5] >> (ci & 31)) & 1u) || (nm > 0 && sh.fragile[ci]);
                 };
                 while (merged0 + nm < num_to_merge) {
                     const bool hc = i < ncand, hq = nq > 0;
@@ -320,7 +319,7 @@ __global__ void __launch_bounds__(kCcThreads, 1) k_carry_cluster(
                     }
                     sh.m_from[nm] = from;
                     sh.m_to[nm] = to;
-                    sh.mm[ci >> 5] |= 1u << (ci & 31);
+                    for (int w = 0; w < kCcWords; ++w) sh.smask[w] |= sh.inv[ci][w];
                     ++nm;
                 }
                 int k = 0;

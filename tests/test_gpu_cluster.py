@@ -20,7 +20,7 @@ def cluster_ctx(gpu):
     ctx = gpu.core.default_context()
     ctx.set_cluster_blocks(0)
     yield ctx
-    ctx.set_cluster_blocks(8192)
+    ctx.set_cluster_blocks(65536)
     ctx.set_cells_budget(16 << 30)
 
 
