@@ -497,16 +497,14 @@ bool ensure_cluster(sbpgpu_graph* g) {
     return true;
 }
 
-// The cluster carry-out's reader lists, allocated on first use.  False when the device
+// The cluster carry-out's per-block candidate array and staging buffer, allocated on first
+// use.  False when the device
 // holds no cluster.
 bool ensure_cluster_carry(sbpgpu_graph* g) {
     if (carry_cluster_size() <= 0) return false;
     Work& w = g->w;
     if (!w.cc_head) {
-        w.cc_node_cap = (int32_t)std::min<int64_t>(std::max<int64_t>(2 * g->E, 1 << 20), int64_t(1) << 24);
         w.cc_head = dalloc<int32_t>(g->owned, g->N);
-        w.cc_nodes = dalloc<int32_t>(g->owned, 3 * (size_t)w.cc_node_cap);
-        w.cc_used = dalloc<int32_t>(g->owned, 1);
         w.cc_stage = dalloc<int32_t>(g->owned, carry_cluster_stage_ints(carry_cluster_size()));
     }
     return true;
@@ -518,9 +516,11 @@ void chain_run(sbpgpu_bm* bm, const int32_t* order, int32_t n, int32_t max_k, in
     if (mode == ACC_NP) ensure_np(g);
     const int64_t B = bm->d.B;
     if (B > kWinSharedMax) ensure_cells(g, mh_window_cells((int32_t)B));
-    // Many blocks: the window spread over a thread-block cluster, cells dense when the
-    // budget holds them, else hashed.
-    if (B >= g->ctx->cluster_blocks && B > kWinSharedMax && max_k <= 4096 && ensure_cluster(g)) {
+    WindowPlan plan{};
+    const bool window = mh_window_plan(bm->d.B, max_k, g->w, &plan);
+    // Many blocks, or a blockmodel whose dense cells exceed the budget: the window spread
+    // over a thread-block cluster, cells dense when the budget holds them, else hashed.
+    if ((B >= g->ctx->cluster_blocks || !window) && B > kWinSharedMax && max_k <= 4096 && ensure_cluster(g)) {
         const bool hashed = !g->w.cells || mh_window_cells((int32_t)B) > g->w.cells_elems;
         if (hashed) chain_init(bm->d, g->w, (uint64_t)(2 * k_sum + 4 * (int64_t)n), g->ctx->stream);
         {
@@ -531,8 +531,7 @@ void chain_run(sbpgpu_bm* bm, const int32_t* order, int32_t n, int32_t max_k, in
         do_rebuild(bm);
         return;
     }
-    WindowPlan plan{};
-    if (mh_window_plan(bm->d.B, max_k, g->w, &plan)) {
+    if (window) {
         Span sp(g->ctx, 1);
         mh_chain_window(g->dg, bm->d, order, n, plan, seed, it, step, mode, g->w, g->ctx->stream);
     } else if (mode != ACC_GREEDY) {

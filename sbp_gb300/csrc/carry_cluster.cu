@@ -10,16 +10,21 @@
 // memory and hardware barriers carry the rest:
 //   1. CTA 0 selects the candidates (the W smallest entries of the sorted proposals, the
 //      global put-back runs and its shared put-back buffer) and the bound (the next entry);
-//   2. each warp re-scores one candidate and registers, in a per-block reader list, every
-//      block its value depends on (its two blocks and the third blocks of its row and
-//      column);
-//   3. each warp walks the reader lists of its candidate's two blocks: the readers are the
-//      candidates a merge of this one would change;
-//   4. CTA 0 collects the values and those sets and replays the rule on one thread (a merge
-//      marks the candidates it changes; popping a marked candidate or put-back entry ends
-//      the round), then folds the round's put-backs into its buffer;
+//   2. each warp re-scores one candidate and publishes its block in a per-block array;
+//   3. each warp finds the candidates a merge of its own would change: a candidate's value
+//      reads the cells of its block's row and column and the degrees of their keys, and x
+//      is a key of block a's row exactly when a is a key of x's column, so walking the row
+//      and column key lists of the merge's two blocks and looking each key up in the
+//      per-block array finds them (a key whose cell has dropped to zero only adds a
+//      conflict that need not be one);
+//   4. CTA 0 collects the values and those sets and replays the rule on one warp: runs of
+//      candidates that merge (or are skipped) without a put-back and that no earlier merge
+//      of the run changes are taken 32 at a time with ballots, every other pop under the
+//      full rule on one lane (a merge marks the candidates it changes; popping a marked
+//      candidate or put-back entry ends the round); the round's put-backs are then folded
+//      into CTA 0's buffer;
 //   5. the round's merges (disjoint rows, columns and targets, by the conflict rule) are
-//      applied by all CTAs at once, and the reader lists are cleared.
+//      applied by all CTAs at once.
 // Merges, their order and every put-back delta equal those of the one-at-a-time loop; ties
 // of equal delta pop in ascending block order.
 #include <cooperative_groups.h>
@@ -56,7 +61,6 @@ struct CcShared {
     long long c_act[kCcMaxW];
     int32_t c_count[kCcMaxW];
     uint32_t inv[kCcMaxW][kCcWords];  // bit j of inv[i]: a merge of candidate i changes j's value
-    int32_t fragile[kCcMaxW];         // its readers are not all listed: any merge changes it
     int32_t m_from[kCcMaxW], m_to[kCcMaxW];
     long long h_d[kCcMaxW];  // replay's put-back heap
     int32_t h_b[kCcMaxW], h_c[kCcMaxW];
@@ -68,7 +72,6 @@ struct CcShared {
     long long my_act[kCcWarps];
     int32_t my_count[kCcWarps];
     uint32_t my_inv[kCcWarps][kCcWords];
-    int32_t my_fragile[kCcWarps];
     // new keys of the row / column of each merge's target, staged, then appended in bulk
     int32_t st_n[kCcWarps / 2][2];
     int32_t st_slot[kCcWarps / 2][2];
@@ -76,22 +79,6 @@ struct CcShared {
     int32_t b_blk;
     int32_t p, q, nR, rsel, ns, ssel, ne;
     int32_t ncand, has_bound, done, nm, cS, nq;
-};
-
-// Per-block reader lists of a round: head[b] (or -1) and nodes (block, candidate, next).
-struct Readers {
-    int32_t* head;
-    int32_t* node;
-    int32_t cap;
-    int32_t* used;
-    __device__ __forceinline__ bool add(int32_t b, int32_t cand) const {
-        const int32_t k = atomicAdd(used, 1);
-        if (k >= cap) return false;
-        node[3 * k] = b;
-        node[3 * k + 1] = cand;
-        node[3 * k + 2] = atomicExch(head + b, k);
-        return true;
-    }
 };
 
 __device__ __forceinline__ void heap_push(CcShared& sh, int& n, long long d, int32_t b, int32_t c) {
@@ -135,7 +122,7 @@ template <class Cells, bool kNP>
 __global__ void __launch_bounds__(kCcThreads, 1) k_carry_cluster(
     DevGraph g, DevBM bm, DevChain ch, Cells cells, const uint64_t* __restrict__ pkeys,
     const int32_t* __restrict__ pblk, int32_t nP, const int32_t* __restrict__ best, long long* r0_dS, int32_t* r0_blk,
-    long long* r1_dS, int32_t* r1_blk, int32_t* parent, long long num_to_merge, Readers rd, int32_t* stage_buf,
+    long long* r1_dS, int32_t* r1_blk, int32_t* parent, long long num_to_merge, int32_t* cand_of, int32_t* stage_buf,
     int32_t* out_merged, DevFlags* flags) {
     cg::cluster_group cluster = cg::this_cluster();
     const int rank = (int)cluster.block_rank(), cs = (int)cluster.num_blocks();
@@ -163,7 +150,6 @@ __global__ void __launch_bounds__(kCcThreads, 1) k_carry_cluster(
                     atomicOr(&flags->err, ERR_STATE);
                     sh.done = 1;
                 }
-                *rd.used = 0;
             }
             __syncthreads();
             if (!sh.done) {
@@ -213,50 +199,61 @@ __global__ void __launch_bounds__(kCcThreads, 1) k_carry_cluster(
         cluster.sync();
         if (ctl.done) break;
         const int ncand = ctl.ncand;
-        // ---- 2. re-score this warp's candidate; register the blocks its value reads
+        // ---- 2. re-score this warp's candidate; publish its block in cand_of
         for (int i = tid; i < kCcWarps * kCcWords; i += kCcThreads) (&sh.my_inv[0][0])[i] = 0u;
         __syncthreads();
         const int j = rank * kCcWarps + warp;
         if (j < ncand) {
             const int32_t from = ctl.c_blk[j];
             int32_t to = 0;
-            bool ok = true;
             if (lane == 0) {
                 const int32_t b = best[from];
                 to = (b < 0 || b >= bm.B) ? from : uf_find(parent, b);
-                ok = rd.add(from, j) && rd.add(to, j);
+                cand_of[from] = j;
             }
             to = __shfl_sync(SBP_FULL_MASK, to, 0);
             long long part = 0;
             // nonparametric: zero when either block is empty (entropy.cpp:1203-1204)
             const bool counted = !kNP || (to != from && bm.sizes[from] != 0 && bm.sizes[to] != 0);
             if (to != from && counted) {
-                part = merge_delta_part<Cells, kNP>(g, bm, ch, cells, from, to, lane, 32, true,
-                                                    [&](int32_t x) { ok = rd.add(x, j) && ok; }, keys_seen);
+                part = merge_delta_part<Cells, kNP>(g, bm, ch, cells, from, to, lane, 32, true, [](int32_t) {},
+                                                    keys_seen);
                 if (lane == 0) ++evals;
             }
-            ok = __all_sync(SBP_FULL_MASK, ok);
             if (lane == 0) {
                 sh.my_to[warp] = to;
                 sh.my_act[warp] = part;
                 sh.my_count[warp] = kNP && counted;
             }
-            // a full reader pool: every merge of the round counts as changing this value
-            if (lane == 0) sh.my_fragile[warp] = !ok;
         }
         cluster.sync();
-        // ---- 3. the candidates a merge of this one would change: the readers of its blocks
-        if (j < ncand && lane == 0) {
+        // ---- 3. the candidates a merge of this one (a -> b) would change: those whose value
+        // reads a cell of row / column a or b or a degree of a or b -- their block is a or b,
+        // their target is a or b, or their block is a key of the row or column of a or b
+        // (cell (x, a) is non-zero only if x is listed in column a, and so on)
+        for (int k = tid; k < ncand; k += kCcThreads)
+            sh.c_to[k] = cluster.map_shared_rank(&sh, k / kCcWarps)->my_to[k % kCcWarps];
+        __syncthreads();
+        if (j < ncand) {
             const int32_t a = ctl.c_blk[j], b = sh.my_to[warp];
-            for (int h = 0; h < 2; ++h) {
-                if (h == 1 && b == a) break;
-                int32_t k = ((volatile int32_t*)rd.head)[h == 0 ? a : b];
-                int guard = 0;
-                while (k >= 0 && k < rd.cap && guard++ < (1 << 22)) {
-                    const int32_t r = rd.node[3 * k + 1];
-                    if (r != j && r >= 0 && r < ncand) sh.my_inv[warp][r >> 5] |= 1u << (r & 31);
-                    k = rd.node[3 * k + 2];
-                }
+            uint32_t* inv = sh.my_inv[warp];
+            auto mark = [&](int32_t x) {
+                const int32_t r = __ldcg(cand_of + x);
+                if (r >= 0 && r != j && r < ncand) atomicOr(inv + (r >> 5), 1u << (r & 31));
+            };
+            if (lane == 0) {
+                mark(a);
+                mark(b);
+            }
+            for (int k = lane; k < ncand; k += 32) {
+                const int32_t t = sh.c_to[k];
+                if (k != j && (t == a || t == b)) atomicOr(inv + (k >> 5), 1u << (k & 31));
+            }
+            list_for_each(bm.row_col, bm.row_off[a], bm.row_off[a + 1], ch.row_head[a], ch, lane, 32, mark);
+            list_for_each(bm.col_row, bm.col_off[a], bm.col_off[a + 1], ch.col_head[a], ch, lane, 32, mark);
+            if (b != a) {
+                list_for_each(bm.row_col, bm.row_off[b], bm.row_off[b + 1], ch.row_head[b], ch, lane, 32, mark);
+                list_for_each(bm.col_row, bm.col_off[b], bm.col_off[b + 1], ch.col_head[b], ch, lane, 32, mark);
             }
         }
         cluster.sync();
@@ -264,7 +261,6 @@ __global__ void __launch_bounds__(kCcThreads, 1) k_carry_cluster(
         if (controller) {
             for (int k = tid; k < ncand; k += kCcThreads) {
                 const CcShared& o = *cluster.map_shared_rank(&sh, k / kCcWarps);
-                sh.c_to[k] = o.my_to[k % kCcWarps];
                 sh.c_act[k] = o.my_act[k % kCcWarps];
                 sh.c_count[k] = o.my_count[k % kCcWarps];
             }
@@ -272,71 +268,178 @@ __global__ void __launch_bounds__(kCcThreads, 1) k_carry_cluster(
                 const int k = e / kCcWords, w = e % kCcWords;
                 sh.inv[k][w] = cluster.map_shared_rank(&sh, k / kCcWarps)->my_inv[k % kCcWarps][w];
             }
-            for (int k = tid; k < ncand; k += kCcThreads)
-                sh.fragile[k] = cluster.map_shared_rank(&sh, k / kCcWarps)->my_fragile[k % kCcWarps];
             if (tid < kCcWords) sh.smask[tid] = 0u;
             __syncthreads();
-            if (tid == 0) {
+            if (warp == 0) {
                 const bool hb = sh.has_bound;
                 const long long bnd_dS = sh.b_dS, merged0 = sh.merged;
                 const int32_t bnd_blk = sh.b_blk, ne0 = sh.ne;
-                int i = 0, nq = 0, nm = 0, cons[3] = {0, 0, 0};
-                auto stale = [&](int ci) {
-                    return ((sh.smask[ci >> 5] >> (ci & 31)) & 1u) || (nm > 0 && sh.fragile[ci]);
-                };
+                // uniform over the warp
+                int i = 0, nq = 0, nm = 0, c0 = 0, c1 = 0, c2 = 0;
                 while (merged0 + nm < num_to_merge) {
-                    const bool hc = i < ncand, hq = nq > 0;
-                    if (!hc && !hq) break;  // queue empty
-                    const bool fromq = hq && (!hc || qless(sh.h_d[0], sh.h_b[0], sh.c_dS[i], sh.c_blk[i]));
-                    const long long kd = fromq ? sh.h_d[0] : sh.c_dS[i];
-                    const int32_t kb = fromq ? sh.h_b[0] : sh.c_blk[i];
-                    if (hb && qless(bnd_dS, bnd_blk, kd, kb)) break;  // next pop not evaluated
-                    int ci;
-                    if (fromq) {
-                        // popped again: unless a merge since touched what it read, its value is
-                        // the one it was put back with (kNP: up to the count term)
-                        ci = sh.h_c[0];
-                        if (stale(ci)) break;
-                        heap_pop(sh, nq);
-                    } else {
-                        if (stale(i)) break;  // its value is stale: re-score it next round
-                        ci = i++;
-                        cons[sh.c_src[ci]]++;
-                        if (sh.c_to[ci] == kb) continue;  // already in the same block
-                    }
-                    const int32_t from = kb, to = sh.c_to[ci];
-                    long long act = sh.c_act[ci];
-                    if (kNP && sh.c_count[ci]) act += __ldg(g.Dm + min(max(ne0 - nm, 0), g.N + 1));
-                    const bool hc2 = i < ncand, hq2 = nq > 0;
-                    if (hc2 || hq2 || hb) {
-                        long long top = hb ? bnd_dS : LLONG_MAX;
-                        if (hc2) top = min(top, sh.c_dS[i]);
-                        if (hq2) top = min(top, sh.h_d[0]);
-                        if (act > top) {  // put back with the recomputed delta
-                            heap_push(sh, nq, act, from, ci);
+                    // -- a run of candidates popped before the put-back heap's top, each merged
+                    // or skipped without a put-back and unchanged by the merges before it,
+                    // taken 32 at a time (greedy entropy only: the nonparametric count term
+                    // changes with every merge)
+                    int f = 0;
+                    if (!kNP) {
+                        const int c = i + lane;
+                        const bool hq = nq > 0;
+                        const long long hqd = hq ? sh.h_d[0] : 0;
+                        const int32_t hqb = hq ? sh.h_b[0] : 0;
+                        bool valid = c < ncand;
+                        long long kd = 0;
+                        int32_t kb = 0;
+                        if (valid) {
+                            kd = sh.c_dS[c];
+                            kb = sh.c_blk[c];
+                            if (hq && !qless(kd, kb, hqd, hqb)) valid = false;           // the heap pops first
+                            if (hb && qless(bnd_dS, bnd_blk, kd, kb)) valid = false;     // not evaluated
+                        }
+                        int32_t to = 0;
+                        bool same = false, ok = false;
+                        if (valid) {
+                            to = sh.c_to[c];
+                            same = to == kb;
+                            const bool more = (c + 1 < ncand) || hq || hb;  // queue not empty after it
+                            long long top = hb ? bnd_dS : LLONG_MAX;
+                            if (c + 1 < ncand) top = min(top, sh.c_dS[c + 1]);
+                            if (hq) top = min(top, hqd);
+                            ok = same || !more || sh.c_act[c] <= top;
+                            if ((sh.smask[c >> 5] >> (c & 31)) & 1u) ok = false;  // changed by a merge
+                        }
+                        const unsigned okm = __ballot_sync(SBP_FULL_MASK, valid && ok);
+                        int nf = ~okm ? __ffs(~okm) - 1 : 32;
+                        // a merge of an earlier lane of the run may change a later one
+                        uint32_t win = 0;
+                        if (lane < nf && !same) {
+                            const int w0 = i >> 5, sft = i & 31;
+                            const uint32_t lo = sh.inv[c][w0];
+                            const uint32_t hi = w0 + 1 < kCcWords ? sh.inv[c][w0 + 1] : 0u;
+                            win = sft ? (lo >> sft) | (hi << (32 - sft)) : lo;
+                        }
+                        uint32_t incl = win;
+#pragma unroll
+                        for (int o = 1; o < 32; o <<= 1) {
+                            const uint32_t y = __shfl_up_sync(SBP_FULL_MASK, incl, o);
+                            if (lane >= o) incl |= y;
+                        }
+                        uint32_t ex = __shfl_up_sync(SBP_FULL_MASK, incl, 1);
+                        if (lane == 0) ex = 0u;
+                        const unsigned stm = __ballot_sync(SBP_FULL_MASK, lane < nf && ((ex >> lane) & 1u));
+                        if (stm) nf = min(nf, __ffs(stm) - 1);
+                        // no merges beyond the pass's count: stop after the last one wanted
+                        const unsigned mgm = __ballot_sync(SBP_FULL_MASK, lane < nf && !same);
+                        const long long need = num_to_merge - merged0 - nm;
+                        if (__popc(mgm) >= need) {
+                            const bool last = lane < nf && !same && __popc(mgm & lanemask_lt()) == need - 1;
+                            nf = min(nf, __ffs(__ballot_sync(SBP_FULL_MASK, last)));
+                        }
+                        f = nf;
+                        if (f > 0) {
+                            const bool com = lane < f, cm = com && !same;
+                            const unsigned cmm = __ballot_sync(SBP_FULL_MASK, cm);
+                            if (cm) {
+                                const int pos = nm + __popc(cmm & lanemask_lt());
+                                sh.m_from[pos] = kb;
+                                sh.m_to[pos] = to;
+                            }
+#pragma unroll
+                            for (int w = 0; w < kCcWords; ++w) {
+                                uint32_t v = cm ? sh.inv[c][w] : 0u;
+#pragma unroll
+                                for (int o = 16; o > 0; o >>= 1) v |= __shfl_xor_sync(SBP_FULL_MASK, v, o);
+                                if (lane == 0) sh.smask[w] |= v;
+                            }
+                            const int src = com ? sh.c_src[c] : -1;
+                            c0 += __popc(__ballot_sync(SBP_FULL_MASK, src == 0));
+                            c1 += __popc(__ballot_sync(SBP_FULL_MASK, src == 1));
+                            c2 += __popc(__ballot_sync(SBP_FULL_MASK, src == 2));
+                            i += f;
+                            nm += __popc(cmm);
+                            __syncwarp();
                             continue;
                         }
                     }
-                    sh.m_from[nm] = from;
-                    sh.m_to[nm] = to;
-                    for (int w = 0; w < kCcWords; ++w) sh.smask[w] |= sh.inv[ci][w];
-                    ++nm;
+                    // -- one pop under the full rule (lane 0)
+                    int br = 0;
+                    if (lane == 0) {
+                        const bool hc = i < ncand, hq = nq > 0;
+                        if (!hc && !hq) {
+                            br = 1;  // queue empty
+                        } else {
+                            const bool fromq = hq && (!hc || qless(sh.h_d[0], sh.h_b[0], sh.c_dS[i], sh.c_blk[i]));
+                            const long long kd = fromq ? sh.h_d[0] : sh.c_dS[i];
+                            const int32_t kb = fromq ? sh.h_b[0] : sh.c_blk[i];
+                            int ci = -1;
+                            if (hb && qless(bnd_dS, bnd_blk, kd, kb)) {
+                                br = 1;  // next pop not evaluated
+                            } else if (fromq) {
+                                // popped again: unless a merge since touched what it read, its
+                                // value is the one it was put back with (kNP: up to the count term)
+                                ci = sh.h_c[0];
+                                if ((sh.smask[ci >> 5] >> (ci & 31)) & 1u) br = 1;
+                                else heap_pop(sh, nq);
+                            } else if ((sh.smask[i >> 5] >> (i & 31)) & 1u) {
+                                br = 1;  // its value is stale: re-score it next round
+                            } else {
+                                ci = i++;
+                                const int src = sh.c_src[ci];
+                                c0 += src == 0;
+                                c1 += src == 1;
+                                c2 += src == 2;
+                                if (sh.c_to[ci] == kb) ci = -1;  // already in the same block
+                            }
+                            if (!br && ci >= 0) {
+                                const int32_t from = kb, to = sh.c_to[ci];
+                                long long act = sh.c_act[ci];
+                                if (kNP && sh.c_count[ci]) act += __ldg(g.Dm + min(max(ne0 - nm, 0), g.N + 1));
+                                const bool hc2 = i < ncand, hq2 = nq > 0;
+                                bool put_back = false;
+                                if (hc2 || hq2 || hb) {
+                                    long long top = hb ? bnd_dS : LLONG_MAX;
+                                    if (hc2) top = min(top, sh.c_dS[i]);
+                                    if (hq2) top = min(top, sh.h_d[0]);
+                                    put_back = act > top;
+                                }
+                                if (put_back) {  // put back with the recomputed delta
+                                    heap_push(sh, nq, act, from, ci);
+                                } else {
+                                    sh.m_from[nm] = from;
+                                    sh.m_to[nm] = to;
+                                    for (int w = 0; w < kCcWords; ++w) sh.smask[w] |= sh.inv[ci][w];
+                                    ++nm;
+                                }
+                            }
+                        }
+                    }
+                    br = __shfl_sync(SBP_FULL_MASK, br, 0);
+                    i = __shfl_sync(SBP_FULL_MASK, i, 0);
+                    nq = __shfl_sync(SBP_FULL_MASK, nq, 0);
+                    nm = __shfl_sync(SBP_FULL_MASK, nm, 0);
+                    c0 = __shfl_sync(SBP_FULL_MASK, c0, 0);
+                    c1 = __shfl_sync(SBP_FULL_MASK, c1, 0);
+                    c2 = __shfl_sync(SBP_FULL_MASK, c2, 0);
+                    __syncwarp();
+                    if (br) break;
                 }
-                int k = 0;
-                while (nq > 0) {
-                    sh.q_dS[k] = sh.h_d[0];
-                    sh.q_blk[k] = sh.h_b[0];
-                    ++k;
-                    heap_pop(sh, nq);
+                if (lane == 0) {
+                    int k = 0;
+                    while (nq > 0) {
+                        sh.q_dS[k] = sh.h_d[0];
+                        sh.q_blk[k] = sh.h_b[0];
+                        ++k;
+                        heap_pop(sh, nq);
+                    }
+                    sh.nq = k;
+                    sh.p += c0;
+                    sh.q += c1;
+                    sh.cS = c2;
+                    sh.nm = nm;
+                    sh.merged += nm;
+                    sh.ne -= nm;  // every merge lowers the count (blockmodel.cpp:356)
+                    sh.rounds += 1;
                 }
-                sh.nq = k;
-                sh.p += cons[0];
-                sh.q += cons[1];
-                sh.cS = cons[2];
-                sh.nm = nm;
-                sh.merged += nm;
-                sh.ne -= nm;  // every merge lowers the count (blockmodel.cpp:356)
-                sh.rounds += 1;
             }
             __syncthreads();
             // S := S[cS..ns) merged with the round's put-backs
@@ -487,9 +590,8 @@ __global__ void __launch_bounds__(kCcThreads, 1) k_carry_cluster(
                 }
                 __syncthreads();
             }
-            // clear the round's reader lists
-            const int32_t used = min(*(volatile int32_t*)rd.used, rd.cap);
-            for (int32_t k = rank * kCcThreads + tid; k < used; k += cs * kCcThreads) rd.head[rd.node[3 * k]] = -1;
+            // this round's candidate blocks leave cand_of
+            if (j < ncand && lane == 0) cand_of[ctl.c_blk[j]] = -1;
         }
         cluster.sync();
     }
@@ -555,11 +657,10 @@ void launch_carry_cluster(const DevGraph& g, DevBM& bm, const Cells& cells, int6
     at[0].val.clusterDim.z = 1;
     cfg.attrs = at;
     cfg.numAttrs = 1;
-    Readers rd{w.cc_head, w.cc_nodes, w.cc_node_cap, w.cc_used};
     const cudaError_t e = cudaLaunchKernelEx(
         &cfg, kernel, g, bm, w.chain, cells, (const uint64_t*)w.keys, (const int32_t*)w.vals, bm.B,
         (const int32_t*)w.best, reinterpret_cast<long long*>(w.heap_dS), w.heap_blk,
-        reinterpret_cast<long long*>(w.keys_alt), w.vals_alt, w.parent, (long long)num_to_merge, rd, w.cc_stage,
+        reinterpret_cast<long long*>(w.keys_alt), w.vals_alt, w.parent, (long long)num_to_merge, w.cc_head, w.cc_stage,
         d_merged, w.flags_dev);
     if (e != cudaSuccess) throw std::runtime_error(std::string("cluster carry-out launch: ") + cudaGetErrorString(e));
 }
@@ -579,7 +680,7 @@ size_t carry_cluster_stage_ints(int cs) { return (size_t)cs * (kCcWarps / 2) * 2
 void carry_out_cluster(const DevGraph& g, DevBM& bm, int64_t num_to_merge, Work& w, cudaStream_t st, bool np) {
     if (np && (!g.LG || !g.Dm || !g.Dp)) throw std::logic_error("nonparametric tables missing");
     const int cs = carry_cluster_size();
-    if (cs <= 0 || !w.cc_head || !w.cc_nodes || !w.cc_stage)
+    if (cs <= 0 || !w.cc_head || !w.cc_stage)
         throw std::logic_error("cluster carry-out buffers missing");
     const int32_t B = bm.B;
     const bool dense = w.cells && (uint64_t)B * (uint64_t)B <= w.cells_elems;

@@ -60,12 +60,10 @@ struct Work {
     // the cluster chain's per-warp neighbour hashes and row scratch (allocated on first use)
     int32_t* cl_hash = nullptr;
     int32_t* cl_scratch = nullptr;
-    // the cluster carry-out's per-block reader lists (allocated on first use)
+    // the cluster carry-out's per-block candidate (or -1) and staged new keys of the merges'
+    // targets (allocated on first use)
     int32_t* cc_head = nullptr;        // [N]
-    int32_t* cc_nodes = nullptr;       // [3 * cc_node_cap]
-    int32_t cc_node_cap = 0;
-    int32_t* cc_used = nullptr;        // device counter
-    int32_t* cc_stage = nullptr;       // staged new keys of the merges' targets
+    int32_t* cc_stage = nullptr;
     // dense B x B cell values of the merge carry-out (allocated on demand within a budget)
     int32_t* cells = nullptr;
     uint64_t cells_elems = 0;
@@ -155,7 +153,7 @@ void carry_out(const DevGraph& g, DevBM& bm, int64_t num_to_merge, int approxima
 // w.cells when B * B <= w.cells_elems, the chain hash otherwise.
 void carry_out_exact(const DevGraph& g, DevBM& bm, int64_t num_to_merge, Work& w, cudaStream_t st, bool np = false);
 // The same on a thread-block cluster of carry_cluster_size() CTAs (0: the device holds
-// none); needs w.cc_head / w.cc_nodes / w.cc_used.
+// none); needs w.cc_head and w.cc_stage.
 int carry_cluster_size();
 size_t carry_cluster_stage_ints(int cs);
 void carry_out_cluster(const DevGraph& g, DevBM& bm, int64_t num_to_merge, Work& w, cudaStream_t st, bool np);
