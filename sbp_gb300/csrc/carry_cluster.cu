@@ -47,6 +47,7 @@ constexpr int kCcMaxW = kCcWarps * kCcMaxCluster;  // candidates per round
 constexpr int kCcWords = kCcMaxW / 32;              // words of a conflict mask
 constexpr int kCcQS = 4096;                         // CTA 0's sorted put-back buffer
 constexpr int kCcStage = 1 << 15;                   // staged new keys per merge and list
+constexpr int kCcQCap = 2 * kCcMaxW;                // the replay's put-back list
 
 // Shared memory of every CTA (dynamic); the queue parts are used by CTA 0 only.
 struct CcShared {
@@ -62,10 +63,8 @@ struct CcShared {
     int32_t c_count[kCcMaxW];
     uint32_t inv[kCcMaxW][kCcWords];  // bit j of inv[i]: a merge of candidate i changes j's value
     int32_t m_from[kCcMaxW], m_to[kCcMaxW];
-    long long h_d[kCcMaxW];  // replay's put-back heap
-    int32_t h_b[kCcMaxW], h_c[kCcMaxW];
-    long long q_dS[kCcMaxW];  // the round's remaining put-backs, sorted
-    int32_t q_blk[kCcMaxW];
+    long long h_d[kCcQCap];  // the round's put-back entries, sorted, live in [qh, qh + nq)
+    int32_t h_b[kCcQCap], h_c[kCcQCap];
     uint32_t smask[kCcWords];  // candidates whose value a merge of the round has changed
     // this CTA's own candidates
     int32_t my_to[kCcWarps];
@@ -78,45 +77,8 @@ struct CcShared {
     long long b_dS, merged, rounds;
     int32_t b_blk;
     int32_t p, q, nR, rsel, ns, ssel, ne;
-    int32_t ncand, has_bound, done, nm, cS, nq;
+    int32_t ncand, has_bound, done, nm, cS, nq, qh;
 };
-
-__device__ __forceinline__ void heap_push(CcShared& sh, int& n, long long d, int32_t b, int32_t c) {
-    int i = n++;
-    while (i > 0) {
-        const int p = (i - 1) >> 1;
-        if (!qless(d, b, sh.h_d[p], sh.h_b[p])) break;
-        sh.h_d[i] = sh.h_d[p];
-        sh.h_b[i] = sh.h_b[p];
-        sh.h_c[i] = sh.h_c[p];
-        i = p;
-    }
-    sh.h_d[i] = d;
-    sh.h_b[i] = b;
-    sh.h_c[i] = c;
-}
-
-__device__ __forceinline__ void heap_pop(CcShared& sh, int& n) {
-    const int m = --n;
-    const long long d = sh.h_d[m];
-    const int32_t b = sh.h_b[m], c = sh.h_c[m];
-    int i = 0;
-    while (true) {
-        int k = 2 * i + 1;
-        if (k >= m) break;
-        if (k + 1 < m && qless(sh.h_d[k + 1], sh.h_b[k + 1], sh.h_d[k], sh.h_b[k])) ++k;
-        if (!qless(sh.h_d[k], sh.h_b[k], d, b)) break;
-        sh.h_d[i] = sh.h_d[k];
-        sh.h_b[i] = sh.h_b[k];
-        sh.h_c[i] = sh.h_c[k];
-        i = k;
-    }
-    if (m > 0) {
-        sh.h_d[i] = d;
-        sh.h_b[i] = b;
-        sh.h_c[i] = c;
-    }
-}
 
 template <class Cells, bool kNP>
 __global__ void __launch_bounds__(kCcThreads, 1) k_carry_cluster(
@@ -271,30 +233,36 @@ __global__ void __launch_bounds__(kCcThreads, 1) k_carry_cluster(
             if (tid < kCcWords) sh.smask[tid] = 0u;
             __syncthreads();
             if (warp == 0) {
+                // The replay, uniform over the warp.  Put-back entries wait in a sorted list
+                // h[qh, qh + nq): a pop advances qh, a put-back shifts the entries after its
+                // place up by one (each lane moves up to 16 of them).
                 const bool hb = sh.has_bound;
                 const long long bnd_dS = sh.b_dS, merged0 = sh.merged;
                 const int32_t bnd_blk = sh.b_blk, ne0 = sh.ne;
-                // uniform over the warp
-                int i = 0, nq = 0, nm = 0, c0 = 0, c1 = 0, c2 = 0;
-                while (merged0 + nm < num_to_merge) {
-                    // -- a run of candidates popped before the put-back heap's top, each merged
-                    // or skipped without a put-back and unchanged by the merges before it,
-                    // taken 32 at a time (greedy entropy only: the nonparametric count term
-                    // changes with every merge)
-                    int f = 0;
-                    if (!kNP) {
+                int i = 0, qh = 0, nq = 0, nm = 0, c0 = 0, c1 = 0, c2 = 0;
+                auto stale = [&](int ci) { return ((sh.smask[ci >> 5] >> (ci & 31)) & 1u) != 0u; };
+                for (int guard = 0; merged0 + nm < num_to_merge && guard < 8 * kCcMaxW; ++guard) {
+                    const bool hc = i < ncand, hq = nq > 0;
+                    if (!hc && !hq) break;  // queue empty
+                    const long long qd = hq ? sh.h_d[qh] : 0;
+                    const int32_t qb = hq ? sh.h_b[qh] : 0;
+                    const long long cd = hc ? sh.c_dS[i] : 0;
+                    const int32_t cb = hc ? sh.c_blk[i] : 0;
+                    const bool fromq = hq && (!hc || qless(qd, qb, cd, cb));
+                    if (!kNP && !fromq) {
+                        // -- a run of candidates popped before the put-back list's head, each
+                        // merged or skipped without a put-back and unchanged by the merges
+                        // before it, taken 32 at a time (greedy entropy only: the
+                        // nonparametric count term changes with every merge)
                         const int c = i + lane;
-                        const bool hq = nq > 0;
-                        const long long hqd = hq ? sh.h_d[0] : 0;
-                        const int32_t hqb = hq ? sh.h_b[0] : 0;
                         bool valid = c < ncand;
                         long long kd = 0;
                         int32_t kb = 0;
                         if (valid) {
                             kd = sh.c_dS[c];
                             kb = sh.c_blk[c];
-                            if (hq && !qless(kd, kb, hqd, hqb)) valid = false;           // the heap pops first
-                            if (hb && qless(bnd_dS, bnd_blk, kd, kb)) valid = false;     // not evaluated
+                            if (hq && !qless(kd, kb, qd, qb)) valid = false;          // the list pops first
+                            if (hb && qless(bnd_dS, bnd_blk, kd, kb)) valid = false;  // not evaluated
                         }
                         int32_t to = 0;
                         bool same = false, ok = false;
@@ -304,9 +272,8 @@ __global__ void __launch_bounds__(kCcThreads, 1) k_carry_cluster(
                             const bool more = (c + 1 < ncand) || hq || hb;  // queue not empty after it
                             long long top = hb ? bnd_dS : LLONG_MAX;
                             if (c + 1 < ncand) top = min(top, sh.c_dS[c + 1]);
-                            if (hq) top = min(top, hqd);
-                            ok = same || !more || sh.c_act[c] <= top;
-                            if ((sh.smask[c >> 5] >> (c & 31)) & 1u) ok = false;  // changed by a merge
+                            if (hq) top = min(top, qd);
+                            ok = (same || !more || sh.c_act[c] <= top) && !stale(c);
                         }
                         const unsigned okm = __ballot_sync(SBP_FULL_MASK, valid && ok);
                         int nf = ~okm ? __ffs(~okm) - 1 : 32;
@@ -335,9 +302,8 @@ __global__ void __launch_bounds__(kCcThreads, 1) k_carry_cluster(
                             const bool last = lane < nf && !same && __popc(mgm & lanemask_lt()) == need - 1;
                             nf = min(nf, __ffs(__ballot_sync(SBP_FULL_MASK, last)));
                         }
-                        f = nf;
-                        if (f > 0) {
-                            const bool com = lane < f, cm = com && !same;
+                        if (nf > 0) {
+                            const bool com = lane < nf, cm = com && !same;
                             const unsigned cmm = __ballot_sync(SBP_FULL_MASK, cm);
                             if (cm) {
                                 const int pos = nm + __popc(cmm & lanemask_lt());
@@ -355,83 +321,118 @@ __global__ void __launch_bounds__(kCcThreads, 1) k_carry_cluster(
                             c0 += __popc(__ballot_sync(SBP_FULL_MASK, src == 0));
                             c1 += __popc(__ballot_sync(SBP_FULL_MASK, src == 1));
                             c2 += __popc(__ballot_sync(SBP_FULL_MASK, src == 2));
-                            i += f;
+                            i += nf;
                             nm += __popc(cmm);
                             __syncwarp();
                             continue;
                         }
                     }
-                    // -- one pop under the full rule (lane 0)
-                    int br = 0;
-                    if (lane == 0) {
-                        const bool hc = i < ncand, hq = nq > 0;
-                        if (!hc && !hq) {
-                            br = 1;  // queue empty
-                        } else {
-                            const bool fromq = hq && (!hc || qless(sh.h_d[0], sh.h_b[0], sh.c_dS[i], sh.c_blk[i]));
-                            const long long kd = fromq ? sh.h_d[0] : sh.c_dS[i];
-                            const int32_t kb = fromq ? sh.h_b[0] : sh.c_blk[i];
-                            int ci = -1;
-                            if (hb && qless(bnd_dS, bnd_blk, kd, kb)) {
-                                br = 1;  // next pop not evaluated
-                            } else if (fromq) {
-                                // popped again: unless a merge since touched what it read, its
-                                // value is the one it was put back with (kNP: up to the count term)
-                                ci = sh.h_c[0];
-                                if ((sh.smask[ci >> 5] >> (ci & 31)) & 1u) br = 1;
-                                else heap_pop(sh, nq);
-                            } else if ((sh.smask[i >> 5] >> (i & 31)) & 1u) {
-                                br = 1;  // its value is stale: re-score it next round
-                            } else {
-                                ci = i++;
-                                const int src = sh.c_src[ci];
-                                c0 += src == 0;
-                                c1 += src == 1;
-                                c2 += src == 2;
-                                if (sh.c_to[ci] == kb) ci = -1;  // already in the same block
-                            }
-                            if (!br && ci >= 0) {
-                                const int32_t from = kb, to = sh.c_to[ci];
-                                long long act = sh.c_act[ci];
-                                if (kNP && sh.c_count[ci]) act += __ldg(g.Dm + min(max(ne0 - nm, 0), g.N + 1));
-                                const bool hc2 = i < ncand, hq2 = nq > 0;
-                                bool put_back = false;
-                                if (hc2 || hq2 || hb) {
-                                    long long top = hb ? bnd_dS : LLONG_MAX;
-                                    if (hc2) top = min(top, sh.c_dS[i]);
-                                    if (hq2) top = min(top, sh.h_d[0]);
-                                    put_back = act > top;
-                                }
-                                if (put_back) {  // put back with the recomputed delta
-                                    heap_push(sh, nq, act, from, ci);
-                                } else {
-                                    sh.m_from[nm] = from;
-                                    sh.m_to[nm] = to;
-                                    for (int w = 0; w < kCcWords; ++w) sh.smask[w] |= sh.inv[ci][w];
-                                    ++nm;
-                                }
-                            }
-                        }
+                    // -- one pop under the full rule
+                    const long long kd = fromq ? qd : cd;
+                    const int32_t kb = fromq ? qb : cb;
+                    if (hb && qless(bnd_dS, bnd_blk, kd, kb)) break;  // next pop not evaluated
+                    int ci;
+                    if (fromq) {
+                        // popped again: unless a merge since touched what it read, its value is
+                        // the one it was put back with (kNP: up to the count term)
+                        ci = sh.h_c[qh];
+                        if (stale(ci)) break;
+                        ++qh;
+                        --nq;
+                    } else {
+                        if (stale(i)) break;  // its value is stale: re-score it next round
+                        if (nq >= kCcQCap) break;  // no room for a put-back: end the round here
+                        ci = i++;
+                        const int src = sh.c_src[ci];
+                        c0 += src == 0;
+                        c1 += src == 1;
+                        c2 += src == 2;
+                        if (sh.c_to[ci] == kb) continue;  // already in the same block
                     }
-                    br = __shfl_sync(SBP_FULL_MASK, br, 0);
-                    i = __shfl_sync(SBP_FULL_MASK, i, 0);
-                    nq = __shfl_sync(SBP_FULL_MASK, nq, 0);
-                    nm = __shfl_sync(SBP_FULL_MASK, nm, 0);
-                    c0 = __shfl_sync(SBP_FULL_MASK, c0, 0);
-                    c1 = __shfl_sync(SBP_FULL_MASK, c1, 0);
-                    c2 = __shfl_sync(SBP_FULL_MASK, c2, 0);
+                    const int32_t to = sh.c_to[ci];
+                    long long act = sh.c_act[ci];
+                    if (kNP && sh.c_count[ci]) act += __ldg(g.Dm + min(max(ne0 - nm, 0), g.N + 1));
+                    const bool hc2 = i < ncand, hq2 = nq > 0;
+                    bool put_back = false;
+                    if (hc2 || hq2 || hb) {
+                        long long top = hb ? bnd_dS : LLONG_MAX;
+                        if (hc2) top = min(top, sh.c_dS[i]);
+                        if (hq2) top = min(top, sh.h_d[qh]);
+                        put_back = act > top;
+                    }
+                    if (put_back) {
+                        // put back with the recomputed delta: its place in the sorted list
+                        int before = 0;
+                        for (int k = lane; k < nq; k += 32) before += qless(sh.h_d[qh + k], sh.h_b[qh + k], act, kb);
+                        const int pos = warp_sum_i(before);
+                        if (qh + nq + 1 > kCcQCap) {  // move the list to the front of its array
+                            long long vd[kCcQCap / 32];
+                            int32_t vb[kCcQCap / 32], vc[kCcQCap / 32];
+#pragma unroll
+                            for (int t = 0; t < kCcQCap / 32; ++t) {
+                                const int k = lane + 32 * t;
+                                if (k < nq) {
+                                    vd[t] = sh.h_d[qh + k];
+                                    vb[t] = sh.h_b[qh + k];
+                                    vc[t] = sh.h_c[qh + k];
+                                }
+                            }
+                            __syncwarp();
+#pragma unroll
+                            for (int t = 0; t < kCcQCap / 32; ++t) {
+                                const int k = lane + 32 * t;
+                                if (k < nq) {
+                                    sh.h_d[k] = vd[t];
+                                    sh.h_b[k] = vb[t];
+                                    sh.h_c[k] = vc[t];
+                                }
+                            }
+                            __syncwarp();
+                            qh = 0;
+                        }
+                        {
+                            long long vd[kCcQCap / 32];
+                            int32_t vb[kCcQCap / 32], vc[kCcQCap / 32];
+#pragma unroll
+                            for (int t = 0; t < kCcQCap / 32; ++t) {
+                                const int k = pos + lane + 32 * t;
+                                if (k < nq) {
+                                    vd[t] = sh.h_d[qh + k];
+                                    vb[t] = sh.h_b[qh + k];
+                                    vc[t] = sh.h_c[qh + k];
+                                }
+                            }
+                            __syncwarp();
+#pragma unroll
+                            for (int t = 0; t < kCcQCap / 32; ++t) {
+                                const int k = pos + lane + 32 * t;
+                                if (k < nq) {
+                                    sh.h_d[qh + k + 1] = vd[t];
+                                    sh.h_b[qh + k + 1] = vb[t];
+                                    sh.h_c[qh + k + 1] = vc[t];
+                                }
+                            }
+                            if (lane == 0) {
+                                sh.h_d[qh + pos] = act;
+                                sh.h_b[qh + pos] = kb;
+                                sh.h_c[qh + pos] = ci;
+                            }
+                            __syncwarp();
+                        }
+                        ++nq;
+                        continue;
+                    }
+                    if (lane == 0) {
+                        sh.m_from[nm] = kb;
+                        sh.m_to[nm] = to;
+                    }
+                    if (lane < kCcWords) sh.smask[lane] |= sh.inv[ci][lane];
+                    ++nm;
                     __syncwarp();
-                    if (br) break;
                 }
                 if (lane == 0) {
-                    int k = 0;
-                    while (nq > 0) {
-                        sh.q_dS[k] = sh.h_d[0];
-                        sh.q_blk[k] = sh.h_b[0];
-                        ++k;
-                        heap_pop(sh, nq);
-                    }
-                    sh.nq = k;
+                    sh.qh = qh;
+                    sh.nq = nq;
                     sh.p += c0;
                     sh.q += c1;
                     sh.cS = c2;
@@ -445,6 +446,8 @@ __global__ void __launch_bounds__(kCcThreads, 1) k_carry_cluster(
             // S := S[cS..ns) merged with the round's put-backs
             {
                 const int cS = sh.cS, nq = sh.nq, ns = sh.ns, ssel = sh.ssel;
+                const long long* q_dS = sh.h_d + sh.qh;
+                const int32_t* q_blk = sh.h_b + sh.qh;
                 if (cS > 0 || nq > 0) {
                     const int rest = ns - cS;
                     const long long* sd = sh.s_dS[ssel] + cS;
@@ -452,14 +455,14 @@ __global__ void __launch_bounds__(kCcThreads, 1) k_carry_cluster(
                     long long* od = sh.s_dS[ssel ^ 1];
                     int32_t* ob = sh.s_blk[ssel ^ 1];
                     for (int i = tid; i < rest; i += kCcThreads) {
-                        const int pos = i + count_before(sh.q_dS, sh.q_blk, nq, sd[i], sb[i]);
+                        const int pos = i + count_before(q_dS, q_blk, nq, sd[i], sb[i]);
                         od[pos] = sd[i];
                         ob[pos] = sb[i];
                     }
                     for (int k = tid; k < nq; k += kCcThreads) {
-                        const int pos = k + count_before(sd, sb, rest, sh.q_dS[k], sh.q_blk[k]);
-                        od[pos] = sh.q_dS[k];
-                        ob[pos] = sh.q_blk[k];
+                        const int pos = k + count_before(sd, sb, rest, q_dS[k], q_blk[k]);
+                        od[pos] = q_dS[k];
+                        ob[pos] = q_blk[k];
                     }
                     __syncthreads();
                     if (tid == 0) {
@@ -470,7 +473,7 @@ __global__ void __launch_bounds__(kCcThreads, 1) k_carry_cluster(
                 }
             }
             // spill S into the global run when it could not take another round's put-backs
-            if (sh.ns > kCcQS - kCcMaxW - 1) {
+            if (sh.ns > kCcQS - kCcQCap - 1) {
                 const int ns = sh.ns, ssel = sh.ssel, q = sh.q, nr = sh.nR - sh.q;
                 const long long* rdS = (sh.rsel ? r1_dS : r0_dS) + q;
                 const int32_t* rb = (sh.rsel ? r1_blk : r0_blk) + q;
