@@ -63,6 +63,9 @@ struct CcShared {
     int32_t c_count[kCcMaxW];
     uint32_t inv[kCcMaxW][kCcWords];  // bit j of inv[i]: a merge of candidate i changes j's value
     int32_t m_from[kCcMaxW], m_to[kCcMaxW];
+    int32_t a_rank[kCcMaxW];    // greedy replay: rank of each candidate by (recomputed delta, block)
+    long long a_d[kCcMaxW];     // ... and the candidates in that order
+    int32_t a_b[kCcMaxW], a_c[kCcMaxW];
     long long h_d[kCcQCap];  // the round's put-back entries, sorted, live in [qh, qh + nq)
     int32_t h_b[kCcQCap], h_c[kCcQCap];
     uint32_t smask[kCcWords];  // candidates whose value a merge of the round has changed
@@ -232,7 +235,119 @@ __global__ void __launch_bounds__(kCcThreads, 1) k_carry_cluster(
             }
             if (tid < kCcWords) sh.smask[tid] = 0u;
             __syncthreads();
-            if (warp == 0) {
+            if constexpr (!kNP) {
+                // Greedy entropy: an entry put back in this round carries its recomputed delta,
+                // which is known for every candidate, so the put-back entries are kept as a set
+                // of ranks in the candidates' (recomputed delta, block) order: a 256-bit mask
+                // whose lowest set bit is the list's head.  The ranks first, in parallel.
+                for (int c = tid; c < ncand; c += kCcThreads) {
+                    const long long d = sh.c_act[c];
+                    const int32_t b = sh.c_blk[c];
+                    int r = 0;
+                    for (int k = 0; k < ncand; ++k) r += qless(sh.c_act[k], sh.c_blk[k], d, b);
+                    sh.a_rank[c] = r;
+                    sh.a_d[r] = d;
+                    sh.a_b[r] = b;
+                    sh.a_c[r] = c;
+                }
+                __syncthreads();
+                if (tid == 0) {
+                    const bool hb = sh.has_bound;
+                    const long long bnd_dS = sh.b_dS, merged0 = sh.merged;
+                    const int32_t bnd_blk = sh.b_blk;
+                    uint32_t pend[kCcWords], stl[kCcWords];
+#pragma unroll
+                    for (int w = 0; w < kCcWords; ++w) pend[w] = stl[w] = 0u;
+                    auto bit_of = [&](const uint32_t* m, int x) {
+                        uint32_t v = 0;
+#pragma unroll
+                        for (int w = 0; w < kCcWords; ++w) v = (w == (x >> 5)) ? m[w] : v;
+                        return (v >> (x & 31)) & 1u;
+                    };
+                    auto first = [&]() {
+                        int r = -1;
+#pragma unroll
+                        for (int w = kCcWords - 1; w >= 0; --w)
+                            if (pend[w]) r = 32 * w + __ffs(pend[w]) - 1;
+                        return r;
+                    };
+                    auto flip = [&](int x) {
+#pragma unroll
+                        for (int w = 0; w < kCcWords; ++w)
+                            if (w == (x >> 5)) pend[w] ^= 1u << (x & 31);
+                    };
+                    int i = 0, nm = 0, c0 = 0, c1 = 0, c2 = 0;
+                    int pr = -1;  // rank of the put-back list's head, or -1
+                    while (merged0 + nm < num_to_merge) {
+                        const bool hc = i < ncand, hq = pr >= 0;
+                        if (!hc && !hq) break;  // queue empty
+                        const long long cd = hc ? sh.c_dS[i] : 0;
+                        const int32_t cb = hc ? sh.c_blk[i] : 0;
+                        const long long qd = hq ? sh.a_d[pr] : 0;
+                        const int32_t qb = hq ? sh.a_b[pr] : 0;
+                        const bool fromq = hq && (!hc || qless(qd, qb, cd, cb));
+                        const long long kd = fromq ? qd : cd;
+                        const int32_t kb = fromq ? qb : cb;
+                        if (hb && qless(bnd_dS, bnd_blk, kd, kb)) break;  // next pop not evaluated
+                        int ci;
+                        if (fromq) {
+                            // popped again: unless a merge since touched what it read, its value
+                            // is the one it was put back with
+                            ci = sh.a_c[pr];
+                            if (bit_of(stl, ci)) break;
+                            flip(pr);
+                            pr = first();
+                        } else {
+                            if (bit_of(stl, i)) break;  // its value is stale: re-score it next round
+                            ci = i++;
+                            const int src = sh.c_src[ci];
+                            c0 += src == 0;
+                            c1 += src == 1;
+                            c2 += src == 2;
+                            if (sh.c_to[ci] == kb) continue;  // already in the same block
+                        }
+                        const long long act = sh.c_act[ci];
+                        const bool hc2 = i < ncand, hq2 = pr >= 0;
+                        if (hc2 || hq2 || hb) {
+                            long long top = hb ? bnd_dS : LLONG_MAX;
+                            if (hc2) top = min(top, sh.c_dS[i]);
+                            if (hq2) top = min(top, sh.a_d[pr]);
+                            if (act > top) {  // put back with the recomputed delta
+                                const int r = sh.a_rank[ci];
+                                flip(r);
+                                if (pr < 0 || r < pr) pr = r;
+                                continue;
+                            }
+                        }
+                        sh.m_from[nm] = kb;
+                        sh.m_to[nm] = sh.c_to[ci];
+#pragma unroll
+                        for (int w = 0; w < kCcWords; ++w) stl[w] |= sh.inv[ci][w];
+                        ++nm;
+                    }
+                    // the put-back entries left, in order, for the shared buffer
+                    int k = 0;
+#pragma unroll
+                    for (int w = 0; w < kCcWords; ++w) {
+                        uint32_t m = pend[w];
+                        while (m) {
+                            const int r = 32 * w + __ffs(m) - 1;
+                            m &= m - 1;
+                            sh.h_d[k] = sh.a_d[r];
+                            sh.h_b[k] = sh.a_b[r];
+                            ++k;
+                        }
+                    }
+                    sh.qh = 0;
+                    sh.nq = k;
+                    sh.p += c0;
+                    sh.q += c1;
+                    sh.cS = c2;
+                    sh.nm = nm;
+                    sh.merged += nm;
+                    sh.rounds += 1;
+                }
+            } else if (warp == 0) {
                 // The replay, uniform over the warp.  Put-back entries wait in a sorted list
                 // h[qh, qh + nq): a pop advances qh, a put-back shifts the entries after its
                 // place up by one (each lane moves up to 16 of them).
