@@ -48,6 +48,7 @@ constexpr int kCcWords = kCcMaxW / 32;              // words of a conflict mask
 constexpr int kCcQS = 4096;                         // CTA 0's sorted put-back buffer
 constexpr int kCcStage = 1 << 15;                   // staged new keys per merge and list
 constexpr int kCcQCap = 2 * kCcMaxW;                // the replay's put-back list
+constexpr int kCcBigKeys = 512;                     // keys above which the whole CTA scores a candidate
 
 // Shared memory of every CTA (dynamic); the queue parts are used by CTA 0 only.
 struct CcShared {
@@ -74,6 +75,9 @@ struct CcShared {
     long long my_act[kCcWarps];
     int32_t my_count[kCcWarps];
     uint32_t my_inv[kCcWarps][kCcWords];
+    int32_t big[kCcWarps];  // this CTA's candidates left to the whole CTA (by warp)
+    int32_t nbig;
+    long long big_acc;
     // new keys of the row / column of each merge's target, staged, then appended in bulk
     int32_t st_n[kCcWarps / 2][2];
     int32_t st_slot[kCcWarps / 2][2];
@@ -164,23 +168,32 @@ __global__ void __launch_bounds__(kCcThreads, 1) k_carry_cluster(
         cluster.sync();
         if (ctl.done) break;
         const int ncand = ctl.ncand;
-        // ---- 2. re-score this warp's candidate; publish its block in cand_of
+        // ---- 2. re-score the candidates; publish their blocks in cand_of.  Each warp takes
+        // one candidate; a candidate whose row and column lists are long is left to the whole
+        // CTA afterwards, so that no round waits on one warp walking a hub block's lists.
         for (int i = tid; i < kCcWarps * kCcWords; i += kCcThreads) (&sh.my_inv[0][0])[i] = 0u;
+        if (tid == 0) sh.nbig = 0;
         __syncthreads();
         const int j = rank * kCcWarps + warp;
         if (j < ncand) {
             const int32_t from = ctl.c_blk[j];
-            int32_t to = 0;
+            int32_t to = 0, len = 0;
             if (lane == 0) {
                 const int32_t b = best[from];
                 to = (b < 0 || b >= bm.B) ? from : uf_find(parent, b);
                 cand_of[from] = j;
+                len = (bm.row_off[from + 1] - bm.row_off[from]) + (bm.col_off[from + 1] - bm.col_off[from]) +
+                      list_chunk_keys(ch.row_head[from], ch) + list_chunk_keys(ch.col_head[from], ch);
             }
             to = __shfl_sync(SBP_FULL_MASK, to, 0);
+            len = __shfl_sync(SBP_FULL_MASK, len, 0);
             long long part = 0;
             // nonparametric: zero when either block is empty (entropy.cpp:1203-1204)
             const bool counted = !kNP || (to != from && bm.sizes[from] != 0 && bm.sizes[to] != 0);
-            if (to != from && counted) {
+            const bool scored = to != from && counted;
+            if (scored && len > kCcBigKeys) {
+                if (lane == 0) sh.big[atomicAdd(&sh.nbig, 1)] = warp;
+            } else if (scored) {
                 part = merge_delta_part<Cells, kNP>(g, bm, ch, cells, from, to, lane, 32, true, [](int32_t) {},
                                                     keys_seen);
                 if (lane == 0) ++evals;
@@ -189,6 +202,21 @@ __global__ void __launch_bounds__(kCcThreads, 1) k_carry_cluster(
                 sh.my_to[warp] = to;
                 sh.my_act[warp] = part;
                 sh.my_count[warp] = kNP && counted;
+            }
+        }
+        __syncthreads();
+        for (int q = 0; q < sh.nbig; ++q) {
+            const int w = sh.big[q];
+            const int32_t from = ctl.c_blk[rank * kCcWarps + w], to = sh.my_to[w];
+            if (tid == 0) sh.big_acc = 0;
+            __syncthreads();
+            const long long part = merge_delta_part<Cells, kNP>(g, bm, ch, cells, from, to, tid, kCcThreads, warp == 0,
+                                                                [](int32_t) {}, keys_seen);
+            if (lane == 0) atomicAdd(reinterpret_cast<unsigned long long*>(&sh.big_acc), (unsigned long long)part);
+            __syncthreads();
+            if (tid == 0) {
+                sh.my_act[w] = sh.big_acc;
+                ++evals;
             }
         }
         cluster.sync();
@@ -278,49 +306,73 @@ __global__ void __launch_bounds__(kCcThreads, 1) k_carry_cluster(
                     };
                     int i = 0, nm = 0, c0 = 0, c1 = 0, c2 = 0;
                     int pr = -1;  // rank of the put-back list's head, or -1
+                    // candidate i's fields in registers, the next one's loaded as i advances
+                    long long cd = 0, cact = 0;
+                    int32_t cb = 0, cto = 0, csrc = 0;
+                    auto load_c = [&]() {
+                        if (i < ncand) {
+                            cd = sh.c_dS[i];
+                            cb = sh.c_blk[i];
+                            cto = sh.c_to[i];
+                            csrc = sh.c_src[i];
+                            cact = sh.c_act[i];
+                        }
+                    };
+                    load_c();
+                    long long qd = 0;
+                    int32_t qb = 0;
                     while (merged0 + nm < num_to_merge) {
                         const bool hc = i < ncand, hq = pr >= 0;
                         if (!hc && !hq) break;  // queue empty
-                        const long long cd = hc ? sh.c_dS[i] : 0;
-                        const int32_t cb = hc ? sh.c_blk[i] : 0;
-                        const long long qd = hq ? sh.a_d[pr] : 0;
-                        const int32_t qb = hq ? sh.a_b[pr] : 0;
                         const bool fromq = hq && (!hc || qless(qd, qb, cd, cb));
                         const long long kd = fromq ? qd : cd;
                         const int32_t kb = fromq ? qb : cb;
                         if (hb && qless(bnd_dS, bnd_blk, kd, kb)) break;  // next pop not evaluated
-                        int ci;
                         if (fromq) {
                             // popped again: unless a merge since touched what it read, its value
-                            // is the one it was put back with
-                            ci = sh.a_c[pr];
+                            // is the one it was put back with, the smallest key left, so it merges
+                            const int ci = sh.a_c[pr];
                             if (bit_of(stl, ci)) break;
                             flip(pr);
                             pr = first();
-                        } else {
-                            if (bit_of(stl, i)) break;  // its value is stale: re-score it next round
-                            ci = i++;
-                            const int src = sh.c_src[ci];
-                            c0 += src == 0;
-                            c1 += src == 1;
-                            c2 += src == 2;
-                            if (sh.c_to[ci] == kb) continue;  // already in the same block
+                            if (pr >= 0) {
+                                qd = sh.a_d[pr];
+                                qb = sh.a_b[pr];
+                            }
+                            sh.m_from[nm] = kb;
+                            sh.m_to[nm] = sh.c_to[ci];
+#pragma unroll
+                            for (int w = 0; w < kCcWords; ++w) stl[w] |= sh.inv[ci][w];
+                            ++nm;
+                            continue;
                         }
-                        const long long act = sh.c_act[ci];
-                        const bool hc2 = i < ncand, hq2 = pr >= 0;
-                        if (hc2 || hq2 || hb) {
+                        if (bit_of(stl, i)) break;  // its value is stale: re-score it next round
+                        const int ci = i++;
+                        const long long act = cact;
+                        const int32_t to = cto;
+                        c0 += csrc == 0;
+                        c1 += csrc == 1;
+                        c2 += csrc == 2;
+                        load_c();
+                        if (to == kb) continue;  // already in the same block
+                        const bool hc2 = i < ncand;
+                        if (hc2 || hq || hb) {
                             long long top = hb ? bnd_dS : LLONG_MAX;
-                            if (hc2) top = min(top, sh.c_dS[i]);
-                            if (hq2) top = min(top, sh.a_d[pr]);
+                            if (hc2) top = min(top, cd);
+                            if (hq) top = min(top, qd);
                             if (act > top) {  // put back with the recomputed delta
                                 const int r = sh.a_rank[ci];
                                 flip(r);
-                                if (pr < 0 || r < pr) pr = r;
+                                if (pr < 0 || r < pr) {
+                                    pr = r;
+                                    qd = act;
+                                    qb = kb;
+                                }
                                 continue;
                             }
                         }
                         sh.m_from[nm] = kb;
-                        sh.m_to[nm] = sh.c_to[ci];
+                        sh.m_to[nm] = to;
 #pragma unroll
                         for (int w = 0; w < kCcWords; ++w) stl[w] |= sh.inv[ci][w];
                         ++nm;

@@ -111,6 +111,17 @@ __device__ __forceinline__ void bulk_append(int32_t* head, const DevChain& ch, i
         for (int i = threadIdx.x; i < n; i += blockDim.x) ch.pool[p + i] = buf[i];
 }
 
+// Number of keys in the appended chunks of a list starting at head (chunk headers only).
+__device__ __forceinline__ int32_t list_chunk_keys(int32_t head, const DevChain& ch) {
+    int32_t n = 0, c = head;
+    int guard = 0;
+    while (c >= 0 && guard++ < (1 << 20)) {
+        n += min(((volatile int32_t*)ch.pool)[c + 1], ((volatile int32_t*)ch.pool)[c + 2]);
+        c = ((volatile int32_t*)ch.pool)[c];
+    }
+    return n;
+}
+
 // Calls f(key) for every key held in the appended chunks of a list starting at head,
 // strided over threads t = 0..nt-1 of a team.
 template <typename F>
