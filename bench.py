@@ -260,19 +260,21 @@ def reference_arm(args):
 def profile_phase(args):
     """One phase of the same workload at a fixed block count, for profilers: the planted
     partition with every planted block split at random into sub-blocks (about --blocks
-    blocks in all), then either the merge pass to half as many blocks or --iterations
-    hybrid-MCMC iterations.  Prints a short JSON summary, not a bench line."""
+    blocks in all; the identity partition when --blocks is at least N), then either the
+    merge pass to half as many blocks or --iterations hybrid-MCMC iterations.  Prints a
+    short JSON summary with the per-kernel CUDA-event times, not a bench line."""
     import torch
     import sbp_gb300 as sb
     from sbp_gb300 import build as _b
     _b.build()
     src, dst, planted = sb.dcsbm.generate_config(CONFIG, seed=0)
     n = sb.dcsbm.CONFIGS[CONFIG]["num_vertices"]
-    a = split_planted(planted, n, args.blocks)
+    a = np.arange(n, dtype=np.int32) if args.blocks >= n else split_planted(planted, n, args.blocks)
     B = int(a.max()) + 1
     ctx = sb.Context(0)
     if args.cells_budget is not None:
         ctx.set_cells_budget(args.cells_budget)
+    ctx.set_timing(True)
     G = sb.Graph(n, src, dst, ctx=ctx)
     bm = sb.Blockmodel(B, G, 0.5, a)
     sargs = sb.Args(algorithm="hybrid_mcmc", seed=SEED, max_iterations=args.iterations)
@@ -284,7 +286,7 @@ def profile_phase(args):
         _, st = sb.finetune.mcmc(0, G, bm, True, sargs)
     ctx.synchronize()
     print(json.dumps({"phase": args.phase, "config": CONFIG, "blocks_before": B, "blocks_after": bm.num_blocks(),
-                      "seconds": time.perf_counter() - t0, "stats": st}))
+                      "seconds": time.perf_counter() - t0, "stats": st, "kernel_timing": ctx.read_timing()}))
 
 
 def mixed_graphs(count, n_lo, n_hi, seed_base=0):
@@ -424,7 +426,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end C ABI run (profiling)")
     ap.add_argument("--no-full-sbp", action="store_true", help="skip the whole-SBP run after the timed steps")
-    ap.add_argument("--config", default=CONFIG, choices=["C1", "C2", "C3"])
+    ap.add_argument("--config", default=CONFIG, choices=["C1", "C2", "C3", "C3S"])
     ap.add_argument("--cells-budget", type=int, default=None,
                     help="device bytes for the carry-out's dense cell counts (library default if unset)")
     ap.add_argument("--phase", default="sbp", choices=["sbp", "merge", "mcmc"],

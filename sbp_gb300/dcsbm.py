@@ -21,6 +21,9 @@ CONFIGS = {
     "C1": dict(num_vertices=1000, num_edges=8000, num_blocks=11, alpha=2.0, dmin=10, dmax=100, ratio=2.5),
     "C2": dict(num_vertices=50000, num_edges=1000000, num_blocks=33, alpha=2.0, dmin=10, dmax=100, ratio=2.5),
     "C3": dict(num_vertices=1000000, num_edges=20000000, num_blocks=100, alpha=0.5, dmin=5, dmax=500, ratio=1.5),
+    # the C3 shape at a fifth of its size: the case profiler captures run on (a full-set
+    # capture saves and restores device memory on every pass)
+    "C3S": dict(num_vertices=200000, num_edges=4000000, num_blocks=100, alpha=0.5, dmin=5, dmax=500, ratio=1.5),
 }
 
 
