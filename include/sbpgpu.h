@@ -78,9 +78,10 @@ const char* sbpgpu_last_error(const sbpgpu_ctx* ctx);
 sbpgpu_status sbpgpu_ctx_synchronize(sbpgpu_ctx* ctx);
 /* The CUDA stream (cudaStream_t) all work of the context is issued on. */
 void* sbpgpu_ctx_stream(sbpgpu_ctx* ctx);
-/* Device memory (bytes) the merge carry-out may hold for a dense num_blocks^2 int32 matrix
- * of cell counts; larger blockmodels use the hashed cell store.  Default 16 GiB; 0
- * always uses the hash.  Results do not depend on it.  No counterpart in the reference. */
+/* Device memory (bytes) the sequential phases (merge carry-out, windowed MH chain) may hold
+ * for dense num_blocks^2 int32 matrices of cell counts; larger blockmodels use the hashed
+ * cell store.  Default 64 GiB (a GB300 holds about 280 GB); 0 always uses the hash.
+ * Results do not depend on it.  No counterpart in the reference. */
 sbpgpu_status sbpgpu_ctx_set_cells_budget(sbpgpu_ctx* ctx, int64_t bytes);
 /* Smallest block count at which the sequential phases -- the Metropolis-Hastings chain and
  * the exact merge carry-out -- are evaluated in wide windows spread over a thread-block

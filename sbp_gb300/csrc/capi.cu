@@ -107,7 +107,7 @@ struct sbpgpu_ctx {
     cudaStream_t stream = nullptr;
     std::string err;
     bool timing = false;
-    int64_t cells_budget = int64_t(16) << 30;  // dense carry-out cells, bytes
+    int64_t cells_budget = int64_t(64) << 30;  // dense cells of the sequential phases, bytes
     int64_t cluster_blocks = 65536;             // smallest B whose sequential phases run on a cluster
     DevFlags* flags_host = nullptr;            // pinned staging of the device flags
     std::vector<TimedSpan> pending;

@@ -184,8 +184,12 @@ __global__ void __launch_bounds__(kClWarps * 32, 1)
     long long dsum = 0;
     int32_t it0 = 0;
     int guard = 0;
+    // entries evaluated per round: doubled while rounds are taken whole, else twice the last
+    // round's take (a round waits on its slowest evaluation, so entries past the likely stop
+    // cost time); the same value on every CTA
+    int wa = W;
     while (it0 < n && guard++ < (1 << 30)) {
-        const int wn = min(W, n - it0);
+        const int wn = min(wa, n - it0);
         const int j = rank * kClWarps + wid;  // this warp's window entry
         // ---- 1. evaluate
         if (j < wn) {
@@ -399,6 +403,7 @@ __global__ void __launch_bounds__(kClWarps * 32, 1)
             }
         }
         it0 += stop;
+        wa = stop >= wn ? min(W, 2 * wa) : min(W, max(2 * kClWarps, (2 * stop + kClWarps - 1) / kClWarps * kClWarps));
         cluster.sync();
     }
     if (rank == 0 && tid == 0) {
