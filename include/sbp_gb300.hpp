@@ -7,8 +7,16 @@
  *   Blockmodel                  include/blockmodel/blockmodel.hpp:46-219
  *   entropy::mdl, delta_mdl, block_merge_delta_mdl, null_mdl_v1, normalize_mdl_v1
  *                               include/entropy.hpp:33-81
- *   finetune::mcmc, asynchronous_gibbs, hybrid_mcmc, metropolis_hastings
+ *   finetune::mcmc, asynchronous_gibbs, hybrid_mcmc, metropolis_hastings, accept,
+ *   early_stop, edge_weights, blockmodel_delta, propose_move, move_vertex
  *                               include/finetune.hpp:36-157
+ *   EdgeWeights, VertexMove     include/typedefs.hpp:16-38, 124-129
+ *   utils::ProposalAndEdgeCounts
+ *                               include/utils.hpp:24-30
+ *   Delta                       include/blockmodel/sparse/delta.hpp:22-148
+ *   BlockMatrix (blockmatrix()) include/blockmodel/sparse/csparse_matrix.hpp:45-112
+ *   BlockmodelTriplet           include/blockmodel/blockmodel_triplet.hpp:12-42
+ *   sbp::done_blockmodeling     src/sbp.cpp:74-86
  *   block_merge::merge_blocks   include/block_merge.hpp:32-56
  *   sbp::stochastic_block_partition
  *                               include/sbp.hpp:18
@@ -19,9 +27,10 @@
  *
  * Differences from the reference, by design:
  *   - randomness comes from the seeded Philox stream (Args::seed), so runs repeat;
- *   - finetune::mcmc takes the golden-ratio flag directly instead of a
- *     BlockmodelTriplet, and block_merge::merge_blocks takes an optional step number
- *     that keys its proposal stream;
+ *   - finetune::mcmc takes the golden-ratio flag or a BlockmodelTriplet;
+ *     block_merge::merge_blocks, propose_move and move_vertex take optional
+ *     iteration/step numbers that key their proposal stream;
+ *   - blockmatrix() returns a read-only host snapshot, not the live device matrix;
  *   - delta_mdl / block_merge_delta_mdl take (block or vertex, proposal) instead of a
  *     Delta; batched forms score many moves per call.
  * Errors: invalid arguments throw std::invalid_argument (as the reference); device
@@ -35,7 +44,10 @@
 #include <cmath>
 #include <cstdint>
 #include <limits>
+#include <map>
 #include <memory>
+#include <random>
+#include <set>
 #include <stdexcept>
 #include <string>
 #include <tuple>
@@ -208,6 +220,106 @@ class Graph {
     sbpgpu_graph* h_ = nullptr;
 };
 
+/// EdgeWeights (include/typedefs.hpp:16-38): the far endpoint of each edge (or the block of
+/// each cell) and its weight.
+struct EdgeWeights {
+    std::vector<long> indices;
+    std::vector<long> values;
+};
+
+/// A read-only host snapshot of the block-edge-count matrix with the reference's
+/// ISparseMatrix query interface (include/blockmodel/sparse/csparse_matrix.hpp:45-112).
+/// Rows and columns iterate in ascending block order, the canonical order of this
+/// implementation.  Taken by Blockmodel::blockmatrix(); it does not follow later changes.
+class BlockMatrix {
+  public:
+    using SparseVector = std::map<long, long>;
+    BlockMatrix(long num_blocks, const std::vector<std::tuple<long, long, long>>& cells)
+        : rows_(num_blocks), cols_(num_blocks) {
+        for (const auto& c : cells) {
+            rows_[std::get<0>(c)][std::get<1>(c)] = std::get<2>(c);
+            cols_[std::get<1>(c)][std::get<0>(c)] = std::get<2>(c);
+            edges_ += std::get<2>(c);
+        }
+    }
+    long get(long row, long col) const {
+        check_index(row);
+        check_index(col);
+        const auto it = rows_[row].find(col);
+        return it == rows_[row].end() ? 0 : it->second;
+    }
+    std::vector<long> getrow(long row) const {
+        check_index(row);
+        std::vector<long> v(rows_.size(), 0);
+        for (const auto& e : rows_[row]) v[e.first] = e.second;
+        return v;
+    }
+    std::vector<long> getcol(long col) const {
+        check_index(col);
+        std::vector<long> v(cols_.size(), 0);
+        for (const auto& e : cols_[col]) v[e.first] = e.second;
+        return v;
+    }
+    const SparseVector& getrow_sparse(long row) const {
+        check_index(row);
+        return rows_[row];
+    }
+    const SparseVector& getcol_sparse(long col) const {
+        check_index(col);
+        return cols_[col];
+    }
+    /// Blocks with edges out of / into `block`, with the edge counts.
+    EdgeWeights outgoing_edges(long block) const { return weights(getrow_sparse(block)); }
+    EdgeWeights incoming_edges(long block) const { return weights(getcol_sparse(block)); }
+    /// Row and column of `block` summed per neighbouring block (neighbors_weights).
+    SparseVector neighbors_weights(long block) const {
+        SparseVector w = getrow_sparse(block);
+        for (const auto& e : getcol_sparse(block)) w[e.first] += e.second;
+        return w;
+    }
+    std::set<long> neighbors(long block) const {
+        std::set<long> n;
+        for (const auto& e : neighbors_weights(block)) n.insert(e.first);
+        return n;
+    }
+    long distinct_edges(long block) const { return (long)neighbors_weights(block).size(); }
+    std::vector<std::tuple<long, long, long>> entries() const {
+        std::vector<std::tuple<long, long, long>> out;
+        for (long r = 0; r < (long)rows_.size(); ++r)
+            for (const auto& e : rows_[r]) out.emplace_back(r, e.first, e.second);
+        return out;
+    }
+    long edges() const { return edges_; }
+    long trace() const {
+        long t = 0;
+        for (long b = 0; b < (long)rows_.size(); ++b) t += get(b, b);
+        return t;
+    }
+    /// Row sums (axis 0) or column sums (axis 1).
+    std::vector<long> sum(long axis = 0) const {
+        std::vector<long> out(rows_.size(), 0);
+        const auto& lines = axis == 0 ? rows_ : cols_;
+        for (long b = 0; b < (long)lines.size(); ++b)
+            for (const auto& e : lines[b]) out[b] += e.second;
+        return out;
+    }
+
+  private:
+    void check_index(long b) const {
+        if (b < 0 || b >= (long)rows_.size()) throw std::out_of_range("block index out of range");
+    }
+    static EdgeWeights weights(const SparseVector& v) {
+        EdgeWeights w;
+        for (const auto& e : v) {
+            w.indices.push_back(e.first);
+            w.values.push_back(e.second);
+        }
+        return w;
+    }
+    std::vector<SparseVector> rows_, cols_;
+    long edges_ = 0;
+};
+
 /// The blockmodel: assignment, block degrees and sizes, and the block-edge-count matrix,
 /// all on the device (Blockmodel::initialize_edge_counts, src/blockmodel/blockmodel.cpp:193-276).
 class Blockmodel {
@@ -227,11 +339,15 @@ class Blockmodel {
     /// here num_blocks must equal the number of vertices.
     Blockmodel(long num_blocks, const Graph& graph, double block_reduction_rate)
         : Blockmodel(num_blocks, graph, block_reduction_rate, range(graph.num_vertices())) {}
+    /// An empty Blockmodel (Blockmodel(), include/blockmodel/blockmodel.hpp): `empty` is
+    /// true and it holds no device state; used for the slots of a BlockmodelTriplet.
+    Blockmodel() : graph_(nullptr) { empty = true; }
     Blockmodel(Blockmodel&&) = default;
     Blockmodel& operator=(Blockmodel&&) = default;
 
     /// Blockmodel::copy (src/blockmodel/blockmodel.cpp:139-153), device to device.
     Blockmodel copy() const {
+        if (!h_) return Blockmodel();
         sbpgpu_bm* h = nullptr;
         check(sbpgpu_bm_copy(h_.get(), &h), ctx());
         Blockmodel b(graph_, rate_, h);
@@ -240,7 +356,7 @@ class Blockmodel {
         return b;
     }
 
-    long num_blocks() const { return (long)sbpgpu_bm_num_blocks(h_.get()); }
+    long num_blocks() const { return h_ ? (long)sbpgpu_bm_num_blocks(h_.get()) : 0; }
     const std::vector<long>& block_assignment() const { return view().assignment; }
     long block_assignment(long vertex) const { return view().assignment.at(vertex); }
     const std::vector<long>& degrees_out() const { return view().d_out; }
@@ -252,6 +368,7 @@ class Blockmodel {
     long block_size(long b) const { return view().sizes.at(b); }
     /// The non-zero cells of the blockmatrix, row-major ascending: (row, col, count).
     std::vector<std::tuple<long, long, long>> blockmatrix_cells() const {
+        if (!h_) throw std::logic_error("empty blockmodel");
         const int64_t nnz = sbpgpu_bm_nnz(h_.get());
         std::vector<int32_t> r(nnz), c(nnz);
         std::vector<int64_t> v(nnz);
@@ -261,6 +378,15 @@ class Blockmodel {
         for (int64_t i = 0; i < nnz; ++i) out[i] = std::make_tuple((long)r[i], (long)c[i], (long)v[i]);
         return out;
     }
+    /// Blockmodel::blockmatrix (include/blockmodel/blockmodel.hpp): a host snapshot of the
+    /// current block-edge-count matrix.
+    std::shared_ptr<const BlockMatrix> blockmatrix() const {
+        return std::make_shared<const BlockMatrix>(num_blocks(), blockmatrix_cells());
+    }
+    /// Blockmodel::block_size over all blocks (block_sizes()).
+    const std::vector<long>& block_sizes() const { return view().sizes; }
+    /// true for a Blockmodel slot of a BlockmodelTriplet that holds nothing yet.
+    bool empty = false;
     double getOverall_entropy() const { return entropy_; }
     void setOverall_entropy(double e) { entropy_ = e; }
     long getNum_blocks_to_merge() const { return num_blocks_to_merge_; }
@@ -287,6 +413,7 @@ class Blockmodel {
     }
     sbpgpu_ctx* ctx() const { return graph_->context().get(); }
     const View& view() const {
+        if (!h_) throw std::logic_error("empty blockmodel");
         if (!view_) {
             const long n = graph_->num_vertices(), B = num_blocks();
             std::vector<int32_t> a(n);
@@ -310,6 +437,140 @@ class Blockmodel {
     double entropy_ = std::numeric_limits<double>::max();
     long num_blocks_to_merge_ = 0;
     mutable std::shared_ptr<View> view_;
+};
+
+/// VertexMove (include/typedefs.hpp:124-129): the outcome of one proposed vertex move.
+struct VertexMove {
+    double delta_entropy;
+    bool did_move;
+    long vertex;
+    long proposed_block;
+};
+
+namespace utils {
+/// utils::ProposalAndEdgeCounts (include/utils.hpp:24-30): a proposed block and the edge
+/// counts of the vertex it was drawn for.
+struct ProposalAndEdgeCounts {
+    long proposal;
+    long num_out_neighbor_edges;
+    long num_in_neighbor_edges;
+    long num_neighbor_edges;
+};
+}  // namespace utils
+
+/// Delta (include/blockmodel/sparse/delta.hpp:22-148): the change to the cells of the rows
+/// and columns of current_block and proposed_block that one vertex move makes.  A cell is
+/// kept under the first of (row == current, row == proposed, col == current,
+/// col == proposed) that holds, as the reference files it; any other cell is a
+/// std::logic_error.  entries() lists the four groups in that order, each ascending.
+class Delta {
+  public:
+    Delta() = default;
+    Delta(long current_block, long proposed_block, long /*buckets*/ = 10)
+        : current_(current_block), proposed_(proposed_block) {}
+    void add(long row, long col, long value) { slot(row, col) += value; }
+    void sub(long row, long col, long value) { slot(row, col) -= value; }
+    long get(long row, long col) const {
+        const std::map<long, long>* m;
+        long key;
+        route(row, col, m, key);
+        const auto it = m->find(key);
+        return it == m->end() ? 0 : it->second;
+    }
+    std::vector<std::tuple<long, long, long>> entries() const {
+        std::vector<std::tuple<long, long, long>> out;
+        for (const auto& e : cur_row_) out.emplace_back(current_, e.first, e.second);
+        for (const auto& e : prop_row_) out.emplace_back(proposed_, e.first, e.second);
+        for (const auto& e : cur_col_) out.emplace_back(e.first, current_, e.second);
+        for (const auto& e : prop_col_) out.emplace_back(e.first, proposed_, e.second);
+        return out;
+    }
+    long self_edge_weight() const { return self_; }
+    void self_edge_weight(long weight) { self_ = weight; }
+    long current_block() const { return current_; }
+    long proposed_block() const { return proposed_; }
+
+  private:
+    void route(long row, long col, const std::map<long, long>*& m, long& key) const {
+        if (row == current_) m = &cur_row_, key = col;
+        else if (row == proposed_) m = &prop_row_, key = col;
+        else if (col == current_) m = &cur_col_, key = row;
+        else if (col == proposed_) m = &prop_col_, key = row;
+        else throw std::logic_error("Neither the row nor column are current_block or proposed_block.");
+    }
+    long& slot(long row, long col) {
+        const std::map<long, long>* m;
+        long key;
+        route(row, col, m, key);
+        return (*const_cast<std::map<long, long>*>(m))[key];
+    }
+    long current_ = -1, proposed_ = -1, self_ = 0;
+    std::map<long, long> cur_row_, prop_row_, cur_col_, prop_col_;
+};
+
+/// BlockmodelTriplet (include/blockmodel/blockmodel_triplet.hpp:12-42,
+/// src/blockmodel/blockmodel_triplet.cpp:4-105): the three blockmodels that bracket the
+/// golden-section search over block counts, in decreasing number of blocks.
+class BlockmodelTriplet {
+  public:
+    bool optimal_num_blocks_found = false;
+    Blockmodel& get(long i) { return blockmodels_[check(i)]; }
+    const Blockmodel& get(long i) const { return blockmodels_[check(i)]; }
+    /// Puts `blockmodel` (a copy) into its slot: the middle when it has the lowest
+    /// description length so far (the old middle moving up or down by block count), else
+    /// the upper or lower slot by its block count.
+    void update(Blockmodel& blockmodel) {
+        long index;
+        if (blockmodels_[1].empty) {
+            index = 1;
+        } else if (blockmodel.getOverall_entropy() <= blockmodels_[1].getOverall_entropy()) {
+            const long old_index = blockmodels_[1].num_blocks() > blockmodel.num_blocks() ? 0 : 2;
+            blockmodels_[old_index] = blockmodels_[1].copy();
+            index = 1;
+        } else {
+            index = blockmodels_[1].num_blocks() > blockmodel.num_blocks() ? 2 : 0;
+        }
+        blockmodels_[index] = blockmodel.copy();
+    }
+    /// true while the lower slot is empty (no bracket yet).
+    bool golden_ratio_not_reached() const { return blockmodels_[2].empty; }
+    bool is_done() {
+        if ((!get(0).empty && get(0).num_blocks() - get(2).num_blocks() == 2) ||
+            (get(0).empty && get(1).num_blocks() - get(2).num_blocks() == 1))
+            optimal_num_blocks_found = true;
+        return optimal_num_blocks_found;
+    }
+    /// The blockmodel the next merge pass starts from, with its number of blocks to merge:
+    /// half the middle's blocks before the bracket exists, else the golden-section point
+    /// of the wider side.
+    Blockmodel get_next_blockmodel(Blockmodel& old_blockmodel) {
+        old_blockmodel.setNum_blocks_to_merge(0);
+        update(old_blockmodel);
+        if (golden_ratio_not_reached()) {
+            Blockmodel next = get(1).copy();
+            next.setNum_blocks_to_merge((long)(next.num_blocks() * next.getBlock_reduction_rate()));
+            if (next.getNum_blocks_to_merge() == 0) optimal_num_blocks_found = true;
+            return next;
+        }
+        if (is_done()) return get(1).copy();
+        long index = 1;
+        if (get(0).empty && get(1).num_blocks() > get(2).num_blocks()) index = 1;
+        else if (upper_difference() >= lower_difference()) index = 0;
+        long next_try = get(index + 1).num_blocks();
+        next_try += (long)((get(index).num_blocks() - get(index + 1).num_blocks()) * 0.618);
+        Blockmodel next = get(index).copy();
+        next.setNum_blocks_to_merge(next.num_blocks() - next_try);
+        return next;
+    }
+    long lower_difference() const { return get(1).num_blocks() - get(2).num_blocks(); }
+    long upper_difference() const { return get(0).num_blocks() - get(1).num_blocks(); }
+
+  private:
+    static long check(long i) {
+        if (i < 0 || i >= 3) throw std::out_of_range("triplet index out of range");
+        return i;
+    }
+    Blockmodel blockmodels_[3];
 };
 
 namespace entropy {
@@ -409,6 +670,120 @@ inline Blockmodel& mcmc(int iteration, const Graph& graph, Blockmodel& blockmode
     blockmodel.setOverall_entropy(sbpgpu_bm_entropy(blockmodel.handle()));
     return blockmodel;
 }
+/// finetune::mcmc with a BlockmodelTriplet (src/finetune.cpp:754-771): the golden-ratio flag
+/// is the triplet's.
+inline Blockmodel& mcmc(int iteration, const Graph& graph, Blockmodel& blockmodel, BlockmodelTriplet& triplet,
+                        const Args& a = args) {
+    return mcmc(iteration, graph, blockmodel, triplet.golden_ratio_not_reached(), a);
+}
+
+/// finetune::accept (src/finetune.cpp:22-32): greedy takes dS < 0; otherwise a uniform
+/// draw from a host generator seeded by Args::seed against min(1, e^(-3 dS) H).  The
+/// device paths draw from the seeded Philox stream instead.
+inline bool accept(double delta_entropy, double hastings_correction, const Args& a = args) {
+    if (a.greedy) return delta_entropy < 0.0;
+    static std::mt19937_64 generator(a.seed);
+    const double p = std::uniform_real_distribution<double>(0.0, 1.0)(generator);
+    const double q = std::min(1.0, std::exp(-3.0 * delta_entropy) * hastings_correction);
+    return p <= q;
+}
+
+/// finetune::early_stop (src/finetune.cpp:265-283): stop on a zero last change, or when the
+/// mean of the last three changes falls below 5e-4 (no bracket yet) or 1e-4 of the
+/// initial description length.
+inline bool early_stop(long iteration, bool golden_ratio_not_reached, double initial_entropy,
+                       const std::vector<double>& delta_entropies) {
+    const size_t last = delta_entropies.size() - 1;
+    if (delta_entropies[last] == 0.0) return true;
+    if (iteration < 3) return false;
+    const double average = -(delta_entropies[last] + delta_entropies[last - 1] + delta_entropies[last - 2]) / 3.0;
+    return average < (golden_ratio_not_reached ? 5e-4 : 1e-4) * initial_entropy;
+}
+/// finetune::early_stop (src/finetune.cpp:285-294): the 1e-4 rule alone.
+inline bool early_stop(long iteration, double initial_entropy, const std::vector<double>& delta_entropies) {
+    if (iteration < 3) return false;
+    const size_t last = delta_entropies.size() - 1;
+    const double average = -(delta_entropies[last] + delta_entropies[last - 1] + delta_entropies[last - 2]) / 3.0;
+    return average < 1e-4 * initial_entropy;
+}
+
+/// finetune::edge_weights (src/finetune.cpp:419-430): the neighbours of `vertex`, weight 1
+/// each (the graph is unweighted).
+inline EdgeWeights edge_weights(const NeighborList& neighbors, long vertex, bool ignore_self = false) {
+    EdgeWeights w;
+    for (long u : neighbors.at(vertex)) {
+        if (ignore_self && u == vertex) continue;
+        w.indices.push_back(u);
+        w.values.push_back(1);
+    }
+    return w;
+}
+
+/// finetune::blockmodel_delta (src/finetune.cpp:201-235): the cell changes of moving
+/// `vertex` from current_block to proposed_block, on the host from the blockmodel's
+/// assignment.  A self edge counts once per direction into (proposed, proposed).
+inline Delta blockmodel_delta(long vertex, long current_block, long proposed_block, const EdgeWeights& out_edges,
+                              const EdgeWeights& in_edges, const Blockmodel& blockmodel) {
+    Delta delta(current_block, proposed_block);
+    const std::vector<long>& assignment = blockmodel.block_assignment();
+    for (size_t i = 0; i < out_edges.indices.size(); ++i) {
+        const long u = out_edges.indices[i], b = assignment.at(u), w = out_edges.values[i];
+        if (u == vertex) {
+            delta.add(proposed_block, proposed_block, w);
+            delta.self_edge_weight(1);
+        } else {
+            delta.add(proposed_block, b, w);
+        }
+        delta.sub(current_block, b, w);
+    }
+    for (size_t i = 0; i < in_edges.indices.size(); ++i) {
+        const long u = in_edges.indices[i], b = assignment.at(u), w = in_edges.values[i];
+        if (u == vertex) {
+            delta.add(proposed_block, proposed_block, w);
+            delta.self_edge_weight(1);
+        } else {
+            delta.add(b, proposed_block, w);
+        }
+        delta.sub(b, current_block, w);
+    }
+    return delta;
+}
+
+/// finetune::propose_move (src/finetune.cpp:842-869) on the device: draws the proposal for
+/// `vertex` from the seeded stream keyed (vertex, iteration, step) -- the draw the
+/// sequential chain makes for it -- and runs move_vertex on it.  A vertex alone in its
+/// block gives delta_entropy = DBL_MAX and proposed_block = -1; a proposal equal to the
+/// current block gives 0 and -1.
+inline VertexMove propose_move(Blockmodel& blockmodel, long vertex, const Graph& graph, int iteration = 0,
+                               int step = 0, const Args& a = args) {
+    const sbpgpu_config cfg = to_config(a);
+    int32_t proposal = -1, moved = 0;
+    double dS = 0.0;
+    check(sbpgpu_propose_move(blockmodel.handle(), &cfg, (int32_t)vertex, a.seed, (uint32_t)iteration,
+                              (uint32_t)step, &proposal, &dS, &moved),
+          graph.context().get());
+    if (moved) blockmodel.invalidate();
+    return VertexMove{dS, moved != 0, proposal < 0 ? -1 : vertex, (long)proposal};
+}
+
+/// finetune::move_vertex (src/finetune.cpp:822-840) on the device: scores the move of
+/// `vertex` into proposal.proposal (with the Hastings correction when not greedy), decides
+/// with the accept rule on the seeded stream and applies an accepted move.  The vertex's
+/// edges are read from the device graph; out_edges and in_edges are accepted for the
+/// reference's signature and not read.
+inline VertexMove move_vertex(long vertex, long /*current_block*/, utils::ProposalAndEdgeCounts proposal,
+                              Blockmodel& blockmodel, const Graph& graph, EdgeWeights& /*out_edges*/,
+                              EdgeWeights& /*in_edges*/, int iteration = 0, int step = 0, const Args& a = args) {
+    const sbpgpu_config cfg = to_config(a);
+    int32_t moved = 0;
+    double dS = 0.0;
+    check(sbpgpu_move_vertex(blockmodel.handle(), &cfg, (int32_t)vertex, (int32_t)proposal.proposal, a.seed,
+                             (uint32_t)iteration, (uint32_t)step, &dS, &moved),
+          graph.context().get());
+    if (moved) blockmodel.invalidate();
+    return VertexMove{dS, moved != 0, vertex, proposal.proposal};
+}
+
 namespace detail {
 inline Blockmodel& run(const char* algorithm, Blockmodel& bm, const Graph& g, bool golden, int iteration) {
     Args a = args;
@@ -450,6 +825,12 @@ inline Blockmodel& merge_blocks(Blockmodel& blockmodel, const Graph& graph, long
 }  // namespace block_merge
 
 namespace sbp {
+
+/// sbp::done_blockmodeling (src/sbp.cpp:74-86).
+inline bool done_blockmodeling(Blockmodel& blockmodel, BlockmodelTriplet& triplet, long min_num_blocks = 0) {
+    if (min_num_blocks > 0 && (blockmodel.num_blocks() <= min_num_blocks || !triplet.get(2).empty)) return true;
+    return triplet.optimal_num_blocks_found;
+}
 
 /// sbp::stochastic_block_partition (src/sbp.cpp:16-72): the golden-section search over
 /// block counts with merge passes and MCMC, all on the device.

@@ -195,6 +195,23 @@ sbpgpu_status sbpgpu_gibbs_batch(sbpgpu_bm* bm, const sbpgpu_config* cfg, int64_
  * before the next proposal (finetune::propose_move / move_vertex, src/finetune.cpp:822-869). */
 sbpgpu_status sbpgpu_mh_chain(sbpgpu_bm* bm, const sbpgpu_config* cfg, int64_t n, const int32_t* vertex,
                               uint64_t seed, uint32_t iteration, uint32_t step, int64_t* applied);
+/* finetune::propose_move (src/finetune.cpp:842-869) for one vertex: the proposal drawn from
+ * the canonical stream (vertex, iteration, step, MH domain) -- the draw the chain above
+ * makes for that vertex -- then finetune::move_vertex on it.  *out_proposal is -1 when the
+ * vertex's block is a singleton (*out_dS = DBL_MAX) or the proposal is its own block
+ * (*out_dS = 0); *out_moved tells whether the move was applied.  Calling it for a sequence
+ * of vertices gives the same state as sbpgpu_mh_chain on that sequence. */
+sbpgpu_status sbpgpu_propose_move(sbpgpu_bm* bm, const sbpgpu_config* cfg, int32_t vertex, uint64_t seed,
+                                  uint32_t iteration, uint32_t step, int32_t* out_proposal, double* out_dS,
+                                  int32_t* out_moved);
+/* finetune::move_vertex (src/finetune.cpp:822-840): scores moving `vertex` into `proposal`
+ * against the current state (entropy::delta_mdl or its nonparametric form; the Hastings
+ * correction when not greedy), decides with finetune::accept -- greedy: dS < 0; otherwise
+ * the uniform draw of (vertex, iteration, step, MH domain) against min(1, e^(-3 dS) H) --
+ * and, when accepted, applies the move (Blockmodel::move_vertex) and rebuilds. */
+sbpgpu_status sbpgpu_move_vertex(sbpgpu_bm* bm, const sbpgpu_config* cfg, int32_t vertex, int32_t proposal,
+                                 uint64_t seed, uint32_t iteration, uint32_t step, double* out_dS,
+                                 int32_t* out_moved);
 /* finetune::mcmc (src/finetune.cpp:754-771) dispatching to asynchronous_gibbs (:34-107),
  * hybrid_mcmc (:563-646) or metropolis_hastings (:773-820). */
 sbpgpu_status sbpgpu_mcmc(sbpgpu_bm* bm, const sbpgpu_config* cfg, uint64_t seed, int32_t step,

@@ -124,6 +124,10 @@ SIGNATURES = {
                                           ctypes.c_uint32, ctypes.c_uint32, i32p, i64p]),
     "sbpgpu_mh_chain": (ctypes.c_int, [vp, ctypes.POINTER(Config), ctypes.c_int64, i32p, ctypes.c_uint64,
                                        ctypes.c_uint32, ctypes.c_uint32, i64p]),
+    "sbpgpu_propose_move": (ctypes.c_int, [vp, ctypes.POINTER(Config), ctypes.c_int32, ctypes.c_uint64,
+                                           ctypes.c_uint32, ctypes.c_uint32, i32p, f64p, i32p]),
+    "sbpgpu_move_vertex": (ctypes.c_int, [vp, ctypes.POINTER(Config), ctypes.c_int32, ctypes.c_int32,
+                                          ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32, f64p, i32p]),
     "sbpgpu_mcmc": (ctypes.c_int, [vp, ctypes.POINTER(Config), ctypes.c_uint64, ctypes.c_int32, ctypes.c_int32,
                                    ctypes.POINTER(Stats)]),
     "sbpgpu_merge_blocks": (ctypes.c_int, [vp, ctypes.POINTER(Config), ctypes.c_uint64, ctypes.c_int32,

@@ -148,7 +148,7 @@ __global__ void k_np_mdl(DevGraph g, DevBM bm, unsigned long long* __restrict__ 
 
 template <bool kNP>
 __global__ void k_vertex_dS_batch(DevGraph g, DevBM bm, const int32_t* __restrict__ vs, const int32_t* __restrict__ ss,
-                                  int64_t n, int log2cap, long long* __restrict__ out) {
+                                  int64_t n, int log2cap, long long* __restrict__ out, double* __restrict__ hout) {
     extern __shared__ int32_t sh[];
     __shared__ long long red[32][8];
     const int cap = 1 << log2cap;
@@ -162,6 +162,15 @@ __global__ void k_vertex_dS_batch(DevGraph g, DevBM bm, const int32_t* __restric
             d = vertex_delta_fixed<kT, CsrAcc, kNP>(g, bm.asg, bm.d_out, bm.d_in, CsrAcc{bm}, v, r, s, hk, hO, hI,
                                                     log2cap, red, bm.sizes, kNP ? *bm.nonempty : 0);
         if (threadIdx.x == 0) out[i] = d;
+        if (hout && !kNP) {  // entropy::hastings_correction over the neighbour hash just filled
+            double H = 1.0;
+            const int32_t o0 = __ldg(g.out_off + v), i0 = __ldg(g.inns_off + v);
+            const int32_t kout = __ldg(g.out_off + v + 1) - o0, kin = __ldg(g.inns_off + v + 1) - i0;
+            if (s != r && kout + kin > 0)
+                H = hastings_fixed<kT>(CsrAcc{bm}, [&](int32_t b) { return bm.d_tot[b]; }, bm.d_out, bm.d_in, bm.B, r,
+                                       s, kout, kin, __ldg(g.selfcnt + v), hk, hO, hI, log2cap, red);
+            if (threadIdx.x == 0) hout[i] = H;
+        }
         __syncthreads();
     }
 }
@@ -323,7 +332,7 @@ void launch_np_mdl(const DevGraph& g, const DevBM& bm, Work& w, cudaStream_t st)
 }
 
 void launch_vertex_dS_batch(const DevGraph& g, const DevBM& bm, const int32_t* v, const int32_t* s, int64_t n,
-                            int32_t max_k, long long* out, Work& w, cudaStream_t st, bool np) {
+                            int32_t max_k, long long* out, Work& w, cudaStream_t st, bool np, double* hastings) {
     if (n <= 0) return;
     if (np && (!g.LG || !g.Dm || !g.Dp)) throw std::logic_error("nonparametric tables missing");
     int log2cap = ceil_log2((uint64_t)(2 * (max_k > 16 ? max_k : 16)));
@@ -333,10 +342,10 @@ void launch_vertex_dS_batch(const DevGraph& g, const DevBM& bm, const int32_t* v
                                     " needs more shared memory for its neighbour hash than a block has");
     if (np) {
         allow_max_dynamic_smem((const void*)k_vertex_dS_batch<true>);
-        k_vertex_dS_batch<true><<<grid_for(n, 1), kT, smem, st>>>(g, bm, v, s, n, log2cap, out);
+        k_vertex_dS_batch<true><<<grid_for(n, 1), kT, smem, st>>>(g, bm, v, s, n, log2cap, out, nullptr);
     } else {
         allow_max_dynamic_smem((const void*)k_vertex_dS_batch<false>);
-        k_vertex_dS_batch<false><<<grid_for(n, 1), kT, smem, st>>>(g, bm, v, s, n, log2cap, out);
+        k_vertex_dS_batch<false><<<grid_for(n, 1), kT, smem, st>>>(g, bm, v, s, n, log2cap, out, hastings);
     }
     count_launches(1);
 }

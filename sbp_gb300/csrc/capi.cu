@@ -1040,6 +1040,57 @@ sbpgpu_status merge_delta_batch_impl(sbpgpu_bm* bm, int64_t n, const int32_t* bl
     });
 }
 
+// finetune::move_vertex (finetune.cpp:822-840) for one vertex and a given proposal: the delta
+// (and, non-greedy, the Hastings correction) against the current state, finetune::accept
+// with the canonical draw of (vertex, iteration, step, DOM_MH) -- word 3, as the chains use
+// it -- and, when accepted, the move applied and the blockmodel rebuilt.
+void move_one(sbpgpu_bm* bm, const sbpgpu_config& cfg, int32_t v, int32_t s, uint64_t seed, uint32_t iteration,
+              uint32_t step, double* out_dS, int32_t* out_moved) {
+    sbpgpu_graph* g = bm->g;
+    const bool np = cfg.nonparametric != 0, greedy = cfg.greedy != 0 && !np;
+    if (np) ensure_np(g);
+    const int32_t max_k = g->kdeg[v];
+    if (max_k > 8192) throw ApiError(SBPGPU_EUNSUPPORTED, "vertex degree above 8192");
+    cudaStream_t st = g->ctx->stream;
+    std::vector<void*> tmp;
+    int32_t* dv = dalloc<int32_t>(tmp, 2);
+    long long* ddS = dalloc<long long>(tmp, 1);
+    double* dH = dalloc<double>(tmp, 1);
+    long long dS_fixed = 0;
+    double H = 1.0;
+    try {
+        const int32_t pair[2] = {v, s};
+        CK(cudaMemcpyAsync(dv, pair, 8, cudaMemcpyHostToDevice, st));
+        launch_vertex_dS_batch(g->dg, bm->d, dv, dv + 1, 1, max_k, ddS, g->w, st, np, greedy || np ? nullptr : dH);
+        CK(cudaMemcpyAsync(&dS_fixed, ddS, 8, cudaMemcpyDeviceToHost, st));
+        if (!greedy && !np) CK(cudaMemcpyAsync(&H, dH, 8, cudaMemcpyDeviceToHost, st));
+        check_flags(g);
+    } catch (...) {
+        free_all(tmp, st);
+        throw;
+    }
+    free_all(tmp, st);
+    const double dS = (double)dS_fixed * (1.0 / 16777216.0);
+    bool accepted;
+    if (greedy) {
+        accepted = dS_fixed < 0;
+    } else {
+        uint32_t w[4];
+        philox_host((uint32_t)v, iteration, step, DOM_MH, seed, w);
+        const double u = (double)w[3] * (1.0 / 4294967296.0);
+        double p = std::exp(-3.0 * dS) * H;
+        p = p >= 1.0 ? 1.0 : p;
+        accepted = u <= p;
+    }
+    if (accepted) {
+        CK(cudaMemcpyAsync(bm->d.asg + v, &s, 4, cudaMemcpyHostToDevice, st));
+        do_rebuild(bm);
+        host_wait(st);
+    }
+    if (out_dS) *out_dS = dS;
+    if (out_moved) *out_moved = accepted ? 1 : 0;
+}
+
 }  // namespace
 
 // ====================================================================== C ABI
@@ -1800,6 +1851,63 @@ sbpgpu_status sbpgpu_mh_chain(sbpgpu_bm* bm, const sbpgpu_config* cfg, int64_t n
         check_flags(g);
         if (applied) *applied = (int64_t)g->flags_host->counters[5];
         reset_counters(g);
+        return SBPGPU_OK;
+    });
+}
+
+sbpgpu_status sbpgpu_move_vertex(sbpgpu_bm* bm, const sbpgpu_config* cfg, int32_t vertex, int32_t proposal,
+                                 uint64_t seed, uint32_t iteration, uint32_t step, double* out_dS,
+                                 int32_t* out_moved) {
+    if (!bm || !cfg) return SBPGPU_EINVAL;
+    sbpgpu_graph* g = bm->g;
+    return guarded(g->ctx, [&] {
+        if (vertex < 0 || vertex >= g->N || proposal < 0 || proposal >= bm->d.B)
+            throw ApiError(SBPGPU_EINVAL, "vertex or proposal out of range");
+        reset_counters(g);
+        move_one(bm, *cfg, vertex, proposal, seed, iteration, step, out_dS, out_moved);
+        return SBPGPU_OK;
+    });
+}
+
+sbpgpu_status sbpgpu_propose_move(sbpgpu_bm* bm, const sbpgpu_config* cfg, int32_t vertex, uint64_t seed,
+                                  uint32_t iteration, uint32_t step, int32_t* out_proposal, double* out_dS,
+                                  int32_t* out_moved) {
+    if (!bm || !cfg) return SBPGPU_EINVAL;
+    sbpgpu_graph* g = bm->g;
+    return guarded(g->ctx, [&] {
+        if (vertex < 0 || vertex >= g->N) throw ApiError(SBPGPU_EINVAL, "vertex out of range");
+        if (bm->d.B < 2) throw ApiError(SBPGPU_EINVAL, "proposals need at least two blocks");
+        cudaStream_t st = g->ctx->stream;
+        int32_t r = 0, size = 0;
+        CK(cudaMemcpyAsync(&r, bm->d.asg + vertex, 4, cudaMemcpyDeviceToHost, st));
+        host_wait(st);
+        CK(cudaMemcpyAsync(&size, bm->d.sizes + r, 4, cudaMemcpyDeviceToHost, st));
+        host_wait(st);
+        int32_t s = -1;
+        double dS = 0.0;
+        int32_t moved = 0;
+        if (size == 1) {  // a singleton block never moves (finetune.cpp:845-847)
+            dS = DBL_MAX;
+        } else {
+            std::vector<void*> tmp;
+            int32_t* dv = dalloc<int32_t>(tmp, 1);
+            int32_t* dp = dalloc<int32_t>(tmp, 1);
+            try {
+                CK(cudaMemcpyAsync(dv, &vertex, 4, cudaMemcpyHostToDevice, st));
+                launch_propose_batch(g->dg, bm->d, dv, 1, seed, iteration, step, DOM_MH, dp, st);
+                CK(cudaMemcpyAsync(&s, dp, 4, cudaMemcpyDeviceToHost, st));
+                check_flags(g);
+            } catch (...) {
+                free_all(tmp, st);
+                throw;
+            }
+            free_all(tmp, st);
+            if (s == r) s = -1;  // proposal equal to the current block: no move (finetune.cpp:863-865)
+            else move_one(bm, *cfg, vertex, s, seed, iteration, step, &dS, &moved);
+        }
+        if (out_proposal) *out_proposal = s;
+        if (out_dS) *out_dS = dS;
+        if (out_moved) *out_moved = moved;
         return SBPGPU_OK;
     });
 }

@@ -81,8 +81,10 @@ void launch_mdl(const DevGraph& g, const DevBM& bm, Work& w, cudaStream_t st);
 // w.d_acc[0]: -sum LG[cell] + sum over blocks (vterm - LG[size]).
 void launch_np_mdl(const DevGraph& g, const DevBM& bm, Work& w, cudaStream_t st);
 // np: nonparametric deltas (the graph's nonparametric tables must exist).
+// hastings (optional, not with np): entropy::hastings_correction of each pair.
 void launch_vertex_dS_batch(const DevGraph& g, const DevBM& bm, const int32_t* v, const int32_t* s, int64_t n,
-                            int32_t max_k, long long* out, Work& w, cudaStream_t st, bool np = false);
+                            int32_t max_k, long long* out, Work& w, cudaStream_t st, bool np = false,
+                            double* hastings = nullptr);
 void launch_merge_dS_batch(const DevGraph& g, const DevBM& bm, const int32_t* r, const int32_t* s, int64_t n,
                            long long* out, Work& w, cudaStream_t st, bool np = false);
 void launch_propose_batch(const DevGraph& g, const DevBM& bm, const int32_t* v, int64_t n, uint64_t seed,

@@ -80,3 +80,35 @@ def mh_chain(blockmodel, vertices, seed, iteration, step, args=None):
                                                             int(seed), int(iteration), int(step),
                                                             ctypes.byref(applied)))
     return applied.value
+
+
+def propose_move(blockmodel, vertex, graph=None, args=None, iteration=0, step=0):
+    """finetune::propose_move (src/finetune.cpp:842-869): the canonical MH proposal for one
+    vertex, scored and accepted as the chain does, applied when accepted.  Returns the
+    reference's VertexMove as (delta_entropy, did_move, vertex, proposed_block); vertex and
+    block are -1 when nothing was proposed."""
+    a = args or Args()
+    cfg = a.config()
+    prop = ctypes.c_int32()
+    dS = ctypes.c_double()
+    moved = ctypes.c_int32()
+    blockmodel.ctx.check(blockmodel.ctx.lib.sbpgpu_propose_move(blockmodel.h, ctypes.byref(cfg), int(vertex),
+                                                                int(a.seed), int(iteration), int(step),
+                                                                ctypes.byref(prop), ctypes.byref(dS),
+                                                                ctypes.byref(moved)))
+    p = prop.value
+    return dS.value, bool(moved.value), (int(vertex) if p >= 0 else -1), p
+
+
+def move_vertex(vertex, proposal, blockmodel, graph=None, args=None, iteration=0, step=0):
+    """finetune::move_vertex (src/finetune.cpp:822-840) for a given proposal.  Returns
+    (delta_entropy, did_move, vertex, proposed_block)."""
+    a = args or Args()
+    cfg = a.config()
+    dS = ctypes.c_double()
+    moved = ctypes.c_int32()
+    blockmodel.ctx.check(blockmodel.ctx.lib.sbpgpu_move_vertex(blockmodel.h, ctypes.byref(cfg), int(vertex),
+                                                               int(proposal), int(a.seed), int(iteration), int(step),
+                                                               ctypes.byref(dS), ctypes.byref(moved)))
+    return dS.value, bool(moved.value), int(vertex), int(proposal)
+

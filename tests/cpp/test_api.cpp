@@ -147,6 +147,115 @@ static void toy_known_answers(const Toy& t) {
     EXPECT(std::fabs(s::entropy::normalize_mdl_v1(mdl, graph) * s::entropy::null_mdl_v1(graph) - mdl) < 1e-9 * mdl);
 }
 
+// The per-vertex boundary and the host-side types: blockmatrix() snapshot, Delta,
+// blockmodel_delta, early_stop, edge_weights, propose_move / move_vertex, BlockmodelTriplet
+// and done_blockmodeling (test/finetune_test.cpp, test/blockmodel_triplet_test.cpp).
+static void boundary_api(const Toy& t) {
+    s::Graph graph(t.n, t.edges);
+    s::Blockmodel bm(t.B, graph, 0.5, t.assignment);
+
+    const auto m = bm.blockmatrix();
+    EXPECT(m->entries() == bm.blockmatrix_cells());
+    EXPECT(m->edges() == t.e);
+    EXPECT(m->sum(0) == t.dout);
+    EXPECT(m->sum(1) == t.din);
+    long cells = 0;
+    for (long r = 0; r < t.B; ++r)
+        for (long c = 0; c < t.B; ++c) cells += m->get(r, c);
+    EXPECT(cells == t.e);
+
+    // Delta of moving vertex 7 to block 0 equals the change of the block matrix
+    const long v = 7, to = 0, from = t.assignment[v];
+    const s::EdgeWeights out = s::finetune::edge_weights(graph.out_neighbors(), v);
+    const s::EdgeWeights in = s::finetune::edge_weights(graph.in_neighbors(), v);
+    EXPECT((long)out.indices.size() == (long)graph.out_neighbors(v).size());
+    const s::Delta delta = s::finetune::blockmodel_delta(v, from, to, out, in, bm);
+    std::vector<long> moved = t.assignment;
+    moved[v] = to;
+    s::Blockmodel bm2(t.B, graph, 0.5, moved);
+    const auto m2 = bm2.blockmatrix();
+    long changed = 0;
+    for (long r = 0; r < t.B; ++r)
+        for (long c = 0; c < t.B; ++c)
+            if (m2->get(r, c) != m->get(r, c)) ++changed;
+    long listed = 0;
+    for (const auto& e : delta.entries()) {
+        const long r = std::get<0>(e), c = std::get<1>(e), d = std::get<2>(e);
+        EXPECT(m2->get(r, c) - m->get(r, c) == d);
+        EXPECT(delta.get(r, c) == d);
+        if (d != 0) ++listed;
+    }
+    EXPECT(listed == changed);
+    bool threw = false;
+    try {
+        s::Delta d2(1, 2);
+        d2.add(3, 4, 1);
+    } catch (const std::logic_error&) {
+        threw = true;
+    }
+    EXPECT(threw);
+
+    // early_stop: zero change stops; three small changes stop; large changes continue
+    EXPECT(s::finetune::early_stop(1, true, 100.0, std::vector<double>{-5.0, 0.0}));
+    EXPECT(!s::finetune::early_stop(4, true, 100.0, std::vector<double>{-5.0, -5.0, -5.0}));
+    EXPECT(s::finetune::early_stop(4, true, 100.0, std::vector<double>{-0.01, -0.01, -0.01}));
+    EXPECT(!s::finetune::early_stop(4, 100.0, std::vector<double>{-0.02, -0.02, -0.02}));
+    EXPECT(s::finetune::early_stop(4, 100.0, std::vector<double>{-0.005, -0.005, -0.005}));
+    s::Args g;
+    g.greedy = true;
+    EXPECT(s::finetune::accept(-1.0, 1.0, g) && !s::finetune::accept(0.5, 1.0, g));
+
+    // move_vertex on a given proposal: the delta-MDL of the entropy interface, applied iff negative
+    s::Blockmodel c = bm.copy();
+    const double want = s::entropy::delta_mdl(bm, v, to);
+    s::utils::ProposalAndEdgeCounts proposal{to, (long)out.indices.size(), (long)in.indices.size(),
+                                             (long)(out.indices.size() + in.indices.size())};
+    s::EdgeWeights o2 = out, i2 = in;
+    const s::VertexMove mv = s::finetune::move_vertex(v, from, proposal, c, graph, o2, i2, 0, 0, g);
+    EXPECT(mv.delta_entropy == want && mv.did_move == (want < 0) && mv.vertex == v && mv.proposed_block == to);
+    EXPECT(c.block_assignment(v) == (mv.did_move ? to : from));
+    // propose_move over every vertex: each applied move changes the MDL by its delta
+    s::Args h;
+    h.seed = 11;
+    for (long u = 0; u < t.n; ++u) {
+        const double before = s::entropy::mdl(c, graph);
+        const s::VertexMove pm = s::finetune::propose_move(c, u, graph, 2, 1, h);
+        if (pm.did_move) {
+            EXPECT(pm.vertex == u && c.block_assignment(u) == pm.proposed_block);
+            EXPECT(std::fabs(s::entropy::mdl(c, graph) - before - pm.delta_entropy) < 1e-5);
+        } else if (pm.proposed_block == -1) {
+            EXPECT(pm.vertex == -1);
+        }
+    }
+
+    // BlockmodelTriplet: the bracket forms as blockmodels with fewer blocks arrive
+    s::BlockmodelTriplet triplet;
+    EXPECT(triplet.golden_ratio_not_reached() && triplet.get(0).empty && triplet.get(1).empty);
+    s::Blockmodel b1 = bm.copy();
+    b1.setOverall_entropy(100.0);
+    s::Blockmodel next = triplet.get_next_blockmodel(b1);
+    EXPECT(!triplet.get(1).empty && triplet.get(1).num_blocks() == t.B);
+    EXPECT(next.num_blocks() == t.B && next.getNum_blocks_to_merge() == (long)(t.B * 0.5));
+    EXPECT(!s::sbp::done_blockmodeling(next, triplet));
+    std::vector<long> two = t.assignment;
+    for (auto& x : two) x = x % 2;
+    s::Blockmodel b2(2, graph, 0.5, two);
+    b2.setOverall_entropy(120.0);  // worse than the middle: goes below it
+    triplet.update(b2);
+    EXPECT(!triplet.golden_ratio_not_reached() && triplet.get(2).num_blocks() == 2);
+    EXPECT(triplet.lower_difference() == t.B - 2);
+    EXPECT(s::sbp::done_blockmodeling(b2, triplet, 2));
+    s::finetune::mcmc(0, graph, b2, triplet, g);
+    EXPECT(b2.num_blocks() == 2);
+    threw = false;
+    try {
+        triplet.get(3);
+    } catch (const std::out_of_range&) {
+        threw = true;
+    }
+    EXPECT(threw);
+}
+
 static void full_partition(const char* graph_path, uint64_t seed, const char* out_path) {
     std::ifstream f(graph_path);
     long n = 0, e = 0;
@@ -192,7 +301,9 @@ int main(int argc, char** argv) {
         return 2;
     }
     try {
-        toy_known_answers(read_toy(argv[1]));
+        const Toy toy = read_toy(argv[1]);
+        toy_known_answers(toy);
+        boundary_api(toy);
         full_partition(argv[2], std::stoull(argv[3]), argv[4]);
     } catch (const std::exception& ex) {
         std::fprintf(stderr, "unexpected exception: %s\n", ex.what());

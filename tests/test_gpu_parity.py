@@ -331,3 +331,50 @@ def test_full_sbp_identical_c2(gpu, oracle):
     assert np.array_equal(a_g, a_o)
     assert abs(mdl_g - mdl_o) <= MDL_REL_TOL_CANONICAL * abs(mdl_o)
     assert st["merges"] == ost.merges and st["proposals"] == ost.proposals
+
+
+# ---- the per-vertex boundary (finetune::propose_move / move_vertex, finetune.cpp:822-869):
+# called vertex by vertex it walks the same chain as the sequential kernel and the oracle.
+
+@pytest.mark.parametrize("B,greedy", [(120, True), (1500, True), (120, False), (1500, False)])
+def test_propose_move_walks_the_chain(gpu, oracle, B, greedy):
+    G, O, gb, ob, a, _ = make_pair(gpu, oracle, 2500, 30000, 9, B, seed=170 + B)
+    order = np.random.default_rng(B + 1).permutation(2500)[:300].astype(np.int32)
+    args = gpu.Args(algorithm="hybrid_mcmc", seed=8, greedy=greedy)
+    moved = 0
+    for v in order:
+        dS, did, vv, p = gpu.finetune.propose_move(gb, int(v), G, args, iteration=1, step=3)
+        assert (vv == -1) == (p == -1)
+        if did:
+            moved += 1
+            assert vv == v and p >= 0
+    want = ob.mh_chain(order, 8, 1, 3, oracle.make_config("hybrid_mcmc", greedy=greedy))
+    assert moved == want
+    same_state(gb, ob)
+
+
+def test_move_vertex_scores_and_applies(gpu, oracle):
+    """Greedy move_vertex on given proposals: the oracle's delta-MDL bit for bit, applied
+    exactly when it is negative, the state the oracle reaches by the same moves."""
+    n, B = 2500, 300
+    G, O, gb, ob, a, _ = make_pair(gpu, oracle, n, 30000, 9, B, seed=180)
+    rng = np.random.default_rng(3)
+    args = gpu.Args(algorithm="hybrid_mcmc", seed=4)
+    moves = 0
+    for _ in range(120):
+        v, p = int(rng.integers(n)), int(rng.integers(B))
+        d = ob.read()
+        if d["sizes"][d["assignment"][v]] == 1:
+            continue  # the oracle's apply refuses to empty a block
+        want = ob.delta_mdl(v, p)[0]
+        dS, did, vv, pp = gpu.finetune.move_vertex(v, p, gb, G, args)
+        assert dS == want and (vv, pp) == (v, p)
+        assert did == (want < 0)
+        if did:
+            m = np.full(n, -1, np.int32)
+            m[v] = p
+            ob.apply_moves(m)
+            moves += 1
+            same_state(gb, ob)
+    assert moves > 0
+    same_state(gb, ob)
