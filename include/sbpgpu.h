@@ -25,7 +25,8 @@ typedef enum sbpgpu_status {
     SBPGPU_ENOMEM = 2,    /* device allocation failed */
     SBPGPU_ETIMEOUT = 3,  /* a bounded device-side wait ran out */
     SBPGPU_EDEVICE = 4,   /* CUDA runtime error or a device-side consistency check failed */
-    SBPGPU_EUNSUPPORTED = 5
+    SBPGPU_EUNSUPPORTED = 5,
+    SBPGPU_ECANCELED = 6  /* the call was cancelled (sbpgpu_ctx_set_cancel, sbpgpu_server_cancel) */
 } sbpgpu_status;
 
 typedef struct sbpgpu_ctx sbpgpu_ctx;
@@ -89,6 +90,17 @@ sbpgpu_status sbpgpu_ctx_set_cells_budget(sbpgpu_ctx* ctx, int64_t bytes);
  * has more than 128 blocks).  Results do not depend on it.  No counterpart in the
  * reference. */
 sbpgpu_status sbpgpu_ctx_set_cluster_blocks(sbpgpu_ctx* ctx, int64_t min_blocks);
+/* Requests (requested != 0) or withdraws cancellation of the context's running
+ * sbpgpu_sbp; safe to call from another thread.  The partition checks the request between
+ * golden-section steps, when none of its work is in flight on the device, withdraws it and
+ * returns SBPGPU_ECANCELED; the context stays usable.  A request made while no partition
+ * runs cancels the next one at its first step.  No counterpart in the reference. */
+sbpgpu_status sbpgpu_ctx_set_cancel(sbpgpu_ctx* ctx, int32_t requested);
+/* Failure injection for tests of the error paths: after `after` more device allocations
+ * through the context, the next one fails as a failed cudaMallocAsync does (the call
+ * returns SBPGPU_ENOMEM and the context stays usable); negative: no injection (default).
+ * Nothing reaches the device.  No counterpart in the reference. */
+sbpgpu_status sbpgpu_ctx_inject_alloc_failure(sbpgpu_ctx* ctx, int64_t after);
 
 /* ---- graph: replaces Graph(out_neighbors, in_neighbors, ...) (include/graph.hpp:29-60)
  * and Graph::add_edge (src/graph.cpp:10-18).  Directed edges in input order; self-loops
@@ -305,7 +317,7 @@ sbpgpu_status sbpgpu_partition_scores(int64_t num_vertices, int64_t nrows, int64
  * each with its own context and stream, take jobs in submission order and run
  * sbpgpu_sbp on them concurrently.  A job is admitted while the estimated device footprint
  * (sbpgpu_job_footprint) of the jobs in flight plus its own stays within hbm_budget_bytes;
- * the first job in flight is always admitted.  Each worker's context uses
+ * a job whose own footprint exceeds the budget is refused at submission (SBPGPU_ENOMEM).  Each worker's context uses
  * cells_budget_bytes for dense cell counts (sbpgpu_ctx_set_cells_budget).  A job's result
  * equals sbpgpu_sbp of the same graph, configuration and seed run alone.  The job's host
  * arrays must stay valid until sbpgpu_server_wait returns for it.  Set the environment
@@ -338,6 +350,22 @@ sbpgpu_status sbpgpu_server_create(int32_t device, int32_t workers, int64_t hbm_
 sbpgpu_status sbpgpu_server_submit(sbpgpu_server* server, const sbpgpu_job* job, int64_t* ticket);
 /* Blocks until the job is done and returns its result (once per ticket). */
 sbpgpu_status sbpgpu_server_wait(sbpgpu_server* server, int64_t ticket, sbpgpu_job_result* result);
+/* As sbpgpu_server_wait, but returns SBPGPU_ETIMEOUT when the job is not done within
+ * timeout_ms; the ticket stays valid. */
+sbpgpu_status sbpgpu_server_wait_for(sbpgpu_server* server, int64_t ticket, int64_t timeout_ms,
+                                     sbpgpu_job_result* result);
+/* Cancels a job: a queued job is removed at once; a running one stops at its next
+ * golden-section step (sbpgpu_ctx_set_cancel).  Its result then has status
+ * SBPGPU_ECANCELED; a job that finishes first keeps its result.  SBPGPU_EINVAL for an
+ * unknown ticket. */
+sbpgpu_status sbpgpu_server_cancel(sbpgpu_server* server, int64_t ticket);
+/* Pauses (paused != 0) or resumes the start of queued jobs; running jobs go on.
+ * Destroying a paused server still finishes every submitted job. */
+sbpgpu_status sbpgpu_server_pause(sbpgpu_server* server, int32_t paused);
+/* Failure injection for tests: the queued job's worker context fails its device
+ * allocation number `after` + 1 (sbpgpu_ctx_inject_alloc_failure).  SBPGPU_EINVAL once the
+ * job has started. */
+sbpgpu_status sbpgpu_server_inject_alloc_failure(sbpgpu_server* server, int64_t ticket, int64_t after);
 /* Finishes every submitted job, then stops the workers. */
 void sbpgpu_server_destroy(sbpgpu_server* server);
 /* The batched form: n jobs through a server, results in job order. */

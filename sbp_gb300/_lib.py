@@ -16,7 +16,7 @@ vp = ctypes.c_void_p
 
 SBPGPU_OK = 0
 STATUS_NAMES = {0: "SBPGPU_OK", 1: "SBPGPU_EINVAL", 2: "SBPGPU_ENOMEM", 3: "SBPGPU_ETIMEOUT",
-                4: "SBPGPU_EDEVICE", 5: "SBPGPU_EUNSUPPORTED"}
+                4: "SBPGPU_EDEVICE", 5: "SBPGPU_EUNSUPPORTED", 6: "SBPGPU_ECANCELED"}
 
 
 class Config(ctypes.Structure):
@@ -94,6 +94,8 @@ SIGNATURES = {
     "sbpgpu_ctx_stream": (vp, [vp]),
     "sbpgpu_ctx_set_cells_budget": (ctypes.c_int, [vp, ctypes.c_int64]),
     "sbpgpu_ctx_set_cluster_blocks": (ctypes.c_int, [vp, ctypes.c_int64]),
+    "sbpgpu_ctx_set_cancel": (ctypes.c_int, [vp, ctypes.c_int32]),
+    "sbpgpu_ctx_inject_alloc_failure": (ctypes.c_int, [vp, ctypes.c_int64]),
     "sbpgpu_graph_create": (ctypes.c_int, [vp, ctypes.c_int64, ctypes.c_int64, i32p, i32p, ctypes.POINTER(vp)]),
     "sbpgpu_graph_create_device": (ctypes.c_int, [vp, ctypes.c_int64, ctypes.c_int64, vp, vp, ctypes.POINTER(vp)]),
     "sbpgpu_graph_load": (ctypes.c_int, [vp, ctypes.c_char_p, ctypes.c_int32, ctypes.POINTER(vp)]),
@@ -154,6 +156,10 @@ SIGNATURES = {
                                             ctypes.POINTER(vp)]),
     "sbpgpu_server_submit": (ctypes.c_int, [vp, ctypes.POINTER(Job), i64p]),
     "sbpgpu_server_wait": (ctypes.c_int, [vp, ctypes.c_int64, ctypes.POINTER(JobResult)]),
+    "sbpgpu_server_wait_for": (ctypes.c_int, [vp, ctypes.c_int64, ctypes.c_int64, ctypes.POINTER(JobResult)]),
+    "sbpgpu_server_cancel": (ctypes.c_int, [vp, ctypes.c_int64]),
+    "sbpgpu_server_pause": (ctypes.c_int, [vp, ctypes.c_int32]),
+    "sbpgpu_server_inject_alloc_failure": (ctypes.c_int, [vp, ctypes.c_int64, ctypes.c_int64]),
     "sbpgpu_server_destroy": (None, [vp]),
     "sbpgpu_sbp_batch": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64,
                                         ctypes.POINTER(Job), ctypes.POINTER(JobResult)]),

@@ -97,6 +97,16 @@ class Context:
         (0: whenever there are more than 128 blocks); results do not depend on it."""
         self.check(self.lib.sbpgpu_ctx_set_cluster_blocks(self.h, int(min_blocks)))
 
+    def set_cancel(self, requested=True):
+        """Requests (or withdraws) cancellation of the running partition on this context;
+        it stops between golden-section steps with SBPGPU_ECANCELED.  Thread-safe."""
+        self.check(self.lib.sbpgpu_ctx_set_cancel(self.h, int(bool(requested))))
+
+    def inject_alloc_failure(self, after):
+        """Test hook: device allocation number `after` + 1 from now fails as an out-of-memory
+        allocation does; negative: none."""
+        self.check(self.lib.sbpgpu_ctx_inject_alloc_failure(self.h, int(after)))
+
     def read_timing(self):
         t = _lib.KernelTiming()
         self.check(self.lib.sbpgpu_read_timing(self.h, ctypes.byref(t)))

@@ -7,6 +7,7 @@
 //     src/blockmodel/blockmodel_triplet.cpp:4-105).
 // Every entry point catches exceptions and reports them as status codes.
 #include <algorithm>
+#include <atomic>
 #include <cfloat>
 #include <climits>
 #include <cmath>
@@ -51,17 +52,29 @@ struct ApiError : std::runtime_error {
 // pool): freeing does not wait for the whole device, so contexts that run concurrently
 // (the partition server's workers) do not stall one another.
 thread_local cudaStream_t tls_stream = nullptr;
+// Allocations left before an injected allocation failure on this thread's current context
+// (sbpgpu_ctx_inject_alloc_failure); null or negative: none injected.
+thread_local int64_t* tls_fail_after = nullptr;
 
 struct StreamScope {
     cudaStream_t prev;
-    explicit StreamScope(cudaStream_t s) : prev(tls_stream) { tls_stream = s; }
-    ~StreamScope() { tls_stream = prev; }
+    int64_t* prev_fail;
+    StreamScope(cudaStream_t s, int64_t* fail_after) : prev(tls_stream), prev_fail(tls_fail_after) {
+        tls_stream = s;
+        tls_fail_after = fail_after;
+    }
+    ~StreamScope() {
+        tls_stream = prev;
+        tls_fail_after = prev_fail;
+    }
 };
 
 template <typename T>
 T* dalloc(std::vector<void*>& owned, size_t n) {
     void* p = nullptr;
     const size_t bytes = (n ? n : 1) * sizeof(T);
+    if (tls_fail_after && *tls_fail_after >= 0 && (*tls_fail_after)-- == 0)
+        throw ApiError(SBPGPU_ENOMEM, "device allocation of " + std::to_string(bytes) + " bytes failed (injected)");
     const cudaError_t e = cudaMallocAsync(&p, bytes, tls_stream);
     if (e != cudaSuccess) {
         cudaGetLastError();
@@ -113,6 +126,8 @@ struct sbpgpu_ctx {
     std::vector<TimedSpan> pending;
     std::vector<cudaEvent_t> free_events;
     sbpgpu_kernel_timing tm{};
+    std::atomic<int32_t> cancel{0};  // cancellation requested (sbpgpu_ctx_set_cancel)
+    int64_t fail_alloc_after = -1;   // injected allocation failure (sbpgpu_ctx_inject_alloc_failure)
 
     cudaEvent_t ev() {
         if (!free_events.empty()) {
@@ -214,7 +229,7 @@ sbpgpu_status fail(sbpgpu_ctx* ctx, sbpgpu_status code, const std::string& msg) 
 
 template <typename F>
 sbpgpu_status guarded(sbpgpu_ctx* ctx, F f) {
-    StreamScope scope(ctx ? ctx->stream : nullptr);
+    StreamScope scope(ctx ? ctx->stream : nullptr, ctx ? &ctx->fail_alloc_after : nullptr);
     try {
         return f();
     } catch (const ApiError& e) {
@@ -1161,6 +1176,18 @@ sbpgpu_status sbpgpu_ctx_set_cluster_blocks(sbpgpu_ctx* ctx, int64_t min_blocks)
     return SBPGPU_OK;
 }
 
+sbpgpu_status sbpgpu_ctx_set_cancel(sbpgpu_ctx* ctx, int32_t requested) {
+    if (!ctx) return SBPGPU_EINVAL;
+    ctx->cancel.store(requested ? 1 : 0);
+    return SBPGPU_OK;
+}
+
+sbpgpu_status sbpgpu_ctx_inject_alloc_failure(sbpgpu_ctx* ctx, int64_t after) {
+    if (!ctx) return SBPGPU_EINVAL;
+    ctx->fail_alloc_after = after < 0 ? -1 : after;
+    return SBPGPU_OK;
+}
+
 sbpgpu_status sbpgpu_ctx_set_cells_budget(sbpgpu_ctx* ctx, int64_t bytes) {
     if (!ctx) return SBPGPU_EINVAL;
     if (bytes < 0) return fail(ctx, SBPGPU_EINVAL, "cells budget must be >= 0");
@@ -1988,6 +2015,8 @@ sbpgpu_status sbpgpu_sbp(sbpgpu_graph* g, const sbpgpu_config* cfg_in, uint64_t 
         bool optimal = false;
         int32_t step = 0;
         while (!optimal) {
+            // between golden-section steps nothing of this call is in flight on the device
+            if (ctx->cancel.exchange(0)) throw ApiError(SBPGPU_ECANCELED, "partition cancelled");
             merge_impl(bm, cfg, seed, step, bm->num_blocks_to_merge);
             mcmc_impl(bm, cfg, seed, step, s[2].empty);
             ++step;

@@ -6,8 +6,10 @@
 // with its own context and stream, take jobs in submission order and run the same host
 // loop as sbpgpu_sbp; their kernels share the device.  A job is admitted only while the
 // estimated device footprint of the jobs in flight plus its own stays within the server's
-// HBM budget (the first job in flight is always admitted), and its graph, blockmodels and
-// work buffers stay on the device until it finishes.  Every job's result equals
+// HBM budget (a job that could never fit is refused at submission), and its graph,
+// blockmodels and work buffers stay on the device until it finishes.  A job can be
+// cancelled: a queued one leaves the queue, a running one stops between golden-section
+// steps through its worker context's cancellation flag.  Every job's result equals
 // sbpgpu_sbp of the same graph, configuration and seed run alone: jobs share no device
 // state, and the proposal stream depends only on the seed.
 #include <algorithm>
@@ -33,7 +35,10 @@ struct JobState {
     sbpgpu_job_result result{};
     int64_t footprint = 0;
     Clock::time_point t_submit, t_start;
+    bool started = false;
     bool done = false;
+    sbpgpu_ctx* ctx = nullptr;  // the worker context while running
+    int64_t inject_after = -1;  // injected allocation failure for the run
 };
 
 double ms_between(Clock::time_point a, Clock::time_point b) {
@@ -60,6 +65,7 @@ struct sbpgpu_server {
     int64_t inflight_bytes = 0;
     int32_t running = 0;
     bool stop = false;
+    bool paused = false;  // workers start no new job
     std::vector<std::thread> threads;
     std::string err;
 };
@@ -67,9 +73,16 @@ struct sbpgpu_server {
 namespace {
 
 bool admissible(const sbpgpu_server* s) {
-    if (s->pending.empty()) return false;
+    if (s->pending.empty() || (s->paused && !s->stop)) return false;
     const JobState* st = s->jobs.at(s->pending.front()).get();
-    return s->running == 0 || s->inflight_bytes + st->footprint <= s->hbm_budget;
+    return s->inflight_bytes + st->footprint <= s->hbm_budget;
+}
+
+void finish(sbpgpu_server* s, JobState* st, sbpgpu_status status, const char* msg) {
+    st->result.status = status;
+    std::strncpy(st->result.error, msg, sizeof(st->result.error) - 1);
+    st->done = true;
+    s->cv_done.notify_all();
 }
 
 void run_job(sbpgpu_ctx* ctx, JobState* st) {
@@ -98,15 +111,22 @@ void worker(sbpgpu_server* s) {
         s->inflight_bytes += st->footprint;
         s->running++;
         st->t_start = Clock::now();
+        st->started = true;
+        st->ctx = ctx;
         lk.unlock();
         if (cs == SBPGPU_OK) {
+            sbpgpu_ctx_inject_alloc_failure(ctx, st->inject_after);
             run_job(ctx, st);
+            sbpgpu_ctx_inject_alloc_failure(ctx, -1);
         } else {
             st->result.status = cs;
             std::strncpy(st->result.error, "cannot create a CUDA context for a worker", sizeof(st->result.error) - 1);
         }
         const auto t_end = Clock::now();
         lk.lock();
+        // a cancellation that arrived after the job's last step must not reach the next job
+        if (ctx) sbpgpu_ctx_set_cancel(ctx, 0);
+        st->ctx = nullptr;
         s->inflight_bytes -= st->footprint;
         s->running--;
         st->result.queued_ms = ms_between(st->t_submit, st->t_start);
@@ -171,6 +191,7 @@ sbpgpu_status sbpgpu_server_submit(sbpgpu_server* s, const sbpgpu_job* job, int6
     st->footprint = sbpgpu_job_footprint(job->num_vertices, job->num_edges, s->cells_budget);
     if (job->config.nonparametric)  // lgamma table and the non-empty-count steps (int64)
         st->footprint += 8 * (std::max(job->num_vertices, job->num_edges) + 2) + 16 * (job->num_vertices + 2);
+    if (st->footprint > s->hbm_budget) return SBPGPU_ENOMEM;  // could never be admitted
     st->t_submit = Clock::now();
     {
         std::lock_guard<std::mutex> lk(s->mu);
@@ -185,14 +206,61 @@ sbpgpu_status sbpgpu_server_submit(sbpgpu_server* s, const sbpgpu_job* job, int6
 }
 
 sbpgpu_status sbpgpu_server_wait(sbpgpu_server* s, int64_t ticket, sbpgpu_job_result* result) {
+    return sbpgpu_server_wait_for(s, ticket, -1, result);
+}
+
+sbpgpu_status sbpgpu_server_wait_for(sbpgpu_server* s, int64_t ticket, int64_t timeout_ms,
+                                     sbpgpu_job_result* result) {
     if (!s || !result) return SBPGPU_EINVAL;
     std::unique_lock<std::mutex> lk(s->mu);
     auto it = s->jobs.find(ticket);
     if (it == s->jobs.end()) return SBPGPU_EINVAL;
     JobState* st = it->second.get();
-    s->cv_done.wait(lk, [&] { return st->done; });
+    if (timeout_ms < 0) {
+        s->cv_done.wait(lk, [&] { return st->done; });
+    } else if (!s->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), [&] { return st->done; })) {
+        return SBPGPU_ETIMEOUT;
+    }
     *result = st->result;
     s->jobs.erase(it);
+    return SBPGPU_OK;
+}
+
+sbpgpu_status sbpgpu_server_cancel(sbpgpu_server* s, int64_t ticket) {
+    if (!s) return SBPGPU_EINVAL;
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->jobs.find(ticket);
+    if (it == s->jobs.end()) return SBPGPU_EINVAL;
+    JobState* st = it->second.get();
+    if (st->done) return SBPGPU_OK;
+    if (!st->started) {
+        s->pending.erase(std::find(s->pending.begin(), s->pending.end(), ticket));
+        st->t_start = Clock::now();
+        st->result.queued_ms = ms_between(st->t_submit, st->t_start);
+        finish(s, st, SBPGPU_ECANCELED, "job cancelled before it started");
+        s->cv_work.notify_all();  // the queue head may have changed
+    } else if (st->ctx) {
+        sbpgpu_ctx_set_cancel(st->ctx, 1);
+    }
+    return SBPGPU_OK;
+}
+
+sbpgpu_status sbpgpu_server_pause(sbpgpu_server* s, int32_t paused) {
+    if (!s) return SBPGPU_EINVAL;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->paused = paused != 0;
+    }
+    s->cv_work.notify_all();
+    return SBPGPU_OK;
+}
+
+sbpgpu_status sbpgpu_server_inject_alloc_failure(sbpgpu_server* s, int64_t ticket, int64_t after) {
+    if (!s) return SBPGPU_EINVAL;
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->jobs.find(ticket);
+    if (it == s->jobs.end() || it->second->started) return SBPGPU_EINVAL;
+    it->second->inject_after = after;
     return SBPGPU_OK;
 }
 

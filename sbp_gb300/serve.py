@@ -52,9 +52,16 @@ class Server:
         self._keep[t.value] = (src, dst, out, job)
         return t.value
 
-    def wait(self, ticket):
+    def wait(self, ticket, timeout=None):
+        """The job's result; with `timeout` (seconds) raises SbpGpuError(SBPGPU_ETIMEOUT)
+        when it is not done by then, and the ticket stays valid."""
         r = _lib.JobResult()
-        st = self.lib.sbpgpu_server_wait(self.h, int(ticket), ctypes.byref(r))
+        if timeout is None:
+            st = self.lib.sbpgpu_server_wait(self.h, int(ticket), ctypes.byref(r))
+        else:
+            st = self.lib.sbpgpu_server_wait_for(self.h, int(ticket), int(timeout * 1000), ctypes.byref(r))
+        if st == 3:
+            raise _lib.SbpGpuError(st, "job not done within %s s" % timeout)
         if st != 0:
             raise _lib.SbpGpuError(st, "unknown ticket")
         src, dst, out, job = self._keep.pop(ticket)
@@ -62,6 +69,23 @@ class Server:
             raise _lib.SbpGpuError(r.status, r.error.decode(errors="replace"))
         info = {"queued_ms": r.queued_ms, "run_ms": r.run_ms, "stats": r.stats.as_dict()}
         return out, int(r.num_blocks), float(r.mdl), info
+
+    def cancel(self, ticket):
+        """Cancels a queued job at once or a running one at its next golden-section step;
+        its wait() then raises SbpGpuError(SBPGPU_ECANCELED) unless it finished first."""
+        st = self.lib.sbpgpu_server_cancel(self.h, int(ticket))
+        if st != 0:
+            raise _lib.SbpGpuError(st, "unknown ticket")
+
+    def pause(self, paused=True):
+        """Stops (or resumes) the start of queued jobs; running jobs go on."""
+        self.lib.sbpgpu_server_pause(self.h, int(bool(paused)))
+
+    def inject_alloc_failure(self, ticket, after):
+        """Test hook: the queued job fails its device allocation number `after` + 1."""
+        st = self.lib.sbpgpu_server_inject_alloc_failure(self.h, int(ticket), int(after))
+        if st != 0:
+            raise _lib.SbpGpuError(st, "job unknown or already started")
 
     def close(self):
         if getattr(self, "h", None):

@@ -186,6 +186,27 @@ static void boundary_api(const Toy& t) {
         if (d != 0) ++listed;
     }
     EXPECT(listed == changed);
+    // the reference's known answers (test/finetune_test.cpp:89-124, :226-238): six keyed cells,
+    // zero-valued ones included, summing to zero, also for vertex 10 with its self edge
+    const s::Delta k7 = s::finetune::blockmodel_delta(7, from, 0, out, in, bm);
+    EXPECT(k7.entries().size() == 6);
+    EXPECT(k7.get(0, 0) == 1 && k7.get(0, 1) == 0 && k7.get(0, 2) == 1 && k7.get(1, 0) == 1);
+    EXPECT(k7.get(1, 2) == -1 && k7.get(2, 0) == 1 && k7.get(2, 1) == 0 && k7.get(2, 2) == -3);
+    for (long u : {7L, 10L}) {
+        const s::Delta du = s::finetune::blockmodel_delta(u, t.assignment[u], 0,
+                                                          s::finetune::edge_weights(graph.out_neighbors(), u),
+                                                          s::finetune::edge_weights(graph.in_neighbors(), u), bm);
+        long sum = 0;
+        for (const auto& e : du.entries()) sum += std::get<2>(e);
+        EXPECT(sum == 0);
+    }
+    const std::vector<long> assignment3 = {0, 0, 0, 1, 2, 3, 3, 4, 5, 1, 5};
+    s::Blockmodel b3(6, graph, 0.5, assignment3);
+    const s::Delta k6 = s::finetune::blockmodel_delta(6, 3, 0, s::finetune::edge_weights(graph.out_neighbors(), 6),
+                                                      s::finetune::edge_weights(graph.in_neighbors(), 6, true), b3);
+    EXPECT(k6.entries().size() == 6);
+    EXPECT(k6.get(0, 2) == 1 && k6.get(2, 0) == 1 && k6.get(2, 3) == -1 && k6.get(3, 0) == 1);
+    EXPECT(k6.get(3, 2) == -1 && k6.get(3, 3) == -1);
     bool threw = false;
     try {
         s::Delta d2(1, 2);

@@ -65,3 +65,75 @@ def test_batch_matches_server_and_reports_errors(gpu):
         with pytest.raises(_lib.SbpGpuError):
             srv.wait(bad)
         assert np.array_equal(srv.wait(good)[0], res[0][0])
+
+
+# ---- failure handling, made on the host: an injected allocation failure, a cancelled
+# request, a wait that runs out, a job refused over the budget.  Nothing faults the GPU.
+
+@pytest.mark.gpu
+def test_context_survives_allocation_failure_and_cancel(gpu):
+    n, src, dst, _ = _graphs(gpu, 1, 950)[0]
+    G = gpu.Graph(n, src, dst)
+    args = gpu.Args(algorithm="hybrid_mcmc", seed=2)
+    want = gpu.sbp.stochastic_block_partition(G, args)
+    ctx = G.ctx
+    ctx.inject_alloc_failure(2)
+    with pytest.raises(_lib.SbpGpuError) as e:
+        gpu.sbp.stochastic_block_partition(G, args)
+    assert e.value.status == 2
+    ctx.inject_alloc_failure(-1)
+    ctx.set_cancel(True)  # requested before the call: it stops at its first step
+    with pytest.raises(_lib.SbpGpuError) as e:
+        gpu.sbp.stochastic_block_partition(G, args)
+    assert e.value.status == 6
+    got = gpu.sbp.stochastic_block_partition(G, args)  # the request was consumed
+    assert got[1] == want[1] and np.array_equal(got[0], want[0]) and got[2] == want[2]
+    G.close()
+
+
+@pytest.mark.gpu
+def test_server_failures_leave_it_serving(gpu):
+    graphs = _graphs(gpu, 2, 960)
+    args = gpu.Args(algorithm="async_gibbs")
+    alone = []
+    for i, (n, src, dst, _) in enumerate(graphs):
+        G = gpu.Graph(n, src, dst)
+        alone.append(gpu.sbp.stochastic_block_partition(G, gpu.Args(algorithm="async_gibbs", seed=i))[0])
+        G.close()
+    big_src, big_dst, _ = gpu.dcsbm.generate_config("C2", seed=3)
+    budget = gpu.serve.footprint(60000, big_src.size, 64 << 20)
+    with gpu.serve.Server(workers=2, hbm_budget=budget, cells_budget=64 << 20) as srv:
+        # a job that could never fit the budget is refused at submission
+        with pytest.raises(_lib.SbpGpuError) as e:
+            srv.submit(3_000_000, big_src, big_dst, args)
+        assert e.value.status == 2
+        srv.pause()
+        (n0, s0, d0, _), (n1, s1, d1, _) = graphs
+        t_fail = srv.submit(n0, s0, d0, args, seed=0)
+        srv.inject_alloc_failure(t_fail, 3)
+        t_cancel = srv.submit(n1, s1, d1, args, seed=1)
+        t_ok = srv.submit(n1, s1, d1, args, seed=1)
+        srv.cancel(t_cancel)
+        with pytest.raises(_lib.SbpGpuError) as e:  # paused: nothing runs
+            srv.wait(t_ok, timeout=0.2)
+        assert e.value.status == 3
+        srv.pause(False)
+        with pytest.raises(_lib.SbpGpuError) as e:
+            srv.wait(t_fail)
+        assert e.value.status == 2
+        with pytest.raises(_lib.SbpGpuError) as e:
+            srv.wait(t_cancel)
+        assert e.value.status == 6
+        assert np.array_equal(srv.wait(t_ok)[0], alone[1])
+        # a running job stops at its next golden-section step
+        t_run = srv.submit(50000, big_src, big_dst, gpu.Args(algorithm="hybrid_mcmc"), seed=0)
+        with pytest.raises(_lib.SbpGpuError) as e:
+            srv.wait(t_run, timeout=0.5)
+        assert e.value.status == 3
+        srv.cancel(t_run)
+        with pytest.raises(_lib.SbpGpuError) as e:
+            srv.wait(t_run)
+        assert e.value.status == 6
+        # and the server goes on serving
+        t_after = srv.submit(n0, s0, d0, args, seed=0)
+        assert np.array_equal(srv.wait(t_after)[0], alone[0])
