@@ -99,7 +99,10 @@ struct Args {
     bool ordered = false;
     bool approximate = false;
     int asynciterations = INT_MAX;
-    bool nonparametric = false;       // entropy::nonparametric, not degree-corrected
+    bool nonparametric = false;       // entropy::nonparametric
+    bool degreecorrected = false;     // args.degreecorrected (include/args.hpp:24): the degree-
+                                      // corrected nonparametric description length; graphs built
+                                      // while it is set take it (evaluation and single moves only)
     bool undirected = false;          // args.undirected (include/args.hpp:55): the nonparametric
                                       // entropy's undirected form; graphs built while it is set
                                       // take it, and stochastic_block_partition applies it
@@ -212,6 +215,7 @@ class Graph {
         assignment_.assign(n_, -1);
         check(sbpgpu_graph_create(ctx_->get(), n_, e_, src.data(), dst.data(), &h_), ctx_->get());
         if (args.undirected) check(sbpgpu_graph_set_undirected(h_, 1), ctx_->get());
+        if (args.degreecorrected) check(sbpgpu_graph_set_degree_corrected(h_, 1), ctx_->get());
     }
     Context* ctx_;
     long n_ = 0, e_ = 0;

@@ -139,6 +139,17 @@ sbpgpu_status sbpgpu_graph_set_model_edges(sbpgpu_graph* g, int64_t num_edges);
  * until set.  The parametric entropy does not read it. */
 int32_t sbpgpu_graph_undirected(const sbpgpu_graph* g);
 sbpgpu_status sbpgpu_graph_set_undirected(sbpgpu_graph* g, int32_t undirected);
+/* args.degreecorrected (include/args.hpp:24) as the nonparametric description length reads
+ * it: vertex terms become lgamma of the block degrees (include/entropy.hpp:117-133) and the
+ * degree prior get_deg_entropy + get_deg_dl_dist (src/entropy.cpp:617-743) is added, with
+ * per-block degree histograms of the current assignment (blockmodel.cpp:209-235) and
+ * log_q, the partition-count asymptotic through the dilogarithm (:677-707).  Applies to
+ * sbpgpu_np_mdl, sbpgpu_np_delta_mdl_batch (get_delta_deg_dl, :1072-1109) and the
+ * nonparametric sbpgpu_move_vertex / sbpgpu_propose_move; sweeps, merges, splits and
+ * partitions of a degree-corrected graph with the nonparametric entropy return
+ * SBPGPU_EUNSUPPORTED, as does sbpgpu_np_merge_delta_mdl_batch. */
+int32_t sbpgpu_graph_degree_corrected(const sbpgpu_graph* g);
+sbpgpu_status sbpgpu_graph_set_degree_corrected(sbpgpu_graph* g, int32_t on);
 
 /* ---- blockmodel: replaces Blockmodel(num_blocks, graph, rate, assignment) and
  * Blockmodel::initialize_edge_counts (src/blockmodel/blockmodel.cpp:193-276).

@@ -109,6 +109,9 @@ struct ora_graph {
     // diagonal cells carry -w log 2, a block's vertex term counts its out-degree only, and
     // the edge count is spread over B (B + 1) / 2 block pairs
     bool und = false;
+    // args.degreecorrected (entropy.hpp:117-133, entropy.cpp:617-764): the degree-corrected
+    // vertex terms and prior, for the description length and vertex-move deltas
+    bool dc = false;
     std::vector<std::vector<int32_t>> out, in, inns;  // inns = in-neighbours without self
     std::vector<int32_t> selfcnt;
     std::vector<double> Ld;     // fastlog table: logf((float)x) (fastlog.hpp:21-30)
@@ -424,10 +427,159 @@ inline int64_t np_dl_step(const ora_graph* g, int64_t b, int dB) {
     const double edges = np_edges_dl(b + dB, g->Em, g->und) - np_edges_dl(b, g->Em, g->und);
     return llrint((part + edges) * kFix);
 }
-/* vterm_exact (entropy.hpp:117-133), not degree-corrected: (d_out + d_in) log w, or
- * d_out log w when undirected. */
+/* vterm_exact (entropy.hpp:117-133): (d_out + d_in) log w, or d_out log w when
+ * undirected; degree-corrected: lgamma(d_out + 1) + lgamma(d_in + 1), or the first alone
+ * when undirected, whatever the block size. */
 inline int64_t np_vterm(const ora_graph* g, int64_t dout, int64_t din, int64_t w) {
+    if (g->dc) return g->LG[dout] + (g->und ? 0 : g->LG[din]);
     return w == 0 ? 0 : (g->und ? dout : dout + din) * g->Lq[w];
+}
+
+// ---------------------------------------------------------------- degree correction
+/* The dilogarithm Li2(z) = sum z^k / k^2 (|z| <= 1/2), continued by Euler's reflection
+ * Li2(z) = pi^2/6 - log(z) log(1 - z) - Li2(1 - z) above 1/2 and by Landen's identity
+ * Li2(z) = -Li2(z / (z - 1)) - log^2(1 - z) / 2 below 0. */
+double dc_li2(double z) {
+    if (z < 0.0) {
+        const double l = log1p(-z);
+        return -dc_li2(z / (z - 1.0)) - 0.5 * l * l;
+    }
+    if (z >= 1.0) return M_PI * M_PI / 6.0;  // Li2(1); the argument here never exceeds 1
+    if (z > 0.5) return M_PI * M_PI / 6.0 - log(z) * log1p(-z) - dc_li2(1.0 - z);
+    double sum = 0.0, p = z;
+    for (int k = 1; k <= 200; ++k) {
+        const double t = p / ((double)k * (double)k);
+        sum += t;
+        if (t <= 1e-18 * sum) break;
+        p *= z;
+    }
+    return sum;
+}
+/* spence(x) = -integral_1^x log(t) / (t - 1) dt = Li2(1 - x) (spence.hpp:9-22, the
+ * Cephes function the reference carries in spence.cpp); here for x = e^-v, with
+ * 1 - e^-v formed as -expm1(-v). */
+inline double dc_spence_exp(double v) { return dc_li2(-expm1(-v)); }
+/* get_v (entropy.cpp:677-686): the fixed point v = u sqrt(spence(e^-v)), to 1e-8. */
+double dc_get_v(double u, double epsilon = 1e-8) {
+    double v = u, delta = 1.0;
+    for (int it = 0; delta > epsilon && it < 100000; ++it) {
+        const double nv = u * sqrt(dc_spence_exp(v));
+        delta = fabs(nv - v);
+        v = nv;
+    }
+    return v;
+}
+/* log_q (entropy.cpp:688-707): log of the number of partitions of n into at most k parts,
+ * by the small-k form lbinom(n - 1, k - 1) - lgamma(k + 1) when k < n^(1/4) and by the
+ * Szekeres asymptotic otherwise. */
+double dc_log_q(int64_t n, int64_t k) {
+    if (n <= 0 || k < 1) return 0.0;
+    if (k > n) k = n;
+    if ((double)k < pow((double)n, 0.25)) return np_lbinom(n - 1, k - 1) - lgamma((double)(k + 1));
+    const double u = (double)k / sqrt((double)n);
+    const double v = dc_get_v(u);
+    const double lf = log(v) - log1p(-exp(-v) * (1 + u * u / 2)) / 2 - log(2.0) * 3 / 2. - log(u) - log(M_PI);
+    const double gg = 2 * v / u - u * log1p(-exp(-v));
+    return lf - log((double)n) + sqrt((double)n) * gg;
+}
+/* A vertex's degrees as the degree terms read them: the sizes of its neighbour lists,
+ * self-loops in both (get_deg_entropy, entropy.cpp:620-624; blockmodel.cpp:234-235). */
+inline int64_t dc_kin(const ora_graph* g, int64_t v) { return (int64_t)g->in[v].size(); }
+inline int64_t dc_kout(const ora_graph* g, int64_t v) { return (int64_t)g->out[v].size(); }
+/* The per-block in- and out-degree histograms, as Blockmodel's constructor builds them
+ * (blockmodel.cpp:209-235), for the current assignment. */
+struct DcHist {
+    std::vector<std::map<int64_t, int64_t>> in, out;
+};
+DcHist dc_hist(const ora_bm* bm) {
+    DcHist h;
+    h.in.resize(bm->B);
+    h.out.resize(bm->B);
+    for (int64_t v = 0; v < bm->g->N; ++v) {
+        h.in[bm->asg[v]][dc_kin(bm->g, v)]++;
+        h.out[bm->asg[v]][dc_kout(bm->g, v)]++;
+    }
+    return h;
+}
+inline int64_t dc_count(const std::map<int64_t, int64_t>& m, int64_t k) {
+    const auto it = m.find(k);
+    return it == m.end() ? 0 : it->second;
+}
+inline int64_t dc_fix(double x) { return llrint(x * kFix); }
+/* sum over vertices of get_deg_entropy (entropy.cpp:620-624, :644-655), canonical. */
+int64_t dc_deg_entropy_fixed(const ora_graph* g) {
+    int64_t t = 0;
+    for (int64_t v = 0; v < g->N; ++v) t -= g->LG[dc_kin(g, v)] + g->LG[dc_kout(g, v)];
+    return t;
+}
+double dc_deg_entropy_literal(const ora_graph* g) {
+    double t = 0.0;
+    for (int64_t v = 0; v < g->N; ++v)
+        t += -lgamma((double)(dc_kin(g, v) + 1)) - lgamma((double)(dc_kout(g, v) + 1));
+    return t;
+}
+/* get_deg_dl_dist (entropy.cpp:709-743): per block log_q(d_out, size) + log_q(d_in, size),
+ * minus lgamma(count + 1) over the in-degree (directed only) and out-degree histograms,
+ * plus lgamma(size + 1) twice (once when undirected).  Canonical: every log_q term and
+ * lgamma term rounded to 2^-24, then summed exactly. */
+int64_t dc_deg_dl_fixed(const ora_bm* bm, const DcHist& h) {
+    const ora_graph* g = bm->g;
+    int64_t t = 0;
+    for (int64_t b = 0; b < bm->B; ++b) {
+        t += dc_fix(dc_log_q(bm->dout[b], bm->sizes[b])) + dc_fix(dc_log_q(bm->din[b], bm->sizes[b]));
+        int64_t total = 0;
+        if (!g->und)
+            for (const auto& e : h.in[b]) t -= g->LG[e.second];
+        for (const auto& e : h.out[b]) {
+            t -= g->LG[e.second];
+            total += e.second;
+        }
+        t += (g->und ? 1 : 2) * g->LG[total];
+    }
+    return t;
+}
+double dc_deg_dl_literal(const ora_bm* bm, const DcHist& h) {
+    const ora_graph* g = bm->g;
+    double S = 0.0;
+    for (int64_t b = 0; b < bm->B; ++b) {
+        S += dc_log_q(bm->dout[b], bm->sizes[b]);
+        S += dc_log_q(bm->din[b], bm->sizes[b]);
+        int64_t total = 0;
+        if (!g->und)
+            for (const auto& e : h.in[b]) S -= lgamma((double)(e.second + 1));
+        for (const auto& e : h.out[b]) {
+            S -= lgamma((double)(e.second + 1));
+            total += e.second;
+        }
+        S += (g->und ? 1.0 : 2.0) * lgamma((double)(total + 1));
+    }
+    return S;
+}
+/* get_delta_deg_dl_dist_change (entropy.cpp:994-1070) for one vertex with degrees
+ * (kin, kout) leaving (diff = -1) or joining (+1) block b; `fix` selects the canonical
+ * arithmetic (terms rounded to 2^-24, result in those units) or the literal one. */
+double dc_change(const ora_bm* bm, const DcHist& h, int64_t b, int64_t kin, int64_t kout, int diff, bool fix) {
+    const ora_graph* g = bm->g;
+    const int64_t total = bm->sizes[b], ep = bm->dout[b], em = bm->din[b];
+    auto lg1 = [&](int64_t x) { return fix ? (double)g->LG[x] : lgamma((double)(x + 1)); };
+    auto lq = [&](int64_t n, int64_t k) { return fix ? (double)dc_fix(dc_log_q(n, k)) : dc_log_q(n, k); };
+    auto Sk = [&](int delta) {
+        double S = 0.0;
+        if (!g->und) S -= lg1(dc_count(h.in[b], kin) + delta);
+        return S - lg1(dc_count(h.out[b], kout) + delta);
+    };
+    auto Se = [&](int delta, int64_t din, int64_t dout) { return lq(em + din, total + delta) + lq(ep + dout, total + delta); };
+    auto Sr = [&](int delta) { return (g->und ? 1.0 : 2.0) * lg1(total + delta); };
+    const double Sb = Sk(0) + Se(0, 0, 0) + Sr(0);
+    const double Sa = Sk(diff) + Se(diff, diff * kin, diff * kout) + Sr(diff);
+    return Sa - Sb;
+}
+/* get_delta_deg_dl (entropy.cpp:1072-1109) for moving v from its block to s. */
+double dc_vertex_delta(const ora_bm* bm, const DcHist& h, int64_t v, int64_t s, bool fix) {
+    const int64_t r = bm->asg[v];
+    if (r == s) return 0.0;
+    const int64_t kin = dc_kin(bm->g, v), kout = dc_kout(bm->g, v);
+    return dc_change(bm, h, r, kin, kout, -1, fix) + dc_change(bm, h, s, kin, kout, +1, fix);
 }
 /* The block terms of virtual_move_sparse (entropy.cpp:822-889), the lgamma terms of
  * get_delta_partition_dl (:892-1000) and the non-empty-count terms for moving `weight`
@@ -456,7 +608,9 @@ int64_t np_vertex_dS(const ora_bm* bm, int64_t v, int64_t s, const DeltaMap& d) 
     const int64_t r = bm->asg[v];
     if (r == s) return 0;
     const VertexInfo vi = vinfo(bm->g, v);
-    return np_entries(bm, d) + np_block_terms(bm, r, s, vi.kout, vi.kin, 1);
+    int64_t t = np_entries(bm, d) + np_block_terms(bm, r, s, vi.kout, vi.kin, 1);
+    if (bm->g->dc) t += (int64_t)dc_vertex_delta(bm, dc_hist(bm), v, s, true);
+    return t;
 }
 /* nonparametric::block_merge_delta_mdl (entropy.cpp:1198-1223), units of 2^-24. */
 int64_t np_merge_dS(const ora_bm* bm, int64_t r, int64_t s, const DeltaMap& d) {
@@ -471,7 +625,10 @@ double np_dS_literal(const ora_bm* bm, int64_t r, int64_t s, const DeltaMap& d, 
                      int64_t weight) {
     const ora_graph* g = bm->g;
     auto lg = [](int64_t x) { return lgamma((double)x); };
-    auto vt = [&](int64_t o, int64_t i, int64_t w) { return w == 0 ? 0.0 : (double)(g->und ? o : o + i) * g->Ld[w]; };
+    auto vt = [&](int64_t o, int64_t i, int64_t w) {
+        if (g->dc) return lgamma((double)(o + 1)) + (g->und ? 0.0 : lgamma((double)(i + 1)));
+        return w == 0 ? 0.0 : (double)(g->und ? o : o + i) * g->Ld[w];
+    };
     const double log_2 = log(2.0);
     auto et = [&](bool diag, int64_t w) { return -lg(w + 1) - (g->und && diag ? (double)w * log_2 : 0.0); };
     double dS = 0.0;
@@ -504,6 +661,7 @@ double np_mdl_canonical(const ora_bm* bm) {
         for (const auto& e : bm->row[r]) fixed -= np_cell(g, e.first == r, e.second, -e.second);  // + eterm
     for (int64_t b = 0; b < bm->B; ++b) fixed += np_vterm(g, bm->dout[b], bm->din[b], bm->sizes[b]) - g->LG[bm->sizes[b]];
     fixed += g->LG[g->N] + g->Lq[g->N];
+    if (g->dc) fixed += dc_deg_entropy_fixed(g) + dc_deg_dl_fixed(bm, dc_hist(bm));
     return (double)fixed * kInvFix +
            (np_lbinom(g->N - 1, bm->nonempty - 1) + np_edges_dl(bm->nonempty, g->Em, g->und));
 }
@@ -515,8 +673,13 @@ void np_terms_literal(const ora_bm* bm, double out[4]) {
     for (int64_t r = 0; r < bm->B; ++r)
         for (const auto& e : bm->row[r])
             S += -lgamma((double)(e.second + 1)) - (g->und && e.first == r ? (double)e.second * log_2 : 0.0);
-    for (int64_t b = 0; b < bm->B; ++b)
-        if (bm->sizes[b] != 0) S += (double)(g->und ? bm->dout[b] : bm->dout[b] + bm->din[b]) * g->Ld[bm->sizes[b]];
+    for (int64_t b = 0; b < bm->B; ++b) {
+        if (g->dc)
+            S += lgamma((double)(bm->dout[b] + 1)) + (g->und ? 0.0 : lgamma((double)(bm->din[b] + 1)));
+        else if (bm->sizes[b] != 0)
+            S += (double)(g->und ? bm->dout[b] : bm->dout[b] + bm->din[b]) * g->Ld[bm->sizes[b]];
+    }
+    if (g->dc) S += dc_deg_entropy_literal(g);
     double P = 0.0;
     P += np_lbinom(g->N - 1, bm->nonempty - 1);
     P += lgamma((double)(g->N + 1));
@@ -524,7 +687,7 @@ void np_terms_literal(const ora_bm* bm, double out[4]) {
     P += g->Ld[g->N];
     out[0] = S;
     out[1] = P;
-    out[2] = 0.0;
+    out[2] = g->dc ? dc_deg_dl_literal(bm, dc_hist(bm)) : 0.0;
     out[3] = np_edges_dl(bm->nonempty, g->Em, g->und);
 }
 
@@ -1723,6 +1886,12 @@ extern "C" int64_t ora_graph_model_edges(const ora_graph* g) { return g->Em; }
 extern "C" void ora_graph_set_model_edges(ora_graph* g, int64_t num_edges) { g->Em = num_edges; }
 extern "C" void ora_graph_set_undirected(ora_graph* g, int32_t undirected) { g->und = undirected != 0; }
 
+extern "C" void ora_graph_set_degree_corrected(ora_graph* g, int32_t on) { g->dc = on != 0; }
+
+extern "C" double ora_log_q(int64_t n, int64_t k) { return dc_log_q(n, k); }
+
+extern "C" double ora_spence(double x) { return x == 1.0 ? 0.0 : dc_li2(1.0 - x); }
+
 extern "C" void ora_extend(const ora_graph* g, const int32_t* sample_asg, int64_t sample_n, int64_t B,
                            const int32_t* mapping, uint64_t seed, int32_t* out) {
     std::vector<int32_t> a;
@@ -1804,7 +1973,10 @@ extern "C" void ora_np_delta_mdl(const ora_bm* bm, int64_t v, int64_t s, double*
     const DeltaMap d = vertex_delta(bm, v, s);
     const VertexInfo vi = vinfo(bm->g, v);
     const int64_t r = bm->asg[v];
-    if (literal) *literal = r == s ? 0.0 : np_dS_literal(bm, r, s, d, vi.kout, vi.kin, 1);
+    if (literal)
+        *literal = r == s ? 0.0
+                          : np_dS_literal(bm, r, s, d, vi.kout, vi.kin, 1) +
+                                (bm->g->dc ? dc_vertex_delta(bm, dc_hist(bm), v, s, false) : 0.0);
     if (fixed) *fixed = np_vertex_dS(bm, v, s, d);
 }
 

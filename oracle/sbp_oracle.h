@@ -162,6 +162,12 @@ int64_t ora_graph_model_edges(const ora_graph* g);
 void ora_graph_set_model_edges(ora_graph* g, int64_t num_edges);
 /* args.undirected for the nonparametric entropy (entropy.hpp:102-133, entropy.cpp:745). */
 void ora_graph_set_undirected(ora_graph* g, int32_t undirected);
+/* args.degreecorrected for the nonparametric description length and vertex-move deltas
+ * (entropy.hpp:117-133, entropy.cpp:617-764, :994-1110). */
+void ora_graph_set_degree_corrected(ora_graph* g, int32_t on);
+/* entropy::nonparametric::log_q (entropy.cpp:688-707) and spence (spence.hpp:9-22). */
+double ora_log_q(int64_t n, int64_t k);
+double ora_spence(double x);
 /* The graph's edges, by source vertex, each source's out-neighbours in order. */
 void ora_graph_edges(const ora_graph* g, int32_t* src, int32_t* dst);
 /* sample::extend (sample.cpp:159-199). */

@@ -106,6 +106,8 @@ SIGNATURES = {
     "sbpgpu_graph_set_model_edges": (ctypes.c_int, [vp, ctypes.c_int64]),
     "sbpgpu_graph_undirected": (ctypes.c_int32, [vp]),
     "sbpgpu_graph_set_undirected": (ctypes.c_int, [vp, ctypes.c_int32]),
+    "sbpgpu_graph_degree_corrected": (ctypes.c_int32, [vp]),
+    "sbpgpu_graph_set_degree_corrected": (ctypes.c_int, [vp, ctypes.c_int32]),
     "sbpgpu_bm_create": (ctypes.c_int, [vp, ctypes.c_int64, i32p, ctypes.POINTER(vp)]),
     "sbpgpu_bm_copy": (ctypes.c_int, [vp, ctypes.POINTER(vp)]),
     "sbpgpu_bm_destroy": (None, [vp]),

@@ -155,9 +155,11 @@ class Graph:
     use; the number of edges given by default.  Pass half of it for arrays that hold both
     directions of an undirected edge list, as the reference's loader counts them
     (src/graph.cpp:145-147).  undirected: args.undirected for the nonparametric entropy
-    (include/sbpgpu.h, sbpgpu_graph_set_undirected)."""
+    (include/sbpgpu.h, sbpgpu_graph_set_undirected).  degree_corrected: args.degreecorrected
+    for the nonparametric description length and single-move deltas
+    (sbpgpu_graph_set_degree_corrected)."""
 
-    def __init__(self, num_vertices, src, dst, ctx=None, num_edges=None, undirected=False):
+    def __init__(self, num_vertices, src, dst, ctx=None, num_edges=None, undirected=False, degree_corrected=False):
         self.ctx = ctx or default_context()
         self.src = np.ascontiguousarray(src, dtype=np.int32)
         self.dst = np.ascontiguousarray(dst, dtype=np.int32)
@@ -177,6 +179,8 @@ class Graph:
             self.ctx.check(self.ctx.lib.sbpgpu_graph_set_model_edges(self.h, int(num_edges)))
         if undirected:
             self.ctx.check(self.ctx.lib.sbpgpu_graph_set_undirected(self.h, 1))
+        if degree_corrected:
+            self.ctx.check(self.ctx.lib.sbpgpu_graph_set_degree_corrected(self.h, 1))
 
     @classmethod
     def _adopt(cls, handle, ctx):
@@ -231,6 +235,10 @@ class Graph:
     def undirected(self):
         """args.undirected as the nonparametric entropy reads it."""
         return bool(self.ctx.lib.sbpgpu_graph_undirected(self.h))
+
+    def degree_corrected(self):
+        """args.degreecorrected as the nonparametric description length reads it."""
+        return bool(self.ctx.lib.sbpgpu_graph_degree_corrected(self.h))
 
     def num_stored_edges(self):
         """The directed edges stored (the length of the edge arrays)."""

@@ -189,6 +189,7 @@ struct sbpgpu_graph {
     int64_t Em = 0;
     // args.undirected for the nonparametric entropy (entropy.hpp:102-133, entropy.cpp:745)
     int32_t und = 0;
+    int32_t dc = 0;       // args.degreecorrected for the nonparametric description length
     int64_t np_Em = -1;   // the count the nonparametric Dm / Dp tables were built for
     int32_t np_und = -1;  // and the form
     DevGraph dg{};
@@ -381,6 +382,19 @@ void ensure_np(sbpgpu_graph* g) {
     g->dg.ln2q = kLn2Fix;
 }
 
+// The sweeps, chains, merges and splits score moves without the degree-corrected terms:
+// the reference's block-merge form of them (entropy.cpp:1180-1196) reads a block's total
+// degree as a key of its vertex-degree histograms and evaluates lgamma at non-positive
+// arguments, so there is no consistent merge score to reproduce, and the device paths do
+// not carry the degree histograms through their moves.
+void ensure_np_sweeps(sbpgpu_graph* g) {
+    if (g->dc)
+        throw ApiError(SBPGPU_EUNSUPPORTED,
+                       "degree-corrected description lengths are evaluated (np_mdl, np_delta_mdl_batch, "
+                       "move_vertex), not used by sweeps, merges or splits");
+    ensure_np(g);
+}
+
 void ensure_split(sbpgpu_graph* g, float mh_percent) {
     if (g->split_mh == mh_percent) return;
     std::vector<int32_t> idx(g->N);
@@ -423,6 +437,7 @@ double do_mdl(sbpgpu_bm* bm, bool np = false) {
     if (np) ensure_np(g);
     if (np) launch_np_mdl(g->dg, bm->d, g->w, g->ctx->stream);
     else launch_mdl(g->dg, bm->d, g->w, g->ctx->stream);
+    if (np && g->dc) launch_dc_mdl(g->dg, bm->d, g->w.d_acc, g->ctx->stream);
     unsigned long long* h_acc = static_cast<unsigned long long*>(host_scratch());
     int32_t* h_ne = reinterpret_cast<int32_t*>(h_acc + 1);
     CK(cudaMemcpyAsync(h_acc, g->w.d_acc, sizeof(*h_acc), cudaMemcpyDeviceToHost, g->ctx->stream));
@@ -469,7 +484,7 @@ void harvest_counters(sbpgpu_graph* g) {
 void gibbs_batch_dev(sbpgpu_bm* bm, const int32_t* list, int32_t n, uint64_t seed, uint32_t it, uint32_t step,
                      int mode) {
     sbpgpu_graph* g = bm->g;
-    if (mode == ACC_NP) ensure_np(g);
+    if (mode == ACC_NP) ensure_np_sweeps(g);
     {
         Span sp(g->ctx, 0);
         gibbs_propose(g->dg, bm->d, list, n, g->max_k, seed, it, step, mode, g->w, g->ctx->stream);
@@ -528,7 +543,7 @@ bool ensure_cluster_carry(sbpgpu_graph* g) {
 void chain_run(sbpgpu_bm* bm, const int32_t* order, int32_t n, int32_t max_k, int64_t k_sum, uint64_t seed,
                uint32_t it, uint32_t step, int mode) {
     sbpgpu_graph* g = bm->g;
-    if (mode == ACC_NP) ensure_np(g);
+    if (mode == ACC_NP) ensure_np_sweeps(g);
     const int64_t B = bm->d.B;
     if (B > kWinSharedMax) ensure_cells(g, mh_window_cells((int32_t)B));
     WindowPlan plan{};
@@ -739,7 +754,7 @@ double split_null_mdl(const sbpgpu_graph* g, int64_t n, int64_t E, bool np) {
 // delta are split until the block count reaches `target`.
 void split_impl(sbpgpu_bm* bm, const sbpgpu_config& cfg, uint64_t seed, uint32_t step, int64_t target) {
     sbpgpu_graph* g = bm->g;
-    ensure_np(g);
+    ensure_np_sweeps(g);
     cudaStream_t st = g->ctx->stream;
     const int64_t B = bm->d.B, N = g->N, P = 10;
     std::vector<void*> tmp;
@@ -827,7 +842,7 @@ void split_impl(sbpgpu_bm* bm, const sbpgpu_config& cfg, uint64_t seed, uint32_t
 }
 
 void mcmc_impl(sbpgpu_bm* bm, const sbpgpu_config& cfg, uint64_t seed, int32_t step, bool golden) {
-    if (cfg.nonparametric) ensure_np(bm->g);
+    if (cfg.nonparametric) ensure_np_sweeps(bm->g);
     if (cfg.algorithm == 0 && step < cfg.asynciterations) async_gibbs(bm, cfg, seed, step, golden);
     else if (cfg.algorithm == 1) hybrid_mcmc(bm, cfg, seed, step, golden);
     else metropolis_hastings(bm, cfg, seed, step, golden);
@@ -840,7 +855,7 @@ void merge_impl(sbpgpu_bm* bm, const sbpgpu_config& cfg, uint64_t seed, int32_t 
     if (num_to_merge >= B) throw ApiError(SBPGPU_EINVAL, "num_blocks_to_merge must be < num_blocks");
     {
         Span sp(g->ctx, 2);
-        if (cfg.nonparametric) ensure_np(g);
+        if (cfg.nonparametric) ensure_np_sweeps(g);
         merge_propose(g->dg, bm->d, seed, (uint32_t)step, g->w, g->ctx->stream, cfg.nonparametric != 0);
     }
     if (!cfg.approximate) ensure_cells(g, (uint64_t)B * (uint64_t)B);
@@ -1010,6 +1025,7 @@ sbpgpu_status delta_batch_impl(sbpgpu_bm* bm, int64_t n, const int32_t* vertex, 
             CK(cudaMemcpyAsync(dv, vertex, n * 4, cudaMemcpyHostToDevice, st));
             CK(cudaMemcpyAsync(ds, proposal, n * 4, cudaMemcpyHostToDevice, st));
             launch_vertex_dS_batch(g->dg, bm->d, dv, ds, n, max_k, dout, g->w, st, np);
+            if (np && g->dc) launch_dc_vertex_deltas(g->dg, bm->d, dv, ds, n, dout, st);
             CK(cudaMemcpyAsync(h.data(), dout, n * 8, cudaMemcpyDeviceToHost, st));
             check_flags(g);
         } catch (...) {
@@ -1032,7 +1048,7 @@ sbpgpu_status merge_delta_batch_impl(sbpgpu_bm* bm, int64_t n, const int32_t* bl
             if (block[i] < 0 || block[i] >= bm->d.B || proposal[i] < 0 || proposal[i] >= bm->d.B ||
                 block[i] == proposal[i])
                 throw ApiError(SBPGPU_EINVAL, "block or proposal out of range");
-        if (np) ensure_np(g);
+        if (np) ensure_np_sweeps(g);
         std::vector<void*> tmp;
         int32_t* dr = dalloc<int32_t>(tmp, n);
         int32_t* ds = dalloc<int32_t>(tmp, n);
@@ -1077,6 +1093,7 @@ void move_one(sbpgpu_bm* bm, const sbpgpu_config& cfg, int32_t v, int32_t s, uin
         const int32_t pair[2] = {v, s};
         CK(cudaMemcpyAsync(dv, pair, 8, cudaMemcpyHostToDevice, st));
         launch_vertex_dS_batch(g->dg, bm->d, dv, dv + 1, 1, max_k, ddS, g->w, st, np, greedy || np ? nullptr : dH);
+        if (np && g->dc) launch_dc_vertex_deltas(g->dg, bm->d, dv, dv + 1, 1, ddS, st);
         CK(cudaMemcpyAsync(&dS_fixed, ddS, 8, cudaMemcpyDeviceToHost, st));
         if (!greedy && !np) CK(cudaMemcpyAsync(&H, dH, 8, cudaMemcpyDeviceToHost, st));
         check_flags(g);
@@ -1600,6 +1617,15 @@ int64_t sbpgpu_graph_num_edges(const sbpgpu_graph* g) { return g ? g->E : 0; }
 int64_t sbpgpu_graph_model_edges(const sbpgpu_graph* g) { return g ? g->Em : 0; }
 
 int32_t sbpgpu_graph_undirected(const sbpgpu_graph* g) { return g ? g->und : 0; }
+
+int32_t sbpgpu_graph_degree_corrected(const sbpgpu_graph* g) { return g ? g->dc : 0; }
+
+sbpgpu_status sbpgpu_graph_set_degree_corrected(sbpgpu_graph* g, int32_t on) {
+    if (!g) return SBPGPU_EINVAL;
+    g->dc = on ? 1 : 0;
+    g->dg.dc = g->dc;
+    return SBPGPU_OK;
+}
 
 sbpgpu_status sbpgpu_graph_set_undirected(sbpgpu_graph* g, int32_t undirected) {
     if (!g) return SBPGPU_EINVAL;

@@ -59,6 +59,9 @@ struct DevGraph {
     // log 2 in units of 2^-24, rounded), vertex terms count out-degrees only
     int32_t np_und;
     long long ln2q;
+    // args.degreecorrected: vertex terms are lgamma of the block degrees, and the degree
+    // prior's terms are added by degcorr.cu
+    int32_t dc;
 };
 
 struct DevBM {

@@ -80,6 +80,11 @@ void launch_mdl(const DevGraph& g, const DevBM& bm, Work& w, cudaStream_t st);
 // The table terms of nonparametric::mdl (entropy.cpp:751-779) in units of 2^-24 into
 // w.d_acc[0]: -sum LG[cell] + sum over blocks (vterm - LG[size]).
 void launch_np_mdl(const DevGraph& g, const DevBM& bm, Work& w, cudaStream_t st);
+// Degree-corrected additions (degcorr.cu): to the description length, added into *acc in
+// units of 2^-24; and to each vertex move's delta out[i] (units of 2^-24).
+void launch_dc_mdl(const DevGraph& g, const DevBM& bm, unsigned long long* acc, cudaStream_t st);
+void launch_dc_vertex_deltas(const DevGraph& g, const DevBM& bm, const int32_t* v, const int32_t* s, int64_t n,
+                             long long* out, cudaStream_t st);
 // np: nonparametric deltas (the graph's nonparametric tables must exist).
 // hastings (optional, not with np): entropy::hastings_correction of each pair.
 void launch_vertex_dS_batch(const DevGraph& g, const DevBM& bm, const int32_t* v, const int32_t* s, int64_t n,

@@ -33,9 +33,11 @@ __device__ __forceinline__ long long np_log(const DevGraph& g, long long x) {
     x = x < 0 ? 0 : (x > g.nlq ? g.nlq : x);
     return (long long)__ldg(g.Lq + x);
 }
-// vterm_exact (include/entropy.hpp:117-133), not degree-corrected: (d_out + d_in) log w,
-// or d_out log w for an undirected graph.
+// vterm_exact (include/entropy.hpp:117-133): (d_out + d_in) log w, or d_out log w for an
+// undirected graph; degree-corrected: lgamma(d_out + 1) + lgamma(d_in + 1), or the first
+// alone when undirected, whatever w.
 __device__ __forceinline__ long long np_vterm(const DevGraph& g, long long dout, long long din, long long w) {
+    if (g.dc) return np_lg(g, dout) + (g.np_und ? 0 : np_lg(g, din));
     return w == 0 ? 0 : (g.np_und ? dout : dout + din) * np_log(g, w);
 }
 // One changed cell of entries_dS: eterm(M + d) - eterm(M), off the diagonal.

@@ -135,6 +135,11 @@ def lib():
         L.ora_graph_model_edges.argtypes = [ctypes.c_void_p]
         L.ora_graph_set_model_edges.argtypes = [ctypes.c_void_p, ctypes.c_int64]
         L.ora_graph_set_undirected.argtypes = [ctypes.c_void_p, ctypes.c_int32]
+        L.ora_graph_set_degree_corrected.argtypes = [ctypes.c_void_p, ctypes.c_int32]
+        L.ora_log_q.restype = ctypes.c_double
+        L.ora_log_q.argtypes = [ctypes.c_int64, ctypes.c_int64]
+        L.ora_spence.restype = ctypes.c_double
+        L.ora_spence.argtypes = [ctypes.c_double]
         L.ora_graph_edges.argtypes = [ctypes.c_void_p, i32p, i32p]
         L.ora_extend.argtypes = [ctypes.c_void_p, i32p, ctypes.c_int64, ctypes.c_int64, i32p, ctypes.c_uint64, i32p]
         L.ora_reattach.argtypes = [ctypes.c_void_p, i32p, ctypes.c_int64, ctypes.c_int64, i32p, ctypes.c_uint64, i32p]
@@ -168,12 +173,20 @@ def philox(ctr, key):
     return out
 
 
+def log_q(n, k):
+    return float(lib().ora_log_q(int(n), int(k)))
+
+
+def spence(x):
+    return float(lib().ora_spence(float(x)))
+
+
 class Graph:
     """num_edges: the count the description lengths use (Graph::num_edges); the stored
     directed edges by default, half of them for an undirected edge list.  undirected:
-    args.undirected for the nonparametric entropy."""
+    args.undirected for the nonparametric entropy.  degree_corrected: args.degreecorrected."""
 
-    def __init__(self, num_vertices, src, dst, num_edges=None, undirected=False):
+    def __init__(self, num_vertices, src, dst, num_edges=None, undirected=False, degree_corrected=False):
         self.src = np.ascontiguousarray(src, dtype=np.int32)
         self.dst = np.ascontiguousarray(dst, dtype=np.int32)
         self.N = int(num_vertices)
@@ -183,6 +196,8 @@ class Graph:
             lib().ora_graph_set_model_edges(self.h, int(num_edges))
         if undirected:
             lib().ora_graph_set_undirected(self.h, 1)
+        if degree_corrected:
+            lib().ora_graph_set_degree_corrected(self.h, 1)
 
     def model_edges(self):
         return int(lib().ora_graph_model_edges(self.h))

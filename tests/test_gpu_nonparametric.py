@@ -175,3 +175,81 @@ def test_np_full_sbp_identical_c1(gpu, oracle):
     assert np.array_equal(a_g, a_o)
     assert abs(mdl_g - mdl_o) <= MDL_REL_TOL_CANONICAL * abs(mdl_o)
     assert st["merges"] == ost.merges and st["mcmc_iterations"] == ost.mcmc_iterations
+
+
+# ---- degree-corrected (args.degreecorrected; entropy.hpp:117-133, entropy.cpp:617-764,
+# :994-1110).  Every log_q term is computed in double and rounded to 2^-24 on each side;
+# the device's log/exp/pow may differ from the host's in a last bit, which moves a rounded
+# term by one unit in rare cases, so the tolerance is one unit per log_q term involved.
+
+DC_UNIT = 2.0 ** -24
+
+
+def dc_pair(gpu, oracle, n, e, blocks, B, seed, empty=2):
+    src, dst, _ = gpu.dcsbm.generate(n, e, blocks, seed=seed)
+    rng = np.random.default_rng(seed)
+    live = B - empty
+    a = rng.integers(0, live, n).astype(np.int32)
+    a[:live] = np.arange(live)
+    G = gpu.Graph(n, src, dst, degree_corrected=True)
+    O = oracle.Graph(n, src, dst, degree_corrected=True)
+    return G, O, gpu.Blockmodel(B, G, 0.5, a), oracle.Blockmodel(O, B, a), a
+
+
+def test_dc_toy(gpu, oracle, golden):
+    e = np.array(golden["edges"], np.int32)
+    G = gpu.Graph(11, e[:, 0], e[:, 1], degree_corrected=True)
+    O = oracle.Graph(11, e[:, 0], e[:, 1], degree_corrected=True)
+    assert G.degree_corrected()
+    gb = gpu.Blockmodel(3, G, 0.5, golden["assignment"])
+    ob = oracle.Blockmodel(O, 3, golden["assignment"])
+    m = gpu.entropy.nonparametric.mdl(gb)
+    assert abs(m - ob.np_mdl()[1]) <= 6 * DC_UNIT
+    t = ob.np_terms()
+    assert float_eq(t["sparse_entropy"], golden["nonparametric"]["degree_corrected"]["sparse_entropy"])
+    mv = golden["vertex_move"]
+    d = gpu.entropy.nonparametric.delta_mdl(gb, [mv["vertex"]], [mv["proposal"]])[0]
+    assert abs(d - ob.np_delta_mdl(mv["vertex"], mv["proposal"])[1] / 2**24) <= 8 * DC_UNIT
+
+
+@pytest.mark.parametrize("B", [6, 80, 700])
+def test_dc_mdl_and_deltas(gpu, oracle, B):
+    G, O, gb, ob, a = dc_pair(gpu, oracle, 2000, 24000, 9, B, seed=300 + B)
+    m = gpu.entropy.nonparametric.mdl(gb)
+    assert abs(m - ob.np_mdl()[1]) <= 2 * B * DC_UNIT
+    rng = np.random.default_rng(B)
+    v = rng.integers(0, 2000, 3000).astype(np.int32)
+    s = rng.integers(0, B, 3000).astype(np.int32)
+    d = np.asarray(gpu.entropy.nonparametric.delta_mdl(gb, v, s))
+    want = np.array([ob.np_delta_mdl(int(x), int(y))[1] for x, y in zip(v, s)], np.int64)
+    diff = np.abs(np.rint(d * 2**24).astype(np.int64) - want)
+    assert diff.max() <= 8
+    assert (diff == 0).mean() > 0.99
+
+
+def test_dc_single_moves_and_unsupported_sweeps(gpu, oracle):
+    G, O, gb, ob, a = dc_pair(gpu, oracle, 1500, 18000, 9, 60, seed=333)
+    args = gpu.Args(algorithm="hybrid_mcmc", nonparametric=True, seed=2)
+    rng = np.random.default_rng(5)
+    moved = 0
+    for _ in range(60):
+        v, p = int(rng.integers(1500)), int(rng.integers(60))
+        d = ob.read()
+        if d["sizes"][d["assignment"][v]] == 1:
+            continue
+        want = ob.np_delta_mdl(v, p)[1]
+        dS, did, _, _ = gpu.finetune.move_vertex(v, p, gb, G, args)
+        assert abs(round(dS * 2**24) - want) <= 8
+        if did:  # accepted by the canonical draw; the oracle applies the same move
+            m = np.full(1500, -1, np.int32)
+            m[v] = p
+            ob.apply_moves(m)
+            moved += 1
+        same_state(gb, ob)
+    assert moved > 0
+    with pytest.raises(gpu._lib.SbpGpuError) as e:
+        gpu.finetune.mcmc(0, G, gb, True, args)
+    assert e.value.status == 5
+    with pytest.raises(gpu._lib.SbpGpuError) as e:
+        gpu.entropy.nonparametric.block_merge_delta_mdl(gb, [0], [1])
+    assert e.value.status == 5

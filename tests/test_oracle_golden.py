@@ -364,3 +364,134 @@ def test_oracle_snowball_splits(oracle, split, init):
     assert b.num_blocks == 9 and np.bincount(d["assignment"], minlength=9).min() > 0
     # every vertex keeps its cluster or moves to one of the new blocks
     assert all(x == y or x >= 5 for x, y in zip(d["assignment"].tolist(), a.tolist()))
+
+
+# ---- degree-corrected nonparametric entropy (args.degreecorrected: entropy.hpp:117-133,
+# entropy.cpp:617-764, :994-1110)
+
+def _toy_dc(oracle, golden):
+    edges = np.array(golden["edges"], dtype=np.int32)
+    g = oracle.Graph(golden["num_vertices"], edges[:, 0], edges[:, 1], degree_corrected=True)
+    return g, oracle.Blockmodel(g, golden["num_blocks"], golden["assignment"])
+
+
+def _li2(z):
+    if z > 0.5:
+        return math.pi ** 2 / 6 - math.log(z) * math.log1p(-z) - _li2(1 - z)
+    s, p, k = 0.0, z, 1
+    while p / (k * k) > 1e-18 * max(s, 1e-300):
+        s += p / (k * k)
+        p *= z
+        k += 1
+    return s
+
+
+def _log_q(n, k):
+    """log_q (entropy.cpp:688-707) in plain Python, independently of the oracle."""
+    if n <= 0 or k < 1:
+        return 0.0
+    k = min(k, n)
+    if k < n ** 0.25:
+        lb = 0.0 if n - 1 == 0 or k - 1 == 0 else math.lgamma(n) - math.lgamma(k) - math.lgamma(n - k + 1)
+        return lb - math.lgamma(k + 1)
+    u = k / math.sqrt(n)
+    v, d = u, 1.0
+    while d > 1e-8:
+        nv = u * math.sqrt(_li2(-math.expm1(-v)))
+        d, v = abs(nv - v), nv
+    lf = math.log(v) - math.log1p(-math.exp(-v) * (1 + u * u / 2)) / 2 - math.log(2) * 1.5 - math.log(u) - math.log(math.pi)
+    return lf - math.log(n) + math.sqrt(n) * (2 * v / u - u * math.log1p(-math.exp(-v)))
+
+
+def _toy_degree_dl(golden):
+    """get_deg_dl_dist (entropy.cpp:709-743) on the toy blockmodel, from its edge list."""
+    from collections import Counter
+    n, a = golden["num_vertices"], golden["assignment"]
+    kout, kin = Counter(), Counter()
+    for u, v in golden["edges"]:
+        kout[u] += 1
+        kin[v] += 1
+    S = 0.0
+    for b in range(golden["num_blocks"]):
+        vs = [v for v in range(n) if a[v] == b]
+        S += _log_q(sum(kout[v] for v in vs), len(vs)) + _log_q(sum(kin[v] for v in vs), len(vs))
+        S -= sum(math.lgamma(c + 1) for c in Counter(kin[v] for v in vs).values())
+        S -= sum(math.lgamma(c + 1) for c in Counter(kout[v] for v in vs).values())
+        S += 2 * math.lgamma(len(vs) + 1)
+    return S
+
+
+def test_dc_toy_terms(oracle, golden):
+    """SPARSE_ENTROPY (nonparametric_entropy_test.cpp:22, :77-83) is the reference's known
+    answer.  Its DEGREE_DL (:26, :101-107) and the MDL built from it (:20) are not what
+    get_deg_dl_dist computes as written: restated independently above it gives 27.8710,
+    not 18.7445 (the reference's own MDL test compares with yet another constant, :70-71),
+    so the degree term is checked against that restatement instead."""
+    _, B = _toy_dc(oracle, golden)
+    npg, dc = golden["nonparametric"], golden["nonparametric"]["degree_corrected"]
+    t = B.np_terms()
+    assert float_eq(t["sparse_entropy"], dc["sparse_entropy"])
+    assert float_eq(t["partition_dl"], npg["partition_dl"])
+    assert float_eq(t["edges_dl"], npg["edges_dl"])
+    assert t["degree_dl"] == pytest.approx(_toy_degree_dl(golden), rel=1e-12)
+    lit, can = B.np_mdl()
+    assert lit == pytest.approx(t["sparse_entropy"] + t["partition_dl"] + t["degree_dl"] + t["edges_dl"], rel=1e-15)
+    assert abs(lit - can) <= 1e-6
+
+
+def test_dc_log_q_approaches_partition_counts(oracle):
+    """log_q is an approximation of the log of q(n, k), the number of partitions of n into
+    at most k parts: against exact counts it is within 4% at n = 8 and closes in as n grows."""
+    nmax, kmax = 2000, 400
+    q = np.zeros((nmax + 1, kmax + 1), dtype=object)
+    q[0, :] = 1
+    for n in range(1, nmax + 1):
+        for k in range(1, kmax + 1):
+            q[n, k] = q[n, k - 1] + (q[n - k, k] if n >= k else 0)
+    for n, k, tol in [(8, 4, 0.05), (50, 10, 0.01), (200, 20, 2e-3), (300, 300, 2e-3), (1000, 5, 3e-3),
+                      (1000, 30, 5e-4), (2000, 50, 2e-4), (2000, 400, 2e-4)]:
+        exact = math.log(q[n, min(k, n)])
+        assert abs(oracle.log_q(n, k) / exact - 1) < tol, (n, k)
+        assert oracle.log_q(n, k) == pytest.approx(_log_q(n, k), rel=1e-12)
+    assert oracle.log_q(0, 3) == 0.0 and oracle.log_q(5, 0) == 0.0
+
+
+def test_dc_spence_identities(oracle):
+    # spence(x) = Li2(1 - x): Li2(0) = 0, Li2(1) = pi^2/6, Li2(1/2) = pi^2/12 - log^2(2)/2,
+    # Li2(-1) = -pi^2/12
+    assert oracle.spence(1.0) == 0.0
+    assert oracle.spence(0.0) == pytest.approx(math.pi ** 2 / 6, rel=1e-15)
+    assert oracle.spence(0.5) == pytest.approx(math.pi ** 2 / 12 - math.log(2) ** 2 / 2, rel=1e-14)
+    assert oracle.spence(2.0) == pytest.approx(-math.pi ** 2 / 12, rel=1e-14)
+
+
+def test_dc_delta_tracks_mdl_on_random_moves(oracle):
+    """Degree-corrected vertex moves: the canonical delta equals the change of the
+    canonical MDL exactly (every log_q term is rounded once, the same way on both sides),
+    and the literal delta the reference's double arithmetic to within its rounding.  The
+    reference's vterm quirk for vertices with a self-loop applies here too."""
+    from sbp_gb300 import dcsbm
+    src, dst, _ = dcsbm.generate(300, 3000, 6, seed=19)
+    loops = set(src[src == dst].tolist())
+    g = oracle.Graph(300, src, dst, degree_corrected=True)
+    rng = np.random.default_rng(8)
+    a = rng.integers(0, 20, 300)
+    a[a == 19] = 18  # block 19 starts empty
+    B = oracle.Blockmodel(g, 20, a)
+    base_lit, base_can = B.np_mdl()
+    checked = 0
+    for _ in range(80):
+        v, s = int(rng.integers(300)), int(rng.integers(20))
+        if s == a[v]:
+            continue
+        lit, fx = B.np_delta_mdl(v, s)
+        assert abs(lit - fx / 2**24) <= 1e-5
+        if v in loops:
+            continue
+        a2 = a.copy()
+        a2[v] = s
+        after_lit, after_can = oracle.Blockmodel(g, 20, a2).np_mdl()
+        assert fx == round((after_can - base_can) * 2**24), (v, s)
+        assert abs(lit - (after_lit - base_lit)) <= 1e-7 * abs(base_lit)
+        checked += 1
+    assert checked > 40
