@@ -289,30 +289,43 @@ def profile_phase(args):
                       "seconds": time.perf_counter() - t0, "stats": st, "kernel_timing": ctx.read_timing()}))
 
 
+def _mixed_graph(n, seed):
+    from sbp_gb300 import dcsbm
+    r = np.random.default_rng(seed)
+    src, dst, planted = dcsbm.generate(int(n), 20 * int(n), int(np.sqrt(n) / 4) + 2, dmin=5, dmax=100,
+                                       ratio=float(r.uniform(1.5, 3.0)), seed=seed)
+    return int(n), src, dst, planted
+
+
 def mixed_graphs(count, n_lo, n_hi, seed_base=0):
     """Independent directed DCSBM graphs: N log-uniform in [n_lo, n_hi], about 20 N edges,
     floor(sqrt(N) / 4) + 2 planted blocks, within:between ratio uniform in [1.5, 3.0], degree
-    propensities power-law 2.1 in [5, 100]; graph i uses seed seed_base + i."""
-    from sbp_gb300 import dcsbm
+    propensities power-law 2.1 in [5, 100]; graph i uses seed seed_base + i.  Many graphs
+    are generated by a pool of spawned processes (before this process starts CUDA)."""
     rng = np.random.default_rng(20240 + seed_base)
     sizes = np.exp(rng.uniform(np.log(n_lo), np.log(n_hi), count)).astype(np.int64)
-    out = []
-    for i, n in enumerate(sizes):
-        r = np.random.default_rng(seed_base + i)
-        src, dst, planted = dcsbm.generate(int(n), 20 * int(n), int(np.sqrt(n) / 4) + 2, dmin=5, dmax=100,
-                                           ratio=float(r.uniform(1.5, 3.0)), seed=seed_base + i)
-        out.append((int(n), src, dst, planted))
-    return out
+    seeds = [seed_base + i for i in range(count)]
+    if count * float(np.mean(sizes)) < 2e6:
+        return [_mixed_graph(n, sd) for n, sd in zip(sizes, seeds)]
+    import concurrent.futures as cf
+    import multiprocessing as mp
+    with cf.ProcessPoolExecutor(max_workers=min(16, os.cpu_count() or 1), mp_context=mp.get_context("spawn")) as ex:
+        return list(ex.map(_mixed_graph, sizes, seeds, chunksize=4))
 
 
-def plain_one_at_a_time(graphs, sargs):
-    """The plain path: each graph uploaded, partitioned and read back in turn on one context."""
+def plain_one_at_a_time(graphs, sargs, only=None):
+    """The plain path: each graph uploaded, partitioned and read back in turn on one context
+    (graph i with seed i); `only`: the indices to run, others get None."""
     import torch
     import sbp_gb300 as sb
     ctx = sb.Context(0)
     ctx.set_cells_budget(256 << 20)
     results, service = [], []
     for i, (n, src, dst, _) in enumerate(graphs):
+        if only is not None and i not in only:
+            results.append(None)
+            service.append(None)
+            continue
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         G = sb.Graph(n, src, dst, ctx=ctx)
@@ -373,9 +386,21 @@ def served_workload(args):
     _b.build()
     graphs = mixed_graphs(args.jobs, 1000, args.max_vertices, seed_base=10000)
     sargs = sb.Args(algorithm="hybrid_mcmc")
-    plain, service = plain_one_at_a_time(graphs, sargs)
+    k = args.plain_sample if 0 < args.plain_sample < len(graphs) else len(graphs)
+    sample = set(np.random.default_rng(5).choice(len(graphs), k, replace=False).tolist())
+    plain, service = plain_one_at_a_time(graphs, sargs, only=sample)
+    fit = None
+    if k < len(graphs):
+        # service time of the requests not run on the plain path: a least-squares line in
+        # the edge count through the measured ones
+        xs = np.array([graphs[i][1].size for i in sorted(sample)], float)
+        ys = np.array([service[i] for i in sorted(sample)], float)
+        b, a = np.polyfit(xs, ys, 1)
+        r2 = 1.0 - float(np.sum((ys - (a + b * xs)) ** 2) / np.sum((ys - ys.mean()) ** 2))
+        fit = {"measured": k, "seconds_per_edge": b, "seconds_fixed": a, "r2": r2}
+        service = [service[i] if i in sample else a + b * graphs[i][1].size for i in range(len(graphs))]
     plain_rate = len(graphs) / float(np.sum(service))
-    rate = args.rate if args.rate else 0.8 * plain_rate  # 0.8 of the plain path's throughput
+    rate = args.rate if args.rate else args.rate_factor * plain_rate
     arrivals = np.cumsum(np.random.default_rng(77).exponential(1.0 / rate, len(graphs)))
     finish_plain, t_free = [], 0.0
     for a_t, s_t in zip(arrivals, service):
@@ -401,7 +426,7 @@ def served_workload(args):
             f.result()
         makespan = time.perf_counter() - t0
     lat = np.array([done[i][0] - arrivals[i] for i in range(len(graphs))])
-    same = all(np.array_equal(plain[i][0], done[i][1][0]) for i in range(len(graphs)))
+    same = all(np.array_equal(plain[i][0], done[i][1][0]) for i in sorted(sample))
     print(json.dumps({"workload": "served", "metric": "jobs/s", "value": len(graphs) / makespan, "unit": "jobs/s",
                       "requests": len(graphs), "offered_rate_per_s": rate, "workers": args.workers,
                       "cuda_device_max_connections": os.environ.get("CUDA_DEVICE_MAX_CONNECTIONS"),
@@ -409,6 +434,10 @@ def served_workload(args):
                       "plain_p50_ms": 1e3 * float(np.percentile(lat_plain, 50)),
                       "plain_p99_ms": 1e3 * float(np.percentile(lat_plain, 99)),
                       "plain_jobs_per_s": plain_rate, "identical_to_plain": bool(same),
+                      "plain_service": "measured for every request" if fit is None else
+                      dict(fit, note="measured for a seeded sample (their partitions compared), the rest "
+                                     "predicted by the fit"),
+                      "served_s": makespan,
                       "mean_nmi": float(np.mean([sb.evaluate.nmi(graphs[i][3], done[i][1][0])
                                                  for i in range(len(graphs))])),
                       "config": {"workload": "%d requests, Poisson arrivals at %.2f/s, N log-uniform in [1000, %d], "
@@ -440,6 +469,10 @@ def main():
     ap.add_argument("--hbm-budget", type=int, default=64 << 30)
     ap.add_argument("--rate", type=float, default=0.0, help="served: offered requests/s (0: derived)")
     ap.add_argument("--max-vertices", type=int, default=50000)
+    ap.add_argument("--plain-sample", type=int, default=0,
+                    help="served: run only this many requests on the plain path (0: all)")
+    ap.add_argument("--rate-factor", type=float, default=0.8,
+                    help="served: offered rate as a multiple of the plain path's throughput")
     args = ap.parse_args()
     globals()["CONFIG"] = args.config
     if args.impl == "reference":
