@@ -426,7 +426,8 @@ def served_workload(args):
             f.result()
         makespan = time.perf_counter() - t0
     lat = np.array([done[i][0] - arrivals[i] for i in range(len(graphs))])
-    same = all(np.array_equal(plain[i][0], done[i][1][0]) for i in sorted(sample))
+    differ = [i for i in sorted(sample) if not np.array_equal(plain[i][0], done[i][1][0])]
+    same = not differ
     print(json.dumps({"workload": "served", "metric": "jobs/s", "value": len(graphs) / makespan, "unit": "jobs/s",
                       "requests": len(graphs), "offered_rate_per_s": rate, "workers": args.workers,
                       "cuda_device_max_connections": os.environ.get("CUDA_DEVICE_MAX_CONNECTIONS"),
@@ -434,6 +435,8 @@ def served_workload(args):
                       "plain_p50_ms": 1e3 * float(np.percentile(lat_plain, 50)),
                       "plain_p99_ms": 1e3 * float(np.percentile(lat_plain, 99)),
                       "plain_jobs_per_s": plain_rate, "identical_to_plain": bool(same),
+                      "differing_requests": [{"request": i, "num_vertices": graphs[i][0], "blocks": [plain[i][1], done[i][1][1]],
+                                              "mdl": [plain[i][2], done[i][1][2]]} for i in differ],
                       "plain_service": "measured for every request" if fit is None else
                       dict(fit, note="measured for a seeded sample (their partitions compared), the rest "
                                      "predicted by the fit"),

@@ -678,13 +678,18 @@ __global__ void __launch_bounds__(kCcThreads, 1) k_carry_cluster(
         // merge k goes to CTA k % cs; a CTA's merges share its warps (row walk and column
         // walk on separate warps when there are few).  The target's own row and column
         // receive their new keys through a staging slice and one bulk append; the lists of
-        // third blocks, which several merges may extend at once, take single keys.
+        // third blocks, which several merges may extend at once, take single keys.  A third
+        // block may be another merge's target (a key of this merge's source), so every CTA
+        // finishes its single-key appends before any CTA reserves room in a target's list:
+        // all CTAs take the same number of passes, with cluster barriers between the phases.
         {
             const int nm = ctl.nm;
             const int mine = nm > rank ? (nm - rank + cs - 1) / cs : 0;
+            const int passes = (((nm + cs - 1) / cs) + kCcWarps / 2 - 1) / (kCcWarps / 2);
             int32_t* my_stage = stage_buf + (int64_t)rank * (kCcWarps / 2) * 2 * kCcStage;
-            for (int base = 0; base < mine; base += kCcWarps / 2) {
-                const int here = min(kCcWarps / 2, mine - base);
+            for (int pass = 0; pass < passes; ++pass) {
+                const int base = pass * (kCcWarps / 2);
+                const int here = max(0, min(kCcWarps / 2, mine - base));
                 const int wpm = here == 1 ? 16 : here == 2 ? 8 : here <= 4 ? 4 : 2;
                 const int slot = warp / wpm;
                 if (tid < kCcWarps) (&sh.st_n[0][0])[tid] = 0;
@@ -729,7 +734,7 @@ __global__ void __launch_bounds__(kCcThreads, 1) k_carry_cluster(
                                       });
                     }
                 }
-                __syncthreads();
+                cluster.sync();  // every CTA's single-key appends of this pass are done
                 if (tid < 2 * here) {
                     const int sl = tid >> 1, which = tid & 1;
                     const int32_t mt = ctl.m_to[rank + cs * (base + sl)];
@@ -758,7 +763,7 @@ __global__ void __launch_bounds__(kCcThreads, 1) k_carry_cluster(
                     bm.sizes[mf] = 0;
                     parent[mf] = mt;
                 }
-                __syncthreads();
+                cluster.sync();  // and the reservations before the next pass appends again
             }
             // this round's candidate blocks leave cand_of
             if (j < ncand && lane == 0) cand_of[ctl.c_blk[j]] = -1;

@@ -54,12 +54,15 @@ __device__ __forceinline__ void list_push1(int32_t* head, const DevChain& ch, in
 // time: a slot of the head chunk is claimed with an atomic increment of its count (a count
 // past the capacity means the chunk is full; readers clamp it), and a full or missing head
 // is replaced by a new chunk published with a compare-and-swap.  A chunk whose publication
-// loses the race is left unused.  No thread may read the list concurrently.
+// loses the race is left unused.  No thread may read the list concurrently.  The appending
+// threads may sit in different CTAs of a cluster: a new chunk's header is published with a
+// device-scope fence before the swap, and the head is read with acquire semantics, so a
+// thread that finds the chunk also sees its count and capacity.
 __device__ __forceinline__ void list_push1_shared(int32_t* head, const DevChain& ch, int32_t b, int32_t item,
                                                   DevFlags* flags) {
     volatile int32_t* vpool = ch.pool;
     for (int tries = 0; tries < 64; ++tries) {
-        const int32_t c = ((volatile int32_t*)head)[b];
+        const int32_t c = ld_acquire_gpu(head + b);
         if (c >= 0) {
             const int32_t pos = atomicAdd(ch.pool + c + 1, 1);
             if (pos < vpool[c + 2]) {
@@ -77,7 +80,7 @@ __device__ __forceinline__ void list_push1_shared(int32_t* head, const DevChain&
         ch.pool[nc + 1] = 1;
         ch.pool[nc + 2] = cap;
         ch.pool[nc + 3] = item;
-        __threadfence_block();
+        __threadfence();
         if (atomicCAS(head + b, c, nc) == c) return;
     }
     atomicOr(&flags->err, ERR_STATE);

@@ -278,6 +278,12 @@ __device__ __forceinline__ unsigned long long cell_key(int32_t r, int32_t c) {
 __device__ __forceinline__ uint32_t cell_slot(unsigned long long k, uint32_t mask) {
     return (uint32_t)((k * 0x9E3779B97F4A7C15ull) >> 32) & mask;
 }
+// A 32-bit load with acquire semantics at device scope.
+__device__ __forceinline__ int32_t ld_acquire_gpu(const int32_t* p) {
+    int32_t v;
+    asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
 __device__ __forceinline__ ulonglong2 ld_slot(const ulonglong2* p) {
     ulonglong2 v;
     asm volatile("ld.volatile.v2.u64 {%0, %1}, [%2];" : "=l"(v.x), "=l"(v.y) : "l"(p));
