@@ -278,6 +278,124 @@ __global__ void __launch_bounds__(kCcThreads, 1) k_carry_cluster(
                     sh.a_b[r] = b;
                     sh.a_c[r] = c;
                 }
+                // The replay runs first in parallel, as far as it provably agrees with the
+                // sequential rule: candidate i (thread i) merges when its recomputed delta is at
+                // most the next key -- the next candidate's or the bound -- and is put back
+                // otherwise, unless it already shares its target's block.  That decision leaves
+                // out the put-back list, so it holds while no entry put back earlier in the round
+                // would pop before candidate i or lower the value it is compared with; P is the
+                // first candidate where that fails.  The pass also ends at the first candidate S
+                // that an earlier merge of the round made stale (the prefix OR of the merges'
+                // conflict sets) and after the merge that completes the pass (L).  The
+                // sequential loop below takes over at P when P comes first.
+                __shared__ uint32_t sp_or[kCcMaxW / 32][kCcWords];
+                __shared__ long long sp_md[kCcMaxW / 32];
+                __shared__ int32_t sp_mb[kCcMaxW / 32], sp_cnt[kCcMaxW / 32];
+                __shared__ uint32_t sp_stl[kCcWords], sp_pend[kCcWords];
+                __shared__ int32_t sp_P, sp_S, sp_L, sp_nm, sp_c[3];
+                if (tid < kCcWords) sp_stl[tid] = sp_pend[tid] = 0u;
+                if (tid == 0) {
+                    sp_P = ncand;
+                    sp_S = ncand;
+                    sp_L = sh.merged < num_to_merge ? INT_MAX : 0;  // after the merge that completes the pass
+                    sp_nm = 0;
+                    sp_c[0] = sp_c[1] = sp_c[2] = 0;
+                }
+                __syncthreads();  // the ranks too
+                const bool lead = tid < kCcMaxW;  // thread i < 256 takes candidate i
+                const int ci0 = tid;
+                bool x_same = false, x_pb = false, x_mg = false;
+                long long x_key = 0, x_T0 = LLONG_MAX, x_exd = LLONG_MAX;
+                int32_t x_kb = 0, x_exb = INT_MAX;
+                int x_before = 0;
+                uint32_t x_ex = 0u;  // word `warp` of the prefix OR before this candidate
+                if (lead) {
+                    const bool hc = ci0 < ncand;
+                    const long long act = hc ? sh.c_act[ci0] : 0;
+                    x_key = hc ? sh.c_dS[ci0] : 0;
+                    x_kb = hc ? sh.c_blk[ci0] : 0;
+                    const bool hc2 = ci0 + 1 < ncand;
+                    x_T0 = sh.has_bound ? sh.b_dS : LLONG_MAX;
+                    if (hc2) x_T0 = min(x_T0, sh.c_dS[ci0 + 1]);
+                    x_same = hc && sh.c_to[ci0] == x_kb;
+                    x_pb = hc && !x_same && (hc2 || sh.has_bound) && act > x_T0;
+                    x_mg = hc && !x_same && !x_pb;
+                    // in-warp prefix minimum, in (delta, block) order, of the entries put back
+                    long long md = x_pb ? act : LLONG_MAX;
+                    int32_t mb = x_pb ? x_kb : INT_MAX;
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const long long od = __shfl_up_sync(SBP_FULL_MASK, md, o);
+                        const int32_t ob = __shfl_up_sync(SBP_FULL_MASK, mb, o);
+                        if (lane >= o && qless(od, ob, md, mb)) {
+                            md = od;
+                            mb = ob;
+                        }
+                    }
+                    x_exd = __shfl_up_sync(SBP_FULL_MASK, md, 1);
+                    x_exb = __shfl_up_sync(SBP_FULL_MASK, mb, 1);
+                    if (lane == 0) {
+                        x_exd = LLONG_MAX;
+                        x_exb = INT_MAX;
+                    }
+                    // in-warp prefix OR of the merges' conflict sets, and the merges before
+#pragma unroll
+                    for (int w = 0; w < kCcWords; ++w) {
+                        uint32_t v = x_mg ? sh.inv[ci0][w] : 0u;
+#pragma unroll
+                        for (int o = 1; o < 32; o <<= 1) {
+                            const uint32_t y = __shfl_up_sync(SBP_FULL_MASK, v, o);
+                            if (lane >= o) v |= y;
+                        }
+                        const uint32_t e = __shfl_up_sync(SBP_FULL_MASK, v, 1);
+                        if (w == warp) x_ex = lane == 0 ? 0u : e;
+                        if (lane == 31) sp_or[warp][w] = v;
+                    }
+                    const unsigned mgm = __ballot_sync(SBP_FULL_MASK, x_mg);
+                    x_before = __popc(mgm & lanemask_lt());
+                    if (lane == 31) {
+                        sp_md[warp] = md;
+                        sp_mb[warp] = mb;
+                        sp_cnt[warp] = __popc(mgm);
+                    }
+                }
+                __syncthreads();
+                if (lead && ci0 < ncand) {
+                    // add the warps before this one
+                    long long qd = x_exd;
+                    int32_t qb = x_exb;
+                    for (int w = 0; w < warp; ++w) {
+                        if (qless(sp_md[w], sp_mb[w], qd, qb)) {
+                            qd = sp_md[w];
+                            qb = sp_mb[w];
+                        }
+                        x_before += sp_cnt[w];
+                        x_ex |= sp_or[w][warp];
+                    }
+                    const bool anypb = qb != INT_MAX;
+                    if (anypb && !(qd >= x_T0 && !qless(qd, qb, x_key, x_kb))) atomicMin(&sp_P, ci0);
+                    if ((x_ex >> (ci0 & 31)) & 1u) atomicMin(&sp_S, ci0);  // ci0 >> 5 == warp
+                    if (x_mg && (long long)x_before == num_to_merge - sh.merged - 1) atomicMin(&sp_L, ci0 + 1);
+                }
+                __syncthreads();
+                const int x_end = min(sp_P, min(sp_S, sp_L));
+                if (lead && ci0 < x_end) {
+                    if (x_mg) {
+                        sh.m_from[x_before] = x_kb;
+                        sh.m_to[x_before] = sh.c_to[ci0];
+                        atomicAdd(&sp_nm, 1);
+#pragma unroll
+                        for (int w = 0; w < kCcWords; ++w) {
+                            const uint32_t v = sh.inv[ci0][w];
+                            if (v) atomicOr(&sp_stl[w], v);
+                        }
+                    }
+                    if (x_pb) {
+                        const int r = sh.a_rank[ci0];
+                        atomicOr(&sp_pend[r >> 5], 1u << (r & 31));
+                    }
+                    atomicAdd(&sp_c[sh.c_src[ci0]], 1);
+                }
                 __syncthreads();
                 if (tid == 0) {
                     const bool hb = sh.has_bound;
@@ -285,7 +403,10 @@ __global__ void __launch_bounds__(kCcThreads, 1) k_carry_cluster(
                     const int32_t bnd_blk = sh.b_blk;
                     uint32_t pend[kCcWords], stl[kCcWords];
 #pragma unroll
-                    for (int w = 0; w < kCcWords; ++w) pend[w] = stl[w] = 0u;
+                    for (int w = 0; w < kCcWords; ++w) {
+                        pend[w] = sp_pend[w];
+                        stl[w] = sp_stl[w];
+                    }
                     auto bit_of = [&](const uint32_t* m, int x) {
                         uint32_t v = 0;
 #pragma unroll
@@ -304,8 +425,8 @@ __global__ void __launch_bounds__(kCcThreads, 1) k_carry_cluster(
                         for (int w = 0; w < kCcWords; ++w)
                             if (w == (x >> 5)) pend[w] ^= 1u << (x & 31);
                     };
-                    int i = 0, nm = 0, c0 = 0, c1 = 0, c2 = 0;
-                    int pr = -1;  // rank of the put-back list's head, or -1
+                    int i = x_end, nm = sp_nm, c0 = sp_c[0], c1 = sp_c[1], c2 = sp_c[2];
+                    int pr = first();  // rank of the put-back list's head, or -1
                     // candidate i's fields in registers, the next one's loaded as i advances
                     long long cd = 0, cact = 0;
                     int32_t cb = 0, cto = 0, csrc = 0;
@@ -319,9 +440,11 @@ __global__ void __launch_bounds__(kCcThreads, 1) k_carry_cluster(
                         }
                     };
                     load_c();
-                    long long qd = 0;
-                    int32_t qb = 0;
-                    while (merged0 + nm < num_to_merge) {
+                    long long qd = pr >= 0 ? sh.a_d[pr] : 0;
+                    int32_t qb = pr >= 0 ? sh.a_b[pr] : 0;
+                    // resume where the parallel pass could not decide (nothing left otherwise)
+                    const bool resume = x_end == sp_P && x_end < sp_L;
+                    while (resume && merged0 + nm < num_to_merge) {
                         const bool hc = i < ncand, hq = pr >= 0;
                         if (!hc && !hq) break;  // queue empty
                         const bool fromq = hq && (!hc || qless(qd, qb, cd, cb));

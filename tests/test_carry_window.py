@@ -216,3 +216,125 @@ def test_chain_window_ballot_stop_matches_serial_replay(seed):
         p = rng.choice([0.05, 0.3, 0.8])
         conf = [sum(1 << u for u in range(j) if accepted[u] and rng.random() < p) for j in range(wn)]
         assert _ballot_stop(conf, accepted, wn) == _serial_stop(conf, accepted, wn)
+
+
+# ---- the cluster carry-out's greedy replay (sbp_gb300/csrc/carry_cluster.cu): the
+# parallel first pass plus the single-thread continuation against the single-thread replay
+# alone, on random rounds with ties, put-backs that pop again, stale candidates and the
+# merge limit.
+
+def _qless(a, b):
+    return a < b  # (delta, block) pairs compare lexicographically
+
+
+def _replay_seq(c, st):
+    """The single-thread replay from state st = (i, nm, pend ranks, stl set)."""
+    n, hb, bound, need = c["n"], c["hb"], c["bound"], c["need"]
+    keys, act, blk, to, inv, rank = c["keys"], c["act"], c["blk"], c["to"], c["inv"], c["rank"]
+    by_rank = sorted(range(n), key=lambda j: (act[j], blk[j]))
+    i, merges, pend, stl = st
+    merges, pend, stl = list(merges), set(pend), set(stl)
+    while len(merges) < need:
+        hc, hq = i < n, bool(pend)
+        if not hc and not hq:
+            break
+        if hq:
+            r = min(pend)
+            q = (act[by_rank[r]], blk[by_rank[r]])
+        fromq = hq and (not hc or _qless(q, keys[i]))
+        k = q if fromq else keys[i]
+        if hb and _qless(bound, k):
+            break
+        if fromq:
+            ci = by_rank[r]
+            if ci in stl:
+                break
+            pend.discard(r)
+            merges.append((blk[ci], to[ci]))
+            stl |= inv[ci]
+            continue
+        if i in stl:
+            break
+        ci = i
+        i += 1
+        if to[ci] == blk[ci]:
+            continue
+        hc2, hq = i < n, bool(pend)
+        if hc2 or hq or hb:
+            top = bound[0] if hb else float("inf")
+            if hc2:
+                top = min(top, keys[i][0])
+            if hq:
+                top = min(top, act[by_rank[min(pend)]])
+            if act[ci] > top:
+                pend.add(rank[ci])
+                continue
+        merges.append((blk[ci], to[ci]))
+        stl |= inv[ci]
+    return i, merges, pend, stl
+
+
+def _replay_parallel(c):
+    """The device's parallel first pass, then the single-thread loop from where it stopped."""
+    n, hb, bound, need = c["n"], c["hb"], c["bound"], c["need"]
+    keys, act, blk, to, inv, rank = c["keys"], c["act"], c["blk"], c["to"], c["inv"], c["rank"]
+    same = [to[i] == blk[i] for i in range(n)]
+    T0 = []
+    for i in range(n):
+        t = bound[0] if hb else float("inf")
+        if i + 1 < n:
+            t = min(t, keys[i + 1][0])
+        T0.append(t)
+    pb = [not same[i] and (i + 1 < n or hb) and act[i] > T0[i] for i in range(n)]
+    mg = [not same[i] and not pb[i] for i in range(n)]
+    P, S, L = n, n, (1 << 30) if need > 0 else 0
+    qmin, before, ex = None, 0, set()
+    for i in range(n):
+        if qmin is not None and not (qmin[0] >= T0[i] and not _qless(qmin, keys[i])):
+            P = min(P, i)
+        if i in ex:
+            S = min(S, i)
+        if mg[i] and before == need - 1:
+            L = min(L, i + 1)
+        if pb[i] and (qmin is None or _qless((act[i], blk[i]), qmin)):
+            qmin = (act[i], blk[i])
+        if mg[i]:
+            before += 1
+            ex |= inv[i]
+    end = min(P, S, L)
+    merges, pend, stl = [], set(), set()
+    for i in range(end):
+        if mg[i]:
+            merges.append((blk[i], to[i]))
+            stl |= inv[i]
+        if pb[i]:
+            pend.add(rank[i])
+    if end == P and end < L:
+        return _replay_seq(c, (end, merges, pend, stl))
+    return end, merges, pend, stl
+
+
+def _round(seed):
+    rng = random.Random(seed)
+    n = rng.randint(1, 40)
+    hb = rng.random() < 0.7
+    vals = sorted((rng.randrange(-6, 6), b) for b in rng.sample(range(1000), n + 1))
+    keys, bound = vals[:n], vals[n]
+    blk = [k[1] for k in keys]
+    act = [k[0] + rng.choice([0, 0, 1, 2, -1, rng.randrange(-3, 8)]) for k in keys]
+    to = [b if rng.random() < 0.1 else rng.randrange(1000, 2000) for b in blk]
+    inv = [set(j for j in range(n) if j != i and rng.random() < rng.choice([0.0, 0.02, 0.1])) for i in range(n)]
+    order = sorted(range(n), key=lambda j: (act[j], blk[j]))
+    rank = [0] * n
+    for r, j in enumerate(order):
+        rank[j] = r
+    need = rng.choice([n + 5, rng.randint(0, n)])
+    return dict(n=n, hb=hb, bound=bound, need=need, keys=keys, act=act, blk=blk, to=to, inv=inv, rank=rank)
+
+
+def test_parallel_replay_equals_single_thread():
+    for seed in range(6000):
+        c = _round(seed)
+        want = _replay_seq(c, (0, [], set(), set()))
+        got = _replay_parallel(c)
+        assert got[0] == want[0] and got[1] == want[1] and got[2] == want[2], seed
