@@ -86,10 +86,13 @@ void* sbpgpu_ctx_stream(sbpgpu_ctx* ctx);
 sbpgpu_status sbpgpu_ctx_set_cells_budget(sbpgpu_ctx* ctx, int64_t bytes);
 /* Smallest block count at which the sequential phases -- the Metropolis-Hastings chain and
  * the exact merge carry-out -- are evaluated in wide windows spread over a thread-block
- * cluster instead of one CTA (default 65536; 0: always, for the chain once the blockmodel
- * has more than 128 blocks).  Results do not depend on it.  No counterpart in the
- * reference. */
+ * cluster instead of one CTA; sets both thresholds (defaults: 65536 for the carry-out, 129
+ * for the chain; 0: always, for the chain once the blockmodel has more than 128 blocks).
+ * Results do not depend on them.  No counterpart in the reference. */
 sbpgpu_status sbpgpu_ctx_set_cluster_blocks(sbpgpu_ctx* ctx, int64_t min_blocks);
+/* The chain's threshold alone (default 129).  The partition server's workers set it to
+ * 65536, so that concurrent jobs keep their chains on one SM each below that size. */
+sbpgpu_status sbpgpu_ctx_set_chain_cluster_blocks(sbpgpu_ctx* ctx, int64_t min_blocks);
 /* Requests (requested != 0) or withdraws cancellation of the context's running
  * sbpgpu_sbp; safe to call from another thread.  The partition checks the request between
  * golden-section steps, when none of its work is in flight on the device, withdraws it and

@@ -94,6 +94,7 @@ SIGNATURES = {
     "sbpgpu_ctx_stream": (vp, [vp]),
     "sbpgpu_ctx_set_cells_budget": (ctypes.c_int, [vp, ctypes.c_int64]),
     "sbpgpu_ctx_set_cluster_blocks": (ctypes.c_int, [vp, ctypes.c_int64]),
+    "sbpgpu_ctx_set_chain_cluster_blocks": (ctypes.c_int, [vp, ctypes.c_int64]),
     "sbpgpu_ctx_set_cancel": (ctypes.c_int, [vp, ctypes.c_int32]),
     "sbpgpu_ctx_inject_alloc_failure": (ctypes.c_int, [vp, ctypes.c_int64]),
     "sbpgpu_graph_create": (ctypes.c_int, [vp, ctypes.c_int64, ctypes.c_int64, i32p, i32p, ctypes.POINTER(vp)]),

@@ -93,9 +93,14 @@ class Context:
         self.check(self.lib.sbpgpu_ctx_set_cells_budget(self.h, int(nbytes)))
 
     def set_cluster_blocks(self, min_blocks):
-        """Smallest block count at which the MH chain runs on a thread-block cluster
-        (0: whenever there are more than 128 blocks); results do not depend on it."""
+        """Smallest block count at which the MH chain and the merge carry-out run on a
+        thread-block cluster (defaults 129 and 65536; 0: always, the chain once there are
+        more than 128 blocks); results do not depend on it."""
         self.check(self.lib.sbpgpu_ctx_set_cluster_blocks(self.h, int(min_blocks)))
+
+    def set_chain_cluster_blocks(self, min_blocks):
+        """The MH chain's threshold alone (default 129)."""
+        self.check(self.lib.sbpgpu_ctx_set_chain_cluster_blocks(self.h, int(min_blocks)))
 
     def set_cancel(self, requested=True):
         """Requests (or withdraws) cancellation of the running partition on this context;

@@ -121,7 +121,11 @@ struct sbpgpu_ctx {
     std::string err;
     bool timing = false;
     int64_t cells_budget = int64_t(64) << 30;  // dense cells of the sequential phases, bytes
-    int64_t cluster_blocks = 65536;             // smallest B whose sequential phases run on a cluster
+    int64_t cluster_blocks = 65536;             // smallest B whose carry-out runs on a cluster
+    // smallest B whose MH chain runs on a cluster (it always does when B > 128 by default:
+    // measured on the C3 steps from 62,500 to 489 blocks, the cluster chain took 17.6 s
+    // where the one-CTA window took 21.0 s)
+    int64_t chain_cluster_blocks = 129;
     DevFlags* flags_host = nullptr;            // pinned staging of the device flags
     std::vector<TimedSpan> pending;
     std::vector<cudaEvent_t> free_events;
@@ -550,7 +554,7 @@ void chain_run(sbpgpu_bm* bm, const int32_t* order, int32_t n, int32_t max_k, in
     const bool window = mh_window_plan(bm->d.B, max_k, g->w, &plan);
     // Many blocks, or a blockmodel whose dense cells exceed the budget: the window spread
     // over a thread-block cluster, cells dense when the budget holds them, else hashed.
-    if ((B >= g->ctx->cluster_blocks || !window) && B > kWinSharedMax && max_k <= 4096 && ensure_cluster(g)) {
+    if ((B >= g->ctx->chain_cluster_blocks || !window) && B > kWinSharedMax && max_k <= 4096 && ensure_cluster(g)) {
         const bool hashed = !g->w.cells || mh_window_cells((int32_t)B) > g->w.cells_elems;
         if (hashed) chain_init(bm->d, g->w, (uint64_t)(2 * k_sum + 4 * (int64_t)n), g->ctx->stream);
         {
@@ -1190,6 +1194,13 @@ void* sbpgpu_ctx_stream(sbpgpu_ctx* ctx) { return ctx ? (void*)ctx->stream : nul
 sbpgpu_status sbpgpu_ctx_set_cluster_blocks(sbpgpu_ctx* ctx, int64_t min_blocks) {
     if (!ctx || min_blocks < 0) return SBPGPU_EINVAL;
     ctx->cluster_blocks = min_blocks;
+    ctx->chain_cluster_blocks = min_blocks;
+    return SBPGPU_OK;
+}
+
+sbpgpu_status sbpgpu_ctx_set_chain_cluster_blocks(sbpgpu_ctx* ctx, int64_t min_blocks) {
+    if (!ctx || min_blocks < 0) return SBPGPU_EINVAL;
+    ctx->chain_cluster_blocks = min_blocks;
     return SBPGPU_OK;
 }
 

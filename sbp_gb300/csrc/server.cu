@@ -100,7 +100,11 @@ void run_job(sbpgpu_ctx* ctx, JobState* st) {
 void worker(sbpgpu_server* s) {
     sbpgpu_ctx* ctx = nullptr;
     const sbpgpu_status cs = sbpgpu_ctx_create(s->device, &ctx);
-    if (cs == SBPGPU_OK) sbpgpu_ctx_set_cells_budget(ctx, s->cells_budget);
+    if (cs == SBPGPU_OK) {
+        sbpgpu_ctx_set_cells_budget(ctx, s->cells_budget);
+        // many jobs share the device: their chains stay on one SM each below 65,536 blocks
+        sbpgpu_ctx_set_chain_cluster_blocks(ctx, 65536);
+    }
     while (true) {
         std::unique_lock<std::mutex> lk(s->mu);
         s->cv_work.wait(lk, [&] { return admissible(s) || (s->stop && s->pending.empty()); });

@@ -21,6 +21,7 @@ def cluster_ctx(gpu):
     ctx.set_cluster_blocks(0)
     yield ctx
     ctx.set_cluster_blocks(65536)
+    ctx.set_chain_cluster_blocks(129)
     ctx.set_cells_budget(16 << 30)
 
 

@@ -11,7 +11,7 @@ change the number of non-empty blocks occur."""
 import numpy as np
 import pytest
 
-from test_gpu_parity import same_state
+from test_gpu_parity import chain_kernel, same_state
 
 pytestmark = pytest.mark.gpu
 
@@ -116,17 +116,20 @@ def test_np_gibbs_batch_identical(gpu, oracle, B):
         assert abs(gpu.entropy.nonparametric.mdl(gb) - ob.np_mdl()[1]) <= MDL_REL_TOL_CANONICAL * ob.np_mdl()[1]
 
 
+@pytest.mark.parametrize("chain", ["window", "cluster"])
 @pytest.mark.parametrize("n,B", [(2500, 8), (2500, 120), (2500, 1500), (24000, 16000)])
-def test_np_mh_chain_identical(gpu, oracle, n, B):
-    """The windowed chain's three cell stores; vertices without edges propose random blocks,
-    some of them empty, so accepted moves change the non-empty block count."""
+def test_np_mh_chain_identical(gpu, oracle, n, B, chain):
+    """The windowed chain's three cell stores, on one CTA and on the cluster; vertices
+    without edges propose random blocks, some of them empty, so accepted moves change the
+    non-empty block count."""
     G, O, gb, ob, a = np_pair(gpu, oracle, n, 12 * n, 9, B, seed=250 + B, isolated=200, empty=4)
     N = a.size
     rng = np.random.default_rng(B)
     order = np.concatenate([rng.permutation(n)[:500], np.arange(n, N)])
     order = rng.permutation(order).astype(np.int32)
     args = gpu.Args(algorithm="hybrid_mcmc", nonparametric=True)
-    applied = gpu.finetune.mh_chain(gb, order, seed=8, iteration=1, step=3, args=args)
+    with chain_kernel(gpu, chain):
+        applied = gpu.finetune.mh_chain(gb, order, seed=8, iteration=1, step=3, args=args)
     want = ob.mh_chain(order, 8, 1, 3, oracle.make_config("hybrid_mcmc", nonparametric=True))
     assert applied == want
     same_state(gb, ob)

@@ -4,6 +4,8 @@ accept/reject decisions must be bit-exact; delta-MDL values are exact multiples 
 2^-24 on both sides and must be identical (tolerance 0); the whole-blockmodel MDL
 must match the oracle's canonical value within 1e-12 relative and the reference's
 literal float-log value within 1e-9 relative."""
+import contextlib
+
 import numpy as np
 import pytest
 
@@ -18,6 +20,19 @@ def same_state(gb, ob):
     d, o = gb.read(), ob.read()
     for k in ("assignment", "d_out", "d_in", "d_tot", "sizes", "rows", "cols", "counts"):
         assert np.array_equal(np.asarray(d[k], np.int64), np.asarray(o[k], np.int64)), k
+
+
+@contextlib.contextmanager
+def chain_kernel(gpu, kind):
+    """Runs the MH chain on the one-CTA window ("window", the kernel below 65,536 blocks
+    when many jobs share the device) or on the thread-block cluster ("cluster", the
+    default above 128 blocks)."""
+    ctx = gpu.core.default_context()
+    ctx.set_chain_cluster_blocks(65536 if kind == "window" else 129)
+    try:
+        yield
+    finally:
+        ctx.set_chain_cluster_blocks(129)
 
 
 def make_pair(gpu, oracle, n, e, blocks, B, seed, assignment=None):
@@ -161,16 +176,18 @@ def test_gibbs_apply_size_one_rule(gpu, oracle):
         same_state(gb, ob)
 
 
+@pytest.mark.parametrize("chain", ["window", "cluster"])
 @pytest.mark.parametrize("n,B,cells", [(2500, 8, "dense"), (2500, 120, "dense"), (2500, 1500, "dense"),
                                        (9000, 5000, "dense"), (24000, 16000, "dense"), (9000, 5000, "hash")])
-def test_mh_chain_identical(gpu, oracle, n, B, cells):
+def test_mh_chain_identical(gpu, oracle, n, B, cells, chain):
     """The windowed chain with cells in shared memory (B <= 128), dense in global memory
-    with degrees in shared memory, and with degrees in global memory (B = 16000); with a
-    zero dense budget, B > 4096 runs the one-vertex-at-a-time hashed chain."""
+    with degrees in shared memory, and with degrees in global memory (B = 16000), on one CTA
+    and on the cluster; with a zero dense budget the cluster chain over hashed cells."""
     ctx = gpu.core.default_context()
     ctx.set_cells_budget(0 if cells == "hash" else 16 << 30)
     try:
-        _mh_chain_case(gpu, oracle, n, B)
+        with chain_kernel(gpu, chain):
+            _mh_chain_case(gpu, oracle, n, B)
     finally:
         ctx.set_cells_budget(16 << 30)
 
@@ -285,13 +302,16 @@ def test_gibbs_batch_identical_non_greedy(gpu, oracle, B):
         same_state(gb, ob)
 
 
+@pytest.mark.parametrize("chain", ["window", "cluster"])
 @pytest.mark.parametrize("n,B", [(2500, 120), (2500, 1500), (24000, 16000)])
-def test_mh_chain_identical_non_greedy(gpu, oracle, n, B):
-    """The three cell stores of the windowed chain with the Hastings-corrected rule."""
+def test_mh_chain_identical_non_greedy(gpu, oracle, n, B, chain):
+    """The three cell stores of the windowed chain with the Hastings-corrected rule, on one
+    CTA and on the cluster."""
     G, O, gb, ob, a, _ = make_pair(gpu, oracle, n, 12 * n, 9, B, seed=150 + B)
     order = np.random.default_rng(B).permutation(n)[:600].astype(np.int32)
-    applied = gpu.finetune.mh_chain(gb, order, seed=8, iteration=1, step=3,
-                                    args=gpu.Args(algorithm="hybrid_mcmc", greedy=False))
+    with chain_kernel(gpu, chain):
+        applied = gpu.finetune.mh_chain(gb, order, seed=8, iteration=1, step=3,
+                                        args=gpu.Args(algorithm="hybrid_mcmc", greedy=False))
     want = ob.mh_chain(order, 8, 1, 3, oracle.make_config("hybrid_mcmc", greedy=False))
     assert applied == want
     same_state(gb, ob)
