@@ -186,7 +186,8 @@ sbpgpu_status sbpgpu_delta_mdl_batch(sbpgpu_bm* bm, int64_t n, const int32_t* ve
  * most 65536; larger batches return SBPGPU_EINVAL.  The first call on a device looks the
  * array up (cudaGetSymbolAddress); make that first call before any stream capture.
  * Nothing needs zeroing beforehand.  Calls that overlap in time on the same device, from
- * any thread or context, share the array and race: serialise them. */
+ * any thread or context, share the array and race: serialise them.  The array's address is
+ * kept for the life of the process: a cudaDeviceReset between calls is not supported. */
 sbpgpu_status sbpgpu_delta_mdl_batch_noalloc(sbpgpu_bm* bm, int64_t n, const int32_t* vertex,
                                              const int32_t* proposal, double* out_delta);
 /* entropy::block_merge_delta_mdl (src/entropy.cpp:129-182) for n merges block[i] -> proposal[i]. */

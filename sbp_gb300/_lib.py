@@ -15,6 +15,7 @@ f64p = ctypes.POINTER(ctypes.c_double)
 vp = ctypes.c_void_p
 
 SBPGPU_OK = 0
+SBPGPU_ENOMEM = 2
 STATUS_NAMES = {0: "SBPGPU_OK", 1: "SBPGPU_EINVAL", 2: "SBPGPU_ENOMEM", 3: "SBPGPU_ETIMEOUT",
                 4: "SBPGPU_EDEVICE", 5: "SBPGPU_EUNSUPPORTED", 6: "SBPGPU_ECANCELED"}
 

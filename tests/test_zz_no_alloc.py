@@ -3,8 +3,12 @@ allocating entry point (sbpgpu_delta_mdl_batch), both called through the C ABI.
 
 Both run the same scoring kernel, so the values must agree to the delta-MDL tolerance
 (they are in fact identical).  Two calls in a row check that the staging array carries
-nothing from one call into the next.  This file is collected last so the check also runs
-after every other GPU test in the same process."""
+nothing from one call into the next; entries whose proposal is the vertex's own block
+take the zero-delta path.  That the call allocates nothing is checked through the
+context's allocation-failure injection: with the next device allocation set to fail, the
+allocation-free call still succeeds while the allocating one reports SBPGPU_ENOMEM.  This
+file is collected last so the check also runs after every other GPU test in the same
+process."""
 import numpy as np
 import pytest
 
@@ -38,12 +42,22 @@ def test_noalloc_delta_matches_allocating_entry_point(gpu):
             v = rng.integers(0, n, size).astype(np.int32)
             s = rng.integers(0, B, size).astype(np.int32)
             s = np.where(s == a[v], (s + 1) % B, s).astype(np.int32)
+            own = rng.random(size) < 0.1  # these propose the vertex's own block
+            s[own] = a[v[own]]
             st, want = _call(lib, "sbpgpu_delta_mdl_batch", bm, v, s)
             assert st == _lib.SBPGPU_OK, lib.sbpgpu_last_error(ctx.h)
+            assert np.all(want[own] == 0.0)
             for _ in range(2):
+                ctx.inject_alloc_failure(0)  # the next device allocation through ctx fails
                 st, got = _call(lib, "sbpgpu_delta_mdl_batch_noalloc", bm, v, s)
+                ctx.inject_alloc_failure(-1)
                 assert st == _lib.SBPGPU_OK, lib.sbpgpu_last_error(ctx.h)
                 assert np.all(np.abs(got - want) <= DELTA_REL_TOL * np.maximum(1.0, np.abs(want)))
+                assert np.all(got[own] == 0.0)
+        ctx.inject_alloc_failure(0)  # control: the allocating entry point does allocate
+        st, _ = _call(lib, "sbpgpu_delta_mdl_batch", bm, v, s)
+        ctx.inject_alloc_failure(-1)
+        assert st == _lib.SBPGPU_ENOMEM
     finally:
         ctx.close()
 
