@@ -21,6 +21,7 @@
 #include <vector>
 
 #include "../../include/sbpgpu.h"
+#include "host_csr.h"
 #include "kernels.cuh"
 #include "noalloc.cuh"
 #include "prims.cuh"
@@ -886,27 +887,15 @@ void merge_impl(sbpgpu_bm* bm, const sbpgpu_config& cfg, uint64_t seed, int32_t 
 
 void upload_graph(sbpgpu_graph* g, const int32_t* src, const int32_t* dst) {
     const int64_t N = g->N, E = g->E;
-    std::vector<int32_t> out_off(N + 1, 0), inns_off(N + 1, 0), selfcnt(N, 0), indeg(N, 0);
-    for (int64_t e = 0; e < E; ++e) {
-        const int32_t u = src[e], v = dst[e];
-        if (u < 0 || u >= N || v < 0 || v >= N) throw ApiError(SBPGPU_EINVAL, "edge endpoint out of range");
-        out_off[u + 1]++;
-        indeg[v]++;
-        if (u == v) selfcnt[u]++;
-        else inns_off[v + 1]++;
+    // stable: neighbour lists keep input order (graph.cpp:10-18); built by several threads
+    HostCsr csr;
+    try {
+        build_host_csr(N, E, src, dst, csr);
+    } catch (const std::invalid_argument& e) {
+        throw ApiError(SBPGPU_EINVAL, e.what());
     }
-    for (int64_t v = 0; v < N; ++v) {
-        out_off[v + 1] += out_off[v];
-        inns_off[v + 1] += inns_off[v];
-    }
-    std::vector<int32_t> out_nbr(E), esrc(E), inns_nbr(inns_off[N]);
-    std::vector<int32_t> po(out_off.begin(), out_off.end() - 1), pi(inns_off.begin(), inns_off.end() - 1);
-    for (int64_t e = 0; e < E; ++e) {  // stable: neighbour lists keep input order (graph.cpp:10-18)
-        const int32_t u = src[e], v = dst[e];
-        esrc[po[u]] = u;
-        out_nbr[po[u]++] = v;
-        if (u != v) inns_nbr[pi[v]++] = u;
-    }
+    const std::vector<int32_t>&out_off = csr.out_off, &inns_off = csr.inns_off, &selfcnt = csr.selfcnt,
+                            &indeg = csr.indeg, &out_nbr = csr.out_nbr, &esrc = csr.esrc, &inns_nbr = csr.inns_nbr;
     g->deg.resize(N);
     g->kdeg.resize(N);
     g->max_k = 0;
@@ -921,7 +910,7 @@ void upload_graph(sbpgpu_graph* g, const int32_t* src, const int32_t* dst) {
     const int64_t nlq = std::max(E, N) + 2;
     std::vector<int32_t> Lq(nlq);
     Lq[0] = 0;
-    for (int64_t x = 1; x < nlq; ++x) Lq[x] = (int32_t)((double)logf((float)x) * 16777216.0);
+    parallel_for(1, nlq, [&](int64_t x) { Lq[x] = (int32_t)((double)logf((float)x) * 16777216.0); });
     cudaStream_t st = g->ctx->stream;
     auto& o = g->owned;
     int32_t* d_out_off = dalloc<int32_t>(o, N + 1);

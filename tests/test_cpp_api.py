@@ -20,6 +20,18 @@ def test_cpp_interface_compiles():
     assert r.returncode == 0, r.stderr
 
 
+def test_host_adjacency_build(tmp_path):
+    """The threaded host adjacency build of graph upload (sbp_gb300/csrc/host_csr.h) equals
+    one sequential pass over the edges, at 1 to 16 threads (tests/cpp/test_host_csr.cpp)."""
+    exe = str(tmp_path / "test_host_csr")
+    r = subprocess.run(["g++", "-std=c++17", "-O2", "-pthread", "-Wall", "-Wextra", "-Werror",
+                        os.path.join(ROOT, "tests", "cpp", "test_host_csr.cpp"), "-o", exe],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([exe], capture_output=True, text=True)
+    assert r.returncode == 0 and r.stdout.strip() == "OK", r.stdout + r.stderr
+
+
 def _write_toy(golden, path):
     with open(path, "w") as f:
         f.write("%d %d\n" % (golden["num_vertices"], len(golden["edges"])))
