@@ -8,7 +8,8 @@
  *   entropy::mdl, delta_mdl, block_merge_delta_mdl, null_mdl_v1, normalize_mdl_v1
  *                               include/entropy.hpp:33-81
  *   finetune::mcmc, asynchronous_gibbs, hybrid_mcmc, metropolis_hastings, accept,
- *   early_stop, edge_weights, blockmodel_delta, propose_move, move_vertex
+ *   early_stop, edge_weights, blockmodel_delta, propose_move, move_vertex,
+ *   propose_gibbs_move_v3 (and the batched propose_gibbs_moves)
  *                               include/finetune.hpp:36-157
  *   EdgeWeights, VertexMove     include/typedefs.hpp:16-38, 124-129
  *   utils::ProposalAndEdgeCounts
@@ -17,7 +18,8 @@
  *   BlockMatrix (blockmatrix()) include/blockmodel/sparse/csparse_matrix.hpp:45-112
  *   BlockmodelTriplet           include/blockmodel/blockmodel_triplet.hpp:12-42
  *   sbp::done_blockmodeling     src/sbp.cpp:74-86
- *   block_merge::merge_blocks   include/block_merge.hpp:32-56
+ *   block_merge::merge_blocks, merge_proposals (propose_merge_sparse for every block)
+ *                               include/block_merge.hpp:32-56
  *   sbp::stochastic_block_partition
  *                               include/sbp.hpp:18
  *
@@ -788,6 +790,35 @@ inline VertexMove move_vertex(long vertex, long /*current_block*/, utils::Propos
     return VertexMove{dS, moved != 0, vertex, proposal.proposal};
 }
 
+/// finetune::propose_gibbs_move_v3 (src/finetune.cpp:871-901) for many vertices against
+/// the current state, nothing applied: the accepted proposal of each, or -1 (the decisions
+/// an asynchronous-Gibbs batch applies in vertex-id order).
+inline std::vector<long> propose_gibbs_moves(const Blockmodel& blockmodel, const std::vector<long>& vertices,
+                                             const Graph& graph, int iteration = 0, int step = 0,
+                                             const Args& a = args) {
+    const sbpgpu_config cfg = to_config(a);
+    std::vector<int32_t> v(vertices.begin(), vertices.end()), out(vertices.size());
+    check(sbpgpu_gibbs_propose(blockmodel.handle(), &cfg, (int64_t)v.size(), v.data(), a.seed, (uint32_t)iteration,
+                               (uint32_t)step, out.data()),
+          graph.context().get());
+    return std::vector<long>(out.begin(), out.end());
+}
+/// finetune::propose_gibbs_move_v3 for one vertex: did_move tells whether the proposal was
+/// accepted (nothing is applied); delta_entropy is its delta-MDL, 0 when nothing was
+/// accepted.
+inline VertexMove propose_gibbs_move_v3(const Blockmodel& blockmodel, long vertex, const Graph& graph,
+                                        int iteration = 0, int step = 0, const Args& a = args) {
+    const long s = propose_gibbs_moves(blockmodel, std::vector<long>{vertex}, graph, iteration, step, a)[0];
+    double dS = 0.0;
+    if (s >= 0) {
+        const int32_t vv = (int32_t)vertex, ss = (int32_t)s;
+        check(a.nonparametric ? sbpgpu_np_delta_mdl_batch(blockmodel.handle(), 1, &vv, &ss, &dS)
+                              : sbpgpu_delta_mdl_batch(blockmodel.handle(), 1, &vv, &ss, &dS),
+              graph.context().get());
+    }
+    return VertexMove{dS, s >= 0, vertex, s};
+}
+
 namespace detail {
 inline Blockmodel& run(const char* algorithm, Blockmodel& bm, const Graph& g, bool golden, int iteration) {
     Args a = args;
@@ -824,6 +855,19 @@ inline Blockmodel& merge_blocks(Blockmodel& blockmodel, const Graph& graph, long
     blockmodel.invalidate();
     blockmodel.setNum_blocks_to_merge((long)(blockmodel.num_blocks() * blockmodel.getBlock_reduction_rate()));
     return blockmodel;
+}
+
+/// block_merge::propose_merge_sparse (src/block_merge.cpp:251-285) for every block, as the
+/// merge pass draws them (10 proposals per block, src/block_merge.cpp:189-217): each
+/// block's best proposal and its delta-MDL.
+inline std::pair<std::vector<long>, std::vector<double>> merge_proposals(const Blockmodel& blockmodel,
+                                                                         const Graph& graph, int step = 0,
+                                                                         const Args& a = args) {
+    const long B = blockmodel.num_blocks();
+    std::vector<int32_t> best(B);
+    std::vector<double> dS(B);
+    check(sbpgpu_merge_proposals(blockmodel.handle(), a.seed, step, best.data(), dS.data()), graph.context().get());
+    return {std::vector<long>(best.begin(), best.end()), dS};
 }
 
 }  // namespace block_merge

@@ -218,6 +218,11 @@ sbpgpu_status sbpgpu_propose_batch(sbpgpu_bm* bm, int64_t n, const int32_t* vert
 sbpgpu_status sbpgpu_gibbs_batch(sbpgpu_bm* bm, const sbpgpu_config* cfg, int64_t n, const int32_t* vertex,
                                  uint64_t seed, uint32_t iteration, uint32_t step, int32_t* out_moves,
                                  int64_t* applied);
+/* finetune::propose_gibbs_move_v3 (src/finetune.cpp:871-901) for vertex[0..n) against the
+ * current blockmodel, with nothing applied: out_moves[i] = the accepted proposal or -1 --
+ * the decisions sbpgpu_gibbs_batch takes before it applies them. */
+sbpgpu_status sbpgpu_gibbs_propose(sbpgpu_bm* bm, const sbpgpu_config* cfg, int64_t n, const int32_t* vertex,
+                                   uint64_t seed, uint32_t iteration, uint32_t step, int32_t* out_moves);
 /* Sequential Metropolis-Hastings over vertex[0..n) in order, each accepted move applied
  * before the next proposal (finetune::propose_move / move_vertex, src/finetune.cpp:822-869). */
 sbpgpu_status sbpgpu_mh_chain(sbpgpu_bm* bm, const sbpgpu_config* cfg, int64_t n, const int32_t* vertex,

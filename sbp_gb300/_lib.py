@@ -128,6 +128,8 @@ SIGNATURES = {
                                             ctypes.c_uint32, ctypes.c_uint32, i32p]),
     "sbpgpu_gibbs_batch": (ctypes.c_int, [vp, ctypes.POINTER(Config), ctypes.c_int64, i32p, ctypes.c_uint64,
                                           ctypes.c_uint32, ctypes.c_uint32, i32p, i64p]),
+    "sbpgpu_gibbs_propose": (ctypes.c_int, [vp, ctypes.POINTER(Config), ctypes.c_int64, i32p, ctypes.c_uint64,
+                                            ctypes.c_uint32, ctypes.c_uint32, i32p]),
     "sbpgpu_mh_chain": (ctypes.c_int, [vp, ctypes.POINTER(Config), ctypes.c_int64, i32p, ctypes.c_uint64,
                                        ctypes.c_uint32, ctypes.c_uint32, i64p]),
     "sbpgpu_propose_move": (ctypes.c_int, [vp, ctypes.POINTER(Config), ctypes.c_int32, ctypes.c_uint64,

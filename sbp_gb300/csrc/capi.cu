@@ -1882,6 +1882,31 @@ sbpgpu_status sbpgpu_gibbs_batch(sbpgpu_bm* bm, const sbpgpu_config* cfg, int64_
     });
 }
 
+sbpgpu_status sbpgpu_gibbs_propose(sbpgpu_bm* bm, const sbpgpu_config* cfg, int64_t n, const int32_t* vertex,
+                                   uint64_t seed, uint32_t iteration, uint32_t step, int32_t* out_moves) {
+    if (!bm || !cfg || n < 0 || (n && (!vertex || !out_moves))) return SBPGPU_EINVAL;
+    sbpgpu_graph* g = bm->g;
+    return guarded(g->ctx, [&] {
+        if (bm->d.B < 2) throw ApiError(SBPGPU_EINVAL, "proposals need at least two blocks");
+        if (n > g->N) throw ApiError(SBPGPU_EINVAL, "a batch holds at most num_vertices vertices");
+        for (int64_t i = 0; i < n; ++i)
+            if (vertex[i] < 0 || vertex[i] >= g->N) throw ApiError(SBPGPU_EINVAL, "vertex out of range");
+        if (n == 0) return SBPGPU_OK;
+        const int mode = accept_mode(*cfg);
+        if (mode == ACC_NP) ensure_np_sweeps(g);
+        cudaStream_t st = g->ctx->stream;
+        CK(cudaMemcpyAsync(g->w.list_tmp, vertex, n * 4, cudaMemcpyHostToDevice, st));
+        reset_counters(g);
+        gibbs_propose(g->dg, bm->d, g->w.list_tmp, (int32_t)n, g->max_k, seed, iteration, step, mode, g->w, st);
+        std::vector<int32_t> mv(g->N);
+        CK(cudaMemcpyAsync(mv.data(), g->w.moves, g->N * 4, cudaMemcpyDeviceToHost, st));
+        check_flags(g);
+        for (int64_t i = 0; i < n; ++i) out_moves[i] = mv[vertex[i]];
+        reset_counters(g);
+        return SBPGPU_OK;
+    });
+}
+
 sbpgpu_status sbpgpu_mh_chain(sbpgpu_bm* bm, const sbpgpu_config* cfg, int64_t n, const int32_t* vertex,
                               uint64_t seed, uint32_t iteration, uint32_t step, int64_t* applied) {
     if (!bm || !cfg || n < 0 || (n && !vertex)) return SBPGPU_EINVAL;

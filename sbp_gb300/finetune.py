@@ -70,6 +70,18 @@ def gibbs_batch(blockmodel, vertices, seed, iteration, step, args=None):
     return moves, applied.value
 
 
+def propose_gibbs_moves(blockmodel, vertices, seed, iteration, step, args=None):
+    """finetune::propose_gibbs_move_v3 (src/finetune.cpp:871-901) for every vertex against
+    the current state, nothing applied: the accepted proposal of each, or -1."""
+    cfg = _cfg(args)
+    v = np.ascontiguousarray(np.atleast_1d(vertices), dtype=np.int32)
+    moves = np.zeros(v.size, np.int32)
+    blockmodel.ctx.check(blockmodel.ctx.lib.sbpgpu_gibbs_propose(blockmodel.h, ctypes.byref(cfg), v.size,
+                                                                 _p(v, i32p), int(seed), int(iteration), int(step),
+                                                                 _p(moves, i32p)))
+    return moves
+
+
 def mh_chain(blockmodel, vertices, seed, iteration, step, args=None):
     """finetune::propose_move over vertices in order, each accepted move applied at once
     (src/finetune.cpp:842-869).  Returns the number of applied moves."""

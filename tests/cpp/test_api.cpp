@@ -249,6 +249,23 @@ static void boundary_api(const Toy& t) {
         }
     }
 
+    // propose_gibbs_move_v3 applies nothing; merge_proposals gives every block a proposal
+    {
+        s::Blockmodel d = bm.copy();
+        const std::vector<long> before = d.block_assignment();
+        const std::vector<long> all = s::finetune::propose_gibbs_moves(d, {0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10}, graph,
+                                                                       1, 0, h);
+        EXPECT(all.size() == 11 && d.block_assignment() == before);
+        for (long u = 0; u < t.n; ++u) {
+            const s::VertexMove gm = s::finetune::propose_gibbs_move_v3(d, u, graph, 1, 0, h);
+            EXPECT(gm.proposed_block == all[u] && gm.did_move == (all[u] >= 0));
+            if (gm.did_move) EXPECT(gm.delta_entropy == s::entropy::delta_mdl(d, u, gm.proposed_block));
+        }
+        const auto mp = s::block_merge::merge_proposals(d, graph, 0, h);
+        EXPECT((long)mp.first.size() == d.num_blocks() && (long)mp.second.size() == d.num_blocks());
+        for (long b = 0; b < d.num_blocks(); ++b) EXPECT(mp.first[b] < d.num_blocks());
+    }
+
     // BlockmodelTriplet: the bracket forms as blockmodels with fewer blocks arrive
     s::BlockmodelTriplet triplet;
     EXPECT(triplet.golden_ratio_not_reached() && triplet.get(0).empty && triplet.get(1).empty);

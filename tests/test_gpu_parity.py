@@ -398,3 +398,16 @@ def test_move_vertex_scores_and_applies(gpu, oracle):
             same_state(gb, ob)
     assert moves > 0
     same_state(gb, ob)
+
+
+@pytest.mark.parametrize("B", [6, 300])
+def test_gibbs_propose_applies_nothing(gpu, oracle, B):
+    """finetune::propose_gibbs_move_v3 on its own: the decisions of an asynchronous-Gibbs
+    batch (the oracle's, before its apply) with the blockmodel left as it was."""
+    G, O, gb, ob, a, _ = make_pair(gpu, oracle, 2500, 30000, 9, B, seed=190 + B)
+    verts = np.arange(2500, dtype=np.int32)
+    before = ob.copy()
+    mv_g = gpu.finetune.propose_gibbs_moves(gb, verts, seed=5, iteration=1, step=2)
+    same_state(gb, before)
+    n_o, mv_o, _ = ob.gibbs_batch(verts, 5, 1, 2, oracle.make_config("async_gibbs"))
+    assert np.array_equal(mv_g, mv_o)
