@@ -44,7 +44,9 @@ typedef struct sbpgpu_config {
     int32_t asynciterations;  /* --asynciterations (default INT32_MAX) */
     int32_t max_iterations;   /* MAX_NUM_ITERATIONS, include/finetune.hpp:34 (default 100) */
     int32_t nonparametric;    /* --nonparametric (default 0): entropy::nonparametric::* for every delta and
-                                 MDL, directed, without degree correction; acceptance is then non-greedy
+                                 MDL, in the graph's directed or undirected form, degree-corrected where
+                                 the graph is marked so (sbpgpu_graph_set_degree_corrected, evaluation
+                                 and single moves only); acceptance is then non-greedy
                                  without the Hastings correction (include/args.hpp:204-207,
                                  src/entropy.cpp:499) whatever `greedy` says */
     int32_t split;            /* --split (top-down): 0 random (default), 1 snowball, 2 single-snowball,
