@@ -7,6 +7,25 @@ import pytest
 from sbp_gb300 import _lib
 
 
+def test_server_host_logic_without_gpu(tmp_path):
+    """The server's queue, admission, pause, bounded waits, cancellation and failure paths,
+    with server.cu compiled as plain C++ against stand-ins for the library calls it makes
+    (tests/cpp/test_server_host.cpp)."""
+    import os
+    import subprocess
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    exe = str(tmp_path / "test_server_host")
+    r = subprocess.run(["g++", "-std=c++17", "-O1", "-pthread", "-Wall", "-Wextra", "-Werror",
+                        "-I", os.path.join(root, "include"), "-x", "c++",
+                        os.path.join(root, "sbp_gb300", "csrc", "server.cu"), "-x", "none",
+                        os.path.join(root, "tests", "cpp", "test_server_host.cpp"), "-o", exe],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    for _ in range(3):
+        r = subprocess.run([exe], capture_output=True, text=True, timeout=60)
+        assert r.returncode == 0 and r.stdout.strip() == "OK", r.stdout + r.stderr
+
+
 def test_footprint_grows_with_the_graph():
     from sbp_gb300 import serve
     a = serve.footprint(1000, 20000, 0)
