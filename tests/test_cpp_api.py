@@ -20,6 +20,18 @@ def test_cpp_interface_compiles():
     assert r.returncode == 0, r.stderr
 
 
+def test_host_types_without_library(tmp_path):
+    """Delta, the BlockMatrix snapshot, edge_weights, early_stop and accept of the C++
+    interface, built and run without the library (tests/cpp/test_host_types.cpp)."""
+    exe = str(tmp_path / "test_host_types")
+    r = subprocess.run(["g++", "-std=c++17", "-O1", "-Wall", "-Wextra", "-Werror", "-I", INC,
+                        os.path.join(ROOT, "tests", "cpp", "test_host_types.cpp"), "-o", exe],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([exe], capture_output=True, text=True)
+    assert r.returncode == 0 and r.stdout.strip() == "OK", r.stdout + r.stderr
+
+
 def test_host_adjacency_build(tmp_path):
     """The threaded host adjacency build of graph upload (sbp_gb300/csrc/host_csr.h) equals
     one sequential pass over the edges, at 1 to 16 threads (tests/cpp/test_host_csr.cpp)."""
