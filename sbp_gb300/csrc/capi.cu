@@ -402,9 +402,7 @@ void ensure_np_sweeps(sbpgpu_graph* g) {
 
 void ensure_split(sbpgpu_graph* g, float mh_percent) {
     if (g->split_mh == mh_percent) return;
-    std::vector<int32_t> idx(g->N);
-    for (int64_t v = 0; v < g->N; ++v) idx[v] = (int32_t)v;
-    std::stable_sort(idx.begin(), idx.end(), [&](int32_t a, int32_t b) { return g->deg[a] > g->deg[b]; });
+    const std::vector<int32_t> idx = order_by_degree_desc(g->deg);  // a stable sort by descending degree
     const float limit = mh_percent * (float)g->N;  // float arithmetic as in graph.cpp:252
     std::vector<int32_t> hdv, ldv;
     for (int64_t i = 0; i < g->N; ++i) ((float)i < limit ? hdv : ldv).push_back(idx[i]);

@@ -1,3 +1,5 @@
+// Host-side helpers of graph upload.
+//
 // Stable compressed adjacency of a directed edge list, built on the host with several
 // threads: the out-neighbour lists (with each edge's source, for the edge-ordered
 // kernels) and the in-neighbour lists without self-loops, every list in input order as
@@ -131,6 +133,32 @@ inline void build_host_csr(int64_t N, int64_t E, const int32_t* src, const int32
             if (u != v) c.inns_nbr[pi[v]++] = u;
         }
     });
+}
+
+// The vertices in order of descending degree, ties by ascending id: what a stable sort of
+// 0..N-1 by descending degree gives (Graph::sort_vertices, src/graph.cpp:235-268), by one
+// counting pass over the degrees (a comparison sort when the degrees span far more values
+// than there are vertices).
+inline std::vector<int32_t> order_by_degree_desc(const std::vector<int32_t>& deg) {
+    const int64_t N = (int64_t)deg.size();
+    std::vector<int32_t> order(N);
+    int32_t mx = 0;
+    for (int32_t d : deg) mx = std::max(mx, d);
+    if ((int64_t)mx > 16 * N + 1024) {
+        for (int64_t v = 0; v < N; ++v) order[v] = (int32_t)v;
+        std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t b) { return deg[a] > deg[b]; });
+        return order;
+    }
+    std::vector<int64_t> start((size_t)mx + 2, 0);
+    for (int32_t d : deg) start[d]++;
+    int64_t run = 0;
+    for (int64_t d = mx; d >= 0; --d) {  // higher degrees first
+        const int64_t c = start[d];
+        start[d] = run;
+        run += c;
+    }
+    for (int64_t v = 0; v < N; ++v) order[start[deg[v]]++] = (int32_t)v;
+    return order;
 }
 
 }  // namespace sbp

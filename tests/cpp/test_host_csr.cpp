@@ -1,6 +1,8 @@
 // The threaded host adjacency build (sbp_gb300/csrc/host_csr.h) against one sequential pass
 // over the edges in order, on random graphs with self-loops, repeated edges and vertices
-// without edges, at thread counts 1 to 16.
+// without edges, at thread counts 1 to 16; and the counting-pass degree order against a
+// stable sort.
+#include <algorithm>
 #include <cstdio>
 #include <random>
 #include <vector>
@@ -41,8 +43,23 @@ static int check(int64_t N, int64_t E, uint32_t seed, int threads) {
     return ok ? 0 : 1;
 }
 
+static int check_order(int64_t N, int32_t maxdeg, uint32_t seed) {
+    std::mt19937 rng(seed);
+    std::vector<int32_t> deg(N);
+    for (auto& d : deg) d = (int32_t)(rng() % (uint32_t)(maxdeg + 1));
+    std::vector<int32_t> want(N);
+    for (int64_t v = 0; v < N; ++v) want[v] = (int32_t)v;
+    std::stable_sort(want.begin(), want.end(), [&](int32_t a, int32_t b) { return deg[a] > deg[b]; });
+    const bool ok = sbp::order_by_degree_desc(deg) == want;
+    if (!ok) std::fprintf(stderr, "order mismatch N=%lld maxdeg=%d\n", (long long)N, maxdeg);
+    return ok ? 0 : 1;
+}
+
 int main() {
     int bad = 0;
+    for (auto nd : {std::pair<int64_t, int32_t>{0, 0}, {1, 0}, {1000, 3}, {1000, 5000}, {100000, 700},
+                    {1000, 2000000000}})
+        bad += check_order(nd.first, nd.second, 5u + (uint32_t)nd.first);
     for (int threads : {1, 2, 3, 7, 16, 0})
         for (auto ne : {std::pair<int64_t, int64_t>{50, 0}, {50, 400}, {1000, 20000}, {200000, 3000000}})
             bad += check(ne.first, ne.second, 11u + (uint32_t)threads, threads);
