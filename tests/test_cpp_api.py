@@ -14,10 +14,12 @@ INC = os.path.join(ROOT, "include")
 
 
 def test_cpp_interface_compiles():
-    """The header and the test program compile without a GPU (no link)."""
-    r = subprocess.run(["g++", "-std=c++17", "-Wall", "-Wextra", "-Werror", "-fsyntax-only", "-I", INC, SRC],
-                       capture_output=True, text=True)
-    assert r.returncode == 0, r.stderr
+    """The header, the test program and the integration guide's search loop compile without
+    a GPU (no link)."""
+    for src in (SRC, os.path.join(ROOT, "tests", "cpp", "example_search_loop.cpp")):
+        r = subprocess.run(["g++", "-std=c++17", "-Wall", "-Wextra", "-Werror", "-fsyntax-only", "-I", INC, src],
+                           capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
 
 
 def test_host_types_without_library(tmp_path):
