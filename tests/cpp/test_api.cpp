@@ -202,6 +202,9 @@ static void boundary_api(const Toy& t) {
     }
     const std::vector<long> assignment3 = {0, 0, 0, 1, 2, 3, 3, 4, 5, 1, 5};
     s::Blockmodel b3(6, graph, 0.5, assignment3);
+    // the neighbours of block 1 (test/dict_transpose_matrix_test.cpp:16-34)
+    EXPECT(m->neighbors(1) == (std::set<long>{0, 1, 2}));
+    EXPECT(b3.blockmatrix()->neighbors(1) == (std::set<long>{0, 3, 4, 5}));
     const s::Delta k6 = s::finetune::blockmodel_delta(6, 3, 0, s::finetune::edge_weights(graph.out_neighbors(), 6),
                                                       s::finetune::edge_weights(graph.in_neighbors(), 6, true), b3);
     EXPECT(k6.entries().size() == 6);

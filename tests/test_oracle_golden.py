@@ -495,3 +495,14 @@ def test_dc_delta_tracks_mdl_on_random_moves(oracle):
         assert abs(lit - (after_lit - base_lit)) <= 1e-7 * abs(base_lit)
         checked += 1
     assert checked > 40
+
+
+def test_block_neighbours_known_answers(oracle, golden):
+    # dict_transpose_matrix_test.cpp:16-34: the neighbours of block 1 (keys of its row and
+    # column) are {0, 1, 2} on the toy blockmodel and {0, 3, 4, 5} on the six-block one
+    edges = np.array(golden["edges"], dtype=np.int32)
+    g = oracle.Graph(golden["num_vertices"], edges[:, 0], edges[:, 1])
+    for B, a, want in ((3, golden["assignment"], {0, 1, 2}), (6, [0, 0, 0, 1, 2, 3, 3, 4, 5, 1, 5], {0, 3, 4, 5})):
+        d = oracle.Blockmodel(g, B, np.array(a, np.int32)).read()
+        rows, cols = np.asarray(d["rows"]), np.asarray(d["cols"])
+        assert set(cols[rows == 1].tolist()) | set(rows[cols == 1].tolist()) == want
