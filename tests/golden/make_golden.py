@@ -36,6 +36,16 @@ def main(root):
     entropy = float(re.search(r"const double ENTROPY = ([0-9.]+);", toy).group(1))
     merge_assignment = ints(re.search(r"assignment2 = \{([^}]*)\};", toy).group(1))
     complex_assignment = ints(re.search(r"ComplexToySetUp.*?assignment = \{([^}]*)\};", toy, re.S).group(1))
+    # the block degrees after the vertex-7 move (test/toy_example.hpp: new_block_degrees,
+    # asserted by test/common_test.cpp:17-36)
+    # in ToySetUp (the vertex-7 move) and BlockMergeTest (block 0 into 1), in that order
+    nbd = [{}, {}, {}]
+    for k, v in re.findall(r"new_block_degrees\.block_degrees(_out|_in|) = \{([^}]*)\};", toy):
+        next(d for d in nbd if k not in d)[k] = ints(v)
+    # ComplexToySetUp: vertex 6 into block 0 of the six-block model (BlockDegreesAfterUpdates,
+    # asserted by test/common_test.cpp:38-77)
+    nbd[2] = {k: ints(v) for k, v in re.findall(r"BlockDegreesAfterUpdates\.block_degrees(_out|_in|) = \{([^}]*)\};",
+                                                 toy)}
 
     bm_test = read(root, "test/blockmodel_test.cpp")
     deg = {}
@@ -80,11 +90,15 @@ def main(root):
         "block_degrees_in": [deg["_in"][i] for i in range(3)],
         "block_degrees": [deg["_tot"][i] for i in range(3)],
         "vertex_move": {"vertex": 7, "proposal": 0, "delta": vdelta, "delta_entries": vdelta_size,
-                        "after_assignment": [0, 0, 0, 0, 1, 1, 1, 0, 2, 2, 2]},
+                        "after_assignment": [0, 0, 0, 0, 1, 1, 1, 0, 2, 2, 2],
+                        "after_degrees_out": nbd[0]["_out"], "after_degrees_in": nbd[0]["_in"],
+                        "after_degrees": nbd[0][""]},
         "special_case": {"num_blocks": 6, "assignment": complex_assignment, "vertex": 6, "proposal": 0,
-                         "delta": sdelta},
+                         "delta": sdelta, "after_degrees_out": nbd[2]["_out"], "after_degrees_in": nbd[2]["_in"],
+                         "after_degrees": nbd[2][""]},
         "block_merge": {"block": 0, "proposal": 1, "delta": mdelta, "delta_entries": mdelta_size,
-                        "after_assignment": merge_assignment},
+                        "after_assignment": merge_assignment, "after_degrees_out": nbd[1]["_out"],
+                        "after_degrees_in": nbd[1]["_in"], "after_degrees": nbd[1][""]},
         "null_mdl_v1": {"num_edges": big_E, "value": null_mdl},
         # nonparametric_entropy_test.cpp:19-27 on the toy blockmodel above (not degree-corrected)
         "nonparametric": {"mdl": npc["SIMPLE_NONPARAMETRIC_ENTROPY"], "sparse_entropy": npc["SIMPLE_SPARSE_ENTROPY"],

@@ -506,3 +506,20 @@ def test_block_neighbours_known_answers(oracle, golden):
         d = oracle.Blockmodel(g, B, np.array(a, np.int32)).read()
         rows, cols = np.asarray(d["rows"]), np.asarray(d["cols"])
         assert set(cols[rows == 1].tolist()) | set(rows[cols == 1].tolist()) == want
+
+
+def test_block_degrees_after_changes(oracle, golden):
+    # toy_example.hpp's degrees after the vertex-7 move, after merging block 0 into 1, and
+    # after moving vertex 6 of the six-block model into block 0 (common_test.cpp:17-77)
+    edges = np.array(golden["edges"], dtype=np.int32)
+    g = oracle.Graph(golden["num_vertices"], edges[:, 0], edges[:, 1])
+    sc = golden["special_case"]
+    moved = list(sc["assignment"])
+    moved[sc["vertex"]] = sc["proposal"]
+    for case, B, a in ((golden["vertex_move"], 3, golden["vertex_move"]["after_assignment"]),
+                       (golden["block_merge"], 3, golden["block_merge"]["after_assignment"]),
+                       (sc, 6, moved)):
+        d = oracle.Blockmodel(g, B, np.array(a, np.int32)).read()
+        assert d["d_out"].tolist() == case["after_degrees_out"]
+        assert d["d_in"].tolist() == case["after_degrees_in"]
+        assert d["d_tot"].tolist() == case["after_degrees"]
