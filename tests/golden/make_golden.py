@@ -59,6 +59,18 @@ def main(root):
     body = re.search(r"TEST_F\(FinetuneTest, SpecialCaseBlockmodelDeltasAreCorrect\)(.*?)\n}", ft, re.S).group(1)
     sdelta = {f"{a},{b}": int(c) for a, b, c in re.findall(r"delta\.get\((\d),(\d)\), (-?\d+)\)", body)}
 
+    # the rows and columns of the two blocks after a move (finetune_test.cpp:44-83, :174-224):
+    # vertex 7 to block 0, vertex 5 (a self-loop) to block 0, and vertex 6 of the six-block
+    # model to block 0
+    cells_after = []
+    for name, which, vertex in (("SparseEdgeCountUpdatesAreCorrect", "toy", 7),
+                                ("SparseEdgeCountUpdatesWithSelfEdgesAreCorrect", "toy", 5),
+                                ("SpecialCaseGivesCorrectSparseEdgeCountUpdates", "complex", 6)):
+        body = re.search(r"TEST_F\(FinetuneTest, %s\)(.*?)\n}" % name, ft, re.S).group(1)
+        vals = [[k, int(i), int(v)] for k, i, v in
+                re.findall(r"updates\.(block_row|block_col|proposal_row|proposal_col)\[(\d)\], (\d+)\)", body)]
+        cells_after.append({"blockmodel": which, "vertex": vertex, "proposal": 0, "values": vals})
+
     bmt = read(root, "test/block_merge_test.cpp")
     mdelta = {f"{a},{b}": int(c) for a, b, c in re.findall(r"delta\.get\((\d),(\d)\), (-?\d+)\)", bmt)}
     mdelta_size = int(re.search(r"entries\(\)\.size\(\), (\d+)\)", bmt).group(1))
@@ -107,6 +119,7 @@ def main(root):
                                                "sparse_entropy": npc["SPARSE_ENTROPY"],
                                                "degree_dl": npc["DEGREE_DL"]}},
     }
+    out["cells_after_move"] = cells_after
     # evaluate_test.cpp:17-44: calculate_f1_score on two contingency tables (EXPECT_FLOAT_EQ)
     out["evaluate"] = {"matrix": matrix("Matrix"), "num_vertices": int(evc["N"]), "f1": evc["F1"],
                        "rand_index": evc["RandIndex"], "recall": evc["Recall"], "precision": evc["Precision"],

@@ -411,3 +411,19 @@ def test_gibbs_propose_applies_nothing(gpu, oracle, B):
     same_state(gb, before)
     n_o, mv_o, _ = ob.gibbs_batch(verts, 5, 1, 2, oracle.make_config("async_gibbs"))
     assert np.array_equal(mv_g, mv_o)
+
+
+def test_cells_after_move_known_answers_on_gpu(gpu, golden):
+    """The reference's row and column values after three moves (finetune_test.cpp), read
+    from device blockmodels built on the moved assignments."""
+    from test_oracle_golden import _cells_after_move_check
+    e = np.array(golden["edges"], np.int32)
+    G = gpu.Graph(11, e[:, 0], e[:, 1])
+
+    def read_after(B, a):
+        d = gpu.Blockmodel(B, G, 0.5, np.array(a, np.int32)).read()
+        M = np.zeros((B, B), np.int64)
+        M[np.asarray(d["rows"]), np.asarray(d["cols"])] = np.asarray(d["counts"])
+        return M
+
+    _cells_after_move_check(read_after, golden)

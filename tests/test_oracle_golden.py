@@ -523,3 +523,31 @@ def test_block_degrees_after_changes(oracle, golden):
         assert d["d_out"].tolist() == case["after_degrees_out"]
         assert d["d_in"].tolist() == case["after_degrees_in"]
         assert d["d_tot"].tolist() == case["after_degrees"]
+
+
+def _cells_after_move_check(read_after, golden):
+    """The rows (block_row / proposal_row) and columns of the current and the proposed block
+    after each move of finetune_test.cpp's edge-count-update tests."""
+    for case in golden["cells_after_move"]:
+        toy = case["blockmodel"] == "toy"
+        a = list(golden["assignment"] if toy else golden["special_case"]["assignment"])
+        B = golden["num_blocks"] if toy else golden["special_case"]["num_blocks"]
+        cur, s = a[case["vertex"]], case["proposal"]
+        a[case["vertex"]] = s
+        M = read_after(B, a)
+        for kind, i, v in case["values"]:
+            got = {"block_row": M[cur][i], "block_col": M[i][cur], "proposal_row": M[s][i], "proposal_col": M[i][s]}[kind]
+            assert got == v, (case["vertex"], kind, i)
+
+
+def test_cells_after_move_known_answers(oracle, golden):
+    edges = np.array(golden["edges"], dtype=np.int32)
+    g = oracle.Graph(golden["num_vertices"], edges[:, 0], edges[:, 1])
+
+    def read_after(B, a):
+        d = oracle.Blockmodel(g, B, np.array(a, np.int32)).read()
+        M = np.zeros((B, B), np.int64)
+        M[np.asarray(d["rows"]), np.asarray(d["cols"])] = np.asarray(d["counts"])
+        return M
+
+    _cells_after_move_check(read_after, golden)
