@@ -71,6 +71,14 @@ def main(root):
                 re.findall(r"updates\.(block_row|block_col|proposal_row|proposal_col)\[(\d)\], (\d+)\)", body)]
         cells_after.append({"blockmodel": which, "vertex": vertex, "proposal": 0, "values": vals})
 
+    # max-degree sampling of the toy graph (sample_test.cpp:8-51): its vertex and edge counts
+    # and the edges the sampled graph must hold, in sample ids
+    smt = read(root, "test/sample_test.cpp")
+    sample_size = float(re.search(r"args\.samplesize = ([0-9.]+);", smt).group(1))
+    sedges_block = re.search(r"sample_edges = \{(.*?)\};", smt, re.S).group(1)
+    sample_edges = [ints(m) for m in re.findall(r"\{([^{}]*)\}", sedges_block)]
+    sample_counts = ints(" ".join(re.findall(r"EXPECT_EQ\(s\.graph\.num_(?:vertices|edges)\(\), (\d+)\);", smt)))
+
     bmt = read(root, "test/block_merge_test.cpp")
     mdelta = {f"{a},{b}": int(c) for a, b, c in re.findall(r"delta\.get\((\d),(\d)\), (-?\d+)\)", bmt)}
     mdelta_size = int(re.search(r"entries\(\)\.size\(\), (\d+)\)", bmt).group(1))
@@ -120,6 +128,8 @@ def main(root):
                                                "degree_dl": npc["DEGREE_DL"]}},
     }
     out["cells_after_move"] = cells_after
+    out["sample_max_degree"] = {"sample_size": sample_size, "num_vertices": sample_counts[0],
+                                "num_edges": sample_counts[1], "edges": sample_edges}
     # evaluate_test.cpp:17-44: calculate_f1_score on two contingency tables (EXPECT_FLOAT_EQ)
     out["evaluate"] = {"matrix": matrix("Matrix"), "num_vertices": int(evc["N"]), "f1": evc["F1"],
                        "rand_index": evc["RandIndex"], "recall": evc["Recall"], "precision": evc["Precision"],

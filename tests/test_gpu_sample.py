@@ -135,3 +135,15 @@ def test_detached_partition_identical(gpu, oracle):
     a_o = oracle.reattach(O, sa, B_o, m, 4)
     assert B_g == B_o and np.array_equal(a_g, a_o)
     assert abs(mdl_g - oracle.Blockmodel(O, B_o, a_o).mdl()[1]) <= 1e-12 * abs(mdl_g)
+
+
+def test_max_degree_sample_of_the_toy_graph(gpu, oracle, golden):
+    """sample_test.cpp's known answer (pinned on the oracle): the device draws the same
+    4-vertex sample of the toy graph."""
+    e = np.array(golden["edges"], np.int32)
+    G, O = gpu.Graph(11, e[:, 0], e[:, 1]), oracle.Graph(11, e[:, 0], e[:, 1])
+    size = golden["sample_max_degree"]["sample_size"]
+    m_g, n_g = gpu.sample.sample_mapping(G, "max_degree", size, seed=0)
+    m_o, n_o = oracle.sample(O, "max_degree", size, 0)
+    assert n_g == n_o == golden["sample_max_degree"]["num_vertices"]
+    assert np.array_equal(m_g, m_o)

@@ -551,3 +551,17 @@ def test_cells_after_move_known_answers(oracle, golden):
         return M
 
     _cells_after_move_check(read_after, golden)
+
+
+def test_max_degree_sample_known_answer(oracle, golden):
+    # sample_test.cpp:26-51: 40% of the toy graph by degree is 4 vertices and 5 edges,
+    # among them the listed ones (sample ids)
+    edges = np.array(golden["edges"], dtype=np.int32)
+    g = oracle.Graph(golden["num_vertices"], edges[:, 0], edges[:, 1])
+    want = golden["sample_max_degree"]
+    m, n = oracle.sample(g, "max_degree", want["sample_size"], 0)
+    assert n == want["num_vertices"]
+    ns, src, dst = oracle.subgraph_edges(g, m)
+    assert ns == want["num_vertices"] and src.size == want["num_edges"]
+    got = set(zip(src.tolist(), dst.tolist()))
+    assert all(tuple(e) in got for e in want["edges"])
